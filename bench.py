@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 solver step on the 65,536-box pile.
+
+One step = ContactRefresher -> ForceUpdater -> Solver (prestep, warm start,
+10 iterations) -> PositionUpdater over the pile's frozen manifold set
+(65,536 manifolds, 262,144 contacts), float32.  The metric is contact-iters/s
+= sum over manifolds of contacts x iterations, per second.
+
+  value       device time of K steps (CUDA events on the scene stream around
+              each graph launch), inputs resident in HBM, L2 flushed between
+              steps by writing a 512 MiB buffer (the step's working set is
+              below L2 size).
+  e2e         the same metric through the C ABI with host records: every step
+              uploads bodies and manifolds from pinned host memory, steps and
+              downloads bodies and manifolds; host wall clock.
+  roofline    the solve kernel (k_solve): algorithmic bytes of the executed
+              manifold visits (76 d + 136 + 48 c per visit, counted by a census
+              before every sweep) / solve-phase device time from events captured
+              in the step graph; peak = measured HBM copy bandwidth.
+  cpu_baseline the oracle port of Solver.UpdateMultithreaded (per-body spin
+              locks, chunked parallel loop) on all host cores, on a bounded
+              sample of steps of the same pile.
+
+`--impl reference` times that CPU port alone (the reference is C# and no .NET
+runtime exists on these machines).  Under torchrun every rank steps its own
+replica of the pile ("replicas only": a single scene does not shard); rank 0
+prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+DT = np.float32(1 / 60)
+WORKLOAD = "pile_64k"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--mode", default="graph", choices=["graph", "persistent"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """dram bytes per k_solve launch from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "k_solve_pile64k.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(bodies, manifolds, contact_iters_per_step, seconds, threads):
+    """The oracle's port of Solver.UpdateMultithreaded on `threads` host cores."""
+    import oracle
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300.solver import default_settings
+    o = oracle.OracleSpace(default_settings(), bodies, manifolds)
+    o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+    o.step_multithreaded(DT, N.STEP_ALL, 1, threads)  # warm-up step (MultithreadedScalingTestDemo.cs:223)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+        steps += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": contact_iters_per_step * steps / dt, "unit": "contact-iters/s", "cores": threads,
+            "kind": "port", "steps": steps,
+            "sample": f"{steps} full steps of the 65,536-box pile after 1 warm-up step "
+                      f"(oracle port of Solver.UpdateMultithreaded, {threads} threads, {dt:.1f} s)"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import default_settings
+    import oracle
+    from bepuphysics1_gb300 import native as N
+    threads = os.cpu_count() or 1
+    bodies, manifolds, _ = scenes.pile_64k()
+    iters = int(default_settings()["iteration_limit"])
+    cips = scenes.contact_count(manifolds) * iters
+    o = oracle.OracleSpace(default_settings(), bodies, manifolds)
+    o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+    for _ in range(max(args.warmup, 1)):
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+    el = time.perf_counter() - t0
+    value = cips * args.steps / el
+    line = {
+        "metric": "contact-iters/s", "value": value, "unit": "contact-iters/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "bodies": int(len(bodies)), "manifolds": int(len(manifolds)),
+                   "contacts": int(scenes.contact_count(manifolds)), "iterations": iters, "dt": float(DT),
+                   "order": "PermutationMapper (Solver.cs:255-260)"},
+        "cpu_baseline": {"value": value, "unit": "contact-iters/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps of the pile after {max(args.warmup, 1)} warm-up steps; "
+                                   "C++ port of Solver.UpdateMultithreaded (the C# reference has no runtime here)"},
+        "e2e": {"value": value, "unit": "contact-iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import Context, GpuSpace, default_settings, profile_step
+
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    bodies, manifolds, _ = scenes.pile_64k()
+    settings = default_settings()
+    iters = int(settings["iteration_limit"])
+    ctx = Context(local, settings)
+    space = GpuSpace(ctx, bodies, manifolds)
+    space.set_mode(N.MODE_GRAPH if args.mode == "graph" else N.MODE_PERSISTENT)
+    colours = space.colouring()[2]
+
+    for _ in range(max(args.warmup, 3)):
+        space.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    live_m, _ = space.download_constraints()
+    contacts = int(live_m["contact_count"].sum())
+    cips = contacts * iters  # contact-iterations per step
+
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    step_ms, solve_ms = [], []
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            space.step(DT, N.STEP_ALL)
+            step_ms.append(space.last_step_ms())
+            if args.mode == "graph":
+                solve_ms.append(float(space.last_step_phase_ms()[3]))
+    torch.cuda.synchronize()
+    total_ms = float(sum(step_ms))
+    launches = space.last_step_launches() * args.steps
+    if pg:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+        pg.barrier()
+    value = world * cips * args.steps / (total_ms / 1000.0)
+
+    # roofline of the solve kernel: census of executed work on one instrumented step
+    prof = profile_step(space, DT, N.STEP_ALL)
+    bytes_per_step = float(prof["solve_algorithmic_bytes"])
+    solve_launches = int(prof["solve_launches"])
+    if solve_ms:
+        mean_solve_s = statistics.mean(solve_ms) / 1000.0
+    else:
+        mean_solve_s = float(prof["solve_ms"]) / 1000.0
+    peak, peak_kind = measured_hbm_peak()
+    achieved = bytes_per_step / mean_solve_s / 1e9 if mean_solve_s > 0 else 0.0
+    traffic = ncu_traffic_per_launch()
+    roofline = {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": traffic,
+                "algorithmic_bytes_per_launch": bytes_per_step / max(solve_launches, 1),
+                "launch_ms_avg": 1000.0 * mean_solve_s / max(solve_launches, 1),
+                "solve_launches_per_step": solve_launches,
+                "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
+                "kernel_only_ms_per_step": {k: float(prof[k]) for k in
+                                            ("refresh_ms", "force_ms", "prestep_ms", "warm_ms", "solve_ms",
+                                             "position_ms")}}
+
+    # e2e through the C ABI with pinned host records
+    e2e = None
+    if not args.no_e2e:
+        hb = torch.empty(bodies.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(N.BODY_DTYPE)
+        hm = torch.empty(manifolds.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(N.MANIFOLD_DTYPE)
+        hb[:] = space.download_bodies()
+        hm[:] = live_m
+        space.download_constraints(hm)
+        ctx.synchronize()
+        k = max(3, min(args.steps, 10))
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            space.upload_bodies(hb)
+            space.update_manifolds(hm)
+            space.step(DT, N.STEP_ALL)
+            space.download_bodies(hb)
+            space.download_constraints(hm)
+        el = time.perf_counter() - t0
+        h2d = hb.nbytes + hm.nbytes
+        d2h = 52 * len(hb) + 288 * len(hm)  # BodyOut and ManifoldOut records copied device -> host
+        e2e = {"value": world * cips * k / el, "unit": "contact-iters/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": 1000 * el / k}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(bodies, manifolds, cips, args.cpu_sample_seconds, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": "contact-iters/s", "value": value, "unit": "contact-iters/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "bodies": int(len(bodies)), "manifolds": int(len(manifolds)),
+                       "contacts": contacts, "iterations": iters, "colours": int(colours), "dt": float(DT),
+                       "step": "refresh+forces+solve+positions", "mode": args.mode,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between timed steps (512 MiB write)"},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    space.close()
+    ctx.close()
+    if pg:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

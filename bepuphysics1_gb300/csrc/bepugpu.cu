@@ -1,0 +1,1051 @@
+// C ABI of the GB300 solver (include/bepugpu.h): contexts, scenes, uploads,
+// colouring and the one-scene step path.
+//
+// One scene step is the device sequence
+//   refresh -> ForceUpdater -> prestep -> warm start (one sweep per colour) ->
+//   I x (one sweep per colour) -> PositionUpdater
+// run either as one kernel per sweep captured in a CUDA graph
+// (BEPUGPU_MODE_GRAPH) or as one cooperative persistent kernel that separates
+// the sweeps with a bounded grid barrier (BEPUGPU_MODE_PERSISTENT).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/bepugpu.h"
+#include "colouring.h"
+#include "solver_device.cuh"
+#include "bepugpu_internal.h"
+
+namespace bepugpu {
+
+// ------------------------------------------------------------------ kernels --
+__global__ void k_unpack_bodies(const bepugpu_body* __restrict__ rec, int n, BodySoA b) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bepugpu_body& r = rec[i];
+    bool dyn = r.is_dynamic != 0;
+    b.pos[i] = make_float4(r.position[0], r.position[1], r.position[2], dyn ? 1.f : 0.f);
+    b.quat[i] = make_float4(r.orientation[0], r.orientation[1], r.orientation[2], r.orientation[3]);
+    const float* L = r.local_inverse_inertia;
+    float l[9];
+    for (int k = 0; k < 9; k++) l[k] = dyn ? L[k] : 0.f;
+    b.vlin[i] = make_float4(r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2], dyn ? r.inverse_mass : 0.f);
+    b.vang[i] = make_float4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2], 0.f);
+    b.loc0[i] = make_float4(l[0], l[1], l[2], l[3]);
+    b.loc1[i] = make_float4(l[4], l[5], l[6], l[7]);
+    b.inv0[i] = make_float4(0, 0, 0, 0);
+    b.inv1[i] = make_float4(0, 0, 0, 0);
+}
+
+// World inverse inertia at upload (Entity orientation setter: R^T L R), so a
+// solve-only step without the force stage sees the same tensor as the oracle.
+__global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.count) return;
+    float4 q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i];
+    float qX2 = q.x + q.x, qY2 = q.y + q.y, qZ2 = q.z + q.z;
+    float XX = qX2 * q.x, YY = qY2 * q.y, ZZ = qZ2 * q.z;
+    float XY = qX2 * q.y, XZ = qX2 * q.z, XW = qX2 * q.w;
+    float YZ = qY2 * q.z, YW = qY2 * q.w, ZW = qZ2 * q.w;
+    float R11 = 1 - YY - ZZ, R21 = XY - ZW, R31 = XZ + YW;
+    float R12 = XY + ZW, R22 = 1 - XX - ZZ, R32 = YZ - XW;
+    float R13 = XZ - YW, R23 = YZ + XW, R33 = 1 - XX - YY;
+    float L11 = l0.x, L12 = l0.y, L13 = l0.z, L21 = l0.w, L22 = l1.x, L23 = l1.y, L31 = l1.z, L32 = l1.w,
+          L33 = localM33[i];
+    float m11 = R11 * L11 + R21 * L21 + R31 * L31;
+    float m12 = R11 * L12 + R21 * L22 + R31 * L32;
+    float m13 = R11 * L13 + R21 * L23 + R31 * L33;
+    float m21 = R12 * L11 + R22 * L21 + R32 * L31;
+    float m22 = R12 * L12 + R22 * L22 + R32 * L32;
+    float m23 = R12 * L13 + R22 * L23 + R32 * L33;
+    float m31 = R13 * L11 + R23 * L21 + R33 * L31;
+    float m32 = R13 * L12 + R23 * L22 + R33 * L32;
+    float m33 = R13 * L13 + R23 * L23 + R33 * L33;
+    float4 a, c, w = b.vang[i];
+    a.x = m11 * R11 + m12 * R21 + m13 * R31;
+    a.y = m11 * R12 + m12 * R22 + m13 * R32;
+    a.z = m11 * R13 + m12 * R23 + m13 * R33;
+    a.w = m21 * R11 + m22 * R21 + m23 * R31;
+    c.x = m21 * R12 + m22 * R22 + m23 * R32;
+    c.y = m21 * R13 + m22 * R23 + m23 * R33;
+    c.z = m31 * R11 + m32 * R21 + m33 * R31;
+    c.w = m31 * R12 + m32 * R22 + m33 * R32;
+    w.w = m31 * R13 + m32 * R23 + m33 * R33;
+    b.inv0[i] = a;
+    b.inv1[i] = c;
+    b.vang[i] = w;
+}
+
+__global__ void k_pack_bodies(BodySoA b, BodyOut* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.count) return;
+    float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i];
+    BodyOut o;
+    o.p[0] = p.x; o.p[1] = p.y; o.p[2] = p.z;
+    o.q[0] = q.x; o.q[1] = q.y; o.q[2] = q.z; o.q[3] = q.w;
+    o.v[0] = v.x; o.v[1] = v.y; o.v[2] = v.z;
+    o.w[0] = w.x; o.w[1] = w.y; o.w[2] = w.z;
+    out[i] = o;
+}
+
+// Manifold records -> slots (slot_of[i] is the colour-order slot of record i).
+__global__ void k_unpack_manifolds(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
+                                   int n, ManifoldSoA m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bepugpu_manifold& r = rec[i];
+    int s = slot_of[i];
+    int cap = m.capacity;
+    int count = r.contact_count < 0 ? 0 : (r.contact_count > 4 ? 4 : r.contact_count);
+    m.head[s] = make_int4(r.body_a, r.body_b, count | (int)(r.flags << 8), i);
+    for (int k = 0; k < 4; k++) {
+        const bepugpu_contact& c = r.contacts[k];
+        m.cpos[k * cap + s] = make_float4(c.position[0], c.position[1], c.position[2], c.penetration_depth);
+        m.cnrm[k * cap + s] = make_float4(c.normal[0], c.normal[1], c.normal[2], __int_as_float(c.id));
+        m.offA[k * cap + s] = make_float4(c.local_offset_a[0], c.local_offset_a[1], c.local_offset_a[2],
+                                          c.base_penetration_depth);
+        m.offB[k * cap + s] = make_float4(c.local_offset_b[0], c.local_offset_b[1], c.local_offset_b[2], 0.f);
+    }
+    float pa[4];
+    for (int k = 0; k < 4; k++) pa[k] = k < count ? r.contacts[k].penetration_impulse : 0.f;
+    m.penacc[s] = make_float4(pa[0], pa[1], pa[2], pa[3]);
+    bool live = count > 0;
+    m.fricacc[s] = make_float4(live ? r.sliding_impulse[0] : 0.f, live ? r.sliding_impulse[1] : 0.f,
+                               live ? r.twist_impulse : 0.f, 0.f);
+    m.saxis[s] = make_float4(r.sliding_axis[0], r.sliding_axis[1], r.sliding_axis[2], 0.f);
+    m.mat[s] = make_float4(r.kinetic_friction, r.static_friction, r.bounciness, 0.f);
+    m.state[s] = make_uint2(0u, 0u);
+}
+
+__global__ void k_pack_manifolds(ManifoldSoA m, ManifoldOut* __restrict__ out) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= m.count) return;
+    int cap = m.capacity;
+    int4 h = m.head[s];
+    ManifoldOut o;
+    o.source = h.w;
+    o.count = h.z & 0xff;
+    float4 pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
+    float acc[4] = {pa.x, pa.y, pa.z, pa.w};
+    for (int k = 0; k < 4; k++) {
+        float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s], oa = m.offA[k * cap + s], ob = m.offB[k * cap + s];
+        o.c[k].pos[0] = cp.x; o.c[k].pos[1] = cp.y; o.c[k].pos[2] = cp.z; o.c[k].depth = cp.w;
+        o.c[k].nrm[0] = cn.x; o.c[k].nrm[1] = cn.y; o.c[k].nrm[2] = cn.z; o.c[k].id = __float_as_int(cn.w);
+        o.c[k].offa[0] = oa.x; o.c[k].offa[1] = oa.y; o.c[k].offa[2] = oa.z; o.c[k].base = oa.w;
+        o.c[k].offb[0] = ob.x; o.c[k].offb[1] = ob.y; o.c[k].offb[2] = ob.z;
+        o.c[k].acc = acc[k];
+    }
+    o.sliding[0] = f.x; o.sliding[1] = f.y; o.twist = f.z;
+    o.axis[0] = ax.x; o.axis[1] = ax.y; o.axis[2] = ax.z;
+    out[s] = o;
+}
+
+__global__ void k_refresh(ManifoldSoA m, BodySoA b, StepParams p) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < m.count) RefreshManifold(m, b, s, p);
+}
+__global__ void k_force(BodySoA b, StepParams p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.count) ForceUpdateBody(b, i, p);
+}
+__global__ void k_position(BodySoA b, StepParams p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.count) PositionUpdateBody(b, i, p);
+}
+__global__ void k_prestep(ManifoldSoA m, BodySoA b, StepParams p) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < m.count) PrestepManifold(m, b, s, p);
+}
+
+__device__ __forceinline__ void LoadPair(const BodySoA& b, int4 h, BodyState& A, BodyState& B) {
+    if (h.x >= 0) LoadBody(b, h.x, A);
+    if (h.y >= 0) LoadBody(b, h.y, B);
+}
+__device__ __forceinline__ void StorePair(const BodySoA& b, int4 h, uint32_t st, const BodyState& A,
+                                          const BodyState& B) {
+    if (st & kDynA) StoreVelocity(b, h.x, A);
+    if (st & kDynB) StoreVelocity(b, h.y, B);
+}
+
+__device__ __forceinline__ void WarmSlot(const ManifoldSoA& m, const BodySoA& b, int s) {
+    uint2 state = m.state[s];
+    if (!(state.x & kGroupActive)) return;
+    int4 h = m.head[s];
+    BodyState A, B;
+    LoadPair(b, h, A, B);
+    WarmStartManifold(m, s, A, B, state.x, h.z & 0xff);
+    StorePair(b, h, state.x, A, B);
+}
+__device__ __forceinline__ void SolveSlot(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
+    uint2 state = m.state[s];
+    if (!(state.x & kGroupActive)) return;
+    int4 h = m.head[s];
+    BodyState A, B;
+    LoadPair(b, h, A, B);
+    SolveManifold(m, s, A, B, state, h.z & 0xff, p);
+    StorePair(b, h, state.x, A, B);
+    m.state[s] = state;
+}
+
+__global__ void k_warm(ManifoldSoA m, BodySoA b, int begin, int end) {
+    int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < end) WarmSlot(m, b, s);
+}
+__global__ void k_solve(ManifoldSoA m, BodySoA b, StepParams p, int begin, int end) {
+    int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < end) SolveSlot(m, b, s, p);
+}
+
+// Bounded grid barrier for the cooperative kernel.  Thread 0 of each block
+// arrives on a counter; the last arrival resets it and bumps the generation.
+// A wait that outlives kBarrierSpinLimit polls sets *err and the kernel returns.
+constexpr long long kBarrierSpinLimit = 1ll << 24;
+__device__ __forceinline__ bool GridBarrier(unsigned int* counter, volatile unsigned int* generation,
+                                            unsigned int& localGen, volatile int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int g = localGen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(counter, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(counter, 0u);
+            __threadfence();
+            atomicAdd((unsigned int*)generation, 1u);
+        } else {
+            long long spins = 0;
+            while (*generation == g) {
+                if (++spins > kBarrierSpinLimit) {
+                    *err = BEPUGPU_TIMEOUT;
+                    break;
+                }
+                if (*err) break;
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    localGen++;
+    __syncthreads();
+    return *err == 0;
+}
+
+struct PersistentArgs {
+    ManifoldSoA m;
+    BodySoA b;
+    StepParams p;
+    const int* colourOffsets;  // manifold slots, colours + 1 entries
+    int colours;
+    uint32_t flags;
+    unsigned int* counter;
+    unsigned int* generation;
+    int* err;
+};
+
+__global__ void k_persistent(PersistentArgs a) {
+    unsigned int localGen = *(volatile unsigned int*)a.generation;
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    volatile int* err = a.err;
+    __syncthreads();
+    if (a.flags & BEPUGPU_STEP_REFRESH_CONTACTS) {
+        for (int s = tid; s < a.m.count; s += stride) RefreshManifold(a.m, a.b, s, a.p);
+        if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
+    }
+    if (a.flags & BEPUGPU_STEP_FORCES) {
+        for (int i = tid; i < a.b.count; i += stride) ForceUpdateBody(a.b, i, a.p);
+        if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
+    }
+    if (a.flags & BEPUGPU_STEP_SOLVE) {
+        for (int s = tid; s < a.m.count; s += stride) PrestepManifold(a.m, a.b, s, a.p);
+        if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
+        for (int c = 0; c < a.colours; c++) {
+            for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride) WarmSlot(a.m, a.b, s);
+            if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
+        }
+        for (int it = 0; it < a.p.iterationLimit; it++)
+            for (int c = 0; c < a.colours; c++) {
+                for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride)
+                    SolveSlot(a.m, a.b, s, a.p);
+                if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
+            }
+    }
+    if (a.flags & BEPUGPU_STEP_POSITIONS) {
+        for (int i = tid; i < a.b.count; i += stride) PositionUpdateBody(a.b, i, a.p);
+    }
+}
+
+
+// Census before a solve sweep: active manifolds of the sweep and their
+// algorithmic bytes 76*d + 136 + 48*c.
+__global__ void k_census(ManifoldSoA m, int begin, int end, unsigned long long* acc) {
+    int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long bytes = 0, visits = 0, contacts = 0;
+    if (s < end) {
+        uint2 st = m.state[s];
+        if (st.x & kGroupActive) {
+            int c = m.head[s].z & 0xff;
+            int d = ((st.x & kDynA) ? 1 : 0) + ((st.x & kDynB) ? 1 : 0);
+            bytes = 76ull * d + 136ull + 48ull * c;
+            visits = 1;
+            contacts = (unsigned long long)c;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bytes += __shfl_down_sync(0xffffffffu, bytes, o);
+        visits += __shfl_down_sync(0xffffffffu, visits, o);
+        contacts += __shfl_down_sync(0xffffffffu, contacts, o);
+    }
+    if ((threadIdx.x & 31) == 0 && visits) {
+        atomicAdd(acc, bytes);
+        atomicAdd(acc + 1, visits);
+        atomicAdd(acc + 2, contacts);
+    }
+}
+
+// ------------------------------------------------------------------ host side --
+static inline int Blocks(int n, int t) { return (n + t - 1) / t; }
+
+void Context::SetError(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    lastError = buf;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            ctx->SetError("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return BEPUGPU_CUDA_ERROR;                                                        \
+        }                                                                                     \
+    } while (0)
+
+static size_t Align(size_t x) { return (x + 255) & ~(size_t)255; }
+
+Scene::~Scene() {
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    if (arena) cudaFree(arena);
+    if (staging) cudaFree(staging);
+    if (counter) cudaFree(counter);
+    if (evStart) cudaEventDestroy(evStart);
+    if (evStop) cudaEventDestroy(evStop);
+    for (auto e : evPhase)
+        if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+StepParams MakeParams(const bepugpu_settings& s, float dt) {
+    StepParams p;
+    p.dt = dt;
+    p.updateRate = 1 / dt;
+    p.gravityDt[0] = s.gravity[0] * dt;
+    p.gravityDt[1] = s.gravity[1] * dt;
+    p.gravityDt[2] = s.gravity[2] * dt;
+    p.iterationLimit = s.iteration_limit < 0 ? 0 : s.iteration_limit;
+    p.maximumIterationCount = s.maximum_iteration_count;
+    p.minimumIterationCount = s.minimum_iteration_count;
+    p.minimumImpulse = s.minimum_impulse;
+    p.softness = s.softness;
+    p.recoveryStiffness = s.penetration_recovery_stiffness;
+    p.maxRecoverySpeed = s.maximum_penetration_recovery_speed;
+    p.staticThreshold = s.static_friction_velocity_threshold;
+    p.twistFactor = s.twist_friction_factor;
+    p.bounceThreshold = s.bounciness_velocity_threshold;
+    p.allowedPenetration = s.allowed_penetration;
+    p.invalidationLengthSquared = s.contact_invalidation_length_squared;
+    p.maximumContactDistance = s.maximum_contact_distance;
+    return p;
+}
+
+// (float)Math.Pow(MathHelper.Clamp(1 - d, 0, 1), dt) (EntityBase.cs:943,952),
+// computed on the host in double like System.Math.Pow.
+static float DampingFactor(float d, float dt) {
+    float c = 1 - d;
+    c = c < 0 ? 0 : (c > 1 ? 1 : c);
+    return (float)std::pow((double)c, (double)dt);
+}
+
+bepugpu_status Scene::RefreshDamping(Context* ctx, float dt) {
+    if (!dampDirty && dt == dampDt) return BEPUGPU_OK;
+    int n = b.count;
+    float lastD = NAN, lastF = 0, lastA = NAN, lastG = 0;
+    for (int i = 0; i < n; i++) {
+        float ld = hostLinDamp[i], ad = hostAngDamp[i];
+        float lin = ld + 0.f, ang = ad + 0.f;
+        uint32_t flags = (lin > 0 ? 1u : 0u) | (ang > 0 ? 2u : 0u);
+        if (!(ld == lastD)) { lastD = ld; lastF = DampingFactor(lin, dt); }
+        if (!(ad == lastA)) { lastA = ad; lastG = DampingFactor(ang, dt); }
+        float fbits;
+        std::memcpy(&fbits, &flags, 4);
+        hostDamp[i] = make_float4(lastF, lastG, hostLocalM33[i], fbits);
+    }
+    CK(cudaMemcpyAsync(b.damp, hostDamp.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, stream));
+    dampDirty = false;
+    dampDt = dt;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj) {
+    maxBodies = nb; maxManifolds = nm; maxJoints = nj;
+    size_t B = nb ? nb : 1, M = nm ? nm : 1;
+    size_t bytes = 0;
+    auto take = [&](size_t n) { size_t o = bytes; bytes += Align(n); return o; };
+    size_t oPos = take(16 * B), oQuat = take(16 * B), oVlin = take(16 * B), oVang = take(16 * B),
+           oInv0 = take(16 * B), oInv1 = take(16 * B), oLoc0 = take(16 * B), oLoc1 = take(16 * B),
+           oDamp = take(16 * B), oM33 = take(4 * B);
+    size_t oHead = take(16 * M), oCpos = take(64 * M), oCnrm = take(64 * M), oOffA = take(64 * M),
+           oOffB = take(64 * M), oMat = take(16 * M), oPen = take(16 * M), oFric = take(16 * M),
+           oAxis = take(16 * M), oPj0 = take(64 * M), oPj1 = take(64 * M), oPj2 = take(64 * M),
+           oS0 = take(16 * M), oS1 = take(16 * M), oS3 = take(16 * M), oS4 = take(16 * M), oS5 = take(16 * M),
+           oS6 = take(16 * M), oS7 = take(16 * M), oLev = take(16 * M), oState = take(8 * M),
+           oSlot = take(4 * M), oOffs = take(4 * (M + 2));
+    arenaBytes = bytes;
+    cudaError_t e = cudaMalloc(&arena, bytes);
+    if (e != cudaSuccess) {
+        arena = nullptr;
+        ctx->SetError("scene arena of %zu bytes: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
+    }
+    char* base = (char*)arena;
+    b.pos = (float4*)(base + oPos); b.quat = (float4*)(base + oQuat); b.vlin = (float4*)(base + oVlin);
+    b.vang = (float4*)(base + oVang); b.inv0 = (float4*)(base + oInv0); b.inv1 = (float4*)(base + oInv1);
+    b.loc0 = (float4*)(base + oLoc0); b.loc1 = (float4*)(base + oLoc1); b.damp = (float4*)(base + oDamp);
+    localM33 = (float*)(base + oM33);
+    b.count = 0;
+    m.head = (int4*)(base + oHead); m.cpos = (float4*)(base + oCpos); m.cnrm = (float4*)(base + oCnrm);
+    m.offA = (float4*)(base + oOffA); m.offB = (float4*)(base + oOffB); m.mat = (float4*)(base + oMat);
+    m.penacc = (float4*)(base + oPen); m.fricacc = (float4*)(base + oFric); m.saxis = (float4*)(base + oAxis);
+    m.pj0 = (float4*)(base + oPj0); m.pj1 = (float4*)(base + oPj1); m.pj2 = (float4*)(base + oPj2);
+    m.s0 = (float4*)(base + oS0); m.s1 = (float4*)(base + oS1); m.s3 = (float4*)(base + oS3);
+    m.s4 = (float4*)(base + oS4); m.s5 = (float4*)(base + oS5); m.s6 = (float4*)(base + oS6);
+    m.s7 = (float4*)(base + oS7); m.lever = (float4*)(base + oLev); m.state = (uint2*)(base + oState);
+    m.count = 0;
+    m.capacity = (int)M;
+    slotOf = (int32_t*)(base + oSlot);
+    colourOffsetsDev = (int32_t*)(base + oOffs);
+    CK(cudaMemset(arena, 0, bytes));
+    stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
+    stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
+    CK(cudaMalloc(&staging, stagingBytes));
+    CK(cudaMalloc(&counter, 256));
+    CK(cudaMemset(counter, 0, 256));
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&evStart));
+    CK(cudaEventCreate(&evStop));
+    for (auto& e : evPhase) CK(cudaEventCreate(&e));
+    return BEPUGPU_OK;
+}
+
+bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t flags) {
+    if (graphExec) { cudaGraphExecDestroy(graphExec); graphExec = nullptr; }
+    const int T = 128;
+    launchesPerStep = 0;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    int nm = m.count, nb = b.count;
+    // Phase events become event-record nodes of the graph: their elapsed times
+    // are the device time of each phase of every launched step.
+    CK(cudaEventRecord(evPhase[0], stream));
+    if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {
+        k_refresh<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+    }
+    if ((flags & BEPUGPU_STEP_FORCES) && nb) {
+        k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
+    }
+    CK(cudaEventRecord(evPhase[1], stream));
+    bool solve = (flags & BEPUGPU_STEP_SOLVE) && nm;
+    if (solve) {
+        k_prestep<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+    }
+    CK(cudaEventRecord(evPhase[2], stream));
+    if (solve) {
+        for (int c = 0; c < colouring.colours; c++) {
+            int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
+            if (b1 > b0) { k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, b0, b1); launchesPerStep++; }
+        }
+    }
+    CK(cudaEventRecord(evPhase[3], stream));
+    if (solve) {
+        for (int it = 0; it < p.iterationLimit; it++)
+            for (int c = 0; c < colouring.colours; c++) {
+                int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
+                if (b1 > b0) { k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, p, b0, b1); launchesPerStep++; }
+            }
+    }
+    CK(cudaEventRecord(evPhase[4], stream));
+    if ((flags & BEPUGPU_STEP_POSITIONS) && nb) {
+        k_position<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
+    }
+    CK(cudaEventRecord(evPhase[5], stream));
+    cudaGraph_t graph;
+    cudaError_t e = cudaStreamEndCapture(stream, &graph);
+    if (e != cudaSuccess) {
+        ctx->SetError("graph capture: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    e = cudaGraphInstantiate(&graphExec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        graphExec = nullptr;
+        ctx->SetError("graph instantiate: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    graphDt = p.dt;
+    graphFlags = flags;
+    graphVersion = version;
+    graphIterations = p.iterationLimit;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t flags) {
+    const int T = 256;
+    if (persistentBlocks == 0) {
+        int perSm = 0;
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_persistent, T, 0));
+        if (perSm < 1) {
+            ctx->SetError("persistent kernel cannot be resident");
+            return BEPUGPU_CUDA_ERROR;
+        }
+        persistentBlocks = std::min(perSm, 2) * ctx->smCount;
+    }
+    PersistentArgs a;
+    a.m = m; a.b = b; a.p = p;
+    a.colourOffsets = colourOffsetsDev;
+    a.colours = colouring.colours;
+    a.flags = flags;
+    a.counter = (unsigned int*)counter;
+    a.generation = (unsigned int*)counter + 32;
+    a.err = (int*)counter + 64;
+    void* args[] = {&a};
+    CK(cudaLaunchCooperativeKernel((void*)k_persistent, dim3(persistentBlocks), dim3(T), args, 0, stream));
+    launchesPerStep = 1;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
+    if (!(dt > 0) || !std::isfinite(dt)) {
+        ctx->SetError("dt must be positive and finite");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    bepugpu_status st = RefreshDamping(ctx, dt);
+    if (st != BEPUGPU_OK) return st;
+    StepParams p = MakeParams(ctx->settings, dt);
+    CK(cudaEventRecord(evStart, stream));
+    if (mode == BEPUGPU_MODE_PERSISTENT) {
+        st = RunPersistent(ctx, p, flags);
+        if (st != BEPUGPU_OK) return st;
+    } else {
+        if (!graphExec || graphDt != dt || graphFlags != flags || graphVersion != version ||
+            graphIterations != p.iterationLimit) {
+            st = BuildGraph(ctx, p, flags);
+            if (st != BEPUGPU_OK) return st;
+        }
+        CK(cudaGraphLaunch(graphExec, stream));
+    }
+    CK(cudaEventRecord(evStop, stream));
+    stepped = true;
+    return BEPUGPU_OK;
+}
+
+}  // namespace bepugpu
+
+// ================================================================== C ABI ==
+using namespace bepugpu;
+
+#define CTX_CHECK(ctx)                               \
+    do {                                             \
+        if (!(ctx)) return BEPUGPU_INVALID_ARGUMENT; \
+        cudaSetDevice((ctx)->device);                \
+    } while (0)
+
+static Scene* FindScene(Context* ctx, int32_t id) {
+    auto it = ctx->scenes.find(id);
+    if (it == ctx->scenes.end()) {
+        ctx->SetError("scene %d does not exist", id);
+        return nullptr;
+    }
+    return it->second.get();
+}
+
+extern "C" {
+
+int32_t bepugpu_abi_version(void) { return BEPUGPU_ABI_VERSION; }
+
+uint32_t bepugpu_record_size(int32_t kind) {
+    switch (kind) {
+        case 0: return sizeof(bepugpu_settings);
+        case 1: return sizeof(bepugpu_body);
+        case 2: return sizeof(bepugpu_contact);
+        case 3: return sizeof(bepugpu_manifold);
+        case 4: return sizeof(bepugpu_joint);
+        default: return 0;
+    }
+}
+
+void bepugpu_default_settings(bepugpu_settings* s) {
+    std::memset(s, 0, sizeof(*s));
+    s->gravity[0] = 0.f; s->gravity[1] = -9.81f; s->gravity[2] = 0.f;
+    s->iteration_limit = 10;
+    s->minimum_impulse = .001f;
+    s->minimum_iteration_count = 1;
+    s->maximum_iteration_count = 0x7fffffff;
+    s->softness = .001f;
+    s->penetration_recovery_stiffness = .2f;
+    s->maximum_penetration_recovery_speed = 2.f;
+    s->static_friction_velocity_threshold = .2f;
+    s->twist_friction_factor = 1.f;
+    s->bounciness_velocity_threshold = 1.f;
+    s->allowed_penetration = .01f;
+    s->contact_invalidation_length_squared = .01f;
+    s->maximum_contact_distance = .1f;
+}
+
+static bepugpu_status ValidateSettings(Context* ctx, const bepugpu_settings* s) {
+    if (s->iteration_limit < 0 || s->iteration_limit > 65535) {
+        ctx->SetError("iteration_limit must be in [0, 65535]");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->minimum_iteration_count < 0 || s->minimum_iteration_count > 14) {
+        ctx->SetError("minimum_iteration_count must be in [0, 14]");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_create(int32_t device, const bepugpu_settings* settings, bepugpu_context** out) {
+    if (!out) return BEPUGPU_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return BEPUGPU_CUDA_ERROR;
+    auto* ctx = new Context();
+    ctx->device = device;
+    if (settings) ctx->settings = *settings;
+    else bepugpu_default_settings(&ctx->settings);
+    if (ValidateSettings(ctx, &ctx->settings) != BEPUGPU_OK) { delete ctx; return BEPUGPU_INVALID_ARGUMENT; }
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return BEPUGPU_CUDA_ERROR; }
+    cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, device);
+    *out = reinterpret_cast<bepugpu_context*>(ctx);
+    return BEPUGPU_OK;
+}
+
+void bepugpu_destroy(bepugpu_context* c) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    ctx->batch.reset();
+    ctx->scenes.clear();
+    delete ctx;
+}
+
+const char* bepugpu_last_error(bepugpu_context* c) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    return ctx ? ctx->lastError.c_str() : "null context";
+}
+
+bepugpu_status bepugpu_set_settings(bepugpu_context* c, const bepugpu_settings* s) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (!s) return BEPUGPU_INVALID_ARGUMENT;
+    bepugpu_status st = ValidateSettings(ctx, s);
+    if (st != BEPUGPU_OK) return st;
+    ctx->settings = *s;
+    for (auto& kv : ctx->scenes) kv.second->version++;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_synchronize(bepugpu_context* c) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    CK(cudaDeviceSynchronize());
+    for (auto& kv : ctx->scenes) {
+        Scene& s = *kv.second;
+        if (s.mode == BEPUGPU_MODE_PERSISTENT && s.counter) {
+            int err = 0;
+            CK(cudaMemcpy(&err, (int*)s.counter + 64, sizeof(int), cudaMemcpyDeviceToHost));
+            if (err) {
+                CK(cudaMemset((int*)s.counter + 64, 0, sizeof(int)));
+                ctx->SetError("persistent step: a grid barrier wait ran out");
+                return BEPUGPU_TIMEOUT;
+            }
+        }
+    }
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_scene_create(bepugpu_context* c, uint32_t nb, uint32_t nm, uint32_t nj, int32_t* out) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (!out) return BEPUGPU_INVALID_ARGUMENT;
+    if (nb > (1u << 30) || nm > (1u << 28) || nj > (1u << 28)) {
+        ctx->SetError("scene capacity too large");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    auto s = std::make_unique<Scene>();
+    bepugpu_status st = s->Allocate(ctx, nb, nm, nj);
+    if (st != BEPUGPU_OK) return st;
+    int32_t id = ctx->nextScene++;
+    s->id = id;
+    ctx->scenes[id] = std::move(s);
+    *out = id;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_scene_destroy(bepugpu_context* c, int32_t id) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (!FindScene(ctx, id)) return BEPUGPU_NOT_FOUND;
+    ctx->scenes.erase(id);
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (n > s->maxBodies || (n && !bodies)) {
+        ctx->SetError("body count %u exceeds scene capacity %u", n, s->maxBodies);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);
+    s->hostDynamic.resize(n);
+    for (uint32_t i = 0; i < n; i++) {
+        s->hostLinDamp[i] = bodies[i].linear_damping;
+        s->hostAngDamp[i] = bodies[i].angular_damping;
+        s->hostDynamic[i] = bodies[i].is_dynamic ? 1 : 0;
+        s->hostLocalM33[i] = bodies[i].is_dynamic ? bodies[i].local_inverse_inertia[8] : 0.f;
+    }
+    if (n != (uint32_t)s->b.count) s->version++;
+    s->b.count = (int)n;
+    s->dampDirty = true;
+    if (n) {
+        CK(cudaMemcpyAsync(s->staging, bodies, sizeof(bepugpu_body) * n, cudaMemcpyHostToDevice, s->stream));
+        k_unpack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging, (int)n, s->b);
+        CK(cudaMemcpyAsync(s->localM33, s->hostLocalM33.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+        k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
+        CK(cudaGetLastError());
+        // The staging buffer and host vectors are reused by the next call: wait.
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    return BEPUGPU_OK;
+}
+
+static bepugpu_status UploadManifoldRecords(Context* ctx, Scene* s, const bepugpu_manifold* rec, uint32_t n) {
+    if (!n) return BEPUGPU_OK;
+    CK(cudaMemcpyAsync(s->staging, rec, sizeof(bepugpu_manifold) * n, cudaMemcpyHostToDevice, s->stream));
+    k_unpack_manifolds<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_manifold*)s->staging, s->slotOf,
+                                                               (int)n, s->m);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const bepugpu_manifold* man, uint32_t nm,
+                                          const bepugpu_joint* joints, uint32_t nj) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (nm > s->maxManifolds || nj > s->maxJoints || (nm && !man) || (nj && !joints)) {
+        ctx->SetError("constraint counts exceed scene capacity");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (nj) {
+        ctx->SetError("joint constraints are not available in this build");
+        return BEPUGPU_INVALID_OPERATION;
+    }
+    int nb = s->b.count;
+    std::vector<int32_t> a(nm + nj), bb(nm + nj);
+    for (uint32_t i = 0; i < nm; i++) {
+        a[nj + i] = man[i].body_a;
+        bb[nj + i] = man[i].body_b;
+        if (man[i].contact_count < 0 || man[i].contact_count > 4) {
+            ctx->SetError("manifold %u has contact_count %d (0..4 allowed)", i, man[i].contact_count);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (man[i].body_a == man[i].body_b && man[i].body_a >= 0) {
+            ctx->SetError("manifold %u connects body %d to itself", i, man[i].body_a);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+    }
+    if (!ColourSolverList(a.data(), bb.data(), (int32_t)(nm + nj), s->hostDynamic.data(), nb, s->colouring)) {
+        ctx->SetError("a constraint references a body outside [0, %d)", nb);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    // Manifold slots: colour-sorted order restricted to manifolds.
+    const Colouring& col = s->colouring;
+    s->manifoldOffsets.assign(col.colours + 1, 0);
+    std::vector<int32_t> slotOf(nm);
+    int slot = 0;
+    for (int cc = 0; cc < col.colours; cc++) {
+        s->manifoldOffsets[cc] = slot;
+        for (int k = col.offsets[cc]; k < col.offsets[cc + 1]; k++) {
+            int u = col.order[k];
+            if (u >= (int)nj) slotOf[u - nj] = slot++;
+        }
+    }
+    s->manifoldOffsets[col.colours] = slot;
+    s->m.count = (int)nm;
+    s->jointCount = nj;
+    s->version++;
+    if (nm) {
+        CK(cudaMemcpyAsync(s->slotOf, slotOf.data(), sizeof(int32_t) * nm, cudaMemcpyHostToDevice, s->stream));
+    }
+    CK(cudaMemcpyAsync(s->colourOffsetsDev, s->manifoldOffsets.data(), sizeof(int32_t) * (col.colours + 1),
+                       cudaMemcpyHostToDevice, s->stream));
+    s->hostSlotOf = std::move(slotOf);
+    return UploadManifoldRecords(ctx, s, man, nm);
+}
+
+bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const bepugpu_manifold* man, uint32_t n) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (n != (uint32_t)s->m.count || (n && !man)) {
+        ctx->SetError("update_manifolds needs the %d manifolds of the last upload", s->m.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    return UploadManifoldRecords(ctx, s, man, n);
+}
+
+bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_body* bodies, uint32_t n) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (n != (uint32_t)s->b.count || (n && !bodies)) {
+        ctx->SetError("download_bodies needs exactly %d records", s->b.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (!n) return BEPUGPU_OK;
+    BodyOut* dev = (BodyOut*)s->staging;
+    k_pack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, dev);
+    s->hostBodyOut.resize(n);
+    CK(cudaMemcpyAsync(s->hostBodyOut.data(), dev, sizeof(BodyOut) * n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (uint32_t i = 0; i < n; i++) {
+        const BodyOut& o = s->hostBodyOut[i];
+        std::memcpy(bodies[i].position, o.p, sizeof(o.p));
+        std::memcpy(bodies[i].orientation, o.q, sizeof(o.q));
+        std::memcpy(bodies[i].linear_velocity, o.v, sizeof(o.v));
+        std::memcpy(bodies[i].angular_velocity, o.w, sizeof(o.w));
+    }
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_download_constraints(bepugpu_context* c, int32_t id, bepugpu_manifold* man, uint32_t nm,
+                                            bepugpu_joint* joints, uint32_t nj) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (nm != (uint32_t)s->m.count || nj != s->jointCount || (nm && !man) || (nj && !joints)) {
+        ctx->SetError("download_constraints needs %d manifolds and %u joints", s->m.count, s->jointCount);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (!nm) return BEPUGPU_OK;
+    ManifoldOut* dev = (ManifoldOut*)s->staging;
+    k_pack_manifolds<<<Blocks(nm, 256), 256, 0, s->stream>>>(s->m, dev);
+    s->hostManifoldOut.resize(nm);
+    CK(cudaMemcpyAsync(s->hostManifoldOut.data(), dev, sizeof(ManifoldOut) * nm, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    for (uint32_t k = 0; k < nm; k++) {
+        const ManifoldOut& o = s->hostManifoldOut[k];
+        bepugpu_manifold& r = man[o.source];
+        r.contact_count = o.count;
+        for (int j = 0; j < 4; j++) {
+            bepugpu_contact& cr = r.contacts[j];
+            if (j < o.count) {
+                std::memcpy(cr.position, o.c[j].pos, 12);
+                cr.penetration_depth = o.c[j].depth;
+                std::memcpy(cr.normal, o.c[j].nrm, 12);
+                cr.id = o.c[j].id;
+                std::memcpy(cr.local_offset_a, o.c[j].offa, 12);
+                std::memcpy(cr.local_offset_b, o.c[j].offb, 12);
+                cr.base_penetration_depth = o.c[j].base;
+                cr.penetration_impulse = o.c[j].acc;
+            } else {
+                std::memset(&cr, 0, sizeof(cr));
+            }
+        }
+        r.sliding_impulse[0] = o.sliding[0];
+        r.sliding_impulse[1] = o.sliding[1];
+        r.twist_impulse = o.twist;
+        std::memcpy(r.sliding_axis, o.axis, 12);
+    }
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_get_colouring(bepugpu_context* c, int32_t id, int32_t* colour, int32_t* order, uint32_t n,
+                                     uint32_t* colours) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (n != s->colouring.colour.size()) {
+        ctx->SetError("colouring has %zu entries", s->colouring.colour.size());
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (colour && n) std::memcpy(colour, s->colouring.colour.data(), 4 * n);
+    if (order && n) std::memcpy(order, s->colouring.order.data(), 4 * n);
+    if (colours) *colours = (uint32_t)s->colouring.colours;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_colour_list(const int32_t* a, const int32_t* b, uint32_t n, const uint8_t* dynamic,
+                                   uint32_t nb, int32_t* colour, int32_t* order, uint32_t* colours) {
+    if ((n && (!a || !b || !colour || !order)) || (nb && !dynamic)) return BEPUGPU_INVALID_ARGUMENT;
+    Colouring col;
+    if (!ColourSolverList(a, b, (int32_t)n, dynamic, (int32_t)nb, col)) return BEPUGPU_INVALID_ARGUMENT;
+    if (n) {
+        std::memcpy(colour, col.colour.data(), 4 * n);
+        std::memcpy(order, col.order.data(), 4 * n);
+    }
+    if (colours) *colours = (uint32_t)col.colours;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_set_solve_mode(bepugpu_context* c, int32_t id, int32_t mode) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (mode != BEPUGPU_MODE_GRAPH && mode != BEPUGPU_MODE_PERSISTENT) return BEPUGPU_INVALID_ARGUMENT;
+    s->mode = mode;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_step(bepugpu_context* c, int32_t id, float dt, uint32_t flags) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    return s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
+}
+
+bepugpu_status bepugpu_last_step_ms(bepugpu_context* c, int32_t id, float* ms) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!ms || !s->stepped) return BEPUGPU_INVALID_ARGUMENT;
+    CK(cudaEventSynchronize(s->evStop));
+    CK(cudaEventElapsedTime(ms, s->evStart, s->evStop));
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* c, int32_t id, float* phase_ms) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!phase_ms || !s->stepped || s->mode != BEPUGPU_MODE_GRAPH) {
+        ctx->SetError("phase times exist after a graph-mode step");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    CK(cudaEventSynchronize(s->evStop));
+    for (int k = 0; k < 5; k++) CK(cudaEventElapsedTime(&phase_ms[k], s->evPhase[k], s->evPhase[k + 1]));
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_last_step_launches(bepugpu_context* c, int32_t id, uint32_t* launches) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!launches) return BEPUGPU_INVALID_ARGUMENT;
+    *launches = s->launchesPerStep;
+    return BEPUGPU_OK;
+}
+
+
+bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, uint32_t flags,
+                                    bepugpu_phase_times* out) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!out || !(dt > 0)) return BEPUGPU_INVALID_ARGUMENT;
+    bepugpu_status st = s->RefreshDamping(ctx, dt);
+    if (st != BEPUGPU_OK) return st;
+    StepParams p = MakeParams(ctx->settings, dt);
+    std::memset(out, 0, sizeof(*out));
+    const int T = 128;
+    cudaStream_t q = s->stream;
+    std::vector<cudaEvent_t> ev;
+    auto mark = [&]() -> cudaEvent_t {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        cudaEventRecord(e, q);
+        ev.push_back(e);
+        return e;
+    };
+    struct Span { cudaEvent_t a, b; float* dst; };
+    std::vector<Span> spans;
+    unsigned long long* acc = (unsigned long long*)s->counter + 16;  // words 16..18 of the scratch block
+    CK(cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), q));
+    int nm = s->m.count, nb = s->b.count;
+    if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {
+        cudaEvent_t a = mark(); k_refresh<<<Blocks(nm, T), T, 0, q>>>(s->m, s->b, p); spans.push_back({a, mark(), &out->refresh_ms});
+    }
+    if ((flags & BEPUGPU_STEP_FORCES) && nb) {
+        cudaEvent_t a = mark(); k_force<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->force_ms});
+    }
+    if ((flags & BEPUGPU_STEP_SOLVE) && nm) {
+        cudaEvent_t a = mark(); k_prestep<<<Blocks(nm, T), T, 0, q>>>(s->m, s->b, p); spans.push_back({a, mark(), &out->prestep_ms});
+        for (int cc = 0; cc < s->colouring.colours; cc++) {
+            int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
+            if (b1 <= b0) continue;
+            cudaEvent_t e0 = mark(); k_warm<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, s->b, b0, b1);
+            spans.push_back({e0, mark(), &out->warm_ms});
+            out->warm_launches++;
+        }
+        for (int it = 0; it < p.iterationLimit; it++)
+            for (int cc = 0; cc < s->colouring.colours; cc++) {
+                int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
+                if (b1 <= b0) continue;
+                k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, b0, b1, acc);
+                cudaEvent_t e0 = mark(); k_solve<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, s->b, p, b0, b1);
+                spans.push_back({e0, mark(), &out->solve_ms});
+                out->solve_launches++;
+            }
+    }
+    if ((flags & BEPUGPU_STEP_POSITIONS) && nb) {
+        cudaEvent_t a = mark(); k_position<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->position_ms});
+    }
+    CK(cudaGetLastError());
+    unsigned long long h[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, q));
+    CK(cudaStreamSynchronize(q));
+    for (auto& sp : spans) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, sp.a, sp.b);
+        *sp.dst += ms;
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+    out->solve_algorithmic_bytes = (double)h[0];
+    out->solve_manifold_visits = (double)h[1];
+    out->solve_contact_visits = (double)h[2];
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_last_call_stats(bepugpu_context* c, uint32_t* launches, float* ms) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (launches) *launches = ctx->lastLaunches;
+    if (ms) *ms = ctx->lastMs;
+    return BEPUGPU_OK;
+}
+
+}  // extern "C"

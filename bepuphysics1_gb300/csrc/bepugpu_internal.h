@@ -1,0 +1,100 @@
+// Host-side objects behind the C ABI: contexts and scenes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/bepugpu.h"
+#include "colouring.h"
+#include "solver_device.cuh"
+
+namespace bepugpu {
+
+// Compact download records (device -> host), scattered into caller records.
+struct BodyOut {
+    float p[3], q[4], v[3], w[3];
+};
+struct ContactOut {
+    float pos[3], depth, nrm[3];
+    int32_t id;
+    float offa[3], base, offb[3], acc;
+};
+struct ManifoldOut {
+    int32_t source, count;
+    ContactOut c[4];
+    float sliding[2], twist, axis[3];
+};
+
+struct Context;
+struct BatchEngine;
+
+StepParams MakeParams(const bepugpu_settings& s, float dt);
+
+struct Scene {
+    int32_t id = 0;
+    uint32_t maxBodies = 0, maxManifolds = 0, maxJoints = 0;
+    void* arena = nullptr;
+    size_t arenaBytes = 0;
+    void* staging = nullptr;
+    size_t stagingBytes = 0;
+    void* counter = nullptr;  // grid barrier counter / generation / error word
+    BodySoA b{};
+    ManifoldSoA m{};
+    float* localM33 = nullptr;
+    int32_t* slotOf = nullptr;           // device: manifold record -> slot
+    int32_t* colourOffsetsDev = nullptr; // device: manifold slot range per colour
+    uint32_t jointCount = 0;
+    Colouring colouring;
+    std::vector<int32_t> manifoldOffsets;
+    std::vector<int32_t> hostSlotOf;
+    std::vector<float> hostLinDamp, hostAngDamp, hostLocalM33;
+    std::vector<uint8_t> hostDynamic;
+    std::vector<float4> hostDamp;
+    std::vector<BodyOut> hostBodyOut;
+    std::vector<ManifoldOut> hostManifoldOut;
+    bool dampDirty = true;
+    float dampDt = 0.f;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t evStart = nullptr, evStop = nullptr;
+    cudaEvent_t evPhase[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    bool stepped = false;
+    int32_t mode = BEPUGPU_MODE_GRAPH;
+    cudaGraphExec_t graphExec = nullptr;
+    float graphDt = 0.f;
+    uint32_t graphFlags = 0;
+    uint64_t version = 1, graphVersion = 0;
+    int graphIterations = -1;
+    uint32_t launchesPerStep = 0;
+    int persistentBlocks = 0;
+
+    ~Scene();
+    bepugpu_status Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj);
+    bepugpu_status RefreshDamping(Context* ctx, float dt);
+    bepugpu_status BuildGraph(Context* ctx, const StepParams& p, uint32_t flags);
+    bepugpu_status RunPersistent(Context* ctx, const StepParams& p, uint32_t flags);
+    bepugpu_status Step(Context* ctx, float dt, uint32_t flags);
+};
+
+struct BatchEngine {
+    virtual ~BatchEngine() = default;
+};
+
+struct Context {
+    int device = 0;
+    int smCount = 0;
+    bepugpu_settings settings{};
+    std::string lastError;
+    std::unordered_map<int32_t, std::unique_ptr<Scene>> scenes;
+    int32_t nextScene = 1;
+    std::unique_ptr<BatchEngine> batch;
+    uint32_t lastLaunches = 0;
+    float lastMs = 0.f;
+    void SetError(const char* fmt, ...);
+};
+
+}  // namespace bepugpu

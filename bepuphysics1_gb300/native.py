@@ -1,0 +1,203 @@
+"""ctypes binding of the C ABI (include/bepugpu.h) and the scene source
+(include/bepuscenes.h).
+
+Records cross the boundary as numpy structured arrays whose dtypes mirror the
+C structs; bepugpu_record_size() checks the layouts when the library loads.
+The binding fails loudly when libbepugpu.so is missing: there is no CPU
+fallback for the solver.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+LIB_DIR = Path(__file__).resolve().parent / "lib"
+
+SETTINGS_DTYPE = np.dtype([
+    ("gravity", "<f4", 3), ("iteration_limit", "<i4"), ("minimum_impulse", "<f4"),
+    ("minimum_iteration_count", "<i4"), ("maximum_iteration_count", "<i4"), ("softness", "<f4"),
+    ("penetration_recovery_stiffness", "<f4"), ("maximum_penetration_recovery_speed", "<f4"),
+    ("static_friction_velocity_threshold", "<f4"), ("twist_friction_factor", "<f4"),
+    ("bounciness_velocity_threshold", "<f4"), ("allowed_penetration", "<f4"),
+    ("contact_invalidation_length_squared", "<f4"), ("maximum_contact_distance", "<f4"),
+    ("reserved", "<i4", 4),
+])
+BODY_DTYPE = np.dtype([
+    ("position", "<f4", 3), ("orientation", "<f4", 4), ("linear_velocity", "<f4", 3),
+    ("angular_velocity", "<f4", 3), ("inverse_mass", "<f4"), ("local_inverse_inertia", "<f4", 9),
+    ("linear_damping", "<f4"), ("angular_damping", "<f4"), ("is_dynamic", "<i4"), ("reserved", "<i4"),
+])
+CONTACT_DTYPE = np.dtype([
+    ("position", "<f4", 3), ("normal", "<f4", 3), ("penetration_depth", "<f4"), ("id", "<i4"),
+    ("local_offset_a", "<f4", 3), ("local_offset_b", "<f4", 3), ("base_penetration_depth", "<f4"),
+    ("penetration_impulse", "<f4"),
+])
+MANIFOLD_DTYPE = np.dtype([
+    ("body_a", "<i4"), ("body_b", "<i4"), ("contact_count", "<i4"), ("flags", "<u4"),
+    ("kinetic_friction", "<f4"), ("static_friction", "<f4"), ("bounciness", "<f4"),
+    ("sliding_impulse", "<f4", 2), ("sliding_axis", "<f4", 3), ("twist_impulse", "<f4"), ("reserved", "<i4"),
+    ("contacts", CONTACT_DTYPE, 4),
+])
+JOINT_DTYPE = np.dtype([
+    ("type", "<i4"), ("body_a", "<i4"), ("body_b", "<i4"), ("flags", "<u4"),
+    ("anchor_a", "<f4", 3), ("anchor_b", "<f4", 3), ("axis_a", "<f4", 3), ("axis_b", "<f4", 3),
+    ("basis_a", "<f4", 3), ("basis_b", "<f4", 3), ("limit", "<f4", 4), ("spring", "<f4", 2),
+    ("impulse", "<f4", 8),
+])
+
+PILE_PARAMS_DTYPE = np.dtype([
+    ("nx", "<i4"), ("ny", "<i4"), ("nz", "<i4"), ("spacing", "<f4"), ("size_min", "<f4"), ("size_max", "<f4"),
+    ("density", "<f4"), ("mass", "<f4"), ("jitter", "<f4"), ("friction_min", "<f4"), ("friction_max", "<f4"),
+    ("ground_friction", "<f4"), ("ground_size", "<f4", 3), ("settle_penetration", "<f4"),
+    ("contact_distance", "<f4"), ("seed", "<u8"),
+], align=True)
+TOWER_PARAMS_DTYPE = np.dtype([
+    ("body_count", "<i4"), ("tower_min", "<i4"), ("tower_max", "<i4"), ("sphere_fraction", "<f4"),
+    ("friction", "<f4"), ("tower_spacing", "<f4"), ("settle_penetration", "<f4"), ("seed", "<u8"),
+], align=True)
+CHAIN_PARAMS_DTYPE = np.dtype([
+    ("chains", "<i4"), ("links", "<i4"), ("capsule_radius", "<f4"), ("capsule_length", "<f4"),
+    ("link_mass", "<f4"), ("swing_limit", "<f4"), ("loose_bodies", "<i4"), ("region", "<f4", 3),
+    ("seed", "<u8"),
+], align=True)
+
+PHASE_TIMES_DTYPE = np.dtype([
+    ("refresh_ms", "<f4"), ("force_ms", "<f4"), ("prestep_ms", "<f4"), ("warm_ms", "<f4"), ("solve_ms", "<f4"),
+    ("position_ms", "<f4"), ("solve_launches", "<u4"), ("warm_launches", "<u4"),
+    ("solve_algorithmic_bytes", "<f8"), ("solve_manifold_visits", "<f8"), ("solve_contact_visits", "<f8"),
+])
+
+# bepugpu_status
+OK, INVALID_ARGUMENT, OUT_OF_MEMORY, ADMISSION_REFUSED, CUDA_ERROR, TIMEOUT, NAN_DETECTED, NOT_FOUND, \
+    QUEUE_FULL, INVALID_OPERATION = range(10)
+STATUS_NAMES = ["OK", "INVALID_ARGUMENT", "OUT_OF_MEMORY", "ADMISSION_REFUSED", "CUDA_ERROR", "TIMEOUT",
+                "NAN_DETECTED", "NOT_FOUND", "QUEUE_FULL", "INVALID_OPERATION"]
+
+STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_ALL = 1, 2, 4, 8, 15
+MODE_GRAPH, MODE_PERSISTENT = 0, 1
+MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE = 1, 2
+JOINT_BALL_SOCKET, JOINT_REVOLUTE_ANGULAR, JOINT_SWING_LIMIT, JOINT_REVOLUTE_LIMIT, JOINT_REVOLUTE = 1, 2, 3, 4, 5
+JOINT_ACTIVE, JOINT_LIMIT_ACTIVE = 1, 2
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int32
+_U = ctypes.c_uint32
+_F = ctypes.c_float
+
+# name: (restype, argtypes)
+GPU_EXPORTS = {
+    "bepugpu_abi_version": (_I, []),
+    "bepugpu_record_size": (_U, [_I]),
+    "bepugpu_default_settings": (None, [_P]),
+    "bepugpu_create": (_I, [_I, _P, ctypes.POINTER(_P)]),
+    "bepugpu_destroy": (None, [_P]),
+    "bepugpu_last_error": (ctypes.c_char_p, [_P]),
+    "bepugpu_set_settings": (_I, [_P, _P]),
+    "bepugpu_synchronize": (_I, [_P]),
+    "bepugpu_scene_create": (_I, [_P, _U, _U, _U, ctypes.POINTER(_I)]),
+    "bepugpu_scene_destroy": (_I, [_P, _I]),
+    "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
+    "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
+    "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
+    "bepugpu_download_bodies": (_I, [_P, _I, _P, _U]),
+    "bepugpu_download_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
+    "bepugpu_get_colouring": (_I, [_P, _I, _P, _P, _U, ctypes.POINTER(_U)]),
+    "bepugpu_colour_list": (_I, [_P, _P, _U, _P, _U, _P, _P, ctypes.POINTER(_U)]),
+    "bepugpu_step": (_I, [_P, _I, _F, _U]),
+    "bepugpu_set_solve_mode": (_I, [_P, _I, _I]),
+    "bepugpu_last_step_ms": (_I, [_P, _I, ctypes.POINTER(_F)]),
+    "bepugpu_last_step_launches": (_I, [_P, _I, ctypes.POINTER(_U)]),
+    "bepugpu_last_step_phase_ms": (_I, [_P, _I, _P]),
+    "bepugpu_batch_step": (_I, [_P, _P, _U, _F, _U, _U]),
+    "bepugpu_profile_step": (_I, [_P, _I, _F, _U, _P]),
+    "bepugpu_last_call_stats": (_I, [_P, ctypes.POINTER(_U), ctypes.POINTER(_F)]),
+}
+
+SCENE_EXPORTS = {
+    "bepuscene_default_pile": (None, [_P]),
+    "bepuscene_default_tower": (None, [_P]),
+    "bepuscene_default_chain": (None, [_P]),
+    "bepuscene_make_pile": (_I, [_P, ctypes.POINTER(_P)]),
+    "bepuscene_make_tower": (_I, [_P, ctypes.POINTER(_P)]),
+    "bepuscene_make_chain": (_I, [_P, ctypes.POINTER(_P)]),
+    "bepuscene_counts": (None, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "bepuscene_copy": (None, [_P, _P, _P, _P]),
+    "bepuscene_free": (None, [_P]),
+}
+
+_gpu = None
+_scenes = None
+
+
+def _bind(lib, table):
+    for name, (res, args) in table.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def load_gpu_library(path: str | None = None):
+    """Loads libbepugpu.so (raises when it has not been built)."""
+    global _gpu
+    if _gpu is not None and path is None:
+        return _gpu
+    p = Path(path) if path else LIB_DIR / "libbepugpu.so"
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build() "
+                           "(the solver has no CPU fallback)")
+    lib = _bind(ctypes.CDLL(str(p)), GPU_EXPORTS)
+    sizes = {0: SETTINGS_DTYPE, 1: BODY_DTYPE, 2: CONTACT_DTYPE, 3: MANIFOLD_DTYPE, 4: JOINT_DTYPE}
+    for kind, dt in sizes.items():
+        got = lib.bepugpu_record_size(kind)
+        if got != dt.itemsize:
+            raise RuntimeError(f"record {kind}: library size {got} != binding size {dt.itemsize}")
+    if path is None:
+        _gpu = lib
+    return lib
+
+
+def load_scene_library():
+    global _scenes
+    if _scenes is None:
+        p = LIB_DIR / "libbepuscenes.so"
+        if not p.exists():
+            raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build()")
+        _scenes = _bind(ctypes.CDLL(str(p)), SCENE_EXPORTS)
+    return _scenes
+
+
+def ptr(a: np.ndarray | None):
+    if a is None or a.size == 0:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class BepuError(RuntimeError):
+    """A failing C-ABI call: carries the status code and the library's message."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"{name}: {message}")
+
+
+class ArgumentException(BepuError, ValueError):
+    """Raised for BEPUGPU_INVALID_ARGUMENT, as the reference throws ArgumentException."""
+
+
+class InvalidOperationException(BepuError):
+    """Raised for BEPUGPU_INVALID_OPERATION (the reference's InvalidOperationException)."""
+
+
+def raise_for(status: int, message: str):
+    if status == OK:
+        return
+    if status in (INVALID_ARGUMENT, NOT_FOUND):
+        raise ArgumentException(status, message)
+    if status == INVALID_OPERATION:
+        raise InvalidOperationException(status, message)
+    raise BepuError(status, message)

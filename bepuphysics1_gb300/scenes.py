@@ -1,0 +1,67 @@
+"""Seeded synthetic workloads (libbepuscenes.so) as numpy record arrays.
+
+The named workloads follow the benchmark configurations:
+    pile_1k     1,000 unit boxes (1 kg, friction 0.6) in a 10x10x10 grid at
+                1.05 m with +-0.05 m jitter, settled on a 100x1x100 ground.
+    pile_64k    65,536 boxes, sizes U(0.5, 1.5) per axis, density 1, friction
+                U(0.4, 0.8), 64x16x64 columns at 2.0 m with +-0.1 m jitter.
+    tower(n)    one scene of n boxes/spheres (1 m, 1 kg) in towers of 4-32.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native as N
+
+
+def _collect(handle) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    lib = N.load_scene_library()
+    nb, nm, nj = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    lib.bepuscene_counts(handle, ctypes.byref(nb), ctypes.byref(nm), ctypes.byref(nj))
+    bodies = np.zeros(nb.value, N.BODY_DTYPE)
+    manifolds = np.zeros(nm.value, N.MANIFOLD_DTYPE)
+    joints = np.zeros(nj.value, N.JOINT_DTYPE)
+    lib.bepuscene_copy(handle, N.ptr(bodies), N.ptr(manifolds), N.ptr(joints))
+    lib.bepuscene_free(handle)
+    return bodies, manifolds, joints
+
+
+def make_pile(**overrides):
+    lib = N.load_scene_library()
+    p = np.zeros(1, N.PILE_PARAMS_DTYPE)
+    lib.bepuscene_default_pile(N.ptr(p))
+    for k, v in overrides.items():
+        p[k] = v
+    h = ctypes.c_void_p()
+    st = lib.bepuscene_make_pile(N.ptr(p), ctypes.byref(h))
+    N.raise_for(st, "bepuscene_make_pile")
+    return _collect(h)
+
+
+def make_tower(body_count: int, seed: int = 1, **overrides):
+    lib = N.load_scene_library()
+    p = np.zeros(1, N.TOWER_PARAMS_DTYPE)
+    lib.bepuscene_default_tower(N.ptr(p))
+    p["body_count"] = body_count
+    p["seed"] = seed
+    for k, v in overrides.items():
+        p[k] = v
+    h = ctypes.c_void_p()
+    st = lib.bepuscene_make_tower(N.ptr(p), ctypes.byref(h))
+    N.raise_for(st, "bepuscene_make_tower")
+    return _collect(h)
+
+
+def pile_1k(seed: int = 1234):
+    return make_pile(seed=seed)
+
+
+def pile_64k(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):
+    return make_pile(nx=nx, ny=ny, nz=nz, spacing=2.0, size_min=0.5, size_max=1.5, density=1.0, jitter=0.1,
+                     friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed)
+
+
+def contact_count(manifolds: np.ndarray) -> int:
+    return int(manifolds["contact_count"].sum())

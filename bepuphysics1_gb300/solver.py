@@ -1,0 +1,205 @@
+"""Host-side mirror of the reference's solver-stage surface over the C ABI.
+
+The reference hands its solver stage a list of SolverUpdateables and calls
+    Solver.Update()            (Constraints/Solver.cs:239-263)
+    ForceUpdater.Update()      (OtherSpaceStages/ForceUpdater.cs:73-92)
+    PositionUpdater.Update()   (PositionUpdating/ContinuousPositionUpdater.cs:134-154)
+once per Space.Update (Space.cs:496-522).  `GpuSpace` keeps one scene resident
+on the device and exposes the same stages; `Solver.iteration_limit` mirrors
+Solver.IterationLimit (Solver.cs:15-19, clamped at zero like the property).
+Errors come back as ArgumentException / InvalidOperationException like the
+reference's.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import native as N
+
+
+class Context:
+    """One device and the reference's global settings (bepugpu_settings)."""
+
+    def __init__(self, device: int = 0, settings: np.ndarray | None = None):
+        self.lib = N.load_gpu_library()
+        if settings is None:
+            settings = default_settings()
+        self.settings = np.array(settings, dtype=N.SETTINGS_DTYPE).reshape(())
+        h = ctypes.c_void_p()
+        st = self.lib.bepugpu_create(device, N.ptr(self.settings.reshape(1)), ctypes.byref(h))
+        if st != N.OK:
+            N.raise_for(st, f"bepugpu_create(device={device}) failed")
+        self.handle = h
+
+    def check(self, status: int):
+        if status != N.OK:
+            msg = self.lib.bepugpu_last_error(self.handle)
+            N.raise_for(status, msg.decode() if msg else "")
+
+    def set_settings(self, settings: np.ndarray):
+        self.settings = np.array(settings, dtype=N.SETTINGS_DTYPE).reshape(())
+        self.check(self.lib.bepugpu_set_settings(self.handle, N.ptr(self.settings.reshape(1))))
+
+    def synchronize(self):
+        self.check(self.lib.bepugpu_synchronize(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.bepugpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_settings() -> np.ndarray:
+    lib = N.load_gpu_library()
+    s = np.zeros(1, dtype=N.SETTINGS_DTYPE)
+    lib.bepugpu_default_settings(N.ptr(s))
+    return s[0].copy()
+
+
+class Solver:
+    """Mirror of Solver's settable surface for one scene."""
+
+    def __init__(self, space: "GpuSpace"):
+        self._space = space
+
+    @property
+    def iteration_limit(self) -> int:
+        return int(self._space.ctx.settings["iteration_limit"])
+
+    @iteration_limit.setter
+    def iteration_limit(self, value: int):
+        s = self._space.ctx.settings.copy()
+        s["iteration_limit"] = max(int(value), 0)
+        self._space.ctx.set_settings(s)
+
+    def update(self, dt: float):
+        """Solver.Update: prestep, warm start and iterations."""
+        self._space.step(dt, N.STEP_SOLVE)
+
+
+class GpuSpace:
+    """One scene resident on the device: bodies plus the solver list."""
+
+    def __init__(self, ctx: Context, bodies: np.ndarray, manifolds: np.ndarray | None = None,
+                 joints: np.ndarray | None = None, capacity: tuple[int, int, int] | None = None):
+        self.ctx = ctx
+        lib = ctx.lib
+        manifolds = np.zeros(0, N.MANIFOLD_DTYPE) if manifolds is None else manifolds
+        joints = np.zeros(0, N.JOINT_DTYPE) if joints is None else joints
+        cap = capacity or (len(bodies), len(manifolds), len(joints))
+        sid = ctypes.c_int32()
+        ctx.check(lib.bepugpu_scene_create(ctx.handle, cap[0], cap[1], cap[2], ctypes.byref(sid)))
+        self.id = sid.value
+        self.solver = Solver(self)
+        self.upload_bodies(bodies)
+        self.upload_constraints(manifolds, joints)
+
+    def upload_bodies(self, bodies: np.ndarray):
+        bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)
+        self.ctx.check(self.ctx.lib.bepugpu_upload_bodies(self.ctx.handle, self.id, N.ptr(bodies), len(bodies)))
+        self.body_count = len(bodies)
+
+    def upload_constraints(self, manifolds: np.ndarray, joints: np.ndarray | None = None):
+        manifolds = np.ascontiguousarray(manifolds, dtype=N.MANIFOLD_DTYPE)
+        joints = np.ascontiguousarray(np.zeros(0, N.JOINT_DTYPE) if joints is None else joints, dtype=N.JOINT_DTYPE)
+        self.ctx.check(self.ctx.lib.bepugpu_upload_constraints(
+            self.ctx.handle, self.id, N.ptr(manifolds), len(manifolds), N.ptr(joints), len(joints)))
+        self.manifold_count = len(manifolds)
+        self.joint_count = len(joints)
+
+    def update_manifolds(self, manifolds: np.ndarray):
+        manifolds = np.ascontiguousarray(manifolds, dtype=N.MANIFOLD_DTYPE)
+        self.ctx.check(self.ctx.lib.bepugpu_update_manifolds(self.ctx.handle, self.id, N.ptr(manifolds),
+                                                             len(manifolds)))
+
+    def set_mode(self, mode: int):
+        self.ctx.check(self.ctx.lib.bepugpu_set_solve_mode(self.ctx.handle, self.id, mode))
+
+    def step(self, dt: float, flags: int = N.STEP_ALL):
+        """Space.Update's velocity and integration stages in pipeline order."""
+        self.ctx.check(self.ctx.lib.bepugpu_step(self.ctx.handle, self.id, float(dt), flags))
+
+    def force_update(self, dt: float):
+        self.step(dt, N.STEP_FORCES)
+
+    def position_update(self, dt: float):
+        self.step(dt, N.STEP_POSITIONS)
+
+    def refresh_contacts(self, dt: float):
+        self.step(dt, N.STEP_REFRESH_CONTACTS)
+
+    def download_bodies(self, into: np.ndarray | None = None) -> np.ndarray:
+        out = np.zeros(self.body_count, N.BODY_DTYPE) if into is None else into
+        self.ctx.check(self.ctx.lib.bepugpu_download_bodies(self.ctx.handle, self.id, N.ptr(out), len(out)))
+        return out
+
+    def download_constraints(self, manifolds: np.ndarray | None = None, joints: np.ndarray | None = None):
+        m = np.zeros(self.manifold_count, N.MANIFOLD_DTYPE) if manifolds is None else manifolds
+        j = np.zeros(self.joint_count, N.JOINT_DTYPE) if joints is None else joints
+        self.ctx.check(self.ctx.lib.bepugpu_download_constraints(self.ctx.handle, self.id, N.ptr(m), len(m),
+                                                                 N.ptr(j), len(j)))
+        return m, j
+
+    def colouring(self):
+        n = self.manifold_count + self.joint_count
+        colour = np.zeros(n, np.int32)
+        order = np.zeros(n, np.int32)
+        k = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bepugpu_get_colouring(self.ctx.handle, self.id, N.ptr(colour), N.ptr(order), n,
+                                                          ctypes.byref(k)))
+        return colour, order, k.value
+
+    def last_step_ms(self) -> float:
+        v = ctypes.c_float()
+        self.ctx.check(self.ctx.lib.bepugpu_last_step_ms(self.ctx.handle, self.id, ctypes.byref(v)))
+        return v.value
+
+    def last_step_phase_ms(self) -> np.ndarray:
+        """[refresh + forces, prestep, warm start, solve, positions] device ms."""
+        out = np.zeros(5, np.float32)
+        self.ctx.check(self.ctx.lib.bepugpu_last_step_phase_ms(self.ctx.handle, self.id, N.ptr(out)))
+        return out
+
+    def last_step_launches(self) -> int:
+        v = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bepugpu_last_step_launches(self.ctx.handle, self.id, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "id", None) is not None and self.ctx.handle:
+            self.ctx.lib.bepugpu_scene_destroy(self.ctx.handle, self.id)
+            self.id = None
+
+
+def colour_list(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | None = None):
+    """The library's colouring of a solver list (joints first, then manifolds),
+    computed on the host: (colour per updateable, colour-sorted order, colours)."""
+    lib = N.load_gpu_library()
+    joints = np.zeros(0, N.JOINT_DTYPE) if joints is None else joints
+    a = np.ascontiguousarray(np.concatenate([joints["body_a"], manifolds["body_a"]]).astype(np.int32))
+    b = np.ascontiguousarray(np.concatenate([joints["body_b"], manifolds["body_b"]]).astype(np.int32))
+    dyn = np.ascontiguousarray((bodies["is_dynamic"] != 0).astype(np.uint8))
+    n = len(a)
+    colour = np.zeros(n, np.int32)
+    order = np.zeros(n, np.int32)
+    k = ctypes.c_uint32()
+    st = lib.bepugpu_colour_list(N.ptr(a), N.ptr(b), n, N.ptr(dyn), len(dyn), N.ptr(colour), N.ptr(order),
+                                 ctypes.byref(k))
+    N.raise_for(st, "bepugpu_colour_list: a constraint references a body outside the body array")
+    return colour, order, k.value
+
+
+def profile_step(space: GpuSpace, dt: float, flags: int = N.STEP_ALL) -> np.ndarray:
+    """One instrumented step (bepugpu_profile_step): per-phase device ms and the
+    solve census."""
+    out = np.zeros(1, N.PHASE_TIMES_DTYPE)
+    space.ctx.check(space.ctx.lib.bepugpu_profile_step(space.ctx.handle, space.id, float(dt), flags, N.ptr(out)))
+    return out[0]

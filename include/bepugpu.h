@@ -1,0 +1,279 @@
+/*
+ * bepugpu.h -- C ABI of the GB300 velocity solver and integration step for
+ * BEPUphysics v1 scenes.
+ *
+ * The library replaces three stages of the reference's Space pipeline:
+ *   ForceUpdater     BEPUphysics/OtherSpaceStages/ForceUpdater.cs:73-92
+ *   Solver           BEPUphysics/Constraints/Solver.cs:239-314
+ *   PositionUpdater  BEPUphysics/PositionUpdating/ContinuousPositionUpdater.cs:134-154
+ * and, for frozen manifold sets, the manifold refresh rule of
+ *   ContactRefresher BEPUphysics/CollisionTests/ContactRefresher.cs:18-69.
+ *
+ * Every function returns a bepugpu_status.  No C++ exception and no CUDA
+ * error crosses the ABI; bepugpu_last_error() gives the message of the last
+ * failing call on a context.  Host arrays passed in are borrowed for the
+ * duration of the call only.  All device memory is owned by the context.
+ *
+ * Threading: one context is driven by one host thread at a time, like the
+ * reference's stage contract (MultithreadedProcessingStage.Update is called
+ * from one thread).  The serving entry points (bepugpu_server_*) are the
+ * exception: submit and poll may be called from different threads.
+ */
+#ifndef BEPUGPU_H
+#define BEPUGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEPUGPU_ABI_VERSION 1
+#define BEPUGPU_MAX_CONTACTS 4
+
+typedef enum bepugpu_status {
+    BEPUGPU_OK = 0,
+    BEPUGPU_INVALID_ARGUMENT = 1,   /* reference: ArgumentException (Solver.cs:109,142) */
+    BEPUGPU_OUT_OF_MEMORY = 2,
+    BEPUGPU_ADMISSION_REFUSED = 3,  /* serving: scene does not fit the device budget */
+    BEPUGPU_CUDA_ERROR = 4,
+    BEPUGPU_TIMEOUT = 5,            /* a bounded device-side wait ran out */
+    BEPUGPU_NAN_DETECTED = 6,
+    BEPUGPU_NOT_FOUND = 7,
+    BEPUGPU_QUEUE_FULL = 8,
+    BEPUGPU_INVALID_OPERATION = 9   /* reference: InvalidOperationException, e.g.
+                                       "Cannot constrain two kinematic bodies"
+                                       (BallSocketJoint.cs:253) */
+} bepugpu_status;
+
+/* Global and per-solver settings.  Each field names the reference setting it
+ * mirrors; bepugpu_default_settings() fills the reference defaults. */
+typedef struct bepugpu_settings {
+    float gravity[3];                      /* ForceUpdater.Gravity (Space default 0,-9.81,0 in the configs) */
+    int32_t iteration_limit;               /* Solver.IterationLimit, Solver.cs:15 (10) */
+    float minimum_impulse;                 /* SolverSettings.DefaultMinimumImpulse, SolverSettings.cs:62 (.001) */
+    int32_t minimum_iteration_count;       /* SolverSettings.DefaultMinimumIterationCount, :70 (1) */
+    int32_t maximum_iteration_count;       /* SolverSettings.maximumIterationCount, :15 (int.MaxValue) */
+    float softness;                        /* CollisionResponseSettings.Softness, :43 (.001) */
+    float penetration_recovery_stiffness;  /* CollisionResponseSettings, :24 (.2) */
+    float maximum_penetration_recovery_speed; /* CollisionResponseSettings, :18 (2) */
+    float static_friction_velocity_threshold; /* CollisionResponseSettings, :31 (.2) */
+    float twist_friction_factor;           /* CollisionResponseSettings, :37 (1) */
+    float bounciness_velocity_threshold;   /* CollisionResponseSettings, :12 (1) */
+    float allowed_penetration;             /* CollisionDetectionSettings.AllowedPenetration, :74 (.01) */
+    float contact_invalidation_length_squared; /* CollisionDetectionSettings, :11 (.01) */
+    float maximum_contact_distance;        /* CollisionDetectionSettings, :82 (.1) */
+    int32_t reserved[4];
+} bepugpu_settings;
+
+/* One rigid body, as the C# shim reads it from an Entity (EntityBase.cs:35-43,
+ * 303-347, 1164-1165).  Kinematic bodies have is_dynamic = 0; their inverse
+ * mass and inverse inertia are ignored by the solver, as in the reference. */
+typedef struct bepugpu_body {
+    float position[3];
+    float orientation[4];            /* quaternion x, y, z, w */
+    float linear_velocity[3];
+    float angular_velocity[3];
+    float inverse_mass;
+    float local_inverse_inertia[9];  /* row-major M11 M12 M13 M21 ... M33 */
+    float linear_damping;            /* Entity.LinearDamping (.03) */
+    float angular_damping;           /* Entity.AngularDamping (.15) */
+    int32_t is_dynamic;
+    int32_t reserved;
+} bepugpu_body;
+
+/* One contact of a convex manifold (Contact.cs:15-31) together with the
+ * ContactSupplementData the refresher reads and the warm-start impulse of its
+ * ContactPenetrationConstraint (ContactPenetrationConstraint.cs:21). */
+typedef struct bepugpu_contact {
+    float position[3];
+    float normal[3];
+    float penetration_depth;
+    int32_t id;
+    float local_offset_a[3];         /* ContactSupplementData.LocalOffsetA */
+    float local_offset_b[3];         /* ContactSupplementData.LocalOffsetB */
+    float base_penetration_depth;    /* ContactSupplementData.BasePenetrationDepth */
+    float penetration_impulse;       /* accumulated impulse, in/out */
+} bepugpu_contact;
+
+/* Manifold flags. */
+#define BEPUGPU_MANIFOLD_ACTIVE      1u  /* SolverUpdateable.IsActive */
+#define BEPUGPU_MANIFOLD_SOLVER_RULE 2u  /* pair collision rule < CollisionRule.NoSolver */
+
+/* One ConvexContactManifoldConstraint (ConvexContactManifoldConstraint.cs:12-212):
+ * up to four penetration children in contact-add order, then one
+ * SlidingFrictionTwoAxis and one TwistFrictionConstraint. */
+typedef struct bepugpu_manifold {
+    int32_t body_a;                  /* index into the body array, -1 = no entity */
+    int32_t body_b;
+    int32_t contact_count;           /* 0..4 */
+    uint32_t flags;                  /* BEPUGPU_MANIFOLD_* */
+    float kinetic_friction;          /* InteractionProperties (MaterialManager.cs:77-85) */
+    float static_friction;
+    float bounciness;
+    float sliding_impulse[2];        /* SlidingFrictionTwoAxis.accumulatedImpulse, in/out */
+    float sliding_axis[3];           /* SlidingFrictionTwoAxis.linearA row 1, kept between
+                                        steps (SlidingFrictionTwoAxis.cs:341-366), in/out */
+    float twist_impulse;             /* TwistFrictionConstraint.accumulatedImpulse, in/out */
+    int32_t reserved;
+    bepugpu_contact contacts[BEPUGPU_MAX_CONTACTS];
+} bepugpu_manifold;
+
+/* Two-body joints.  A joint is one SolverUpdateable of the solver list; a
+ * REVOLUTE joint is the SolverGroup RevoluteJoint (RevoluteJoint.cs:46-95) with
+ * its BallSocketJoint, RevoluteAngularJoint and RevoluteLimit children. */
+typedef enum bepugpu_joint_type {
+    BEPUGPU_JOINT_BALL_SOCKET = 1,      /* BallSocketJoint.cs:210-372 */
+    BEPUGPU_JOINT_REVOLUTE_ANGULAR = 2, /* RevoluteAngularJoint.cs:226-365 */
+    BEPUGPU_JOINT_SWING_LIMIT = 3,      /* SwingLimit.cs:211-347 */
+    BEPUGPU_JOINT_REVOLUTE_LIMIT = 4,   /* RevoluteLimit.cs:285-649 */
+    BEPUGPU_JOINT_REVOLUTE = 5          /* RevoluteJoint group: ball socket + angular + limit */
+} bepugpu_joint_type;
+
+#define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
+#define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE: RevoluteJoint.Limit.IsActive */
+
+/* Joint record.  Field meaning per type:
+ *  BALL_SOCKET:      anchor_a, anchor_b = local anchors (BallSocketJoint.LocalOffsetA/B);
+ *                    impulse[0..2] = accumulated impulse.
+ *  REVOLUTE_ANGULAR: axis_a = WorldFreeAxisA's local axis on A, axis_b = local free axis on B;
+ *                    impulse[0..1].
+ *  SWING_LIMIT:      axis_a, axis_b = local hinge axes; limit[0] = maximum swing angle (rad);
+ *                    impulse[0].
+ *  REVOLUTE_LIMIT:   axis_a = local free axis on A, basis_a = local measurement axis on A,
+ *                    basis_b = local test axis on B, limit[0] = minimum angle, limit[1] =
+ *                    maximum angle; impulse[0..1].
+ *  REVOLUTE:         anchor_a/b, axis_a/b, basis_a/b and limit[0..1] as above;
+ *                    impulse[0..2] ball socket, impulse[3..4] angular, impulse[5..6] limit.
+ * spring[0..1] = SpringSettings stiffness and damping (600000, 90000);
+ * limit[2] = margin (limits), limit[3] = maximum corrective velocity (float max = none). */
+typedef struct bepugpu_joint {
+    int32_t type;                    /* bepugpu_joint_type */
+    int32_t body_a;                  /* -1 = TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17) */
+    int32_t body_b;
+    uint32_t flags;                  /* BEPUGPU_JOINT_* */
+    float anchor_a[3];
+    float anchor_b[3];
+    float axis_a[3];
+    float axis_b[3];
+    float basis_a[3];
+    float basis_b[3];
+    float limit[4];
+    float spring[2];
+    float impulse[8];                /* accumulated impulses, in/out */
+} bepugpu_joint;
+
+typedef struct bepugpu_context bepugpu_context;
+
+/* Step flags: which stages bepugpu_step runs, in pipeline order. */
+#define BEPUGPU_STEP_REFRESH_CONTACTS 1u  /* ContactRefresher on every manifold */
+#define BEPUGPU_STEP_FORCES           2u  /* ForceUpdater */
+#define BEPUGPU_STEP_SOLVE            4u  /* Solver */
+#define BEPUGPU_STEP_POSITIONS        8u  /* PositionUpdater (Discrete) */
+#define BEPUGPU_STEP_ALL              15u
+
+/* Solve strategies for the one-scene path. */
+#define BEPUGPU_MODE_GRAPH      0  /* one launch per colour sweep, captured in a CUDA graph */
+#define BEPUGPU_MODE_PERSISTENT 1  /* one cooperative launch, bounded grid barrier per colour */
+
+int32_t bepugpu_abi_version(void);
+/* sizeof of the record types, so a binding can check its marshalling:
+ * kind 0 settings, 1 body, 2 contact, 3 manifold, 4 joint. */
+uint32_t bepugpu_record_size(int32_t kind);
+void bepugpu_default_settings(bepugpu_settings* out);
+
+bepugpu_status bepugpu_create(int32_t device, const bepugpu_settings* settings,
+                              bepugpu_context** out);
+void bepugpu_destroy(bepugpu_context* ctx);
+const char* bepugpu_last_error(bepugpu_context* ctx);
+bepugpu_status bepugpu_set_settings(bepugpu_context* ctx, const bepugpu_settings* settings);
+bepugpu_status bepugpu_synchronize(bepugpu_context* ctx);
+
+/* Scenes.  A scene is one Space's body set and solver list.  Capacities are
+ * fixed at creation; uploads may use any count up to them. */
+bepugpu_status bepugpu_scene_create(bepugpu_context* ctx, uint32_t max_bodies,
+                                    uint32_t max_manifolds, uint32_t max_joints,
+                                    int32_t* scene_out);
+bepugpu_status bepugpu_scene_destroy(bepugpu_context* ctx, int32_t scene);
+
+/* Uploads copy host records to the device.  bepugpu_upload_constraints sets the
+ * solver list -- joints first, then manifolds, in array order, the order the
+ * reference's Solver.Add calls would have produced -- and colours it. */
+bepugpu_status bepugpu_upload_bodies(bepugpu_context* ctx, int32_t scene,
+                                     const bepugpu_body* bodies, uint32_t count);
+bepugpu_status bepugpu_upload_constraints(bepugpu_context* ctx, int32_t scene,
+                                          const bepugpu_manifold* manifolds, uint32_t manifold_count,
+                                          const bepugpu_joint* joints, uint32_t joint_count);
+/* Rewrites manifold records in place without recolouring.  Body pairs and the
+ * manifold count must be those of the last bepugpu_upload_constraints. */
+bepugpu_status bepugpu_update_manifolds(bepugpu_context* ctx, int32_t scene,
+                                        const bepugpu_manifold* manifolds, uint32_t count);
+
+bepugpu_status bepugpu_download_bodies(bepugpu_context* ctx, int32_t scene,
+                                       bepugpu_body* bodies, uint32_t count);
+bepugpu_status bepugpu_download_constraints(bepugpu_context* ctx, int32_t scene,
+                                            bepugpu_manifold* manifolds, uint32_t manifold_count,
+                                            bepugpu_joint* joints, uint32_t joint_count);
+
+/* Colouring of the solver list: colour per updateable (joints first, then
+ * manifolds) and the colour-sorted order the sweeps use.  Reading it is how the
+ * oracle's colour-order run is set up. */
+bepugpu_status bepugpu_get_colouring(bepugpu_context* ctx, int32_t scene,
+                                     int32_t* colour, int32_t* order, uint32_t count,
+                                     uint32_t* colour_count);
+
+/* The same colouring on host arrays, without a device: body_a/body_b of each
+ * updateable (-1 = none) and is_dynamic per body.  No context is needed. */
+bepugpu_status bepugpu_colour_list(const int32_t* body_a, const int32_t* body_b, uint32_t count,
+                                   const uint8_t* is_dynamic, uint32_t body_count,
+                                   int32_t* colour, int32_t* order, uint32_t* colour_count);
+
+/* Stages.  bepugpu_step runs the flagged stages as one device sequence:
+ * refresh -> ForceUpdater -> Solver (prestep, warm start, iterations) ->
+ * PositionUpdater.  dt = TimeStepSettings.TimeStepDuration. */
+bepugpu_status bepugpu_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags);
+bepugpu_status bepugpu_set_solve_mode(bepugpu_context* ctx, int32_t scene, int32_t mode);
+
+/* Device time of the last bepugpu_step on this scene, in milliseconds, taken
+ * with CUDA events on the scene's stream. */
+bepugpu_status bepugpu_last_step_ms(bepugpu_context* ctx, int32_t scene, float* ms);
+
+/* Device time of the phases of the last bepugpu_step in graph mode, from
+ * events captured into the graph: [0] refresh + ForceUpdater, [1] prestep,
+ * [2] warm start, [3] solve iterations, [4] PositionUpdater. */
+bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* ctx, int32_t scene, float* phase_ms);
+
+/* Number of kernel launches the last bepugpu_step issued (graph nodes count
+ * as launches). */
+bepugpu_status bepugpu_last_step_launches(bepugpu_context* ctx, int32_t scene, uint32_t* launches);
+
+/* Batched stepping: every listed scene advances `steps` steps in one
+ * persistent launch, one CTA per scene, body state in shared memory when it
+ * fits (ParallelSpaceTestDemo.cs:24-64 is the reference's analogue). */
+bepugpu_status bepugpu_batch_step(bepugpu_context* ctx, const int32_t* scenes, uint32_t count,
+                                  float dt, uint32_t steps, uint32_t flags);
+
+/* Per-phase device times of one step run as separate launches, each bracketed
+ * by CUDA events on the scene's stream (an instrumented copy of bepugpu_step:
+ * it advances the scene like bepugpu_step does).  The solve census counts,
+ * before each solve sweep, the manifolds still active and their algorithmic
+ * bytes 76*d + 136 + 48*c (c contacts, d dynamic bodies). */
+typedef struct bepugpu_phase_times {
+    float refresh_ms, force_ms, prestep_ms, warm_ms, solve_ms, position_ms;
+    uint32_t solve_launches, warm_launches;
+    double solve_algorithmic_bytes;
+    double solve_manifold_visits;
+    double solve_contact_visits;
+} bepugpu_phase_times;
+
+bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags,
+                                    bepugpu_phase_times* out);
+
+/* Kernel counters of the last call on the context: launches and device ms. */
+bepugpu_status bepugpu_last_call_stats(bepugpu_context* ctx, uint32_t* launches, float* device_ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BEPUGPU_H */
