@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--mode", default="graph", choices=["graph", "persistent"])
+    ap.add_argument("--persistent-blocks", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
@@ -225,6 +226,8 @@ def main():
     ctx = Context(local, settings)
     space = GpuSpace(ctx, bodies, manifolds)
     space.set_mode(N.MODE_GRAPH if args.mode == "graph" else N.MODE_PERSISTENT)
+    if args.mode == "persistent":
+        ctx.check(ctx.lib.bepugpu_set_persistent_blocks_per_sm(ctx.handle, space.id, args.persistent_blocks))
     colours = space.colouring()[2]
 
     for _ in range(max(args.warmup, 3)):
@@ -245,8 +248,7 @@ def main():
             torch.cuda.synchronize()
             space.step(DT, N.STEP_ALL)
             step_ms.append(space.last_step_ms())
-            if args.mode == "graph":
-                solve_ms.append(float(space.last_step_phase_ms()[3]))
+            solve_ms.append(float(space.last_step_phase_ms()[3]))
     torch.cuda.synchronize()
     total_ms = float(sum(step_ms))
     launches = space.last_step_launches() * args.steps
@@ -284,8 +286,10 @@ def main():
     if not args.no_e2e:
         hb = torch.empty(bodies.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(N.BODY_DTYPE)
         hm = torch.empty(manifolds.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(N.MANIFOLD_DTYPE)
-        hb[:] = space.download_bodies()
-        hm[:] = live_m
+        # downloads fill the state fields of existing records: start from the scene's records
+        hb[:] = bodies
+        hm[:] = manifolds
+        space.download_bodies(hb)
         space.download_constraints(hm)
         ctx.synchronize()
         k = max(3, min(args.steps, 10))

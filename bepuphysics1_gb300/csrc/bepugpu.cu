@@ -152,6 +152,13 @@ __global__ void k_refresh(ManifoldSoA m, BodySoA b, StepParams p) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < m.count) RefreshManifold(m, b, s, p);
 }
+// Refresh and force update in one launch: the refresh reads poses only and the
+// force update writes velocities and inertia only.
+__global__ void k_refresh_force(ManifoldSoA m, BodySoA b, StepParams p) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m.count) RefreshManifold(m, b, t, p);
+    else if (t - m.count < b.count) ForceUpdateBody(b, t - m.count, p);
+}
 __global__ void k_force(BodySoA b, StepParams p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < b.count) ForceUpdateBody(b, i, p);
@@ -247,7 +254,14 @@ struct PersistentArgs {
     unsigned int* counter;
     unsigned int* generation;
     int* err;
+    unsigned long long* stamps;  // globaltimer at solve start and solve end (block 0)
 };
+
+__device__ __forceinline__ unsigned long long GlobalTimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __global__ void k_persistent(PersistentArgs a) {
     unsigned int localGen = *(volatile unsigned int*)a.generation;
@@ -255,12 +269,13 @@ __global__ void k_persistent(PersistentArgs a) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     volatile int* err = a.err;
     __syncthreads();
-    if (a.flags & BEPUGPU_STEP_REFRESH_CONTACTS) {
-        for (int s = tid; s < a.m.count; s += stride) RefreshManifold(a.m, a.b, s, a.p);
-        if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
-    }
-    if (a.flags & BEPUGPU_STEP_FORCES) {
-        for (int i = tid; i < a.b.count; i += stride) ForceUpdateBody(a.b, i, a.p);
+    // The refresh reads poses only and the force update writes velocities and
+    // inertia only, so the two share one phase.
+    if (a.flags & (BEPUGPU_STEP_REFRESH_CONTACTS | BEPUGPU_STEP_FORCES)) {
+        if (a.flags & BEPUGPU_STEP_REFRESH_CONTACTS)
+            for (int s = tid; s < a.m.count; s += stride) RefreshManifold(a.m, a.b, s, a.p);
+        if (a.flags & BEPUGPU_STEP_FORCES)
+            for (int i = tid; i < a.b.count; i += stride) ForceUpdateBody(a.b, i, a.p);
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
     }
     if (a.flags & BEPUGPU_STEP_SOLVE) {
@@ -270,12 +285,14 @@ __global__ void k_persistent(PersistentArgs a) {
             for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride) WarmSlot(a.m, a.b, s);
             if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
         }
+        if (tid == 0) a.stamps[0] = GlobalTimer();
         for (int it = 0; it < a.p.iterationLimit; it++)
             for (int c = 0; c < a.colours; c++) {
                 for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride)
                     SolveSlot(a.m, a.b, s, a.p);
                 if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
             }
+        if (tid == 0) a.stamps[1] = GlobalTimer();
     }
     if (a.flags & BEPUGPU_STEP_POSITIONS) {
         for (int i = tid; i < a.b.count; i += stride) PositionUpdateBody(a.b, i, a.p);
@@ -438,8 +455,8 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
     stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
     CK(cudaMalloc(&staging, stagingBytes));
-    CK(cudaMalloc(&counter, 256));
-    CK(cudaMemset(counter, 0, 256));
+    CK(cudaMalloc(&counter, kScratchBytes));
+    CK(cudaMemset(counter, 0, kScratchBytes));
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&evStart));
     CK(cudaEventCreate(&evStop));
@@ -455,26 +472,28 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     int nm = m.count, nb = b.count;
     // Phase events become event-record nodes of the graph: their elapsed times
     // are the device time of each phase of every launched step.
-    CK(cudaEventRecord(evPhase[0], stream));
-    if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {
+    CK(cudaEventRecordWithFlags(evPhase[0], stream, cudaEventRecordExternal));
+    bool refresh = (flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm, force = (flags & BEPUGPU_STEP_FORCES) && nb;
+    if (refresh && force) {
+        k_refresh_force<<<Blocks(nm + nb, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+    } else if (refresh) {
         k_refresh<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
-    }
-    if ((flags & BEPUGPU_STEP_FORCES) && nb) {
+    } else if (force) {
         k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
-    CK(cudaEventRecord(evPhase[1], stream));
+    CK(cudaEventRecordWithFlags(evPhase[1], stream, cudaEventRecordExternal));
     bool solve = (flags & BEPUGPU_STEP_SOLVE) && nm;
     if (solve) {
         k_prestep<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
     }
-    CK(cudaEventRecord(evPhase[2], stream));
+    CK(cudaEventRecordWithFlags(evPhase[2], stream, cudaEventRecordExternal));
     if (solve) {
         for (int c = 0; c < colouring.colours; c++) {
             int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
             if (b1 > b0) { k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, b0, b1); launchesPerStep++; }
         }
     }
-    CK(cudaEventRecord(evPhase[3], stream));
+    CK(cudaEventRecordWithFlags(evPhase[3], stream, cudaEventRecordExternal));
     if (solve) {
         for (int it = 0; it < p.iterationLimit; it++)
             for (int c = 0; c < colouring.colours; c++) {
@@ -482,11 +501,11 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
                 if (b1 > b0) { k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, p, b0, b1); launchesPerStep++; }
             }
     }
-    CK(cudaEventRecord(evPhase[4], stream));
+    CK(cudaEventRecordWithFlags(evPhase[4], stream, cudaEventRecordExternal));
     if ((flags & BEPUGPU_STEP_POSITIONS) && nb) {
         k_position<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
-    CK(cudaEventRecord(evPhase[5], stream));
+    CK(cudaEventRecordWithFlags(evPhase[5], stream, cudaEventRecordExternal));
     cudaGraph_t graph;
     cudaError_t e = cudaStreamEndCapture(stream, &graph);
     if (e != cudaSuccess) {
@@ -516,16 +535,20 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
             ctx->SetError("persistent kernel cannot be resident");
             return BEPUGPU_CUDA_ERROR;
         }
-        persistentBlocks = std::min(perSm, 2) * ctx->smCount;
+        persistentBlocks = std::min(perSm, persistentBlocksPerSm) * ctx->smCount;
     }
     PersistentArgs a;
     a.m = m; a.b = b; a.p = p;
     a.colourOffsets = colourOffsetsDev;
     a.colours = colouring.colours;
     a.flags = flags;
-    a.counter = (unsigned int*)counter;
-    a.generation = (unsigned int*)counter + 32;
-    a.err = (int*)counter + 64;
+    a.counter = BarrierCounter();
+    a.generation = BarrierGeneration();
+    a.err = ErrorWord();
+    a.stamps = Stamps();
+    // A barrier abandoned by an earlier timed-out launch must not count here.
+    CK(cudaMemsetAsync(BarrierCounter(), 0, sizeof(unsigned int), stream));
+    CK(cudaMemsetAsync(ErrorWord(), 0, sizeof(int), stream));
     void* args[] = {&a};
     CK(cudaLaunchCooperativeKernel((void*)k_persistent, dim3(persistentBlocks), dim3(T), args, 0, stream));
     launchesPerStep = 1;
@@ -536,6 +559,10 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
     if (!(dt > 0) || !std::isfinite(dt)) {
         ctx->SetError("dt must be positive and finite");
         return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (maxBodyReferenced >= b.count) {
+        ctx->SetError("constraints reference body %d but the scene holds %d bodies", maxBodyReferenced, b.count);
+        return BEPUGPU_INVALID_OPERATION;
     }
     bepugpu_status st = RefreshDamping(ctx, dt);
     if (st != BEPUGPU_OK) return st;
@@ -671,9 +698,9 @@ bepugpu_status bepugpu_synchronize(bepugpu_context* c) {
         Scene& s = *kv.second;
         if (s.mode == BEPUGPU_MODE_PERSISTENT && s.counter) {
             int err = 0;
-            CK(cudaMemcpy(&err, (int*)s.counter + 64, sizeof(int), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(&err, s.ErrorWord(), sizeof(int), cudaMemcpyDeviceToHost));
             if (err) {
-                CK(cudaMemset((int*)s.counter + 64, 0, sizeof(int)));
+                CK(cudaMemset(s.ErrorWord(), 0, sizeof(int)));
                 ctx->SetError("persistent step: a grid barrier wait ran out");
                 return BEPUGPU_TIMEOUT;
             }
@@ -804,6 +831,10 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     CK(cudaMemcpyAsync(s->colourOffsetsDev, s->manifoldOffsets.data(), sizeof(int32_t) * (col.colours + 1),
                        cudaMemcpyHostToDevice, s->stream));
     s->hostSlotOf = std::move(slotOf);
+    s->hostBodyA.assign(a.begin() + nj, a.end());
+    s->hostBodyB.assign(bb.begin() + nj, bb.end());
+    s->maxBodyReferenced = -1;
+    for (uint32_t u = 0; u < nm + nj; u++) s->maxBodyReferenced = std::max(s->maxBodyReferenced, std::max(a[u], bb[u]));
     return UploadManifoldRecords(ctx, s, man, nm);
 }
 
@@ -815,6 +846,17 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
     if (n != (uint32_t)s->m.count || (n && !man)) {
         ctx->SetError("update_manifolds needs the %d manifolds of the last upload", s->m.count);
         return BEPUGPU_INVALID_ARGUMENT;
+    }
+    // The colouring is kept, so every manifold must still join the same bodies.
+    for (uint32_t i = 0; i < n; i++) {
+        if (man[i].body_a != s->hostBodyA[i] || man[i].body_b != s->hostBodyB[i]) {
+            ctx->SetError("manifold %u changed its bodies; use bepugpu_upload_constraints to recolour", i);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (man[i].contact_count < 0 || man[i].contact_count > 4) {
+            ctx->SetError("manifold %u has contact_count %d (0..4 allowed)", i, man[i].contact_count);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
     }
     return UploadManifoldRecords(ctx, s, man, n);
 }
@@ -926,6 +968,20 @@ bepugpu_status bepugpu_set_solve_mode(bepugpu_context* c, int32_t id, int32_t mo
     return BEPUGPU_OK;
 }
 
+bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* c, int32_t id, int32_t blocks) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (blocks < 1 || blocks > 2) {
+        ctx->SetError("persistent blocks per SM must be 1 or 2");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    s->persistentBlocksPerSm = blocks;
+    s->persistentBlocks = 0;
+    return BEPUGPU_OK;
+}
+
 bepugpu_status bepugpu_step(bepugpu_context* c, int32_t id, float dt, uint32_t flags) {
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
@@ -950,11 +1006,19 @@ bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* c, int32_t id, float*
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
     if (!s) return BEPUGPU_NOT_FOUND;
-    if (!phase_ms || !s->stepped || s->mode != BEPUGPU_MODE_GRAPH) {
-        ctx->SetError("phase times exist after a graph-mode step");
+    if (!phase_ms || !s->stepped) {
+        ctx->SetError("phase times exist after a step");
         return BEPUGPU_INVALID_ARGUMENT;
     }
     CK(cudaEventSynchronize(s->evStop));
+    if (s->mode == BEPUGPU_MODE_PERSISTENT) {
+        // globaltimer stamps taken by block 0 around the solve iterations
+        unsigned long long t[2];
+        CK(cudaMemcpy(t, s->Stamps(), sizeof(t), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 5; k++) phase_ms[k] = 0.f;
+        phase_ms[3] = t[1] > t[0] ? (float)((double)(t[1] - t[0]) * 1e-6) : 0.f;
+        return BEPUGPU_OK;
+    }
     for (int k = 0; k < 5; k++) CK(cudaEventElapsedTime(&phase_ms[k], s->evPhase[k], s->evPhase[k + 1]));
     return BEPUGPU_OK;
 }
@@ -977,6 +1041,10 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     Scene* s = FindScene(ctx, id);
     if (!s) return BEPUGPU_NOT_FOUND;
     if (!out || !(dt > 0)) return BEPUGPU_INVALID_ARGUMENT;
+    if (s->maxBodyReferenced >= s->b.count) {
+        ctx->SetError("constraints reference body %d but the scene holds %d bodies", s->maxBodyReferenced, s->b.count);
+        return BEPUGPU_INVALID_OPERATION;
+    }
     bepugpu_status st = s->RefreshDamping(ctx, dt);
     if (st != BEPUGPU_OK) return st;
     StepParams p = MakeParams(ctx->settings, dt);
@@ -993,7 +1061,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     };
     struct Span { cudaEvent_t a, b; float* dst; };
     std::vector<Span> spans;
-    unsigned long long* acc = (unsigned long long*)s->counter + 16;  // words 16..18 of the scratch block
+    unsigned long long* acc = s->Census();
     CK(cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), q));
     int nm = s->m.count, nb = s->b.count;
     if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {

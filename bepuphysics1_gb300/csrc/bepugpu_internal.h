@@ -35,8 +35,23 @@ struct BatchEngine;
 
 StepParams MakeParams(const bepugpu_settings& s, float dt);
 
+// Layout of a scene's device scratch block (kScratchBytes): grid barrier
+// arrival counter, barrier generation, error word, census accumulators --
+// each on its own 128-byte line.
+constexpr size_t kScratchBytes = 1024;
+constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 256, kCensusAt = 512,
+                 kStampsAt = 640;
+
 struct Scene {
     int32_t id = 0;
+    unsigned int* BarrierCounter() const { return (unsigned int*)((char*)counter + kBarrierCounterAt); }
+    unsigned int* BarrierGeneration() const { return (unsigned int*)((char*)counter + kBarrierGenerationAt); }
+    int* ErrorWord() const { return (int*)((char*)counter + kErrorAt); }
+    unsigned long long* Census() const { return (unsigned long long*)((char*)counter + kCensusAt); }
+    unsigned long long* Stamps() const { return (unsigned long long*)((char*)counter + kStampsAt); }
+    int persistentBlocksPerSm = 1;
+    std::vector<int32_t> hostBodyA, hostBodyB;  // manifold body pairs of the last constraint upload
+    int32_t maxBodyReferenced = -1;
     uint32_t maxBodies = 0, maxManifolds = 0, maxJoints = 0;
     void* arena = nullptr;
     size_t arenaBytes = 0;

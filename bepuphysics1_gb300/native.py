@@ -107,6 +107,7 @@ GPU_EXPORTS = {
     "bepugpu_colour_list": (_I, [_P, _P, _U, _P, _U, _P, _P, ctypes.POINTER(_U)]),
     "bepugpu_step": (_I, [_P, _I, _F, _U]),
     "bepugpu_set_solve_mode": (_I, [_P, _I, _I]),
+    "bepugpu_set_persistent_blocks_per_sm": (_I, [_P, _I, _I]),
     "bepugpu_last_step_ms": (_I, [_P, _I, ctypes.POINTER(_F)]),
     "bepugpu_last_step_launches": (_I, [_P, _I, ctypes.POINTER(_U)]),
     "bepugpu_last_step_phase_ms": (_I, [_P, _I, _P]),

@@ -233,14 +233,18 @@ bepugpu_status bepugpu_colour_list(const int32_t* body_a, const int32_t* body_b,
  * PositionUpdater.  dt = TimeStepSettings.TimeStepDuration. */
 bepugpu_status bepugpu_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags);
 bepugpu_status bepugpu_set_solve_mode(bepugpu_context* ctx, int32_t scene, int32_t mode);
+/* Persistent mode: resident blocks per SM of the cooperative launch (1 or 2). */
+bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* ctx, int32_t scene, int32_t blocks);
 
 /* Device time of the last bepugpu_step on this scene, in milliseconds, taken
  * with CUDA events on the scene's stream. */
 bepugpu_status bepugpu_last_step_ms(bepugpu_context* ctx, int32_t scene, float* ms);
 
-/* Device time of the phases of the last bepugpu_step in graph mode, from
- * events captured into the graph: [0] refresh + ForceUpdater, [1] prestep,
- * [2] warm start, [3] solve iterations, [4] PositionUpdater. */
+/* Device time of the phases of the last bepugpu_step.  Graph mode: from
+ * events captured into the graph, [0] refresh + ForceUpdater, [1] prestep,
+ * [2] warm start, [3] solve iterations, [4] PositionUpdater.  Persistent mode:
+ * [3] only, from globaltimer stamps around the solve iterations; the others
+ * are 0. */
 bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* ctx, int32_t scene, float* phase_ms);
 
 /* Number of kernel launches the last bepugpu_step issued (graph nodes count
