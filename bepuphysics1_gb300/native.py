@@ -76,6 +76,7 @@ STATUS_NAMES = ["OK", "INVALID_ARGUMENT", "OUT_OF_MEMORY", "ADMISSION_REFUSED", 
                 "NAN_DETECTED", "NOT_FOUND", "QUEUE_FULL", "INVALID_OPERATION"]
 
 STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_ALL = 1, 2, 4, 8, 15
+NOALLOC_MAX_BODIES, NOALLOC_MAX_MANIFOLDS = 1024, 2048  # bepugpu_step_noalloc limits
 MODE_GRAPH, MODE_PERSISTENT = 0, 1
 MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE = 1, 2
 JOINT_BALL_SOCKET, JOINT_REVOLUTE_ANGULAR, JOINT_SWING_LIMIT, JOINT_REVOLUTE_LIMIT, JOINT_REVOLUTE = 1, 2, 3, 4, 5
@@ -113,6 +114,7 @@ GPU_EXPORTS = {
     "bepugpu_last_step_phase_ms": (_I, [_P, _I, _P]),
     "bepugpu_batch_step": (_I, [_P, _P, _U, _F, _U, _U]),
     "bepugpu_profile_step": (_I, [_P, _I, _F, _U, _P]),
+    "bepugpu_step_noalloc": (_I, [_P, _P, _U, _P, _U, _F, _U, _P]),
     "bepugpu_last_call_stats": (_I, [_P, ctypes.POINTER(_U), ctypes.POINTER(_F)]),
 }
 

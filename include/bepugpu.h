@@ -273,6 +273,29 @@ typedef struct bepugpu_phase_times {
 bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags,
                                     bepugpu_phase_times* out);
 
+/* Step without allocating.  It has no counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- a plugin inside an engine or
+ * sandbox that owns the device heap, or code held to a memory budget fixed in
+ * advance.  `bodies` and `manifolds` are the caller's records in DEVICE memory
+ * (in/out, like upload + step + download of the other entry points); joints are
+ * not taken.  All scratch lives in one fixed array of
+ * BEPUGPU_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * the process exits, so a call takes at most BEPUGPU_NOALLOC_MAX_BODIES bodies
+ * and BEPUGPU_NOALLOC_MAX_MANIFOLDS manifolds and returns
+ * BEPUGPU_INVALID_ARGUMENT above that.  The step runs on the current device, on
+ * `stream` (a cudaStream_t, NULL = legacy default stream), in one thread block,
+ * and the call returns when it is done.  The first call on a device looks up
+ * the scratch array's device address; make that first call before any stream
+ * capture.  Calls share the scratch array: calls whose work overlaps on the GPU
+ * (other host threads, other streams) race and must be serialised by the
+ * caller.  Damping factors are computed with the device's double pow. */
+#define BEPUGPU_NOALLOC_MAX_BODIES 1024
+#define BEPUGPU_NOALLOC_MAX_MANIFOLDS 2048
+#define BEPUGPU_NOALLOC_SCRATCH_BYTES 1606656
+bepugpu_status bepugpu_step_noalloc(const bepugpu_settings* settings, bepugpu_body* bodies,
+                                    uint32_t body_count, bepugpu_manifold* manifolds,
+                                    uint32_t manifold_count, float dt, uint32_t flags, void* stream);
+
 /* Kernel counters of the last call on the context: launches and device ms. */
 bepugpu_status bepugpu_last_call_stats(bepugpu_context* ctx, uint32_t* launches, float* device_ms);
 
