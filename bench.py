@@ -55,6 +55,10 @@ def parse_args():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--mode", default="graph", choices=["graph", "persistent"])
     ap.add_argument("--persistent-blocks", type=int, default=1)
+    ap.add_argument("--groups", default="on", choices=["on", "off"],
+                    help="island groups: whole steps of small islands in one CTA")
+    ap.add_argument("--group-target", type=int, default=64, help="manifolds packed per group CTA")
+    ap.add_argument("--group-threads", type=int, default=0, help="threads per group CTA (0 = from the plan)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
@@ -224,7 +228,8 @@ def main():
     settings = default_settings()
     iters = int(settings["iteration_limit"])
     ctx = Context(local, settings)
-    space = GpuSpace(ctx, bodies, manifolds)
+    policy = (0 if args.groups == "off" else 1, 1024, 4096, args.group_target, args.group_threads)
+    space = GpuSpace(ctx, bodies, manifolds, group_policy=policy)
     space.set_mode(N.MODE_GRAPH if args.mode == "graph" else N.MODE_PERSISTENT)
     if args.mode == "persistent":
         ctx.check(ctx.lib.bepugpu_set_persistent_blocks_per_sm(ctx.handle, space.id, args.persistent_blocks))
@@ -238,7 +243,7 @@ def main():
     cips = contacts * iters  # contact-iterations per step
 
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
-    step_ms, solve_ms = [], []
+    step_ms, solve_ms, group_ms = [], [], []
     if pg:
         pg.barrier()
     torch.cuda.synchronize()
@@ -248,7 +253,9 @@ def main():
             torch.cuda.synchronize()
             space.step(DT, N.STEP_ALL)
             step_ms.append(space.last_step_ms())
-            solve_ms.append(float(space.last_step_phase_ms()[3]))
+            phases = space.last_step_phase_ms()
+            solve_ms.append(float(phases[3]))
+            group_ms.append(float(phases[5]))
     torch.cuda.synchronize()
     total_ms = float(sum(step_ms))
     launches = space.last_step_launches() * args.steps
@@ -259,27 +266,40 @@ def main():
         pg.barrier()
     value = world * cips * args.steps / (total_ms / 1000.0)
 
-    # roofline of the solve kernel: census of executed work on one instrumented step
+    # roofline of the dominant kernel, from a census of one instrumented step
     prof = profile_step(space, DT, N.STEP_ALL)
-    bytes_per_step = float(prof["solve_algorithmic_bytes"])
-    solve_launches = int(prof["solve_launches"])
-    if solve_ms:
-        mean_solve_s = statistics.mean(solve_ms) / 1000.0
-    else:
-        mean_solve_s = float(prof["solve_ms"]) / 1000.0
     peak, peak_kind = measured_hbm_peak()
-    achieved = bytes_per_step / mean_solve_s / 1e9 if mean_solve_s > 0 else 0.0
     traffic = ncu_traffic_per_launch()
-    roofline = {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind,
-                "traffic": traffic,
-                "algorithmic_bytes_per_launch": bytes_per_step / max(solve_launches, 1),
-                "launch_ms_avg": 1000.0 * mean_solve_s / max(solve_launches, 1),
-                "solve_launches_per_step": solve_launches,
-                "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
-                "kernel_only_ms_per_step": {k: float(prof[k]) for k in
-                                            ("refresh_ms", "force_ms", "prestep_ms", "warm_ms", "solve_ms",
-                                             "position_ms")}}
+    kernel_only = {k: float(prof[k]) for k in ("refresh_ms", "force_ms", "prestep_ms", "warm_ms", "solve_ms",
+                                               "position_ms", "group_ms")}
+    if int(prof["groups"]) > 0 and statistics.mean(group_ms) >= statistics.mean(solve_ms):
+        # Island groups: one launch runs whole steps of the small islands.  Its
+        # DRAM floor is the compulsory traffic of a step (inputs read once,
+        # outputs and prestep products written once).
+        bytes_per_launch = float(prof["group_compulsory_bytes"])
+        launch_s = statistics.mean(group_ms) / 1000.0
+        achieved = bytes_per_launch / launch_s / 1e9
+        roofline = {"bound": "hbm", "kernel": "k_groups", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                    "algorithmic_bytes_per_launch": bytes_per_launch,
+                    "algorithmic": "compulsory bytes per step: 288 + 112 c per manifold, 208 per body",
+                    "launch_ms_avg": 1000.0 * launch_s, "launches_per_step": 1, "ctas": int(prof["groups"]),
+                    "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
+                    "sweep_equivalent_bytes_per_step": float(prof["solve_algorithmic_bytes"]),
+                    "kernel_only_ms_per_step": kernel_only}
+    else:
+        bytes_per_step = float(prof["solve_algorithmic_bytes"])
+        solve_launches = int(prof["solve_launches"])
+        mean_solve_s = statistics.mean(solve_ms) / 1000.0 if solve_ms else float(prof["solve_ms"]) / 1000.0
+        achieved = bytes_per_step / mean_solve_s / 1e9 if mean_solve_s > 0 else 0.0
+        roofline = {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                    "algorithmic_bytes_per_launch": bytes_per_step / max(solve_launches, 1),
+                    "algorithmic": "76 d + 136 + 48 c per executed manifold visit",
+                    "launch_ms_avg": 1000.0 * mean_solve_s / max(solve_launches, 1),
+                    "solve_launches_per_step": solve_launches,
+                    "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
+                    "kernel_only_ms_per_step": kernel_only}
 
     # e2e through the C ABI with pinned host records
     e2e = None
@@ -321,6 +341,9 @@ def main():
             "config": {"workload": WORKLOAD, "bodies": int(len(bodies)), "manifolds": int(len(manifolds)),
                        "contacts": contacts, "iterations": iters, "colours": int(colours), "dt": float(DT),
                        "step": "refresh+forces+solve+positions", "mode": args.mode,
+                       "island_groups": {"enabled": args.groups == "on", "ctas": int(prof["groups"]),
+                                         "target_manifolds": args.group_target,
+                                         "threads": args.group_threads or "plan"},
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between timed steps (512 MiB write)"},
             "gpu_launches": int(launches),

@@ -154,18 +154,36 @@ __global__ void k_refresh(ManifoldSoA m, BodySoA b, StepParams p) {
 }
 // Refresh and force update in one launch: the refresh reads poses only and the
 // force update writes velocities and inertia only.
+// Bodies a group kernel steps are skipped by the sweep path's body kernels.
+__device__ __forceinline__ bool OwnedByGroup(const BodySoA& b, int i) {
+    return __float_as_uint(b.damp[i].w) & kOwnedByGroup;
+}
 __global__ void k_refresh_force(ManifoldSoA m, BodySoA b, StepParams p) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < m.count) RefreshManifold(m, b, t, p);
-    else if (t - m.count < b.count) ForceUpdateBody(b, t - m.count, p);
+    else if (t - m.count < b.count && !OwnedByGroup(b, t - m.count)) ForceUpdateBody(b, t - m.count, p);
 }
 __global__ void k_force(BodySoA b, StepParams p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < b.count) ForceUpdateBody(b, i, p);
+    if (i < b.count && !OwnedByGroup(b, i)) ForceUpdateBody(b, i, p);
+}
+// Body stages over the bodies no group kernel steps (the scene has groups).
+__global__ void k_refresh_force_list(ManifoldSoA m, BodySoA b, StepParams p, const int32_t* __restrict__ list, int n,
+                                     uint32_t flags) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m.count) {
+        if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifold(m, b, t, p);
+    } else if (t - m.count < n) {
+        if (flags & BEPUGPU_STEP_FORCES) ForceUpdateBody(b, list[t - m.count], p);
+    }
+}
+__global__ void k_position_list(BodySoA b, StepParams p, const int32_t* __restrict__ list, int n) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) PositionUpdateBody(b, list[t], p);
 }
 __global__ void k_position(BodySoA b, StepParams p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < b.count) PositionUpdateBody(b, i, p);
+    if (i < b.count && !OwnedByGroup(b, i)) PositionUpdateBody(b, i, p);
 }
 __global__ void k_prestep(ManifoldSoA m, BodySoA b, StepParams p) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -275,7 +293,8 @@ __global__ void k_persistent(PersistentArgs a) {
         if (a.flags & BEPUGPU_STEP_REFRESH_CONTACTS)
             for (int s = tid; s < a.m.count; s += stride) RefreshManifold(a.m, a.b, s, a.p);
         if (a.flags & BEPUGPU_STEP_FORCES)
-            for (int i = tid; i < a.b.count; i += stride) ForceUpdateBody(a.b, i, a.p);
+            for (int i = tid; i < a.b.count; i += stride)
+                if (!OwnedByGroup(a.b, i)) ForceUpdateBody(a.b, i, a.p);
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
     }
     if (a.flags & BEPUGPU_STEP_SOLVE) {
@@ -295,7 +314,8 @@ __global__ void k_persistent(PersistentArgs a) {
         if (tid == 0) a.stamps[1] = GlobalTimer();
     }
     if (a.flags & BEPUGPU_STEP_POSITIONS) {
-        for (int i = tid; i < a.b.count; i += stride) PositionUpdateBody(a.b, i, a.p);
+        for (int i = tid; i < a.b.count; i += stride)
+            if (!OwnedByGroup(a.b, i)) PositionUpdateBody(a.b, i, a.p);
     }
 }
 
@@ -359,6 +379,8 @@ Scene::~Scene() {
     if (evStop) cudaEventDestroy(evStop);
     for (auto e : evPhase)
         if (e) cudaEventDestroy(e);
+    for (auto e : evGroup)
+        if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -400,7 +422,8 @@ bepugpu_status Scene::RefreshDamping(Context* ctx, float dt) {
     for (int i = 0; i < n; i++) {
         float ld = hostLinDamp[i], ad = hostAngDamp[i];
         float lin = ld + 0.f, ang = ad + 0.f;
-        uint32_t flags = (lin > 0 ? 1u : 0u) | (ang > 0 ? 2u : 0u);
+        uint32_t flags = (lin > 0 ? 1u : 0u) | (ang > 0 ? 2u : 0u) |
+                         ((size_t)i < hostOwned.size() && hostOwned[i] ? kOwnedByGroup : 0u);
         if (!(ld == lastD)) { lastD = ld; lastF = DampingFactor(lin, dt); }
         if (!(ad == lastA)) { lastA = ad; lastG = DampingFactor(ang, dt); }
         float fbits;
@@ -427,6 +450,8 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
            oS0 = take(16 * M), oS1 = take(16 * M), oS3 = take(16 * M), oS4 = take(16 * M), oS5 = take(16 * M),
            oS6 = take(16 * M), oS7 = take(16 * M), oLev = take(16 * M), oState = take(8 * M),
            oSlot = take(4 * M), oOffs = take(4 * (M + 2));
+    size_t oGroups = take(sizeof(GroupDesc) * M), oGroupBodies = take(4 * B), oGroupRefs = take(8 * M),
+           oGroupOffsets = take(4 * (2 * M + 2)), oSweepBodies = take(4 * B);
     arenaBytes = bytes;
     cudaError_t e = cudaMalloc(&arena, bytes);
     if (e != cudaSuccess) {
@@ -451,6 +476,11 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     m.capacity = (int)M;
     slotOf = (int32_t*)(base + oSlot);
     colourOffsetsDev = (int32_t*)(base + oOffs);
+    groupDescDev = (GroupDesc*)(base + oGroups);
+    groupBodiesDev = (int32_t*)(base + oGroupBodies);
+    groupRefsDev = (int2*)(base + oGroupRefs);
+    groupColourOffsetsDev = (int32_t*)(base + oGroupOffsets);
+    sweepBodiesDev = (int32_t*)(base + oSweepBodies);
     CK(cudaMemset(arena, 0, bytes));
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
     stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
@@ -461,6 +491,23 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     CK(cudaEventCreate(&evStart));
     CK(cudaEventCreate(&evStop));
     for (auto& e : evPhase) CK(cudaEventCreate(&e));
+    for (auto& e : evGroup) CK(cudaEventCreate(&e));
+    return BEPUGPU_OK;
+}
+
+// The bodies the sweep path's body stages handle once groups exist: every
+// body no group kernel steps.
+bepugpu_status Scene::RebuildSweepBodies(Context* ctx) {
+    std::vector<int32_t> list;
+    list.reserve(b.count);
+    for (int32_t e = 0; e < b.count; e++)
+        if (!((size_t)e < hostOwned.size() && hostOwned[e])) list.push_back(e);
+    sweepBodyCount = (uint32_t)list.size();
+    if (!list.empty())
+        CK(cudaMemcpyAsync(sweepBodiesDev, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice,
+                           stream));
+    CK(cudaStreamSynchronize(stream));
+    version++;
     return BEPUGPU_OK;
 }
 
@@ -469,40 +516,68 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     const int T = 128;
     launchesPerStep = 0;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    int nm = m.count, nb = b.count;
+    // Island groups first: one CTA per group runs the group's whole step.
+    // They share only kinematic bodies (read only) with the sweep path, whose
+    // position update of moving kinematic bodies therefore has to follow.
+    CK(cudaEventRecordWithFlags(evGroup[0], stream, cudaEventRecordExternal));
+    if (!groupPlan.groups.empty()) {
+        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false);
+        if (gs != BEPUGPU_OK) {
+            cudaGraph_t dropped;
+            cudaStreamEndCapture(stream, &dropped);
+            if (dropped) cudaGraphDestroy(dropped);
+            return gs;
+        }
+        launchesPerStep += GroupLaunchCount(groupPlan);
+    }
+    CK(cudaEventRecordWithFlags(evGroup[1], stream, cudaEventRecordExternal));
+    const ManifoldSoA ms = SweepManifolds();
+    const int colours = SweepColours();
+    int nm = ms.count, nb = b.count;
     // Phase events become event-record nodes of the graph: their elapsed times
     // are the device time of each phase of every launched step.
     CK(cudaEventRecordWithFlags(evPhase[0], stream, cudaEventRecordExternal));
     bool refresh = (flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm, force = (flags & BEPUGPU_STEP_FORCES) && nb;
-    if (refresh && force) {
-        k_refresh_force<<<Blocks(nm + nb, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+    const bool listed = !groupPlan.groups.empty();  // body stages over the sweep path's own bodies
+    const int nl = (int)sweepBodyCount;
+    if (listed) {
+        if ((refresh || force) && nm + nl > 0) {
+            k_refresh_force_list<<<Blocks(nm + nl, T), T, 0, stream>>>(ms, b, p, sweepBodiesDev, nl, flags);
+            launchesPerStep++;
+        }
+    } else if (refresh && force) {
+        k_refresh_force<<<Blocks(nm + nb, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
     } else if (refresh) {
-        k_refresh<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+        k_refresh<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
     } else if (force) {
         k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[1], stream, cudaEventRecordExternal));
     bool solve = (flags & BEPUGPU_STEP_SOLVE) && nm;
     if (solve) {
-        k_prestep<<<Blocks(nm, T), T, 0, stream>>>(m, b, p); launchesPerStep++;
+        k_prestep<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[2], stream, cudaEventRecordExternal));
     if (solve) {
-        for (int c = 0; c < colouring.colours; c++) {
+        for (int c = 0; c < colours; c++) {
             int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
-            if (b1 > b0) { k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, b0, b1); launchesPerStep++; }
+            if (b1 > b0) { k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, b0, b1); launchesPerStep++; }
         }
     }
     CK(cudaEventRecordWithFlags(evPhase[3], stream, cudaEventRecordExternal));
     if (solve) {
         for (int it = 0; it < p.iterationLimit; it++)
-            for (int c = 0; c < colouring.colours; c++) {
+            for (int c = 0; c < colours; c++) {
                 int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
-                if (b1 > b0) { k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(m, b, p, b0, b1); launchesPerStep++; }
+                if (b1 > b0) { k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1); launchesPerStep++; }
             }
     }
     CK(cudaEventRecordWithFlags(evPhase[4], stream, cudaEventRecordExternal));
-    if ((flags & BEPUGPU_STEP_POSITIONS) && nb) {
+    if (listed) {
+        if ((flags & BEPUGPU_STEP_POSITIONS) && nl > 0) {
+            k_position_list<<<Blocks(nl, T), T, 0, stream>>>(b, p, sweepBodiesDev, nl); launchesPerStep++;
+        }
+    } else if ((flags & BEPUGPU_STEP_POSITIONS) && nb) {
         k_position<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[5], stream, cudaEventRecordExternal));
@@ -537,10 +612,18 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
         }
         persistentBlocks = std::min(perSm, persistentBlocksPerSm) * ctx->smCount;
     }
+    launchesPerStep = 0;
+    CK(cudaEventRecord(evGroup[0], stream));
+    if (!groupPlan.groups.empty()) {
+        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false);
+        if (gs != BEPUGPU_OK) return gs;
+        launchesPerStep += GroupLaunchCount(groupPlan);
+    }
+    CK(cudaEventRecord(evGroup[1], stream));
     PersistentArgs a;
-    a.m = m; a.b = b; a.p = p;
+    a.m = SweepManifolds(); a.b = b; a.p = p;
     a.colourOffsets = colourOffsetsDev;
-    a.colours = colouring.colours;
+    a.colours = SweepColours();
     a.flags = flags;
     a.counter = BarrierCounter();
     a.generation = BarrierGeneration();
@@ -551,7 +634,7 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
     CK(cudaMemsetAsync(ErrorWord(), 0, sizeof(int), stream));
     void* args[] = {&a};
     CK(cudaLaunchCooperativeKernel((void*)k_persistent, dim3(persistentBlocks), dim3(T), args, 0, stream));
-    launchesPerStep = 1;
+    launchesPerStep++;
     return BEPUGPU_OK;
 }
 
@@ -752,9 +835,14 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         s->hostDynamic[i] = bodies[i].is_dynamic ? 1 : 0;
         s->hostLocalM33[i] = bodies[i].is_dynamic ? bodies[i].local_inverse_inertia[8] : 0.f;
     }
-    if (n != (uint32_t)s->b.count) s->version++;
+    const bool resized = n != (uint32_t)s->b.count;
+    if (resized) s->version++;
     s->b.count = (int)n;
     s->dampDirty = true;
+    if (resized && !s->groupPlan.groups.empty()) {
+        bepugpu_status lst = s->RebuildSweepBodies(ctx);
+        if (lst != BEPUGPU_OK) return lst;
+    }
     if (n) {
         CK(cudaMemcpyAsync(s->staging, bodies, sizeof(bepugpu_body) * n, cudaMemcpyHostToDevice, s->stream));
         k_unpack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging, (int)n, s->b);
@@ -809,28 +897,35 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         ctx->SetError("a constraint references a body outside [0, %d)", nb);
         return BEPUGPU_INVALID_ARGUMENT;
     }
-    // Manifold slots: colour-sorted order restricted to manifolds.
-    const Colouring& col = s->colouring;
-    s->manifoldOffsets.assign(col.colours + 1, 0);
-    std::vector<int32_t> slotOf(nm);
-    int slot = 0;
-    for (int cc = 0; cc < col.colours; cc++) {
-        s->manifoldOffsets[cc] = slot;
-        for (int k = col.offsets[cc]; k < col.offsets[cc + 1]; k++) {
-            int u = col.order[k];
-            if (u >= (int)nj) slotOf[u - nj] = slot++;
-        }
+    // Manifold slots: the colour-sweep part in colour-major order, then the
+    // island groups (groups.cu); the persistent mode keeps everything on the
+    // sweep path.
+    GroupPolicy pol = s->policy;
+    if (s->mode == BEPUGPU_MODE_PERSISTENT) pol.enabled = false;
+    PlanGroups(pol, a.data(), bb.data(), s->colouring.colour.data(), (int32_t)nj, (int32_t)nm,
+               s->hostDynamic.data(), nb, s->groupPlan);
+    const GroupPlan& plan = s->groupPlan;
+    s->manifoldOffsets = plan.globalOffsets;
+    s->hostOwned.assign(nb, 0);
+    for (int32_t e = 0; e < nb && e < (int32_t)plan.localOf.size(); e++) s->hostOwned[e] = plan.localOf[e] >= 0;
+    {
+        bepugpu_status lst = s->RebuildSweepBodies(ctx);
+        if (lst != BEPUGPU_OK) return lst;
     }
-    s->manifoldOffsets[col.colours] = slot;
+    s->dampDirty = true;
     s->m.count = (int)nm;
     s->jointCount = nj;
     s->version++;
     if (nm) {
-        CK(cudaMemcpyAsync(s->slotOf, slotOf.data(), sizeof(int32_t) * nm, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->slotOf, plan.slotOf.data(), sizeof(int32_t) * nm, cudaMemcpyHostToDevice, s->stream));
     }
-    CK(cudaMemcpyAsync(s->colourOffsetsDev, s->manifoldOffsets.data(), sizeof(int32_t) * (col.colours + 1),
+    CK(cudaMemcpyAsync(s->colourOffsetsDev, s->manifoldOffsets.data(), sizeof(int32_t) * s->manifoldOffsets.size(),
                        cudaMemcpyHostToDevice, s->stream));
-    s->hostSlotOf = std::move(slotOf);
+    {
+        bepugpu_status gst = s->UploadGroups(ctx);
+        if (gst != BEPUGPU_OK) return gst;
+    }
+    s->hostSlotOf = plan.slotOf;
     s->hostBodyA.assign(a.begin() + nj, a.end());
     s->hostBodyB.assign(bb.begin() + nj, bb.end());
     s->maxBodyReferenced = -1;
@@ -968,6 +1063,26 @@ bepugpu_status bepugpu_set_solve_mode(bepugpu_context* c, int32_t id, int32_t mo
     return BEPUGPU_OK;
 }
 
+bepugpu_status bepugpu_set_group_policy(bepugpu_context* c, int32_t id, int32_t enabled, int32_t maxBodies,
+                                        int32_t maxManifolds, int32_t target, int32_t threads) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    // 96 bytes of shared memory per body must fit a CTA's 227 KB
+    if (maxBodies < 1 || maxBodies > 2400 || maxManifolds < 1 || target < 1 || threads < 0 || threads > 256 ||
+        threads % 32) {
+        ctx->SetError("group policy out of range (bodies 1..2400, manifolds >= 1, threads 0 or 32..256 by 32)");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    s->policy.enabled = enabled != 0;
+    s->policy.maxGroupBodies = maxBodies;
+    s->policy.maxGroupManifolds = maxManifolds;
+    s->policy.targetGroupManifolds = target;
+    s->groupThreadsOverride = threads;
+    return BEPUGPU_OK;
+}
+
 bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* c, int32_t id, int32_t blocks) {
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
@@ -1011,6 +1126,7 @@ bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* c, int32_t id, float*
         return BEPUGPU_INVALID_ARGUMENT;
     }
     CK(cudaEventSynchronize(s->evStop));
+    CK(cudaEventElapsedTime(&phase_ms[5], s->evGroup[0], s->evGroup[1]));
     if (s->mode == BEPUGPU_MODE_PERSISTENT) {
         // globaltimer stamps taken by block 0 around the solve iterations
         unsigned long long t[2];
@@ -1062,29 +1178,38 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     struct Span { cudaEvent_t a, b; float* dst; };
     std::vector<Span> spans;
     unsigned long long* acc = s->Census();
-    CK(cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), q));
-    int nm = s->m.count, nb = s->b.count;
+    CK(cudaMemsetAsync(acc, 0, 4 * sizeof(unsigned long long), q));
+    if (!s->groupPlan.groups.empty()) {  // the census variant of the group kernel counts its visits
+        cudaEvent_t a = mark();
+        bepugpu_status gs = LaunchGroups(ctx, s, p, flags, true);
+        if (gs != BEPUGPU_OK) return gs;
+        spans.push_back({a, mark(), &out->group_ms});
+        out->groups = (uint32_t)s->groupPlan.groups.size();
+    }
+    const ManifoldSoA ms = s->SweepManifolds();
+    const int colours = s->SweepColours();
+    int nm = ms.count, nb = s->b.count;
     if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {
-        cudaEvent_t a = mark(); k_refresh<<<Blocks(nm, T), T, 0, q>>>(s->m, s->b, p); spans.push_back({a, mark(), &out->refresh_ms});
+        cudaEvent_t a = mark(); k_refresh<<<Blocks(nm, T), T, 0, q>>>(ms, s->b, p); spans.push_back({a, mark(), &out->refresh_ms});
     }
     if ((flags & BEPUGPU_STEP_FORCES) && nb) {
         cudaEvent_t a = mark(); k_force<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->force_ms});
     }
     if ((flags & BEPUGPU_STEP_SOLVE) && nm) {
-        cudaEvent_t a = mark(); k_prestep<<<Blocks(nm, T), T, 0, q>>>(s->m, s->b, p); spans.push_back({a, mark(), &out->prestep_ms});
-        for (int cc = 0; cc < s->colouring.colours; cc++) {
+        cudaEvent_t a = mark(); k_prestep<<<Blocks(nm, T), T, 0, q>>>(ms, s->b, p); spans.push_back({a, mark(), &out->prestep_ms});
+        for (int cc = 0; cc < colours; cc++) {
             int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
             if (b1 <= b0) continue;
-            cudaEvent_t e0 = mark(); k_warm<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, s->b, b0, b1);
+            cudaEvent_t e0 = mark(); k_warm<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, s->b, b0, b1);
             spans.push_back({e0, mark(), &out->warm_ms});
             out->warm_launches++;
         }
         for (int it = 0; it < p.iterationLimit; it++)
-            for (int cc = 0; cc < s->colouring.colours; cc++) {
+            for (int cc = 0; cc < colours; cc++) {
                 int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
                 if (b1 <= b0) continue;
-                k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, b0, b1, acc);
-                cudaEvent_t e0 = mark(); k_solve<<<Blocks(b1 - b0, T), T, 0, q>>>(s->m, s->b, p, b0, b1);
+                k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, b0, b1, acc);
+                cudaEvent_t e0 = mark(); k_solve<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, s->b, p, b0, b1);
                 spans.push_back({e0, mark(), &out->solve_ms});
                 out->solve_launches++;
             }
@@ -1093,7 +1218,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
         cudaEvent_t a = mark(); k_position<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->position_ms});
     }
     CK(cudaGetLastError());
-    unsigned long long h[3] = {0, 0, 0};
+    unsigned long long h[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, q));
     CK(cudaStreamSynchronize(q));
     for (auto& sp : spans) {
@@ -1105,6 +1230,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     out->solve_algorithmic_bytes = (double)h[0];
     out->solve_manifold_visits = (double)h[1];
     out->solve_contact_visits = (double)h[2];
+    out->group_compulsory_bytes = (double)h[3];
     return BEPUGPU_OK;
 }
 

@@ -32,8 +32,49 @@ struct ManifoldOut {
 
 struct Context;
 struct BatchEngine;
+struct Scene;
 
 StepParams MakeParams(const bepugpu_settings& s, float dt);
+
+// Island groups (groups.cu).  A group is a set of whole islands run by one CTA.
+struct GroupDesc {
+    int32_t mBegin, mEnd;   // manifold slots
+    int32_t bBegin, bEnd;   // entries of the group body list
+    int32_t cBegin, cCount; // colour offsets (relative to mBegin) in the offsets table
+    int32_t pad0, pad1;
+};
+struct GroupTables {
+    const GroupDesc* groups;
+    const int32_t* bodies;        // global indices of each group's dynamic bodies
+    const int2* refs;             // per manifold slot: body refs inside the group kernel
+    const int32_t* colourOffsets;
+};
+struct GroupPolicy {
+    bool enabled = true;
+    int32_t maxGroupBodies = 1024;       // shared memory: 96 bytes per body
+    int32_t maxGroupManifolds = 4096;    // larger islands stay on the sweep path
+    int32_t targetGroupManifolds = 64;   // small islands are packed up to this size
+};
+// Groups [begin, end) of one kernel variant and the sizes its launch needs.
+struct GroupClass {
+    int32_t begin = 0, end = 0, maxLocal = 0, maxManifolds = 0, maxColourMembers = 0;
+};
+struct GroupPlan {
+    std::vector<GroupDesc> groups;  // groups whose solve lanes fit shared memory first
+    std::vector<int32_t> groupBodies, localOf, groupOfManifold, slotOf, globalOffsets, colourOffsets;
+    std::vector<int2> refs;  // per slot
+    int32_t globalCount = 0;
+    GroupClass shared, global;
+};
+// Shared memory a group may use: 96 bytes per body, plus 400 per manifold when
+// its solve lanes live there.
+constexpr size_t kGroupSmemBudget = 200 * 1024;
+void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
+                int32_t nm, const uint8_t* dynamic, int32_t nb, GroupPlan& plan);
+bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
+int GroupLaunchCount(const GroupPlan& g);
+// Damping flags bit 2 marks a body stepped by a group kernel.
+constexpr uint32_t kOwnedByGroup = 4u;
 
 // Layout of a scene's device scratch block (kScratchBytes): grid barrier
 // arrival counter, barrier generation, error word, census accumulators --
@@ -52,6 +93,26 @@ struct Scene {
     int persistentBlocksPerSm = 1;
     std::vector<int32_t> hostBodyA, hostBodyB;  // manifold body pairs of the last constraint upload
     int32_t maxBodyReferenced = -1;
+    GroupPolicy policy;
+    GroupPlan groupPlan;
+    GroupDesc* groupDescDev = nullptr;
+    int32_t* groupBodiesDev = nullptr;
+    int2* groupRefsDev = nullptr;
+    int32_t* groupColourOffsetsDev = nullptr;
+    std::vector<uint8_t> hostOwned;  // body stepped by a group kernel
+    int32_t* sweepBodiesDev = nullptr;  // bodies no group steps (valid when groups exist)
+    uint32_t sweepBodyCount = 0;
+    int groupThreadsOverride = 0;    // 0 = derived from the plan
+    cudaEvent_t evGroup[2] = {nullptr, nullptr};
+    bepugpu_status UploadGroups(Context* ctx);
+    bepugpu_status RebuildSweepBodies(Context* ctx);
+    // The colour-sweep part of the manifold list: slots [0, globalCount).
+    ManifoldSoA SweepManifolds() const {
+        ManifoldSoA g = m;
+        g.count = groupPlan.globalCount;
+        return g;
+    }
+    int SweepColours() const { return manifoldOffsets.empty() ? 0 : (int)manifoldOffsets.size() - 1; }
     uint32_t maxBodies = 0, maxManifolds = 0, maxJoints = 0;
     void* arena = nullptr;
     size_t arenaBytes = 0;

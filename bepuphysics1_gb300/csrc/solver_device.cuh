@@ -94,16 +94,36 @@ struct BodyState {
     float I11, I12, I13, I21, I22, I23, I31, I32, I33;
 };
 
-__device__ __forceinline__ void LoadBody(const BodySoA& b, int i, BodyState& s) {
-    float4 v = b.vlin[i], w = b.vang[i], a = b.inv0[i], c = b.inv1[i];
+// Body storage views.  A ref names a body; -1 is "no entity".  The global
+// path's refs are body indices; a group kernel keeps its bodies in shared
+// memory and uses its own refs (GroupBodies in groups.cu).  The constraint
+// routines are templated on the view, so both paths run the same arithmetic.
+struct GlobalBodies {
+    BodySoA b;
+    __device__ __forceinline__ float4 Pos(int r) const { return b.pos[r]; }
+    __device__ __forceinline__ float4 Quat(int r) const { return b.quat[r]; }
+    __device__ __forceinline__ float4 Vlin(int r) const { return b.vlin[r]; }
+    __device__ __forceinline__ float4 Vang(int r) const { return b.vang[r]; }
+    __device__ __forceinline__ float4 Inv0(int r) const { return b.inv0[r]; }
+    __device__ __forceinline__ float4 Inv1(int r) const { return b.inv1[r]; }
+    __device__ __forceinline__ void SetVelocity(int r, float4 v, float4 w) const { b.vlin[r] = v; b.vang[r] = w; }
+};
+
+template <class V>
+__device__ __forceinline__ void LoadBodyV(const V& bv, int r, BodyState& s) {
+    float4 v = bv.Vlin(r), w = bv.Vang(r), a = bv.Inv0(r), c = bv.Inv1(r);
     s.vx = v.x; s.vy = v.y; s.vz = v.z; s.invMass = v.w;
     s.wx = w.x; s.wy = w.y; s.wz = w.z; s.I33 = w.w;
     s.I11 = a.x; s.I12 = a.y; s.I13 = a.z; s.I21 = a.w;
     s.I22 = c.x; s.I23 = c.y; s.I31 = c.z; s.I32 = c.w;
 }
+template <class V>
+__device__ __forceinline__ void StoreVelocityV(const V& bv, int r, const BodyState& s) {
+    bv.SetVelocity(r, make_float4(s.vx, s.vy, s.vz, s.invMass), make_float4(s.wx, s.wy, s.wz, s.I33));
+}
+__device__ __forceinline__ void LoadBody(const BodySoA& b, int i, BodyState& s) { LoadBodyV(GlobalBodies{b}, i, s); }
 __device__ __forceinline__ void StoreVelocity(const BodySoA& b, int i, const BodyState& s) {
-    b.vlin[i] = make_float4(s.vx, s.vy, s.vz, s.invMass);
-    b.vang[i] = make_float4(s.wx, s.wy, s.wz, s.I33);
+    StoreVelocityV(GlobalBodies{b}, i, s);
 }
 // EntityBase.ApplyLinearImpulse (EntityBase.cs:754-761)
 __device__ __forceinline__ void ApplyLinear(BodyState& s, float x, float y, float z) {
@@ -119,10 +139,10 @@ __device__ __forceinline__ void ApplyAngular(BodyState& s, float x, float y, flo
 }
 
 // Entity.UpdateForForces (EntityBase.cs:911-975), stabilization boost off.
-__device__ __forceinline__ void ForceUpdateBody(const BodySoA& b, int i, const StepParams& p) {
-    float4 pos = b.pos[i];
-    if (pos.w == 0.f) return;  // ForceUpdater only holds dynamic entities
-    float4 v = b.vlin[i], w = b.vang[i], q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i], d = b.damp[i];
+// The arithmetic on one body's lanes: v and w in/out, world inverse inertia to
+// a (M11 M12 M13 M21), c (M22 M23 M31 M32) and w.w (M33).
+__device__ __forceinline__ void ForceMath(float4& v, float4& w, float4 q, float4 l0, float4 l1, float4 d, float4& a,
+                                          float4& c, const StepParams& p) {
     uint32_t flags = __float_as_uint(d.w);
     v.x = p.gravityDt[0] + v.x;
     v.y = p.gravityDt[1] + v.y;
@@ -150,7 +170,6 @@ __device__ __forceinline__ void ForceUpdateBody(const BodySoA& b, int i, const S
     float m32 = R13 * L12 + R23 * L22 + R33 * L32;
     float m33 = R13 * L13 + R23 * L23 + R33 * L33;
     // inertiaTensorInverse = multiplied * R (Matrix3x3.Multiply, :766-790)
-    float4 a, c;
     a.x = m11 * R11 + m12 * R21 + m13 * R31;
     a.y = m11 * R12 + m12 * R22 + m13 * R32;
     a.z = m11 * R13 + m12 * R23 + m13 * R33;
@@ -160,18 +179,25 @@ __device__ __forceinline__ void ForceUpdateBody(const BodySoA& b, int i, const S
     c.z = m31 * R11 + m32 * R21 + m33 * R31;
     c.w = m31 * R12 + m32 * R22 + m33 * R32;
     w.w = m31 * R13 + m32 * R23 + m33 * R33;
+}
+__device__ __forceinline__ void ForceUpdateBody(const BodySoA& b, int i, const StepParams& p) {
+    float4 pos = b.pos[i];
+    if (pos.w == 0.f) return;  // ForceUpdater only holds dynamic entities
+    float4 v = b.vlin[i], w = b.vang[i], q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i], d = b.damp[i];
+    float4 a, c;
+    ForceMath(v, w, q, l0, l1, d, a, c, p);
     b.vlin[i] = v;
     b.vang[i] = w;
     b.inv0[i] = a;
     b.inv1[i] = c;
 }
 
-// Entity.PreUpdatePosition, Discrete mode (EntityBase.cs:1124-1160).
-__device__ __forceinline__ void PositionUpdateBody(const BodySoA& b, int i, const StepParams& p) {
-    float4 pos = b.pos[i];
-    float4 v = b.vlin[i], w = b.vang[i], q = b.quat[i];
+// Entity.PreUpdatePosition, Discrete mode (EntityBase.cs:1124-1160).  Returns
+// false for a body that does not move this step.
+__device__ __forceinline__ bool PositionMath(float4& pos, float4& q, float4 v, float4 w, const StepParams& p) {
     // Kinematic entities are integrated while they move (SimulationIslandMember.cs:225-248).
-    if (pos.w == 0.f && v.x == 0.f && v.y == 0.f && v.z == 0.f && w.x == 0.f && w.y == 0.f && w.z == 0.f) return;
+    if (pos.w == 0.f && v.x == 0.f && v.y == 0.f && v.z == 0.f && w.x == 0.f && w.y == 0.f && w.z == 0.f)
+        return false;
     float h = p.dt * .5f;
     float ix = w.x * h, iy = w.y * h, iz = w.z * h;
     // Quaternion.Multiply(multiplier = (ix, iy, iz, 0), orientation) (Quaternion.cs:66-79)
@@ -187,6 +213,11 @@ __device__ __forceinline__ void PositionUpdateBody(const BodySoA& b, int i, cons
     pos.x = pos.x + v.x * p.dt;
     pos.y = pos.y + v.y * p.dt;
     pos.z = pos.z + v.z * p.dt;
+    return true;
+}
+__device__ __forceinline__ void PositionUpdateBody(const BodySoA& b, int i, const StepParams& p) {
+    float4 pos = b.pos[i], q = b.quat[i];
+    if (!PositionMath(pos, q, b.vlin[i], b.vang[i], p)) return;
     b.quat[i] = q;
     b.pos[i] = pos;
 }
@@ -199,6 +230,13 @@ __device__ __forceinline__ float Clampf(float v, float lo, float hi) {
     else if (v > hi) return hi;
     return v;
 }
+
+// (float)System.Math.Sqrt((double)x) for a float x.  Rounding the double
+// square root to float gives the correctly rounded float square root, since
+// double carries at least 2*24+2 significant bits (Figueroa, "When is double
+// rounding innocuous?", 1995); the IEEE single-precision square root therefore
+// returns the same bits without using the FP64 pipe.
+__device__ __forceinline__ float SqrtOfFloat(float x) { return __fsqrt_rn(x); }
 
 // Quaternion.Transform (Quaternion.cs:509-535)
 __device__ __forceinline__ float3 QTransform(float vx, float vy, float vz, float4 r) {
@@ -217,54 +255,70 @@ __device__ __forceinline__ float3 QTransform(float vx, float vy, float vz, float
 // order-preserving removal of the contacts it queues.  Removed contacts lose
 // their accumulated impulse (ContactPenetrationConstraint.CleanUp, :65-75); a
 // manifold left empty clears sliding and twist (ConvexContactManifoldConstraint.cs:148-154).
-__device__ __forceinline__ void RefreshManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
+template <class V>
+__device__ __forceinline__ void RefreshManifoldV(const ManifoldSoA& m, const V& bv, int s, int ra, int rb,
+                                                 const StepParams& p) {
     int4 h = m.head[s];
     int count = h.z & 0xff;
     if (count == 0) return;
     int cap = m.capacity;
     float4 pa = make_float4(0, 0, 0, 0), qa = make_float4(0, 0, 0, 1);
     float4 pb = pa, qb = qa;
-    if (h.x >= 0) { pa = b.pos[h.x]; qa = b.quat[h.x]; }
-    if (h.y >= 0) { pb = b.pos[h.y]; qb = b.quat[h.y]; }
+    if (ra != -1) { pa = bv.Pos(ra); qa = bv.Quat(ra); }
+    if (rb != -1) { pb = bv.Pos(rb); qb = bv.Quat(rb); }
     float4 acc = m.penacc[s];
-    float accs[4] = {acc.x, acc.y, acc.z, acc.w};
-    float4 keepPos[4], keepNrm[4], keepOffA[4], keepOffB[4];
-    float keepAcc[4];
-    int kept = 0;
-    for (int k = 0; k < count; k++) {
-        float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s];
-        float4 oa = m.offA[k * cap + s], ob = m.offB[k * cap + s];
-        float3 ta = QTransform(oa.x, oa.y, oa.z, qa);
-        float3 tb = QTransform(ob.x, ob.y, ob.z, qb);
-        float ax = ta.x + pa.x, ay = ta.y + pa.y, az = ta.z + pa.z;  // RigidTransform.Transform
-        float bx = tb.x + pb.x, by = tb.y + pb.y, bz = tb.z + pb.z;
-        float abx = bx - ax, aby = by - ay, abz = bz - az;
-        float dot = abx * cn.x + aby * cn.y + abz * cn.z;
-        float tx = cn.x * dot, ty = cn.y * dot, tz = cn.z * dot;
-        tx = abx - tx; ty = aby - ty; tz = abz - tz;
-        dot = tx * tx + ty * ty + tz * tz;
-        if (dot > p.invalidationLengthSquared) continue;
-        dot = abx * cn.x + aby * cn.y + abz * cn.z;
-        float depth = oa.w - dot;
-        if (depth < -p.maximumContactDistance) continue;
-        float nx = bx + ax, ny = by + ay, nz = bz + az;
-        cp = make_float4(nx * .5f, ny * .5f, nz * .5f, depth);
-        keepPos[kept] = cp; keepNrm[kept] = cn; keepOffA[kept] = oa; keepOffB[kept] = ob;
-        keepAcc[kept] = accs[k];
-        kept++;
-    }
-    for (int k = 0; k < kept; k++) {
-        m.cpos[k * cap + s] = keepPos[k];
-        if (kept != count) {
-            m.cnrm[k * cap + s] = keepNrm[k];
-            m.offA[k * cap + s] = keepOffA[k];
-            m.offB[k * cap + s] = keepOffB[k];
+    const float accs[4] = {acc.x, acc.y, acc.z, acc.w};
+    // All contact loops are unrolled over the four lanes with a count guard so
+    // per-contact values stay in registers.
+    float4 cp[4], cn[4], oa[4], ob[4];
+    bool keep[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        keep[k] = false;
+        if (k < count) {
+            cn[k] = m.cnrm[k * cap + s];
+            oa[k] = m.offA[k * cap + s];
+            ob[k] = m.offB[k * cap + s];
+            float3 ta = QTransform(oa[k].x, oa[k].y, oa[k].z, qa);
+            float3 tb = QTransform(ob[k].x, ob[k].y, ob[k].z, qb);
+            float ax = ta.x + pa.x, ay = ta.y + pa.y, az = ta.z + pa.z;  // RigidTransform.Transform
+            float bx = tb.x + pb.x, by = tb.y + pb.y, bz = tb.z + pb.z;
+            float abx = bx - ax, aby = by - ay, abz = bz - az;
+            float dot = abx * cn[k].x + aby * cn[k].y + abz * cn[k].z;
+            float tx = cn[k].x * dot, ty = cn[k].y * dot, tz = cn[k].z * dot;
+            tx = abx - tx; ty = aby - ty; tz = abz - tz;
+            dot = tx * tx + ty * ty + tz * tz;
+            if (!(dot > p.invalidationLengthSquared)) {
+                dot = abx * cn[k].x + aby * cn[k].y + abz * cn[k].z;
+                float depth = oa[k].w - dot;
+                if (!(depth < -p.maximumContactDistance)) {
+                    float nx = bx + ax, ny = by + ay, nz = bz + az;
+                    cp[k] = make_float4(nx * .5f, ny * .5f, nz * .5f, depth);
+                    keep[k] = true;
+                }
+            }
         }
     }
+    // Kept contacts move down in order; every input is already in registers.
+    int kept = 0;
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f, n3 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (!keep[k]) continue;
+        m.cpos[kept * cap + s] = cp[k];
+        if (kept != k) {
+            m.cnrm[kept * cap + s] = cn[k];
+            m.offA[kept * cap + s] = oa[k];
+            m.offB[kept * cap + s] = ob[k];
+        }
+        n0 = kept == 0 ? accs[k] : n0;
+        n1 = kept == 1 ? accs[k] : n1;
+        n2 = kept == 2 ? accs[k] : n2;
+        n3 = kept == 3 ? accs[k] : n3;
+        kept++;
+    }
     if (kept != count) {
-        float na[4] = {0, 0, 0, 0};
-        for (int k = 0; k < kept; k++) na[k] = keepAcc[k];
-        m.penacc[s] = make_float4(na[0], na[1], na[2], na[3]);
+        m.penacc[s] = make_float4(n0, n1, n2, n3);
         h.z = (h.z & ~0xff) | kept;
         m.head[s] = h;
         if (kept == 0) {
@@ -272,6 +326,10 @@ __device__ __forceinline__ void RefreshManifold(const ManifoldSoA& m, const Body
             m.fricacc[s] = make_float4(0.f, 0.f, 0.f, f.w);
         }
     }
+}
+__device__ __forceinline__ void RefreshManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
+    int4 h = m.head[s];
+    RefreshManifoldV(m, GlobalBodies{b}, s, h.x, h.y, p);
 }
 
 // Reads velocity-relevant body data for the prestep.
@@ -282,8 +340,9 @@ struct PrestepBody {
     float I11, I12, I13, I21, I22, I23, I31, I32, I33;
     bool dynamic;
 };
-__device__ __forceinline__ void LoadPrestepBody(const BodySoA& b, int i, PrestepBody& o) {
-    float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i], a = b.inv0[i], c = b.inv1[i];
+template <class V>
+__device__ __forceinline__ void LoadPrestepBody(const V& bv, int r, PrestepBody& o) {
+    float4 p = bv.Pos(r), v = bv.Vlin(r), w = bv.Vang(r), a = bv.Inv0(r), c = bv.Inv1(r);
     o.px = p.x; o.py = p.y; o.pz = p.z; o.dynamic = p.w != 0.f;
     o.vx = v.x; o.vy = v.y; o.vz = v.z; o.invMass = v.w;
     o.wx = w.x; o.wy = w.y; o.wz = w.z; o.I33 = w.w;
@@ -294,19 +353,26 @@ __device__ __forceinline__ void LoadPrestepBody(const BodySoA& b, int i, Prestep
 // Solver.UnsafePrestep on one ConvexContactManifoldConstraint:
 // UpdateSolverActivity (ContactManifoldConstraint.cs:128-145), then Update
 // (ConvexContactManifoldConstraint.cs:171-177) on each active child.
-__device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
-    int4 h = m.head[s];
+// Inputs (head, contacts, material, previous sliding axis) are read from
+// `mi` at slot `si`; products (Jacobians, friction lanes, state, head) are
+// written to `mo` at slot `so`.  The sweep path passes the same arrays twice;
+// a group kernel writes its products to shared memory.
+template <class V>
+__device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si, const ManifoldSoA& mo, int so,
+                                                  const V& bv, int ra, int rb, const StepParams& p) {
+    int4 h = mi.head[si];
+    if (mo.head != mi.head) mo.head[so] = h;
     int count = h.z & 0xff;
     uint32_t mflags = (uint32_t)h.z >> 8;
-    const int cap = m.capacity;
+    const int cap = mi.capacity, capo = mo.capacity;
     PrestepBody A, B;
-    bool hasA = h.x >= 0, hasB = h.y >= 0;
-    if (hasA) LoadPrestepBody(b, h.x, A); else A.dynamic = false;
-    if (hasB) LoadPrestepBody(b, h.y, B); else B.dynamic = false;
+    bool hasA = ra != -1, hasB = rb != -1;
+    if (hasA) LoadPrestepBody(bv, ra, A); else A.dynamic = false;
+    if (hasB) LoadPrestepBody(bv, rb, B); else B.dynamic = false;
     uint32_t st = 0;
     // BEPUGPU_MANIFOLD_ACTIVE = 1, BEPUGPU_MANIFOLD_SOLVER_RULE = 2
     bool groupActive = (mflags & 1u) && (mflags & 2u) && ((hasA && A.dynamic) || (hasB && B.dynamic));
-    if (!groupActive) { m.state[s] = make_uint2(0u, 0u); return; }
+    if (!groupActive) { mo.state[so] = make_uint2(0u, 0u); return; }
     st |= kGroupActive;
     for (int k = 0; k < count; k++) st |= 1u << (kChildShift + k);
     if (count > 0) st |= kSlidingBit | kTwistBit;
@@ -315,13 +381,15 @@ __device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const Body
     if (dynB) st |= kDynB;
     if (hasA) st |= kHasA;
     if (hasB) st |= kHasB;
-    float4 mat = m.mat[s];
+    float4 mat = mi.mat[si];
     const float kinetic = mat.x, staticF = mat.y, bounciness = mat.z;
     float updateRate = p.updateRate;
 
     // ContactPenetrationConstraint.Update (ContactPenetrationConstraint.cs:114-233)
-    for (int k = 0; k < count; k++) {
-        float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k >= count) break;
+        float4 cp = mi.cpos[k * cap + si], cn = mi.cnrm[k * cap + si];
         float lx = -cn.x, ly = -cn.y, lz = -cn.z;
         float aAx = 0, aAy = 0, aAz = 0, aBx = 0, aBy = 0, aBz = 0;
         if (hasA) {
@@ -371,32 +439,32 @@ __device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const Body
         } else {
             bias = depth * updateRate;
         }
-        m.pj0[k * cap + s] = make_float4(lx, ly, lz, bias);
-        m.pj1[k * cap + s] = make_float4(aAx, aAy, aAz, softness);
-        m.pj2[k * cap + s] = make_float4(aBx, aBy, aBz, v2i);
+        mo.pj0[k * capo + so] = make_float4(lx, ly, lz, bias);
+        mo.pj1[k * capo + so] = make_float4(aAx, aAy, aAz, softness);
+        mo.pj2[k * capo + so] = make_float4(aBx, aBy, aBz, v2i);
     }
     if (count == 0) {
-        m.state[s] = make_uint2(st, 0u);
+        mo.state[so] = make_uint2(st, 0u);
         return;
     }
 
     // SlidingFrictionTwoAxis.Update (SlidingFrictionTwoAxis.cs:242-440)
-    float4 c0 = m.cpos[s];
+    float4 c0 = mi.cpos[si];
     float mcx, mcy, mcz;
     if (count == 1) {
         mcx = c0.x; mcy = c0.y; mcz = c0.z;
     } else {
-        float4 c1 = m.cpos[cap + s];
+        float4 c1 = mi.cpos[cap + si];
         mcx = c0.x + c1.x; mcy = c0.y + c1.y; mcz = c0.z + c1.z;
         if (count == 2) {
             mcx *= .5f; mcy *= .5f; mcz *= .5f;
         } else {
-            float4 c2 = m.cpos[2 * cap + s];
+            float4 c2 = mi.cpos[2 * cap + si];
             mcx = c2.x + mcx; mcy = c2.y + mcy; mcz = c2.z + mcz;
             if (count == 3) {
                 mcx *= .333333333f; mcy *= .333333333f; mcz *= .333333333f;
             } else {
-                float4 c3 = m.cpos[3 * cap + s];
+                float4 c3 = mi.cpos[3 * cap + si];
                 mcx = c3.x + mcx; mcy = c3.y + mcy; mcz = c3.z + mcz;
                 mcx *= .25f; mcy *= .25f; mcz *= .25f;
             }
@@ -419,18 +487,18 @@ __device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const Body
         vBx = vBx + B.vx; vBy = vBy + B.vy; vBz = vBz + B.vz;
     }
     float rvx = vAx - vBx, rvy = vAy - vBy, rvz = vAz - vBz;
-    float4 n0 = m.cnrm[s];
+    float4 n0 = mi.cnrm[si];
     float nx = n0.x, ny = n0.y, nz = n0.z;
     float normalVelocityScalar = nx * rvx + ny * rvy + nz * rvz;
     rvx -= normalVelocityScalar * nx;
     rvy -= normalVelocityScalar * ny;
     rvz -= normalVelocityScalar * nz;
-    float4 axis = m.saxis[s];
+    float4 axis = mi.saxis[si];
     float l11 = axis.x, l12 = axis.y, l13 = axis.z;
     float friction;
     float length = rvx * rvx + rvy * rvy + rvz * rvz;
     if (length > 1e-7f) {
-        length = (float)sqrt((double)length);
+        length = SqrtOfFloat(length);
         float inverseLength = 1 / length;
         l11 = rvx * inverseLength;
         l12 = rvy * inverseLength;
@@ -443,7 +511,7 @@ __device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const Body
             float x1 = ny * 0.f - nz * 0.f, y1 = nz * 1.f - nx * 0.f, z1 = nx * 0.f - ny * 1.f;
             length = x1 * x1 + y1 * y1 + z1 * z1;
             if (length > 1e-7f) {
-                length = (float)sqrt((double)length);
+                length = SqrtOfFloat(length);
                 float inverseLength = 1 / length;
                 l11 = x1 * inverseLength; l12 = y1 * inverseLength; l13 = z1 * inverseLength;
             } else {
@@ -534,22 +602,33 @@ __device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const Body
                           : staticF;
     tfriction *= p.twistFactor;
     float lev[4] = {0, 0, 0, 0};
-    for (int k = 0; k < count; k++) {
-        float4 cp = m.cpos[k * cap + s];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k >= count) break;
+        float4 cp = mi.cpos[k * cap + si];
         float ox = cp.x - mcx, oy = cp.y - mcy, oz = cp.z - mcz;
-        lev[k] = (float)sqrt((double)(ox * ox + oy * oy + oz * oz));
+        lev[k] = SqrtOfFloat(ox * ox + oy * oy + oz * oz);
     }
 
-    m.s0[s] = make_float4(rax, ray, raz, friction);
-    m.s1[s] = make_float4(rbx, rby, rbz, i11);
-    m.saxis[s] = make_float4(l11, l12, l13, i12);
-    m.s3[s] = make_float4(l21, l22, l23, i21);
-    m.s4[s] = make_float4(aA11, aA12, aA13, i22);
-    m.s5[s] = make_float4(aA21, aA22, aA23, tv2i);
-    m.s6[s] = make_float4(aB11, aB12, aB13, tfriction);
-    m.s7[s] = make_float4(aB21, aB22, aB23, 0.f);
-    m.lever[s] = make_float4(lev[0], lev[1], lev[2], lev[3]);
-    m.state[s] = make_uint2(st, 0u);
+    mo.s0[so] = make_float4(rax, ray, raz, friction);
+    mo.s1[so] = make_float4(rbx, rby, rbz, i11);
+    mo.saxis[so] = make_float4(l11, l12, l13, i12);
+    mo.s3[so] = make_float4(l21, l22, l23, i21);
+    mo.s4[so] = make_float4(aA11, aA12, aA13, i22);
+    mo.s5[so] = make_float4(aA21, aA22, aA23, tv2i);
+    mo.s6[so] = make_float4(aB11, aB12, aB13, tfriction);
+    mo.s7[so] = make_float4(aB21, aB22, aB23, 0.f);
+    mo.lever[so] = make_float4(lev[0], lev[1], lev[2], lev[3]);
+    mo.state[so] = make_uint2(st, 0u);
+}
+template <class V>
+__device__ __forceinline__ void PrestepManifoldV(const ManifoldSoA& m, const V& bv, int s, int ra, int rb,
+                                                 const StepParams& p) {
+    PrestepManifoldIO(m, s, m, s, bv, ra, rb, p);
+}
+__device__ __forceinline__ void PrestepManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
+    int4 h = m.head[s];
+    PrestepManifoldV(m, GlobalBodies{b}, s, h.x, h.y, p);
 }
 
 // Warm start: ConvexContactManifoldConstraint.ExclusiveUpdate
@@ -562,8 +641,10 @@ __device__ __forceinline__ void WarmStartManifold(const ManifoldSoA& m, int s, B
     const int cap = m.capacity;
     bool dynA = st & kDynA, dynB = st & kDynB;
     float4 acc4 = m.penacc[s];
-    float accs[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
-    for (int k = 0; k < count; k++) {
+    const float accs[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k >= count) break;
         if (!(st & (1u << (kChildShift + k)))) continue;
         float4 j0 = m.pj0[k * cap + s], j1 = m.pj1[k * cap + s], j2 = m.pj2[k * cap + s];
         float acc = accs[k];
@@ -625,8 +706,25 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
     bool hasA = st & kHasA, hasB = st & kHasB;  // kinematic partners' velocities still enter
     bool dynA = st & kDynA, dynB = st & kDynB;
     int activeConstraints = 0;
+    // Every load of the visit is issued before the sequential solves start.
     float4 acc4 = m.penacc[s];
     float accs[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
+    float4 J0[4], J1[4], J2[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k < count) {
+            J0[k] = m.pj0[k * cap + s];
+            J1[k] = m.pj1[k * cap + s];
+            J2[k] = m.pj2[k * cap + s];
+        }
+    }
+    float4 f = m.fricacc[s];
+    float4 S0, S1, L1, L2, A1, A2, B1, B2, LEV;
+    if (st & (kSlidingBit | kTwistBit)) {
+        S0 = m.s0[s]; S1 = m.s1[s]; L1 = m.saxis[s]; L2 = m.s3[s];
+        A1 = m.s4[s]; A2 = m.s5[s]; B1 = m.s6[s]; B2 = m.s7[s];
+        LEV = m.lever[s];
+    }
     // SolveUpdateable bookkeeping for child c given its |impulse|.
     auto account = [&](int c, float r) {
         uint32_t z = (zeros >> (4 * c)) & 0xfu;
@@ -640,10 +738,12 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
         }
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
-    for (int k = 0; k < count; k++) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k >= count) break;
         if (!(st & (1u << (kChildShift + k)))) continue;
         // child currentIterations equals the group's here; the cap passed above
-        float4 j0 = m.pj0[k * cap + s], j1 = m.pj1[k * cap + s], j2 = m.pj2[k * cap + s];
+        const float4 j0 = J0[k], j1 = J1[k], j2 = J2[k];
         float lx = j0.x, ly = j0.y, lz = j0.z, bias = j0.w, softness = j1.w, v2i = j2.w;
         float rv = 0;
         if (hasA) rv = A.vx * lx + A.vy * ly + A.vz * lz + A.wx * j1.x + A.wy * j1.y + A.wz * j1.z;
@@ -663,11 +763,8 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
         }
         account(k, fabsf(lambda));
     }
-    float4 f = m.fricacc[s];
     if (st & kSlidingBit) {
         // SlidingFrictionTwoAxis.SolveIteration (SlidingFrictionTwoAxis.cs:155-234)
-        float4 S0 = m.s0[s], S1 = m.s1[s], L1 = m.saxis[s], L2 = m.s3[s];
-        float4 A1 = m.s4[s], A2 = m.s5[s], B1 = m.s6[s], B2 = m.s7[s];
         float dvx = 0, dvy = 0, dvz = 0;
         if (hasA) {
             dvx = A.vx + (A.wy * S0.z) - (A.wz * S0.y);
@@ -689,10 +786,12 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
         f.y += lyv;
         float length = f.x * f.x + f.y * f.y;
         float maximumFrictionForce = 0;
-        for (int k = 0; k < count; k++) maximumFrictionForce += accs[k];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (k < count) maximumFrictionForce += accs[k];
         maximumFrictionForce *= S0.w;
         if (length > maximumFrictionForce * maximumFrictionForce) {
-            length = maximumFrictionForce / (float)sqrt((double)length);
+            length = maximumFrictionForce / SqrtOfFloat(length);
             f.x *= length;
             f.y *= length;
         }
@@ -711,17 +810,19 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
     }
     if (st & kTwistBit) {
         // TwistFrictionConstraint.SolveIteration (TwistFrictionConstraint.cs:65-107)
-        float4 j0 = m.pj0[s], lev = m.lever[s];
-        float v2i = m.s5[s].w, friction = m.s6[s].w;
+        const float4 j0 = J0[0], lev = LEV;
+        float v2i = A2.w, friction = B1.w;
         float nx = -j0.x, ny = -j0.y, nz = -j0.z;
         float lambda = 0;
         if (hasA) lambda = A.wx * nx + A.wy * ny + A.wz * nz;
         if (hasB) lambda -= B.wx * nx + B.wy * ny + B.wz * nz;
         lambda *= v2i;
         float prev = f.z;
-        float levs[4] = {lev.x, lev.y, lev.z, lev.w};
+        const float levs[4] = {lev.x, lev.y, lev.z, lev.w};
         float maximumFrictionForce = 0;
-        for (int k = 0; k < count; k++) maximumFrictionForce += levs[k] * accs[k];
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            if (k < count) maximumFrictionForce += levs[k] * accs[k];
         maximumFrictionForce *= friction;
         f.z = Clampf(f.z + lambda, -maximumFrictionForce, maximumFrictionForce);
         lambda = f.z - prev;

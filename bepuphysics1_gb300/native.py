@@ -67,6 +67,7 @@ PHASE_TIMES_DTYPE = np.dtype([
     ("refresh_ms", "<f4"), ("force_ms", "<f4"), ("prestep_ms", "<f4"), ("warm_ms", "<f4"), ("solve_ms", "<f4"),
     ("position_ms", "<f4"), ("solve_launches", "<u4"), ("warm_launches", "<u4"),
     ("solve_algorithmic_bytes", "<f8"), ("solve_manifold_visits", "<f8"), ("solve_contact_visits", "<f8"),
+    ("group_ms", "<f4"), ("groups", "<u4"), ("group_compulsory_bytes", "<f8"),
 ])
 
 # bepugpu_status
@@ -109,6 +110,7 @@ GPU_EXPORTS = {
     "bepugpu_step": (_I, [_P, _I, _F, _U]),
     "bepugpu_set_solve_mode": (_I, [_P, _I, _I]),
     "bepugpu_set_persistent_blocks_per_sm": (_I, [_P, _I, _I]),
+    "bepugpu_set_group_policy": (_I, [_P, _I, _I, _I, _I, _I, _I]),
     "bepugpu_last_step_ms": (_I, [_P, _I, ctypes.POINTER(_F)]),
     "bepugpu_last_step_launches": (_I, [_P, _I, ctypes.POINTER(_U)]),
     "bepugpu_last_step_phase_ms": (_I, [_P, _I, _P]),

@@ -89,7 +89,10 @@ class GpuSpace:
     """One scene resident on the device: bodies plus the solver list."""
 
     def __init__(self, ctx: Context, bodies: np.ndarray, manifolds: np.ndarray | None = None,
-                 joints: np.ndarray | None = None, capacity: tuple[int, int, int] | None = None):
+                 joints: np.ndarray | None = None, capacity: tuple[int, int, int] | None = None,
+                 group_policy: tuple[int, int, int, int, int] | None = None):
+        """group_policy = (enabled, max_bodies, max_manifolds, target_manifolds, threads),
+        see bepugpu_set_group_policy; None keeps the library defaults."""
         self.ctx = ctx
         lib = ctx.lib
         manifolds = np.zeros(0, N.MANIFOLD_DTYPE) if manifolds is None else manifolds
@@ -99,8 +102,15 @@ class GpuSpace:
         ctx.check(lib.bepugpu_scene_create(ctx.handle, cap[0], cap[1], cap[2], ctypes.byref(sid)))
         self.id = sid.value
         self.solver = Solver(self)
+        if group_policy is not None:
+            self.set_group_policy(*group_policy)
         self.upload_bodies(bodies)
         self.upload_constraints(manifolds, joints)
+
+    def set_group_policy(self, enabled: int = 1, max_bodies: int = 1024, max_manifolds: int = 4096,
+                         target_manifolds: int = 64, threads: int = 0):
+        self.ctx.check(self.ctx.lib.bepugpu_set_group_policy(self.ctx.handle, self.id, enabled, max_bodies,
+                                                             max_manifolds, target_manifolds, threads))
 
     def upload_bodies(self, bodies: np.ndarray):
         bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)
@@ -163,8 +173,8 @@ class GpuSpace:
         return v.value
 
     def last_step_phase_ms(self) -> np.ndarray:
-        """[refresh + forces, prestep, warm start, solve, positions] device ms."""
-        out = np.zeros(5, np.float32)
+        """[refresh + forces, prestep, warm start, solve, positions, island groups] device ms."""
+        out = np.zeros(6, np.float32)
         self.ctx.check(self.ctx.lib.bepugpu_last_step_phase_ms(self.ctx.handle, self.id, N.ptr(out)))
         return out
 

@@ -233,6 +233,17 @@ bepugpu_status bepugpu_colour_list(const int32_t* body_a, const int32_t* body_b,
  * PositionUpdater.  dt = TimeStepSettings.TimeStepDuration. */
 bepugpu_status bepugpu_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags);
 bepugpu_status bepugpu_set_solve_mode(bepugpu_context* ctx, int32_t scene, int32_t mode);
+/* Island groups.  An island (dynamic bodies connected through constraints)
+ * with at most max_bodies bodies and max_manifolds manifolds runs its whole
+ * step inside one CTA with its bodies in shared memory; small islands are
+ * packed together up to target_manifolds per CTA.  Islands holding joints,
+ * larger islands and enabled = 0 use the colour-sweep path.  threads = 0 lets
+ * the plan choose the CTA size (else a multiple of 32 up to 256).  Takes
+ * effect at the next bepugpu_upload_constraints.  Defaults: 1, 1024, 4096,
+ * 64, 0. */
+bepugpu_status bepugpu_set_group_policy(bepugpu_context* ctx, int32_t scene, int32_t enabled, int32_t max_bodies,
+                                        int32_t max_manifolds, int32_t target_manifolds, int32_t threads);
+
 /* Persistent mode: resident blocks per SM of the cooperative launch (1 or 2). */
 bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* ctx, int32_t scene, int32_t blocks);
 
@@ -240,11 +251,12 @@ bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* ctx, int32_
  * with CUDA events on the scene's stream. */
 bepugpu_status bepugpu_last_step_ms(bepugpu_context* ctx, int32_t scene, float* ms);
 
-/* Device time of the phases of the last bepugpu_step.  Graph mode: from
- * events captured into the graph, [0] refresh + ForceUpdater, [1] prestep,
- * [2] warm start, [3] solve iterations, [4] PositionUpdater.  Persistent mode:
- * [3] only, from globaltimer stamps around the solve iterations; the others
- * are 0. */
+/* Device time of the phases of the last bepugpu_step (six floats).  [5] is
+ * the island-group kernel, which runs first.  Graph mode: the colour-sweep
+ * path's phases from events captured into the graph, [0] refresh +
+ * ForceUpdater, [1] prestep, [2] warm start, [3] solve iterations, [4]
+ * PositionUpdater.  Persistent mode: [3] only, from globaltimer stamps around
+ * the solve iterations; [0], [1], [2], [4] are 0. */
 bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* ctx, int32_t scene, float* phase_ms);
 
 /* Number of kernel launches the last bepugpu_step issued (graph nodes count
@@ -265,9 +277,14 @@ bepugpu_status bepugpu_batch_step(bepugpu_context* ctx, const int32_t* scenes, u
 typedef struct bepugpu_phase_times {
     float refresh_ms, force_ms, prestep_ms, warm_ms, solve_ms, position_ms;
     uint32_t solve_launches, warm_launches;
-    double solve_algorithmic_bytes;
+    double solve_algorithmic_bytes;   /* sweep path and island groups together */
     double solve_manifold_visits;
     double solve_contact_visits;
+    float group_ms;                   /* the island-group kernel (whole steps of small islands) */
+    uint32_t groups;                  /* CTAs of that kernel */
+    double group_compulsory_bytes;    /* DRAM bytes the group kernel cannot avoid in one step:
+                                         every input lane read once, every output or prestep
+                                         lane written once (288 + 112 c per manifold, 208 per body) */
 } bepugpu_phase_times;
 
 bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags,

@@ -49,10 +49,10 @@ class Pair:
     """A GPU scene and the oracle over the same records, the oracle's solver
     list permuted into the GPU's colour order (identity mapping)."""
 
-    def __init__(self, ctx, bodies, manifolds, joints=None, settings=None, mode=N.MODE_GRAPH):
+    def __init__(self, ctx, bodies, manifolds, joints=None, settings=None, mode=N.MODE_GRAPH, group_policy=None):
         self.settings = default_settings() if settings is None else settings
         ctx.set_settings(self.settings)
-        self.gpu = GpuSpace(ctx, bodies, manifolds, joints)
+        self.gpu = GpuSpace(ctx, bodies, manifolds, joints, group_policy=group_policy)
         self.gpu.set_mode(mode)
         colour, order, k = self.gpu.colouring()
         self.colours = k

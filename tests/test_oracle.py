@@ -180,3 +180,17 @@ def test_multithreaded_baseline_runs():
     o.step_multithreaded(DT, N.STEP_ALL, 3, 4)
     v = o.get_bodies()["linear_velocity"]
     assert np.isfinite(v).all() and np.abs(v).max() < 1.0
+
+
+def test_float_sqrt_through_double_is_float_sqrt():
+    """(float)Math.Sqrt((double)x) == IEEE sqrtf(x) for every float x: double
+    has at least 2*24+2 significant bits, so the double rounding is innocuous
+    (Figueroa 1995).  The device solver relies on this identity."""
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 0x7f800000, size=2_000_000, dtype=np.uint32)  # every finite non-negative float
+    x = bits.view(np.float32)
+    edge = np.array([0.0, -0.0, 1e-45, 1.17549435e-38, 3.4028235e38, 1.0, 2.0, 0.25, np.inf], np.float32)
+    x = np.concatenate([x, edge])
+    via_double = np.sqrt(x.astype(np.float64)).astype(np.float32)
+    direct = np.sqrt(x)
+    np.testing.assert_array_equal(via_double.view(np.uint32), direct.view(np.uint32))
