@@ -1,13 +1,320 @@
-// Batched stepping of many scenes (bepugpu_batch_step).
+// Batched stepping: many scenes advanced in one launch.
+//
+// The reference's analogue is ParallelSpaceTestDemo.cs:24-64: independent
+// Spaces updated side by side, each single-threaded.  Here every island group
+// of every listed scene is one CTA of one launch (two when some groups keep
+// their solve lanes in global memory); a CTA runs its group's `steps` steps
+// back to back with the group's bodies and lanes on chip, so one launch
+// advances the whole batch by several steps.  The launches are captured in a
+// CUDA graph and reused while the scene list, step counts, dt and settings
+// stay the same.
+//
+// A scene joins the batched launch when its whole step is island groups: no
+// constraints on the colour-sweep path, no joints, no dynamic body outside a
+// group and no moving kinematic body.  Other listed scenes are stepped with
+// their own one-scene path, after the batched launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "../../include/bepugpu.h"
 #include "bepugpu_internal.h"
+#include "groups_device.cuh"
+#include "solver_device.cuh"
+
+namespace bepugpu {
+
+struct SceneView {
+    ManifoldSoA m;
+    BodySoA b;
+    GroupTables t;
+};
+
+template <bool kShared>
+__global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
+                               uint32_t flags, int Bc, int Lc) {
+    extern __shared__ float4 smem[];
+    __shared__ SceneView sv;
+    const int4 w = work[blockIdx.x];  // scene view, group, steps
+    {
+        const int* src = (const int*)(views + w.x);
+        int* dst = (int*)&sv;
+        for (int i = threadIdx.x; i < (int)(sizeof(SceneView) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    const GroupDesc g = sv.t.groups[w.y];
+    for (int k = 0; k < w.z; k++) {
+        if (k) __syncthreads();  // the previous step's write-back is visible to the next step's loads
+        GroupStep<false, kShared>(sv.m, sv.b, p, flags, sv.t, g, Bc, Lc, smem, nullptr);
+    }
+}
+
+namespace {
+
+struct ClassLaunch {
+    std::vector<int4> work;
+    int Bc = 1, Lc = 1, members = 0;
+    int4* dev = nullptr;
+    size_t cap = 0;
+};
+
+struct Batch : BatchEngine {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    SceneView* viewsDev = nullptr;
+    size_t viewsCap = 0;
+    ClassLaunch shared, global;
+    cudaGraphExec_t graph = nullptr;
+    // key of the cached graph
+    std::vector<int32_t> keyScenes;
+    std::vector<uint32_t> keySteps;
+    std::vector<uint64_t> keyVersions;
+    float keyDt = 0.f;
+    uint32_t keyFlags = 0;
+    bepugpu_settings keySettings{};
+    uint32_t launches = 0;
+
+    ~Batch() override {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (viewsDev) cudaFree(viewsDev);
+        if (shared.dev) cudaFree(shared.dev);
+        if (global.dev) cudaFree(global.dev);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+int ThreadsFor(int members, int override_) {
+    if (override_ > 0) return override_;
+    int t = ((members + 31) / 32) * 32;
+    return std::min(std::max(t, 32), 256);
+}
+
+template <class T>
+cudaError_t Ensure(T*& p, size_t& cap, size_t n) {
+    if (n <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    size_t want = std::max(n, cap * 2);
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * want);
+    cap = e == cudaSuccess ? want : 0;
+    return e;
+}
+
+template <bool kShared>
+cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags) {
+    if (c.work.empty()) return cudaSuccess;
+    size_t smemBytes = GroupSmemBytes(kShared, c.Bc, c.Lc);
+    if (smemBytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_batch_groups<kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smemBytes);
+        if (e != cudaSuccess) return e;
+    }
+    k_batch_groups<kShared><<<(unsigned)c.work.size(), ThreadsFor(c.members, 0), smemBytes, bt.stream>>>(
+        bt.viewsDev, c.dev, p, flags, c.Bc, c.Lc);
+    bt.launches++;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool Scene::BatchReady() const {
+    return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && jointCount == 0 && sweepDynamicCount == 0 &&
+           !kinematicMoving;
+}
+
+}  // namespace bepugpu
 
 using namespace bepugpu;
 
-extern "C" bepugpu_status bepugpu_batch_step(bepugpu_context* c, const int32_t* scenes, uint32_t count, float dt,
-                                             uint32_t steps, uint32_t flags) {
+static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const uint32_t* stepsEach, uint32_t steps,
+                                uint32_t count, float dt, uint32_t flags) {
     auto* ctx = reinterpret_cast<Context*>(c);
     if (!ctx) return BEPUGPU_INVALID_ARGUMENT;
-    (void)scenes; (void)count; (void)dt; (void)steps; (void)flags;
-    ctx->SetError("batched stepping is not available in this build");
-    return BEPUGPU_INVALID_OPERATION;
+    cudaSetDevice(ctx->device);
+    if ((count && !scenes) || !(dt > 0)) {
+        ctx->SetError("batch: scenes must be given and dt must be positive");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    flags &= BEPUGPU_STEP_ALL;
+    if (!ctx->batch) {
+        auto* b = new Batch();
+        if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+            delete b;
+            ctx->SetError("batch: stream or event creation failed");
+            return BEPUGPU_CUDA_ERROR;
+        }
+        ctx->batch.reset(b);
+    }
+    Batch& bt = *static_cast<Batch*>(ctx->batch.get());
+    std::vector<Scene*> list(count);
+    std::vector<uint32_t> stepCount(count);
+    std::vector<uint64_t> versions(count);
+    for (uint32_t i = 0; i < count; i++) {
+        auto it = ctx->scenes.find(scenes[i]);
+        if (it == ctx->scenes.end()) {
+            ctx->SetError("batch: scene %d does not exist", scenes[i]);
+            return BEPUGPU_NOT_FOUND;
+        }
+        Scene* s = it->second.get();
+        uint32_t k = stepsEach ? stepsEach[i] : steps;
+        if (k > 65535) {
+            ctx->SetError("batch: at most 65535 steps per call");
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (s->maxBodyReferenced >= s->b.count) {
+            ctx->SetError("batch: scene %d references body %d of %d", scenes[i], s->maxBodyReferenced, s->b.count);
+            return BEPUGPU_INVALID_OPERATION;
+        }
+        for (uint32_t j = 0; j < i; j++)
+            if (list[j] == s) {
+                ctx->SetError("batch: scene %d is listed twice", scenes[i]);
+                return BEPUGPU_INVALID_ARGUMENT;
+            }
+        list[i] = s;
+        stepCount[i] = k;
+        versions[i] = s->version;
+        if (s->asyncPending) {  // a one-scene step may still run on the scene's stream
+            if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+                ctx->SetError("batch: scene %d stream failed", scenes[i]);
+                return BEPUGPU_CUDA_ERROR;
+            }
+            s->asyncPending = false;
+        }
+        bepugpu_status st = s->RefreshDamping(ctx, dt);
+        if (st != BEPUGPU_OK) return st;
+    }
+    StepParams p = MakeParams(ctx->settings, dt);
+    bool same = bt.graph && bt.keyDt == dt && bt.keyFlags == flags &&
+                std::memcmp(&bt.keySettings, &ctx->settings, sizeof(bepugpu_settings)) == 0 &&
+                bt.keyScenes.size() == count && std::equal(scenes, scenes + count, bt.keyScenes.begin()) &&
+                bt.keySteps == stepCount && bt.keyVersions == versions;
+    cudaError_t e = cudaSuccess;
+    if (!same) {
+        if (bt.graph) {
+            cudaGraphExecDestroy(bt.graph);
+            bt.graph = nullptr;
+        }
+        std::vector<SceneView> views;
+        bt.shared = ClassLaunch{{}, 1, 1, 0, bt.shared.dev, bt.shared.cap};
+        bt.global = ClassLaunch{{}, 1, 1, 0, bt.global.dev, bt.global.cap};
+        for (uint32_t i = 0; i < count; i++) {
+            Scene* s = list[i];
+            if (!s->BatchReady() || stepCount[i] == 0) continue;
+            const GroupPlan& g = s->groupPlan;
+            SceneView v;
+            v.m = s->m;
+            v.b = s->b;
+            v.t.groups = s->groupDescDev;
+            v.t.bodies = s->groupBodiesDev;
+            v.t.refs = s->groupRefsDev;
+            v.t.colourOffsets = s->groupColourOffsetsDev;
+            const int vi = (int)views.size();
+            views.push_back(v);
+            for (int k = g.shared.begin; k < g.shared.end; k++)
+                bt.shared.work.push_back(make_int4(vi, k, (int)stepCount[i], 0));
+            for (int k = g.global.begin; k < g.global.end; k++)
+                bt.global.work.push_back(make_int4(vi, k, (int)stepCount[i], 0));
+            if (g.shared.end > g.shared.begin) {
+                bt.shared.Bc = std::max(bt.shared.Bc, g.shared.maxLocal);
+                bt.shared.Lc = std::max(bt.shared.Lc, g.shared.maxManifolds);
+                bt.shared.members = std::max(bt.shared.members, g.shared.maxColourMembers);
+            }
+            if (g.global.end > g.global.begin) {
+                bt.global.Bc = std::max(bt.global.Bc, g.global.maxLocal);
+                bt.global.members = std::max(bt.global.members, g.global.maxColourMembers);
+            }
+        }
+        // the shared-lane groups of different scenes must fit one launch's budget together
+        if (GroupSmemBytes(true, bt.shared.Bc, bt.shared.Lc) > kGroupSmemBudget + 16 * 1024) {
+            ctx->SetError("batch: shared-lane groups need %zu bytes of shared memory",
+                          GroupSmemBytes(true, bt.shared.Bc, bt.shared.Lc));
+            return BEPUGPU_INVALID_OPERATION;
+        }
+        if ((e = Ensure(bt.viewsDev, bt.viewsCap, std::max<size_t>(views.size(), 1))) ||
+            (e = Ensure(bt.shared.dev, bt.shared.cap, std::max<size_t>(bt.shared.work.size(), 1))) ||
+            (e = Ensure(bt.global.dev, bt.global.cap, std::max<size_t>(bt.global.work.size(), 1)))) {
+            ctx->SetError("batch tables: %s", cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
+        }
+        if ((!views.empty() && (e = cudaMemcpyAsync(bt.viewsDev, views.data(), sizeof(SceneView) * views.size(),
+                                                    cudaMemcpyHostToDevice, bt.stream))) ||
+            (!bt.shared.work.empty() &&
+             (e = cudaMemcpyAsync(bt.shared.dev, bt.shared.work.data(), sizeof(int4) * bt.shared.work.size(),
+                                  cudaMemcpyHostToDevice, bt.stream))) ||
+            (!bt.global.work.empty() &&
+             (e = cudaMemcpyAsync(bt.global.dev, bt.global.work.data(), sizeof(int4) * bt.global.work.size(),
+                                  cudaMemcpyHostToDevice, bt.stream))) ||
+            (e = cudaStreamSynchronize(bt.stream))) {
+            ctx->SetError("batch tables: %s", cudaGetErrorString(e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        bt.launches = 0;
+        if ((e = cudaStreamBeginCapture(bt.stream, cudaStreamCaptureModeThreadLocal))) {
+            ctx->SetError("batch capture: %s", cudaGetErrorString(e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags);
+        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags);
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamEndCapture(bt.stream, &graph);
+        if (le != cudaSuccess || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            ctx->SetError("batch launch: %s", cudaGetErrorString(le != cudaSuccess ? le : e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        e = cudaGraphInstantiate(&bt.graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            bt.graph = nullptr;
+            ctx->SetError("batch graph: %s", cudaGetErrorString(e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        bt.keyScenes.assign(scenes, scenes + count);
+        bt.keySteps = stepCount;
+        bt.keyVersions = versions;
+        bt.keyDt = dt;
+        bt.keyFlags = flags;
+        bt.keySettings = ctx->settings;
+    }
+    if ((e = cudaEventRecord(bt.ev0, bt.stream)) || (e = cudaGraphLaunch(bt.graph, bt.stream)) ||
+        (e = cudaEventRecord(bt.ev1, bt.stream)) || (e = cudaStreamSynchronize(bt.stream))) {
+        ctx->SetError("batch step: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    uint32_t launches = bt.launches;
+    // Scenes outside the batched launch take their own path, step by step.
+    for (uint32_t i = 0; i < count; i++) {
+        Scene* s = list[i];
+        if (s->BatchReady()) continue;
+        for (uint32_t k = 0; k < stepCount[i]; k++) {
+            bepugpu_status st = s->Step(ctx, dt, flags);
+            if (st != BEPUGPU_OK) return st;
+            launches += s->launchesPerStep;
+        }
+        if (stepCount[i] && cudaStreamSynchronize(s->stream) != cudaSuccess) {
+            ctx->SetError("batch: one-scene steps failed");
+            return BEPUGPU_CUDA_ERROR;
+        }
+        s->asyncPending = false;
+    }
+    ctx->lastLaunches = launches;
+    cudaEventElapsedTime(&ctx->lastMs, bt.ev0, bt.ev1);
+    return BEPUGPU_OK;
+}
+
+extern "C" bepugpu_status bepugpu_batch_step(bepugpu_context* c, const int32_t* scenes, uint32_t count, float dt,
+                                             uint32_t steps, uint32_t flags) {
+    return BatchStep(c, scenes, nullptr, steps, count, dt, flags);
+}
+
+extern "C" bepugpu_status bepugpu_batch_step_each(bepugpu_context* c, const int32_t* scenes, const uint32_t* steps,
+                                                  uint32_t count, float dt, uint32_t flags) {
+    if (count && !steps) return BEPUGPU_INVALID_ARGUMENT;
+    return BatchStep(c, scenes, steps, 0, count, dt, flags);
 }

@@ -500,8 +500,12 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
 bepugpu_status Scene::RebuildSweepBodies(Context* ctx) {
     std::vector<int32_t> list;
     list.reserve(b.count);
+    sweepDynamicCount = 0;
     for (int32_t e = 0; e < b.count; e++)
-        if (!((size_t)e < hostOwned.size() && hostOwned[e])) list.push_back(e);
+        if (!((size_t)e < hostOwned.size() && hostOwned[e])) {
+            list.push_back(e);
+            if ((size_t)e < hostDynamic.size() && hostDynamic[e]) sweepDynamicCount++;
+        }
     sweepBodyCount = (uint32_t)list.size();
     if (!list.empty())
         CK(cudaMemcpyAsync(sweepBodiesDev, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice,
@@ -664,6 +668,7 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
     }
     CK(cudaEventRecord(evStop, stream));
     stepped = true;
+    asyncPending = true;
     return BEPUGPU_OK;
 }
 
@@ -829,7 +834,13 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
     }
     s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);
     s->hostDynamic.resize(n);
+    s->kinematicMoving = false;
     for (uint32_t i = 0; i < n; i++) {
+        if (!bodies[i].is_dynamic) {
+            const float* v = bodies[i].linear_velocity;
+            const float* w = bodies[i].angular_velocity;
+            if (v[0] != 0 || v[1] != 0 || v[2] != 0 || w[0] != 0 || w[1] != 0 || w[2] != 0) s->kinematicMoving = true;
+        }
         s->hostLinDamp[i] = bodies[i].linear_damping;
         s->hostAngDamp[i] = bodies[i].angular_damping;
         s->hostDynamic[i] = bodies[i].is_dynamic ? 1 : 0;

@@ -102,6 +102,11 @@ struct Scene {
     std::vector<uint8_t> hostOwned;  // body stepped by a group kernel
     int32_t* sweepBodiesDev = nullptr;  // bodies no group steps (valid when groups exist)
     uint32_t sweepBodyCount = 0;
+    uint32_t sweepDynamicCount = 0;     // dynamic bodies among them
+    bool kinematicMoving = false;       // a kinematic body has a velocity
+    bool asyncPending = false;          // a one-scene step may still run on `stream`
+    // The whole step is island groups, so a batched launch can run it (batch.cu).
+    bool BatchReady() const;
     int groupThreadsOverride = 0;    // 0 = derived from the plan
     cudaEvent_t evGroup[2] = {nullptr, nullptr};
     bepugpu_status UploadGroups(Context* ctx);

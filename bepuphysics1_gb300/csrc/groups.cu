@@ -21,180 +21,17 @@
 
 #include "../../include/bepugpu.h"
 #include "bepugpu_internal.h"
+#include "groups_device.cuh"
 #include "solver_device.cuh"
 
 namespace bepugpu {
-
-// Body view of a group kernel.  Refs >= 0 are the group's bodies in shared
-// memory, -1 is "no entity", refs <= -2 name global body -2 - ref (kinematic
-// bodies, read only).
-struct GroupBodies {
-    float4 *pos, *quat, *vlin, *vang, *inv0, *inv1;
-    BodySoA g;
-    __device__ __forceinline__ float4 Pos(int r) const { return r >= 0 ? pos[r] : g.pos[-2 - r]; }
-    __device__ __forceinline__ float4 Quat(int r) const { return r >= 0 ? quat[r] : g.quat[-2 - r]; }
-    __device__ __forceinline__ float4 Vlin(int r) const { return r >= 0 ? vlin[r] : g.vlin[-2 - r]; }
-    __device__ __forceinline__ float4 Vang(int r) const { return r >= 0 ? vang[r] : g.vang[-2 - r]; }
-    __device__ __forceinline__ float4 Inv0(int r) const { return r >= 0 ? inv0[r] : g.inv0[-2 - r]; }
-    __device__ __forceinline__ float4 Inv1(int r) const { return r >= 0 ? inv1[r] : g.inv1[-2 - r]; }
-    __device__ __forceinline__ void SetVelocity(int r, float4 v, float4 w) const {
-        if (r >= 0) { vlin[r] = v; vang[r] = w; }  // only a group's own (dynamic) bodies are written
-    }
-};
-
-// Shared memory of one CTA: 6 body lanes per body; with kShared also 24 float4
-// lanes, a state word and a ref pair per manifold (400 bytes).
-__host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int manifolds) {
-    return 96 * (size_t)bodies + (shared ? 400 * (size_t)manifolds : 0);
-}
 
 template <bool kCensus, bool kShared>
 __global__ void k_groups(ManifoldSoA m, BodySoA b, StepParams p, uint32_t flags, GroupTables t, int groupBase,
                          int Bc, int Lc, unsigned long long* census) {
     extern __shared__ float4 smem[];
     const GroupDesc g = t.groups[groupBase + blockIdx.x];
-    const int nLocal = g.bEnd - g.bBegin, nm = g.mEnd - g.mBegin;
-    GroupBodies bv;
-    bv.pos = smem;
-    bv.quat = bv.pos + Bc;
-    bv.vlin = bv.quat + Bc;
-    bv.vang = bv.vlin + Bc;
-    bv.inv0 = bv.vang + Bc;
-    bv.inv1 = bv.inv0 + Bc;
-    bv.g = b;
-    // Solve lanes: in shared memory at local slot j, or the global lanes at
-    // slot mBegin + j.
-    ManifoldSoA ml = m;
-    int2* sRefs = nullptr;
-    if (kShared) {
-        float4* lanes = smem + 6 * Bc;
-        ml.pj0 = lanes;
-        ml.pj1 = lanes + 4 * Lc;
-        ml.pj2 = lanes + 8 * Lc;
-        ml.s0 = lanes + 12 * Lc;
-        ml.s1 = lanes + 13 * Lc;
-        ml.saxis = lanes + 14 * Lc;
-        ml.s3 = lanes + 15 * Lc;
-        ml.s4 = lanes + 16 * Lc;
-        ml.s5 = lanes + 17 * Lc;
-        ml.s6 = lanes + 18 * Lc;
-        ml.s7 = lanes + 19 * Lc;
-        ml.lever = lanes + 20 * Lc;
-        ml.penacc = lanes + 21 * Lc;
-        ml.fricacc = lanes + 22 * Lc;
-        ml.head = (int4*)(lanes + 23 * Lc);
-        ml.state = (uint2*)(lanes + 24 * Lc);
-        sRefs = (int2*)(ml.state + Lc);
-        ml.capacity = Lc;
-    }
-    const int tid = threadIdx.x, T = blockDim.x;
-    const int lbase = kShared ? 0 : g.mBegin;  // slot of local manifold 0 in ml
-
-    // Bodies into shared memory, through the force update (EntityBase.cs:911-975).
-    for (int i = tid; i < nLocal; i += T) {
-        int gi = t.bodies[g.bBegin + i];
-        float4 v = b.vlin[gi], w = b.vang[gi], q = b.quat[gi], a, c;
-        if (flags & BEPUGPU_STEP_FORCES) {
-            ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], a, c, p);
-        } else {
-            a = b.inv0[gi];
-            c = b.inv1[gi];
-        }
-        bv.pos[i] = b.pos[gi];
-        bv.quat[i] = q;
-        bv.vlin[i] = v;
-        bv.vang[i] = w;
-        bv.inv0[i] = a;
-        bv.inv1[i] = c;
-    }
-    __syncthreads();
-    // Refresh, lanes in, prestep: a thread keeps the same manifolds throughout.
-    for (int j = tid; j < nm; j += T) {
-        const int s = g.mBegin + j;
-        int2 r = t.refs[s];
-        if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifoldV(m, bv, s, r.x, r.y, p);
-        if (kShared) {
-            ml.penacc[j] = m.penacc[s];  // after the refresh, which may compact them
-            ml.fricacc[j] = m.fricacc[s];
-            sRefs[j] = r;
-        }
-        if (flags & BEPUGPU_STEP_SOLVE) PrestepManifoldIO(m, s, ml, lbase + j, bv, r.x, r.y, p);
-        if (kCensus) {
-            // Compulsory DRAM bytes of the step for this manifold.  Lanes in shared memory:
-            // head, refs, 3 input lanes per contact, material, axis and impulses read once,
-            // positions, impulses and axis written once: 136 + 64 c.  Lanes in global
-            // memory add the prestep products written once: 288 + 112 c.
-            unsigned long long c4 = (unsigned long long)(m.head[s].z & 0xff);
-            atomicAdd(census + 3, kShared ? 136ull + 64ull * c4 : 288ull + 112ull * c4);
-        }
-    }
-    if (kCensus && tid == 0) atomicAdd(census + 3, 208ull * (unsigned long long)nLocal);  // 7 lanes in, 6 out
-    __syncthreads();
-    if (flags & BEPUGPU_STEP_SOLVE) {
-        const int* co = t.colourOffsets + g.cBegin;
-        for (int c = 0; c < g.cCount; c++) {
-            for (int j = co[c] + tid; j < co[c + 1]; j += T) {
-                const int sl = lbase + j;
-                uint2 st = ml.state[sl];
-                if (!(st.x & kGroupActive)) continue;
-                int2 r = kShared ? sRefs[j] : t.refs[g.mBegin + j];
-                BodyState A, B;
-                if (r.x != -1) LoadBodyV(bv, r.x, A);
-                if (r.y != -1) LoadBodyV(bv, r.y, B);
-                WarmStartManifold(ml, sl, A, B, st.x, ml.head[sl].z & 0xff);
-                if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
-                if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
-            }
-            __syncthreads();
-        }
-        for (int it = 0; it < p.iterationLimit; it++)
-            for (int c = 0; c < g.cCount; c++) {
-                for (int j = co[c] + tid; j < co[c + 1]; j += T) {
-                    const int sl = lbase + j;
-                    uint2 st = ml.state[sl];
-                    if (!(st.x & kGroupActive)) continue;
-                    int2 r = kShared ? sRefs[j] : t.refs[g.mBegin + j];
-                    const int count = ml.head[sl].z & 0xff;
-                    BodyState A, B;
-                    if (r.x != -1) LoadBodyV(bv, r.x, A);
-                    if (r.y != -1) LoadBodyV(bv, r.y, B);
-                    if (kCensus) {  // algorithmic bytes of the visit: 76 d + 136 + 48 c
-                        int d = ((st.x & kDynA) ? 1 : 0) + ((st.x & kDynB) ? 1 : 0);
-                        atomicAdd(census, 76ull * d + 136ull + 48ull * count);
-                        atomicAdd(census + 1, 1ull);
-                        atomicAdd(census + 2, (unsigned long long)count);
-                    }
-                    SolveManifold(ml, sl, A, B, st, count, p);
-                    if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
-                    if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
-                    ml.state[sl] = st;
-                }
-                __syncthreads();
-            }
-        if (kShared) {  // impulses and sliding axis back to the manifold records
-            for (int j = tid; j < nm; j += T) {
-                const int s = g.mBegin + j;
-                m.penacc[s] = ml.penacc[j];
-                m.fricacc[s] = ml.fricacc[j];
-                m.saxis[s] = ml.saxis[j];
-            }
-        }
-    }
-    // Position update (EntityBase.cs:1124-1160) and write-back.
-    for (int i = tid; i < nLocal; i += T) {
-        int gi = t.bodies[g.bBegin + i];
-        float4 pos = bv.pos[i], q = bv.quat[i], v = bv.vlin[i], w = bv.vang[i];
-        if (flags & BEPUGPU_STEP_POSITIONS) {
-            if (PositionMath(pos, q, v, w, p)) {
-                b.pos[gi] = pos;
-                b.quat[gi] = q;
-            }
-        }
-        b.vlin[gi] = v;
-        b.vang[gi] = w;
-        b.inv0[gi] = bv.inv0[i];
-        b.inv1[gi] = bv.inv1[i];
-    }
+    GroupStep<kCensus, kShared>(m, b, p, flags, t, g, Bc, Lc, smem, census);
 }
 
 // ------------------------------------------------------------------ host side --

@@ -115,6 +115,7 @@ GPU_EXPORTS = {
     "bepugpu_last_step_launches": (_I, [_P, _I, ctypes.POINTER(_U)]),
     "bepugpu_last_step_phase_ms": (_I, [_P, _I, _P]),
     "bepugpu_batch_step": (_I, [_P, _P, _U, _F, _U, _U]),
+    "bepugpu_batch_step_each": (_I, [_P, _P, _P, _U, _F, _U]),
     "bepugpu_profile_step": (_I, [_P, _I, _F, _U, _P]),
     "bepugpu_step_noalloc": (_I, [_P, _P, _U, _P, _U, _F, _U, _P]),
     "bepugpu_last_call_stats": (_I, [_P, ctypes.POINTER(_U), ctypes.POINTER(_F)]),

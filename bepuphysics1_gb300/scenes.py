@@ -63,5 +63,16 @@ def pile_64k(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):
                      friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed)
 
 
+def batch_body_counts(n: int, lo: int, hi: int, seed: int) -> np.ndarray:
+    """Scene sizes log-uniform in [lo, hi] (the batching and serving workloads)."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), n)).round().astype(np.int64)
+
+
+def tower_batch(n: int = 4096, lo: int = 8, hi: int = 2048, seed: int = 4):
+    """n independent tower scenes, body counts log-uniform in [lo, hi]."""
+    return [make_tower(int(k), seed=seed * 100003 + i) for i, k in enumerate(batch_body_counts(n, lo, hi, seed))]
+
+
 def contact_count(manifolds: np.ndarray) -> int:
     return int(manifolds["contact_count"].sum())

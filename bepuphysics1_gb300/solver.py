@@ -207,6 +207,26 @@ def colour_list(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | 
     return colour, order, k.value
 
 
+def batch_step(ctx: Context, spaces, dt: float, steps: int = 1, flags: int = N.STEP_ALL):
+    """bepugpu_batch_step: every space advances `steps` steps in one batched launch."""
+    ids = np.ascontiguousarray([s.id for s in spaces], dtype=np.int32)
+    ctx.check(ctx.lib.bepugpu_batch_step(ctx.handle, N.ptr(ids), len(ids), float(dt), steps, flags))
+
+
+def batch_step_each(ctx: Context, spaces, steps, dt: float, flags: int = N.STEP_ALL):
+    """bepugpu_batch_step_each: a step count per space."""
+    ids = np.ascontiguousarray([s.id for s in spaces], dtype=np.int32)
+    k = np.ascontiguousarray(steps, dtype=np.uint32)
+    ctx.check(ctx.lib.bepugpu_batch_step_each(ctx.handle, N.ptr(ids), N.ptr(k), len(ids), float(dt), flags))
+
+
+def last_call_stats(ctx: Context):
+    """(kernel launches, device ms) of the last batched call."""
+    n, ms = ctypes.c_uint32(), ctypes.c_float()
+    ctx.check(ctx.lib.bepugpu_last_call_stats(ctx.handle, ctypes.byref(n), ctypes.byref(ms)))
+    return n.value, ms.value
+
+
 def profile_step(space: GpuSpace, dt: float, flags: int = N.STEP_ALL) -> np.ndarray:
     """One instrumented step (bepugpu_profile_step): per-phase device ms and the
     solve census."""

@@ -263,11 +263,21 @@ bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* ctx, int32_t scene, f
  * as launches). */
 bepugpu_status bepugpu_last_step_launches(bepugpu_context* ctx, int32_t scene, uint32_t* launches);
 
-/* Batched stepping: every listed scene advances `steps` steps in one
- * persistent launch, one CTA per scene, body state in shared memory when it
- * fits (ParallelSpaceTestDemo.cs:24-64 is the reference's analogue). */
+/* Batched stepping (ParallelSpaceTestDemo.cs:24-64 is the reference's
+ * analogue: independent Spaces updated side by side).  Every island group of
+ * every listed scene becomes one CTA of one graph-captured launch, and each CTA
+ * runs its group's `steps` steps back to back with the group's bodies and
+ * solve lanes in shared memory.  A scene joins that launch when its whole step
+ * is island groups (no colour-sweep constraints, no joints, no dynamic body
+ * outside a group, no moving kinematic body); other listed scenes take their
+ * one-scene path after it.  The call returns when every scene has advanced.
+ * Results equal `steps` calls of bepugpu_step on each scene.  A scene may be
+ * listed once per call. */
 bepugpu_status bepugpu_batch_step(bepugpu_context* ctx, const int32_t* scenes, uint32_t count,
                                   float dt, uint32_t steps, uint32_t flags);
+/* The same with a step count per scene (0 leaves a scene as it is). */
+bepugpu_status bepugpu_batch_step_each(bepugpu_context* ctx, const int32_t* scenes, const uint32_t* steps,
+                                       uint32_t count, float dt, uint32_t flags);
 
 /* Per-phase device times of one step run as separate launches, each bracketed
  * by CUDA events on the scene's stream (an instrumented copy of bepugpu_step:
