@@ -62,6 +62,12 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
+    ap.add_argument("--no-batch", action="store_true", help="skip the many-scene batching section")
+    ap.add_argument("--batch-scenes", type=int, default=4096)
+    ap.add_argument("--batch-rounds", type=int, default=5, help="timed rounds of the plain and batched paths")
+    ap.add_argument("--tune-seconds", type=float, default=45.0, help="autotuner time limit")
+    ap.add_argument("--tune-out", default=None, help="write the autotuner's trials to this JSON file")
+    ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
     return ap.parse_args()
 
 
@@ -166,6 +172,152 @@ def cpu_baseline(bodies, manifolds, contact_iters_per_step, seconds, threads):
             "kind": "port", "steps": steps,
             "sample": f"{steps} full steps of the 65,536-box pile after 1 warm-up step "
                       f"(oracle port of Solver.UpdateMultithreaded, {threads} threads, {dt:.1f} s)"}
+
+
+BATCH_WORKLOAD = "towers_4096"
+BATCH_ITERATIONS = 8
+
+
+def batch_records(n, rank=0, world=1):
+    """The many-scene workload: n tower scenes, body counts log-uniform in
+    [8, 2048]; a rank takes every world-th scene."""
+    from bepuphysics1_gb300 import scenes
+    sizes = scenes.batch_body_counts(n, 8, 2048, 4)
+    return [scenes.make_tower(int(k), seed=4 * 100003 + i)[:2] for i, k in enumerate(sizes) if i % world == rank]
+
+
+def batch_settings():
+    from bepuphysics1_gb300.solver import default_settings
+    s = default_settings()
+    s["iteration_limit"] = BATCH_ITERATIONS
+    return s
+
+
+def cpu_batch_baseline(records, seconds, threads):
+    """Scene-parallel CPU stepping (ParallelSpaceTestDemo.cs:64): one oracle
+    Space per scene, single-threaded each, scenes spread over `threads` host
+    threads; one untimed round, then whole rounds until `seconds` pass."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    from bepuphysics1_gb300 import native as N
+    settings = batch_settings()
+    spaces = [oracle.OracleSpace(settings, b, m) for b, m in records]
+    for o in spaces:
+        o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+
+    def one(o):
+        o.step(DT, N.STEP_ALL, 1)
+
+    rounds = 0
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, spaces))
+        t0 = time.perf_counter()
+        while True:
+            list(ex.map(one, spaces))
+            rounds += 1
+            if time.perf_counter() - t0 >= seconds:
+                break
+        el = time.perf_counter() - t0
+    for o in spaces:
+        o.close()
+    return {"value": len(records) * rounds / el, "unit": "scene-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{rounds} rounds of all {len(records)} scenes after 1 warm-up round, one single-threaded "
+                      f"oracle Space per scene on {threads} threads ({el:.1f} s)"}
+
+
+def batch_section(args, local, rank, world, pg):
+    """Config-4 workload: the plain one-scene-per-launch path (bepugpu_step on
+    every scene) against batched stepping (bepugpu_batch_step) at the
+    autotuned configuration.  Both are timed on the host clock around calls
+    that return with the work finished; results are bit-identical between the
+    two paths (tests/test_gpu_batch.py)."""
+    from bepuphysics1_gb300 import autotune
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300.solver import Context, GpuSpace
+
+    t0 = time.perf_counter()
+    records = batch_records(args.batch_scenes, rank, world)
+    ctx = Context(local, batch_settings())
+    spaces = [GpuSpace(ctx, b, m) for b, m in records]
+    setup_s = time.perf_counter() - t0
+    n = len(spaces)
+    bodies = sum(len(b) for b, _ in records)
+    manifolds = sum(len(m) for _, m in records)
+    contacts = sum(int(m["contact_count"].sum()) for _, m in records)
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    # plain path: one bepugpu_step per scene, each its own graph launch
+    for _ in range(max(args.warmup, 3)):
+        for sp in spaces:
+            sp.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.batch_rounds):
+        for sp in spaces:
+            sp.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    plain_s = time.perf_counter() - t0
+    plain_launches = sum(sp.last_step_launches() for sp in spaces)
+
+    # autotuned batched path
+    res = autotune.tune(ctx, spaces, records, DT, max_seconds=args.tune_seconds)
+    if args.tune_out:
+        autotune.save(args.tune_out, res, BATCH_WORKLOAD)
+    best = res.best
+    per_k = {}
+    for k in sorted({1, best.steps_per_launch}):
+        barrier()
+        t = autotune.measure(ctx, spaces, DT, k, calls=max(args.batch_rounds, 3))
+        per_k[k] = t
+    tb = per_k[best.steps_per_launch]
+    t1 = per_k[1]
+
+    def whole(v):
+        if not pg:
+            return v
+        import torch
+        x = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+        pg.all_reduce(x)
+        return float(x.item())
+
+    plain_rate = whole(n * args.batch_rounds / plain_s)
+    batched_rate = whole(tb.scene_steps_per_s)
+    batched_1 = whole(t1.scene_steps_per_s)
+    out = {
+        "metric": "scene-steps/s", "workload": BATCH_WORKLOAD,
+        "config": {"scenes": args.batch_scenes, "bodies": bodies, "manifolds": manifolds, "contacts": contacts,
+                   "body_counts": "log-uniform in [8, 2048], towers of height 4..32 on a per-scene ground",
+                   "iterations": BATCH_ITERATIONS, "dt": float(DT), "setup_s": setup_s},
+        "plain": {"value": plain_rate, "unit": "scene-steps/s", "rounds": args.batch_rounds,
+                  "ms_per_round": 1000 * plain_s / args.batch_rounds, "gpu_launches_per_round": int(plain_launches),
+                  "path": "bepugpu_step per scene (one graph launch per scene-step), host clock"},
+        "batched": {"value": batched_rate, "unit": "scene-steps/s", "steps_per_launch": best.steps_per_launch,
+                    "ms_per_call": 1000 * n * best.steps_per_launch / tb.scene_steps_per_s,
+                    "device_ms_per_call": tb.device_ms_per_launch, "gpu_launches_per_call": tb.launches,
+                    "path": "bepugpu_batch_step, host clock around calls that return finished"},
+        "batched_1_step_per_launch": {"value": batched_1, "unit": "scene-steps/s",
+                                      "device_ms_per_call": t1.device_ms_per_launch,
+                                      "gpu_launches_per_call": t1.launches},
+        "speedup_vs_plain": batched_rate / plain_rate,
+        "speedup_vs_plain_1_step_per_launch": batched_1 / plain_rate,
+        "contact_iters_per_s_batched": contacts * BATCH_ITERATIONS * batched_rate / max(args.batch_scenes, 1),
+        "autotune": {"best": autotune.asdict(best), "trials": len(res.trials),
+                     "table": [[t.config.target_manifolds, t.config.smem_budget, t.config.threads,
+                                t.config.steps_per_launch, round(t.scene_steps_per_s)] for t in res.trials],
+                     "columns": ["target_manifolds", "smem_budget", "threads", "steps_per_launch",
+                                 "scene_steps_per_s"]},
+        "equal_error": "bit-identical to the plain path and to the colour-ordered oracle",
+    }
+    for sp in spaces:
+        sp.close()
+    ctx.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_batch_baseline(records, args.batch_cpu_seconds, os.cpu_count() or 1)
+    return out
 
 
 def run_reference(args, rank, world):
@@ -332,6 +484,11 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(bodies, manifolds, cips, args.cpu_sample_seconds, os.cpu_count() or 1)
 
+    batch = None
+    if not args.no_batch:
+        space.close()
+        batch = batch_section(args, local, rank, world, pg)
+
     if rank == 0:
         line = {
             "metric": "contact-iters/s", "value": value, "unit": "contact-iters/s", "n_gpus": world,
@@ -351,6 +508,7 @@ def main():
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     space.close()

@@ -74,6 +74,7 @@ struct Batch : BatchEngine {
     std::vector<uint64_t> keyVersions;
     float keyDt = 0.f;
     uint32_t keyFlags = 0;
+    int keyThreads = 0;
     bepugpu_settings keySettings{};
     uint32_t launches = 0;
 
@@ -106,7 +107,7 @@ cudaError_t Ensure(T*& p, size_t& cap, size_t n) {
 }
 
 template <bool kShared>
-cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags) {
+cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags, int threads) {
     if (c.work.empty()) return cudaSuccess;
     size_t smemBytes = GroupSmemBytes(kShared, c.Bc, c.Lc);
     if (smemBytes > 48 * 1024) {
@@ -114,7 +115,7 @@ cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uin
                                              (int)smemBytes);
         if (e != cudaSuccess) return e;
     }
-    k_batch_groups<kShared><<<(unsigned)c.work.size(), ThreadsFor(c.members, 0), smemBytes, bt.stream>>>(
+    k_batch_groups<kShared><<<(unsigned)c.work.size(), ThreadsFor(c.members, threads), smemBytes, bt.stream>>>(
         bt.viewsDev, c.dev, p, flags, c.Bc, c.Lc);
     bt.launches++;
     return cudaGetLastError();
@@ -190,7 +191,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         if (st != BEPUGPU_OK) return st;
     }
     StepParams p = MakeParams(ctx->settings, dt);
-    bool same = bt.graph && bt.keyDt == dt && bt.keyFlags == flags &&
+    bool same = bt.graph && bt.keyDt == dt && bt.keyFlags == flags && bt.keyThreads == ctx->batchThreads &&
                 std::memcmp(&bt.keySettings, &ctx->settings, sizeof(bepugpu_settings)) == 0 &&
                 bt.keyScenes.size() == count && std::equal(scenes, scenes + count, bt.keyScenes.begin()) &&
                 bt.keySteps == stepCount && bt.keyVersions == versions;
@@ -259,8 +260,8 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             ctx->SetError("batch capture: %s", cudaGetErrorString(e));
             return BEPUGPU_CUDA_ERROR;
         }
-        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags);
-        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags);
+        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads);
+        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(bt.stream, &graph);
         if (le != cudaSuccess || e != cudaSuccess) {
@@ -280,6 +281,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         bt.keyVersions = versions;
         bt.keyDt = dt;
         bt.keyFlags = flags;
+        bt.keyThreads = ctx->batchThreads;
         bt.keySettings = ctx->settings;
     }
     if ((e = cudaEventRecord(bt.ev0, bt.stream)) || (e = cudaGraphLaunch(bt.graph, bt.stream)) ||
@@ -317,4 +319,15 @@ extern "C" bepugpu_status bepugpu_batch_step_each(bepugpu_context* c, const int3
                                                   uint32_t count, float dt, uint32_t flags) {
     if (count && !steps) return BEPUGPU_INVALID_ARGUMENT;
     return BatchStep(c, scenes, steps, 0, count, dt, flags);
+}
+
+extern "C" bepugpu_status bepugpu_set_batch_threads(bepugpu_context* c, int32_t threads) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    if (!ctx) return BEPUGPU_INVALID_ARGUMENT;
+    if (threads != 0 && (threads < 32 || threads > 256 || threads % 32)) {
+        ctx->SetError("batch threads must be 0 or a multiple of 32 in [32, 256]");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    ctx->batchThreads = threads;
+    return BEPUGPU_OK;
 }

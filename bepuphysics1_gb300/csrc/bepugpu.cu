@@ -1094,6 +1094,19 @@ bepugpu_status bepugpu_set_group_policy(bepugpu_context* c, int32_t id, int32_t 
     return BEPUGPU_OK;
 }
 
+bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* c, int32_t id, uint32_t bytes) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return BEPUGPU_NOT_FOUND;
+    if (bytes > kGroupSmemBudget) {
+        ctx->SetError("shared-lane budget above %zu bytes", kGroupSmemBudget);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    s->policy.sharedLanesBudget = bytes;
+    return BEPUGPU_OK;
+}
+
 bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* c, int32_t id, int32_t blocks) {
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);

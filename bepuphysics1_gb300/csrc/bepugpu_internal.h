@@ -54,6 +54,7 @@ struct GroupPolicy {
     int32_t maxGroupBodies = 1024;       // shared memory: 96 bytes per body
     int32_t maxGroupManifolds = 4096;    // larger islands stay on the sweep path
     int32_t targetGroupManifolds = 64;   // small islands are packed up to this size
+    uint32_t sharedLanesBudget = 200 * 1024;  // groups needing more keep their lanes in global memory
 };
 // Groups [begin, end) of one kernel variant and the sizes its launch needs.
 struct GroupClass {
@@ -175,6 +176,7 @@ struct Context {
     std::unique_ptr<BatchEngine> batch;
     uint32_t lastLaunches = 0;
     float lastMs = 0.f;
+    int batchThreads = 0;  // threads per CTA of batched launches, 0 = from the groups' colour sizes
     void SetError(const char* fmt, ...);
 };
 

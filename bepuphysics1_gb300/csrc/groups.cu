@@ -128,7 +128,8 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
     std::iota(order.begin(), order.end(), 0);
     std::vector<uint8_t> fits(G);
     for (int32_t gId = 0; gId < G; gId++)
-        fits[gId] = GroupSmemBytes(true, (int)gBodies[gId].size(), (int)members[gId].size()) <= kGroupSmemBudget;
+        fits[gId] = GroupSmemBytes(true, (int)gBodies[gId].size(), (int)members[gId].size()) <=
+                    std::min<size_t>(pol.sharedLanesBudget, kGroupSmemBudget);
     std::stable_partition(order.begin(), order.end(), [&](int32_t gId) { return fits[gId] != 0; });
 
     // Slots: the sweep part, then the groups in launch order.

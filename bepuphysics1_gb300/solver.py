@@ -90,9 +90,10 @@ class GpuSpace:
 
     def __init__(self, ctx: Context, bodies: np.ndarray, manifolds: np.ndarray | None = None,
                  joints: np.ndarray | None = None, capacity: tuple[int, int, int] | None = None,
-                 group_policy: tuple[int, int, int, int, int] | None = None):
+                 group_policy: tuple[int, int, int, int, int] | None = None, smem_budget: int | None = None):
         """group_policy = (enabled, max_bodies, max_manifolds, target_manifolds, threads),
-        see bepugpu_set_group_policy; None keeps the library defaults."""
+        see bepugpu_set_group_policy; smem_budget = bepugpu_set_group_smem_budget;
+        None keeps the library defaults."""
         self.ctx = ctx
         lib = ctx.lib
         manifolds = np.zeros(0, N.MANIFOLD_DTYPE) if manifolds is None else manifolds
@@ -104,6 +105,8 @@ class GpuSpace:
         self.solver = Solver(self)
         if group_policy is not None:
             self.set_group_policy(*group_policy)
+        if smem_budget is not None:
+            self.set_group_smem_budget(smem_budget)
         self.upload_bodies(bodies)
         self.upload_constraints(manifolds, joints)
 
@@ -111,6 +114,11 @@ class GpuSpace:
                          target_manifolds: int = 64, threads: int = 0):
         self.ctx.check(self.ctx.lib.bepugpu_set_group_policy(self.ctx.handle, self.id, enabled, max_bodies,
                                                              max_manifolds, target_manifolds, threads))
+
+    def set_group_smem_budget(self, nbytes: int):
+        """bepugpu_set_group_smem_budget: groups needing more shared memory keep
+        their solve lanes in global memory (next upload_constraints)."""
+        self.ctx.check(self.ctx.lib.bepugpu_set_group_smem_budget(self.ctx.handle, self.id, int(nbytes)))
 
     def upload_bodies(self, bodies: np.ndarray):
         bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)
@@ -218,6 +226,11 @@ def batch_step_each(ctx: Context, spaces, steps, dt: float, flags: int = N.STEP_
     ids = np.ascontiguousarray([s.id for s in spaces], dtype=np.int32)
     k = np.ascontiguousarray(steps, dtype=np.uint32)
     ctx.check(ctx.lib.bepugpu_batch_step_each(ctx.handle, N.ptr(ids), N.ptr(k), len(ids), float(dt), flags))
+
+
+def set_batch_threads(ctx: Context, threads: int):
+    """bepugpu_set_batch_threads: CTA size of batched launches (0 = from the plan)."""
+    ctx.check(ctx.lib.bepugpu_set_batch_threads(ctx.handle, int(threads)))
 
 
 def last_call_stats(ctx: Context):

@@ -244,6 +244,13 @@ bepugpu_status bepugpu_set_solve_mode(bepugpu_context* ctx, int32_t scene, int32
 bepugpu_status bepugpu_set_group_policy(bepugpu_context* ctx, int32_t scene, int32_t enabled, int32_t max_bodies,
                                         int32_t max_manifolds, int32_t target_manifolds, int32_t threads);
 
+/* Shared-memory residency threshold of island groups: a group whose bodies and
+ * solve lanes need at most `bytes` (96 per body + 400 per manifold) keeps its
+ * solve lanes in shared memory; larger groups keep them in global memory.
+ * 0 keeps every group's lanes in global memory.  At most 200 KiB (default).
+ * Takes effect at the next bepugpu_upload_constraints. */
+bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* ctx, int32_t scene, uint32_t bytes);
+
 /* Persistent mode: resident blocks per SM of the cooperative launch (1 or 2). */
 bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* ctx, int32_t scene, int32_t blocks);
 
@@ -278,6 +285,10 @@ bepugpu_status bepugpu_batch_step(bepugpu_context* ctx, const int32_t* scenes, u
 /* The same with a step count per scene (0 leaves a scene as it is). */
 bepugpu_status bepugpu_batch_step_each(bepugpu_context* ctx, const int32_t* scenes, const uint32_t* steps,
                                        uint32_t count, float dt, uint32_t flags);
+/* Threads per CTA of the batched launches: 0 (default) sizes them from the
+ * largest colour of the listed groups; else a multiple of 32 in [32, 256].
+ * Results do not depend on it. */
+bepugpu_status bepugpu_set_batch_threads(bepugpu_context* ctx, int32_t threads);
 
 /* Per-phase device times of one step run as separate launches, each bracketed
  * by CUDA events on the scene's stream (an instrumented copy of bepugpu_step:

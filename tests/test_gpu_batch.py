@@ -87,3 +87,30 @@ def test_batch_errors(gpu_context):
         batch_step(gpu_context, [sp], 0.0)
     for _, _, s in made:
         s.close()
+
+
+def test_autotune_keeps_results(gpu_context, tmp_path):
+    """Every autotuner setting gives the oracle's bits; the tuned plan is saved and reloaded."""
+    from bepuphysics1_gb300 import autotune
+    from bepuphysics1_gb300.solver import set_batch_threads
+    gpu_context.set_settings(default_settings())
+    made = _make(gpu_context, count=12, seed=21)
+    spaces = [sp for _, _, sp in made]
+    records = [(b, m) for b, m, _ in made]
+    res = autotune.tune(gpu_context, spaces, records, DT, targets=(16, 64), budgets=(0, 200 * 1024),
+                        threads=(0, 64), steps=(1, 4), calls=1, max_seconds=60)
+    assert len(res.trials) >= 5 and res.scene_steps_per_s > 0
+    path = tmp_path / "tune.json"
+    autotune.save(path, res, "test")
+    cfg = autotune.load(path)
+    assert cfg == res.best
+    for cand in (cfg, autotune.BatchConfig(16, 0, 32, 2)):
+        autotune.apply(gpu_context, spaces, records, cand)
+        batch_step(gpu_context, spaces, DT, steps=4)
+        for b, m, sp in made:
+            ob, om = _oracle_after(b, m, sp, 4)
+            errs, exact = compare(sp.download_bodies(b.copy()), sp.download_constraints(m.copy())[0], ob, om)
+            assert exact, (cand, errs)
+    set_batch_threads(gpu_context, 0)
+    for sp in spaces:
+        sp.close()
