@@ -229,6 +229,47 @@ __global__ void k_solve(ManifoldSoA m, BodySoA b, StepParams p, int begin, int e
     if (s < end) SolveSlot(m, b, s, p);
 }
 
+// Joints (joints_device.cuh).  A colour's joints and manifolds touch different
+// dynamic bodies, so one launch runs both: threads [0, joints) take the joints.
+__device__ __forceinline__ void WarmJointSlot(const JointSoA& j, const BodySoA& b, int s) {
+    uint2 st = j.state[s];
+    if (!(st.x & kGroupActive)) return;
+    int4 h = j.head[s];
+    BodyState A, B;
+    LoadJointVelocity(b, h.x, A);
+    LoadJointVelocity(b, h.y, B);
+    WarmJoint(j, s, A, B, st.x, h.z & 0xff);
+    if (st.x & kDynA) StoreVelocity(b, h.x, A);
+    if (st.x & kDynB) StoreVelocity(b, h.y, B);
+}
+__device__ __forceinline__ void SolveJointSlot(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
+    uint2 st = j.state[s];
+    if (!(st.x & kGroupActive)) return;
+    int4 h = j.head[s];
+    BodyState A, B;
+    LoadJointVelocity(b, h.x, A);
+    LoadJointVelocity(b, h.y, B);
+    SolveJoint(j, s, A, B, st, h.z & 0xff, p);
+    if (st.x & kDynA) StoreVelocity(b, h.x, A);
+    if (st.x & kDynB) StoreVelocity(b, h.y, B);
+    j.state[s] = st;
+}
+__global__ void k_prestep_mixed(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < j.count) PrestepJoint(j, b, t, p);
+    else if (t - j.count < m.count) PrestepManifold(m, b, t - j.count, p);
+}
+__global__ void k_warm_mixed(ManifoldSoA m, BodySoA b, JointSoA j, int mb, int me, int jb, int je) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < je - jb) WarmJointSlot(j, b, jb + t);
+    else if (mb + t - (je - jb) < me) WarmSlot(m, b, mb + t - (je - jb));
+}
+__global__ void k_solve_mixed(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, int mb, int me, int jb, int je) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < je - jb) SolveJointSlot(j, b, jb + t, p);
+    else if (mb + t - (je - jb) < me) SolveSlot(m, b, mb + t - (je - jb), p);
+}
+
 // Bounded grid barrier for the cooperative kernel.  Thread 0 of each block
 // arrives on a counter; the last arrival resets it and bumps the generation.
 // A wait that outlives kBarrierSpinLimit polls sets *err and the kernel returns.
@@ -265,8 +306,10 @@ __device__ __forceinline__ bool GridBarrier(unsigned int* counter, volatile unsi
 struct PersistentArgs {
     ManifoldSoA m;
     BodySoA b;
+    JointSoA j;
     StepParams p;
     const int* colourOffsets;  // manifold slots, colours + 1 entries
+    const int* jointOffsets;   // joint slots, colours + 1 entries
     int colours;
     uint32_t flags;
     unsigned int* counter;
@@ -298,15 +341,21 @@ __global__ void k_persistent(PersistentArgs a) {
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
     }
     if (a.flags & BEPUGPU_STEP_SOLVE) {
+        for (int s = tid; s < a.j.count; s += stride) PrestepJoint(a.j, a.b, s, a.p);
         for (int s = tid; s < a.m.count; s += stride) PrestepManifold(a.m, a.b, s, a.p);
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
         for (int c = 0; c < a.colours; c++) {
+            if (a.j.count)
+                for (int s = a.jointOffsets[c] + tid; s < a.jointOffsets[c + 1]; s += stride) WarmJointSlot(a.j, a.b, s);
             for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride) WarmSlot(a.m, a.b, s);
             if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
         }
         if (tid == 0) a.stamps[0] = GlobalTimer();
         for (int it = 0; it < a.p.iterationLimit; it++)
             for (int c = 0; c < a.colours; c++) {
+                if (a.j.count)
+                    for (int s = a.jointOffsets[c] + tid; s < a.jointOffsets[c + 1]; s += stride)
+                        SolveJointSlot(a.j, a.b, s, a.p);
                 for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride)
                     SolveSlot(a.m, a.b, s, a.p);
                 if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
@@ -438,7 +487,7 @@ bepugpu_status Scene::RefreshDamping(Context* ctx, float dt) {
 
 bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj) {
     maxBodies = nb; maxManifolds = nm; maxJoints = nj;
-    size_t B = nb ? nb : 1, M = nm ? nm : 1;
+    size_t B = nb ? nb : 1, M = nm ? nm : 1, J = nj ? nj : 1;
     size_t bytes = 0;
     auto take = [&](size_t n) { size_t o = bytes; bytes += Align(n); return o; };
     size_t oPos = take(16 * B), oQuat = take(16 * B), oVlin = take(16 * B), oVang = take(16 * B),
@@ -449,7 +498,9 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
            oAxis = take(16 * M), oPj0 = take(64 * M), oPj1 = take(64 * M), oPj2 = take(64 * M),
            oS0 = take(16 * M), oS1 = take(16 * M), oS3 = take(16 * M), oS4 = take(16 * M), oS5 = take(16 * M),
            oS6 = take(16 * M), oS7 = take(16 * M), oLev = take(16 * M), oState = take(8 * M),
-           oSlot = take(4 * M), oOffs = take(4 * (M + 2));
+           oSlot = take(4 * M), oOffs = take(4 * (M + J + 2));
+    size_t oJHead = take(16 * J), oJLanes = take(16 * (size_t)kJointLanes * J), oJState = take(8 * J),
+           oJOffs = take(4 * (M + J + 2));
     size_t oGroups = take(sizeof(GroupDesc) * M), oGroupBodies = take(4 * B), oGroupRefs = take(8 * M),
            oGroupOffsets = take(4 * (2 * M + 2)), oSweepBodies = take(4 * B);
     arenaBytes = bytes;
@@ -481,6 +532,12 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     groupRefsDev = (int2*)(base + oGroupRefs);
     groupColourOffsetsDev = (int32_t*)(base + oGroupOffsets);
     sweepBodiesDev = (int32_t*)(base + oSweepBodies);
+    j.head = (int4*)(base + oJHead);
+    j.lanes = (float4*)(base + oJLanes);
+    j.state = (uint2*)(base + oJState);
+    j.count = 0;
+    j.capacity = (int)J;
+    jointOffsetsDev = (int32_t*)(base + oJOffs);
     CK(cudaMemset(arena, 0, bytes));
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
     stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
@@ -557,15 +614,25 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
         k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[1], stream, cudaEventRecordExternal));
-    bool solve = (flags & BEPUGPU_STEP_SOLVE) && nm;
+    const int nj = j.count;
+    bool solve = (flags & BEPUGPU_STEP_SOLVE) && (nm || nj);
     if (solve) {
-        k_prestep<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
+        if (nj) k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, stream>>>(ms, b, j, p);
+        else k_prestep<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p);
+        launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[2], stream, cudaEventRecordExternal));
     if (solve) {
         for (int c = 0; c < colours; c++) {
             int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
-            if (b1 > b0) { k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, b0, b1); launchesPerStep++; }
+            int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
+            if (j1 > j0) {
+                k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, j, b0, b1, j0, j1);
+                launchesPerStep++;
+            } else if (b1 > b0) {
+                k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, b0, b1);
+                launchesPerStep++;
+            }
         }
     }
     CK(cudaEventRecordWithFlags(evPhase[3], stream, cudaEventRecordExternal));
@@ -573,7 +640,14 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
         for (int it = 0; it < p.iterationLimit; it++)
             for (int c = 0; c < colours; c++) {
                 int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
-                if (b1 > b0) { k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1); launchesPerStep++; }
+                int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
+                if (j1 > j0) {
+                    k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, j, p, b0, b1, j0, j1);
+                    launchesPerStep++;
+                } else if (b1 > b0) {
+                    k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1);
+                    launchesPerStep++;
+                }
             }
     }
     CK(cudaEventRecordWithFlags(evPhase[4], stream, cudaEventRecordExternal));
@@ -625,8 +699,9 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
     }
     CK(cudaEventRecord(evGroup[1], stream));
     PersistentArgs a;
-    a.m = SweepManifolds(); a.b = b; a.p = p;
+    a.m = SweepManifolds(); a.b = b; a.j = j; a.p = p;
     a.colourOffsets = colourOffsetsDev;
+    a.jointOffsets = jointOffsetsDev;
     a.colours = SweepColours();
     a.flags = flags;
     a.counter = BarrierCounter();
@@ -886,12 +961,16 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         ctx->SetError("constraint counts exceed scene capacity");
         return BEPUGPU_INVALID_ARGUMENT;
     }
-    if (nj) {
-        ctx->SetError("joint constraints are not available in this build");
-        return BEPUGPU_INVALID_OPERATION;
-    }
     int nb = s->b.count;
+    if (nj) {
+        bepugpu_status jst = CheckJointRecords(ctx, joints, nj, nb);
+        if (jst != BEPUGPU_OK) return jst;
+    }
     std::vector<int32_t> a(nm + nj), bb(nm + nj);
+    for (uint32_t u = 0; u < nj; u++) {
+        a[u] = joints[u].body_a;
+        bb[u] = joints[u].body_b;
+    }
     for (uint32_t i = 0; i < nm; i++) {
         a[nj + i] = man[i].body_a;
         bb[nj + i] = man[i].body_b;
@@ -917,6 +996,19 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
                s->hostDynamic.data(), nb, s->groupPlan);
     const GroupPlan& plan = s->groupPlan;
     s->manifoldOffsets = plan.globalOffsets;
+    {  // joint slots: colour-major, list order inside a colour; every joint is on the sweep path
+        const int colours = (int)plan.globalOffsets.size() - 1;
+        std::vector<std::vector<int32_t>> byColour(std::max(colours, 0));
+        for (uint32_t u = 0; u < nj; u++) byColour[s->colouring.colour[u]].push_back((int32_t)u);
+        s->jointOffsets.assign(colours + 1, 0);
+        s->hostJointSlotOf.assign(nj, -1);
+        int32_t slot = 0;
+        for (int c = 0; c < colours; c++) {
+            s->jointOffsets[c] = slot;
+            for (int32_t u : byColour[c]) s->hostJointSlotOf[u] = slot++;
+        }
+        s->jointOffsets[colours] = slot;
+    }
     s->hostOwned.assign(nb, 0);
     for (int32_t e = 0; e < nb && e < (int32_t)plan.localOf.size(); e++) s->hostOwned[e] = plan.localOf[e] >= 0;
     {
@@ -941,6 +1033,10 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     s->hostBodyB.assign(bb.begin() + nj, bb.end());
     s->maxBodyReferenced = -1;
     for (uint32_t u = 0; u < nm + nj; u++) s->maxBodyReferenced = std::max(s->maxBodyReferenced, std::max(a[u], bb[u]));
+    {
+        bepugpu_status jst = UploadJoints(ctx, s, joints, nj);
+        if (jst != BEPUGPU_OK) return jst;
+    }
     return UploadManifoldRecords(ctx, s, man, nm);
 }
 
@@ -1001,6 +1097,10 @@ bepugpu_status bepugpu_download_constraints(bepugpu_context* c, int32_t id, bepu
     if (nm != (uint32_t)s->m.count || nj != s->jointCount || (nm && !man) || (nj && !joints)) {
         ctx->SetError("download_constraints needs %d manifolds and %u joints", s->m.count, s->jointCount);
         return BEPUGPU_INVALID_ARGUMENT;
+    }
+    {
+        bepugpu_status jst = DownloadJoints(ctx, s, joints, nj);
+        if (jst != BEPUGPU_OK) return jst;
     }
     if (!nm) return BEPUGPU_OK;
     ManifoldOut* dev = (ManifoldOut*)s->staging;
@@ -1219,21 +1319,28 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     if ((flags & BEPUGPU_STEP_FORCES) && nb) {
         cudaEvent_t a = mark(); k_force<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->force_ms});
     }
-    if ((flags & BEPUGPU_STEP_SOLVE) && nm) {
-        cudaEvent_t a = mark(); k_prestep<<<Blocks(nm, T), T, 0, q>>>(ms, s->b, p); spans.push_back({a, mark(), &out->prestep_ms});
+    const int nj = s->j.count;
+    if ((flags & BEPUGPU_STEP_SOLVE) && (nm || nj)) {
+        cudaEvent_t a = mark();
+        k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, q>>>(ms, s->b, s->j, p);
+        spans.push_back({a, mark(), &out->prestep_ms});
         for (int cc = 0; cc < colours; cc++) {
             int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
-            if (b1 <= b0) continue;
-            cudaEvent_t e0 = mark(); k_warm<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, s->b, b0, b1);
+            int j0 = nj ? s->jointOffsets[cc] : 0, j1 = nj ? s->jointOffsets[cc + 1] : 0;
+            if (b1 - b0 + j1 - j0 <= 0) continue;
+            cudaEvent_t e0 = mark();
+            k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, s->j, b0, b1, j0, j1);
             spans.push_back({e0, mark(), &out->warm_ms});
             out->warm_launches++;
         }
         for (int it = 0; it < p.iterationLimit; it++)
             for (int cc = 0; cc < colours; cc++) {
                 int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
-                if (b1 <= b0) continue;
-                k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, b0, b1, acc);
-                cudaEvent_t e0 = mark(); k_solve<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, s->b, p, b0, b1);
+                int j0 = nj ? s->jointOffsets[cc] : 0, j1 = nj ? s->jointOffsets[cc + 1] : 0;
+                if (b1 - b0 + j1 - j0 <= 0) continue;
+                if (b1 > b0) k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, b0, b1, acc);
+                cudaEvent_t e0 = mark();
+                k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, s->j, p, b0, b1, j0, j1);
                 spans.push_back({e0, mark(), &out->solve_ms});
                 out->solve_launches++;
             }

@@ -11,6 +11,7 @@
 
 #include "../../include/bepugpu.h"
 #include "colouring.h"
+#include "joints_device.cuh"
 #include "solver_device.cuh"
 
 namespace bepugpu {
@@ -73,6 +74,11 @@ constexpr size_t kGroupSmemBudget = 200 * 1024;
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
                 int32_t nm, const uint8_t* dynamic, int32_t nb, GroupPlan& plan);
 bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
+// Joints (joints.cu): record checks, upload into the scene's joint slots, and
+// the accumulated impulses back into records.
+bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint32_t nj, int32_t bodies);
+bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints, uint32_t nj);
+bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uint32_t nj);
 int GroupLaunchCount(const GroupPlan& g);
 // Damping flags bit 2 marks a body stepped by a group kernel.
 constexpr uint32_t kOwnedByGroup = 4u;
@@ -131,6 +137,11 @@ struct Scene {
     int32_t* slotOf = nullptr;           // device: manifold record -> slot
     int32_t* colourOffsetsDev = nullptr; // device: manifold slot range per colour
     uint32_t jointCount = 0;
+    JointSoA j{};                         // joint slots in colour order (joints.cu)
+    std::vector<int32_t> jointOffsets;    // joint slot range per sweep colour
+    std::vector<int32_t> hostJointSlotOf; // joint record -> slot
+    int32_t* jointOffsetsDev = nullptr;
+    std::vector<float4> hostJointAcc;     // download scratch: [2][joints]
     Colouring colouring;
     std::vector<int32_t> manifoldOffsets;
     std::vector<int32_t> hostSlotOf;

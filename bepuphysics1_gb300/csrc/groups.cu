@@ -133,8 +133,8 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
     std::stable_partition(order.begin(), order.end(), [&](int32_t gId) { return fits[gId] != 0; });
 
     // Slots: the sweep part, then the groups in launch order.
-    int32_t colours = 0;
-    for (int32_t i = 0; i < nm; i++) colours = std::max(colours, mc[i] + 1);
+    int32_t colours = 0;  // the sweep covers every colour of the list (joints sweep too)
+    for (int32_t u = 0; u < nj + nm; u++) colours = std::max(colours, colour[u] + 1);
     plan.slotOf.assign(nm, -1);
     plan.globalOffsets.assign(colours + 1, 0);
     int32_t slot = 0;

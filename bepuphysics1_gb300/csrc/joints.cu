@@ -1,0 +1,183 @@
+// Host side of the two-body joints: record checks, upload into the scene's
+// joint slots (colour order) and download of the accumulated impulses.
+//
+// The constants a joint's Update takes from System.Math in double -- the sine
+// and cosine of RevoluteLimit's plane angles (Matrix3x3.CreateFromAxisAngle,
+// Matrix3x3.cs:1392-1393, called at RevoluteLimit.cs:293-296) -- depend only on
+// the record, so they are computed here once, with the host's libm, in the
+// reference's expression: (float)Math.Sin((double)angle) and
+// 1 - (float)Math.Cos((double)angle).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/bepugpu.h"
+#include "bepugpu_internal.h"
+#include "joints_device.cuh"
+
+namespace bepugpu {
+
+namespace {
+
+constexpr float kHostTwoPi = 6.28318548f, kHostPiOver2 = 1.57079637f;  // MathHelper.cs:13-33
+
+// RevoluteLimit.GetDistanceFromMinimum (RevoluteLimit.cs:622-646)
+float DistanceFromMinimum(float minimumAngle, float angle) {
+    if (minimumAngle > 0) {
+        if (angle >= minimumAngle) return angle - minimumAngle;
+        if (angle > 0) return kHostTwoPi - minimumAngle + angle;
+        return kHostTwoPi - minimumAngle + angle;
+    }
+    if (angle < minimumAngle) return kHostTwoPi - minimumAngle + angle;
+    return angle - minimumAngle;
+}
+
+uint32_t ChildrenOf(int32_t type) {
+    switch (type) {
+        case BEPUGPU_JOINT_BALL_SOCKET: return kJChildBall;
+        case BEPUGPU_JOINT_REVOLUTE_ANGULAR: return kJChildAngular;
+        case BEPUGPU_JOINT_SWING_LIMIT:
+        case BEPUGPU_JOINT_REVOLUTE_LIMIT: return kJChildLimit;
+        case BEPUGPU_JOINT_REVOLUTE: return kJChildBall | kJChildAngular | kJChildLimit;
+        default: return 0;
+    }
+}
+
+float4 F4(const float* v, float w) { return make_float4(v[0], v[1], v[2], w); }
+
+}  // namespace
+
+bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint32_t nj, int32_t bodies) {
+    for (uint32_t u = 0; u < nj; u++) {
+        const bepugpu_joint& r = joints[u];
+        if (!ChildrenOf(r.type)) {
+            ctx->SetError("joint %u has unknown type %d", u, r.type);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (r.body_a < -1 || r.body_a >= bodies || r.body_b < -1 || r.body_b >= bodies) {
+            ctx->SetError("joint %u references a body outside [-1, %d)", u, bodies);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (r.body_a == r.body_b && r.body_a >= 0) {
+            ctx->SetError("joint %u connects body %d to itself", u, r.body_a);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        // SpringSettings.ComputeErrorReductionAndSoftness throws on this (SpringSettings.cs:104-105)
+        if (r.spring_stiffness == 0 && r.spring_damping == 0) {
+            ctx->SetError("joint %u: constraints cannot have both 0 stiffness and 0 damping", u);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+    }
+    return BEPUGPU_OK;
+}
+
+// Records in slot order into the input and impulse lanes (kJLA .. kJACC1),
+// heads and a cleared state.
+bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints, uint32_t nj) {
+    s->j.count = (int)nj;
+    if (!nj) return BEPUGPU_OK;
+    constexpr int kIn = kJACC1 + 1;
+    std::vector<float4> lanes((size_t)kIn * nj);
+    std::vector<int4> head(nj);
+    auto at = [&](int k, int slot) -> float4& { return lanes[(size_t)k * nj + slot]; };
+    for (uint32_t u = 0; u < nj; u++) {
+        const bepugpu_joint& r = joints[u];
+        const int slot = s->hostJointSlotOf[u];
+        const uint32_t present = ChildrenOf(r.type);
+        uint32_t childIsActive = present;
+        if (r.type == BEPUGPU_JOINT_REVOLUTE && !(r.flags & BEPUGPU_JOINT_LIMIT_ACTIVE))
+            childIsActive &= ~kJChildLimit;
+        uint32_t z = (uint32_t)r.type | (present << kJPresentShift) | (childIsActive << kJChildActiveShift) |
+                     ((r.flags & BEPUGPU_JOINT_ACTIVE) ? kJGroupIsActive : 0u);
+        head[slot] = make_int4(r.body_a, r.body_b, (int)z, (int)u);
+        // Joint.MaxCorrectiveVelocity setter (Joint.cs:23-36)
+        float maxCorr = std::max(0.f, r.max_corrective_velocity);
+        float maxCorrSq = maxCorr >= FLT_MAX ? FLT_MAX : maxCorr * maxCorr;
+        float minAngle = r.limit_min, maxAngle = r.limit_max;
+        float span = DistanceFromMinimum(minAngle, maxAngle);
+        float aMin = minAngle + kHostPiOver2, aMax = maxAngle - kHostPiOver2;
+        float sinMin = (float)std::sin((double)aMin), omcMin = 1 - (float)std::cos((double)aMin);
+        float sinMax = (float)std::sin((double)aMax), omcMax = 1 - (float)std::cos((double)aMax);
+        at(kJLA, slot) = F4(r.anchor_a, r.spring_stiffness);
+        at(kJLB, slot) = F4(r.anchor_b, r.spring_damping);
+        at(kJAXA, slot) = F4(r.axis_a, maxCorr);
+        at(kJAXB, slot) = F4(r.axis_b, r.margin);
+        at(kJC1, slot) = F4(r.constrained_1, r.bounciness);
+        at(kJC2, slot) = F4(r.constrained_2, r.bounce_velocity_threshold);
+        at(kJBP, slot) = F4(r.basis_primary, span);
+        at(kJBX, slot) = F4(r.basis_x, r.type == BEPUGPU_JOINT_SWING_LIMIT ? r.limit_min : 0.f);
+        at(kJTA, slot) = F4(r.test_axis, maxCorrSq);
+        at(kJTRIG, slot) = make_float4(sinMin, omcMin, sinMax, omcMax);
+        // impulses: ball xyz | angular x, angular y | limit x | limit y
+        float ball[3] = {0, 0, 0}, ang[2] = {0, 0}, lim[2] = {0, 0};
+        switch (r.type) {
+            case BEPUGPU_JOINT_BALL_SOCKET: std::memcpy(ball, r.impulse, 12); break;
+            case BEPUGPU_JOINT_REVOLUTE_ANGULAR: std::memcpy(ang, r.impulse, 8); break;
+            case BEPUGPU_JOINT_SWING_LIMIT: lim[0] = r.impulse[0]; break;
+            case BEPUGPU_JOINT_REVOLUTE_LIMIT: std::memcpy(lim, r.impulse, 8); break;
+            case BEPUGPU_JOINT_REVOLUTE:
+                std::memcpy(ball, r.impulse, 12);
+                std::memcpy(ang, r.impulse + 3, 8);
+                std::memcpy(lim, r.impulse + 5, 8);
+                break;
+        }
+        at(kJACC0, slot) = make_float4(ball[0], ball[1], ball[2], ang[0]);
+        at(kJACC1, slot) = make_float4(ang[1], lim[0], lim[1], 0.f);
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpy2DAsync(s->j.lanes, sizeof(float4) * s->j.capacity, lanes.data(), sizeof(float4) * nj,
+                               sizeof(float4) * nj, kIn, cudaMemcpyHostToDevice, s->stream)) ||
+        (e = cudaMemcpyAsync(s->j.head, head.data(), sizeof(int4) * nj, cudaMemcpyHostToDevice, s->stream)) ||
+        (e = cudaMemsetAsync(s->j.state, 0, sizeof(uint2) * nj, s->stream)) ||
+        (e = cudaMemcpyAsync(s->jointOffsetsDev, s->jointOffsets.data(), sizeof(int32_t) * s->jointOffsets.size(),
+                             cudaMemcpyHostToDevice, s->stream)) ||
+        (e = cudaStreamSynchronize(s->stream))) {
+        ctx->SetError("joint upload: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    return BEPUGPU_OK;
+}
+
+bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uint32_t nj) {
+    if (!nj) return BEPUGPU_OK;
+    s->hostJointAcc.resize(2 * (size_t)nj);
+    cudaError_t e;
+    if ((e = cudaMemcpy2DAsync(s->hostJointAcc.data(), sizeof(float4) * nj,
+                               s->j.lanes + (size_t)kJACC0 * s->j.capacity, sizeof(float4) * s->j.capacity,
+                               sizeof(float4) * nj, 2, cudaMemcpyDeviceToHost, s->stream)) ||
+        (e = cudaStreamSynchronize(s->stream))) {
+        ctx->SetError("joint download: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    for (uint32_t u = 0; u < nj; u++) {
+        bepugpu_joint& r = joints[u];
+        const int slot = s->hostJointSlotOf[u];
+        const float4 a0 = s->hostJointAcc[slot], a1 = s->hostJointAcc[(size_t)nj + slot];
+        switch (r.type) {
+            case BEPUGPU_JOINT_BALL_SOCKET:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                break;
+            case BEPUGPU_JOINT_REVOLUTE_ANGULAR:
+                r.impulse[0] = a0.w; r.impulse[1] = a1.x;
+                break;
+            case BEPUGPU_JOINT_SWING_LIMIT:
+                r.impulse[0] = a1.y;
+                break;
+            case BEPUGPU_JOINT_REVOLUTE_LIMIT:
+                r.impulse[0] = a1.y; r.impulse[1] = a1.z;
+                break;
+            case BEPUGPU_JOINT_REVOLUTE:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                r.impulse[3] = a0.w; r.impulse[4] = a1.x;
+                r.impulse[5] = a1.y; r.impulse[6] = a1.z;
+                break;
+        }
+    }
+    return BEPUGPU_OK;
+}
+
+}  // namespace bepugpu

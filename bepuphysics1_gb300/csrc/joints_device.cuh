@@ -1,0 +1,652 @@
+// Device side of the two-body joints: layout and per-joint math.
+//
+// A joint slot is one SolverUpdateable of the solver list.  Every joint is run
+// as a SolverGroup of up to three children -- ball socket, revolute angular,
+// limit (swing or revolute) -- in that order: RevoluteJoint is exactly that
+// group (SolverGroups/RevoluteJoint.cs:46-95, its motor inactive), and a
+// stand-alone joint is a group of one, which has the same activity sequence
+// (its own zero-impulse streak and the group's emptiness end it at the same
+// visit).  Arithmetic follows the reference classes operation for operation:
+//   BallSocketJoint       TwoEntity/Joints/BallSocketJoint.cs:210-372
+//   RevoluteAngularJoint  TwoEntity/Joints/RevoluteAngularJoint.cs:226-365
+//   SwingLimit            TwoEntity/JointLimits/SwingLimit.cs:211-347
+//   RevoluteLimit         TwoEntity/JointLimits/RevoluteLimit.cs:285-649
+//   SpringSettings        Constraints/SpringSettings.cs:95-110
+// A connection of -1 is TwoEntityConstraint.WorldEntity: kinematic, at the
+// origin, identity orientation, zero velocity.  Its zeros go through the same
+// arithmetic as a real body's so signed zeros come out as the reference's.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/bepugpu.h"
+#include "solver_device.cuh"
+
+namespace bepugpu {
+
+// Lanes of a joint slot: lanes[k * capacity + slot].
+enum JointLane : int {
+    // inputs (upload)
+    kJLA = 0,    // ball socket localAnchorA, w = spring stiffness
+    kJLB,        // ball socket localAnchorB, w = spring damping
+    kJAXA,       // angular / swing local axis A, w = max corrective velocity
+    kJAXB,       // angular / swing local axis B, w = margin
+    kJC1,        // angular localConstrainedAxis1 (A's frame), w = bounciness
+    kJC2,        // angular localConstrainedAxis2, w = bounce velocity threshold
+    kJBP,        // revolute limit basis local primary axis (A's frame), w = GetDistanceFromMinimum(max)
+    kJBX,        // revolute limit basis local x axis, w = swing minimum cosine
+    kJTA,        // revolute limit local test axis (B's frame), w = max corrective velocity squared
+    kJTRIG,      // sin(min + pi/2), 1 - cos(min + pi/2), sin(max - pi/2), 1 - cos(max - pi/2)
+    // accumulated impulses (in/out)
+    kJACC0,      // ball socket xyz, angular x
+    kJACC1,      // angular y, limit x (swing: its impulse), limit y
+    // prestep products
+    kJOA,        // ball worldOffsetA, w = ball softness
+    kJOB,        // ball worldOffsetB, w = angular softness
+    kJM0,        // ball mass M11 M12 M13 M21
+    kJM1,        // ball mass M22 M23 M31 M32
+    kJM2,        // ball mass M33, ball bias xyz
+    kJW1,        // angular worldConstrainedAxis1, w = angular bias x
+    kJW2,        // angular worldConstrainedAxis2, w = angular bias y
+    kJE,         // angular effective mass M11 M12 M21 M22
+    kJL0,        // limit jacobianMinA (swing: hinge axis), w = limit softness
+    kJL1,        // limit jacobianMaxA
+    kJL2,        // limit bias x, bias y, velocityToImpulse x, y
+    kJointLanes
+};
+
+// head.z: type (bits 0-7), children present (8-10), children IsActive (11-13),
+// joint / group IsActive (14).
+enum : uint32_t {
+    kJChildBall = 1u,
+    kJChildAngular = 2u,
+    kJChildLimit = 4u,
+    kJPresentShift = 8,
+    kJChildActiveShift = 11,
+    kJGroupIsActive = 1u << 14,
+};
+// State word x: kGroupActive (bit 0), child isActiveInSolver bits 1-3,
+// limit minIsActive / maxIsActive bits 4-5, kDynA / kDynB, iterations << 16.
+// Word y: 4-bit zero-impulse streaks of the three children.
+enum : uint32_t {
+    kJMinActive = 1u << 4,
+    kJMaxActive = 1u << 5,
+};
+
+struct JointSoA {
+    int4* head;     // body A, body B, type | flags, source record index
+    float4* lanes;  // [kJointLanes][capacity]
+    uint2* state;
+    int count;
+    int capacity;
+    __device__ __forceinline__ float4& L(int k, int s) const { return lanes[(size_t)k * capacity + s]; }
+};
+
+// ------------------------------------------------------------- joint math --
+struct JM3 {
+    float M11, M12, M13, M21, M22, M23, M31, M32, M33;
+};
+
+// Matrix3x3.CreateFromQuaternion (Matrix3x3.cs:1303-1328), as in ForceMath.
+__device__ __forceinline__ JM3 JRotation(float4 q) {
+    float qX2 = q.x + q.x, qY2 = q.y + q.y, qZ2 = q.z + q.z;
+    float XX = qX2 * q.x, YY = qY2 * q.y, ZZ = qZ2 * q.z;
+    float XY = qX2 * q.y, XZ = qX2 * q.z, XW = qX2 * q.w;
+    float YZ = qY2 * q.z, YW = qY2 * q.w, ZW = qZ2 * q.w;
+    JM3 r;
+    r.M11 = 1 - YY - ZZ; r.M21 = XY - ZW; r.M31 = XZ + YW;
+    r.M12 = XY + ZW; r.M22 = 1 - XX - ZZ; r.M32 = YZ - XW;
+    r.M13 = XZ - YW; r.M23 = YZ + XW; r.M33 = 1 - XX - YY;
+    return r;
+}
+// Matrix3x3.Transform (:1071-1082): row vector times matrix.
+__device__ __forceinline__ float3 JTransform(float3 v, const JM3& m) {
+    return make_float3(v.x * m.M11 + v.y * m.M21 + v.z * m.M31, v.x * m.M12 + v.y * m.M22 + v.z * m.M32,
+                       v.x * m.M13 + v.y * m.M23 + v.z * m.M33);
+}
+// Matrix3x3.Multiply (:766-790)
+__device__ __forceinline__ JM3 JMul(const JM3& a, const JM3& b) {
+    JM3 r;
+    r.M11 = a.M11 * b.M11 + a.M12 * b.M21 + a.M13 * b.M31;
+    r.M12 = a.M11 * b.M12 + a.M12 * b.M22 + a.M13 * b.M32;
+    r.M13 = a.M11 * b.M13 + a.M12 * b.M23 + a.M13 * b.M33;
+    r.M21 = a.M21 * b.M11 + a.M22 * b.M21 + a.M23 * b.M31;
+    r.M22 = a.M21 * b.M12 + a.M22 * b.M22 + a.M23 * b.M32;
+    r.M23 = a.M21 * b.M13 + a.M22 * b.M23 + a.M23 * b.M33;
+    r.M31 = a.M31 * b.M11 + a.M32 * b.M21 + a.M33 * b.M31;
+    r.M32 = a.M31 * b.M12 + a.M32 * b.M22 + a.M33 * b.M32;
+    r.M33 = a.M31 * b.M13 + a.M32 * b.M23 + a.M33 * b.M33;
+    return r;
+}
+__device__ __forceinline__ JM3 JSub(const JM3& a, const JM3& b) {
+    return {a.M11 - b.M11, a.M12 - b.M12, a.M13 - b.M13, a.M21 - b.M21, a.M22 - b.M22,
+            a.M23 - b.M23, a.M31 - b.M31, a.M32 - b.M32, a.M33 - b.M33};
+}
+// Matrix3x3.CreateCrossProduct (:378-389)
+__device__ __forceinline__ JM3 JCrossMatrix(float3 v) { return {0, -v.z, v.y, v.z, 0, -v.x, -v.y, v.x, 0}; }
+// Matrix3x3.CreateScale
+__device__ __forceinline__ JM3 JScale(float s) { return {s, 0, 0, 0, s, 0, 0, 0, s}; }
+// Matrix3x3.Invert (:505-534) with Determinant (:1231-1235)
+__device__ __forceinline__ JM3 JInvert(const JM3& m) {
+    float det = m.M11 * m.M22 * m.M33 + m.M12 * m.M23 * m.M31 + m.M13 * m.M21 * m.M32 -
+                m.M31 * m.M22 * m.M13 - m.M32 * m.M23 * m.M11 - m.M33 * m.M21 * m.M12;
+    float d = 1 / det;
+    JM3 r;
+    r.M11 = (m.M22 * m.M33 - m.M23 * m.M32) * d;
+    r.M12 = (m.M13 * m.M32 - m.M33 * m.M12) * d;
+    r.M13 = (m.M12 * m.M23 - m.M22 * m.M13) * d;
+    r.M21 = (m.M23 * m.M31 - m.M21 * m.M33) * d;
+    r.M22 = (m.M11 * m.M33 - m.M13 * m.M31) * d;
+    r.M23 = (m.M13 * m.M21 - m.M11 * m.M23) * d;
+    r.M31 = (m.M21 * m.M32 - m.M22 * m.M31) * d;
+    r.M32 = (m.M12 * m.M31 - m.M11 * m.M32) * d;
+    r.M33 = (m.M11 * m.M22 - m.M12 * m.M21) * d;
+    return r;
+}
+__device__ __forceinline__ float3 JCross(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float JDot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 JXYZ(float4 v) { return make_float3(v.x, v.y, v.z); }
+// Vector3.Normalize (Vector3.cs:81-87): the reciprocal square root in double.
+__device__ __forceinline__ float3 JNormalize(float3 v) {
+    float inverse = (float)(1.0 / sqrt((double)(v.x * v.x + v.y * v.y + v.z * v.z)));
+    return make_float3(v.x * inverse, v.y * inverse, v.z * inverse);
+}
+__device__ __forceinline__ JM3 JInertia(const BodyState& s) {
+    return {s.I11, s.I12, s.I13, s.I21, s.I22, s.I23, s.I31, s.I32, s.I33};
+}
+// (float)System.Math.Sqrt((double)x) equals the float square root (see SqrtOfFloat).
+// SpringSettings.ComputeErrorReductionAndSoftness (SpringSettings.cs:95-110)
+__device__ __forceinline__ void JSpring(float stiffness, float damping, float dt, float updateRate, float& erp,
+                                        float& softness) {
+    float multiplier = 1 / (dt * stiffness + damping);
+    erp = stiffness * multiplier;
+    softness = updateRate * multiplier;
+}
+// JointLimit.ComputeBounceVelocity (JointLimit.cs:60-66)
+__device__ __forceinline__ float JBounce(float impactVelocity, float threshold, float bounciness) {
+    float lowThreshold = threshold * 0.3f;
+    float velocityFraction = Clampf((impactVelocity - lowThreshold) / (threshold - lowThreshold + 1e-7f), 0, 1);
+    return velocityFraction * impactVelocity * bounciness;
+}
+
+// A joint connection: body state plus pose, or the world entity.
+struct JointBody {
+    BodyState s;
+    float3 pos;
+    JM3 R;
+    bool dynamic;
+};
+__device__ __forceinline__ void LoadJointBody(const BodySoA& b, int r, JointBody& o) {
+    if (r < 0) {
+        o.s.vx = o.s.vy = o.s.vz = 0.f; o.s.invMass = 0.f;
+        o.s.wx = o.s.wy = o.s.wz = 0.f;
+        o.s.I11 = o.s.I12 = o.s.I13 = o.s.I21 = o.s.I22 = o.s.I23 = o.s.I31 = o.s.I32 = o.s.I33 = 0.f;
+        o.pos = make_float3(0.f, 0.f, 0.f);
+        o.R = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        o.dynamic = false;
+        return;
+    }
+    LoadBody(b, r, o.s);
+    float4 p = b.pos[r];
+    o.pos = make_float3(p.x, p.y, p.z);
+    o.R = JRotation(b.quat[r]);
+    o.dynamic = p.w != 0.f;
+}
+// Velocity-only view for the warm start and the solve.
+__device__ __forceinline__ void LoadJointVelocity(const BodySoA& b, int r, BodyState& s) {
+    if (r < 0) {
+        s.vx = s.vy = s.vz = 0.f; s.invMass = 0.f;
+        s.wx = s.wy = s.wz = 0.f;
+        s.I11 = s.I12 = s.I13 = s.I21 = s.I22 = s.I23 = s.I31 = s.I32 = s.I33 = 0.f;
+        return;
+    }
+    LoadBody(b, r, s);
+}
+
+// ------------------------------------------------------------- prestep --
+// Solver.UnsafePrestep (Solver.cs:265-275) of one joint: UpdateSolverActivity,
+// then Update of every active child (SolverGroup.cs:94-100).
+__device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
+    const int4 h = j.head[s];
+    const uint32_t present = (h.z >> kJPresentShift) & 7u, childIsActive = (h.z >> kJChildActiveShift) & 7u;
+    const int type = h.z & 0xff;
+    JointBody A, B;
+    LoadJointBody(b, h.x, A);
+    LoadJointBody(b, h.y, B);
+    uint32_t st = (A.dynamic ? kDynA : 0u) | (B.dynamic ? kDynB : 0u);
+    if (!(h.z & kJGroupIsActive) || !(A.dynamic || B.dynamic)) {
+        j.state[s] = make_uint2(st, 0u);
+        return;
+    }
+    const float4 la = j.L(kJLA, s), lb = j.L(kJLB, s), axa = j.L(kJAXA, s), axb = j.L(kJAXB, s);
+    const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
+    const float maxCorrSq = j.L(kJTA, s).w;
+    float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
+    uint32_t active = present & childIsActive;
+    if (active & kJChildBall) {
+        // BallSocketJoint.Update (BallSocketJoint.cs:210-278)
+        float3 offA = JTransform(JXYZ(la), A.R), offB = JTransform(JXYZ(lb), B.R);
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        JM3 rA = JCrossMatrix(offA), rB = JCrossMatrix(offB), k;
+        if (A.dynamic && B.dynamic) {
+            JM3 lin = JScale(A.s.invMass + B.s.invMass);
+            JM3 angA = JMul(rA, JInertia(A.s)), angB = JMul(rB, JInertia(B.s));
+            angA = JMul(angA, rA);
+            angB = JMul(angB, rB);
+            k = JSub(lin, angA);
+            k = JSub(k, angB);
+        } else if (A.dynamic) {
+            JM3 lin = JScale(A.s.invMass);
+            JM3 angA = JMul(JMul(rA, JInertia(A.s)), rA);
+            k = JSub(lin, angA);
+        } else {
+            JM3 lin = JScale(B.s.invMass);
+            JM3 angB = JMul(JMul(rB, JInertia(B.s)), rB);
+            k = JSub(lin, angB);
+        }
+        k.M11 += softness;
+        k.M22 += softness;
+        k.M33 += softness;
+        JM3 mass = JInvert(k);
+        float ex = B.pos.x + offB.x, ey = B.pos.y + offB.y, ez = B.pos.z + offB.z;
+        ex = ex - A.pos.x; ey = ey - A.pos.y; ez = ez - A.pos.z;
+        ex = ex - offA.x; ey = ey - offA.y; ez = ez - offA.z;
+        float nerp = -erp;
+        float bx = ex * nerp, by = ey * nerp, bz = ez * nerp;
+        float length = bx * bx + by * by + bz * bz;
+        if (length > maxCorrSq) {
+            float multiplier = maxCorr / SqrtOfFloat(length);
+            bx *= multiplier; by *= multiplier; bz *= multiplier;
+        }
+        j.L(kJOA, s) = make_float4(offA.x, offA.y, offA.z, softness);
+        j.L(kJOB, s).x = offB.x;  // w of kJOB belongs to the angular child
+        j.L(kJOB, s).y = offB.y;
+        j.L(kJOB, s).z = offB.z;
+        j.L(kJM0, s) = make_float4(mass.M11, mass.M12, mass.M13, mass.M21);
+        j.L(kJM1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
+        j.L(kJM2, s) = make_float4(mass.M33, bx, by, bz);
+        st |= 1u << (kChildShift + 0);
+    }
+    if (active & kJChildAngular) {
+        // RevoluteAngularJoint.Update (RevoluteAngularJoint.cs:226-289)
+        float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
+        float3 c1 = JTransform(JXYZ(j.L(kJC1, s)), A.R), c2 = JTransform(JXYZ(j.L(kJC2, s)), A.R);
+        float3 e3 = JCross(wA, wB);
+        float errX = JDot(e3, c1), errY = JDot(e3, c2);
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        erp = -erp;
+        float bx = erp * errX, by = erp * errY;
+        float length = bx * bx + by * by;
+        if (length > maxCorrSq) {
+            float multiplier = maxCorr / SqrtOfFloat(length);
+            bx *= multiplier; by *= multiplier;
+        }
+        float3 a1, a2;
+        if (A.dynamic && B.dynamic) {
+            JM3 ia = JInertia(A.s), ib = JInertia(B.s);
+            JM3 sum = {ia.M11 + ib.M11, ia.M12 + ib.M12, ia.M13 + ib.M13, ia.M21 + ib.M21, ia.M22 + ib.M22,
+                       ia.M23 + ib.M23, ia.M31 + ib.M31, ia.M32 + ib.M32, ia.M33 + ib.M33};
+            a1 = JTransform(c1, sum);
+            a2 = JTransform(c2, sum);
+        } else if (A.dynamic) {
+            JM3 ia = JInertia(A.s);
+            a1 = JTransform(c1, ia);
+            a2 = JTransform(c2, ia);
+        } else {
+            JM3 ib = JInertia(B.s);
+            a1 = JTransform(c1, ib);
+            a2 = JTransform(c2, ib);
+        }
+        float m11 = JDot(a1, c1), m12 = JDot(a1, c2), m21 = JDot(a2, c1), m22 = JDot(a2, c2);
+        m11 += softness;
+        m22 += softness;
+        // Matrix2x2.Invert (Matrix2x2.cs:160-174), then Negate (:259-273)
+        float d = 1 / (m11 * m22 - m12 * m21);
+        float i11 = m22 * d, i12 = -m12 * d, i21 = -m21 * d, i22 = m11 * d;
+        j.L(kJOB, s).w = softness;
+        j.L(kJW1, s) = make_float4(c1.x, c1.y, c1.z, bx);
+        j.L(kJW2, s) = make_float4(c2.x, c2.y, c2.z, by);
+        j.L(kJE, s) = make_float4(-i11, -i12, -i21, -i22);
+        st |= 1u << (kChildShift + 1);
+    }
+    if (active & kJChildLimit) {
+        const float bounciness = j.L(kJC1, s).w, threshold = j.L(kJC2, s).w;
+        float erp, softness;
+        bool on = true;
+        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+            // SwingLimit.Update (SwingLimit.cs:249-331)
+            float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
+            float dot = JDot(wA, wB);
+            const float minimumCosine = j.L(kJBX, s).w;
+            if (dot > minimumCosine) {
+                on = false;
+                acc1.y = 0.f;
+            } else {
+                float3 hinge = JCross(wA, wB);
+                float lengthSquared = JDot(hinge, hinge);
+                if (lengthSquared < 1e-7f) {
+                    hinge = JCross(wA, make_float3(0.f, 1.f, 0.f));
+                    lengthSquared = JDot(hinge, hinge);
+                    if (lengthSquared < 1e-7f) hinge = JCross(wA, make_float3(1.f, 0.f, 0.f));
+                }
+                JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+                float error = minimumCosine - dot - margin;
+                error = error > 0.f ? error : 0.f;  // Math.Max(0, x)
+                float bias = Clampf(erp * error, -maxCorr, maxCorr);
+                if (bounciness > 0) {
+                    float rx = A.s.wx - B.s.wx, ry = A.s.wy - B.s.wy, rz = A.s.wz - B.s.wz;
+                    float relativeSpeed = rx * hinge.x + ry * hinge.y + rz * hinge.z;
+                    bias = Maxf(bias, JBounce(-relativeSpeed, threshold, bounciness));
+                }
+                float entryA = 0, entryB = 0;
+                if (A.dynamic) entryA = JDot(JTransform(hinge, JInertia(A.s)), hinge);
+                if (B.dynamic) entryB = JDot(JTransform(hinge, JInertia(B.s)), hinge);
+                float v2i = 1 / (softness + entryA + entryB);
+                j.L(kJL0, s) = make_float4(hinge.x, hinge.y, hinge.z, softness);
+                j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
+            }
+        } else {
+            // RevoluteLimit.Update (RevoluteLimit.cs:285-575)
+            float3 primary = JTransform(JXYZ(j.L(kJBP, s)), A.R), xAxis = JTransform(JXYZ(j.L(kJBX, s)), A.R);
+            float3 test = JTransform(JXYZ(j.L(kJTA, s)), B.R);
+            const float4 trig = j.L(kJTRIG, s);
+            // Matrix3x3.CreateFromAxisAngle (Matrix3x3.cs:1383-1406) with the
+            // double sine and cosine of the constant angles taken at upload.
+            float xx = primary.x * primary.x, yy = primary.y * primary.y, zz = primary.z * primary.z;
+            float xy = primary.x * primary.y, xz = primary.x * primary.z, yz = primary.y * primary.z;
+            auto rotate = [&](float sinAngle, float omc) {
+                JM3 r;
+                r.M11 = 1 + omc * (xx - 1);
+                r.M21 = -primary.z * sinAngle + omc * xy;
+                r.M31 = primary.y * sinAngle + omc * xz;
+                r.M12 = primary.z * sinAngle + omc * xy;
+                r.M22 = 1 + omc * (yy - 1);
+                r.M32 = -primary.x * sinAngle + omc * yz;
+                r.M13 = -primary.y * sinAngle + omc * xz;
+                r.M23 = primary.x * sinAngle + omc * yz;
+                r.M33 = 1 + omc * (zz - 1);
+                return JTransform(xAxis, r);
+            };
+            float3 minN = rotate(trig.x, trig.y), maxN = rotate(trig.z, trig.w);
+            float pMin = JDot(minN, test), pMax = JDot(maxN, test);
+            const float span = j.L(kJBP, s).w;
+            float errX = 0, errY = 0;
+            bool minOn = false, maxOn = false;
+            if (span >= 3.14159274f) {
+                if (pMax > 0 || pMin > 0) {
+                    on = false;
+                } else if (pMax > pMin) {
+                    errY = -pMax; acc1.y = 0.f; maxOn = true;
+                } else {
+                    errX = -pMin; acc1.z = 0.f; minOn = true;
+                }
+            } else {
+                if (pMax > 0 && pMin > 0) {
+                    on = false;
+                } else if (pMin <= 0 && pMax <= 0) {
+                    errX = -pMin; errY = -pMax; minOn = maxOn = true;
+                } else if (pMin <= 0) {
+                    errX = -pMin; acc1.z = 0.f; minOn = true;
+                } else {
+                    errY = -pMax; acc1.y = 0.f; maxOn = true;
+                }
+            }
+            if (!on) {
+                acc1.y = 0.f;
+                acc1.z = 0.f;
+            } else {
+                JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+                float4 l0 = j.L(kJL0, s), l1 = j.L(kJL1, s), l2 = j.L(kJL2, s);
+                float3 jMin = JXYZ(l0), jMax = JXYZ(l1);  // kept from earlier steps when a plane is off
+                if (minOn) {
+                    jMin = JCross(minN, test);
+                    if (JDot(jMin, jMin) < 1e-7f) jMin = primary;
+                    jMin = JNormalize(jMin);
+                }
+                if (maxOn) {
+                    jMax = JCross(maxN, test);
+                    if (JDot(jMax, jMax) < 1e-7f) jMax = primary;
+                    jMax = JNormalize(jMax);
+                }
+                float3 jMinB = make_float3(-jMin.x, -jMin.y, -jMin.z), jMaxB = make_float3(-jMax.x, -jMax.y, -jMax.z);
+                float biasX = l2.x, biasY = l2.y;
+                if (minOn) {
+                    biasX = Minf(Maxf(0, errX - margin) * erp, maxCorr);
+                    if (bounciness > 0) {
+                        float rel = A.s.wx * jMin.x + A.s.wy * jMin.y + A.s.wz * jMin.z;
+                        float dot = B.s.wx * jMinB.x + B.s.wy * jMinB.y + B.s.wz * jMinB.z;
+                        rel += dot;
+                        biasX = Maxf(biasX, JBounce(-rel, threshold, bounciness));
+                    }
+                }
+                if (maxOn) {
+                    biasY = Minf(Maxf(0, errY - margin) * erp, maxCorr);
+                    if (bounciness > 0) {
+                        float rel = A.s.wx * jMax.x + A.s.wy * jMax.y + A.s.wz * jMax.z;
+                        float dot = B.s.wx * jMaxB.x + B.s.wy * jMaxB.y + B.s.wz * jMaxB.z;
+                        rel += dot;
+                        biasY = Maxf(biasY, JBounce(-rel, threshold, bounciness));
+                    }
+                }
+                float minEA = 0, minEB = 0, maxEA = 0, maxEB = 0;
+                if (A.dynamic) {
+                    JM3 ia = JInertia(A.s);
+                    if (minOn) minEA = JDot(JTransform(jMin, ia), jMin);
+                    if (maxOn) maxEA = JDot(JTransform(jMax, ia), jMax);
+                }
+                if (B.dynamic) {
+                    JM3 ib = JInertia(B.s);
+                    if (minOn) minEB = JDot(JTransform(jMinB, ib), jMinB);
+                    if (maxOn) maxEB = JDot(JTransform(jMaxB, ib), jMaxB);
+                }
+                float v2iX = 1 / (softness + minEA + minEB);
+                float v2iY = 1 / (softness + maxEA + maxEB);
+                j.L(kJL0, s) = make_float4(jMin.x, jMin.y, jMin.z, softness);
+                j.L(kJL1, s) = make_float4(jMax.x, jMax.y, jMax.z, 0.f);
+                j.L(kJL2, s) = make_float4(biasX, biasY, v2iX, v2iY);
+                st |= (minOn ? kJMinActive : 0u) | (maxOn ? kJMaxActive : 0u);
+            }
+        }
+        if (on) st |= 1u << (kChildShift + 2);
+        j.L(kJACC1, s) = acc1;
+    }
+    if (st & (7u << kChildShift)) st |= kGroupActive;
+    j.state[s] = make_uint2(st, 0u);
+}
+
+// ---------------------------------------------------------- warm start --
+// ExclusiveUpdate of every active child in order.
+__device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint32_t st,
+                                          int type) {
+    const bool dynA = st & kDynA, dynB = st & kDynB;
+    const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
+    if (st & (1u << kChildShift)) {
+        // BallSocketJoint.ExclusiveUpdate (BallSocketJoint.cs:285-311)
+        const float3 offA = JXYZ(j.L(kJOA, s)), offB = JXYZ(j.L(kJOB, s));
+        const float3 acc = make_float3(acc0.x, acc0.y, acc0.z);
+        if (dynA) {
+            float3 lin = make_float3(-acc.x, -acc.y, -acc.z);
+            ApplyLinear(A, lin.x, lin.y, lin.z);
+            float3 t = JCross(offA, lin);
+            ApplyAngular(A, t.x, t.y, t.z);
+        }
+        if (dynB) {
+            ApplyLinear(B, acc.x, acc.y, acc.z);
+            float3 t = JCross(offB, acc);
+            ApplyAngular(B, t.x, t.y, t.z);
+        }
+    }
+    if (st & (2u << kChildShift)) {
+        // RevoluteAngularJoint.ExclusiveUpdate (RevoluteAngularJoint.cs:291-310)
+        const float3 c1 = JXYZ(j.L(kJW1, s)), c2 = JXYZ(j.L(kJW2, s));
+        float ix = c1.x * acc0.w + c2.x * acc1.x, iy = c1.y * acc0.w + c2.y * acc1.x,
+              iz = c1.z * acc0.w + c2.z * acc1.x;
+        if (dynA) ApplyAngular(A, ix, iy, iz);
+        if (dynB) ApplyAngular(B, -ix, -iy, -iz);
+    }
+    if (st & (4u << kChildShift)) {
+        const float4 l0 = j.L(kJL0, s);
+        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+            // SwingLimit.ExclusiveUpdate (SwingLimit.cs:333-347)
+            float ix = l0.x * acc1.y, iy = l0.y * acc1.y, iz = l0.z * acc1.y;
+            if (dynA) ApplyAngular(A, ix, iy, iz);
+            if (dynB) ApplyAngular(B, -ix, -iy, -iz);
+        } else {
+            // RevoluteLimit.ExclusiveUpdate (RevoluteLimit.cs:577-620)
+            const float4 l1 = j.L(kJL1, s);
+            const bool minOn = st & kJMinActive, maxOn = st & kJMaxActive;
+            if (dynA) {
+                float ix = 0.f, iy = 0.f, iz = 0.f;
+                if (minOn) { ix = l0.x * acc1.y; iy = l0.y * acc1.y; iz = l0.z * acc1.y; }
+                if (maxOn) { ix = ix + l1.x * acc1.z; iy = iy + l1.y * acc1.z; iz = iz + l1.z * acc1.z; }
+                ApplyAngular(A, ix, iy, iz);
+            }
+            if (dynB) {
+                float ix = 0.f, iy = 0.f, iz = 0.f;
+                if (minOn) { ix = -l0.x * acc1.y; iy = -l0.y * acc1.y; iz = -l0.z * acc1.y; }
+                if (maxOn) { ix = ix + -l1.x * acc1.z; iy = iy + -l1.y * acc1.z; iz = iz + -l1.z * acc1.z; }
+                ApplyAngular(B, ix, iy, iz);
+            }
+        }
+    }
+}
+
+// -------------------------------------------------------------- solve --
+// Solver.UnsafeSolveIteration (Solver.cs:285-314) on the joint, then
+// SolverGroup.SolveUpdateable (SolverGroup.cs:117-150) on each child.
+__device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint2& state,
+                                           int type, const StepParams& p) {
+    uint32_t st = state.x, zeros = state.y;
+    uint32_t iter = (st >> kIterShift) + 1;
+    st = (st & 0xffffu) | (iter << kIterShift);
+    if (!((int)iter <= p.iterationLimit && (int)iter <= p.maximumIterationCount)) {
+        state = make_uint2(st & ~kGroupActive, zeros);
+        return;
+    }
+    const bool dynA = st & kDynA, dynB = st & kDynB;
+    int activeConstraints = 0;
+    auto account = [&](int c, float r) {
+        uint32_t z = (zeros >> (4 * c)) & 0xfu;
+        if (r < p.minimumImpulse) {
+            z++;
+            if ((int)z > p.minimumIterationCount) st &= ~(1u << (kChildShift + c));
+            else activeConstraints++;
+        } else {
+            z = 0;
+            activeConstraints++;
+        }
+        zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
+    };
+    float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
+    if (st & (1u << kChildShift)) {
+        // BallSocketJoint.SolveIteration (BallSocketJoint.cs:318-372)
+        const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
+                     m2 = j.L(kJM2, s);
+        const float softness = oa.w;
+        float crx = A.wy * oa.z - A.wz * oa.y, cry = A.wz * oa.x - A.wx * oa.z, crz = A.wx * oa.y - A.wy * oa.x;
+        float ax = A.vx + crx, ay = A.vy + cry, az = A.vz + crz;
+        crx = B.wy * ob.z - B.wz * ob.y; cry = B.wz * ob.x - B.wx * ob.z; crz = B.wx * ob.y - B.wy * ob.x;
+        float bx = B.vx + crx, by = B.vy + cry, bz = B.vz + crz;
+        float lx = ax - bx + m2.y - softness * acc0.x;
+        float ly = ay - by + m2.z - softness * acc0.y;
+        float lz = az - bz + m2.w - softness * acc0.z;
+        // Matrix3x3.Transform by the mass matrix
+        float tx = lx * m0.x + ly * m0.w + lz * m1.z;
+        float ty = lx * m0.y + ly * m1.x + lz * m1.w;
+        float tz = lx * m0.z + ly * m1.y + lz * m2.x;
+        acc0.x = acc0.x + tx;
+        acc0.y = acc0.y + ty;
+        acc0.z = acc0.z + tz;
+        if (dynA) {
+            float nx = -tx, ny = -ty, nz = -tz;
+            ApplyLinear(A, nx, ny, nz);
+            ApplyAngular(A, oa.y * nz - oa.z * ny, oa.z * nx - oa.x * nz, oa.x * ny - oa.y * nx);
+        }
+        if (dynB) {
+            ApplyLinear(B, tx, ty, tz);
+            ApplyAngular(B, ob.y * tz - ob.z * ty, ob.z * tx - ob.x * tz, ob.x * ty - ob.y * tx);
+        }
+        account(0, fabsf(tx) + fabsf(ty) + fabsf(tz));
+    }
+    if (st & (2u << kChildShift)) {
+        // RevoluteAngularJoint.SolveIteration (RevoluteAngularJoint.cs:313-356)
+        const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s), e = j.L(kJE, s);
+        const float softness = j.L(kJOB, s).w;
+        float vx = A.wx - B.wx, vy = A.wy - B.wy, vz = A.wz - B.wz;
+        float lx = w1.x * vx + w1.y * vy + w1.z * vz;
+        float ly = w2.x * vx + w2.y * vy + w2.z * vz;
+        lx = lx + w1.w;
+        ly = ly + w2.w;
+        float sx = acc0.w * softness, sy = acc1.x * softness;
+        lx = lx + sx;
+        ly = ly + sy;
+        float tx = lx * e.x + ly * e.z;
+        float ty = lx * e.y + ly * e.w;
+        acc0.w = acc0.w + tx;
+        acc1.x = acc1.x + ty;
+        float ix = w1.x * tx + w2.x * ty, iy = w1.y * tx + w2.y * ty, iz = w1.z * tx + w2.z * ty;
+        if (dynA) ApplyAngular(A, ix, iy, iz);
+        if (dynB) ApplyAngular(B, -ix, -iy, -iz);
+        account(1, fabsf(tx) + fabsf(ty));
+    }
+    if (st & (4u << kChildShift)) {
+        const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
+        const float softness = l0.w;
+        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+            // SwingLimit.SolveIteration (SwingLimit.cs:211-243)
+            float rx = A.wx - B.wx, ry = A.wy - B.wy, rz = A.wz - B.wz;
+            float lambda = rx * l0.x + ry * l0.y + rz * l0.z;
+            lambda = -lambda + l2.x - softness * acc1.y;
+            lambda *= l2.z;
+            float previous = acc1.y;
+            acc1.y = Maxf(acc1.y + lambda, 0);
+            lambda = acc1.y - previous;
+            float ix = l0.x * lambda, iy = l0.y * lambda, iz = l0.z * lambda;
+            if (dynA) ApplyAngular(A, ix, iy, iz);
+            if (dynB) ApplyAngular(B, -ix, -iy, -iz);
+            account(2, fabsf(lambda));
+        } else {
+            // RevoluteLimit.SolveIteration (RevoluteLimit.cs:211-283)
+            const float4 l1 = j.L(kJL1, s);
+            float lambdaTotal = 0;
+            if (st & kJMinActive) {
+                float nx = -l0.x, ny = -l0.y, nz = -l0.z;
+                float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;
+                float velocityB = B.wx * nx + B.wy * ny + B.wz * nz;
+                float lambda = -(velocityA + velocityB) + l2.x - softness * acc1.y;
+                lambda *= l2.z;
+                float previous = acc1.y;
+                acc1.y = Maxf(acc1.y + lambda, 0);
+                lambda = acc1.y - previous;
+                if (dynA) ApplyAngular(A, l0.x * lambda, l0.y * lambda, l0.z * lambda);
+                if (dynB) ApplyAngular(B, nx * lambda, ny * lambda, nz * lambda);
+                lambdaTotal += fabsf(lambda);
+            }
+            if (st & kJMaxActive) {
+                float nx = -l1.x, ny = -l1.y, nz = -l1.z;
+                float velocityA = A.wx * l1.x + A.wy * l1.y + A.wz * l1.z;
+                float velocityB = B.wx * nx + B.wy * ny + B.wz * nz;
+                float lambda = -(velocityA + velocityB) + l2.y - softness * acc1.z;
+                lambda *= l2.w;
+                float previous = acc1.z;
+                acc1.z = Maxf(acc1.z + lambda, 0);
+                lambda = acc1.z - previous;
+                if (dynA) ApplyAngular(A, l1.x * lambda, l1.y * lambda, l1.z * lambda);
+                if (dynB) ApplyAngular(B, nx * lambda, ny * lambda, nz * lambda);
+                lambdaTotal += fabsf(lambda);
+            }
+            account(2, lambdaTotal);
+        }
+    }
+    if (activeConstraints <= 0) st &= ~kGroupActive;
+    j.L(kJACC0, s) = acc0;
+    j.L(kJACC1, s) = acc1;
+    state = make_uint2(st, zeros);
+}
+
+}  // namespace bepugpu

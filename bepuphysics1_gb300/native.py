@@ -43,8 +43,10 @@ MANIFOLD_DTYPE = np.dtype([
 JOINT_DTYPE = np.dtype([
     ("type", "<i4"), ("body_a", "<i4"), ("body_b", "<i4"), ("flags", "<u4"),
     ("anchor_a", "<f4", 3), ("anchor_b", "<f4", 3), ("axis_a", "<f4", 3), ("axis_b", "<f4", 3),
-    ("basis_a", "<f4", 3), ("basis_b", "<f4", 3), ("limit", "<f4", 4), ("spring", "<f4", 2),
-    ("impulse", "<f4", 8),
+    ("constrained_1", "<f4", 3), ("constrained_2", "<f4", 3), ("basis_primary", "<f4", 3), ("basis_x", "<f4", 3),
+    ("test_axis", "<f4", 3), ("limit_min", "<f4"), ("limit_max", "<f4"), ("margin", "<f4"), ("bounciness", "<f4"),
+    ("bounce_velocity_threshold", "<f4"), ("max_corrective_velocity", "<f4"), ("spring_stiffness", "<f4"),
+    ("spring_damping", "<f4"), ("impulse", "<f4", 8),
 ])
 
 PILE_PARAMS_DTYPE = np.dtype([

@@ -54,6 +54,26 @@ def make_tower(body_count: int, seed: int = 1, **overrides):
     return _collect(h)
 
 
+def make_chain(**overrides):
+    """Articulated capsule chains plus loose spheres and boxes (bepuscene_make_chain)."""
+    lib = N.load_scene_library()
+    p = np.zeros(1, N.CHAIN_PARAMS_DTYPE)
+    lib.bepuscene_default_chain(N.ptr(p))
+    for k, v in overrides.items():
+        p[k] = v
+    h = ctypes.c_void_p()
+    st = lib.bepuscene_make_chain(N.ptr(p), ctypes.byref(h))
+    N.raise_for(st, "bepuscene_make_chain")
+    return _collect(h)
+
+
+def chains_8k(seed: int = 3):
+    """The mixed contacts-and-joints workload: 8,192 chains of 16 capsules
+    (radius 0.1 m, length 0.4 m, 1 kg), 45 degree limits, 20,000 loose spheres
+    and boxes in a 200 x 50 x 200 m region."""
+    return make_chain(seed=seed)
+
+
 def pile_1k(seed: int = 1234):
     return make_pile(seed=seed)
 

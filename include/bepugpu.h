@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 1
+#define BEPUGPU_ABI_VERSION 2
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -119,9 +119,10 @@ typedef struct bepugpu_manifold {
     bepugpu_contact contacts[BEPUGPU_MAX_CONTACTS];
 } bepugpu_manifold;
 
-/* Two-body joints.  A joint is one SolverUpdateable of the solver list; a
- * REVOLUTE joint is the SolverGroup RevoluteJoint (RevoluteJoint.cs:46-95) with
- * its BallSocketJoint, RevoluteAngularJoint and RevoluteLimit children. */
+/* Two-body joints.  A joint record is one SolverUpdateable of the solver list;
+ * a REVOLUTE record is the SolverGroup RevoluteJoint (RevoluteJoint.cs:46-95)
+ * with its BallSocketJoint, RevoluteAngularJoint and RevoluteLimit children
+ * solved in that order (its RevoluteMotor is inactive and not carried). */
 typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_BALL_SOCKET = 1,      /* BallSocketJoint.cs:210-372 */
     BEPUGPU_JOINT_REVOLUTE_ANGULAR = 2, /* RevoluteAngularJoint.cs:226-365 */
@@ -133,34 +134,47 @@ typedef enum bepugpu_joint_type {
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
 #define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE: RevoluteJoint.Limit.IsActive */
 
-/* Joint record.  Field meaning per type:
- *  BALL_SOCKET:      anchor_a, anchor_b = local anchors (BallSocketJoint.LocalOffsetA/B);
- *                    impulse[0..2] = accumulated impulse.
- *  REVOLUTE_ANGULAR: axis_a = WorldFreeAxisA's local axis on A, axis_b = local free axis on B;
- *                    impulse[0..1].
- *  SWING_LIMIT:      axis_a, axis_b = local hinge axes; limit[0] = maximum swing angle (rad);
- *                    impulse[0].
- *  REVOLUTE_LIMIT:   axis_a = local free axis on A, basis_a = local measurement axis on A,
- *                    basis_b = local test axis on B, limit[0] = minimum angle, limit[1] =
- *                    maximum angle; impulse[0..1].
- *  REVOLUTE:         anchor_a/b, axis_a/b, basis_a/b and limit[0..1] as above;
- *                    impulse[0..2] ball socket, impulse[3..4] angular, impulse[5..6] limit.
- * spring[0..1] = SpringSettings stiffness and damping (600000, 90000);
- * limit[2] = margin (limits), limit[3] = maximum corrective velocity (float max = none). */
+/* Joint record: the state each reference object keeps between steps.  Body -1
+ * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic
+ * entity at the origin with identity orientation and zero velocity.
+ *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE)
+ *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
+ *                     SwingLimit.localAxisA/B (SWING_LIMIT)
+ *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame
+ *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame
+ *   test_axis         RevoluteLimit.localTestAxis, in B's frame
+ *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine
+ *   limit_max         RevoluteLimit.maximumAngle
+ *   margin, bounciness, bounce_velocity_threshold   JointLimit fields (0.005, 0, 1)
+ *   max_corrective_velocity   Joint.MaxCorrectiveVelocity (FLT_MAX = unlimited)
+ *   spring_stiffness/damping  SpringSettings (600000, 90000)
+ * The last three apply to every child of a REVOLUTE record.
+ *   impulse           accumulated impulses, in/out: BALL_SOCKET [0..2];
+ *                     REVOLUTE_ANGULAR [0..1]; SWING_LIMIT [0]; REVOLUTE_LIMIT [0..1];
+ *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */
-    int32_t body_a;                  /* -1 = TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17) */
+    int32_t body_a;
     int32_t body_b;
     uint32_t flags;                  /* BEPUGPU_JOINT_* */
     float anchor_a[3];
     float anchor_b[3];
     float axis_a[3];
     float axis_b[3];
-    float basis_a[3];
-    float basis_b[3];
-    float limit[4];
-    float spring[2];
-    float impulse[8];                /* accumulated impulses, in/out */
+    float constrained_1[3];
+    float constrained_2[3];
+    float basis_primary[3];
+    float basis_x[3];
+    float test_axis[3];
+    float limit_min;
+    float limit_max;
+    float margin;
+    float bounciness;
+    float bounce_velocity_threshold;
+    float max_corrective_velocity;
+    float spring_stiffness;
+    float spring_damping;
+    float impulse[8];
 } bepugpu_joint;
 
 typedef struct bepugpu_context bepugpu_context;

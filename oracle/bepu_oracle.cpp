@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -184,6 +185,7 @@ struct Space {
     std::atomic<long long> childSolves{0};
     bool countSolves = true;  // single-threaded runs only: a shared counter would serialize threads
     size_t jointCount = 0;
+    Entity world;  // TwoEntityConstraint.WorldEntity: kinematic, at the origin, identity orientation
 };
 
 // SolverGroup.cs:52-165
@@ -1009,6 +1011,8 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
         e.linearDamping = b.linear_damping;
         e.angularDamping = b.angular_damping;
     }
+    sp.world.index = -1;
+    sp.world.orientationMatrix = CreateFromQuaternion(sp.world.orientation);
     auto ent = [&](int idx) -> Entity* { return idx >= 0 && idx < nb ? &sp.entities[idx] : nullptr; };
     for (int j = 0; j < nj; j++) {
         SolverUpdateable* u = CreateJoint(sp, joints[j], ent(joints[j].body_a), ent(joints[j].body_b));

@@ -25,7 +25,7 @@ def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.abs(a - b).max(initial=0.0) / scale)
 
 
-def compare(gb, gm, ob, om):
+def compare(gb, gm, ob, om, gj=None, oj=None):
     """Relative errors of velocities, positions and impulses; the contact
     counts and indexing must agree exactly."""
     np.testing.assert_array_equal(gm["contact_count"], om["contact_count"])
@@ -42,6 +42,9 @@ def compare(gb, gm, ob, om):
     exact = (np.array_equal(gb["linear_velocity"], ob["linear_velocity"]) and
              np.array_equal(gb["angular_velocity"], ob["angular_velocity"]) and
              np.array_equal(gm["contacts"]["penetration_impulse"], om["contacts"]["penetration_impulse"]))
+    if gj is not None and len(gj):
+        errs["joint_impulse"] = rel_err(gj["impulse"], oj["impulse"])
+        exact = exact and np.array_equal(gj["impulse"], oj["impulse"])
     return errs, exact
 
 
@@ -50,6 +53,7 @@ class Pair:
     list permuted into the GPU's colour order (identity mapping)."""
 
     def __init__(self, ctx, bodies, manifolds, joints=None, settings=None, mode=N.MODE_GRAPH, group_policy=None):
+        self.joints = joints
         self.settings = default_settings() if settings is None else settings
         ctx.set_settings(self.settings)
         self.gpu = GpuSpace(ctx, bodies, manifolds, joints, group_policy=group_policy)
@@ -68,10 +72,11 @@ class Pair:
 
     def compare(self):
         gb = self.gpu.download_bodies()
-        gm, gj = self.gpu.download_constraints()
+        gj0 = None if self.joints is None else self.joints.copy()
+        gm, gj = self.gpu.download_constraints(joints=gj0)
         ob = self.oracle.get_bodies()
         om, oj = self.oracle.get_constraints()
-        return compare(gb, gm, ob, om)
+        return compare(gb, gm, ob, om, gj, oj)
 
     def close(self):
         self.gpu.close()

@@ -1,0 +1,159 @@
+"""Joints on the device against the oracle: BallSocketJoint, SwingLimit,
+RevoluteAngularJoint, RevoluteLimit and the RevoluteJoint group, alone and
+mixed with contact manifolds in one colouring (the chains workload)."""
+import numpy as np
+import pytest
+
+import oracle
+from bepuphysics1_gb300 import native as N
+from bepuphysics1_gb300 import scenes
+from bepuphysics1_gb300.solver import GpuSpace, default_settings
+
+from parity import DT, LONG_TOL, STEP_TOL, Pair
+
+pytestmark = pytest.mark.gpu
+
+
+def _settings(iterations=15):
+    s = default_settings()
+    s["iteration_limit"] = iterations
+    return s
+
+
+def _small_chains(seed=5, chains=48, links=16, loose=300):
+    return scenes.make_chain(chains=chains, links=links, loose_bodies=loose, seed=seed,
+                             region=np.array([30.0, 12.0, 30.0], np.float32))
+
+
+def test_chain_colouring_mixes_joints_and_manifolds(gpu_context):
+    b, m, j = _small_chains()
+    assert len(j) and len(m)
+    sp = GpuSpace(gpu_context, b, m, j)
+    col, order, k = sp.colouring()
+    col2, order2, k2 = oracle.colour(b, m, j)
+    assert k == k2
+    np.testing.assert_array_equal(col, col2)
+    np.testing.assert_array_equal(order, order2)
+    # joints and manifolds share colours: the sweep is mixed
+    jc, mc = set(col[:len(j)]), set(col[len(j):])
+    assert jc & mc
+    sp.close()
+
+
+def test_chains_every_step(gpu_context):
+    b, m, j = _small_chains()
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    for step in range(8):
+        p.step()
+        errs, exact = p.compare()
+        for k, v in errs.items():
+            assert v <= STEP_TOL, (step, k, v)
+        assert exact, (step, errs)
+    p.close()
+
+
+def test_chains_sixty_steps(gpu_context):
+    b, m, j = _small_chains(seed=6)
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    p.step(steps=60)
+    errs, exact = p.compare()
+    for k, v in errs.items():
+        assert v <= LONG_TOL, (k, v)
+    assert exact, errs
+    p.close()
+
+
+def test_chains_persistent_mode(gpu_context):
+    b, m, j = _small_chains(seed=7, chains=16)
+    p = Pair(gpu_context, b, m, j, settings=_settings(), mode=N.MODE_PERSISTENT)
+    p.step(steps=10)
+    errs, exact = p.compare()
+    assert exact, errs
+    p.close()
+
+
+@pytest.mark.parametrize("kind", ["ball", "swing", "angular", "revolute_limit", "revolute"])
+def test_each_joint_type_alone(gpu_context, kind):
+    """Every record type on its own, between two bodies and to the world, with
+    limits started inside and outside their range and stale impulses."""
+    b, m, j = _small_chains(seed=11, chains=24, loose=0)
+    t = j["type"]
+    if kind == "ball":
+        keep = t == N.JOINT_BALL_SOCKET
+    elif kind == "swing":
+        keep = (t == N.JOINT_SWING_LIMIT) | ((t == N.JOINT_BALL_SOCKET) & (j["body_a"] == -1))
+    elif kind == "angular":
+        keep = t == N.JOINT_REVOLUTE
+        j = j.copy()
+        j["type"][keep] = N.JOINT_REVOLUTE_ANGULAR
+    elif kind == "revolute_limit":
+        keep = t == N.JOINT_REVOLUTE
+        j = j.copy()
+        j["type"][keep] = N.JOINT_REVOLUTE_LIMIT
+        j["impulse"][keep, 0:2] = j["impulse"][keep, 5:7]
+    else:
+        keep = (t == N.JOINT_REVOLUTE) | (t == N.JOINT_BALL_SOCKET)
+    jj = j[keep].copy()
+    rng = np.random.default_rng(3)
+    jj["impulse"] = rng.uniform(0, 0.05, jj["impulse"].shape).astype(np.float32)
+    p = Pair(gpu_context, b, m, jj, settings=_settings())
+    for step in range(4):
+        p.step()
+        errs, exact = p.compare()
+        assert exact, (kind, step, errs)
+    p.close()
+
+
+def test_inactive_joints_and_world_anchors(gpu_context):
+    """IsActive off on some joints and on revolute limits; both connections
+    kinematic on others: they never enter the solver."""
+    b, m, j = _small_chains(seed=12, chains=12, loose=40)
+    j = j.copy()
+    j["flags"][::5] &= ~np.uint32(N.JOINT_ACTIVE)
+    rev = np.flatnonzero(j["type"] == N.JOINT_REVOLUTE)
+    j["flags"][rev[::2]] &= ~np.uint32(N.JOINT_LIMIT_ACTIVE)
+    b = b.copy()
+    b["is_dynamic"][len(b) - 3:] = 0  # the last chain's tail becomes kinematic
+    b["inverse_mass"][len(b) - 3:] = 0
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    p.step(steps=6)
+    errs, exact = p.compare()
+    assert exact, errs
+    p.close()
+
+
+def test_joint_records_roundtrip_and_checks(gpu_context):
+    b, m, j = _small_chains(seed=13, chains=4, loose=0)
+    j = j.copy()
+    j["impulse"] = np.random.default_rng(1).normal(size=j["impulse"].shape).astype(np.float32)
+    sp = GpuSpace(gpu_context, b, m, j)
+    _, back = sp.download_constraints(joints=j.copy())
+    used = {N.JOINT_BALL_SOCKET: 3, N.JOINT_SWING_LIMIT: 1, N.JOINT_REVOLUTE: 7}
+    for t, n in used.items():
+        sel = j["type"] == t
+        np.testing.assert_array_equal(back["impulse"][sel, :n], j["impulse"][sel, :n])
+    bad = j.copy()
+    bad["type"][0] = 42
+    with pytest.raises(N.BepuError):
+        sp.upload_constraints(m, bad)
+    bad = j.copy()
+    bad["spring_stiffness"][1] = 0
+    bad["spring_damping"][1] = 0
+    with pytest.raises(N.BepuError):
+        sp.upload_constraints(m, bad)
+    bad = j.copy()
+    bad["body_b"][2] = len(b)
+    with pytest.raises(N.BepuError):
+        sp.upload_constraints(m, bad)
+    sp.close()
+
+
+def test_chains_full_size_two_steps(gpu_context):
+    """The full mixed workload (8,192 chains of 16 capsules, 20,000 loose
+    bodies, 15 iterations) against the oracle for two steps."""
+    b, m, j = scenes.chains_8k()
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    p.step(steps=2)
+    errs, exact = p.compare()
+    assert exact, errs
+    p.close()

@@ -1,0 +1,151 @@
+"""Known-answer tests pinning the oracle's joint restatements.
+
+The reference ships no solver golden vectors, so each joint is pinned by a
+hand-derived closed form of one prestep and one solve iteration from rest
+(no gravity, no damping, no warm start), evaluated here in float64:
+  BallSocketJoint.Update/SolveIteration   BallSocketJoint.cs:210-278, 318-372
+  SwingLimit.Update/SolveIteration        SwingLimit.cs:211-331
+  RevoluteLimit.Update                    RevoluteLimit.cs:285-575
+and the switches the reference makes between active and inactive limits.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from bepuphysics1_gb300 import native as N
+from bepuphysics1_gb300.solver import default_settings
+
+DT = np.float32(1 / 60)
+K, D = 600000.0, 90000.0  # SpringSettings defaults
+
+
+def _settings(iterations=1):
+    s = default_settings()
+    s["gravity"] = (0, 0, 0)
+    s["iteration_limit"] = iterations
+    return s
+
+
+def _body(pos, inv_mass=1.0, inv_inertia=(2.0, 3.0, 4.0), quat=(0, 0, 0, 1)):
+    b = np.zeros(1, N.BODY_DTYPE)
+    b["position"] = pos
+    b["orientation"] = quat
+    b["inverse_mass"] = inv_mass
+    b["local_inverse_inertia"] = np.diag(inv_inertia).reshape(9)
+    b["is_dynamic"] = 1
+    return b
+
+
+def _joint(jtype, a, b):
+    j = np.zeros(1, N.JOINT_DTYPE)
+    j["type"], j["body_a"], j["body_b"], j["flags"] = jtype, a, b, N.JOINT_ACTIVE
+    j["margin"], j["bounce_velocity_threshold"] = 0.005, 1.0
+    j["max_corrective_velocity"] = np.finfo(np.float32).max
+    j["spring_stiffness"], j["spring_damping"] = K, D
+    return j
+
+
+def _spring(dt):
+    m = 1 / (dt * K + D)
+    return K * m, (1 / dt) * m  # error reduction, softness
+
+
+def _cross_matrix(v):
+    return np.array([[0, -v[2], v[1]], [v[2], 0, -v[0]], [-v[1], v[0], 0]])
+
+
+def _step(bodies, joints):
+    o = oracle.OracleSpace(_settings(), bodies, np.zeros(0, N.MANIFOLD_DTYPE), joints)
+    o.set_order_mode(oracle.ORDER_IDENTITY)
+    o.step(DT, N.STEP_SOLVE, 1)
+    return o.get_bodies(), o.get_constraints()[1]
+
+
+def _rot_z(phi):
+    return (0.0, 0.0, np.sin(phi / 2), np.cos(phi / 2))
+
+
+def test_ball_socket_to_world_closed_form():
+    # body B at (0, -1, 0) hangs from the world anchor at the origin by a local
+    # anchor 1.1 above its centre: position error (0, 0.1, 0)
+    b = _body((0, -1, 0))
+    j = _joint(N.JOINT_BALL_SOCKET, -1, 0)
+    j["anchor_a"] = (0, 0, 0)
+    j["anchor_b"] = (0, 1.1, 0)
+    ob, oj = _step(b, j)
+    dt = float(DT)
+    erp, soft = _spring(dt)
+    r = np.array([0, 1.1, 0])
+    inv_i = np.diag([2.0, 3.0, 4.0])
+    rx = _cross_matrix(r)
+    k = np.eye(3) * 1.0 - rx @ inv_i @ rx + soft * np.eye(3)
+    # Matrix3x3 is row-vector: lambda = v * M with M = K^-1 (K is symmetric here)
+    err = np.array([0, -1, 0]) + r
+    bias = -erp * err
+    lam = bias @ np.linalg.inv(k)
+    v = lam * 1.0
+    w = np.cross(r, lam) @ inv_i
+    np.testing.assert_allclose(oj["impulse"][0, :3], lam, rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(ob["linear_velocity"][0], v, rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(ob["angular_velocity"][0], w, rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("phi_deg,active", [(30.0, False), (60.0, True)])
+def test_swing_limit_switch(phi_deg, active):
+    phi = np.radians(phi_deg)
+    b = _body((0, 0, 0), quat=_rot_z(phi))
+    j = _joint(N.JOINT_SWING_LIMIT, -1, 0)
+    j["axis_a"] = (0, 1, 0)
+    j["axis_b"] = (0, 1, 0)
+    j["limit_min"] = np.float32(np.cos(np.radians(45.0)))
+    j["impulse"][0, 0] = 0.25  # a stale impulse: zeroed when the limit is not reached (SwingLimit.cs:259-266)
+    ob, oj = _step(b, j)
+    if not active:
+        assert oj["impulse"][0, 0] == 0.0
+        assert np.all(ob["angular_velocity"][0] == 0.0)
+        return
+    dt = float(DT)
+    erp, soft = _spring(dt)
+    axis_a = np.array([0, 1.0, 0])
+    axis_b = np.array([-np.sin(phi), np.cos(phi), 0])
+    hinge = np.cross(axis_a, axis_b)
+    # the body inertia in world: R^T L R for a rotation about z
+    c, s = np.cos(phi), np.sin(phi)
+    rot = np.array([[c, s, 0], [-s, c, 0], [0, 0, 1]])  # CreateFromQuaternion, row-vector convention
+    inv_i = rot.T @ np.diag([2.0, 3.0, 4.0]) @ rot
+    error = max(0.0, np.cos(np.radians(45.0)) - np.dot(axis_a, axis_b) - 0.005)
+    bias = erp * error
+    v2i = 1 / (soft + hinge @ inv_i @ hinge)
+    # warm start applies the stale 0.25 first; one solve from that state
+    w_warm = -(hinge * 0.25) @ inv_i
+    lam = (-(np.zeros(3) - w_warm) @ hinge + bias - soft * 0.25) * v2i
+    acc = max(0.25 + lam, 0.0)
+    w = w_warm - (hinge * (acc - 0.25)) @ inv_i
+    np.testing.assert_allclose(oj["impulse"][0, 0], acc, rtol=1e-5)
+    np.testing.assert_allclose(ob["angular_velocity"][0], w, rtol=1e-4, atol=1e-7)
+
+
+@pytest.mark.parametrize("phi_deg,active", [(20.0, False), (-20.0, False), (60.0, True), (-60.0, True)])
+def test_revolute_limit_planes(phi_deg, active):
+    # free axis z; A = world with x axis (1,0,0); B rotated about z by phi with
+    # local test axis x: the test axis makes angle phi with the basis x axis
+    phi = np.radians(phi_deg)
+    b = _body((0, 0, 0), quat=_rot_z(phi))
+    j = _joint(N.JOINT_REVOLUTE_LIMIT, -1, 0)
+    j["basis_primary"] = (0, 0, 1)
+    j["basis_x"] = (1, 0, 0)
+    j["test_axis"] = (1, 0, 0)
+    j["limit_min"] = np.float32(-np.pi / 4)
+    j["limit_max"] = np.float32(np.pi / 4)
+    j["impulse"][0, :2] = (0.5, 0.5)
+    ob, oj = _step(b, j)
+    imp = oj["impulse"][0, :2]
+    if not active:
+        assert np.all(imp == 0.0)
+        assert np.all(ob["angular_velocity"][0] == 0.0)
+        return
+    # exactly one plane is violated; the other impulse is zeroed (RevoluteLimit.cs:365-395)
+    assert (imp[0] == 0.0) != (imp[1] == 0.0)
+    # the correction turns B back toward the allowed range about the free axis
+    wz = ob["angular_velocity"][0][2]
+    assert np.sign(wz) == -np.sign(phi)
