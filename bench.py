@@ -68,6 +68,8 @@ def parse_args():
     ap.add_argument("--tune-seconds", type=float, default=45.0, help="autotuner time limit")
     ap.add_argument("--tune-out", default=None, help="write the autotuner's trials to this JSON file")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
+    ap.add_argument("--chain-cpu-seconds", type=float, default=8.0)
     return ap.parse_args()
 
 
@@ -320,6 +322,82 @@ def batch_section(args, local, rank, world, pg):
     return out
 
 
+CHAIN_WORKLOAD = "chains_8k"
+CHAIN_ITERATIONS = 15
+
+
+def chain_section(args, local, rank, world, pg):
+    """Mixed joints and contacts: 8,192 chains of 16 capsules joined alternately
+    by BallSocketJoint + SwingLimit and RevoluteJoint (limit active, +-45
+    degrees), plus 20,000 loose spheres and boxes, 15 iterations.  Device time
+    per step with L2 flushed between steps; the unit of work is one solver
+    visit of one updateable (joint or manifold) per iteration."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import Context, GpuSpace, default_settings
+    settings = default_settings()
+    settings["iteration_limit"] = CHAIN_ITERATIONS
+    bodies, manifolds, joints = scenes.chains_8k()
+    ctx = Context(local, settings)
+    sp = GpuSpace(ctx, bodies, manifolds, joints)
+    for _ in range(max(args.warmup, 3)):
+        sp.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    step_ms, solve_ms = [], []
+    if pg:
+        pg.barrier()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        sp.step(DT, N.STEP_ALL)
+        step_ms.append(sp.last_step_ms())
+        solve_ms.append(float(sp.last_step_phase_ms()[3]))
+    total_ms = float(sum(step_ms))
+    if pg:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_upd = len(joints) + len(manifolds)
+    contacts = scenes.contact_count(manifolds)
+    colours = sp.colouring()[2]
+    out = {
+        "metric": "updateable-iters/s", "workload": CHAIN_WORKLOAD,
+        "value": world * n_upd * CHAIN_ITERATIONS * args.steps / (total_ms / 1000.0), "unit": "updateable-iters/s",
+        "steps_per_s": world * args.steps / (total_ms / 1000.0), "ms_per_step": total_ms / args.steps,
+        "solve_ms_per_step": statistics.mean(solve_ms), "gpu_launches_per_step": int(sp.last_step_launches()),
+        "config": {"bodies": int(len(bodies)), "joints": int(len(joints)), "manifolds": int(len(manifolds)),
+                   "contacts": int(contacts), "iterations": CHAIN_ITERATIONS, "colours": int(colours),
+                   "joint_records": {name: int((joints["type"] == t).sum()) for name, t in
+                                     (("ball_socket", N.JOINT_BALL_SOCKET), ("swing_limit", N.JOINT_SWING_LIMIT),
+                                      ("revolute", N.JOINT_REVOLUTE))},
+                   "l2": "flushed between timed steps (512 MiB write)"},
+        "parity": "bit-exact vs the colour-ordered oracle (tests/test_gpu_joints.py)",
+    }
+    sp.close()
+    ctx.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        o = oracle.OracleSpace(settings, bodies, manifolds, joints)
+        o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+        steps, t0 = 0, time.perf_counter()
+        while True:
+            o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+            steps += 1
+            if time.perf_counter() - t0 >= args.chain_cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        o.close()
+        out["cpu_baseline"] = {"value": n_upd * CHAIN_ITERATIONS * steps / el, "unit": "updateable-iters/s",
+                               "steps_per_s": steps / el, "cores": threads, "kind": "port",
+                               "sample": f"{steps} full steps after 1 warm-up step (oracle port of "
+                                         f"Solver.UpdateMultithreaded, {threads} threads, {el:.1f} s)"}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -488,6 +566,10 @@ def main():
     if not args.no_batch:
         space.close()
         batch = batch_section(args, local, rank, world, pg)
+    chains = None
+    if not args.no_chains:
+        space.close()
+        chains = chain_section(args, local, rank, world, pg)
 
     if rank == 0:
         line = {
@@ -509,6 +591,7 @@ def main():
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "batch": batch,
+            "chains": chains,
         }
         print(json.dumps(line), flush=True)
     space.close()

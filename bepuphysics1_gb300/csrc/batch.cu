@@ -27,12 +27,6 @@
 
 namespace bepugpu {
 
-struct SceneView {
-    ManifoldSoA m;
-    BodySoA b;
-    GroupTables t;
-};
-
 template <bool kShared>
 __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
                                uint32_t flags, int Bc, int Lc) {
@@ -109,19 +103,36 @@ cudaError_t Ensure(T*& p, size_t& cap, size_t n) {
 template <bool kShared>
 cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags, int threads) {
     if (c.work.empty()) return cudaSuccess;
-    size_t smemBytes = GroupSmemBytes(kShared, c.Bc, c.Lc);
-    if (smemBytes > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_batch_groups<kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smemBytes);
-        if (e != cudaSuccess) return e;
-    }
-    k_batch_groups<kShared><<<(unsigned)c.work.size(), ThreadsFor(c.members, threads), smemBytes, bt.stream>>>(
-        bt.viewsDev, c.dev, p, flags, c.Bc, c.Lc);
     bt.launches++;
-    return cudaGetLastError();
+    return LaunchBatchedGroups(kShared, bt.viewsDev, c.dev, (int)c.work.size(), p, flags, c.Bc, c.Lc, c.members,
+                               threads, bt.stream);
 }
 
 }  // namespace
+
+cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
+                                uint32_t flags, int Bc, int Lc, int members, int threads, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    size_t smemBytes = GroupSmemBytes(shared, Bc, Lc);
+    auto kernel = shared ? k_batch_groups<true> : k_batch_groups<false>;
+    if (smemBytes > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+        if (e != cudaSuccess) return e;
+    }
+    kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc);
+    return cudaGetLastError();
+}
+
+SceneView MakeView(const Scene& s) {
+    SceneView v;
+    v.m = s.m;
+    v.b = s.b;
+    v.t.groups = s.groupDescDev;
+    v.t.bodies = s.groupBodiesDev;
+    v.t.refs = s.groupRefsDev;
+    v.t.colourOffsets = s.groupColourOffsetsDev;
+    return v;
+}
 
 bool Scene::BatchReady() const {
     return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && jointCount == 0 && sweepDynamicCount == 0 &&
@@ -163,6 +174,10 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             return BEPUGPU_NOT_FOUND;
         }
         Scene* s = it->second.get();
+        if (s->server) {
+            ctx->SetError("batch: scene %d is served; release it first", scenes[i]);
+            return BEPUGPU_INVALID_OPERATION;
+        }
         uint32_t k = stepsEach ? stepsEach[i] : steps;
         if (k > 65535) {
             ctx->SetError("batch: at most 65535 steps per call");
@@ -208,15 +223,8 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             Scene* s = list[i];
             if (!s->BatchReady() || stepCount[i] == 0) continue;
             const GroupPlan& g = s->groupPlan;
-            SceneView v;
-            v.m = s->m;
-            v.b = s->b;
-            v.t.groups = s->groupDescDev;
-            v.t.bodies = s->groupBodiesDev;
-            v.t.refs = s->groupRefsDev;
-            v.t.colourOffsets = s->groupColourOffsetsDev;
             const int vi = (int)views.size();
-            views.push_back(v);
+            views.push_back(MakeView(*s));
             for (int k = g.shared.begin; k < g.shared.end; k++)
                 bt.shared.work.push_back(make_int4(vi, k, (int)stepCount[i], 0));
             for (int k = g.global.begin; k < g.global.end; k++)

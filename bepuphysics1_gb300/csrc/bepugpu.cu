@@ -422,6 +422,7 @@ static size_t Align(size_t x) { return (x + 255) & ~(size_t)255; }
 Scene::~Scene() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (arena) cudaFree(arena);
+    if (spillHost) cudaFreeHost(spillHost);
     if (staging) cudaFree(staging);
     if (counter) cudaFree(counter);
     if (evStart) cudaEventDestroy(evStart);
@@ -490,19 +491,20 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     size_t B = nb ? nb : 1, M = nm ? nm : 1, J = nj ? nj : 1;
     size_t bytes = 0;
     auto take = [&](size_t n) { size_t o = bytes; bytes += Align(n); return o; };
-    size_t oPos = take(16 * B), oQuat = take(16 * B), oVlin = take(16 * B), oVang = take(16 * B),
-           oInv0 = take(16 * B), oInv1 = take(16 * B), oLoc0 = take(16 * B), oLoc1 = take(16 * B),
-           oDamp = take(16 * B), oM33 = take(4 * B);
-    size_t oHead = take(16 * M), oCpos = take(64 * M), oCnrm = take(64 * M), oOffA = take(64 * M),
-           oOffB = take(64 * M), oMat = take(16 * M), oPen = take(16 * M), oFric = take(16 * M),
-           oAxis = take(16 * M), oPj0 = take(64 * M), oPj1 = take(64 * M), oPj2 = take(64 * M),
-           oS0 = take(16 * M), oS1 = take(16 * M), oS3 = take(16 * M), oS4 = take(16 * M), oS5 = take(16 * M),
-           oS6 = take(16 * M), oS7 = take(16 * M), oLev = take(16 * M), oState = take(8 * M),
-           oSlot = take(4 * M), oOffs = take(4 * (M + J + 2));
-    size_t oJHead = take(16 * J), oJLanes = take(16 * (size_t)kJointLanes * J), oJState = take(8 * J),
-           oJOffs = take(4 * (M + J + 2));
-    size_t oGroups = take(sizeof(GroupDesc) * M), oGroupBodies = take(4 * B), oGroupRefs = take(8 * M),
-           oGroupOffsets = take(4 * (2 * M + 2)), oSweepBodies = take(4 * B);
+    ArenaLayout& L = layout;
+    L.pos = take(16 * B); L.quat = take(16 * B); L.vlin = take(16 * B); L.vang = take(16 * B);
+    L.inv0 = take(16 * B); L.inv1 = take(16 * B); L.loc0 = take(16 * B); L.loc1 = take(16 * B);
+    L.damp = take(16 * B); L.m33 = take(4 * B);
+    L.head = take(16 * M); L.cpos = take(64 * M); L.cnrm = take(64 * M); L.offA = take(64 * M);
+    L.offB = take(64 * M); L.mat = take(16 * M); L.pen = take(16 * M); L.fric = take(16 * M);
+    L.axis = take(16 * M); L.pj0 = take(64 * M); L.pj1 = take(64 * M); L.pj2 = take(64 * M);
+    L.s0 = take(16 * M); L.s1 = take(16 * M); L.s3 = take(16 * M); L.s4 = take(16 * M); L.s5 = take(16 * M);
+    L.s6 = take(16 * M); L.s7 = take(16 * M); L.lev = take(16 * M); L.state = take(8 * M);
+    L.slot = take(4 * M); L.offs = take(4 * (M + J + 2));
+    L.jhead = take(16 * J); L.jlanes = take(16 * (size_t)kJointLanes * J); L.jstate = take(8 * J);
+    L.joffs = take(4 * (M + J + 2));
+    L.groups = take(sizeof(GroupDesc) * M); L.groupBodies = take(4 * B); L.groupRefs = take(8 * M);
+    L.groupOffsets = take(4 * (2 * M + 2)); L.sweepBodies = take(4 * B);
     arenaBytes = bytes;
     cudaError_t e = cudaMalloc(&arena, bytes);
     if (e != cudaSuccess) {
@@ -510,34 +512,12 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
         ctx->SetError("scene arena of %zu bytes: %s", bytes, cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
     }
-    char* base = (char*)arena;
-    b.pos = (float4*)(base + oPos); b.quat = (float4*)(base + oQuat); b.vlin = (float4*)(base + oVlin);
-    b.vang = (float4*)(base + oVang); b.inv0 = (float4*)(base + oInv0); b.inv1 = (float4*)(base + oInv1);
-    b.loc0 = (float4*)(base + oLoc0); b.loc1 = (float4*)(base + oLoc1); b.damp = (float4*)(base + oDamp);
-    localM33 = (float*)(base + oM33);
     b.count = 0;
-    m.head = (int4*)(base + oHead); m.cpos = (float4*)(base + oCpos); m.cnrm = (float4*)(base + oCnrm);
-    m.offA = (float4*)(base + oOffA); m.offB = (float4*)(base + oOffB); m.mat = (float4*)(base + oMat);
-    m.penacc = (float4*)(base + oPen); m.fricacc = (float4*)(base + oFric); m.saxis = (float4*)(base + oAxis);
-    m.pj0 = (float4*)(base + oPj0); m.pj1 = (float4*)(base + oPj1); m.pj2 = (float4*)(base + oPj2);
-    m.s0 = (float4*)(base + oS0); m.s1 = (float4*)(base + oS1); m.s3 = (float4*)(base + oS3);
-    m.s4 = (float4*)(base + oS4); m.s5 = (float4*)(base + oS5); m.s6 = (float4*)(base + oS6);
-    m.s7 = (float4*)(base + oS7); m.lever = (float4*)(base + oLev); m.state = (uint2*)(base + oState);
     m.count = 0;
     m.capacity = (int)M;
-    slotOf = (int32_t*)(base + oSlot);
-    colourOffsetsDev = (int32_t*)(base + oOffs);
-    groupDescDev = (GroupDesc*)(base + oGroups);
-    groupBodiesDev = (int32_t*)(base + oGroupBodies);
-    groupRefsDev = (int2*)(base + oGroupRefs);
-    groupColourOffsetsDev = (int32_t*)(base + oGroupOffsets);
-    sweepBodiesDev = (int32_t*)(base + oSweepBodies);
-    j.head = (int4*)(base + oJHead);
-    j.lanes = (float4*)(base + oJLanes);
-    j.state = (uint2*)(base + oJState);
     j.count = 0;
     j.capacity = (int)J;
-    jointOffsetsDev = (int32_t*)(base + oJOffs);
+    Rebase();
     CK(cudaMemset(arena, 0, bytes));
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
     stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
@@ -549,6 +529,76 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     CK(cudaEventCreate(&evStop));
     for (auto& e : evPhase) CK(cudaEventCreate(&e));
     for (auto& e : evGroup) CK(cudaEventCreate(&e));
+    return BEPUGPU_OK;
+}
+
+// Every device pointer of the scene from the arena base and the layout.
+void Scene::Rebase() {
+    char* base = (char*)arena;
+    const ArenaLayout& L = layout;
+    b.pos = (float4*)(base + L.pos); b.quat = (float4*)(base + L.quat); b.vlin = (float4*)(base + L.vlin);
+    b.vang = (float4*)(base + L.vang); b.inv0 = (float4*)(base + L.inv0); b.inv1 = (float4*)(base + L.inv1);
+    b.loc0 = (float4*)(base + L.loc0); b.loc1 = (float4*)(base + L.loc1); b.damp = (float4*)(base + L.damp);
+    localM33 = (float*)(base + L.m33);
+    m.head = (int4*)(base + L.head); m.cpos = (float4*)(base + L.cpos); m.cnrm = (float4*)(base + L.cnrm);
+    m.offA = (float4*)(base + L.offA); m.offB = (float4*)(base + L.offB); m.mat = (float4*)(base + L.mat);
+    m.penacc = (float4*)(base + L.pen); m.fricacc = (float4*)(base + L.fric); m.saxis = (float4*)(base + L.axis);
+    m.pj0 = (float4*)(base + L.pj0); m.pj1 = (float4*)(base + L.pj1); m.pj2 = (float4*)(base + L.pj2);
+    m.s0 = (float4*)(base + L.s0); m.s1 = (float4*)(base + L.s1); m.s3 = (float4*)(base + L.s3);
+    m.s4 = (float4*)(base + L.s4); m.s5 = (float4*)(base + L.s5); m.s6 = (float4*)(base + L.s6);
+    m.s7 = (float4*)(base + L.s7); m.lever = (float4*)(base + L.lev); m.state = (uint2*)(base + L.state);
+    slotOf = (int32_t*)(base + L.slot);
+    colourOffsetsDev = (int32_t*)(base + L.offs);
+    groupDescDev = (GroupDesc*)(base + L.groups);
+    groupBodiesDev = (int32_t*)(base + L.groupBodies);
+    groupRefsDev = (int2*)(base + L.groupRefs);
+    groupColourOffsetsDev = (int32_t*)(base + L.groupOffsets);
+    sweepBodiesDev = (int32_t*)(base + L.sweepBodies);
+    j.head = (int4*)(base + L.jhead);
+    j.lanes = (float4*)(base + L.jlanes);
+    j.state = (uint2*)(base + L.jstate);
+    jointOffsetsDev = (int32_t*)(base + L.joffs);
+}
+
+// Moves the arena to pinned host memory and releases the scene's device
+// memory but the 1 KiB scratch block.  The scene's step graph is dropped: it
+// holds device addresses.
+bepugpu_status Scene::Spill(Context* ctx) {
+    if (!arena) return BEPUGPU_OK;
+    if (!spillHost) CK(cudaMallocHost(&spillHost, arenaBytes));
+    CK(cudaMemcpyAsync(spillHost, arena, arenaBytes, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaFree(arena));
+    arena = nullptr;
+    if (staging) CK(cudaFree(staging));
+    staging = nullptr;
+    if (graphExec) cudaGraphExecDestroy(graphExec);
+    graphExec = nullptr;
+    asyncPending = false;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status Scene::Restore(Context* ctx) {
+    if (arena) return BEPUGPU_OK;
+    cudaError_t e = cudaMalloc(&arena, arenaBytes);
+    if (e == cudaSuccess) {
+        e = cudaMalloc(&staging, stagingBytes);
+        if (e != cudaSuccess) {
+            cudaFree(arena);
+            arena = nullptr;
+            staging = nullptr;
+        }
+    } else {
+        arena = nullptr;
+    }
+    if (e != cudaSuccess) {
+        ctx->SetError("scene restore of %zu bytes: %s", arenaBytes + stagingBytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
+    }
+    Rebase();
+    CK(cudaMemcpyAsync(arena, spillHost, arenaBytes, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    version++;
     return BEPUGPU_OK;
 }
 
@@ -758,13 +808,23 @@ using namespace bepugpu;
         cudaSetDevice((ctx)->device);                \
     } while (0)
 
+// A scene of this context that no server owns (a served scene's device
+// state belongs to the server's worker until it is released).
 static Scene* FindScene(Context* ctx, int32_t id) {
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) {
         ctx->SetError("scene %d does not exist", id);
         return nullptr;
     }
+    if (it->second->server) {
+        ctx->SetError("scene %d is served; release it from its server first", id);
+        return nullptr;
+    }
     return it->second.get();
+}
+static bepugpu_status SceneMissing(Context* ctx, int32_t id) {
+    auto it = ctx->scenes.find(id);
+    return it != ctx->scenes.end() && it->second->server ? BEPUGPU_INVALID_OPERATION : BEPUGPU_NOT_FOUND;
 }
 
 extern "C" {
@@ -893,7 +953,7 @@ bepugpu_status bepugpu_scene_create(bepugpu_context* c, uint32_t nb, uint32_t nm
 bepugpu_status bepugpu_scene_destroy(bepugpu_context* c, int32_t id) {
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
-    if (!FindScene(ctx, id)) return BEPUGPU_NOT_FOUND;
+    if (!FindScene(ctx, id)) return SceneMissing(ctx, id);
     ctx->scenes.erase(id);
     return BEPUGPU_OK;
 }
@@ -902,7 +962,7 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (n > s->maxBodies || (n && !bodies)) {
         ctx->SetError("body count %u exceeds scene capacity %u", n, s->maxBodies);
         return BEPUGPU_INVALID_ARGUMENT;
@@ -956,7 +1016,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (nm > s->maxManifolds || nj > s->maxJoints || (nm && !man) || (nj && !joints)) {
         ctx->SetError("constraint counts exceed scene capacity");
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1044,7 +1104,7 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (n != (uint32_t)s->m.count || (n && !man)) {
         ctx->SetError("update_manifolds needs the %d manifolds of the last upload", s->m.count);
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1067,7 +1127,7 @@ bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_b
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (n != (uint32_t)s->b.count || (n && !bodies)) {
         ctx->SetError("download_bodies needs exactly %d records", s->b.count);
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1093,7 +1153,7 @@ bepugpu_status bepugpu_download_constraints(bepugpu_context* c, int32_t id, bepu
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (nm != (uint32_t)s->m.count || nj != s->jointCount || (nm && !man) || (nj && !joints)) {
         ctx->SetError("download_constraints needs %d manifolds and %u joints", s->m.count, s->jointCount);
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1140,7 +1200,7 @@ bepugpu_status bepugpu_get_colouring(bepugpu_context* c, int32_t id, int32_t* co
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (n != s->colouring.colour.size()) {
         ctx->SetError("colouring has %zu entries", s->colouring.colour.size());
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1168,7 +1228,7 @@ bepugpu_status bepugpu_set_solve_mode(bepugpu_context* c, int32_t id, int32_t mo
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (mode != BEPUGPU_MODE_GRAPH && mode != BEPUGPU_MODE_PERSISTENT) return BEPUGPU_INVALID_ARGUMENT;
     s->mode = mode;
     return BEPUGPU_OK;
@@ -1179,7 +1239,7 @@ bepugpu_status bepugpu_set_group_policy(bepugpu_context* c, int32_t id, int32_t 
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     // 96 bytes of shared memory per body must fit a CTA's 227 KB
     if (maxBodies < 1 || maxBodies > 2400 || maxManifolds < 1 || target < 1 || threads < 0 || threads > 256 ||
         threads % 32) {
@@ -1198,7 +1258,7 @@ bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* c, int32_t id, uin
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (bytes > kGroupSmemBudget) {
         ctx->SetError("shared-lane budget above %zu bytes", kGroupSmemBudget);
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1211,7 +1271,7 @@ bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* c, int32_t 
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (blocks < 1 || blocks > 2) {
         ctx->SetError("persistent blocks per SM must be 1 or 2");
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1225,7 +1285,7 @@ bepugpu_status bepugpu_step(bepugpu_context* c, int32_t id, float dt, uint32_t f
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     return s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
 }
 
@@ -1233,7 +1293,7 @@ bepugpu_status bepugpu_last_step_ms(bepugpu_context* c, int32_t id, float* ms) {
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (!ms || !s->stepped) return BEPUGPU_INVALID_ARGUMENT;
     CK(cudaEventSynchronize(s->evStop));
     CK(cudaEventElapsedTime(ms, s->evStart, s->evStop));
@@ -1244,7 +1304,7 @@ bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* c, int32_t id, float*
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (!phase_ms || !s->stepped) {
         ctx->SetError("phase times exist after a step");
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1267,7 +1327,7 @@ bepugpu_status bepugpu_last_step_launches(bepugpu_context* c, int32_t id, uint32
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (!launches) return BEPUGPU_INVALID_ARGUMENT;
     *launches = s->launchesPerStep;
     return BEPUGPU_OK;
@@ -1279,7 +1339,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
-    if (!s) return BEPUGPU_NOT_FOUND;
+    if (!s) return SceneMissing(ctx, id);
     if (!out || !(dt > 0)) return BEPUGPU_INVALID_ARGUMENT;
     if (s->maxBodyReferenced >= s->b.count) {
         ctx->SetError("constraints reference body %d but the scene holds %d bodies", s->maxBodyReferenced, s->b.count);

@@ -90,8 +90,20 @@ constexpr size_t kScratchBytes = 1024;
 constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 256, kCensusAt = 512,
                  kStampsAt = 640;
 
+// Byte offsets of a scene's device arrays inside its arena.
+struct ArenaLayout {
+    size_t pos, quat, vlin, vang, inv0, inv1, loc0, loc1, damp, m33;
+    size_t head, cpos, cnrm, offA, offB, mat, pen, fric, axis, pj0, pj1, pj2, s0, s1, s3, s4, s5, s6, s7, lev,
+        state, slot, offs;
+    size_t jhead, jlanes, jstate, joffs;
+    size_t groups, groupBodies, groupRefs, groupOffsets, sweepBodies;
+};
+
+struct Server;
+
 struct Scene {
     int32_t id = 0;
+    Server* server = nullptr;     // a server owns the scene's residency and steps (serve.cu)
     unsigned int* BarrierCounter() const { return (unsigned int*)((char*)counter + kBarrierCounterAt); }
     unsigned int* BarrierGeneration() const { return (unsigned int*)((char*)counter + kBarrierGenerationAt); }
     int* ErrorWord() const { return (int*)((char*)counter + kErrorAt); }
@@ -126,8 +138,14 @@ struct Scene {
     }
     int SweepColours() const { return manifoldOffsets.empty() ? 0 : (int)manifoldOffsets.size() - 1; }
     uint32_t maxBodies = 0, maxManifolds = 0, maxJoints = 0;
-    void* arena = nullptr;
+    void* arena = nullptr;          // null while spilled
     size_t arenaBytes = 0;
+    ArenaLayout layout{};
+    void* spillHost = nullptr;      // pinned copy of the arena while spilled
+    void Rebase();
+    bepugpu_status Spill(Context* ctx);
+    bepugpu_status Restore(Context* ctx);
+    size_t DeviceBytes() const { return arenaBytes + stagingBytes; }
     void* staging = nullptr;
     size_t stagingBytes = 0;
     void* counter = nullptr;  // grid barrier counter / generation / error word
@@ -176,6 +194,16 @@ struct Scene {
 struct BatchEngine {
     virtual ~BatchEngine() = default;
 };
+
+// Batched launches (batch.cu): one CTA per work item {view, group, steps}.
+struct SceneView {
+    ManifoldSoA m;
+    BodySoA b;
+    GroupTables t;
+};
+SceneView MakeView(const Scene& s);
+cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
+                                uint32_t flags, int Bc, int Lc, int members, int threads, cudaStream_t stream);
 
 struct Context {
     int device = 0;

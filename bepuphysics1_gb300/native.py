@@ -65,6 +65,20 @@ CHAIN_PARAMS_DTYPE = np.dtype([
     ("seed", "<u8"),
 ], align=True)
 
+SERVER_CONFIG_DTYPE = np.dtype([
+    ("device_budget_bytes", "<u8"), ("max_wave_scenes", "<u4"), ("max_waves_in_flight", "<u4"),
+    ("queue_capacity", "<u4"), ("batching", "<u4"), ("dt", "<f4"), ("flags", "<u4"), ("reserved", "<u4", 4),
+])
+COMPLETION_DTYPE = np.dtype([
+    ("tag", "<u8"), ("scene", "<i4"), ("status", "<i4"), ("steps", "<u4"), ("wave", "<u4"),
+    ("submit_us", "<f8"), ("start_us", "<f8"), ("done_us", "<f8"),
+])
+SERVER_STATS_DTYPE = np.dtype([
+    ("submitted", "<u8"), ("completed", "<u8"), ("waves", "<u8"), ("wave_scenes", "<u8"), ("launches", "<u8"),
+    ("spills", "<u8"), ("restores", "<u8"), ("resident_bytes", "<u8"), ("peak_resident_bytes", "<u8"),
+    ("spilled_bytes", "<u8"), ("scenes", "<u4"), ("resident_scenes", "<u4"),
+])
+
 PHASE_TIMES_DTYPE = np.dtype([
     ("refresh_ms", "<f4"), ("force_ms", "<f4"), ("prestep_ms", "<f4"), ("warm_ms", "<f4"), ("solve_ms", "<f4"),
     ("position_ms", "<f4"), ("solve_launches", "<u4"), ("warm_launches", "<u4"),
@@ -123,6 +137,17 @@ GPU_EXPORTS = {
     "bepugpu_profile_step": (_I, [_P, _I, _F, _U, _P]),
     "bepugpu_step_noalloc": (_I, [_P, _P, _U, _P, _U, _F, _U, _P]),
     "bepugpu_last_call_stats": (_I, [_P, ctypes.POINTER(_U), ctypes.POINTER(_F)]),
+    "bepugpu_server_default_config": (None, [_P]),
+    "bepugpu_server_create": (_I, [_P, _P, ctypes.POINTER(_P)]),
+    "bepugpu_server_destroy": (_I, [_P]),
+    "bepugpu_server_add_scene": (_I, [_P, _I]),
+    "bepugpu_server_release_scene": (_I, [_P, _I, _U]),
+    "bepugpu_serve_submit": (_I, [_P, _I, _U, ctypes.c_uint64]),
+    "bepugpu_serve_poll": (_I, [_P, _P, _U, ctypes.POINTER(_U)]),
+    "bepugpu_server_drain": (_I, [_P, _U]),
+    "bepugpu_server_stats_get": (_I, [_P, _P]),
+    "bepugpu_server_last_error": (ctypes.c_char_p, [_P]),
+    "bepugpu_clock_us": (ctypes.c_double, []),
 }
 
 SCENE_EXPORTS = {

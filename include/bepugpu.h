@@ -351,6 +351,76 @@ bepugpu_status bepugpu_step_noalloc(const bepugpu_settings* settings, bepugpu_bo
 /* Kernel counters of the last call on the context: launches and device ms. */
 bepugpu_status bepugpu_last_call_stats(bepugpu_context* ctx, uint32_t* launches, float* device_ms);
 
+/* ------------------------------------------------------------------ serving --
+ * A server steps scenes on request.  A worker thread drains a lock-free
+ * submit ring, keeps a FIFO of requests per scene, and launches waves: every
+ * scene with a request that is not already on the device joins the next wave
+ * (continuous batching), up to `max_wave_scenes`, and up to
+ * `max_waves_in_flight` waves overlap on the device on their own streams.  In
+ * a batched wave every island group of every scene is one CTA of one launch
+ * running that request's steps; scenes whose step is not all island groups
+ * (joints, large islands) take their one-scene path in the same wave.  With
+ * `batching` 0 every request takes the one-scene path (one graph launch per
+ * scene step): the plain baseline.
+ * Residency: the device bytes of resident scenes stay within
+ * `device_budget_bytes`; to make room the least recently used idle scene is
+ * spilled to pinned host memory (its arena, impulses included) and restored
+ * when a request needs it; a scene larger than the budget is refused
+ * (ADMISSION_REFUSED).  Results are the same bits as stepping each scene with
+ * bepugpu_step, whatever the mix and the spills.
+ * While a scene is added to a server, the other per-scene calls on it return
+ * INVALID_OPERATION; bepugpu_server_release_scene gives it back (resident).
+ * Submit and poll may be called from any thread.  No reference counterpart:
+ * the reference steps each Space on the caller's thread (Space.Update). */
+typedef struct bepugpu_server bepugpu_server;
+
+typedef struct bepugpu_server_config {
+    uint64_t device_budget_bytes;
+    uint32_t max_wave_scenes;      /* scenes per wave (>= 1) */
+    uint32_t max_waves_in_flight;  /* 1..4 */
+    uint32_t queue_capacity;       /* submit and completion rings, a power of two >= 2 */
+    uint32_t batching;             /* 1 continuous batching, 0 one launch per scene step */
+    float dt;
+    uint32_t flags;                /* BEPUGPU_STEP_* */
+    uint32_t reserved[4];
+} bepugpu_server_config;
+
+typedef struct bepugpu_completion {
+    uint64_t tag;                  /* as submitted */
+    int32_t scene;
+    int32_t status;                /* BEPUGPU_OK, NOT_FOUND, ADMISSION_REFUSED, CUDA_ERROR */
+    uint32_t steps;
+    uint32_t wave;                 /* wave number that ran it */
+    double submit_us, start_us, done_us;  /* bepugpu_clock_us() at submit, wave launch, completion seen */
+} bepugpu_completion;
+
+typedef struct bepugpu_server_stats {
+    uint64_t submitted, completed, waves, wave_scenes, launches, spills, restores;
+    uint64_t resident_bytes, peak_resident_bytes, spilled_bytes;
+    uint32_t scenes, resident_scenes;
+} bepugpu_server_stats;
+
+void bepugpu_server_default_config(bepugpu_server_config* out);
+bepugpu_status bepugpu_server_create(bepugpu_context* ctx, const bepugpu_server_config* config,
+                                     bepugpu_server** out);
+/* Waits for waves on the device, drops queued requests, restores spilled scenes
+ * and gives every scene back. */
+bepugpu_status bepugpu_server_destroy(bepugpu_server* server);
+bepugpu_status bepugpu_server_add_scene(bepugpu_server* server, int32_t scene);
+/* Waits (up to timeout_ms) until the scene has no queued or running request,
+ * restores it if spilled and gives it back. */
+bepugpu_status bepugpu_server_release_scene(bepugpu_server* server, int32_t scene, uint32_t timeout_ms);
+/* Queues `steps` steps of `scene`; QUEUE_FULL when the submit ring is full. */
+bepugpu_status bepugpu_serve_submit(bepugpu_server* server, int32_t scene, uint32_t steps, uint64_t tag);
+/* Moves up to `max` completions to `out`; *count receives how many. */
+bepugpu_status bepugpu_serve_poll(bepugpu_server* server, bepugpu_completion* out, uint32_t max, uint32_t* count);
+/* Waits until every submitted request has completed (TIMEOUT after timeout_ms). */
+bepugpu_status bepugpu_server_drain(bepugpu_server* server, uint32_t timeout_ms);
+bepugpu_status bepugpu_server_stats_get(bepugpu_server* server, bepugpu_server_stats* out);
+const char* bepugpu_server_last_error(bepugpu_server* server);
+/* Microseconds of the steady clock the completion times use. */
+double bepugpu_clock_us(void);
+
 #ifdef __cplusplus
 }
 #endif
