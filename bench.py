@@ -69,6 +69,12 @@ def parse_args():
     ap.add_argument("--tune-out", default=None, help="write the autotuner's trials to this JSON file")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--serve-scenes", type=int, default=16384)
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
+    ap.add_argument("--serve-rates", default="1000,5000,20000,50000,100000,200000",
+                    help="Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-plain-rates", default="1000,5000,20000")
     ap.add_argument("--chain-cpu-seconds", type=float, default=8.0)
     return ap.parse_args()
 
@@ -152,6 +158,23 @@ def ncu_traffic_per_launch():
             except ValueError:
                 return None
     return None
+
+
+def step_static_bytes(bodies, manifolds):
+    """Algorithmic bytes of a step beside the solve visits (the per-step
+    formula's warm-start, prestep and body terms): per manifold with a contact
+    and a dynamic body, one warm-start visit 76 d + 136 + 48 c and a prestep
+    64 d + 136 + 56 c; 152 per dynamic body (force and position updates)."""
+    dyn = np.asarray(bodies["is_dynamic"]) != 0
+    a, b = np.asarray(manifolds["body_a"]), np.asarray(manifolds["body_b"])
+    da = (a >= 0) & dyn[np.clip(a, 0, None)]
+    db = (b >= 0) & dyn[np.clip(b, 0, None)]
+    d = da.astype(np.int64) + db.astype(np.int64)
+    c = np.asarray(manifolds["contact_count"]).astype(np.int64)
+    live = (d > 0) & (c > 0)
+    warm = float((76 * d + 136 + 48 * c)[live].sum())
+    prestep = float((64 * d + 136 + 56 * c)[live].sum())
+    return warm, prestep, 152.0 * float(dyn.sum())
 
 
 def cpu_baseline(bodies, manifolds, contact_iters_per_step, seconds, threads):
@@ -398,6 +421,145 @@ def chain_section(args, local, rank, world, pg):
     return out
 
 
+SERVE_WORKLOAD = "serve_16k"
+SERVE_ITERATIONS = 8
+
+
+def serve_records(n, rank=0, world=1):
+    """The serving pool: n tower scenes, body counts log-uniform in [16, 4096]."""
+    from bepuphysics1_gb300 import scenes
+    sizes = scenes.batch_body_counts(n, 16, 4096, 5)
+    return [scenes.make_tower(int(k), seed=5 * 100003 + i)[:2] for i, k in enumerate(sizes) if i % world == rank]
+
+
+def poisson_load(srv, ids, rate, seconds, seed):
+    """Submits Poisson arrivals at `rate` requests/s for `seconds` (each a uniform
+    choice of scene and of k in {1, 4, 16} steps) while a second thread polls
+    completions; returns the completions and the achieved submit rate."""
+    import threading
+    from bepuphysics1_gb300 import native as N
+    rng = np.random.default_rng(seed)
+    n = max(1, int(rate * seconds))
+    gaps = rng.exponential(1.0 / rate, n)
+    when = np.cumsum(gaps)
+    scene = rng.integers(0, len(ids), n)
+    steps = rng.choice(np.array([1, 4, 16]), n)
+    out, stop = [], threading.Event()
+
+    def poller():
+        while not stop.is_set():
+            c = srv.poll()
+            if len(c):
+                out.append(c)
+            else:
+                time.sleep(0.0005)
+
+    th = threading.Thread(target=poller)
+    th.start()
+    t0 = time.perf_counter()
+    full = 0
+    for i in range(n):
+        while time.perf_counter() - t0 < when[i]:
+            pass
+        while srv.submit(ids[scene[i]], int(steps[i]), i) == N.QUEUE_FULL:
+            full += 1
+    submit_s = time.perf_counter() - t0
+    srv.drain(600000)
+    stop.set()
+    th.join()
+    while True:
+        c = srv.poll()
+        if not len(c):
+            break
+        out.append(c)
+    done = np.concatenate(out) if out else np.zeros(0, N.COMPLETION_DTYPE)
+    return done, n / submit_s, full
+
+
+def serve_level(srv, ids, rate, seconds, seed):
+    from bepuphysics1_gb300 import native as N
+    s0 = srv.stats()
+    done, achieved, full = poisson_load(srv, ids, rate, seconds, seed)
+    s1 = srv.stats()
+    ok = done[done["status"] == N.OK]
+    lat = (ok["done_us"] - ok["submit_us"]) / 1000.0
+    span_s = (ok["done_us"].max() - ok["submit_us"].min()) / 1e6 if len(ok) else 1.0
+    waves = int(s1["waves"] - s0["waves"])
+    return {"rate": rate, "achieved_rate": achieved, "requests": int(len(done)), "ok": int(len(ok)),
+            "scene_steps_per_s": float(ok["steps"].sum()) / span_s,
+            "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+            "max_ms": float(lat.max()) if len(lat) else None,
+            "queue_ms_p50": float(np.percentile((ok["start_us"] - ok["submit_us"]) / 1000.0, 50)) if len(ok) else None,
+            "waves": waves, "scenes_per_wave": float(s1["wave_scenes"] - s0["wave_scenes"]) / max(waves, 1),
+            "launches": int(s1["launches"] - s0["launches"]), "spills": int(s1["spills"] - s0["spills"]),
+            "restores": int(s1["restores"] - s0["restores"]), "submit_ring_full": int(full)}
+
+
+def serve_section(args, local, rank, world, pg):
+    """Serving workload: a pool of tower scenes resident on the device, Poisson
+    step requests (k in {1, 4, 16}) at swept arrival rates, p50/p99 request
+    latency (submit to completion seen, host steady clock) and sustained
+    scene-steps/s; continuously batched against plain one-launch-per-step
+    serving, and once under a device budget of half the pool (LRU spills)."""
+    from bepuphysics1_gb300.serve import Server
+    from bepuphysics1_gb300.solver import Context, GpuSpace
+
+    t0 = time.perf_counter()
+    records = serve_records(args.serve_scenes, rank, world)
+    settings = batch_settings()
+    settings["iteration_limit"] = SERVE_ITERATIONS
+    ctx = Context(local, settings)
+    spaces = [GpuSpace(ctx, b, m) for b, m in records]
+    setup_s = time.perf_counter() - t0
+    ids = [sp.id for sp in spaces]
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    plain_rates = [float(r) for r in args.serve_plain_rates.split(",") if r]
+    out = {"metric": "scene-steps/s and request latency", "workload": SERVE_WORKLOAD,
+           "config": {"scenes": args.serve_scenes, "bodies": int(sum(len(b) for b, _ in records)),
+                      "manifolds": int(sum(len(m) for _, m in records)),
+                      "body_counts": "log-uniform in [16, 4096], towers of height 4..32",
+                      "iterations": SERVE_ITERATIONS, "k": [1, 4, 16], "arrival_window_s": args.serve_seconds,
+                      "setup_s": setup_s, "latency": "submit to completion seen by the server, steady clock"}}
+
+    def run(mode_rates, **kw):
+        srv = Server(ctx, dt=float(DT), **kw)
+        for sp in spaces:
+            srv.add(sp)
+        # warm-up: one 1-step request per scene (first launches, one-scene graphs), untimed
+        for i in ids:
+            while srv.submit(i, 1, 0) != 0:
+                srv.poll()
+        srv.drain(600000)
+        while len(srv.poll()):
+            pass
+        st = srv.stats()
+        levels = [serve_level(srv, ids, r, args.serve_seconds, 17 + i) for i, r in enumerate(mode_rates)]
+        res = {"levels": levels, "resident_bytes": int(st["resident_bytes"]),
+               "resident_scenes": int(st["resident_scenes"])}
+        srv.close()
+        return res
+
+    out["batched"] = run(rates, batching=True, budget_bytes=120 << 30)
+    out["batched"]["device_budget_bytes"] = 120 << 30
+    out["plain"] = run(plain_rates, batching=False, budget_bytes=120 << 30)
+    total = out["batched"]["resident_bytes"]
+    spill_rate = [r for r in rates if r <= 5000][-1:] or rates[:1]
+    out["batched_half_budget"] = run(spill_rate, batching=True, budget_bytes=max(total // 2, 1 << 20))
+    out["batched_half_budget"]["device_budget_bytes"] = max(total // 2, 1 << 20)
+    by_rate = {lv["rate"]: lv for lv in out["plain"]["levels"]}
+    out["vs_plain"] = [{"rate": lv["rate"], "p99_ms_batched": lv["p99_ms"],
+                        "p99_ms_plain": by_rate[lv["rate"]]["p99_ms"],
+                        "scene_steps_per_s_batched": lv["scene_steps_per_s"],
+                        "scene_steps_per_s_plain": by_rate[lv["rate"]]["scene_steps_per_s"]}
+                       for lv in out["batched"]["levels"] if lv["rate"] in by_rate]
+    out["equal_error"] = "bit-identical to stepping each scene alone (tests/test_gpu_serve.py)"
+    for sp in spaces:
+        sp.close()
+    ctx.close()
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -502,20 +664,33 @@ def main():
     traffic = ncu_traffic_per_launch()
     kernel_only = {k: float(prof[k]) for k in ("refresh_ms", "force_ms", "prestep_ms", "warm_ms", "solve_ms",
                                                "position_ms", "group_ms")}
+    warm_b, prestep_b, body_b = step_static_bytes(bodies, live_m)
+    step_alg = float(prof["solve_algorithmic_bytes"]) + warm_b + prestep_b + body_b
+    step_achieved = step_alg / (total_ms / args.steps / 1000.0) / 1e9
     if int(prof["groups"]) > 0 and statistics.mean(group_ms) >= statistics.mean(solve_ms):
         # Island groups: one launch runs whole steps of the small islands.  Its
-        # DRAM floor is the compulsory traffic of a step (inputs read once,
-        # outputs and prestep products written once).
-        bytes_per_launch = float(prof["group_compulsory_bytes"])
+        # algorithmic bytes are the step formula over the units it processes:
+        # its executed solve visits (census), one warm-start visit and one
+        # prestep per active manifold, force and position per body.  With the
+        # sweep part empty (every manifold in a group) all of the step is its.
+        group_visits = float(prof["group_solve_algorithmic_bytes"])
+        share = 1.0 if int(prof["solve_launches"]) == 0 else \
+            float(prof["group_solve_manifold_visits"]) / max(float(prof["solve_manifold_visits"]), 1.0)
+        bytes_per_launch = group_visits + share * (warm_b + prestep_b + body_b)
         launch_s = statistics.mean(group_ms) / 1000.0
         achieved = bytes_per_launch / launch_s / 1e9
+        floor = float(prof["group_compulsory_bytes"])
         roofline = {"bound": "hbm", "kernel": "k_groups", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                     "algorithmic_bytes_per_launch": bytes_per_launch,
-                    "algorithmic": "compulsory bytes per step: 288 + 112 c per manifold, 208 per body",
+                    "algorithmic": "76 d + 136 + 48 c per executed solve visit and per warm-start visit, "
+                                   "64 d + 136 + 56 c per prestep, 152 per dynamic body",
                     "launch_ms_avg": 1000.0 * launch_s, "launches_per_step": 1, "ctas": int(prof["groups"]),
-                    "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
-                    "sweep_equivalent_bytes_per_step": float(prof["solve_algorithmic_bytes"]),
+                    "manifold_visits_per_step": float(prof["group_solve_manifold_visits"]),
+                    "dram_floor_bytes_per_launch": floor,
+                    "dram_floor_frac": floor / launch_s / 1e9 / peak,
+                    "dram_floor": "each input lane read once and each output lane written once "
+                                  "(136 + 64 c per manifold with shared-memory lanes, 208 per body)",
                     "kernel_only_ms_per_step": kernel_only}
     else:
         bytes_per_step = float(prof["solve_algorithmic_bytes"])
@@ -530,6 +705,9 @@ def main():
                     "solve_launches_per_step": solve_launches,
                     "manifold_visits_per_step": float(prof["solve_manifold_visits"]),
                     "kernel_only_ms_per_step": kernel_only}
+    roofline["step"] = {"algorithmic_bytes_per_step": step_alg, "achieved": step_achieved,
+                        "frac": step_achieved / peak, "ms_per_step": total_ms / args.steps,
+                        "what": "the whole step (every kernel, launch gaps included) against the same bytes"}
 
     # e2e through the C ABI with pinned host records
     e2e = None
@@ -570,6 +748,10 @@ def main():
     if not args.no_chains:
         space.close()
         chains = chain_section(args, local, rank, world, pg)
+    serve = None
+    if not args.no_serve:
+        space.close()
+        serve = serve_section(args, local, rank, world, pg)
 
     if rank == 0:
         line = {
@@ -592,6 +774,7 @@ def main():
             "clocks": clk.summary(),
             "batch": batch,
             "chains": chains,
+            "serve": serve,
         }
         print(json.dumps(line), flush=True)
     space.close()

@@ -183,8 +183,9 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             ctx->SetError("batch: at most 65535 steps per call");
             return BEPUGPU_INVALID_ARGUMENT;
         }
-        if (s->maxBodyReferenced >= s->b.count) {
-            ctx->SetError("batch: scene %d references body %d of %d", scenes[i], s->maxBodyReferenced, s->b.count);
+        if (s->maxBodyReferenced >= s->b.count || s->planStale) {
+            ctx->SetError("batch: scene %d references body %d of %d or changed dynamic bodies since its constraints "
+                          "were uploaded", scenes[i], s->maxBodyReferenced, s->b.count);
             return BEPUGPU_INVALID_OPERATION;
         }
         for (uint32_t j = 0; j < i; j++)

@@ -125,27 +125,64 @@ __global__ void k_unpack_manifolds(const bepugpu_manifold* __restrict__ rec, con
     m.state[s] = make_uint2(0u, 0u);
 }
 
-__global__ void k_pack_manifolds(ManifoldSoA m, ManifoldOut* __restrict__ out) {
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= m.count) return;
-    int cap = m.capacity;
-    int4 h = m.head[s];
-    ManifoldOut o;
-    o.source = h.w;
-    o.count = h.z & 0xff;
-    float4 pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
-    float acc[4] = {pa.x, pa.y, pa.z, pa.w};
-    for (int k = 0; k < 4; k++) {
-        float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s], oa = m.offA[k * cap + s], ob = m.offB[k * cap + s];
-        o.c[k].pos[0] = cp.x; o.c[k].pos[1] = cp.y; o.c[k].pos[2] = cp.z; o.c[k].depth = cp.w;
-        o.c[k].nrm[0] = cn.x; o.c[k].nrm[1] = cn.y; o.c[k].nrm[2] = cn.z; o.c[k].id = __float_as_int(cn.w);
-        o.c[k].offa[0] = oa.x; o.c[k].offa[1] = oa.y; o.c[k].offa[2] = oa.z; o.c[k].base = oa.w;
-        o.c[k].offb[0] = ob.x; o.c[k].offb[1] = ob.y; o.c[k].offb[2] = ob.z;
-        o.c[k].acc = acc[k];
+// Whole manifold records in record order (the caller's array), built in
+// shared memory and written out as contiguous 8-byte stores: the download
+// is then one copy straight into the caller's records.
+constexpr int kRecordBlock = 128;
+static_assert(sizeof(bepugpu_manifold) % 8 == 0, "manifold records must tile 8-byte stores");
+__global__ void __launch_bounds__(kRecordBlock) k_pack_manifold_records(ManifoldSoA m,
+                                                                         const int32_t* __restrict__ slot_of, int n,
+                                                                         uint2* __restrict__ out) {
+    __shared__ __align__(16) bepugpu_manifold recs[kRecordBlock];
+    const int first = blockIdx.x * kRecordBlock;
+    const int i = first + threadIdx.x;
+    if (i < n) {
+        const int s = slot_of[i], cap = m.capacity;
+        const int4 h = m.head[s];
+        const int count = h.z & 0xff;
+        bepugpu_manifold& r = recs[threadIdx.x];
+        r.body_a = h.x;
+        r.body_b = h.y;
+        r.contact_count = count;
+        r.flags = (uint32_t)h.z >> 8;
+        const float4 mat = m.mat[s], pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
+        r.kinetic_friction = mat.x;
+        r.static_friction = mat.y;
+        r.bounciness = mat.z;
+        r.sliding_impulse[0] = f.x;
+        r.sliding_impulse[1] = f.y;
+        r.sliding_axis[0] = ax.x;
+        r.sliding_axis[1] = ax.y;
+        r.sliding_axis[2] = ax.z;
+        r.twist_impulse = f.z;
+        r.reserved = 0;
+        const float acc[4] = {pa.x, pa.y, pa.z, pa.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            bepugpu_contact& c = r.contacts[k];
+            if (k < count) {
+                const float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s], oa = m.offA[k * cap + s],
+                             ob = m.offB[k * cap + s];
+                c.position[0] = cp.x; c.position[1] = cp.y; c.position[2] = cp.z;
+                c.normal[0] = cn.x; c.normal[1] = cn.y; c.normal[2] = cn.z;
+                c.penetration_depth = cp.w;
+                c.id = __float_as_int(cn.w);
+                c.local_offset_a[0] = oa.x; c.local_offset_a[1] = oa.y; c.local_offset_a[2] = oa.z;
+                c.local_offset_b[0] = ob.x; c.local_offset_b[1] = ob.y; c.local_offset_b[2] = ob.z;
+                c.base_penetration_depth = oa.w;
+                c.penetration_impulse = acc[k];
+            } else {
+                uint32_t* w = (uint32_t*)&c;
+                for (int q = 0; q < (int)(sizeof(bepugpu_contact) / 4); q++) w[q] = 0u;
+            }
+        }
     }
-    o.sliding[0] = f.x; o.sliding[1] = f.y; o.twist = f.z;
-    o.axis[0] = ax.x; o.axis[1] = ax.y; o.axis[2] = ax.z;
-    out[s] = o;
+    __syncthreads();
+    const int rows = min(kRecordBlock, n - first);
+    const int words = rows * (int)(sizeof(bepugpu_manifold) / 8);
+    const uint2* src = (const uint2*)recs;
+    uint2* dst = out + (size_t)first * (sizeof(bepugpu_manifold) / 8);
+    for (int k = threadIdx.x; k < words; k += kRecordBlock) dst[k] = src[k];
 }
 
 __global__ void k_refresh(ManifoldSoA m, BodySoA b, StepParams p) {
@@ -520,7 +557,7 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     Rebase();
     CK(cudaMemset(arena, 0, bytes));
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
-    stagingBytes = std::max(stagingBytes, std::max(sizeof(BodyOut) * B, sizeof(ManifoldOut) * M));
+    stagingBytes = std::max(stagingBytes, sizeof(BodyOut) * B);
     CK(cudaMalloc(&staging, stagingBytes));
     CK(cudaMalloc(&counter, kScratchBytes));
     CK(cudaMemset(counter, 0, kScratchBytes));
@@ -563,15 +600,17 @@ void Scene::Rebase() {
 // Moves the arena to pinned host memory and releases the scene's device
 // memory but the 1 KiB scratch block.  The scene's step graph is dropped: it
 // holds device addresses.
+// Stream-ordered frees and allocations (cudaFreeAsync / cudaMallocAsync) keep
+// a spill or restore from synchronising the device with work of other scenes.
 bepugpu_status Scene::Spill(Context* ctx) {
     if (!arena) return BEPUGPU_OK;
     if (!spillHost) CK(cudaMallocHost(&spillHost, arenaBytes));
     CK(cudaMemcpyAsync(spillHost, arena, arenaBytes, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    CK(cudaFree(arena));
+    CK(cudaFreeAsync(arena, stream));
     arena = nullptr;
-    if (staging) CK(cudaFree(staging));
+    if (staging) CK(cudaFreeAsync(staging, stream));
     staging = nullptr;
+    CK(cudaStreamSynchronize(stream));
     if (graphExec) cudaGraphExecDestroy(graphExec);
     graphExec = nullptr;
     asyncPending = false;
@@ -580,11 +619,11 @@ bepugpu_status Scene::Spill(Context* ctx) {
 
 bepugpu_status Scene::Restore(Context* ctx) {
     if (arena) return BEPUGPU_OK;
-    cudaError_t e = cudaMalloc(&arena, arenaBytes);
+    cudaError_t e = cudaMallocAsync(&arena, arenaBytes, stream);
     if (e == cudaSuccess) {
-        e = cudaMalloc(&staging, stagingBytes);
+        e = cudaMallocAsync(&staging, stagingBytes, stream);
         if (e != cudaSuccess) {
-            cudaFree(arena);
+            cudaFreeAsync(arena, stream);
             arena = nullptr;
             staging = nullptr;
         }
@@ -645,6 +684,30 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     const ManifoldSoA ms = SweepManifolds();
     const int colours = SweepColours();
     int nm = ms.count, nb = b.count;
+    // A scene whose whole step is island groups has nothing left for the sweep
+    // path: no sweep manifolds or joints, no dynamic body outside the groups,
+    // no moving kinematic body.  Its graph is the group launch alone.
+    phaseEvents = !(BatchReady());
+    if (!phaseEvents) {
+        cudaGraph_t graph;
+        cudaError_t e = cudaStreamEndCapture(stream, &graph);
+        if (e != cudaSuccess) {
+            ctx->SetError("graph capture: %s", cudaGetErrorString(e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        e = cudaGraphInstantiate(&graphExec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            graphExec = nullptr;
+            ctx->SetError("graph instantiate: %s", cudaGetErrorString(e));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        graphDt = p.dt;
+        graphFlags = flags;
+        graphVersion = version;
+        graphIterations = p.iterationLimit;
+        return BEPUGPU_OK;
+    }
     // Phase events become event-record nodes of the graph: their elapsed times
     // are the device time of each phase of every launched step.
     CK(cudaEventRecordWithFlags(evPhase[0], stream, cudaEventRecordExternal));
@@ -774,6 +837,10 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
     }
     if (maxBodyReferenced >= b.count) {
         ctx->SetError("constraints reference body %d but the scene holds %d bodies", maxBodyReferenced, b.count);
+        return BEPUGPU_INVALID_OPERATION;
+    }
+    if (planStale) {
+        ctx->SetError("bodies changed between dynamic and kinematic: upload the constraints again to recolour");
         return BEPUGPU_INVALID_OPERATION;
     }
     bepugpu_status st = RefreshDamping(ctx, dt);
@@ -968,9 +1035,12 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         return BEPUGPU_INVALID_ARGUMENT;
     }
     s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);
+    const bool wasMoving = s->kinematicMoving;
+    bool dynamicChanged = s->hostDynamic.size() != n;
     s->hostDynamic.resize(n);
     s->kinematicMoving = false;
     for (uint32_t i = 0; i < n; i++) {
+        if (!dynamicChanged && s->hostDynamic[i] != (bodies[i].is_dynamic ? 1 : 0)) dynamicChanged = true;
         if (!bodies[i].is_dynamic) {
             const float* v = bodies[i].linear_velocity;
             const float* w = bodies[i].angular_velocity;
@@ -982,7 +1052,9 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         s->hostLocalM33[i] = bodies[i].is_dynamic ? bodies[i].local_inverse_inertia[8] : 0.f;
     }
     const bool resized = n != (uint32_t)s->b.count;
-    if (resized) s->version++;
+    if (resized || wasMoving != s->kinematicMoving) s->version++;
+    // The colouring and the island groups depend on which bodies are dynamic.
+    if (dynamicChanged && (s->m.count || s->jointCount)) s->planStale = true;
     s->b.count = (int)n;
     s->dampDirty = true;
     if (resized && !s->groupPlan.groups.empty()) {
@@ -1076,6 +1148,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         if (lst != BEPUGPU_OK) return lst;
     }
     s->dampDirty = true;
+    s->planStale = false;
     s->m.count = (int)nm;
     s->jointCount = nj;
     s->version++;
@@ -1163,35 +1236,14 @@ bepugpu_status bepugpu_download_constraints(bepugpu_context* c, int32_t id, bepu
         if (jst != BEPUGPU_OK) return jst;
     }
     if (!nm) return BEPUGPU_OK;
-    ManifoldOut* dev = (ManifoldOut*)s->staging;
-    k_pack_manifolds<<<Blocks(nm, 256), 256, 0, s->stream>>>(s->m, dev);
-    s->hostManifoldOut.resize(nm);
-    CK(cudaMemcpyAsync(s->hostManifoldOut.data(), dev, sizeof(ManifoldOut) * nm, cudaMemcpyDeviceToHost, s->stream));
+    // Whole records are rebuilt on the device in record order and copied
+    // straight into the caller's array (their fields are the uploaded ones,
+    // the state fields current; `reserved` comes back 0).
+    k_pack_manifold_records<<<Blocks(nm, kRecordBlock), kRecordBlock, 0, s->stream>>>(s->m, s->slotOf, (int)nm,
+                                                                                    (uint2*)s->staging);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(man, s->staging, sizeof(bepugpu_manifold) * nm, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    for (uint32_t k = 0; k < nm; k++) {
-        const ManifoldOut& o = s->hostManifoldOut[k];
-        bepugpu_manifold& r = man[o.source];
-        r.contact_count = o.count;
-        for (int j = 0; j < 4; j++) {
-            bepugpu_contact& cr = r.contacts[j];
-            if (j < o.count) {
-                std::memcpy(cr.position, o.c[j].pos, 12);
-                cr.penetration_depth = o.c[j].depth;
-                std::memcpy(cr.normal, o.c[j].nrm, 12);
-                cr.id = o.c[j].id;
-                std::memcpy(cr.local_offset_a, o.c[j].offa, 12);
-                std::memcpy(cr.local_offset_b, o.c[j].offb, 12);
-                cr.base_penetration_depth = o.c[j].base;
-                cr.penetration_impulse = o.c[j].acc;
-            } else {
-                std::memset(&cr, 0, sizeof(cr));
-            }
-        }
-        r.sliding_impulse[0] = o.sliding[0];
-        r.sliding_impulse[1] = o.sliding[1];
-        r.twist_impulse = o.twist;
-        std::memcpy(r.sliding_axis, o.axis, 12);
-    }
     return BEPUGPU_OK;
 }
 
@@ -1319,6 +1371,10 @@ bepugpu_status bepugpu_last_step_phase_ms(bepugpu_context* c, int32_t id, float*
         phase_ms[3] = t[1] > t[0] ? (float)((double)(t[1] - t[0]) * 1e-6) : 0.f;
         return BEPUGPU_OK;
     }
+    if (!s->phaseEvents) {  // the step was the group launch alone
+        for (int k = 0; k < 5; k++) phase_ms[k] = 0.f;
+        return BEPUGPU_OK;
+    }
     for (int k = 0; k < 5; k++) CK(cudaEventElapsedTime(&phase_ms[k], s->evPhase[k], s->evPhase[k + 1]));
     return BEPUGPU_OK;
 }
@@ -1362,13 +1418,15 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     struct Span { cudaEvent_t a, b; float* dst; };
     std::vector<Span> spans;
     unsigned long long* acc = s->Census();
-    CK(cudaMemsetAsync(acc, 0, 4 * sizeof(unsigned long long), q));
+    CK(cudaMemsetAsync(acc, 0, 8 * sizeof(unsigned long long), q));
     if (!s->groupPlan.groups.empty()) {  // the census variant of the group kernel counts its visits
         cudaEvent_t a = mark();
         bepugpu_status gs = LaunchGroups(ctx, s, p, flags, true);
         if (gs != BEPUGPU_OK) return gs;
         spans.push_back({a, mark(), &out->group_ms});
         out->groups = (uint32_t)s->groupPlan.groups.size();
+        // the groups' own share of the visit census
+        CK(cudaMemcpyAsync(acc + 4, acc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, q));
     }
     const ManifoldSoA ms = s->SweepManifolds();
     const int colours = s->SweepColours();
@@ -1409,7 +1467,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
         cudaEvent_t a = mark(); k_position<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->position_ms});
     }
     CK(cudaGetLastError());
-    unsigned long long h[4] = {0, 0, 0, 0};
+    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(h, acc, sizeof(h), cudaMemcpyDeviceToHost, q));
     CK(cudaStreamSynchronize(q));
     for (auto& sp : spans) {
@@ -1422,6 +1480,8 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     out->solve_manifold_visits = (double)h[1];
     out->solve_contact_visits = (double)h[2];
     out->group_compulsory_bytes = (double)h[3];
+    out->group_solve_algorithmic_bytes = (double)h[4];
+    out->group_solve_manifold_visits = (double)h[5];
     return BEPUGPU_OK;
 }
 

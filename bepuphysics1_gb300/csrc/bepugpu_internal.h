@@ -16,19 +16,10 @@
 
 namespace bepugpu {
 
-// Compact download records (device -> host), scattered into caller records.
+// Compact body download record (device -> host), scattered into the caller's
+// records (manifold records are rebuilt whole on the device instead).
 struct BodyOut {
     float p[3], q[4], v[3], w[3];
-};
-struct ContactOut {
-    float pos[3], depth, nrm[3];
-    int32_t id;
-    float offa[3], base, offb[3], acc;
-};
-struct ManifoldOut {
-    int32_t source, count;
-    ContactOut c[4];
-    float sliding[2], twist, axis[3];
 };
 
 struct Context;
@@ -127,6 +118,8 @@ struct Scene {
     // The whole step is island groups, so a batched launch can run it (batch.cu).
     bool BatchReady() const;
     int groupThreadsOverride = 0;    // 0 = derived from the plan
+    bool phaseEvents = true;         // the step graph records the sweep-path phase events
+    bool planStale = false;          // dynamic flags changed since the constraints were planned
     cudaEvent_t evGroup[2] = {nullptr, nullptr};
     bepugpu_status UploadGroups(Context* ctx);
     bepugpu_status RebuildSweepBodies(Context* ctx);
@@ -167,7 +160,6 @@ struct Scene {
     std::vector<uint8_t> hostDynamic;
     std::vector<float4> hostDamp;
     std::vector<BodyOut> hostBodyOut;
-    std::vector<ManifoldOut> hostManifoldOut;
     bool dampDirty = true;
     float dampDt = 0.f;
     cudaStream_t stream = nullptr;

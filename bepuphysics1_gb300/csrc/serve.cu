@@ -286,8 +286,14 @@ struct Server {
         EnsureViewCapacity();
         cudaError_t e = viewsDev ? cudaSuccess : cudaErrorMemoryAllocation;
         // Synchronous copies: any later wave, on any stream, may read these entries.
-        for (int id : dirtyViews)
-            if (e == cudaSuccess) e = cudaMemcpy(viewsDev + id, &viewsHost[id], sizeof(SceneView), cudaMemcpyHostToDevice);
+        if (dirtyViews.size() > 32) {
+            if (e == cudaSuccess)
+                e = cudaMemcpy(viewsDev, viewsHost.data(), sizeof(SceneView) * viewsHost.size(), cudaMemcpyHostToDevice);
+        } else {
+            for (int id : dirtyViews)
+                if (e == cudaSuccess)
+                    e = cudaMemcpy(viewsDev + id, &viewsHost[id], sizeof(SceneView), cudaMemcpyHostToDevice);
+        }
         dirtyViews.clear();
         size_t nWork = shared.size() + global.size();
         if (e == cudaSuccess && nWork > w.workCap) {
@@ -415,6 +421,13 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
     s->cfg = *config;
     s->cfg.flags &= BEPUGPU_STEP_ALL;
     s->p = MakeParams(ctx->settings, config->dt);
+    // Let the device's stream-ordered pool keep up to a budget of freed spill
+    // memory, so restores reuse it instead of returning it to the driver.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
+        uint64_t keep = config->device_budget_bytes;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     s->waves.resize(config->max_waves_in_flight);
     for (auto& w : s->waves) {
         if (cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -478,7 +491,7 @@ bepugpu_status bepugpu_server_add_scene(bepugpu_server* h, int32_t scene) {
         s->SetError("scene " + std::to_string(scene) + " is in persistent mode; serving takes graph-mode scenes");
         return BEPUGPU_INVALID_OPERATION;
     }
-    if (sc->maxBodyReferenced >= sc->b.count) {
+    if (sc->maxBodyReferenced >= sc->b.count || sc->planStale) {
         s->SetError("scene " + std::to_string(scene) + " references bodies it does not hold");
         return BEPUGPU_INVALID_OPERATION;
     }

@@ -84,6 +84,7 @@ PHASE_TIMES_DTYPE = np.dtype([
     ("position_ms", "<f4"), ("solve_launches", "<u4"), ("warm_launches", "<u4"),
     ("solve_algorithmic_bytes", "<f8"), ("solve_manifold_visits", "<f8"), ("solve_contact_visits", "<f8"),
     ("group_ms", "<f4"), ("groups", "<u4"), ("group_compulsory_bytes", "<f8"),
+    ("group_solve_algorithmic_bytes", "<f8"), ("group_solve_manifold_visits", "<f8"),
 ])
 
 # bepugpu_status

@@ -223,8 +223,14 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* ctx, int32_t scene,
 bepugpu_status bepugpu_update_manifolds(bepugpu_context* ctx, int32_t scene,
                                         const bepugpu_manifold* manifolds, uint32_t count);
 
+/* Writes position, orientation and velocities into the caller's records
+ * (their other fields are left as they are). */
 bepugpu_status bepugpu_download_bodies(bepugpu_context* ctx, int32_t scene,
                                        bepugpu_body* bodies, uint32_t count);
+/* Writes whole manifold records, in upload order: the uploaded fields as they
+ * were, the state (contacts after refresh, accumulated impulses, sliding axis)
+ * as it is now, unused contact slots and `reserved` zero.  Joint records get
+ * their accumulated impulses written. */
 bepugpu_status bepugpu_download_constraints(bepugpu_context* ctx, int32_t scene,
                                             bepugpu_manifold* manifolds, uint32_t manifold_count,
                                             bepugpu_joint* joints, uint32_t joint_count);
@@ -318,8 +324,12 @@ typedef struct bepugpu_phase_times {
     float group_ms;                   /* the island-group kernel (whole steps of small islands) */
     uint32_t groups;                  /* CTAs of that kernel */
     double group_compulsory_bytes;    /* DRAM bytes the group kernel cannot avoid in one step:
-                                         every input lane read once, every output or prestep
-                                         lane written once (288 + 112 c per manifold, 208 per body) */
+                                         every input lane read once, every output lane written
+                                         once (136 + 64 c per manifold with its solve lanes in
+                                         shared memory, 288 + 112 c with them in global memory,
+                                         208 per body) */
+    double group_solve_algorithmic_bytes; /* the group kernel's share of solve_algorithmic_bytes */
+    double group_solve_manifold_visits;   /* the group kernel's share of solve_manifold_visits */
 } bepugpu_phase_times;
 
 bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float dt, uint32_t flags,

@@ -207,3 +207,21 @@ def test_update_manifolds_round_trip(gpu_context):
     np.testing.assert_array_equal(ab["linear_velocity"], cb["linear_velocity"])
     a.close()
     c.close()
+
+
+def test_manifold_records_roundtrip(gpu_context):
+    """Downloading right after an upload gives back the uploaded records (whole
+    records are rebuilt on the device)."""
+    gpu_context.set_settings(default_settings())
+    b, m, _ = scenes.pile_1k()
+    m = m.copy()
+    rng = np.random.default_rng(2)
+    live = np.arange(4)[None, :] < m["contact_count"][:, None]
+    m["contacts"]["penetration_impulse"] = np.where(live, rng.uniform(0, 1, live.shape), 0).astype(np.float32)
+    m["sliding_impulse"] = rng.normal(size=m["sliding_impulse"].shape).astype(np.float32)
+    m["twist_impulse"] = rng.normal(size=m["twist_impulse"].shape).astype(np.float32)
+    m["reserved"] = 0
+    sp = GpuSpace(gpu_context, b, m)
+    back, _ = sp.download_constraints(np.zeros_like(m))
+    assert back.tobytes() == m.tobytes()
+    sp.close()
