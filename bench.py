@@ -146,9 +146,10 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """dram bytes per k_solve launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / "k_solve_pile64k.md"
+def ncu_traffic_per_launch(kernel: str):
+    """DRAM bytes per launch of `kernel` on the pile from the committed ncu
+    summary (profiles/<kernel>_pile64k.md), if any."""
+    p = ROOT / "profiles" / f"{kernel}_pile64k.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -661,7 +662,6 @@ def main():
     # roofline of the dominant kernel, from a census of one instrumented step
     prof = profile_step(space, DT, N.STEP_ALL)
     peak, peak_kind = measured_hbm_peak()
-    traffic = ncu_traffic_per_launch()
     kernel_only = {k: float(prof[k]) for k in ("refresh_ms", "force_ms", "prestep_ms", "warm_ms", "solve_ms",
                                                "position_ms", "group_ms")}
     warm_b, prestep_b, body_b = step_static_bytes(bodies, live_m)
@@ -681,7 +681,7 @@ def main():
         achieved = bytes_per_launch / launch_s / 1e9
         floor = float(prof["group_compulsory_bytes"])
         roofline = {"bound": "hbm", "kernel": "k_groups", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": ncu_traffic_per_launch("k_groups"),
                     "algorithmic_bytes_per_launch": bytes_per_launch,
                     "algorithmic": "76 d + 136 + 48 c per executed solve visit and per warm-start visit, "
                                    "64 d + 136 + 56 c per prestep, 152 per dynamic body",
@@ -698,7 +698,7 @@ def main():
         mean_solve_s = statistics.mean(solve_ms) / 1000.0 if solve_ms else float(prof["solve_ms"]) / 1000.0
         achieved = bytes_per_step / mean_solve_s / 1e9 if mean_solve_s > 0 else 0.0
         roofline = {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                    "frac": achieved / peak, "peak_kind": peak_kind, "traffic": ncu_traffic_per_launch("k_solve"),
                     "algorithmic_bytes_per_launch": bytes_per_step / max(solve_launches, 1),
                     "algorithmic": "76 d + 136 + 48 c per executed manifold visit",
                     "launch_ms_avg": 1000.0 * mean_solve_s / max(solve_launches, 1),
