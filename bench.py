@@ -11,8 +11,10 @@ One step = ContactRefresher -> ForceUpdater -> Solver (prestep, warm start,
               steps by writing a 512 MiB buffer (the step's working set is
               below L2 size).
   e2e         the same metric through the C ABI with host records: every step
-              uploads bodies and manifolds from pinned host memory, steps and
-              downloads bodies and manifolds; host wall clock.
+              sends the bodies' state and the manifolds from pinned host memory
+              (bepugpu_update_bodies / bepugpu_update_manifolds, checked on the
+              device), steps, and downloads whole body and manifold records;
+              host wall clock.
   roofline    the solve kernel (k_solve): algorithmic bytes of the executed
               manifold visits (76 d + 136 + 48 c per visit, counted by a census
               before every sweep) / solve-phase device time from events captured
@@ -725,14 +727,14 @@ def main():
             pg.barrier()
         t0 = time.perf_counter()
         for _ in range(k):
-            space.upload_bodies(hb)
+            space.update_bodies(hb)
             space.update_manifolds(hm)
             space.step(DT, N.STEP_ALL)
             space.download_bodies(hb)
             space.download_constraints(hm)
         el = time.perf_counter() - t0
         h2d = hb.nbytes + hm.nbytes
-        d2h = 52 * len(hb) + 288 * len(hm)  # BodyOut and ManifoldOut records copied device -> host
+        d2h = hb.nbytes + hm.nbytes  # downloads copy whole body and manifold records
         e2e = {"value": world * cips * k / el, "unit": "contact-iters/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": 1000 * el / k}
 

@@ -84,16 +84,62 @@ __global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
     b.vang[i] = w;
 }
 
-__global__ void k_pack_bodies(BodySoA b, BodyOut* __restrict__ out) {
+// The state fields of the scene's device copy of the caller's body records
+// (kept since the upload): the download is then one copy of whole records,
+// their other fields exactly as uploaded.
+__global__ void k_patch_body_records(BodySoA b, bepugpu_body* __restrict__ rec) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= b.count) return;
     float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i];
-    BodyOut o;
-    o.p[0] = p.x; o.p[1] = p.y; o.p[2] = p.z;
-    o.q[0] = q.x; o.q[1] = q.y; o.q[2] = q.z; o.q[3] = q.w;
-    o.v[0] = v.x; o.v[1] = v.y; o.v[2] = v.z;
-    o.w[0] = w.x; o.w[1] = w.y; o.w[2] = w.z;
-    out[i] = o;
+    bepugpu_body& r = rec[i];
+    r.position[0] = p.x; r.position[1] = p.y; r.position[2] = p.z;
+    r.orientation[0] = q.x; r.orientation[1] = q.y; r.orientation[2] = q.z; r.orientation[3] = q.w;
+    r.linear_velocity[0] = v.x; r.linear_velocity[1] = v.y; r.linear_velocity[2] = v.z;
+    r.angular_velocity[0] = w.x; r.angular_velocity[1] = w.y; r.angular_velocity[2] = w.z;
+}
+
+// Checks of the update calls, before anything is written: check[0] receives
+// the lowest offending record index (stays INT_MAX when none), check[1] is set
+// when a kinematic body has a velocity.
+__device__ __forceinline__ bool SameWord(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+__global__ void k_check_body_records(const bepugpu_body* __restrict__ in, const bepugpu_body* __restrict__ kept, int n,
+                                     int* check) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bepugpu_body &r = in[i], &k = kept[i];
+    bool same = r.is_dynamic == k.is_dynamic && SameWord(r.inverse_mass, k.inverse_mass) &&
+                SameWord(r.linear_damping, k.linear_damping) && SameWord(r.angular_damping, k.angular_damping);
+    for (int q = 0; q < 9; q++) same = same && SameWord(r.local_inverse_inertia[q], k.local_inverse_inertia[q]);
+    if (!same) atomicMin(check, i);
+    if (!r.is_dynamic && (r.linear_velocity[0] != 0 || r.linear_velocity[1] != 0 || r.linear_velocity[2] != 0 ||
+                          r.angular_velocity[0] != 0 || r.angular_velocity[1] != 0 || r.angular_velocity[2] != 0))
+        atomicOr(check + 1, 1);
+}
+// The state fields of checked records into the body lanes and the kept records.
+__global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, BodySoA b, bepugpu_body* kept) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bepugpu_body& r = in[i];
+    bepugpu_body& k = kept[i];
+    float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i];
+    b.pos[i] = make_float4(r.position[0], r.position[1], r.position[2], p.w);
+    b.quat[i] = make_float4(r.orientation[0], r.orientation[1], r.orientation[2], r.orientation[3]);
+    b.vlin[i] = make_float4(r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2], v.w);
+    b.vang[i] = make_float4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2], w.w);
+    for (int q = 0; q < 3; q++) {
+        k.position[q] = r.position[q];
+        k.linear_velocity[q] = r.linear_velocity[q];
+        k.angular_velocity[q] = r.angular_velocity[q];
+    }
+    for (int q = 0; q < 4; q++) k.orientation[q] = r.orientation[q];
+}
+__global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
+                                         int n, ManifoldSoA m, int* check) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bepugpu_manifold& r = rec[i];
+    int4 h = m.head[slot_of[i]];
+    if (r.body_a != h.x || r.body_b != h.y || r.contact_count < 0 || r.contact_count > 4) atomicMin(check, i);
 }
 
 // Manifold records -> slots (slot_of[i] is the colour-order slot of record i).
@@ -542,6 +588,7 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     L.joffs = take(4 * (M + J + 2));
     L.groups = take(sizeof(GroupDesc) * M); L.groupBodies = take(4 * B); L.groupRefs = take(8 * M);
     L.groupOffsets = take(4 * (2 * M + 2)); L.sweepBodies = take(4 * B);
+    L.bodyRecords = take(sizeof(bepugpu_body) * B);
     arenaBytes = bytes;
     cudaError_t e = cudaMalloc(&arena, bytes);
     if (e != cudaSuccess) {
@@ -557,7 +604,6 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     Rebase();
     CK(cudaMemset(arena, 0, bytes));
     stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
-    stagingBytes = std::max(stagingBytes, sizeof(BodyOut) * B);
     CK(cudaMalloc(&staging, stagingBytes));
     CK(cudaMalloc(&counter, kScratchBytes));
     CK(cudaMemset(counter, 0, kScratchBytes));
@@ -595,6 +641,7 @@ void Scene::Rebase() {
     j.lanes = (float4*)(base + L.jlanes);
     j.state = (uint2*)(base + L.jstate);
     jointOffsetsDev = (int32_t*)(base + L.joffs);
+    bodyRecords = (bepugpu_body*)(base + L.bodyRecords);
 }
 
 // Moves the arena to pinned host memory and releases the scene's device
@@ -866,6 +913,28 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
 
 }  // namespace bepugpu
 
+namespace bepugpu {
+// Copies `n` records to the device, runs `check` over them and returns the
+// offending index (-1 when none) and the flag word.
+template <class Launch>
+bepugpu_status CheckRecords(Context* ctx, Scene* s, const void* rec, size_t bytes, Launch launch, int& bad,
+                                   int& flag) {
+    int* check = s->CheckWords();
+    CK(cudaMemcpyAsync(s->staging, rec, bytes, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(check, 0x7f, sizeof(int), s->stream));
+    CK(cudaMemsetAsync(check + 1, 0, sizeof(int), s->stream));
+    launch(check);
+    CK(cudaGetLastError());
+    int h[2];
+    CK(cudaMemcpyAsync(h, check, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    bad = h[0] == 0x7f7f7f7f ? -1 : h[0];
+    flag = h[1];
+    return BEPUGPU_OK;
+}
+
+}  // namespace bepugpu
+
 // ================================================================== C ABI ==
 using namespace bepugpu;
 
@@ -1062,8 +1131,8 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         if (lst != BEPUGPU_OK) return lst;
     }
     if (n) {
-        CK(cudaMemcpyAsync(s->staging, bodies, sizeof(bepugpu_body) * n, cudaMemcpyHostToDevice, s->stream));
-        k_unpack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging, (int)n, s->b);
+        CK(cudaMemcpyAsync(s->bodyRecords, bodies, sizeof(bepugpu_body) * n, cudaMemcpyHostToDevice, s->stream));
+        k_unpack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>(s->bodyRecords, (int)n, s->b);
         CK(cudaMemcpyAsync(s->localM33, s->hostLocalM33.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
         k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
         CK(cudaGetLastError());
@@ -1073,9 +1142,11 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
     return BEPUGPU_OK;
 }
 
-static bepugpu_status UploadManifoldRecords(Context* ctx, Scene* s, const bepugpu_manifold* rec, uint32_t n) {
+static bepugpu_status UploadManifoldRecords(Context* ctx, Scene* s, const bepugpu_manifold* rec, uint32_t n,
+                                            bool staged = false) {
     if (!n) return BEPUGPU_OK;
-    CK(cudaMemcpyAsync(s->staging, rec, sizeof(bepugpu_manifold) * n, cudaMemcpyHostToDevice, s->stream));
+    if (!staged)
+        CK(cudaMemcpyAsync(s->staging, rec, sizeof(bepugpu_manifold) * n, cudaMemcpyHostToDevice, s->stream));
     k_unpack_manifolds<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_manifold*)s->staging, s->slotOf,
                                                                (int)n, s->m);
     CK(cudaGetLastError());
@@ -1162,8 +1233,6 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         if (gst != BEPUGPU_OK) return gst;
     }
     s->hostSlotOf = plan.slotOf;
-    s->hostBodyA.assign(a.begin() + nj, a.end());
-    s->hostBodyB.assign(bb.begin() + nj, bb.end());
     s->maxBodyReferenced = -1;
     for (uint32_t u = 0; u < nm + nj; u++) s->maxBodyReferenced = std::max(s->maxBodyReferenced, std::max(a[u], bb[u]));
     {
@@ -1182,18 +1251,53 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
         ctx->SetError("update_manifolds needs the %d manifolds of the last upload", s->m.count);
         return BEPUGPU_INVALID_ARGUMENT;
     }
-    // The colouring is kept, so every manifold must still join the same bodies.
-    for (uint32_t i = 0; i < n; i++) {
-        if (man[i].body_a != s->hostBodyA[i] || man[i].body_b != s->hostBodyB[i]) {
-            ctx->SetError("manifold %u changed its bodies; use bepugpu_upload_constraints to recolour", i);
-            return BEPUGPU_INVALID_ARGUMENT;
-        }
-        if (man[i].contact_count < 0 || man[i].contact_count > 4) {
-            ctx->SetError("manifold %u has contact_count %d (0..4 allowed)", i, man[i].contact_count);
-            return BEPUGPU_INVALID_ARGUMENT;
-        }
+    if (!n) return BEPUGPU_OK;
+    // The colouring is kept, so every manifold must still join the same bodies:
+    // checked on the device against the stored slots before anything changes.
+    int bad = -1, flag = 0;
+    bepugpu_status st = CheckRecords(ctx, s, man, sizeof(bepugpu_manifold) * n, [&](int* check) {
+        k_check_manifold_records<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_manifold*)s->staging,
+                                                                         s->slotOf, (int)n, s->m, check);
+    }, bad, flag);
+    if (st != BEPUGPU_OK) return st;
+    if (bad >= 0) {
+        ctx->SetError("manifold %d changed its bodies or has a contact count outside 0..4; use "
+                      "bepugpu_upload_constraints to recolour", bad);
+        return BEPUGPU_INVALID_ARGUMENT;
     }
-    return UploadManifoldRecords(ctx, s, man, n);
+    return UploadManifoldRecords(ctx, s, man, n, true);
+}
+
+bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    if (n != (uint32_t)s->b.count || (n && !bodies)) {
+        ctx->SetError("update_bodies needs the %d bodies of the last upload", s->b.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (!n) return BEPUGPU_OK;
+    int bad = -1, moving = 0;
+    bepugpu_status st = CheckRecords(ctx, s, bodies, sizeof(bepugpu_body) * n, [&](int* check) {
+        k_check_body_records<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging,
+                                                                     s->bodyRecords, (int)n, check);
+    }, bad, moving);
+    if (st != BEPUGPU_OK) return st;
+    if (bad >= 0) {
+        ctx->SetError("body %d changed more than its state (position, orientation, velocities); use "
+                      "bepugpu_upload_bodies", bad);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    k_update_body_state<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging, (int)n, s->b,
+                                                                 s->bodyRecords);
+    k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
+    CK(cudaGetLastError());
+    if ((moving != 0) != s->kinematicMoving) {
+        s->kinematicMoving = moving != 0;
+        s->version++;
+    }
+    return BEPUGPU_OK;
 }
 
 bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_body* bodies, uint32_t n) {
@@ -1206,18 +1310,10 @@ bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_b
         return BEPUGPU_INVALID_ARGUMENT;
     }
     if (!n) return BEPUGPU_OK;
-    BodyOut* dev = (BodyOut*)s->staging;
-    k_pack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, dev);
-    s->hostBodyOut.resize(n);
-    CK(cudaMemcpyAsync(s->hostBodyOut.data(), dev, sizeof(BodyOut) * n, cudaMemcpyDeviceToHost, s->stream));
+    k_patch_body_records<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->bodyRecords);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(bodies, s->bodyRecords, sizeof(bepugpu_body) * n, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    for (uint32_t i = 0; i < n; i++) {
-        const BodyOut& o = s->hostBodyOut[i];
-        std::memcpy(bodies[i].position, o.p, sizeof(o.p));
-        std::memcpy(bodies[i].orientation, o.q, sizeof(o.q));
-        std::memcpy(bodies[i].linear_velocity, o.v, sizeof(o.v));
-        std::memcpy(bodies[i].angular_velocity, o.w, sizeof(o.w));
-    }
     return BEPUGPU_OK;
 }
 

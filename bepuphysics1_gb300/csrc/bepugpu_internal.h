@@ -16,12 +16,6 @@
 
 namespace bepugpu {
 
-// Compact body download record (device -> host), scattered into the caller's
-// records (manifold records are rebuilt whole on the device instead).
-struct BodyOut {
-    float p[3], q[4], v[3], w[3];
-};
-
 struct Context;
 struct BatchEngine;
 struct Scene;
@@ -75,10 +69,10 @@ int GroupLaunchCount(const GroupPlan& g);
 constexpr uint32_t kOwnedByGroup = 4u;
 
 // Layout of a scene's device scratch block (kScratchBytes): grid barrier
-// arrival counter, barrier generation, error word, census accumulators --
-// each on its own 128-byte line.
+// arrival counter, barrier generation, error word, record-check words, census
+// accumulators, timer stamps -- each on its own 128-byte line.
 constexpr size_t kScratchBytes = 1024;
-constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 256, kCensusAt = 512,
+constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 256, kCheckAt = 384, kCensusAt = 512,
                  kStampsAt = 640;
 
 // Byte offsets of a scene's device arrays inside its arena.
@@ -88,6 +82,7 @@ struct ArenaLayout {
         state, slot, offs;
     size_t jhead, jlanes, jstate, joffs;
     size_t groups, groupBodies, groupRefs, groupOffsets, sweepBodies;
+    size_t bodyRecords;
 };
 
 struct Server;
@@ -99,9 +94,9 @@ struct Scene {
     unsigned int* BarrierGeneration() const { return (unsigned int*)((char*)counter + kBarrierGenerationAt); }
     int* ErrorWord() const { return (int*)((char*)counter + kErrorAt); }
     unsigned long long* Census() const { return (unsigned long long*)((char*)counter + kCensusAt); }
+    int* CheckWords() const { return (int*)((char*)counter + kCheckAt); }  // record checks of update calls
     unsigned long long* Stamps() const { return (unsigned long long*)((char*)counter + kStampsAt); }
     int persistentBlocksPerSm = 1;
-    std::vector<int32_t> hostBodyA, hostBodyB;  // manifold body pairs of the last constraint upload
     int32_t maxBodyReferenced = -1;
     GroupPolicy policy;
     GroupPlan groupPlan;
@@ -152,6 +147,7 @@ struct Scene {
     std::vector<int32_t> jointOffsets;    // joint slot range per sweep colour
     std::vector<int32_t> hostJointSlotOf; // joint record -> slot
     int32_t* jointOffsetsDev = nullptr;
+    bepugpu_body* bodyRecords = nullptr;  // device copy of the last uploaded body records (downloads patch it)
     std::vector<float4> hostJointAcc;     // download scratch: [2][joints]
     Colouring colouring;
     std::vector<int32_t> manifoldOffsets;
@@ -159,7 +155,6 @@ struct Scene {
     std::vector<float> hostLinDamp, hostAngDamp, hostLocalM33;
     std::vector<uint8_t> hostDynamic;
     std::vector<float4> hostDamp;
-    std::vector<BodyOut> hostBodyOut;
     bool dampDirty = true;
     float dampDt = 0.f;
     cudaStream_t stream = nullptr;

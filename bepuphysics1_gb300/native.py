@@ -120,6 +120,7 @@ GPU_EXPORTS = {
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
+    "bepugpu_update_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_download_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_download_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_get_colouring": (_I, [_P, _I, _P, _P, _U, ctypes.POINTER(_U)]),

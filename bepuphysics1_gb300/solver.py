@@ -133,6 +133,11 @@ class GpuSpace:
         self.manifold_count = len(manifolds)
         self.joint_count = len(joints)
 
+    def update_bodies(self, bodies: np.ndarray):
+        """bepugpu_update_bodies: new position, orientation and velocities only."""
+        bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)
+        self.ctx.check(self.ctx.lib.bepugpu_update_bodies(self.ctx.handle, self.id, N.ptr(bodies), len(bodies)))
+
     def update_manifolds(self, manifolds: np.ndarray):
         manifolds = np.ascontiguousarray(manifolds, dtype=N.MANIFOLD_DTYPE)
         self.ctx.check(self.ctx.lib.bepugpu_update_manifolds(self.ctx.handle, self.id, N.ptr(manifolds),

@@ -219,12 +219,22 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* ctx, int32_t scene,
                                           const bepugpu_manifold* manifolds, uint32_t manifold_count,
                                           const bepugpu_joint* joints, uint32_t joint_count);
 /* Rewrites manifold records in place without recolouring.  Body pairs and the
- * manifold count must be those of the last bepugpu_upload_constraints. */
+ * manifold count must be those of the last bepugpu_upload_constraints (checked
+ * on the device before anything changes; INVALID_ARGUMENT otherwise). */
 bepugpu_status bepugpu_update_manifolds(bepugpu_context* ctx, int32_t scene,
                                         const bepugpu_manifold* manifolds, uint32_t count);
 
-/* Writes position, orientation and velocities into the caller's records
- * (their other fields are left as they are). */
+/* Per-step body update: only position, orientation and velocities may differ
+ * from the last bepugpu_upload_bodies (mass, inertia, damping and the dynamic
+ * flag are checked on the device before anything changes; INVALID_ARGUMENT
+ * otherwise).  The world inverse inertia follows the new orientation as on
+ * upload.  No reference counterpart: the reference's entities are the state. */
+bepugpu_status bepugpu_update_bodies(bepugpu_context* ctx, int32_t scene, const bepugpu_body* bodies,
+                                     uint32_t count);
+
+/* Writes whole body records: the fields as last uploaded, with position,
+ * orientation and velocities as they are now (one copy of the scene's device
+ * copy of the records). */
 bepugpu_status bepugpu_download_bodies(bepugpu_context* ctx, int32_t scene,
                                        bepugpu_body* bodies, uint32_t count);
 /* Writes whole manifold records, in upload order: the uploaded fields as they

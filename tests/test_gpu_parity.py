@@ -225,3 +225,46 @@ def test_manifold_records_roundtrip(gpu_context):
     back, _ = sp.download_constraints(np.zeros_like(m))
     assert back.tobytes() == m.tobytes()
     sp.close()
+
+
+def test_update_bodies_and_manifolds_per_step(gpu_context):
+    """The per-step update calls (device-checked) give the same bits as full
+    uploads, refuse records that change more than their state, and a kinematic
+    body set moving by an update is integrated."""
+    gpu_context.set_settings(default_settings())
+    b, m, _ = scenes.pile_1k()
+    full = GpuSpace(gpu_context, b, m)
+    fast = GpuSpace(gpu_context, b, m)
+    hb, hm = b.copy(), m.copy()
+    for _ in range(3):
+        full.upload_bodies(hb)
+        full.update_manifolds(hm)
+        fast.update_bodies(hb)
+        fast.update_manifolds(hm)
+        full.step(DT)
+        fast.step(DT)
+        hb = full.download_bodies(hb.copy())
+        hm = full.download_constraints(hm.copy())[0]
+        fb = fast.download_bodies(hb.copy())
+        fm = fast.download_constraints(hm.copy())[0]
+        assert fb.tobytes() == hb.tobytes() and fm.tobytes() == hm.tobytes()
+    bad = hb.copy()
+    bad["inverse_mass"][5] *= 2
+    with pytest.raises(N.ArgumentException):
+        fast.update_bodies(bad)
+    bad = hm.copy()
+    bad["body_b"][7] = bad["body_a"][7]
+    with pytest.raises(N.ArgumentException):
+        fast.update_manifolds(bad)
+    # the ground (kinematic, body 0) starts moving: integrated like the oracle does
+    moving = hb.copy()
+    moving["linear_velocity"][0] = (0.0, 0.5, 0.0)
+    fast.update_bodies(moving)
+    fast.step(DT)
+    ref = oracle.OracleSpace(default_settings(), moving, hm)
+    ref.set_list_order(fast.colouring()[1])
+    ref.step(DT, N.STEP_ALL, 1)
+    got = fast.download_bodies(moving.copy())
+    assert np.array_equal(got["position"], ref.get_bodies()["position"])
+    full.close()
+    fast.close()
