@@ -42,7 +42,7 @@ __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* 
     const GroupDesc g = sv.t.groups[w.y];
     for (int k = 0; k < w.z; k++) {
         if (k) __syncthreads();  // the previous step's write-back is visible to the next step's loads
-        GroupStep<false, kShared>(sv.m, sv.b, p, flags, sv.t, g, Bc, Lc, smem, nullptr);
+        GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr);
     }
 }
 
@@ -131,13 +131,12 @@ SceneView MakeView(const Scene& s) {
     v.t.bodies = s.groupBodiesDev;
     v.t.refs = s.groupRefsDev;
     v.t.colourOffsets = s.groupColourOffsetsDev;
+    v.t.jointRefs = nullptr;  // batched scenes hold no joints
+    v.t.jointColourOffsets = nullptr;
     return v;
 }
 
-bool Scene::BatchReady() const {
-    return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && jointCount == 0 && sweepDynamicCount == 0 &&
-           !kinematicMoving;
-}
+bool Scene::BatchReady() const { return SweepEmpty() && jointCount == 0; }
 
 }  // namespace bepugpu
 

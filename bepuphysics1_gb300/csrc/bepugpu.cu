@@ -319,8 +319,8 @@ __device__ __forceinline__ void WarmJointSlot(const JointSoA& j, const BodySoA& 
     if (!(st.x & kGroupActive)) return;
     int4 h = j.head[s];
     BodyState A, B;
-    LoadJointVelocity(b, h.x, A);
-    LoadJointVelocity(b, h.y, B);
+    LoadJointVelocityV(GlobalBodies{b}, h.x, A);
+    LoadJointVelocityV(GlobalBodies{b}, h.y, B);
     WarmJoint(j, s, A, B, st.x, h.z & 0xff);
     if (st.x & kDynA) StoreVelocity(b, h.x, A);
     if (st.x & kDynB) StoreVelocity(b, h.y, B);
@@ -330,8 +330,8 @@ __device__ __forceinline__ void SolveJointSlot(const JointSoA& j, const BodySoA&
     if (!(st.x & kGroupActive)) return;
     int4 h = j.head[s];
     BodyState A, B;
-    LoadJointVelocity(b, h.x, A);
-    LoadJointVelocity(b, h.y, B);
+    LoadJointVelocityV(GlobalBodies{b}, h.x, A);
+    LoadJointVelocityV(GlobalBodies{b}, h.y, B);
     SolveJoint(j, s, A, B, st, h.z & 0xff, p);
     if (st.x & kDynA) StoreVelocity(b, h.x, A);
     if (st.x & kDynB) StoreVelocity(b, h.y, B);
@@ -586,8 +586,12 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     L.slot = take(4 * M); L.offs = take(4 * (M + J + 2));
     L.jhead = take(16 * J); L.jlanes = take(16 * (size_t)kJointLanes * J); L.jstate = take(8 * J);
     L.joffs = take(4 * (M + J + 2));
-    L.groups = take(sizeof(GroupDesc) * M); L.groupBodies = take(4 * B); L.groupRefs = take(8 * M);
-    L.groupOffsets = take(4 * (2 * M + 2)); L.sweepBodies = take(4 * B);
+    // a group holds at least one manifold or joint: at most M + J groups
+    L.groups = take(sizeof(GroupDesc) * (M + J)); L.groupBodies = take(4 * B); L.groupRefs = take(8 * M);
+    // colour offset tables of groups: cCount + 1 entries a group, and a group's
+    // colours are at most its members, so 2 (M + J) + 2 entries suffice
+    L.groupOffsets = take(4 * (2 * (M + J) + 2)); L.sweepBodies = take(4 * B);
+    L.groupJointRefs = take(8 * J); L.groupJointOffsets = take(4 * (2 * (M + J) + 2));
     L.bodyRecords = take(sizeof(bepugpu_body) * B);
     arenaBytes = bytes;
     cudaError_t e = cudaMalloc(&arena, bytes);
@@ -637,6 +641,8 @@ void Scene::Rebase() {
     groupRefsDev = (int2*)(base + L.groupRefs);
     groupColourOffsetsDev = (int32_t*)(base + L.groupOffsets);
     sweepBodiesDev = (int32_t*)(base + L.sweepBodies);
+    groupJointRefsDev = (int2*)(base + L.groupJointRefs);
+    groupJointColourOffsetsDev = (int32_t*)(base + L.groupJointOffsets);
     j.head = (int4*)(base + L.jhead);
     j.lanes = (float4*)(base + L.jlanes);
     j.state = (uint2*)(base + L.jstate);
@@ -734,7 +740,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     // A scene whose whole step is island groups has nothing left for the sweep
     // path: no sweep manifolds or joints, no dynamic body outside the groups,
     // no moving kinematic body.  Its graph is the group launch alone.
-    phaseEvents = !(BatchReady());
+    phaseEvents = !SweepEmpty();
     if (!phaseEvents) {
         cudaGraph_t graph;
         cudaError_t e = cudaStreamEndCapture(stream, &graph);
@@ -774,10 +780,11 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
         k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[1], stream, cudaEventRecordExternal));
-    const int nj = j.count;
+    const JointSoA js = SweepJoints();
+    const int nj = js.count;
     bool solve = (flags & BEPUGPU_STEP_SOLVE) && (nm || nj);
     if (solve) {
-        if (nj) k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, stream>>>(ms, b, j, p);
+        if (nj) k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, stream>>>(ms, b, js, p);
         else k_prestep<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p);
         launchesPerStep++;
     }
@@ -787,7 +794,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
             int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
             int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
             if (j1 > j0) {
-                k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, j, b0, b1, j0, j1);
+                k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, b0, b1, j0, j1);
                 launchesPerStep++;
             } else if (b1 > b0) {
                 k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, b0, b1);
@@ -802,7 +809,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
                 int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
                 int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
                 if (j1 > j0) {
-                    k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, j, p, b0, b1, j0, j1);
+                    k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, p, b0, b1, j0, j1);
                     launchesPerStep++;
                 } else if (b1 > b0) {
                     k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1);
@@ -859,7 +866,7 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
     }
     CK(cudaEventRecord(evGroup[1], stream));
     PersistentArgs a;
-    a.m = SweepManifolds(); a.b = b; a.j = j; a.p = p;
+    a.m = SweepManifolds(); a.b = b; a.j = SweepJoints(); a.p = p;
     a.colourOffsets = colourOffsetsDev;
     a.jointOffsets = jointOffsetsDev;
     a.colours = SweepColours();
@@ -1190,28 +1197,17 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         ctx->SetError("a constraint references a body outside [0, %d)", nb);
         return BEPUGPU_INVALID_ARGUMENT;
     }
-    // Manifold slots: the colour-sweep part in colour-major order, then the
-    // island groups (groups.cu); the persistent mode keeps everything on the
-    // sweep path.
+    // Manifold and joint slots: the colour-sweep part in colour-major order,
+    // then the island groups (groups.cu); the persistent mode keeps everything
+    // on the sweep path.
     GroupPolicy pol = s->policy;
     if (s->mode == BEPUGPU_MODE_PERSISTENT) pol.enabled = false;
     PlanGroups(pol, a.data(), bb.data(), s->colouring.colour.data(), (int32_t)nj, (int32_t)nm,
-               s->hostDynamic.data(), nb, s->groupPlan);
+               s->hostDynamic.data(), nb, s->colouring.colours, s->groupPlan);
     const GroupPlan& plan = s->groupPlan;
     s->manifoldOffsets = plan.globalOffsets;
-    {  // joint slots: colour-major, list order inside a colour; every joint is on the sweep path
-        const int colours = (int)plan.globalOffsets.size() - 1;
-        std::vector<std::vector<int32_t>> byColour(std::max(colours, 0));
-        for (uint32_t u = 0; u < nj; u++) byColour[s->colouring.colour[u]].push_back((int32_t)u);
-        s->jointOffsets.assign(colours + 1, 0);
-        s->hostJointSlotOf.assign(nj, -1);
-        int32_t slot = 0;
-        for (int c = 0; c < colours; c++) {
-            s->jointOffsets[c] = slot;
-            for (int32_t u : byColour[c]) s->hostJointSlotOf[u] = slot++;
-        }
-        s->jointOffsets[colours] = slot;
-    }
+    s->jointOffsets = plan.jointGlobalOffsets;
+    s->hostJointSlotOf = plan.jointSlotOf;
     s->hostOwned.assign(nb, 0);
     for (int32_t e = 0; e < nb && e < (int32_t)plan.localOf.size(); e++) s->hostOwned[e] = plan.localOf[e] >= 0;
     {
@@ -1533,17 +1529,18 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     if ((flags & BEPUGPU_STEP_FORCES) && nb) {
         cudaEvent_t a = mark(); k_force<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->force_ms});
     }
-    const int nj = s->j.count;
+    const JointSoA js = s->SweepJoints();
+    const int nj = js.count;
     if ((flags & BEPUGPU_STEP_SOLVE) && (nm || nj)) {
         cudaEvent_t a = mark();
-        k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, q>>>(ms, s->b, s->j, p);
+        k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, q>>>(ms, s->b, js, p);
         spans.push_back({a, mark(), &out->prestep_ms});
         for (int cc = 0; cc < colours; cc++) {
             int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
             int j0 = nj ? s->jointOffsets[cc] : 0, j1 = nj ? s->jointOffsets[cc + 1] : 0;
             if (b1 - b0 + j1 - j0 <= 0) continue;
             cudaEvent_t e0 = mark();
-            k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, s->j, b0, b1, j0, j1);
+            k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, js, b0, b1, j0, j1);
             spans.push_back({e0, mark(), &out->warm_ms});
             out->warm_launches++;
         }
@@ -1554,7 +1551,7 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
                 if (b1 - b0 + j1 - j0 <= 0) continue;
                 if (b1 > b0) k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, b0, b1, acc);
                 cudaEvent_t e0 = mark();
-                k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, s->j, p, b0, b1, j0, j1);
+                k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, js, p, b0, b1, j0, j1);
                 spans.push_back({e0, mark(), &out->solve_ms});
                 out->solve_launches++;
             }

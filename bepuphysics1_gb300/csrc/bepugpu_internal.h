@@ -27,13 +27,17 @@ struct GroupDesc {
     int32_t mBegin, mEnd;   // manifold slots
     int32_t bBegin, bEnd;   // entries of the group body list
     int32_t cBegin, cCount; // colour offsets (relative to mBegin) in the offsets table
-    int32_t pad0, pad1;
+    int32_t jBegin, jEnd;   // joint slots
+    int32_t jcBegin;        // joint colour offsets (relative to jBegin), cCount + 1 entries
+    int32_t pad0, pad1, pad2;
 };
 struct GroupTables {
     const GroupDesc* groups;
     const int32_t* bodies;        // global indices of each group's dynamic bodies
     const int2* refs;             // per manifold slot: body refs inside the group kernel
     const int32_t* colourOffsets;
+    const int2* jointRefs;        // per joint slot: body refs (-1 = the world entity)
+    const int32_t* jointColourOffsets;
 };
 struct GroupPolicy {
     bool enabled = true;
@@ -44,20 +48,29 @@ struct GroupPolicy {
 };
 // Groups [begin, end) of one kernel variant and the sizes its launch needs.
 struct GroupClass {
-    int32_t begin = 0, end = 0, maxLocal = 0, maxManifolds = 0, maxColourMembers = 0;
+    int32_t begin = 0, end = 0, maxLocal = 0, maxManifolds = 0, maxColourMembers = 0, maxJoints = 0;
 };
 struct GroupPlan {
-    std::vector<GroupDesc> groups;  // groups whose solve lanes fit shared memory first
+    // groups in launch order: without joints (manifold lanes in shared memory,
+    // then in global memory), then with joints (the same two kinds); each kind
+    // is one launch sized for its own largest group
+    std::vector<GroupDesc> groups;
     std::vector<int32_t> groupBodies, localOf, groupOfManifold, slotOf, globalOffsets, colourOffsets;
     std::vector<int2> refs;  // per slot
     int32_t globalCount = 0;
-    GroupClass shared, global;
+    GroupClass shared, global, sharedJoints, globalJoints;
+    // joints: slots (sweep part first, then the groups'), sweep colour offsets,
+    // group colour offsets and refs per slot
+    std::vector<int32_t> jointSlotOf, jointGlobalOffsets, jointColourOffsets;
+    std::vector<int2> jointRefs;
+    int32_t jointGlobalCount = 0;
+    bool groupJoints = false;  // some group holds joints
 };
 // Shared memory a group may use: 96 bytes per body, plus 400 per manifold when
 // its solve lanes live there.
 constexpr size_t kGroupSmemBudget = 200 * 1024;
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
-                int32_t nm, const uint8_t* dynamic, int32_t nb, GroupPlan& plan);
+                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan);
 bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
 // Joints (joints.cu): record checks, upload into the scene's joint slots, and
 // the accumulated impulses back into records.
@@ -82,6 +95,7 @@ struct ArenaLayout {
         state, slot, offs;
     size_t jhead, jlanes, jstate, joffs;
     size_t groups, groupBodies, groupRefs, groupOffsets, sweepBodies;
+    size_t groupJointRefs, groupJointOffsets;
     size_t bodyRecords;
 };
 
@@ -104,14 +118,28 @@ struct Scene {
     int32_t* groupBodiesDev = nullptr;
     int2* groupRefsDev = nullptr;
     int32_t* groupColourOffsetsDev = nullptr;
+    int2* groupJointRefsDev = nullptr;
+    int32_t* groupJointColourOffsetsDev = nullptr;
     std::vector<uint8_t> hostOwned;  // body stepped by a group kernel
     int32_t* sweepBodiesDev = nullptr;  // bodies no group steps (valid when groups exist)
     uint32_t sweepBodyCount = 0;
     uint32_t sweepDynamicCount = 0;     // dynamic bodies among them
     bool kinematicMoving = false;       // a kinematic body has a velocity
     bool asyncPending = false;          // a one-scene step may still run on `stream`
-    // The whole step is island groups, so a batched launch can run it (batch.cu).
+    // Nothing is left for the colour-sweep path: every constraint and dynamic
+    // body is in an island group and no kinematic body moves.
+    bool SweepEmpty() const {
+        return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && groupPlan.jointGlobalCount == 0 &&
+               sweepDynamicCount == 0 && !kinematicMoving;
+    }
+    // The whole step is island groups without joints, so a batched launch can run it (batch.cu).
     bool BatchReady() const;
+    // The colour-sweep part of the joint list: slots [0, jointGlobalCount).
+    JointSoA SweepJoints() const {
+        JointSoA s = j;
+        s.count = groupPlan.jointGlobalCount;
+        return s;
+    }
     int groupThreadsOverride = 0;    // 0 = derived from the plan
     bool phaseEvents = true;         // the step graph records the sweep-path phase events
     bool planStale = false;          // dynamic flags changed since the constraints were planned

@@ -26,12 +26,12 @@
 
 namespace bepugpu {
 
-template <bool kCensus, bool kShared>
-__global__ void k_groups(ManifoldSoA m, BodySoA b, StepParams p, uint32_t flags, GroupTables t, int groupBase,
-                         int Bc, int Lc, unsigned long long* census) {
+template <bool kCensus, bool kShared, bool kJoints>
+__global__ void k_groups(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, uint32_t flags, GroupTables t,
+                         int groupBase, int Bc, int Lc, int Jc, unsigned long long* census) {
     extern __shared__ float4 smem[];
     const GroupDesc g = t.groups[groupBase + blockIdx.x];
-    GroupStep<kCensus, kShared>(m, b, p, flags, t, g, Bc, Lc, smem, census);
+    GroupStep<kCensus, kShared, kJoints>(m, b, j, p, flags, t, g, Bc, Lc, Jc, smem, census);
 }
 
 // ------------------------------------------------------------------ host side --
@@ -54,59 +54,66 @@ struct UnionFind {
 };
 }  // namespace
 
-// Splits the manifold list into the colour-sweep part and island groups and
-// assigns every manifold its slot.  colour[u] is the solver-list colouring
-// (joints first).  The sweep part takes slots [0, globalCount) in colour-major
-// order; each group takes a contiguous range in colour-major order.
+// Splits the solver list into the colour-sweep part and island groups and
+// assigns every manifold and joint its slot.  colour[u] is the solver-list
+// colouring (joints first, u < nj).  The sweep part takes manifold slots
+// [0, globalCount) and joint slots [0, jointGlobalCount) in colour-major
+// order; each group takes a contiguous manifold range and a contiguous joint
+// range, each in colour-major order.
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
-                int32_t nm, const uint8_t* dynamic, int32_t nb, GroupPlan& plan) {
+                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan) {
     plan = GroupPlan();
-    const int32_t* mc = colour + nj;  // manifold colours
-    std::vector<int32_t> groupOfManifold(nm, -1);
+    const int32_t n = nj + nm;
+    std::vector<int32_t> groupOf(n, -1);  // per updateable
     std::vector<std::vector<int32_t>> gBodies;
     plan.localOf.assign(nb, -1);
-    if (pol.enabled && nm > 0) {
+    if (pol.enabled && n > 0) {
         UnionFind uf(nb);
-        for (int32_t u = 0; u < nj + nm; u++)
+        for (int32_t u = 0; u < n; u++)
             if (a[u] >= 0 && b[u] >= 0 && dynamic[a[u]] && dynamic[b[u]]) uf.Join(a[u], b[u]);
-        std::vector<int32_t> idOfRoot(nb, -1), manifolds, bodiesCount, islandOf(nm, -1);
-        std::vector<uint8_t> jointTouched(nb, 0);
-        for (int32_t u = 0; u < nj; u++)  // islands holding a joint stay on the sweep path
-            for (int32_t e : {a[u], b[u]})
-                if (e >= 0 && dynamic[e]) jointTouched[uf.Find(e)] = 1;
-        for (int32_t i = 0; i < nm; i++) {
-            int32_t ea = a[nj + i], eb = b[nj + i];
+        std::vector<int32_t> idOfRoot(nb, -1), members, bodiesCount, islandOf(n, -1);
+        for (int32_t u = 0; u < n; u++) {
+            int32_t ea = a[u], eb = b[u];
             int32_t e = ea >= 0 && dynamic[ea] ? ea : (eb >= 0 && dynamic[eb] ? eb : -1);
             if (e < 0) continue;  // no dynamic body: never active, sweep path
             int32_t root = uf.Find(e);
-            if (jointTouched[root]) continue;
             if (idOfRoot[root] < 0) {
-                idOfRoot[root] = (int32_t)manifolds.size();
-                manifolds.push_back(0);
+                idOfRoot[root] = (int32_t)members.size();
+                members.push_back(0);
                 bodiesCount.push_back(0);
             }
-            islandOf[i] = idOfRoot[root];
-            manifolds[islandOf[i]]++;
+            islandOf[u] = idOfRoot[root];
+            members[islandOf[u]]++;
         }
         for (int32_t e = 0; e < nb; e++)
             if (dynamic[e] && idOfRoot[uf.Find(e)] >= 0) bodiesCount[idOfRoot[uf.Find(e)]]++;
         // islands too large for one CTA stay on the sweep path
-        std::vector<uint8_t> small(manifolds.size());
-        for (size_t k = 0; k < manifolds.size(); k++)
-            small[k] = bodiesCount[k] <= pol.maxGroupBodies && manifolds[k] <= pol.maxGroupManifolds;
-        // pack small islands into groups in island order
-        std::vector<int32_t> groupOfIsland(manifolds.size(), -1);
-        int32_t gm = 0, gb = 0, groups = 0;
-        for (size_t k = 0; k < manifolds.size(); k++) {
+        std::vector<uint8_t> small(members.size());
+        // joints keep their solve lanes in shared memory: an island's bodies and
+        // joints must fit a CTA's budget
+        std::vector<int32_t> jointsOf(members.size(), 0);
+        for (int32_t u = 0; u < nj; u++)
+            if (islandOf[u] >= 0) jointsOf[islandOf[u]]++;
+        auto fitsCta = [&](int64_t bodies, int64_t joints) {
+            return GroupSmemBytes(false, (int)bodies, 0, (int)joints) <= kGroupSmemBudget;
+        };
+        for (size_t k = 0; k < members.size(); k++)
+            small[k] = bodiesCount[k] <= pol.maxGroupBodies && members[k] <= pol.maxGroupManifolds &&
+                       fitsCta(bodiesCount[k], jointsOf[k]);
+        // pack small islands into groups in island order (joints count like manifolds)
+        std::vector<int32_t> groupOfIsland(members.size(), -1);
+        int32_t gm = 0, gb = 0, gj = 0, groups = 0;
+        for (size_t k = 0; k < members.size(); k++) {
             if (!small[k]) continue;
-            if (groups == 0 || gm + manifolds[k] > pol.targetGroupManifolds ||
-                gb + bodiesCount[k] > pol.maxGroupBodies) {
+            if (groups == 0 || gm + members[k] > pol.targetGroupManifolds || gb + bodiesCount[k] > pol.maxGroupBodies ||
+                !fitsCta(gb + bodiesCount[k], gj + jointsOf[k])) {
                 groups++;
-                gm = gb = 0;
+                gm = gb = gj = 0;
             }
             groupOfIsland[k] = groups - 1;
-            gm += manifolds[k];
+            gm += members[k];
             gb += bodiesCount[k];
+            gj += jointsOf[k];
         }
         gBodies.resize(groups);
         for (int32_t e = 0; e < nb; e++) {
@@ -116,76 +123,103 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
             plan.localOf[e] = (int32_t)gBodies[groupOfIsland[id]].size();
             gBodies[groupOfIsland[id]].push_back(e);
         }
-        for (int32_t i = 0; i < nm; i++)
-            if (islandOf[i] >= 0) groupOfManifold[i] = groupOfIsland[islandOf[i]];
+        for (int32_t u = 0; u < n; u++)
+            if (islandOf[u] >= 0) groupOf[u] = groupOfIsland[islandOf[u]];
     }
     const int32_t G = (int32_t)gBodies.size();
-    std::vector<std::vector<int32_t>> members(G);
-    for (int32_t i = 0; i < nm; i++)
-        if (groupOfManifold[i] >= 0) members[groupOfManifold[i]].push_back(i);
-    // groups whose solve lanes fit shared memory run the shared variant; they come first
+    std::vector<std::vector<int32_t>> mMembers(G), jMembers(G);
+    for (int32_t u = 0; u < n; u++)
+        if (groupOf[u] >= 0) (u < nj ? jMembers : mMembers)[groupOf[u]].push_back(u);
+    // Launch order by kind: no joints before joints, shared-memory manifold
+    // lanes before global ones (kind 0..3), stable inside a kind.
     std::vector<int32_t> order(G);
     std::iota(order.begin(), order.end(), 0);
-    std::vector<uint8_t> fits(G);
-    for (int32_t gId = 0; gId < G; gId++)
-        fits[gId] = GroupSmemBytes(true, (int)gBodies[gId].size(), (int)members[gId].size()) <=
-                    std::min<size_t>(pol.sharedLanesBudget, kGroupSmemBudget);
-    std::stable_partition(order.begin(), order.end(), [&](int32_t gId) { return fits[gId] != 0; });
+    std::vector<uint8_t> fits(G), kind(G);
+    for (int32_t gId = 0; gId < G; gId++) {
+        fits[gId] = GroupSmemBytes(true, (int)gBodies[gId].size(), (int)mMembers[gId].size(),
+                                   (int)jMembers[gId].size()) <= std::min<size_t>(pol.sharedLanesBudget, kGroupSmemBudget);
+        kind[gId] = (uint8_t)((jMembers[gId].empty() ? 0 : 2) + (fits[gId] ? 0 : 1));
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return kind[x] < kind[y]; });
+    GroupClass* classes[4] = {&plan.shared, &plan.global, &plan.sharedJoints, &plan.globalJoints};
 
-    // Slots: the sweep part, then the groups in launch order.
-    int32_t colours = 0;  // the sweep covers every colour of the list (joints sweep too)
-    for (int32_t u = 0; u < nj + nm; u++) colours = std::max(colours, colour[u] + 1);
+    // Sweep slots, colour-major: manifolds and joints not in a group.
     plan.slotOf.assign(nm, -1);
+    plan.jointSlotOf.assign(nj, -1);
     plan.globalOffsets.assign(colours + 1, 0);
-    int32_t slot = 0;
+    plan.jointGlobalOffsets.assign(colours + 1, 0);
+    int32_t slot = 0, jslot = 0;
     {
         std::vector<std::vector<int32_t>> byColour(colours);
-        for (int32_t i = 0; i < nm; i++)
-            if (groupOfManifold[i] < 0) byColour[mc[i]].push_back(i);
+        for (int32_t u = 0; u < n; u++)
+            if (groupOf[u] < 0) byColour[colour[u]].push_back(u);
         for (int32_t c = 0; c < colours; c++) {
             plan.globalOffsets[c] = slot;
-            for (int32_t i : byColour[c]) plan.slotOf[i] = slot++;
+            plan.jointGlobalOffsets[c] = jslot;
+            for (int32_t u : byColour[c]) {
+                if (u < nj) plan.jointSlotOf[u] = jslot++;
+                else plan.slotOf[u - nj] = slot++;
+            }
         }
         plan.globalOffsets[colours] = slot;
+        plan.jointGlobalOffsets[colours] = jslot;
         plan.globalCount = slot;
+        plan.jointGlobalCount = jslot;
     }
     plan.refs.assign(nm, make_int2(-1, -1));
+    plan.jointRefs.assign(nj, make_int2(-1, -1));
     plan.groupOfManifold.assign(nm, -1);
     plan.groups.resize(G);
+    auto ref = [&](int32_t e) -> int32_t {
+        if (e < 0) return -1;
+        return dynamic[e] ? plan.localOf[e] : -2 - e;
+    };
     for (int32_t k = 0; k < G; k++) {
         const int32_t gId = order[k];
         GroupDesc& d = plan.groups[k];
-        GroupClass& cls = fits[gId] ? plan.shared : plan.global;
+        d = GroupDesc{};
+        GroupClass& cls = *classes[kind[gId]];
         if (cls.end == cls.begin) cls.begin = cls.end = k;
         cls.end = k + 1;
         d.bBegin = (int32_t)plan.groupBodies.size();
         plan.groupBodies.insert(plan.groupBodies.end(), gBodies[gId].begin(), gBodies[gId].end());
         d.bEnd = (int32_t)plan.groupBodies.size();
         cls.maxLocal = std::max(cls.maxLocal, d.bEnd - d.bBegin);
-        cls.maxManifolds = std::max(cls.maxManifolds, (int32_t)members[gId].size());
+        cls.maxManifolds = std::max(cls.maxManifolds, (int32_t)mMembers[gId].size());
+        cls.maxJoints = std::max(cls.maxJoints, (int32_t)jMembers[gId].size());
         int32_t gc = 0;
-        for (int32_t i : members[gId]) gc = std::max(gc, mc[i] + 1);
-        std::vector<std::vector<int32_t>> byColour(gc);
-        for (int32_t i : members[gId]) byColour[mc[i]].push_back(i);
+        for (int32_t u : mMembers[gId]) gc = std::max(gc, colour[u] + 1);
+        for (int32_t u : jMembers[gId]) gc = std::max(gc, colour[u] + 1);
+        std::vector<std::vector<int32_t>> mByColour(gc), jByColour(gc);
+        for (int32_t u : mMembers[gId]) mByColour[colour[u]].push_back(u - nj);
+        for (int32_t u : jMembers[gId]) jByColour[colour[u]].push_back(u);
+        d.cCount = gc;
         d.mBegin = slot;
         d.cBegin = (int32_t)plan.colourOffsets.size();
-        d.cCount = gc;
+        d.jBegin = jslot;
+        d.jcBegin = (int32_t)plan.jointColourOffsets.size();
         for (int32_t c = 0; c < gc; c++) {
             plan.colourOffsets.push_back(slot - d.mBegin);
-            cls.maxColourMembers = std::max(cls.maxColourMembers, (int32_t)byColour[c].size());
-            for (int32_t i : byColour[c]) {
+            plan.jointColourOffsets.push_back(jslot - d.jBegin);
+            cls.maxColourMembers = std::max(
+                cls.maxColourMembers, (int32_t)std::max(mByColour[c].size(), jByColour[c].size()));
+            for (int32_t i : mByColour[c]) {
                 plan.slotOf[i] = slot;
                 plan.groupOfManifold[i] = k;
-                auto ref = [&](int32_t e) -> int32_t {
-                    if (e < 0) return -1;
-                    return dynamic[e] ? plan.localOf[e] : -2 - e;
-                };
                 plan.refs[slot] = make_int2(ref(a[nj + i]), ref(b[nj + i]));
                 slot++;
             }
+            for (int32_t u : jByColour[c]) {
+                plan.jointSlotOf[u] = jslot;
+                plan.jointRefs[jslot] = make_int2(ref(a[u]), ref(b[u]));
+                jslot++;
+            }
         }
         plan.colourOffsets.push_back(slot - d.mBegin);
+        plan.jointColourOffsets.push_back(jslot - d.jBegin);
         d.mEnd = slot;
+        d.jEnd = jslot;
+        if (d.jEnd > d.jBegin) plan.groupJoints = true;
     }
 }
 
@@ -201,6 +235,11 @@ bepugpu_status Scene::UploadGroups(Context* ctx) {
                              stream)) ||
         (e = cudaMemcpyAsync(groupColourOffsetsDev, g.colourOffsets.data(), sizeof(int32_t) * g.colourOffsets.size(),
                              cudaMemcpyHostToDevice, stream)) ||
+        (!g.jointRefs.empty() &&
+         (e = cudaMemcpyAsync(groupJointRefsDev, g.jointRefs.data(), sizeof(int2) * g.jointRefs.size(),
+                              cudaMemcpyHostToDevice, stream))) ||
+        (e = cudaMemcpyAsync(groupJointColourOffsetsDev, g.jointColourOffsets.data(),
+                             sizeof(int32_t) * g.jointColourOffsets.size(), cudaMemcpyHostToDevice, stream)) ||
         (e = cudaStreamSynchronize(stream))) {
         ctx->SetError("group tables: %s", cudaGetErrorString(e));
         return BEPUGPU_CUDA_ERROR;
@@ -215,17 +254,18 @@ int ClassThreads(const GroupClass& c, int override_) {
     return std::min(std::max(t, 32), 256);
 }
 
-template <bool kShared>
+template <bool kShared, bool kJoints>
 bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const StepParams& p, uint32_t flags,
                            bool count, GroupTables t) {
     if (c.end <= c.begin) return BEPUGPU_OK;
-    const int Bc = std::max(c.maxLocal, 1), Lc = std::max(c.maxManifolds, 1);
-    size_t smemBytes = GroupSmemBytes(kShared, Bc, Lc);
+    const int Bc = std::max(c.maxLocal, 1), Lc = std::max(c.maxManifolds, 1), Jc = std::max(c.maxJoints, 1);
+    size_t smemBytes = GroupSmemBytes(kShared, Bc, Lc, kJoints ? Jc : 0);
     cudaError_t e = cudaSuccess;
     if (smemBytes > 48 * 1024) {
-        e = cudaFuncSetAttribute(k_groups<false, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
+        e = cudaFuncSetAttribute(k_groups<false, kShared, kJoints>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smemBytes);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_groups<true, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            e = cudaFuncSetAttribute(k_groups<true, kShared, kJoints>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smemBytes);
         if (e != cudaSuccess) {
             ctx->SetError("group kernel shared memory %zu bytes: %s", smemBytes, cudaGetErrorString(e));
@@ -235,11 +275,11 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
     const int threads = ClassThreads(c, s->groupThreadsOverride);
     const unsigned blocks = (unsigned)(c.end - c.begin);
     if (count)
-        k_groups<true, kShared><<<blocks, threads, smemBytes, s->stream>>>(s->m, s->b, p, flags, t, c.begin, Bc, Lc,
-                                                                            s->Census());
+        k_groups<true, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census());
     else
-        k_groups<false, kShared><<<blocks, threads, smemBytes, s->stream>>>(s->m, s->b, p, flags, t, c.begin, Bc, Lc,
-                                                                             nullptr);
+        k_groups<false, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         ctx->SetError("group kernel launch: %s", cudaGetErrorString(e));
@@ -250,7 +290,9 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
 }  // namespace
 
 int GroupLaunchCount(const GroupPlan& g) {
-    return (g.shared.end > g.shared.begin ? 1 : 0) + (g.global.end > g.global.begin ? 1 : 0);
+    int n = 0;
+    for (const GroupClass* c : {&g.shared, &g.global, &g.sharedJoints, &g.globalJoints}) n += c->end > c->begin;
+    return n;
 }
 
 bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count) {
@@ -261,9 +303,13 @@ bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_
     t.bodies = s->groupBodiesDev;
     t.refs = s->groupRefsDev;
     t.colourOffsets = s->groupColourOffsetsDev;
-    bepugpu_status st = LaunchClass<true>(ctx, s, g.shared, p, flags, count, t);
-    if (st != BEPUGPU_OK) return st;
-    return LaunchClass<false>(ctx, s, g.global, p, flags, count, t);
+    t.jointRefs = s->groupJointRefsDev;
+    t.jointColourOffsets = s->groupJointColourOffsetsDev;
+    bepugpu_status st = LaunchClass<true, false>(ctx, s, g.shared, p, flags, count, t);
+    if (st == BEPUGPU_OK) st = LaunchClass<false, false>(ctx, s, g.global, p, flags, count, t);
+    if (st == BEPUGPU_OK) st = LaunchClass<true, true>(ctx, s, g.sharedJoints, p, flags, count, t);
+    if (st == BEPUGPU_OK) st = LaunchClass<false, true>(ctx, s, g.globalJoints, p, flags, count, t);
+    return st;
 }
 
 }  // namespace bepugpu

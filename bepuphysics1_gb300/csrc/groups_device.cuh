@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include "bepugpu_internal.h"
+#include "joints_device.cuh"
 #include "solver_device.cuh"
 
 namespace bepugpu {
@@ -27,16 +28,22 @@ struct GroupBodies {
 };
 
 // Shared memory of one CTA: 6 body lanes per body; with kShared also 24 float4
-// lanes, a state word and a ref pair per manifold (400 bytes).
-__host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int manifolds) {
-    return 96 * (size_t)bodies + (shared ? 400 * (size_t)manifolds : 0);
+// lanes, a state word and a ref pair per manifold (400 bytes); with joints the
+// joints' solve lanes, state and refs (kJointSmemBytes each).
+__host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int manifolds, int joints = 0) {
+    return 96 * (size_t)bodies + (shared ? 400 * (size_t)manifolds : 0) + (size_t)kJointSmemBytes * joints;
 }
 
 // One step of group g by the calling CTA (the body of the group kernels).
 // smem holds GroupSmemBytes(kShared, Bc, Lc) bytes.
-template <bool kCensus, bool kShared>
-__device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const StepParams& p, uint32_t flags,
-                                          const GroupTables& t, const GroupDesc& g, int Bc, int Lc, float4* smem,
+// With kJoints the group's joints (slots [jBegin, jEnd)) are prestepped beside
+// the manifolds into shared-memory solve lanes (Jc per lane) and swept colour
+// by colour with them -- a colour's joints and manifolds share no dynamic
+// body -- and their impulses go back to the joint lanes after the sweeps.
+template <bool kCensus, bool kShared, bool kJoints>
+__device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const JointSoA& jt,
+                                          const StepParams& p, uint32_t flags, const GroupTables& t,
+                                          const GroupDesc& g, int Bc, int Lc, int Jc, float4* smem,
                                           unsigned long long* census) {
     const int nLocal = g.bEnd - g.bBegin, nm = g.mEnd - g.mBegin;
     GroupBodies bv;
@@ -71,6 +78,18 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
         ml.state = (uint2*)(lanes + 24 * Lc);
         sRefs = (int2*)(ml.state + Lc);
         ml.capacity = Lc;
+    }
+    // Joint solve lanes after the bodies and manifold lanes.
+    JointSoA jl{};
+    int2* jRefs = nullptr;
+    const int nj = g.jEnd - g.jBegin;
+    if (kJoints) {
+        float4* jbase = smem + 6 * Bc + (kShared ? 25 * Lc : 0);
+        jl.lanes = jbase;
+        jl.capacity = Jc;
+        jl.state = (uint2*)(jbase + kJSolveLanes * Jc);
+        jRefs = (int2*)(jl.state + Jc);
+        jl.count = nj;
     }
     const int tid = threadIdx.x, T = blockDim.x;
     const int lbase = kShared ? 0 : g.mBegin;  // slot of local manifold 0 in ml
@@ -113,11 +132,30 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
             atomicAdd(census + 3, kShared ? 136ull + 64ull * c4 : 288ull + 112ull * c4);
         }
     }
+    if (kJoints && (flags & BEPUGPU_STEP_SOLVE))
+        for (int q = tid; q < nj; q += T) {
+            const int2 r = t.jointRefs[g.jBegin + q];
+            jRefs[q] = r;
+            PrestepJointIO(jt, g.jBegin + q, jl, q, bv, r.x, r.y, p);
+        }
     if (kCensus && tid == 0) atomicAdd(census + 3, 208ull * (unsigned long long)nLocal);  // 7 lanes in, 6 out
     __syncthreads();
     if (flags & BEPUGPU_STEP_SOLVE) {
         const int* co = t.colourOffsets + g.cBegin;
+        const int* jco = kJoints ? t.jointColourOffsets + g.jcBegin : nullptr;
         for (int c = 0; c < g.cCount; c++) {
+            if (kJoints)
+                for (int q = jco[c] + tid; q < jco[c + 1]; q += T) {
+                    const uint2 st = jl.state[q];
+                    if (!(st.x & kGroupActive)) continue;
+                    const int2 r = jRefs[q];
+                    BodyState A, B;
+                    LoadJointVelocityV(bv, r.x, A);
+                    LoadJointVelocityV(bv, r.y, B);
+                    WarmJoint(jl, q, A, B, st.x, JointType(st.x));
+                    if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
+                    if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
+                }
             for (int j = co[c] + tid; j < co[c + 1]; j += T) {
                 const int sl = lbase + j;
                 uint2 st = ml.state[sl];
@@ -134,6 +172,19 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
         }
         for (int it = 0; it < p.iterationLimit; it++)
             for (int c = 0; c < g.cCount; c++) {
+                if (kJoints)
+                    for (int q = jco[c] + tid; q < jco[c + 1]; q += T) {
+                        uint2 st = jl.state[q];
+                        if (!(st.x & kGroupActive)) continue;
+                        const int2 r = jRefs[q];
+                        BodyState A, B;
+                        LoadJointVelocityV(bv, r.x, A);
+                        LoadJointVelocityV(bv, r.y, B);
+                        SolveJoint(jl, q, A, B, st, JointType(st.x), p);
+                        if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
+                        if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
+                        jl.state[q] = st;
+                    }
                 for (int j = co[c] + tid; j < co[c + 1]; j += T) {
                     const int sl = lbase + j;
                     uint2 st = ml.state[sl];
@@ -155,6 +206,11 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
                     ml.state[sl] = st;
                 }
                 __syncthreads();
+            }
+        if (kJoints)  // joint impulses back to the joint lanes
+            for (int q = tid; q < nj; q += T) {
+                jt.L(kJACC0, g.jBegin + q) = jl.L(kJACC0, q);
+                jt.L(kJACC1, g.jBegin + q) = jl.L(kJACC1, q);
             }
         if (kShared) {  // impulses and sliding axis back to the manifold records
             for (int j = tid; j < nm; j += T) {

@@ -75,15 +75,17 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
     return BEPUGPU_OK;
 }
 
-// Records in slot order into the input and impulse lanes (kJLA .. kJACC1),
-// heads and a cleared state.
+// Records in slot order into the input lanes (kJLA .. kJTRIG), the impulse
+// lanes (kJACC0, kJACC1), heads and a cleared state.
 bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints, uint32_t nj) {
     s->j.count = (int)nj;
     if (!nj) return BEPUGPU_OK;
-    constexpr int kIn = kJACC1 + 1;
-    std::vector<float4> lanes((size_t)kIn * nj);
+    constexpr int kIn = kJointLanes - kJLA;
+    std::vector<float4> lanes((size_t)kIn * nj), acc(2 * (size_t)nj);
     std::vector<int4> head(nj);
-    auto at = [&](int k, int slot) -> float4& { return lanes[(size_t)k * nj + slot]; };
+    auto at = [&](int k, int slot) -> float4& {
+        return k >= kJLA ? lanes[(size_t)(k - kJLA) * nj + slot] : acc[(size_t)(k - kJACC0) * nj + slot];
+    };
     for (uint32_t u = 0; u < nj; u++) {
         const bepugpu_joint& r = joints[u];
         const int slot = s->hostJointSlotOf[u];
@@ -129,8 +131,12 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
         at(kJACC1, slot) = make_float4(ang[1], lim[0], lim[1], 0.f);
     }
     cudaError_t e;
-    if ((e = cudaMemcpy2DAsync(s->j.lanes, sizeof(float4) * s->j.capacity, lanes.data(), sizeof(float4) * nj,
-                               sizeof(float4) * nj, kIn, cudaMemcpyHostToDevice, s->stream)) ||
+    if ((e = cudaMemcpy2DAsync(s->j.lanes + (size_t)kJLA * s->j.capacity, sizeof(float4) * s->j.capacity,
+                               lanes.data(), sizeof(float4) * nj, sizeof(float4) * nj, kIn, cudaMemcpyHostToDevice,
+                               s->stream)) ||
+        (e = cudaMemcpy2DAsync(s->j.lanes + (size_t)kJACC0 * s->j.capacity, sizeof(float4) * s->j.capacity,
+                               acc.data(), sizeof(float4) * nj, sizeof(float4) * nj, 2, cudaMemcpyHostToDevice,
+                               s->stream)) ||
         (e = cudaMemcpyAsync(s->j.head, head.data(), sizeof(int4) * nj, cudaMemcpyHostToDevice, s->stream)) ||
         (e = cudaMemsetAsync(s->j.state, 0, sizeof(uint2) * nj, s->stream)) ||
         (e = cudaMemcpyAsync(s->jointOffsetsDev, s->jointOffsets.data(), sizeof(int32_t) * s->jointOffsets.size(),

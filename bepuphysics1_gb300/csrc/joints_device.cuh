@@ -25,21 +25,12 @@
 
 namespace bepugpu {
 
-// Lanes of a joint slot: lanes[k * capacity + slot].
+// Lanes of a joint slot: lanes[k * capacity + slot].  The first kJSolveLanes
+// are the ones warm start and solve touch (impulses and prestep products); a
+// group kernel keeps those in shared memory.
 enum JointLane : int {
-    // inputs (upload)
-    kJLA = 0,    // ball socket localAnchorA, w = spring stiffness
-    kJLB,        // ball socket localAnchorB, w = spring damping
-    kJAXA,       // angular / swing local axis A, w = max corrective velocity
-    kJAXB,       // angular / swing local axis B, w = margin
-    kJC1,        // angular localConstrainedAxis1 (A's frame), w = bounciness
-    kJC2,        // angular localConstrainedAxis2, w = bounce velocity threshold
-    kJBP,        // revolute limit basis local primary axis (A's frame), w = GetDistanceFromMinimum(max)
-    kJBX,        // revolute limit basis local x axis, w = swing minimum cosine
-    kJTA,        // revolute limit local test axis (B's frame), w = max corrective velocity squared
-    kJTRIG,      // sin(min + pi/2), 1 - cos(min + pi/2), sin(max - pi/2), 1 - cos(max - pi/2)
     // accumulated impulses (in/out)
-    kJACC0,      // ball socket xyz, angular x
+    kJACC0 = 0,  // ball socket xyz, angular x
     kJACC1,      // angular y, limit x (swing: its impulse), limit y
     // prestep products
     kJOA,        // ball worldOffsetA, w = ball softness
@@ -53,8 +44,23 @@ enum JointLane : int {
     kJL0,        // limit jacobianMinA (swing: hinge axis), w = limit softness
     kJL1,        // limit jacobianMaxA
     kJL2,        // limit bias x, bias y, velocityToImpulse x, y
+    kJSolveLanes,
+    // inputs (upload)
+    kJLA = kJSolveLanes,  // ball socket localAnchorA, w = spring stiffness
+    kJLB,        // ball socket localAnchorB, w = spring damping
+    kJAXA,       // angular / swing local axis A, w = max corrective velocity
+    kJAXB,       // angular / swing local axis B, w = margin
+    kJC1,        // angular localConstrainedAxis1 (A's frame), w = bounciness
+    kJC2,        // angular localConstrainedAxis2, w = bounce velocity threshold
+    kJBP,        // revolute limit basis local primary axis (A's frame), w = GetDistanceFromMinimum(max)
+    kJBX,        // revolute limit basis local x axis, w = swing minimum cosine
+    kJTA,        // revolute limit local test axis (B's frame), w = max corrective velocity squared
+    kJTRIG,      // sin(min + pi/2), 1 - cos(min + pi/2), sin(max - pi/2), 1 - cos(max - pi/2)
     kJointLanes
 };
+// Shared memory of one joint in a group kernel: the solve lanes, a state
+// word and a ref pair.
+constexpr int kJointSmemBytes = 16 * kJSolveLanes + 8 + 8;
 
 // head.z: type (bits 0-7), children present (8-10), children IsActive (11-13),
 // joint / group IsActive (14).
@@ -67,12 +73,15 @@ enum : uint32_t {
     kJGroupIsActive = 1u << 14,
 };
 // State word x: kGroupActive (bit 0), child isActiveInSolver bits 1-3,
-// limit minIsActive / maxIsActive bits 4-5, kDynA / kDynB, iterations << 16.
-// Word y: 4-bit zero-impulse streaks of the three children.
+// limit minIsActive / maxIsActive bits 4-5, kDynA / kDynB (bits 7-8), the
+// record type (bits 9-11), iterations << 16.  Word y: 4-bit zero-impulse
+// streaks of the three children.
 enum : uint32_t {
     kJMinActive = 1u << 4,
     kJMaxActive = 1u << 5,
+    kJTypeShift = 9,
 };
+__device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 7u); }
 
 struct JointSoA {
     int4* head;     // body A, body B, type | flags, source record index
@@ -172,15 +181,18 @@ __device__ __forceinline__ float JBounce(float impactVelocity, float threshold, 
     return velocityFraction * impactVelocity * bounciness;
 }
 
-// A joint connection: body state plus pose, or the world entity.
+// A joint connection: body state plus pose, or the world entity.  Body refs go
+// through a body view (GlobalBodies on the sweep path, GroupBodies in island
+// groups); ref -1 is the world entity.
 struct JointBody {
     BodyState s;
     float3 pos;
     JM3 R;
     bool dynamic;
 };
-__device__ __forceinline__ void LoadJointBody(const BodySoA& b, int r, JointBody& o) {
-    if (r < 0) {
+template <class V>
+__device__ __forceinline__ void LoadJointBodyV(const V& bv, int r, JointBody& o) {
+    if (r == -1) {
         o.s.vx = o.s.vy = o.s.vz = 0.f; o.s.invMass = 0.f;
         o.s.wx = o.s.wy = o.s.wz = 0.f;
         o.s.I11 = o.s.I12 = o.s.I13 = o.s.I21 = o.s.I22 = o.s.I23 = o.s.I31 = o.s.I32 = o.s.I33 = 0.f;
@@ -189,42 +201,53 @@ __device__ __forceinline__ void LoadJointBody(const BodySoA& b, int r, JointBody
         o.dynamic = false;
         return;
     }
-    LoadBody(b, r, o.s);
-    float4 p = b.pos[r];
+    LoadBodyV(bv, r, o.s);
+    float4 p = bv.Pos(r);
     o.pos = make_float3(p.x, p.y, p.z);
-    o.R = JRotation(b.quat[r]);
+    o.R = JRotation(bv.Quat(r));
     o.dynamic = p.w != 0.f;
 }
 // Velocity-only view for the warm start and the solve.
-__device__ __forceinline__ void LoadJointVelocity(const BodySoA& b, int r, BodyState& s) {
-    if (r < 0) {
+template <class V>
+__device__ __forceinline__ void LoadJointVelocityV(const V& bv, int r, BodyState& s) {
+    if (r == -1) {
         s.vx = s.vy = s.vz = 0.f; s.invMass = 0.f;
         s.wx = s.wy = s.wz = 0.f;
         s.I11 = s.I12 = s.I13 = s.I21 = s.I22 = s.I23 = s.I31 = s.I32 = s.I33 = 0.f;
         return;
     }
-    LoadBody(b, r, s);
+    LoadBodyV(bv, r, s);
 }
 
 // ------------------------------------------------------------- prestep --
 // Solver.UnsafePrestep (Solver.cs:265-275) of one joint: UpdateSolverActivity,
 // then Update of every active child (SolverGroup.cs:94-100).
-__device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
-    const int4 h = j.head[s];
+// Reads the joint's inputs and impulses at (ji, si) and writes its impulses,
+// prestep products and state at (jo, so): the same slot on the sweep path, the
+// group's shared-memory lanes in a group kernel.  ra, rb: the connections'
+// refs in the body view.
+template <class V>
+__device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const JointSoA& jo, int so, const V& bv,
+                                               int ra, int rb, const StepParams& p) {
+    const JointSoA& j = jo;
+    const int s = so;
+    const int4 h = ji.head[si];
     const uint32_t present = (h.z >> kJPresentShift) & 7u, childIsActive = (h.z >> kJChildActiveShift) & 7u;
     const int type = h.z & 0xff;
     JointBody A, B;
-    LoadJointBody(b, h.x, A);
-    LoadJointBody(b, h.y, B);
-    uint32_t st = (A.dynamic ? kDynA : 0u) | (B.dynamic ? kDynB : 0u);
+    LoadJointBodyV(bv, ra, A);
+    LoadJointBodyV(bv, rb, B);
+    float4 acc0 = ji.L(kJACC0, si), acc1 = ji.L(kJACC1, si);
+    j.L(kJACC0, s) = acc0;
+    uint32_t st = (A.dynamic ? kDynA : 0u) | (B.dynamic ? kDynB : 0u) | ((uint32_t)type << kJTypeShift);
     if (!(h.z & kJGroupIsActive) || !(A.dynamic || B.dynamic)) {
+        j.L(kJACC1, s) = acc1;
         j.state[s] = make_uint2(st, 0u);
         return;
     }
-    const float4 la = j.L(kJLA, s), lb = j.L(kJLB, s), axa = j.L(kJAXA, s), axb = j.L(kJAXB, s);
+    const float4 la = ji.L(kJLA, si), lb = ji.L(kJLB, si), axa = ji.L(kJAXA, si), axb = ji.L(kJAXB, si);
     const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
-    const float maxCorrSq = j.L(kJTA, s).w;
-    float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
+    const float maxCorrSq = ji.L(kJTA, si).w;
     uint32_t active = present & childIsActive;
     if (active & kJChildBall) {
         // BallSocketJoint.Update (BallSocketJoint.cs:210-278)
@@ -274,7 +297,7 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
     if (active & kJChildAngular) {
         // RevoluteAngularJoint.Update (RevoluteAngularJoint.cs:226-289)
         float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
-        float3 c1 = JTransform(JXYZ(j.L(kJC1, s)), A.R), c2 = JTransform(JXYZ(j.L(kJC2, s)), A.R);
+        float3 c1 = JTransform(JXYZ(ji.L(kJC1, si)), A.R), c2 = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
         float3 e3 = JCross(wA, wB);
         float errX = JDot(e3, c1), errY = JDot(e3, c2);
         float erp, softness;
@@ -315,14 +338,14 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
         st |= 1u << (kChildShift + 1);
     }
     if (active & kJChildLimit) {
-        const float bounciness = j.L(kJC1, s).w, threshold = j.L(kJC2, s).w;
+        const float bounciness = ji.L(kJC1, si).w, threshold = ji.L(kJC2, si).w;
         float erp, softness;
         bool on = true;
         if (type == BEPUGPU_JOINT_SWING_LIMIT) {
             // SwingLimit.Update (SwingLimit.cs:249-331)
             float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
             float dot = JDot(wA, wB);
-            const float minimumCosine = j.L(kJBX, s).w;
+            const float minimumCosine = ji.L(kJBX, si).w;
             if (dot > minimumCosine) {
                 on = false;
                 acc1.y = 0.f;
@@ -352,9 +375,9 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
             }
         } else {
             // RevoluteLimit.Update (RevoluteLimit.cs:285-575)
-            float3 primary = JTransform(JXYZ(j.L(kJBP, s)), A.R), xAxis = JTransform(JXYZ(j.L(kJBX, s)), A.R);
-            float3 test = JTransform(JXYZ(j.L(kJTA, s)), B.R);
-            const float4 trig = j.L(kJTRIG, s);
+            float3 primary = JTransform(JXYZ(ji.L(kJBP, si)), A.R), xAxis = JTransform(JXYZ(ji.L(kJBX, si)), A.R);
+            float3 test = JTransform(JXYZ(ji.L(kJTA, si)), B.R);
+            const float4 trig = ji.L(kJTRIG, si);
             // Matrix3x3.CreateFromAxisAngle (Matrix3x3.cs:1383-1406) with the
             // double sine and cosine of the constant angles taken at upload.
             float xx = primary.x * primary.x, yy = primary.y * primary.y, zz = primary.z * primary.z;
@@ -374,7 +397,7 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
             };
             float3 minN = rotate(trig.x, trig.y), maxN = rotate(trig.z, trig.w);
             float pMin = JDot(minN, test), pMax = JDot(maxN, test);
-            const float span = j.L(kJBP, s).w;
+            const float span = ji.L(kJBP, si).w;
             float errX = 0, errY = 0;
             bool minOn = false, maxOn = false;
             if (span >= 3.14159274f) {
@@ -453,10 +476,15 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
             }
         }
         if (on) st |= 1u << (kChildShift + 2);
-        j.L(kJACC1, s) = acc1;
     }
+    j.L(kJACC1, s) = acc1;
     if (st & (7u << kChildShift)) st |= kGroupActive;
     j.state[s] = make_uint2(st, 0u);
+}
+
+__device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
+    const int4 h = j.head[s];
+    PrestepJointIO(j, s, j, s, GlobalBodies{b}, h.x, h.y, p);
 }
 
 // ---------------------------------------------------------- warm start --

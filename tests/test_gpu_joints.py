@@ -157,3 +157,18 @@ def test_chains_full_size_two_steps(gpu_context):
     errs, exact = p.compare()
     assert exact, errs
     p.close()
+
+
+@pytest.mark.parametrize("policy", [(0, 1024, 4096, 64, 0), (1, 1024, 4096, 16, 0), (1, 1024, 4096, 256, 64)])
+def test_chains_in_island_groups(gpu_context, policy):
+    """Joint islands run whole steps inside island-group CTAs (or on the sweep
+    path with groups off); every policy gives the oracle's bits."""
+    b, m, j = _small_chains(seed=14, chains=20)
+    p = Pair(gpu_context, b, m, j, settings=_settings(), group_policy=policy)
+    p.step(steps=5)
+    errs, exact = p.compare()
+    assert exact, (policy, errs)
+    if policy[0]:
+        # chains and loose stacks are small islands: the step is the group launch alone
+        assert p.gpu.last_step_launches() <= 2
+    p.close()
