@@ -28,7 +28,7 @@ from dataclasses import asdict, dataclass, field
 from pathlib import Path
 
 from . import native as N
-from .solver import Context, GpuSpace, batch_step, last_call_stats, set_batch_threads
+from .solver import Context, GpuSpace, batch_step, last_call_stats, scene_ids, set_batch_threads
 
 
 @dataclass
@@ -80,10 +80,11 @@ def measure(ctx: Context, spaces: list[GpuSpace], dt: float, steps_per_launch: i
             flags: int = N.STEP_ALL) -> Trial:
     """Scene-steps/s of `calls` batched calls after one untimed call (which also
     captures the launch graph)."""
-    batch_step(ctx, spaces, dt, steps_per_launch, flags)
+    ids = scene_ids(spaces)
+    batch_step(ctx, ids, dt, steps_per_launch, flags)
     dev, t0 = 0.0, time.perf_counter()
     for _ in range(calls):
-        batch_step(ctx, spaces, dt, steps_per_launch, flags)
+        batch_step(ctx, ids, dt, steps_per_launch, flags)
         dev += last_call_stats(ctx)[1]
     el = time.perf_counter() - t0
     launches = last_call_stats(ctx)[0]

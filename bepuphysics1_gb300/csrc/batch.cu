@@ -165,6 +165,12 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
     Batch& bt = *static_cast<Batch*>(ctx->batch.get());
     std::vector<Scene*> list(count);
     std::vector<uint32_t> stepCount(count);
+    // A stamp per call marks the listed scenes (duplicate check in one pass);
+    // the epoch advances whether or not the call succeeds.
+    struct EpochBump {
+        Context* c;
+        ~EpochBump() { c->batchEpoch++; }
+    } bump{ctx};
     std::vector<uint64_t> versions(count);
     for (uint32_t i = 0; i < count; i++) {
         auto it = ctx->scenes.find(scenes[i]);
@@ -187,11 +193,11 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
                           "were uploaded", scenes[i], s->maxBodyReferenced, s->b.count);
             return BEPUGPU_INVALID_OPERATION;
         }
-        for (uint32_t j = 0; j < i; j++)
-            if (list[j] == s) {
-                ctx->SetError("batch: scene %d is listed twice", scenes[i]);
-                return BEPUGPU_INVALID_ARGUMENT;
-            }
+        if (s->batchStamp == ctx->batchEpoch + 1) {
+            ctx->SetError("batch: scene %d is listed twice", scenes[i]);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        s->batchStamp = ctx->batchEpoch + 1;
         list[i] = s;
         stepCount[i] = k;
         versions[i] = s->version;

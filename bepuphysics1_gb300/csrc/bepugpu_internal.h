@@ -143,6 +143,7 @@ struct Scene {
     int groupThreadsOverride = 0;    // 0 = derived from the plan
     bool phaseEvents = true;         // the step graph records the sweep-path phase events
     bool planStale = false;          // dynamic flags changed since the constraints were planned
+    uint64_t batchStamp = 0;         // last batched call listing the scene (duplicate check)
     cudaEvent_t evGroup[2] = {nullptr, nullptr};
     bepugpu_status UploadGroups(Context* ctx);
     bepugpu_status RebuildSweepBodies(Context* ctx);
@@ -231,6 +232,7 @@ struct Context {
     uint32_t lastLaunches = 0;
     float lastMs = 0.f;
     int batchThreads = 0;  // threads per CTA of batched launches, 0 = from the groups' colour sizes
+    uint64_t batchEpoch = 0;  // batched calls so far (Scene::batchStamp)
     void SetError(const char* fmt, ...);
 };
 

@@ -220,9 +220,15 @@ def colour_list(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | 
     return colour, order, k.value
 
 
+def scene_ids(spaces) -> np.ndarray:
+    """The scene ids of `spaces` as the int32 array the batched calls take."""
+    return np.ascontiguousarray([s.id for s in spaces], dtype=np.int32)
+
+
 def batch_step(ctx: Context, spaces, dt: float, steps: int = 1, flags: int = N.STEP_ALL):
-    """bepugpu_batch_step: every space advances `steps` steps in one batched launch."""
-    ids = np.ascontiguousarray([s.id for s in spaces], dtype=np.int32)
+    """bepugpu_batch_step: every space advances `steps` steps in one batched launch.
+    `spaces` is a list of GpuSpace or an int32 array from scene_ids()."""
+    ids = spaces if isinstance(spaces, np.ndarray) else scene_ids(spaces)
     ctx.check(ctx.lib.bepugpu_batch_step(ctx.handle, N.ptr(ids), len(ids), float(dt), steps, flags))
 
 
