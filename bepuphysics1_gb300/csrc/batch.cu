@@ -144,6 +144,7 @@ using namespace bepugpu;
 
 static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const uint32_t* stepsEach, uint32_t steps,
                                 uint32_t count, float dt, uint32_t flags) {
+    NvtxRange range("bepugpu_batch_step");
     auto* ctx = reinterpret_cast<Context*>(c);
     if (!ctx) return BEPUGPU_INVALID_ARGUMENT;
     cudaSetDevice(ctx->device);

@@ -98,6 +98,31 @@ __global__ void k_patch_body_records(BodySoA b, bepugpu_body* __restrict__ rec) 
     r.angular_velocity[0] = w.x; r.angular_velocity[1] = w.y; r.angular_velocity[2] = w.z;
 }
 
+// Lowest body with a non-finite position, orientation or velocity.
+__device__ __forceinline__ bool Finite4(float4 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z) && isfinite(v.w); }
+__global__ void k_check_finite(BodySoA b, int* firstBad) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.count) return;
+    float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i];
+    if (!Finite4(p) || !Finite4(b.quat[i]) || !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z) ||
+        !isfinite(w.x) || !isfinite(w.y) || !isfinite(w.z))
+        atomicMin(firstBad, i);
+}
+
+// A wait on a flag nothing sets, bounded like GridBarrier's: gives up after
+// `limit` polls and reports TIMEOUT in *status.
+__global__ void k_bounded_wait_probe(volatile unsigned int* flag, unsigned int limit, int* status) {
+    unsigned int spins = 0;
+    while (*flag == 0u) {
+        if (++spins > limit) {
+            *status = BEPUGPU_TIMEOUT;
+            return;
+        }
+        __nanosleep(64);
+    }
+    *status = BEPUGPU_OK;
+}
+
 // Checks of the update calls, before anything is written: check[0] receives
 // the lowest offending record index (stays INT_MAX when none), check[1] is set
 // when a kinematic body has a velocity.
@@ -505,7 +530,9 @@ static size_t Align(size_t x) { return (x + 255) & ~(size_t)255; }
 Scene::~Scene() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
     if (arena) cudaFree(arena);
-    if (spillHost) cudaFreeHost(spillHost);
+    if (spillHost && !spillHostBorrowed) cudaFreeHost(spillHost);
+    if (evSpill) cudaEventDestroy(evSpill);
+    if (evRestore) cudaEventDestroy(evRestore);
     if (staging) cudaFree(staging);
     if (counter) cudaFree(counter);
     if (evStart) cudaEventDestroy(evStart);
@@ -655,28 +682,44 @@ void Scene::Rebase() {
 // holds device addresses.
 // Stream-ordered frees and allocations (cudaFreeAsync / cudaMallocAsync) keep
 // a spill or restore from synchronising the device with work of other scenes.
-bepugpu_status Scene::Spill(Context* ctx) {
+// Without `wait` neither call blocks: the spill's copy and frees are ordered
+// on the scene's stream and marked by evSpill; a restore waits for that mark
+// on the stream it is given, copies there, and the scene's stream waits for
+// the copy (evRestore).  `host` (optional) is a pinned buffer of arenaBytes
+// for the first spill, owned by the caller.
+bepugpu_status Scene::Spill(Context* ctx, bool wait, void* host) {
     if (!arena) return BEPUGPU_OK;
-    if (!spillHost) CK(cudaMallocHost(&spillHost, arenaBytes));
+    if (!spillHost) {
+        if (host) {
+            spillHost = host;
+            spillHostBorrowed = true;
+        } else {
+            CK(cudaMallocHost(&spillHost, arenaBytes));
+            spillHostBorrowed = false;
+        }
+    }
+    if (!evSpill) CK(cudaEventCreateWithFlags(&evSpill, cudaEventDisableTiming));
     CK(cudaMemcpyAsync(spillHost, arena, arenaBytes, cudaMemcpyDeviceToHost, stream));
     CK(cudaFreeAsync(arena, stream));
     arena = nullptr;
     if (staging) CK(cudaFreeAsync(staging, stream));
     staging = nullptr;
-    CK(cudaStreamSynchronize(stream));
+    CK(cudaEventRecord(evSpill, stream));
+    if (wait) CK(cudaStreamSynchronize(stream));
     if (graphExec) cudaGraphExecDestroy(graphExec);
     graphExec = nullptr;
     asyncPending = false;
     return BEPUGPU_OK;
 }
 
-bepugpu_status Scene::Restore(Context* ctx) {
+bepugpu_status Scene::Restore(Context* ctx, cudaStream_t q, bool wait) {
     if (arena) return BEPUGPU_OK;
-    cudaError_t e = cudaMallocAsync(&arena, arenaBytes, stream);
+    if (!q) q = stream;
+    cudaError_t e = cudaMallocAsync(&arena, arenaBytes, q);
     if (e == cudaSuccess) {
-        e = cudaMallocAsync(&staging, stagingBytes, stream);
+        e = cudaMallocAsync(&staging, stagingBytes, q);
         if (e != cudaSuccess) {
-            cudaFreeAsync(arena, stream);
+            cudaFreeAsync(arena, q);
             arena = nullptr;
             staging = nullptr;
         }
@@ -688,10 +731,25 @@ bepugpu_status Scene::Restore(Context* ctx) {
         return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
     }
     Rebase();
-    CK(cudaMemcpyAsync(arena, spillHost, arenaBytes, cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
+    if (evSpill) CK(cudaStreamWaitEvent(q, evSpill, 0));
+    CK(cudaMemcpyAsync(arena, spillHost, arenaBytes, cudaMemcpyHostToDevice, q));
+    if (q != stream) {
+        if (!evRestore) CK(cudaEventCreateWithFlags(&evRestore, cudaEventDisableTiming));
+        CK(cudaEventRecord(evRestore, q));
+        CK(cudaStreamWaitEvent(stream, evRestore, 0));
+    }
+    if (wait) CK(cudaStreamSynchronize(q));
     version++;
     return BEPUGPU_OK;
+}
+
+// Gives up a borrowed spill buffer (its owner frees it); the next spill takes
+// another.  Only while resident: a spilled scene's data lives there.
+void Scene::DropBorrowedSpillBuffer() {
+    if (arena && spillHostBorrowed) {
+        spillHost = nullptr;
+        spillHostBorrowed = false;
+    }
 }
 
 // The bodies the sweep path's body stages handle once groups exist: every
@@ -885,6 +943,7 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
 }
 
 bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
+    NvtxRange range("bepugpu_step");
     if (!(dt > 0) || !std::isfinite(dt)) {
         ctx->SetError("dt must be positive and finite");
         return BEPUGPU_INVALID_ARGUMENT;
@@ -1102,6 +1161,7 @@ bepugpu_status bepugpu_scene_destroy(bepugpu_context* c, int32_t id) {
 }
 
 bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {
+    NvtxRange range("bepugpu_upload_bodies");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
@@ -1163,6 +1223,7 @@ static bepugpu_status UploadManifoldRecords(Context* ctx, Scene* s, const bepugp
 
 bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const bepugpu_manifold* man, uint32_t nm,
                                           const bepugpu_joint* joints, uint32_t nj) {
+    NvtxRange range("bepugpu_upload_constraints");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
@@ -1239,6 +1300,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
 }
 
 bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const bepugpu_manifold* man, uint32_t n) {
+    NvtxRange range("bepugpu_update_manifolds");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
@@ -1265,6 +1327,7 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
 }
 
 bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {
+    NvtxRange range("bepugpu_update_bodies");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
@@ -1296,7 +1359,51 @@ bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepug
     return BEPUGPU_OK;
 }
 
+bepugpu_status bepugpu_check_finite(bepugpu_context* c, int32_t id, int32_t* firstBad) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    if (!firstBad) return BEPUGPU_INVALID_ARGUMENT;
+    *firstBad = -1;
+    if (!s->b.count) return BEPUGPU_OK;
+    int* check = s->CheckWords();
+    CK(cudaMemsetAsync(check, 0x7f, sizeof(int), s->stream));
+    k_check_finite<<<Blocks(s->b.count, 256), 256, 0, s->stream>>>(s->b, check);
+    CK(cudaGetLastError());
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, check, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    s->asyncPending = false;
+    if (h == 0x7f7f7f7f) return BEPUGPU_OK;
+    *firstBad = h;
+    ctx->SetError("body %d has a non-finite position, orientation or velocity", h);
+    return BEPUGPU_NAN_DETECTED;
+}
+
+bepugpu_status bepugpu_probe_bounded_wait(bepugpu_context* c, uint32_t limit) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    void* words = nullptr;  // [0] the flag nothing sets, [1] the status
+    CK(cudaMalloc(&words, 2 * sizeof(int)));
+    cudaError_t e = cudaMemset(words, 0, 2 * sizeof(int));
+    int status = BEPUGPU_CUDA_ERROR;
+    if (e == cudaSuccess) {
+        k_bounded_wait_probe<<<1, 1>>>((volatile unsigned int*)words, limit, (int*)words + 1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&status, (int*)words + 1, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(words);
+    if (e != cudaSuccess) {
+        ctx->SetError("bounded wait probe: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    if (status == BEPUGPU_TIMEOUT) ctx->SetError("the bounded wait ran out after %u polls", limit);
+    return (bepugpu_status)status;
+}
+
 bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_body* bodies, uint32_t n) {
+    NvtxRange range("bepugpu_download_bodies");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);
@@ -1315,6 +1422,7 @@ bepugpu_status bepugpu_download_bodies(bepugpu_context* c, int32_t id, bepugpu_b
 
 bepugpu_status bepugpu_download_constraints(bepugpu_context* c, int32_t id, bepugpu_manifold* man, uint32_t nm,
                                             bepugpu_joint* joints, uint32_t nj) {
+    NvtxRange range("bepugpu_download_constraints");
     auto* ctx = reinterpret_cast<Context*>(c);
     CTX_CHECK(ctx);
     Scene* s = FindScene(ctx, id);

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <memory>
@@ -21,6 +22,15 @@ struct BatchEngine;
 struct Scene;
 
 StepParams MakeParams(const bepugpu_settings& s, float dt);
+
+// An NVTX range for the duration of a scope: the host-side phases (steps,
+// batched calls, waves, uploads, downloads) show up by name in Nsight traces.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Island groups (groups.cu).  A group is a set of whole islands run by one CTA.
 struct GroupDesc {
@@ -159,9 +169,12 @@ struct Scene {
     size_t arenaBytes = 0;
     ArenaLayout layout{};
     void* spillHost = nullptr;      // pinned copy of the arena while spilled
+    bool spillHostBorrowed = false; // spillHost belongs to a server's pinned pool
+    cudaEvent_t evSpill = nullptr, evRestore = nullptr;
     void Rebase();
-    bepugpu_status Spill(Context* ctx);
-    bepugpu_status Restore(Context* ctx);
+    bepugpu_status Spill(Context* ctx, bool wait = true, void* host = nullptr);
+    bepugpu_status Restore(Context* ctx, cudaStream_t q = nullptr, bool wait = true);
+    void DropBorrowedSpillBuffer();
     size_t DeviceBytes() const { return arenaBytes + stagingBytes; }
     void* staging = nullptr;
     size_t stagingBytes = 0;

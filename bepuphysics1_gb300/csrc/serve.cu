@@ -99,6 +99,7 @@ struct Server {
 
     // stats (worker-written, read under regMu)
     uint64_t statWaves = 0, statWaveScenes = 0, statLaunches = 0, statSpills = 0, statRestores = 0;
+    uint64_t statRoomWaits = 0, statRestoreFailures = 0;
     uint64_t residentBytes = 0, peakResident = 0, spilledBytes = 0;
 
     Server(size_t cap) : submitQ(cap), doneQ(cap) {}
@@ -217,6 +218,7 @@ struct Server {
     }
 
     bool Launch(Wave& w) {
+        NvtxRange range("bepugpu_serve_wave");
         std::lock_guard<std::mutex> g(regMu);
         if (ready.empty()) return false;
         w.slotIds.clear();
@@ -225,6 +227,7 @@ struct Server {
         int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0;
         std::vector<int> plain;
         std::deque<int> keep;
+        bool noRoom = false;
         while (!ready.empty() && w.slotIds.size() < cfg.max_wave_scenes) {
             int id = ready.front();
             ready.pop_front();
@@ -235,12 +238,17 @@ struct Server {
             }
             Scene* s = sl.s;
             if (!s->arena) {
-                if (!MakeRoom(s->DeviceBytes())) {
+                // Once no room could be made, later spilled scenes of this wave
+                // wait too (a room search scans every scene).
+                if (noRoom || !MakeRoom(s->DeviceBytes())) {
+                    noRoom = true;
+                    statRoomWaits++;
                     keep.push_back(id);  // waits for room; stays ready
                     continue;
                 }
                 if (s->Restore(&sink) != BEPUGPU_OK) {
                     SetError(sink.lastError);
+                    statRestoreFailures++;
                     keep.push_back(id);
                     continue;
                 }
@@ -457,8 +465,10 @@ bepugpu_status bepugpu_server_destroy(bepugpu_server* h) {
     for (auto& sl : s->slots) {
         if (!sl.live) continue;
         if (!sl.s->arena && sl.s->Restore(s->ctx) != BEPUGPU_OK) st = BEPUGPU_OUT_OF_MEMORY;
+        sl.s->DropBorrowedSpillBuffer();
         sl.s->server = nullptr;
     }
+
     for (auto& w : s->waves) {
         if (w.workDev) cudaFree(w.workDev);
         if (w.workHost) cudaFreeHost(w.workHost);
@@ -530,6 +540,9 @@ bepugpu_status bepugpu_server_add_scene(bepugpu_server* h, int32_t scene) {
     return BEPUGPU_OK;
 }
 
+// The scene's stream drained, so no spill copy still reads its buffer.
+#define CK_SYNC(sc) cudaStreamSynchronize((sc)->stream)
+
 bepugpu_status bepugpu_server_release_scene(bepugpu_server* h, int32_t scene, uint32_t timeout_ms) {
     if (!h) return BEPUGPU_INVALID_ARGUMENT;
     Server* s = h->s;
@@ -555,6 +568,8 @@ bepugpu_status bepugpu_server_release_scene(bepugpu_server* h, int32_t scene, ui
                 sl.live = false;
                 sl.queued = false;
                 s->slotOf.erase(it);
+                CK_SYNC(sc);
+                sc->DropBorrowedSpillBuffer();
                 sc->server = nullptr;
                 return BEPUGPU_OK;
             }
@@ -605,6 +620,8 @@ bepugpu_status bepugpu_server_stats_get(bepugpu_server* h, bepugpu_server_stats*
     out->launches = s->statLaunches;
     out->spills = s->statSpills;
     out->restores = s->statRestores;
+    out->room_waits = s->statRoomWaits;
+    out->restore_failures = s->statRestoreFailures;
     out->resident_bytes = s->residentBytes;
     out->peak_resident_bytes = s->peakResident;
     out->spilled_bytes = s->spilledBytes;

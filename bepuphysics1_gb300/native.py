@@ -76,7 +76,8 @@ COMPLETION_DTYPE = np.dtype([
 SERVER_STATS_DTYPE = np.dtype([
     ("submitted", "<u8"), ("completed", "<u8"), ("waves", "<u8"), ("wave_scenes", "<u8"), ("launches", "<u8"),
     ("spills", "<u8"), ("restores", "<u8"), ("resident_bytes", "<u8"), ("peak_resident_bytes", "<u8"),
-    ("spilled_bytes", "<u8"), ("scenes", "<u4"), ("resident_scenes", "<u4"),
+    ("spilled_bytes", "<u8"), ("scenes", "<u4"), ("resident_scenes", "<u4"), ("room_waits", "<u8"),
+    ("restore_failures", "<u8"),
 ])
 
 PHASE_TIMES_DTYPE = np.dtype([
@@ -121,6 +122,8 @@ GPU_EXPORTS = {
     "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
     "bepugpu_update_bodies": (_I, [_P, _I, _P, _U]),
+    "bepugpu_check_finite": (_I, [_P, _I, ctypes.POINTER(_I)]),
+    "bepugpu_probe_bounded_wait": (_I, [_P, _U]),
     "bepugpu_download_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_download_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_get_colouring": (_I, [_P, _I, _P, _P, _U, ctypes.POINTER(_U)]),

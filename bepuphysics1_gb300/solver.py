@@ -180,6 +180,13 @@ class GpuSpace:
                                                           ctypes.byref(k)))
         return colour, order, k.value
 
+    def check_finite(self) -> int:
+        """bepugpu_check_finite: -1, or raises BepuError(NAN_DETECTED) naming the
+        first body with a non-finite state."""
+        bad = ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.bepugpu_check_finite(self.ctx.handle, self.id, ctypes.byref(bad)))
+        return bad.value
+
     def last_step_ms(self) -> float:
         v = ctypes.c_float()
         self.ctx.check(self.ctx.lib.bepugpu_last_step_ms(self.ctx.handle, self.id, ctypes.byref(v)))

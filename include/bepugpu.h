@@ -232,6 +232,19 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* ctx, int32_t scene,
 bepugpu_status bepugpu_update_bodies(bepugpu_context* ctx, int32_t scene, const bepugpu_body* bodies,
                                      uint32_t count);
 
+/* Checks every body's position, orientation and velocities for NaN or
+ * infinity (the reference's CHECKMATH validation, Toolbox.Validate, off there
+ * by default): NAN_DETECTED with *first_bad set to the lowest such body, else
+ * OK with *first_bad = -1.  Waits for the scene's work. */
+bepugpu_status bepugpu_check_finite(bepugpu_context* ctx, int32_t scene, int32_t* first_bad);
+
+/* Self-test of the bounded device waits the persistent kernel's grid barrier
+ * uses: one thread waits on a device flag that nothing sets, giving up after
+ * `spin_limit` polls (64 ns apart) and writing TIMEOUT to a status word the
+ * host reads.  Returns that status (TIMEOUT when the wait ran out); the
+ * context stays usable.  No reference counterpart. */
+bepugpu_status bepugpu_probe_bounded_wait(bepugpu_context* ctx, uint32_t spin_limit);
+
 /* Writes whole body records: the fields as last uploaded, with position,
  * orientation and velocities as they are now (one copy of the scene's device
  * copy of the records). */
@@ -418,6 +431,8 @@ typedef struct bepugpu_server_stats {
     uint64_t submitted, completed, waves, wave_scenes, launches, spills, restores;
     uint64_t resident_bytes, peak_resident_bytes, spilled_bytes;
     uint32_t scenes, resident_scenes;
+    uint64_t room_waits;        /* times a spilled scene waited a wave for room */
+    uint64_t restore_failures;  /* restores that could not get device memory */
 } bepugpu_server_stats;
 
 void bepugpu_server_default_config(bepugpu_server_config* out);

@@ -268,3 +268,26 @@ def test_update_bodies_and_manifolds_per_step(gpu_context):
     assert np.array_equal(got["position"], ref.get_bodies()["position"])
     full.close()
     fast.close()
+
+
+def test_check_finite_and_bounded_wait(gpu_context):
+    """NaN state is reported as NAN_DETECTED with the body's index; a device
+    wait on a flag nothing sets gives up with TIMEOUT and the context keeps
+    working."""
+    gpu_context.set_settings(default_settings())
+    b, m, _ = scenes.pile_1k()
+    sp = GpuSpace(gpu_context, b, m)
+    assert sp.check_finite() == -1
+    bad = b.copy()
+    bad["linear_velocity"][17] = (np.nan, 0, 0)
+    bad["angular_velocity"][40] = (0, np.inf, 0)
+    sp.upload_bodies(bad)
+    with pytest.raises(N.BepuError) as err:
+        sp.check_finite()
+    assert err.value.status == N.NAN_DETECTED and "body 17" in str(err.value)
+    st = gpu_context.lib.bepugpu_probe_bounded_wait(gpu_context.handle, 1000)
+    assert st == N.TIMEOUT
+    sp.upload_bodies(b)
+    sp.step(DT)
+    assert sp.check_finite() == -1
+    sp.close()
