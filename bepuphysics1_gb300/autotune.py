@@ -8,7 +8,8 @@ Four knobs decide how a batch of independent scenes maps onto the GPU:
                     and solve lanes fit it keeps its lanes on chip, larger ones
                     keep them in global memory (bepugpu_set_group_smem_budget);
   threads           CTA size of the batched launches (bepugpu_set_batch_threads);
-  steps_per_launch  how many steps every CTA runs back to back per launch.
+  steps_per_launch  how many steps one call runs: that many one-step launches
+                    captured in one CUDA graph, so the host cost is paid once.
 
 None of them changes results: island groups are independent and each one runs
 its manifolds in the list's colour order, so every setting gives the same bits

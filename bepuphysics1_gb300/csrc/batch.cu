@@ -27,12 +27,18 @@
 
 namespace bepugpu {
 
+// One step of one island group of one scene per CTA.  A call of k steps is k
+// launches (pass 0..k-1); a work item whose scene asked for fewer steps than
+// the launch's pass returns at once.  Steps run as separate launches rather
+// than a loop inside the CTA: the loop keeps the step's body state live across
+// iterations and pushes the kernel past the register file into spills.
 template <bool kShared>
 __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
-                               uint32_t flags, int Bc, int Lc) {
+                               uint32_t flags, int Bc, int Lc, int pass) {
     extern __shared__ float4 smem[];
     __shared__ SceneView sv;
     const int4 w = work[blockIdx.x];  // scene view, group, steps
+    if (pass >= w.z) return;
     {
         const int* src = (const int*)(views + w.x);
         int* dst = (int*)&sv;
@@ -40,10 +46,7 @@ __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* 
     }
     __syncthreads();
     const GroupDesc g = sv.t.groups[w.y];
-    for (int k = 0; k < w.z; k++) {
-        if (k) __syncthreads();  // the previous step's write-back is visible to the next step's loads
-        GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr);
-    }
+    GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr);
 }
 
 namespace {
@@ -101,17 +104,19 @@ cudaError_t Ensure(T*& p, size_t& cap, size_t n) {
 }
 
 template <bool kShared>
-cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags, int threads) {
+cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags, int threads,
+                             int passes) {
     if (c.work.empty()) return cudaSuccess;
-    bt.launches++;
+    bt.launches += passes;
     return LaunchBatchedGroups(kShared, bt.viewsDev, c.dev, (int)c.work.size(), p, flags, c.Bc, c.Lc, c.members,
-                               threads, bt.stream);
+                               threads, passes, bt.stream);
 }
 
 }  // namespace
 
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
-                                uint32_t flags, int Bc, int Lc, int members, int threads, cudaStream_t stream) {
+                                uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
+                                cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     size_t smemBytes = GroupSmemBytes(shared, Bc, Lc);
     auto kernel = shared ? k_batch_groups<true> : k_batch_groups<false>;
@@ -119,8 +124,12 @@ cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4*
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
         if (e != cudaSuccess) return e;
     }
-    kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc);
-    return cudaGetLastError();
+    for (int pass = 0; pass < passes; pass++) {
+        kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 SceneView MakeView(const Scene& s) {
@@ -224,11 +233,13 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             bt.graph = nullptr;
         }
         std::vector<SceneView> views;
+        int passes = 0;  // launches per class: the most steps any batched scene asked for
         bt.shared = ClassLaunch{{}, 1, 1, 0, bt.shared.dev, bt.shared.cap};
         bt.global = ClassLaunch{{}, 1, 1, 0, bt.global.dev, bt.global.cap};
         for (uint32_t i = 0; i < count; i++) {
             Scene* s = list[i];
             if (!s->BatchReady() || stepCount[i] == 0) continue;
+            passes = std::max(passes, (int)stepCount[i]);
             const GroupPlan& g = s->groupPlan;
             const int vi = (int)views.size();
             views.push_back(MakeView(*s));
@@ -275,8 +286,8 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             ctx->SetError("batch capture: %s", cudaGetErrorString(e));
             return BEPUGPU_CUDA_ERROR;
         }
-        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads);
-        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads);
+        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads, passes);
+        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads, passes);
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(bt.stream, &graph);
         if (le != cudaSuccess || e != cudaSuccess) {

@@ -232,7 +232,8 @@ struct SceneView {
 };
 SceneView MakeView(const Scene& s);
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
-                                uint32_t flags, int Bc, int Lc, int members, int threads, cudaStream_t stream);
+                                uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
+                                cudaStream_t stream);
 
 struct Context {
     int device = 0;

@@ -224,7 +224,7 @@ struct Server {
         w.slotIds.clear();
         w.reqs.clear();
         std::vector<int4> shared, global;
-        int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0;
+        int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0, passes = 0;
         std::vector<int> plain;
         std::deque<int> keep;
         bool noRoom = false;
@@ -267,6 +267,7 @@ struct Server {
             w.reqs.push_back(r);
             if (cfg.batching && s->BatchReady()) {
                 const GroupPlan& gp = s->groupPlan;
+                passes = std::max(passes, (int)r.steps);
                 for (int k = gp.shared.begin; k < gp.shared.end; k++) shared.push_back(make_int4(id, k, (int)r.steps, 0));
                 for (int k = gp.global.begin; k < gp.global.end; k++) global.push_back(make_int4(id, k, (int)r.steps, 0));
                 if (gp.shared.end > gp.shared.begin) {
@@ -324,13 +325,13 @@ struct Server {
             e = cudaMemcpyAsync(w.workDev, w.workHost, sizeof(int4) * nWork, cudaMemcpyHostToDevice, w.stream);
             if (e == cudaSuccess && !shared.empty()) {
                 e = LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc, sMem, 0,
-                                        w.stream);
-                statLaunches++;
+                                        passes, w.stream);
+                statLaunches += passes;
             }
             if (e == cudaSuccess && !global.empty()) {
                 e = LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p, cfg.flags,
-                                        gBc, 1, gMem, 0, w.stream);
-                statLaunches++;
+                                        gBc, 1, gMem, 0, passes, w.stream);
+                statLaunches += passes;
             }
         }
         // one-scene path: each scene's own stream, joined into the wave's event
