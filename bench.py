@@ -77,6 +77,8 @@ def parse_args():
     ap.add_argument("--serve-rates", default="1000,5000,20000,50000,100000,200000",
                     help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-plain-rates", default="1000,5000,20000")
+    ap.add_argument("--serve-spill-rates", default="1000,5000,20000",
+                    help="arrival rates under a device budget of half the served bytes")
     ap.add_argument("--chain-cpu-seconds", type=float, default=8.0)
     return ap.parse_args()
 
@@ -496,7 +498,10 @@ def serve_level(srv, ids, rate, seconds, seed):
             "queue_ms_p50": float(np.percentile((ok["start_us"] - ok["submit_us"]) / 1000.0, 50)) if len(ok) else None,
             "waves": waves, "scenes_per_wave": float(s1["wave_scenes"] - s0["wave_scenes"]) / max(waves, 1),
             "launches": int(s1["launches"] - s0["launches"]), "spills": int(s1["spills"] - s0["spills"]),
-            "restores": int(s1["restores"] - s0["restores"]), "submit_ring_full": int(full)}
+            "restores": int(s1["restores"] - s0["restores"]), "submit_ring_full": int(full),
+            "spill_ms": (int(s1["spill_us"]) - int(s0["spill_us"])) / 1e3,
+            "restore_ms": (int(s1["restore_us"]) - int(s0["restore_us"])) / 1e3,
+            "room_waits": int(s1["room_waits"] - s0["room_waits"])}
 
 
 def serve_section(args, local, rank, world, pg):
@@ -527,8 +532,10 @@ def serve_section(args, local, rank, world, pg):
 
     def run(mode_rates, **kw):
         srv = Server(ctx, dt=float(DT), **kw)
+        t_add = time.perf_counter()
         for sp in spaces:
             srv.add(sp)
+        t_add = time.perf_counter() - t_add
         # warm-up: one 1-step request per scene (first launches, one-scene graphs), untimed
         for i in ids:
             while srv.submit(i, 1, 0) != 0:
@@ -539,7 +546,8 @@ def serve_section(args, local, rank, world, pg):
         st = srv.stats()
         levels = [serve_level(srv, ids, r, args.serve_seconds, 17 + i) for i, r in enumerate(mode_rates)]
         res = {"levels": levels, "resident_bytes": int(st["resident_bytes"]),
-               "resident_scenes": int(st["resident_scenes"])}
+               "resident_scenes": int(st["resident_scenes"]), "pinned_spill_bytes": int(st["pinned_bytes"]),
+               "add_scenes_s": t_add}
         srv.close()
         return res
 
@@ -547,7 +555,7 @@ def serve_section(args, local, rank, world, pg):
     out["batched"]["device_budget_bytes"] = 120 << 30
     out["plain"] = run(plain_rates, batching=False, budget_bytes=120 << 30)
     total = out["batched"]["resident_bytes"]
-    spill_rate = [r for r in rates if r <= 5000][-1:] or rates[:1]
+    spill_rate = [float(r) for r in args.serve_spill_rates.split(",") if r]
     out["batched_half_budget"] = run(spill_rate, batching=True, budget_bytes=max(total // 2, 1 << 20))
     out["batched_half_budget"]["device_budget_bytes"] = max(total // 2, 1 << 20)
     by_rate = {lv["rate"]: lv for lv in out["plain"]["levels"]}

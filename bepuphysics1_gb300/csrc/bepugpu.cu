@@ -752,6 +752,19 @@ void Scene::DropBorrowedSpillBuffer() {
     }
 }
 
+// A spilled scene whose borrowed buffer's owner goes away moves its data to a
+// pinned buffer of its own.  False if that allocation fails.
+bool Scene::OwnSpillBuffer() {
+    if (arena || !spillHostBorrowed) return true;
+    if (stream) cudaStreamSynchronize(stream);  // the spill copy has landed
+    void* own = nullptr;
+    if (cudaMallocHost(&own, arenaBytes) != cudaSuccess) return false;
+    std::memcpy(own, spillHost, arenaBytes);
+    spillHost = own;
+    spillHostBorrowed = false;
+    return true;
+}
+
 // The bodies the sweep path's body stages handle once groups exist: every
 // body no group kernel steps.
 bepugpu_status Scene::RebuildSweepBodies(Context* ctx) {
@@ -1094,6 +1107,7 @@ void bepugpu_destroy(bepugpu_context* c) {
     auto* ctx = reinterpret_cast<Context*>(c);
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    ShutdownServers(ctx);  // their workers step these scenes
     ctx->batch.reset();
     ctx->scenes.clear();
     delete ctx;

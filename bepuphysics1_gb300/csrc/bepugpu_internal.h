@@ -175,6 +175,15 @@ struct Scene {
     bepugpu_status Spill(Context* ctx, bool wait = true, void* host = nullptr);
     bepugpu_status Restore(Context* ctx, cudaStream_t q = nullptr, bool wait = true);
     void DropBorrowedSpillBuffer();
+    bool OwnSpillBuffer();
+    // Lends a pinned buffer of arenaBytes for spills (kept until dropped);
+    // false if the scene already has one.
+    bool LendSpillBuffer(void* host) {
+        if (spillHost || !host) return false;
+        spillHost = host;
+        spillHostBorrowed = true;
+        return true;
+    }
     size_t DeviceBytes() const { return arenaBytes + stagingBytes; }
     void* staging = nullptr;
     size_t stagingBytes = 0;
@@ -247,7 +256,12 @@ struct Context {
     float lastMs = 0.f;
     int batchThreads = 0;  // threads per CTA of batched launches, 0 = from the groups' colour sizes
     uint64_t batchEpoch = 0;  // batched calls so far (Scene::batchStamp)
+    std::vector<bepugpu_server*> servers;  // live servers: shut down before the scenes go
     void SetError(const char* fmt, ...);
 };
+
+// Stops every server of the context and gives its scenes back; their handles
+// then accept only bepugpu_server_destroy (serve.cu).
+void ShutdownServers(Context* ctx);
 
 }  // namespace bepugpu

@@ -6,9 +6,10 @@
 // the device budget with least-recently-used spills to pinned host memory,
 // and up to four waves in flight.  A wave takes every ready scene that is not
 // already on the device (one request each) and launches, on the wave's own
-// stream, the batched group kernel over all their island groups
-// (batch.cu) -- each CTA running its request's steps back to back -- plus the
-// one-scene path for scenes the batched kernel cannot take.  Completion of a
+// stream, the batched group kernel over all their island groups (batch.cu;
+// one launch per step, up to the most steps a request of the wave asked for,
+// CTAs of requests with fewer steps returning at once) plus the one-scene
+// path for scenes the batched kernel cannot take.  Completion of a
 // wave is seen through its event; its requests go to the completion ring.  A
 // scene is in at most one wave at a time, so its requests run in submission
 // order and every result equals stepping that scene alone.
@@ -20,7 +21,9 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -45,6 +48,83 @@ struct ServeRequest {
     uint64_t tag;
     double submitUs;
 };
+
+// Pinned host memory for spill buffers, carved from large slabs.  Pinning
+// costs about as much per byte as a copy, so it is paid once, when the served
+// set first outgrows the device budget, and not on a request's path.
+// Returned buffers are reused best fit (within twice the size asked).
+class HostPool {
+  public:
+    ~HostPool() {
+        for (void* p : slabs_) cudaFreeHost(p);
+    }
+    void* Take(size_t bytes) {
+        bytes = (bytes + 255) & ~(size_t)255;
+        auto it = free_.lower_bound(bytes);
+        if (it != free_.end() && it->first <= 2 * bytes) {
+            void* p = it->second;
+            size_[p] = it->first;
+            free_.erase(it);
+            return p;
+        }
+        if (left_ < bytes) {
+            if (left_ >= (64u << 10)) Give(cur_, left_);
+            size_t slab = std::max(bytes, kSlab);
+            void* p = nullptr;
+            if (cudaMallocHost(&p, slab) != cudaSuccess) return nullptr;
+            slabs_.push_back(p);
+            pinned_ += slab;
+            cur_ = (char*)p;
+            left_ = slab;
+        }
+        void* p = cur_;
+        cur_ += bytes;
+        left_ -= bytes;
+        size_[p] = bytes;
+        return p;
+    }
+    void Give(void* p) {
+        auto it = size_.find(p);
+        if (it == size_.end()) return;
+        free_.emplace(it->second, p);
+        size_.erase(it);
+    }
+    size_t Pinned() const { return pinned_; }
+    void Abandon() { slabs_.clear(); }
+
+  private:
+    void Give(char* p, size_t bytes) { free_.emplace(bytes, p); }
+    static constexpr size_t kSlab = 256u << 20;
+    std::vector<void*> slabs_;
+    std::multimap<size_t, void*> free_;
+    std::unordered_map<void*, size_t> size_;
+    char* cur_ = nullptr;
+    size_t left_ = 0, pinned_ = 0;
+};
+
+// While a server lives, the device's stream-ordered pool keeps the memory that
+// spills free instead of handing it back to the driver at the next
+// synchronisation: a restore then reuses mapped memory (tens of microseconds)
+// rather than mapping new pages.  The pool's own threshold is put back when
+// the last server of the device goes.
+void HoldPoolMemory(int device, bool hold) {
+    static std::mutex mu;
+    static std::unordered_map<int, std::pair<int, uint64_t>> held;  // device -> servers, saved threshold
+    std::lock_guard<std::mutex> g(mu);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
+    auto& h = held[device];
+    if (hold) {
+        if (h.first++ == 0) {
+            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &h.second);
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    } else if (h.first > 0 && --h.first == 0) {
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &h.second);
+        cudaMemPoolTrimTo(pool, 0);
+    }
+}
 
 }  // namespace
 
@@ -76,6 +156,13 @@ struct Server {
     std::unordered_map<int32_t, int> slotOf;
     std::deque<int> ready;
     uint64_t useClock = 0;
+    // resident scenes by last use; an entry whose scene has queued or running
+    // requests is skipped (and dropped) when victims are picked, and comes back
+    // when the scene's wave finishes
+    std::set<std::pair<uint64_t, int>> lru;
+    HostPool hostPool;
+    bool lending = false;  // the served set outgrew the budget: every scene holds a spill buffer
+    uint64_t servedBytes = 0;
 
     std::vector<SceneView> viewsHost;
     SceneView* viewsDev = nullptr;
@@ -100,6 +187,7 @@ struct Server {
     // stats (worker-written, read under regMu)
     uint64_t statWaves = 0, statWaveScenes = 0, statLaunches = 0, statSpills = 0, statRestores = 0;
     uint64_t statRoomWaits = 0, statRestoreFailures = 0;
+    double usSpill = 0, usRestore = 0;
     uint64_t residentBytes = 0, peakResident = 0, spilledBytes = 0;
 
     Server(size_t cap) : submitQ(cap), doneQ(cap) {}
@@ -128,27 +216,57 @@ struct Server {
         completed.fetch_add(1, std::memory_order_release);
     }
 
-    // Spill least recently used idle scenes until `need` more bytes fit.
+    void Touch(int id) {
+        Slot& sl = slots[id];
+        lru.erase({sl.lastUse, id});
+        sl.lastUse = ++useClock;
+        lru.insert({sl.lastUse, id});
+    }
+
+    // Every served scene gets a pinned spill buffer from the pool.
+    void LendSpillBuffers(Scene* only) {
+        for (Slot& sl : slots) {
+            if (!sl.live || (only && sl.s != only) || sl.s->spillHost) continue;
+            sl.s->LendSpillBuffer(hostPool.Take(sl.s->arenaBytes));
+        }
+    }
+
+    // Spill least recently used idle scenes until `need` more bytes fit.  The
+    // victims' copies run together; their streams are drained before this
+    // returns, so the freed device memory is back in the pool for restores.
     bool MakeRoom(size_t need) {
+        if (residentBytes + need <= cfg.device_budget_bytes) return true;
+        double t0 = NowUs();
+        std::vector<Scene*> spilled;
+        bool ok = true;
         while (residentBytes + need > cfg.device_budget_bytes) {
-            int victim = -1;
-            for (int i = 0; i < (int)slots.size(); i++) {
-                const Slot& v = slots[i];
-                if (!v.live || !v.s->arena || v.inFlight || !v.pending.empty()) continue;
-                if (victim < 0 || v.lastUse < slots[victim].lastUse) victim = i;
+            if (lru.empty()) {
+                ok = false;
+                break;
             }
-            if (victim < 0) return false;
-            Scene* s = slots[victim].s;
+            const int id = lru.begin()->second;
+            lru.erase(lru.begin());
+            const Slot& v = slots[id];
+            if (!v.live || !v.s->arena || v.inFlight || !v.pending.empty()) continue;
+            Scene* s = v.s;
             size_t bytes = s->DeviceBytes();
-            if (s->Spill(&sink) != BEPUGPU_OK) {
+            if (s->Spill(&sink, false) != BEPUGPU_OK) {
                 SetError(sink.lastError);
-                return false;
+                ok = false;
+                break;
             }
+            spilled.push_back(s);
             residentBytes -= bytes;
             spilledBytes += bytes;
             statSpills++;
         }
-        return true;
+        for (Scene* s : spilled)
+            if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
+                SetError("spill copy failed");
+                ok = false;
+            }
+        usSpill += NowUs() - t0;
+        return ok;
     }
 
     void EnsureViewCapacity() {
@@ -178,7 +296,7 @@ struct Server {
             for (size_t k = 0; k < w.slotIds.size(); k++) {
                 Slot& sl = slots[w.slotIds[k]];
                 sl.inFlight = false;
-                sl.lastUse = ++useClock;
+                Touch(w.slotIds[k]);
                 sl.s->asyncPending = false;
                 if (!sl.pending.empty() && !sl.queued) {
                     sl.queued = true;
@@ -227,8 +345,12 @@ struct Server {
         int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0, passes = 0;
         std::vector<int> plain;
         std::deque<int> keep;
-        bool noRoom = false;
-        while (!ready.empty() && w.slotIds.size() < cfg.max_wave_scenes) {
+        std::vector<Scene*> restored;  // copies in flight on their scenes' streams
+        // The wave's scenes first, then room for all of its spilled ones at
+        // once (one round of spill copies), then their restores.
+        std::vector<int> chosen;
+        size_t need = 0;
+        while (!ready.empty() && chosen.size() < cfg.max_wave_scenes) {
             int id = ready.front();
             ready.pop_front();
             Slot& sl = slots[id];
@@ -236,22 +358,54 @@ struct Server {
                 sl.queued = false;
                 continue;
             }
+            chosen.push_back(id);
+            if (!sl.s->arena) need += sl.s->DeviceBytes();
+        }
+        if (need) MakeRoom(need);  // may free less; the scenes that do not fit wait
+        bool noRoom = false;
+        for (size_t c = 0;; c++) {
+            int id;
+            if (c < chosen.size()) {
+                id = chosen[c];
+            } else {
+                // Some chosen scenes wait for room: resident scenes queued behind
+                // them fill the wave (they need none), so the scenes that hold
+                // the device keep finishing and become spill victims.
+                if (ready.empty() || w.slotIds.size() >= cfg.max_wave_scenes) break;
+                id = ready.front();
+                ready.pop_front();
+                Slot& sl = slots[id];
+                if (!sl.live || sl.pending.empty()) {
+                    sl.queued = false;
+                    continue;
+                }
+                if (!sl.s->arena) {
+                    statRoomWaits++;
+                    keep.push_back(id);
+                    continue;
+                }
+            }
+            Slot& sl = slots[id];
             Scene* s = sl.s;
             if (!s->arena) {
-                // Once no room could be made, later spilled scenes of this wave
-                // wait too (a room search scans every scene).
-                if (noRoom || !MakeRoom(s->DeviceBytes())) {
+                // Once one spilled scene finds no room, later ones of this wave
+                // wait too, so they keep their order.
+                if (noRoom || residentBytes + s->DeviceBytes() > cfg.device_budget_bytes) {
                     noRoom = true;
                     statRoomWaits++;
                     keep.push_back(id);  // waits for room; stays ready
                     continue;
                 }
-                if (s->Restore(&sink) != BEPUGPU_OK) {
+                const double t0 = NowUs();
+                const bepugpu_status rs = s->Restore(&sink, nullptr, false);
+                usRestore += NowUs() - t0;
+                if (rs != BEPUGPU_OK) {
                     SetError(sink.lastError);
                     statRestoreFailures++;
                     keep.push_back(id);
                     continue;
                 }
+                restored.push_back(s);
                 residentBytes += s->DeviceBytes();
                 spilledBytes -= s->DeviceBytes();
                 peakResident = std::max(peakResident, residentBytes);
@@ -284,6 +438,13 @@ struct Server {
             }
         }
         for (auto it = keep.rbegin(); it != keep.rend(); ++it) ready.push_front(*it);
+        cudaError_t e = cudaSuccess;
+        if (!restored.empty()) {
+            const double t0 = NowUs();
+            for (Scene* s : restored)
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            usRestore += NowUs() - t0;
+        }
         if (w.slotIds.empty()) return false;
         // one launch's shared-lane groups must fit a CTA's shared memory together
         if (GroupSmemBytes(true, sBc, sLc) > kGroupSmemBudget + 16 * 1024) {
@@ -293,7 +454,7 @@ struct Server {
             shared.clear();
         }
         EnsureViewCapacity();
-        cudaError_t e = viewsDev ? cudaSuccess : cudaErrorMemoryAllocation;
+        if (e == cudaSuccess && !viewsDev) e = cudaErrorMemoryAllocation;
         // Synchronous copies: any later wave, on any stream, may read these entries.
         if (dirtyViews.size() > 32) {
             if (e == cudaSuccess)
@@ -352,7 +513,13 @@ struct Server {
         if (e != cudaSuccess) {
             SetError(std::string("wave launch: ") + cudaGetErrorString(e));
             for (size_t k = 0; k < w.slotIds.size(); k++) {
-                slots[w.slotIds[k]].inFlight = false;
+                Slot& sl = slots[w.slotIds[k]];
+                sl.inFlight = false;
+                Touch(w.slotIds[k]);
+                if (!sl.pending.empty() && !sl.queued) {
+                    sl.queued = true;
+                    ready.push_back(w.slotIds[k]);
+                }
                 Complete(w.reqs[k], BEPUGPU_CUDA_ERROR, w.id, w.startUs);
             }
             return true;
@@ -388,13 +555,56 @@ struct Server {
     }
 };
 
+// Stops the worker (waves on the device finish first), restores spilled
+// scenes and hands every scene back to its context.
+bepugpu_status Shutdown(Server* s) {
+    s->stop.store(true);
+    s->wake.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    cudaSetDevice(s->ctx->device);
+    bepugpu_status st = BEPUGPU_OK;
+    bool stranded = false;
+    for (auto& sl : s->slots) {
+        if (!sl.live) continue;
+        if (!sl.s->arena && sl.s->Restore(s->ctx) != BEPUGPU_OK) {
+            st = BEPUGPU_OUT_OF_MEMORY;
+            // still spilled: its data must outlive the server's pool
+            if (!sl.s->OwnSpillBuffer()) stranded = true;
+        }
+        sl.s->DropBorrowedSpillBuffer();
+        sl.s->server = nullptr;
+    }
+    if (stranded) s->hostPool.Abandon();  // a scene still reads a slab: keep them all
+
+    for (auto& w : s->waves) {
+        if (w.workDev) cudaFree(w.workDev);
+        if (w.workHost) cudaFreeHost(w.workHost);
+        cudaEventDestroy(w.done);
+        cudaStreamDestroy(w.stream);
+    }
+    if (s->viewsDev) cudaFree(s->viewsDev);
+    HoldPoolMemory(s->ctx->device, false);
+    delete s;
+    return st;
+}
+
 }  // namespace bepugpu
 
 using namespace bepugpu;
 
 struct bepugpu_server {
-    Server* s;
+    Server* s;  // null once the server's context was destroyed
 };
+
+namespace bepugpu {
+void ShutdownServers(Context* ctx) {
+    for (bepugpu_server* h : ctx->servers) {
+        Shutdown(h->s);
+        h->s = nullptr;
+    }
+    ctx->servers.clear();
+}
+}  // namespace bepugpu
 
 extern "C" {
 
@@ -430,13 +640,7 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
     s->cfg = *config;
     s->cfg.flags &= BEPUGPU_STEP_ALL;
     s->p = MakeParams(ctx->settings, config->dt);
-    // Let the device's stream-ordered pool keep up to a budget of freed spill
-    // memory, so restores reuse it instead of returning it to the driver.
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) {
-        uint64_t keep = config->device_budget_bytes;
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-    }
+    HoldPoolMemory(ctx->device, true);
     s->waves.resize(config->max_waves_in_flight);
     for (auto& w : s->waves) {
         if (cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -446,44 +650,39 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
                 if (x.stream) cudaStreamDestroy(x.stream);
                 if (x.done) cudaEventDestroy(x.done);
             }
+            HoldPoolMemory(ctx->device, false);
             delete s;
             return BEPUGPU_CUDA_ERROR;
         }
     }
     s->worker = std::thread([s] { s->Run(); });
     *out = new bepugpu_server{s};
+    ctx->servers.push_back(*out);
     return BEPUGPU_OK;
 }
 
 bepugpu_status bepugpu_server_destroy(bepugpu_server* h) {
     if (!h) return BEPUGPU_INVALID_ARGUMENT;
-    Server* s = h->s;
-    s->stop.store(true);
-    s->wake.notify_all();
-    if (s->worker.joinable()) s->worker.join();
-    cudaSetDevice(s->ctx->device);
     bepugpu_status st = BEPUGPU_OK;
-    for (auto& sl : s->slots) {
-        if (!sl.live) continue;
-        if (!sl.s->arena && sl.s->Restore(s->ctx) != BEPUGPU_OK) st = BEPUGPU_OUT_OF_MEMORY;
-        sl.s->DropBorrowedSpillBuffer();
-        sl.s->server = nullptr;
+    if (h->s) {
+        auto& list = h->s->ctx->servers;
+        list.erase(std::remove(list.begin(), list.end(), h), list.end());
+        st = Shutdown(h->s);
     }
-
-    for (auto& w : s->waves) {
-        if (w.workDev) cudaFree(w.workDev);
-        if (w.workHost) cudaFreeHost(w.workHost);
-        cudaEventDestroy(w.done);
-        cudaStreamDestroy(w.stream);
-    }
-    if (s->viewsDev) cudaFree(s->viewsDev);
-    delete s;
     delete h;
     return st;
 }
 
+#define SERVER_CHECK(h)                                               \
+    do {                                                              \
+        if (!(h)) return BEPUGPU_INVALID_ARGUMENT;                    \
+        if (!(h)->s) return BEPUGPU_INVALID_OPERATION; /* context gone */ \
+    } while (0)
+
+
+
 bepugpu_status bepugpu_server_add_scene(bepugpu_server* h, int32_t scene) {
-    if (!h) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
     Server* s = h->s;
     Context* ctx = s->ctx;
     cudaSetDevice(ctx->device);
@@ -526,6 +725,14 @@ bepugpu_status bepugpu_server_add_scene(bepugpu_server* h, int32_t scene) {
     sl.lastUse = ++s->useClock;
     s->slots.push_back(sl);
     s->slotOf[scene] = id;
+    s->lru.insert({sl.lastUse, id});
+    s->servedBytes += sc->DeviceBytes();
+    // Once the served scenes outgrow the budget any of them may be spilled:
+    // all get pinned spill buffers now rather than on a request's path.
+    if (s->servedBytes > s->cfg.device_budget_bytes) {
+        s->LendSpillBuffers(s->lending ? sc : nullptr);
+        s->lending = true;
+    }
     s->viewsHost.push_back(MakeView(*sc));
     s->dirtyViews.push_back(id);
     sc->server = s;
@@ -545,7 +752,7 @@ bepugpu_status bepugpu_server_add_scene(bepugpu_server* h, int32_t scene) {
 #define CK_SYNC(sc) cudaStreamSynchronize((sc)->stream)
 
 bepugpu_status bepugpu_server_release_scene(bepugpu_server* h, int32_t scene, uint32_t timeout_ms) {
-    if (!h) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
     Server* s = h->s;
     cudaSetDevice(s->ctx->device);
     double until = NowUs() + 1000.0 * timeout_ms;
@@ -568,8 +775,11 @@ bepugpu_status bepugpu_server_release_scene(bepugpu_server* h, int32_t scene, ui
                 }
                 sl.live = false;
                 sl.queued = false;
+                s->lru.erase({sl.lastUse, it->second});
+                s->servedBytes -= sc->DeviceBytes();
                 s->slotOf.erase(it);
                 CK_SYNC(sc);
+                if (sc->spillHostBorrowed) s->hostPool.Give(sc->spillHost);
                 sc->DropBorrowedSpillBuffer();
                 sc->server = nullptr;
                 return BEPUGPU_OK;
@@ -581,7 +791,8 @@ bepugpu_status bepugpu_server_release_scene(bepugpu_server* h, int32_t scene, ui
 }
 
 bepugpu_status bepugpu_serve_submit(bepugpu_server* h, int32_t scene, uint32_t steps, uint64_t tag) {
-    if (!h || steps == 0 || steps > 65535) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
+    if (steps == 0 || steps > 65535) return BEPUGPU_INVALID_ARGUMENT;
     Server* s = h->s;
     ServeRequest r{scene, steps, tag, NowUs()};
     if (!s->submitQ.Push(r)) return BEPUGPU_QUEUE_FULL;
@@ -591,7 +802,8 @@ bepugpu_status bepugpu_serve_submit(bepugpu_server* h, int32_t scene, uint32_t s
 }
 
 bepugpu_status bepugpu_serve_poll(bepugpu_server* h, bepugpu_completion* out, uint32_t max, uint32_t* count) {
-    if (!h || (max && !out) || !count) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
+    if ((max && !out) || !count) return BEPUGPU_INVALID_ARGUMENT;
     uint32_t n = 0;
     while (n < max && h->s->doneQ.Pop(out[n])) n++;
     *count = n;
@@ -599,7 +811,7 @@ bepugpu_status bepugpu_serve_poll(bepugpu_server* h, bepugpu_completion* out, ui
 }
 
 bepugpu_status bepugpu_server_drain(bepugpu_server* h, uint32_t timeout_ms) {
-    if (!h) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
     Server* s = h->s;
     double until = NowUs() + 1000.0 * timeout_ms;
     while (s->completed.load(std::memory_order_acquire) < s->submitted.load(std::memory_order_acquire)) {
@@ -610,7 +822,8 @@ bepugpu_status bepugpu_server_drain(bepugpu_server* h, uint32_t timeout_ms) {
 }
 
 bepugpu_status bepugpu_server_stats_get(bepugpu_server* h, bepugpu_server_stats* out) {
-    if (!h || !out) return BEPUGPU_INVALID_ARGUMENT;
+    SERVER_CHECK(h);
+    if (!out) return BEPUGPU_INVALID_ARGUMENT;
     Server* s = h->s;
     std::lock_guard<std::mutex> g(s->regMu);
     std::memset(out, 0, sizeof(*out));
@@ -623,6 +836,9 @@ bepugpu_status bepugpu_server_stats_get(bepugpu_server* h, bepugpu_server_stats*
     out->restores = s->statRestores;
     out->room_waits = s->statRoomWaits;
     out->restore_failures = s->statRestoreFailures;
+    out->spill_us = (uint64_t)s->usSpill;
+    out->restore_us = (uint64_t)s->usRestore;
+    out->pinned_bytes = s->hostPool.Pinned();
     out->resident_bytes = s->residentBytes;
     out->peak_resident_bytes = s->peakResident;
     out->spilled_bytes = s->spilledBytes;
@@ -636,6 +852,7 @@ bepugpu_status bepugpu_server_stats_get(bepugpu_server* h, bepugpu_server_stats*
 
 const char* bepugpu_server_last_error(bepugpu_server* h) {
     if (!h) return "";
+    if (!h->s) return "the server's context was destroyed";
     static thread_local std::string copy;
     std::lock_guard<std::mutex> g(h->s->errMu);
     copy = h->s->lastError;

@@ -77,7 +77,7 @@ SERVER_STATS_DTYPE = np.dtype([
     ("submitted", "<u8"), ("completed", "<u8"), ("waves", "<u8"), ("wave_scenes", "<u8"), ("launches", "<u8"),
     ("spills", "<u8"), ("restores", "<u8"), ("resident_bytes", "<u8"), ("peak_resident_bytes", "<u8"),
     ("spilled_bytes", "<u8"), ("scenes", "<u4"), ("resident_scenes", "<u4"), ("room_waits", "<u8"),
-    ("restore_failures", "<u8"),
+    ("restore_failures", "<u8"), ("spill_us", "<u8"), ("restore_us", "<u8"), ("pinned_bytes", "<u8"),
 ])
 
 PHASE_TIMES_DTYPE = np.dtype([

@@ -433,6 +433,9 @@ typedef struct bepugpu_server_stats {
     uint32_t scenes, resident_scenes;
     uint64_t room_waits;        /* times a spilled scene waited a wave for room */
     uint64_t restore_failures;  /* restores that could not get device memory */
+    uint64_t spill_us;          /* worker time spent spilling (copies included) */
+    uint64_t restore_us;        /* worker time spent restoring (copies included) */
+    uint64_t pinned_bytes;      /* pinned host memory the server holds for spill buffers */
 } bepugpu_server_stats;
 
 void bepugpu_server_default_config(bepugpu_server_config* out);

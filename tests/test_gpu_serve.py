@@ -90,7 +90,7 @@ def test_same_alone_and_in_the_mix(gpu_context):
     results, done, stats = _serve(gpu_context, pool, reqs)
     assert len(done) == len(reqs) and np.all(done["status"] == N.OK)
     assert sorted(done["tag"].tolist()) == list(range(len(reqs)))
-    assert stats["waves"] >= 1 and stats["spills"] == 0
+    assert stats["waves"] >= 1 and stats["spills"] == 0 and stats["pinned_bytes"] == 0
     assert np.all(done["done_us"] >= done["start_us"]) and np.all(done["start_us"] >= done["submit_us"])
     _check_same_alone(gpu_context, pool, reqs, results)
 
@@ -117,7 +117,37 @@ def test_spill_and_restore_are_bit_identical(gpu_context):
     results, done, stats = _serve(gpu_context, pool, reqs, budget_bytes=budget, max_wave_scenes=4)
     assert np.all(done["status"] == N.OK)
     assert stats["spills"] > 0 and stats["restores"] > 0
+    # the served set outgrew the budget: spill buffers come from the pinned pool
+    assert stats["pinned_bytes"] > 0
     _check_same_alone(gpu_context, pool, reqs, results)
+
+
+def test_close_with_scenes_spilled(gpu_context):
+    """Closing a server restores its spilled scenes before its pinned pool goes:
+    the scenes keep their state and step on alone afterwards."""
+    gpu_context.set_settings(default_settings())
+    pool = _pool(12, 43)
+    budget = _resident_bytes(gpu_context, pool) // 3
+    spaces = [GpuSpace(gpu_context, b, m) for b, m in pool]
+    srv = Server(gpu_context, dt=float(DT), budget_bytes=budget, max_wave_scenes=3)
+    for sp in spaces:
+        srv.add(sp)
+    reqs = _requests(len(pool), 40, 9)
+    for tag, (i, k) in reqs:
+        while srv.submit(spaces[i].id, k, tag) == N.QUEUE_FULL:
+            pass
+    srv.drain()
+    assert int(srv.stats()["resident_scenes"]) < len(pool)
+    srv.close()  # no release: destroy restores every scene
+    total = np.zeros(len(pool), int)
+    for _, (i, k) in reqs:
+        total[i] += k
+    for i, (sp, (b, m)) in enumerate(zip(spaces, pool)):
+        sp.step(float(DT))  # usable alone again
+        gb = sp.download_bodies(b.copy())
+        ab, _ = _alone(gpu_context, b, m, int(total[i]) + 1)
+        np.testing.assert_array_equal(gb["position"], ab["position"], err_msg=f"scene {i}")
+        sp.close()
 
 
 def test_plain_mode_same_results(gpu_context):
@@ -170,3 +200,23 @@ def test_served_scene_is_locked_and_limits(gpu_context):
     sp.step(DT)
     srv.close()
     sp.close()
+
+
+def test_context_destroyed_under_a_live_server():
+    """Destroying a context stops its servers first (their workers step the
+    context's scenes); the server handle then refuses calls but closes."""
+    from bepuphysics1_gb300.solver import Context
+    ctx = Context(0)
+    ctx.set_settings(default_settings())
+    pool = _pool(6, 61)
+    spaces = [GpuSpace(ctx, b, m) for b, m in pool]
+    srv = Server(ctx, dt=float(DT), budget_bytes=_resident_bytes(ctx, pool) // 2, max_wave_scenes=2)
+    for sp in spaces:
+        srv.add(sp)
+    for t, (i, k) in _requests(len(pool), 30, 3):
+        while srv.submit(spaces[i].id, k, t) == N.QUEUE_FULL:
+            pass
+    ctx.close()  # requests may still be queued or running
+    with pytest.raises(N.BepuError):
+        srv.drain(1000)
+    srv.close()
