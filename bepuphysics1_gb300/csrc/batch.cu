@@ -145,7 +145,7 @@ SceneView MakeView(const Scene& s) {
     return v;
 }
 
-bool Scene::BatchReady() const { return SweepEmpty() && jointCount == 0; }
+bool Scene::BatchReady() const { return SweepEmpty() && jointCount == 0 && generatedCount == 0; }
 
 }  // namespace bepugpu
 

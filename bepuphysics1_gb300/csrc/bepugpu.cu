@@ -164,7 +164,16 @@ __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ re
     if (i >= n) return;
     const bepugpu_manifold& r = rec[i];
     int4 h = m.head[slot_of[i]];
-    if (r.body_a != h.x || r.body_b != h.y || r.contact_count < 0 || r.contact_count > 4) atomicMin(check, i);
+    const uint32_t was = (uint32_t)h.z >> 8;
+    bool bad = r.body_a != h.x || r.body_b != h.y || r.contact_count < 0 || r.contact_count > 4 ||
+               ((r.flags ^ was) & BEPUGPU_MANIFOLD_GENERATED);
+    if (!bad && (r.flags & BEPUGPU_MANIFOLD_GENERATED)) {  // contact_order: a permutation of the contacts
+        const uint32_t code = (uint32_t)r.contact_order ^ 0xE4u;
+        uint32_t seen = 0;
+        for (int k = 0; k < r.contact_count; k++) seen |= 1u << ((code >> (2 * k)) & 3u);
+        bad = seen != (1u << r.contact_count) - 1u;
+    }
+    if (bad) atomicMin(check, i);
 }
 
 // Manifold records -> slots (slot_of[i] is the colour-order slot of record i).
@@ -189,8 +198,9 @@ __global__ void k_unpack_manifolds(const bepugpu_manifold* __restrict__ rec, con
     for (int k = 0; k < 4; k++) pa[k] = k < count ? r.contacts[k].penetration_impulse : 0.f;
     m.penacc[s] = make_float4(pa[0], pa[1], pa[2], pa[3]);
     bool live = count > 0;
+    const int order = (r.flags & BEPUGPU_MANIFOLD_GENERATED) ? r.contact_order : 0;
     m.fricacc[s] = make_float4(live ? r.sliding_impulse[0] : 0.f, live ? r.sliding_impulse[1] : 0.f,
-                               live ? r.twist_impulse : 0.f, 0.f);
+                               live ? r.twist_impulse : 0.f, __int_as_float(order));
     m.saxis[s] = make_float4(r.sliding_axis[0], r.sliding_axis[1], r.sliding_axis[2], 0.f);
     m.mat[s] = make_float4(r.kinetic_friction, r.static_friction, r.bounciness, 0.f);
     m.state[s] = make_uint2(0u, 0u);
@@ -226,7 +236,7 @@ __global__ void __launch_bounds__(kRecordBlock) k_pack_manifold_records(Manifold
         r.sliding_axis[1] = ax.y;
         r.sliding_axis[2] = ax.z;
         r.twist_impulse = f.z;
-        r.reserved = 0;
+        r.contact_order = __float_as_int(f.w);
         const float acc[4] = {pa.x, pa.y, pa.z, pa.w};
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -620,6 +630,7 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     L.groupOffsets = take(4 * (2 * (M + J) + 2)); L.sweepBodies = take(4 * B);
     L.groupJointRefs = take(8 * J); L.groupJointOffsets = take(4 * (2 * (M + J) + 2));
     L.bodyRecords = take(sizeof(bepugpu_body) * B);
+    L.shape = take(16 * B); L.genSlots = take(4 * M);
     arenaBytes = bytes;
     cudaError_t e = cudaMalloc(&arena, bytes);
     if (e != cudaSuccess) {
@@ -675,6 +686,8 @@ void Scene::Rebase() {
     j.state = (uint2*)(base + L.jstate);
     jointOffsetsDev = (int32_t*)(base + L.joffs);
     bodyRecords = (bepugpu_body*)(base + L.bodyRecords);
+    shape = (float4*)(base + L.shape);
+    genSlotsDev = (int32_t*)(base + L.genSlots);
 }
 
 // Moves the arena to pinned host memory and releases the scene's device
@@ -790,7 +803,20 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     const int T = 128;
     launchesPerStep = 0;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-    // Island groups first: one CTA per group runs the group's whole step.
+    // The narrow phase first: it rewrites the GENERATED manifolds' contacts
+    // from the poses the rest of the step starts from.
+    if ((flags & BEPUGPU_STEP_COLLIDE) && generatedCount) {
+        cudaError_t ce = LaunchCollide(this, p, stream);
+        if (ce != cudaSuccess) {
+            cudaGraph_t dropped;
+            cudaStreamEndCapture(stream, &dropped);
+            if (dropped) cudaGraphDestroy(dropped);
+            ctx->SetError("narrow phase launch: %s", cudaGetErrorString(ce));
+            return BEPUGPU_CUDA_ERROR;
+        }
+        launchesPerStep++;
+    }
+    // Island groups next: one CTA per group runs the group's whole step.
     // They share only kinematic bodies (read only) with the sweep path, whose
     // position update of moving kinematic bodies therefore has to follow.
     CK(cudaEventRecordWithFlags(evGroup[0], stream, cudaEventRecordExternal));
@@ -929,6 +955,10 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
         persistentBlocks = std::min(perSm, persistentBlocksPerSm) * ctx->smCount;
     }
     launchesPerStep = 0;
+    if ((flags & BEPUGPU_STEP_COLLIDE) && generatedCount) {
+        CK(LaunchCollide(this, p, stream));
+        launchesPerStep++;
+    }
     CK(cudaEventRecord(evGroup[0], stream));
     if (!groupPlan.groups.empty()) {
         bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false);
@@ -967,6 +997,10 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
     }
     if (planStale) {
         ctx->SetError("bodies changed between dynamic and kinematic: upload the constraints again to recolour");
+        return BEPUGPU_INVALID_OPERATION;
+    }
+    if (generatedCount && (flags & BEPUGPU_STEP_COLLIDE) && hostShapes.size() != (size_t)b.count) {
+        ctx->SetError("the body count changed since the shapes were uploaded: upload the shapes again");
         return BEPUGPU_INVALID_OPERATION;
     }
     bepugpu_status st = RefreshDamping(ctx, dt);
@@ -1025,7 +1059,7 @@ using namespace bepugpu;
 
 // A scene of this context that no server owns (a served scene's device
 // state belongs to the server's worker until it is released).
-static Scene* FindScene(Context* ctx, int32_t id) {
+Scene* bepugpu::FindScene(Context* ctx, int32_t id) {
     auto it = ctx->scenes.find(id);
     if (it == ctx->scenes.end()) {
         ctx->SetError("scene %d does not exist", id);
@@ -1037,7 +1071,7 @@ static Scene* FindScene(Context* ctx, int32_t id) {
     }
     return it->second.get();
 }
-static bepugpu_status SceneMissing(Context* ctx, int32_t id) {
+bepugpu_status bepugpu::SceneMissing(Context* ctx, int32_t id) {
     auto it = ctx->scenes.find(id);
     return it != ctx->scenes.end() && it->second->server ? BEPUGPU_INVALID_OPERATION : BEPUGPU_NOT_FOUND;
 }
@@ -1310,6 +1344,10 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         bepugpu_status jst = UploadJoints(ctx, s, joints, nj);
         if (jst != BEPUGPU_OK) return jst;
     }
+    {
+        bepugpu_status gst = PrepareGenerated(ctx, s, man, nm, s->hostSlotOf);
+        if (gst != BEPUGPU_OK) return gst;
+    }
     return UploadManifoldRecords(ctx, s, man, nm);
 }
 
@@ -1333,8 +1371,8 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
     }, bad, flag);
     if (st != BEPUGPU_OK) return st;
     if (bad >= 0) {
-        ctx->SetError("manifold %d changed its bodies or has a contact count outside 0..4; use "
-                      "bepugpu_upload_constraints to recolour", bad);
+        ctx->SetError("manifold %d changed its bodies or its GENERATED flag, has a contact count outside "
+                      "0..4 or a contact_order that is no permutation; use bepugpu_upload_constraints", bad);
         return BEPUGPU_INVALID_ARGUMENT;
     }
     return UploadManifoldRecords(ctx, s, man, n, true);

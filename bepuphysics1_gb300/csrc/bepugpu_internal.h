@@ -107,6 +107,7 @@ struct ArenaLayout {
     size_t groups, groupBodies, groupRefs, groupOffsets, sweepBodies;
     size_t groupJointRefs, groupJointOffsets;
     size_t bodyRecords;
+    size_t shape, genSlots;
 };
 
 struct Server;
@@ -142,8 +143,16 @@ struct Scene {
         return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && groupPlan.jointGlobalCount == 0 &&
                sweepDynamicCount == 0 && !kinematicMoving;
     }
-    // The whole step is island groups without joints, so a batched launch can run it (batch.cu).
+    // The whole step is island groups without joints or narrow-phase manifolds,
+    // so a batched launch can run it (batch.cu).
     bool BatchReady() const;
+    // Narrow phase (collide.cu): one shape per body once uploaded, and the
+    // slots of GENERATED manifolds.
+    std::vector<bepugpu_shape> hostShapes;
+    float4* shape = nullptr;           // device: size xyz, type bits in w
+    int32_t* genSlotsDev = nullptr;    // device: slots of GENERATED manifolds, ascending
+    int32_t generatedCount = 0;
+    std::vector<int2> hostGenPairs;    // bodies of each GENERATED manifold
     // The colour-sweep part of the joint list: slots [0, jointGlobalCount).
     JointSoA SweepJoints() const {
         JointSoA s = j;
@@ -259,6 +268,19 @@ struct Context {
     std::vector<bepugpu_server*> servers;  // live servers: shut down before the scenes go
     void SetError(const char* fmt, ...);
 };
+
+// A scene of the context that no server owns (null and an error message
+// otherwise), and the status for a missing one: NOT_FOUND, or
+// INVALID_OPERATION when a server owns it.
+Scene* FindScene(Context* ctx, int32_t id);
+bepugpu_status SceneMissing(Context* ctx, int32_t id);
+
+// Narrow phase (collide.cu).  Checks the GENERATED manifolds of a constraint
+// upload against the scene's shapes and their contact_order fields, and
+// stores their slots; LaunchCollide runs the narrow phase over them.
+bepugpu_status PrepareGenerated(Context* ctx, Scene* s, const bepugpu_manifold* man, uint32_t nm,
+                                const std::vector<int32_t>& slotOf);
+cudaError_t LaunchCollide(Scene* s, const StepParams& p, cudaStream_t stream);
 
 // Stops every server of the context and gives its scenes back; their handles
 // then accept only bepugpu_server_destroy (serve.cu).

@@ -151,6 +151,7 @@ struct Generator {
     std::vector<bepugpu_manifold> manifolds;
     std::vector<bepugpu_joint> joints;
     float contactDistance = .1f;
+    bool narrowPhase = false;  // emit empty GENERATED manifolds for candidate pairs
 
     void AddContact(bepugpu_manifold& m, const float p[3], const float n[3], float depth, int id) {
         bepugpu_contact& c = m.contacts[m.contact_count++];
@@ -282,8 +283,24 @@ struct Generator {
         }
     }
 
+    // An empty GENERATED manifold for a pair whose bounding boxes come within
+    // the contact distance: the library's narrow phase fills it.
+    void Candidate(int a, int b) {
+        const Body &A = bodies[a], &B = bodies[b];
+        for (int k = 0; k < 3; k++) {
+            float ea = A.shape == kBox ? A.h[k] : A.h[0], eb = B.shape == kBox ? B.h[k] : B.h[0];
+            if (std::fabs(A.c[k] - B.c[k]) > ea + eb + contactDistance) return;
+        }
+        if (A.shape == kSphere && B.shape == kBox) std::swap(a, b);  // box-sphere pairs put the box first
+        bepugpu_manifold m = NewManifold(a, b);
+        m.flags |= BEPUGPU_MANIFOLD_GENERATED;
+        manifolds.push_back(m);
+    }
+
     void Pair(int a, int b) {
-        if (bodies[a].shape == kBox && bodies[b].shape == kBox) BoxBox(a, b);
+        const bool collidable = bodies[a].shape != kCapsule && bodies[b].shape != kCapsule;
+        if (narrowPhase && collidable) Candidate(a, b);
+        else if (bodies[a].shape == kBox && bodies[b].shape == kBox) BoxBox(a, b);
         else WithSphere(a, b);
     }
 };
@@ -291,6 +308,7 @@ struct Generator {
 }  // namespace
 
 struct bepuscene {
+    std::vector<bepugpu_shape> shapes;
     std::vector<bepugpu_body> bodies;
     std::vector<bepugpu_manifold> manifolds;
     std::vector<bepugpu_joint> joints;
@@ -299,7 +317,19 @@ struct bepuscene {
 static bepuscene* Finish(Generator& g) {
     auto* s = new bepuscene();
     s->bodies.reserve(g.bodies.size());
-    for (const Body& b : g.bodies) s->bodies.push_back(MakeRecord(b));
+    for (const Body& b : g.bodies) {
+        s->bodies.push_back(MakeRecord(b));
+        bepugpu_shape sh;
+        std::memset(&sh, 0, sizeof(sh));
+        if (b.shape == kBox) {
+            sh.type = BEPUGPU_SHAPE_BOX;
+            for (int k = 0; k < 3; k++) sh.size[k] = b.h[k];
+        } else if (b.shape == kSphere) {
+            sh.type = BEPUGPU_SHAPE_SPHERE;
+            sh.size[0] = b.h[0];
+        }
+        s->shapes.push_back(sh);
+    }
     s->manifolds = std::move(g.manifolds);
     s->joints = std::move(g.joints);
     return s;
@@ -349,6 +379,7 @@ int32_t bepuscene_make_pile(const bepuscene_pile_params* p, bepuscene** out) {
     Rng rng(p->seed);
     Generator g;
     g.contactDistance = p->contact_distance;
+    g.narrowPhase = p->narrow_phase != 0;
     Body ground{kBox, {0, -.5f * p->ground_size[1], 0},
                 {.5f * p->ground_size[0], .5f * p->ground_size[1], .5f * p->ground_size[2]}, 0.f, p->ground_friction};
     g.bodies.push_back(ground);
@@ -380,6 +411,7 @@ int32_t bepuscene_make_tower(const bepuscene_tower_params* p, bepuscene** out) {
         return BEPUGPU_INVALID_ARGUMENT;
     Rng rng(p->seed);
     Generator g;
+    g.narrowPhase = p->narrow_phase != 0;
     std::vector<int> heights;
     for (int left = p->body_count; left > 0;) {
         int h = std::min(left, rng.range(p->tower_min, p->tower_max));
@@ -636,6 +668,19 @@ void bepuscene_copy(const bepuscene* s, bepugpu_body* b, bepugpu_manifold* m, be
     if (b && !s->bodies.empty()) std::memcpy(b, s->bodies.data(), s->bodies.size() * sizeof(bepugpu_body));
     if (m && !s->manifolds.empty()) std::memcpy(m, s->manifolds.data(), s->manifolds.size() * sizeof(bepugpu_manifold));
     if (j && !s->joints.empty()) std::memcpy(j, s->joints.data(), s->joints.size() * sizeof(bepugpu_joint));
+}
+
+uint32_t bepuscene_params_size(int32_t kind) {
+    switch (kind) {
+        case 0: return sizeof(bepuscene_pile_params);
+        case 1: return sizeof(bepuscene_tower_params);
+        case 2: return sizeof(bepuscene_chain_params);
+        default: return 0;
+    }
+}
+
+void bepuscene_shapes(const bepuscene* s, bepugpu_shape* shapes) {
+    if (shapes && !s->shapes.empty()) std::memcpy(shapes, s->shapes.data(), s->shapes.size() * sizeof(bepugpu_shape));
 }
 
 void bepuscene_free(bepuscene* s) { delete s; }

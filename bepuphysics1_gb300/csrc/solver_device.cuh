@@ -260,7 +260,8 @@ __device__ __forceinline__ void RefreshManifoldV(const ManifoldSoA& m, const V& 
                                                  const StepParams& p) {
     int4 h = m.head[s];
     int count = h.z & 0xff;
-    if (count == 0) return;
+    // narrow-phase manifolds (flag 4, BEPUGPU_MANIFOLD_GENERATED) are not refreshed
+    if (count == 0 || ((h.z >> 8) & 4)) return;
     int cap = m.capacity;
     float4 pa = make_float4(0, 0, 0, 0), qa = make_float4(0, 0, 0, 1);
     float4 pb = pa, qb = qa;
@@ -372,7 +373,13 @@ __device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si,
     uint32_t st = 0;
     // BEPUGPU_MANIFOLD_ACTIVE = 1, BEPUGPU_MANIFOLD_SOLVER_RULE = 2
     bool groupActive = (mflags & 1u) && (mflags & 2u) && ((hasA && A.dynamic) || (hasB && B.dynamic));
-    if (!groupActive) { mo.state[so] = make_uint2(0u, 0u); return; }
+    // A manifold the sliding update skips keeps its axis; lanes staged in
+    // shared memory must carry it too (they are written back whole).
+    if (!groupActive) {
+        mo.state[so] = make_uint2(0u, 0u);
+        if (mo.saxis != mi.saxis) mo.saxis[so] = mi.saxis[si];
+        return;
+    }
     st |= kGroupActive;
     for (int k = 0; k < count; k++) st |= 1u << (kChildShift + k);
     if (count > 0) st |= kSlidingBit | kTwistBit;
@@ -445,6 +452,7 @@ __device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si,
     }
     if (count == 0) {
         mo.state[so] = make_uint2(st, 0u);
+        if (mo.saxis != mi.saxis) mo.saxis[so] = mi.saxis[si];
         return;
     }
 

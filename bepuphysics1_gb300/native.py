@@ -37,9 +37,10 @@ CONTACT_DTYPE = np.dtype([
 MANIFOLD_DTYPE = np.dtype([
     ("body_a", "<i4"), ("body_b", "<i4"), ("contact_count", "<i4"), ("flags", "<u4"),
     ("kinetic_friction", "<f4"), ("static_friction", "<f4"), ("bounciness", "<f4"),
-    ("sliding_impulse", "<f4", 2), ("sliding_axis", "<f4", 3), ("twist_impulse", "<f4"), ("reserved", "<i4"),
+    ("sliding_impulse", "<f4", 2), ("sliding_axis", "<f4", 3), ("twist_impulse", "<f4"), ("contact_order", "<i4"),
     ("contacts", CONTACT_DTYPE, 4),
 ])
+SHAPE_DTYPE = np.dtype([("type", "<i4"), ("size", "<f4", 3)])
 JOINT_DTYPE = np.dtype([
     ("type", "<i4"), ("body_a", "<i4"), ("body_b", "<i4"), ("flags", "<u4"),
     ("anchor_a", "<f4", 3), ("anchor_b", "<f4", 3), ("axis_a", "<f4", 3), ("axis_b", "<f4", 3),
@@ -53,11 +54,12 @@ PILE_PARAMS_DTYPE = np.dtype([
     ("nx", "<i4"), ("ny", "<i4"), ("nz", "<i4"), ("spacing", "<f4"), ("size_min", "<f4"), ("size_max", "<f4"),
     ("density", "<f4"), ("mass", "<f4"), ("jitter", "<f4"), ("friction_min", "<f4"), ("friction_max", "<f4"),
     ("ground_friction", "<f4"), ("ground_size", "<f4", 3), ("settle_penetration", "<f4"),
-    ("contact_distance", "<f4"), ("seed", "<u8"),
+    ("contact_distance", "<f4"), ("seed", "<u8"), ("narrow_phase", "<i4"),
 ], align=True)
 TOWER_PARAMS_DTYPE = np.dtype([
     ("body_count", "<i4"), ("tower_min", "<i4"), ("tower_max", "<i4"), ("sphere_fraction", "<f4"),
     ("friction", "<f4"), ("tower_spacing", "<f4"), ("settle_penetration", "<f4"), ("seed", "<u8"),
+    ("narrow_phase", "<i4"),
 ], align=True)
 CHAIN_PARAMS_DTYPE = np.dtype([
     ("chains", "<i4"), ("links", "<i4"), ("capsule_radius", "<f4"), ("capsule_length", "<f4"),
@@ -94,10 +96,11 @@ OK, INVALID_ARGUMENT, OUT_OF_MEMORY, ADMISSION_REFUSED, CUDA_ERROR, TIMEOUT, NAN
 STATUS_NAMES = ["OK", "INVALID_ARGUMENT", "OUT_OF_MEMORY", "ADMISSION_REFUSED", "CUDA_ERROR", "TIMEOUT",
                 "NAN_DETECTED", "NOT_FOUND", "QUEUE_FULL", "INVALID_OPERATION"]
 
-STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_ALL = 1, 2, 4, 8, 15
+STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_COLLIDE, STEP_ALL = 1, 2, 4, 8, 16, 31
+SHAPE_NONE, SHAPE_BOX, SHAPE_SPHERE = 0, 1, 2
 NOALLOC_MAX_BODIES, NOALLOC_MAX_MANIFOLDS = 1024, 2048  # bepugpu_step_noalloc limits
 MODE_GRAPH, MODE_PERSISTENT = 0, 1
-MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE = 1, 2
+MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE, MANIFOLD_GENERATED = 1, 2, 4
 JOINT_BALL_SOCKET, JOINT_REVOLUTE_ANGULAR, JOINT_SWING_LIMIT, JOINT_REVOLUTE_LIMIT, JOINT_REVOLUTE = 1, 2, 3, 4, 5
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE = 1, 2
 
@@ -119,6 +122,7 @@ GPU_EXPORTS = {
     "bepugpu_scene_create": (_I, [_P, _U, _U, _U, ctypes.POINTER(_I)]),
     "bepugpu_scene_destroy": (_I, [_P, _I]),
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
+    "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
     "bepugpu_update_bodies": (_I, [_P, _I, _P, _U]),
@@ -164,6 +168,8 @@ SCENE_EXPORTS = {
     "bepuscene_make_chain": (_I, [_P, ctypes.POINTER(_P)]),
     "bepuscene_counts": (None, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "bepuscene_copy": (None, [_P, _P, _P, _P]),
+    "bepuscene_shapes": (None, [_P, _P]),
+    "bepuscene_params_size": (_U, [_I]),
     "bepuscene_free": (None, [_P]),
 }
 

@@ -16,7 +16,7 @@ import numpy as np
 from . import native as N
 
 
-def _collect(handle) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+def _collect(handle, with_shapes: bool = False):
     lib = N.load_scene_library()
     nb, nm, nj = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
     lib.bepuscene_counts(handle, ctypes.byref(nb), ctypes.byref(nm), ctypes.byref(nj))
@@ -24,7 +24,11 @@ def _collect(handle) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
     manifolds = np.zeros(nm.value, N.MANIFOLD_DTYPE)
     joints = np.zeros(nj.value, N.JOINT_DTYPE)
     lib.bepuscene_copy(handle, N.ptr(bodies), N.ptr(manifolds), N.ptr(joints))
+    shapes = np.zeros(nb.value, N.SHAPE_DTYPE)
+    lib.bepuscene_shapes(handle, N.ptr(shapes))
     lib.bepuscene_free(handle)
+    if with_shapes:
+        return bodies, manifolds, joints, shapes
     return bodies, manifolds, joints
 
 
@@ -37,7 +41,7 @@ def make_pile(**overrides):
     h = ctypes.c_void_p()
     st = lib.bepuscene_make_pile(N.ptr(p), ctypes.byref(h))
     N.raise_for(st, "bepuscene_make_pile")
-    return _collect(h)
+    return _collect(h, with_shapes=bool(p["narrow_phase"][0]))
 
 
 def make_tower(body_count: int, seed: int = 1, **overrides):
@@ -51,7 +55,7 @@ def make_tower(body_count: int, seed: int = 1, **overrides):
     h = ctypes.c_void_p()
     st = lib.bepuscene_make_tower(N.ptr(p), ctypes.byref(h))
     N.raise_for(st, "bepuscene_make_tower")
-    return _collect(h)
+    return _collect(h, with_shapes=bool(p["narrow_phase"][0]))
 
 
 def make_chain(**overrides):
@@ -81,6 +85,15 @@ def pile_1k(seed: int = 1234):
 def pile_64k(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):
     return make_pile(nx=nx, ny=ny, nz=nz, spacing=2.0, size_min=0.5, size_max=1.5, density=1.0, jitter=0.1,
                      friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed)
+
+
+def pile_64k_collide(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):
+    """pile_64k with the narrow phase on the device: the same boxes, every pair
+    within the contact distance an empty GENERATED manifold; returns
+    (bodies, manifolds, joints, shapes)."""
+    return make_pile(nx=nx, ny=ny, nz=nz, spacing=2.0, size_min=0.5, size_max=1.5, density=1.0, jitter=0.1,
+                     friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed,
+                     narrow_phase=1)
 
 
 def batch_body_counts(n: int, lo: int, hi: int, seed: int) -> np.ndarray:

@@ -90,10 +90,12 @@ class GpuSpace:
 
     def __init__(self, ctx: Context, bodies: np.ndarray, manifolds: np.ndarray | None = None,
                  joints: np.ndarray | None = None, capacity: tuple[int, int, int] | None = None,
-                 group_policy: tuple[int, int, int, int, int] | None = None, smem_budget: int | None = None):
+                 group_policy: tuple[int, int, int, int, int] | None = None, smem_budget: int | None = None,
+                 shapes: np.ndarray | None = None):
         """group_policy = (enabled, max_bodies, max_manifolds, target_manifolds, threads),
         see bepugpu_set_group_policy; smem_budget = bepugpu_set_group_smem_budget;
-        None keeps the library defaults."""
+        None keeps the library defaults.  shapes: one bepugpu_shape per body,
+        needed by GENERATED manifolds (uploaded before the constraints)."""
         self.ctx = ctx
         lib = ctx.lib
         manifolds = np.zeros(0, N.MANIFOLD_DTYPE) if manifolds is None else manifolds
@@ -108,7 +110,14 @@ class GpuSpace:
         if smem_budget is not None:
             self.set_group_smem_budget(smem_budget)
         self.upload_bodies(bodies)
+        if shapes is not None:
+            self.upload_shapes(shapes)
         self.upload_constraints(manifolds, joints)
+
+    def upload_shapes(self, shapes: np.ndarray):
+        """bepugpu_upload_shapes: one collision shape per body for the narrow phase."""
+        shapes = np.ascontiguousarray(shapes, dtype=N.SHAPE_DTYPE)
+        self.ctx.check(self.ctx.lib.bepugpu_upload_shapes(self.ctx.handle, self.id, N.ptr(shapes), len(shapes)))
 
     def set_group_policy(self, enabled: int = 1, max_bodies: int = 1024, max_manifolds: int = 4096,
                          target_manifolds: int = 64, threads: int = 0):

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 2
+#define BEPUGPU_ABI_VERSION 3
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -99,6 +99,14 @@ typedef struct bepugpu_contact {
 /* Manifold flags. */
 #define BEPUGPU_MANIFOLD_ACTIVE      1u  /* SolverUpdateable.IsActive */
 #define BEPUGPU_MANIFOLD_SOLVER_RULE 2u  /* pair collision rule < CollisionRule.NoSolver */
+/* The narrow phase regenerates this manifold's contacts every step from the
+ * two bodies' shapes (bepugpu_upload_shapes), as the reference's pair handlers
+ * do: BoxContactManifold.cs:122-196 for two boxes, BoxSphereContactManifold.cs
+ * for a box (body_a) and a sphere (body_b), SphereContactManifold.cs for two
+ * spheres.  Contacts are matched to the previous step's by id; matched
+ * contacts keep their warm-start impulse, new ones start at zero.  The
+ * refresher skips such manifolds. */
+#define BEPUGPU_MANIFOLD_GENERATED   4u
 
 /* One ConvexContactManifoldConstraint (ConvexContactManifoldConstraint.cs:12-212):
  * up to four penetration children in contact-add order, then one
@@ -115,7 +123,11 @@ typedef struct bepugpu_manifold {
     float sliding_axis[3];           /* SlidingFrictionTwoAxis.linearA row 1, kept between
                                         steps (SlidingFrictionTwoAxis.cs:341-366), in/out */
     float twist_impulse;             /* TwistFrictionConstraint.accumulatedImpulse, in/out */
-    int32_t reserved;
+    int32_t contact_order;           /* GENERATED manifolds: the order of the manifold's own contact
+                                        list (ContactManifold.contacts, which removes by moving its
+                                        last entry into the gap) as 2-bit indices into contacts[],
+                                        entry i in bits 2i..2i+1, xor 0xE4 -- so 0 means the list is
+                                        in solver order.  Other manifolds: 0.  In/out. */
     bepugpu_contact contacts[BEPUGPU_MAX_CONTACTS];
 } bepugpu_manifold;
 
@@ -184,7 +196,17 @@ typedef struct bepugpu_context bepugpu_context;
 #define BEPUGPU_STEP_FORCES           2u  /* ForceUpdater */
 #define BEPUGPU_STEP_SOLVE            4u  /* Solver */
 #define BEPUGPU_STEP_POSITIONS        8u  /* PositionUpdater (Discrete) */
-#define BEPUGPU_STEP_ALL              15u
+#define BEPUGPU_STEP_COLLIDE         16u  /* narrow phase of GENERATED manifolds (NarrowPhase) */
+#define BEPUGPU_STEP_ALL              31u
+
+/* Collision shapes, one per body, for the narrow phase. */
+#define BEPUGPU_SHAPE_NONE   0
+#define BEPUGPU_SHAPE_BOX    1  /* BoxShape.cs: size = HalfWidth, HalfHeight, HalfLength */
+#define BEPUGPU_SHAPE_SPHERE 2  /* SphereShape.cs: size[0] = Radius (its collision margin) */
+typedef struct bepugpu_shape {
+    int32_t type;                    /* BEPUGPU_SHAPE_* */
+    float size[3];
+} bepugpu_shape;
 
 /* Solve strategies for the one-scene path. */
 #define BEPUGPU_MODE_GRAPH      0  /* one launch per colour sweep, captured in a CUDA graph */
@@ -218,6 +240,13 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* ctx, int32_t scene,
 bepugpu_status bepugpu_upload_constraints(bepugpu_context* ctx, int32_t scene,
                                           const bepugpu_manifold* manifolds, uint32_t manifold_count,
                                           const bepugpu_joint* joints, uint32_t joint_count);
+/* One shape per body, centred on the body's position and turned with its
+ * orientation (a convex entity's collidable, ConvexCollidable.UpdateWorldTransform).
+ * Box sizes and sphere radii must be positive and finite.  A GENERATED manifold
+ * needs both bodies shaped (box-box, box-sphere with the box as body_a, or
+ * sphere-sphere); bepugpu_upload_constraints checks it. */
+bepugpu_status bepugpu_upload_shapes(bepugpu_context* ctx, int32_t scene, const bepugpu_shape* shapes,
+                                     uint32_t count);
 /* Rewrites manifold records in place without recolouring.  Body pairs and the
  * manifold count must be those of the last bepugpu_upload_constraints (checked
  * on the device before anything changes; INVALID_ARGUMENT otherwise). */
@@ -373,7 +402,9 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float d
  * the scratch array's device address; make that first call before any stream
  * capture.  Calls share the scratch array: calls whose work overlaps on the GPU
  * (other host threads, other streams) race and must be serialised by the
- * caller.  Damping factors are computed with the device's double pow. */
+ * caller.  Damping factors are computed with the device's double pow.  There
+ * is no narrow phase here: GENERATED manifolds are stepped with the contacts
+ * they hold (and not refreshed). */
 #define BEPUGPU_NOALLOC_MAX_BODIES 1024
 #define BEPUGPU_NOALLOC_MAX_MANIFOLDS 2048
 #define BEPUGPU_NOALLOC_SCRATCH_BYTES 1606656

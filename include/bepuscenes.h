@@ -41,6 +41,9 @@ typedef struct bepuscene_pile_params {
     float settle_penetration;  /* each resting contact penetrates uniform [0, this] */
     float contact_distance;    /* speculative contacts for gaps up to this */
     uint64_t seed;
+    int32_t narrow_phase;      /* nonzero: every pair whose boxes are within contact_distance gets an
+                                  empty BEPUGPU_MANIFOLD_GENERATED manifold (box first in box-sphere
+                                  pairs) for the library's narrow phase to fill, instead of contacts */
 } bepuscene_pile_params;
 
 /* Towers: one scene of `body_count` bodies (boxes and spheres, 1 m, 1 kg) in
@@ -53,6 +56,7 @@ typedef struct bepuscene_tower_params {
     float tower_spacing;
     float settle_penetration;
     uint64_t seed;
+    int32_t narrow_phase;      /* as in bepuscene_pile_params */
 } bepuscene_tower_params;
 
 /* Chains: `chains` articulated chains of `links` capsules joined alternately by
@@ -78,6 +82,11 @@ int32_t bepuscene_make_chain(const bepuscene_chain_params* p, bepuscene** out);
 void bepuscene_counts(const bepuscene* s, int32_t* bodies, int32_t* manifolds, int32_t* joints);
 void bepuscene_copy(const bepuscene* s, bepugpu_body* bodies, bepugpu_manifold* manifolds,
                     bepugpu_joint* joints);
+/* sizeof of the parameter structs (kind 0 pile, 1 tower, 2 chain), so a
+ * binding can check its layout. */
+uint32_t bepuscene_params_size(int32_t kind);
+/* One collision shape per body: boxes and spheres; capsules have none. */
+void bepuscene_shapes(const bepuscene* s, bepugpu_shape* shapes);
 void bepuscene_free(bepuscene* s);
 
 #ifdef __cplusplus

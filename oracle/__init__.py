@@ -37,6 +37,7 @@ def _load():
             "oracle_permutation_map": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int64, I]),
             "oracle_prime_count": (I, []),
             "oracle_colour": (I, [P, I, P, I, P, I, P, P]),
+            "oracle_set_shapes": (I, [P, P, I]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -75,7 +76,7 @@ def colour(bodies, manifolds, joints=None):
 class OracleSpace:
     """The reference's Space solver stages restated on the CPU."""
 
-    def __init__(self, settings, bodies, manifolds, joints=None):
+    def __init__(self, settings, bodies, manifolds, joints=None, shapes=None):
         from bepuphysics1_gb300 import native as N
         self.N = N
         lib = _load()
@@ -90,6 +91,10 @@ class OracleSpace:
         if not h:
             raise ValueError("oracle rejected the scene")
         self.h = ctypes.c_void_p(h)
+        if shapes is not None:
+            self.shapes = np.ascontiguousarray(shapes, dtype=N.SHAPE_DTYPE)
+            if lib.oracle_set_shapes(self.h, _ptr(self.shapes), len(self.shapes)) != 0:
+                raise ValueError("one shape per body")
 
     def set_list_order(self, order):
         order = np.ascontiguousarray(order, dtype=np.int32)
@@ -99,10 +104,10 @@ class OracleSpace:
     def set_order_mode(self, mode: int, permutation_index: int = 0):
         self.lib.oracle_set_order_mode(self.h, mode, permutation_index)
 
-    def step(self, dt: float, flags: int = 15, steps: int = 1):
+    def step(self, dt: float, flags: int = 31, steps: int = 1):
         self.lib.oracle_step(self.h, dt, flags, steps)
 
-    def step_multithreaded(self, dt: float, flags: int = 15, steps: int = 1, threads: int = 8):
+    def step_multithreaded(self, dt: float, flags: int = 31, steps: int = 1, threads: int = 8):
         self.lib.oracle_step_multithreaded(self.h, dt, flags, steps, threads)
 
     def get_bodies(self):

@@ -31,6 +31,7 @@ inline float Clamp(float v, float lo, float hi) {
 
 // Toolbox constants (BEPUutilities/Toolbox.cs:20,25)
 constexpr float Epsilon = 1e-7f;
+constexpr float BigEpsilon = 1e-5f;
 
 // Vector3 (BEPUutilities/Vector3.cs)
 inline Vec3 Add(const Vec3& a, const Vec3& b) { return {a.X + b.X, a.Y + b.Y, a.Z + b.Z}; }

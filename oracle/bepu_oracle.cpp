@@ -185,6 +185,7 @@ struct Space {
     std::atomic<long long> childSolves{0};
     bool countSolves = true;  // single-threaded runs only: a shared counter would serialize threads
     size_t jointCount = 0;
+    std::vector<bepugpu_shape> shapes;  // one per entity, for GENERATED manifolds
     Entity world;  // TwoEntityConstraint.WorldEntity: kinematic, at the origin, identity orientation
 };
 
@@ -433,6 +434,10 @@ struct ConvexManifold : SolverGroup {
     bool solverRule = true;
     PenetrationConstraint pool[4];
     std::vector<PenetrationConstraint*> penetrationConstraints;  // contact-add order
+    // ContactManifold.contacts: the same contacts in the manifold's own list
+    // order (FastRemoveAt moves the last entry into a removed one's place)
+    std::vector<PenetrationConstraint*> contactList;
+    bool generated = false;  // contacts come from the narrow phase each step
     SlidingFriction slidingFriction;
     TwistFriction twistFriction;
     int sourceIndex = 0;
@@ -481,6 +486,7 @@ struct ConvexManifold : SolverGroup {
         p->entityA = entityA; p->entityB = entityB;
         p->accumulatedImpulse = impulse;
         penetrationConstraints.push_back(p);
+        contactList.push_back(p);
         if (!twistFriction.isActive) {
             twistFriction.isActive = true;
             twistFriction.entityA = entityA; twistFriction.entityB = entityB;
@@ -489,8 +495,22 @@ struct ConvexManifold : SolverGroup {
             slidingFriction.linearA = Mat2x3();
         }
     }
-    // RemoveContact (:135-155): order-preserving removal (RawList.RemoveAt).
+    // ContactManifold.Remove (ContactManifold.cs:51-57): the manifold's list
+    // drops the contact by RawList.FastRemoveAt; the constraint's by RemoveAt.
+    void RemoveListAt(int i) {
+        PenetrationConstraint* p = contactList[i];
+        contactList[i] = contactList.back();
+        contactList.pop_back();
+        for (int k = 0; k < (int)penetrationConstraints.size(); k++)
+            if (penetrationConstraints[k] == p) { RemovePenetrationAt(k); return; }
+    }
     void RemoveContactAt(int i) {
+        PenetrationConstraint* p = penetrationConstraints[i];
+        for (int k = 0; k < (int)contactList.size(); k++)
+            if (contactList[k] == p) { RemoveListAt(k); return; }
+    }
+    // RemoveContact (:135-155): order-preserving removal (RawList.RemoveAt).
+    void RemovePenetrationAt(int i) {
         PenetrationConstraint* p = penetrationConstraints[i];
         p->accumulatedImpulse = 0;
         p->isActive = false;
@@ -810,6 +830,93 @@ static void RefreshManifold(ConvexManifold& m, const Settings& S) {
 }
 
 #include "bepu_oracle_joints.inc"
+#include "bepu_oracle_collide.inc"
+
+// BoxContactManifold.Update, managed branch (BoxContactManifold.cs:122-196):
+// match the new contacts to the kept ones by id (the last match in the new
+// list wins and is consumed), remove the unmatched kept ones from the highest
+// list index down, then add what is left of the new list in its order.
+static void UpdateBoxBoxManifold(Space& sp, ConvexManifold& m) {
+    const bepugpu_shape &sa = sp.shapes[m.entityA->index], &sb = sp.shapes[m.entityB->index];
+    BoxDims a{sa.size[0], sa.size[1], sa.size[2]}, b{sb.size[0], sb.size[1], sb.size[2]};
+    float distance;
+    Vec3 axis;
+    TinyContacts manifold;
+    if (AreBoxesColliding(a, b, m.entityA->position, m.entityA->orientation, m.entityB->position,
+                          m.entityB->orientation, distance, axis, manifold)) {
+        axis = Neg(axis);
+        std::vector<int> toRemove;
+        for (int i = 0; i < (int)m.contactList.size(); i++) {
+            Contact& c = m.contactList[i]->contact;
+            bool found = false;
+            for (int j = manifold.Count - 1; j >= 0; j--) {
+                if (c.Id == manifold.e[j].Id) {
+                    found = true;
+                    c.Position = manifold.e[j].Position;
+                    c.PenetrationDepth = -manifold.e[j].Depth;
+                    c.Normal = axis;
+                    manifold.RemoveAt(j);
+                    break;
+                }
+            }
+            if (!found) toRemove.push_back(i);
+        }
+        for (int i = (int)toRemove.size() - 1; i >= 0; i--) m.RemoveListAt(toRemove[i]);
+        for (int i = 0; i < manifold.Count; i++) {
+            Contact c;
+            c.Position = manifold.e[i].Position;
+            c.PenetrationDepth = -manifold.e[i].Depth;
+            c.Normal = axis;
+            c.Id = manifold.e[i].Id;
+            c.LocalOffsetA = Vec3(); c.LocalOffsetB = Vec3(); c.BasePenetrationDepth = 0;
+            m.AddContact(c, 0.f);
+        }
+    } else {
+        for (int i = (int)m.contactList.size() - 1; i >= 0; i--) m.RemoveListAt(i);
+    }
+}
+
+// SphereContactManifold / BoxSphereContactManifold.Update (:55-83): one
+// contact; a first contact is taken only at non-negative depth.
+static void UpdateOneContactManifold(ConvexManifold& m, bool colliding, const ContactDataO& cd) {
+    bool previouslyColliding = !m.penetrationConstraints.empty();
+    if (colliding) {
+        if (!previouslyColliding && cd.PenetrationDepth >= 0) {
+            Contact c;
+            c.Position = cd.Position;
+            c.Normal = cd.Normal;
+            c.PenetrationDepth = cd.PenetrationDepth;
+            c.Id = 0;
+            c.LocalOffsetA = Vec3(); c.LocalOffsetB = Vec3(); c.BasePenetrationDepth = 0;
+            m.AddContact(c, 0.f);
+        } else if (previouslyColliding) {
+            Contact& c = m.penetrationConstraints[0]->contact;
+            c.Normal = cd.Normal;
+            c.PenetrationDepth = cd.PenetrationDepth;
+            c.Position = cd.Position;
+        }
+    } else if (previouslyColliding) {
+        m.RemoveListAt(0);
+    }
+}
+
+static void CollideManifold(Space& sp, ConvexManifold& m) {
+    const bepugpu_shape &sa = sp.shapes[m.entityA->index], &sb = sp.shapes[m.entityB->index];
+    if (sa.type == BEPUGPU_SHAPE_BOX && sb.type == BEPUGPU_SHAPE_BOX) {
+        UpdateBoxBoxManifold(sp, m);
+    } else if (sa.type == BEPUGPU_SHAPE_SPHERE && sb.type == BEPUGPU_SHAPE_SPHERE) {
+        ContactDataO cd;
+        bool hit = AreSpheresColliding(sa.size[0], sb.size[0], m.entityA->position, m.entityB->position,
+                                       sp.s.maximumContactDistance, cd);
+        UpdateOneContactManifold(m, hit, cd);
+    } else {  // box (A) and sphere (B)
+        ContactDataO cd;
+        BoxDims box{sa.size[0], sa.size[1], sa.size[2]};
+        bool hit = AreBoxSphereColliding(box, sb.size[0], m.entityA->position, m.entityA->orientation,
+                                         m.entityB->position, sp.s.maximumContactDistance, cd);
+        UpdateOneContactManifold(m, hit, cd);
+    }
+}
 
 // ---------------------------------------------------------------- Solver --
 // Solver.cs:265-275
@@ -925,9 +1032,19 @@ static void SolverUpdateMultithreaded(Space& sp, float dt, int threads) {
 }
 
 static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
+    // The narrow phase and the refresher read poses only, so they run before
+    // the force update here (the reference runs them after it, Space.cs:504-513).
+    if (flags & BEPUGPU_STEP_COLLIDE) {
+        for (size_t i = sp.jointCount; i < sp.updateables.size(); i++) {
+            auto* m = static_cast<ConvexManifold*>(sp.updateables[i].get());
+            if (m->generated) CollideManifold(sp, *m);
+        }
+    }
     if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) {
-        for (size_t i = sp.jointCount; i < sp.updateables.size(); i++)
-            RefreshManifold(*static_cast<ConvexManifold*>(sp.updateables[i].get()), sp.s);
+        for (size_t i = sp.jointCount; i < sp.updateables.size(); i++) {
+            auto* m = static_cast<ConvexManifold*>(sp.updateables[i].get());
+            if (!m->generated) RefreshManifold(*m, sp.s);
+        }
     }
     if (flags & BEPUGPU_STEP_FORCES) {  // ForceUpdater.cs:85-92
         Vec3 gravityDt = Multiply(sp.s.gravity, dt);
@@ -1030,6 +1147,7 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
         m->entityB = ent(mr.body_b);
         m->SetInvolved(m->entityA, m->entityB);
         m->isActive = (mr.flags & BEPUGPU_MANIFOLD_ACTIVE) != 0;
+        m->generated = (mr.flags & BEPUGPU_MANIFOLD_GENERATED) != 0;
         m->solverRule = (mr.flags & BEPUGPU_MANIFOLD_SOLVER_RULE) != 0;
         m->kineticFriction = mr.kinetic_friction;
         m->staticFriction = mr.static_friction;
@@ -1055,12 +1173,20 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
             c.BasePenetrationDepth = cr.base_penetration_depth;
             m->AddContact(c, cr.penetration_impulse);
         }
+        if (m->generated && cc > 0) {  // the list order carried in contact_order
+            std::vector<PenetrationConstraint*> list(cc);
+            const uint32_t code = (uint32_t)mr.contact_order ^ 0xE4u;
+            for (int k = 0; k < cc; k++) list[k] = m->penetrationConstraints[(code >> (2 * k)) & 3];
+            m->contactList = list;
+        }
+        // The sliding axis is kept whatever the count (CleanUp leaves linearA;
+        // Setup clears it when a first contact comes); impulses only with contacts.
+        m->slidingFriction.linearA.M11 = mr.sliding_axis[0];
+        m->slidingFriction.linearA.M12 = mr.sliding_axis[1];
+        m->slidingFriction.linearA.M13 = mr.sliding_axis[2];
         if (cc > 0) {
             m->slidingFriction.accX = mr.sliding_impulse[0];
             m->slidingFriction.accY = mr.sliding_impulse[1];
-            m->slidingFriction.linearA.M11 = mr.sliding_axis[0];
-            m->slidingFriction.linearA.M12 = mr.sliding_axis[1];
-            m->slidingFriction.linearA.M13 = mr.sliding_axis[2];
             m->twistFriction.accumulatedImpulse = mr.twist_impulse;
         }
         sp.updateables.emplace_back(m);
@@ -1147,7 +1273,25 @@ void oracle_get_constraints(oracle_space* s, bepugpu_manifold* manifolds, bepugp
         mr.sliding_axis[1] = m->slidingFriction.linearA.M12;
         mr.sliding_axis[2] = m->slidingFriction.linearA.M13;
         mr.twist_impulse = m->twistFriction.accumulatedImpulse;
+        uint32_t code = 0;
+        if (m->generated) {
+            for (int k = 0; k < 4; k++) {
+                uint32_t at = (uint32_t)k;
+                if (k < cc)
+                    for (int q = 0; q < cc; q++)
+                        if (m->penetrationConstraints[q] == m->contactList[k]) at = (uint32_t)q;
+                code |= at << (2 * k);
+            }
+            code ^= 0xE4u;
+        }
+        mr.contact_order = (int32_t)code;
     }
+}
+
+int32_t oracle_set_shapes(oracle_space* s, const bepugpu_shape* shapes, int32_t count) {
+    if (count != (int32_t)s->sp.entities.size()) return -1;
+    s->sp.shapes.assign(shapes, shapes + count);
+    return 0;
 }
 
 int64_t oracle_permutation_map(int64_t permutation_index, int64_t index, int32_t set_size) {

@@ -33,6 +33,8 @@ int32_t oracle_step(oracle_space* s, float dt, uint32_t flags, int32_t steps);
  * stages on `threads` worker threads. */
 int32_t oracle_step_multithreaded(oracle_space* s, float dt, uint32_t flags, int32_t steps,
                                   int32_t threads);
+/* One shape per body, for manifolds flagged BEPUGPU_MANIFOLD_GENERATED. */
+int32_t oracle_set_shapes(oracle_space* s, const bepugpu_shape* shapes, int32_t count);
 void oracle_get_bodies(oracle_space* s, bepugpu_body* out);
 void oracle_get_constraints(oracle_space* s, bepugpu_manifold* manifolds, bepugpu_joint* joints);
 /* Counts of solves executed by the last step (manifold-children and joints). */

@@ -52,16 +52,17 @@ class Pair:
     """A GPU scene and the oracle over the same records, the oracle's solver
     list permuted into the GPU's colour order (identity mapping)."""
 
-    def __init__(self, ctx, bodies, manifolds, joints=None, settings=None, mode=N.MODE_GRAPH, group_policy=None):
+    def __init__(self, ctx, bodies, manifolds, joints=None, settings=None, mode=N.MODE_GRAPH, group_policy=None,
+                 shapes=None):
         self.joints = joints
         self.settings = default_settings() if settings is None else settings
         ctx.set_settings(self.settings)
-        self.gpu = GpuSpace(ctx, bodies, manifolds, joints, group_policy=group_policy)
+        self.gpu = GpuSpace(ctx, bodies, manifolds, joints, group_policy=group_policy, shapes=shapes)
         self.gpu.set_mode(mode)
         colour, order, k = self.gpu.colouring()
         self.colours = k
         self.order = order
-        self.oracle = oracle.OracleSpace(self.settings, bodies, manifolds, joints)
+        self.oracle = oracle.OracleSpace(self.settings, bodies, manifolds, joints, shapes=shapes)
         self.oracle.set_list_order(order)
         self.oracle.set_order_mode(oracle.ORDER_IDENTITY)
 

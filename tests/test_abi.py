@@ -37,7 +37,7 @@ def test_binding_covers_header():
 
 def test_record_sizes():
     lib = N.load_gpu_library()
-    assert lib.bepugpu_abi_version() == 2
+    assert lib.bepugpu_abi_version() == 3
     assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 108
     assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 64
     assert lib.bepugpu_record_size(3) == N.MANIFOLD_DTYPE.itemsize
@@ -70,6 +70,8 @@ def test_create_without_device_fails_cleanly():
 
 
 def test_scene_source_params_layout():
-    # The scene-parameter dtypes mirror the C structs (8-byte aligned seed last).
-    assert N.PILE_PARAMS_DTYPE.itemsize == 80
-    assert N.TOWER_PARAMS_DTYPE.itemsize == 40
+    # The scene-parameter dtypes mirror the C structs (sizes from the library).
+    lib = N.load_scene_library()
+    assert lib.bepuscene_params_size(0) == N.PILE_PARAMS_DTYPE.itemsize == 88
+    assert lib.bepuscene_params_size(1) == N.TOWER_PARAMS_DTYPE.itemsize == 48
+    assert lib.bepuscene_params_size(2) == N.CHAIN_PARAMS_DTYPE.itemsize

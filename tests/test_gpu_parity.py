@@ -220,7 +220,7 @@ def test_manifold_records_roundtrip(gpu_context):
     m["contacts"]["penetration_impulse"] = np.where(live, rng.uniform(0, 1, live.shape), 0).astype(np.float32)
     m["sliding_impulse"] = rng.normal(size=m["sliding_impulse"].shape).astype(np.float32)
     m["twist_impulse"] = rng.normal(size=m["twist_impulse"].shape).astype(np.float32)
-    m["reserved"] = 0
+    m["contact_order"] = 0
     sp = GpuSpace(gpu_context, b, m)
     back, _ = sp.download_constraints(np.zeros_like(m))
     assert back.tobytes() == m.tobytes()
