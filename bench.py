@@ -72,6 +72,8 @@ def parse_args():
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
+    ap.add_argument("--no-collide", action="store_true", help="skip the narrow-phase section")
+    ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
     ap.add_argument("--serve-rates", default="1000,5000,20000,50000,100000,200000",
@@ -426,6 +428,97 @@ def chain_section(args, local, rank, world, pg):
     return out
 
 
+COLLIDE_WORKLOAD = "pile_64k_collide"
+
+
+def collide_section(args, local, rank, world, pg):
+    """The full step with the narrow phase on the device: the 65,536-box pile
+    with every pair an empty GENERATED manifold, so each step regenerates the
+    contacts from the poses (BoxBoxCollider + BoxContactManifold id matching)
+    before the solver.  Device time per step with L2 flushed between steps;
+    the narrow phase alone is timed as steps of the collide stage only."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import Context, GpuSpace, default_settings
+    settings = default_settings()
+    bodies, manifolds, _, shapes = scenes.pile_64k_collide()
+    ctx = Context(local, settings)
+    sp = GpuSpace(ctx, bodies, manifolds, shapes=shapes)
+    for _ in range(max(args.warmup, 3)):
+        sp.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    gm, _ = sp.download_constraints()
+    contacts = int(gm["contact_count"].sum())
+    iters = int(settings["iteration_limit"])
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    step_ms, collide_ms = [], []
+    if pg:
+        pg.barrier()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        sp.step(DT, N.STEP_ALL)
+        step_ms.append(sp.last_step_ms())
+    launches = int(sp.last_step_launches())
+    for _ in range(args.steps):  # the narrow phase alone over the same poses
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        sp.step(DT, N.STEP_COLLIDE)
+        collide_ms.append(sp.last_step_ms())
+    total_ms = float(sum(step_ms))
+    if pg:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        total_ms = float(t.item())
+    pairs = len(manifolds)
+    cms = statistics.mean(collide_ms)
+    # algorithmic bytes of one pair: head, two shapes, two poses, impulses and
+    # the kept contacts' four lanes read (144 + 64 c), the same lanes of the new
+    # contacts and the impulses written (32 + 64 c); c = 4 on the resting pile
+    c_avg = contacts / max(pairs, 1)
+    pair_bytes = 176 + 128 * c_avg
+    peak, peak_kind = measured_hbm_peak()
+    achieved = pairs * pair_bytes / (cms / 1000.0) / 1e9
+    out = {
+        "metric": "contact-iters/s", "workload": COLLIDE_WORKLOAD,
+        "value": world * contacts * iters * args.steps / (total_ms / 1000.0), "unit": "contact-iters/s",
+        "ms_per_step": total_ms / args.steps, "steps_per_s": world * args.steps / (total_ms / 1000.0),
+        "narrow_phase": {"pairs_per_s": world * pairs / (cms / 1000.0), "ms_per_launch": cms,
+                         "kernel": "k_collide", "share_of_step": cms / (total_ms / args.steps),
+                         "roofline": {"bound": "latency (per-pair SAT and clipping in registers and local "
+                                               "memory)", "algorithmic_bytes_per_pair": pair_bytes,
+                                      "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                      "frac": achieved / peak, "peak_kind": peak_kind}},
+        "gpu_launches_per_step": launches,
+        "config": {"bodies": int(len(bodies)), "pairs": pairs, "contacts_after_warmup": contacts,
+                   "iterations": iters, "step": "collide+refresh+forces+solve+positions",
+                   "l2": "flushed between timed steps (512 MiB write)"},
+        "parity": "bit-exact vs the oracle's narrow phase and solver (tests/test_gpu_collide.py)",
+    }
+    sp.close()
+    ctx.close()
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        o = oracle.OracleSpace(settings, bodies, manifolds, shapes=shapes)
+        o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+        steps, t0 = 0, time.perf_counter()
+        while True:
+            o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+            steps += 1
+            if time.perf_counter() - t0 >= args.collide_cpu_seconds:
+                break
+        el = time.perf_counter() - t0
+        o.close()
+        out["cpu_baseline"] = {"value": contacts * iters * steps / el, "unit": "contact-iters/s",
+                               "steps_per_s": steps / el, "cores": threads, "kind": "port",
+                               "sample": f"{steps} full steps with the narrow phase after 1 warm-up step "
+                                         f"(oracle port, {threads} threads, {el:.1f} s)"}
+    return out
+
+
 SERVE_WORKLOAD = "serve_16k"
 SERVE_ITERATIONS = 8
 
@@ -758,6 +851,10 @@ def main():
     if not args.no_chains:
         space.close()
         chains = chain_section(args, local, rank, world, pg)
+    collide = None
+    if not args.no_collide:
+        space.close()
+        collide = collide_section(args, local, rank, world, pg)
     serve = None
     if not args.no_serve:
         space.close()
@@ -784,6 +881,7 @@ def main():
             "clocks": clk.summary(),
             "batch": batch,
             "chains": chains,
+            "collide": collide,
             "serve": serve,
         }
         print(json.dumps(line), flush=True)

@@ -19,7 +19,9 @@
 
 namespace bepugpu {
 
-__global__ void __launch_bounds__(128) k_collide(ManifoldSoA m, BodySoA b, const float4* __restrict__ shape,
+// 64-thread blocks: the pair count (65,536 on the pile) fills only about a
+// fifth of the SMs' warp slots, so smaller blocks spread it more evenly.
+__global__ void __launch_bounds__(64) k_collide(ManifoldSoA m, BodySoA b, const float4* __restrict__ shape,
                                                  const int32_t* __restrict__ slots, int n, StepParams p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) nphase::CollideManifold(m, b, shape, slots[i], p);
@@ -28,7 +30,7 @@ __global__ void __launch_bounds__(128) k_collide(ManifoldSoA m, BodySoA b, const
 cudaError_t LaunchCollide(Scene* s, const StepParams& p, cudaStream_t stream) {
     const int n = s->generatedCount;
     if (n <= 0) return cudaSuccess;
-    const int T = 128;
+    const int T = 64;
     k_collide<<<(n + T - 1) / T, T, 0, stream>>>(s->m, s->b, s->shape, s->genSlotsDev, n, p);
     return cudaGetLastError();
 }

@@ -160,7 +160,7 @@ __device__ __forceinline__ bool SegmentClosest(V3 p1, V3 q1, V3 p2, V3 q2, V3& c
     return true;
 }
 
-__device__ __noinline__ void EdgeEdge(V3 ha, V3 hb, V3 pa, const V3 oa[3], V3 pb, const V3 ob[3], V3 mtd, Cands& out) {
+__device__ __forceinline__ void EdgeEdge(V3 ha, V3 hb, V3 pa, const V3 oa[3], V3 pb, const V3 ob[3], V3 mtd, Cands& out) {
     V3 mA = TimesRows(-mtd, oa), mB = TimesRows(mtd, ob);
     V3 sa[2], ea[2], sb[2], eb[2];
     int saId[2], eaId[2], sbId[2], ebId[2];
@@ -266,7 +266,7 @@ __device__ __forceinline__ bool Intersect(V3 a1, V3 a2, const ClipEdge& ce, V3& 
 
 // ClipFacesDirect (:4517-5278): inside flags per vertex as bits
 // 1 = MaxX, 2 = MinX, 4 = MaxY, 8 = MinY.
-__device__ __noinline__ void ClipFaces(const Face& clip, const Face& face, V3 mtd, Cands& out) {
+__device__ __forceinline__ void ClipFaces(const Face& clip, const Face& face, V3 mtd, Cands& out) {
     V3 clipX = clip.v[3] - clip.v[2], clipY = clip.v[1] - clip.v[2];
     float icw = 1 / clip.width, ich = 1 / clip.height;
     float icw2 = icw * icw;
@@ -391,7 +391,7 @@ __device__ __forceinline__ void Prune(V3 mtd, Cands& c) {
 
 // AreBoxesColliding (:1494-2388).  Returns false when an axis separates the
 // boxes; otherwise the contacts and the minimum axis (pointing from B to A).
-__device__ __noinline__ bool BoxBox(V3 ha, V3 hb, V3 pa, float4 qa, V3 pb, float4 qb, V3& axis, Cands& out) {
+__device__ __forceinline__ bool BoxBox(V3 ha, V3 hb, V3 pa, float4 qa, V3 pb, float4 qb, V3& axis, Cands& out) {
     V3 A[3], B[3];
     Rows(qa, A);
     Rows(qb, B);

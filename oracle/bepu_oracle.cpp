@@ -1034,11 +1034,14 @@ static void SolverUpdateMultithreaded(Space& sp, float dt, int threads) {
 static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
     // The narrow phase and the refresher read poses only, so they run before
     // the force update here (the reference runs them after it, Space.cs:504-513).
-    if (flags & BEPUGPU_STEP_COLLIDE) {
-        for (size_t i = sp.jointCount; i < sp.updateables.size(); i++) {
-            auto* m = static_cast<ConvexManifold*>(sp.updateables[i].get());
+    if (flags & BEPUGPU_STEP_COLLIDE) {  // pairs are independent: the narrow phase's pair loop
+        auto pair = [&](long long i) {
+            auto* m = static_cast<ConvexManifold*>(sp.updateables[sp.jointCount + (size_t)i].get());
             if (m->generated) CollideManifold(sp, *m);
-        }
+        };
+        const long long n = (long long)(sp.updateables.size() - sp.jointCount);
+        if (threads > 1) ForLoop(threads, 0, n, pair);
+        else for (long long i = 0; i < n; i++) pair(i);
     }
     if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) {
         for (size_t i = sp.jointCount; i < sp.updateables.size(); i++) {

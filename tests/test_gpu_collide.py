@@ -202,3 +202,16 @@ def test_boundary_errors(gpu_context):
     sp.step(DT)
     sp.close()
     sp2.close()
+
+
+def test_pile_64k_collide_full_size_two_steps(gpu_context):
+    """The full narrow-phase workload (65,536 pairs of the 65,536-box pile)
+    against the oracle for two steps."""
+    b, m, _, sh = scenes.pile_64k_collide()
+    p = Pair(gpu_context, b, m, settings=default_settings(), shapes=sh)
+    p.step(steps=2)
+    errs, exact = p.compare()
+    assert exact, errs
+    gm = _exact_contacts(p)
+    assert gm["contact_count"].sum() > 250000
+    p.close()
