@@ -828,16 +828,25 @@ def main():
             pg.barrier()
         t0 = time.perf_counter()
         for _ in range(k):
+            space.step_host(hb, hm, DT, N.STEP_ALL)
+        el = time.perf_counter() - t0
+        # the same through the separate calls (update, step, download), for comparison
+        t1 = time.perf_counter()
+        for _ in range(k):
             space.update_bodies(hb)
             space.update_manifolds(hm)
             space.step(DT, N.STEP_ALL)
             space.download_bodies(hb)
             space.download_constraints(hm)
-        el = time.perf_counter() - t0
+        el_calls = time.perf_counter() - t1
         h2d = hb.nbytes + hm.nbytes
-        d2h = hb.nbytes + hm.nbytes  # downloads copy whole body and manifold records
+        d2h = hb.nbytes + hm.nbytes  # whole body and manifold records come back
         e2e = {"value": world * cips * k / el, "unit": "contact-iters/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": 1000 * el / k}
+               "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": 1000 * el / k,
+               "path": "bepugpu_step_host (records up, checked, one step, whole records down; host wall clock)",
+               "separate_calls": {"value": world * cips * k / el_calls, "ms_per_step": 1000 * el_calls / k,
+                                  "path": "update_bodies, update_manifolds, step, download_bodies, "
+                                          "download_constraints"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

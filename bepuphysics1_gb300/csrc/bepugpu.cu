@@ -645,7 +645,9 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     j.capacity = (int)J;
     Rebase();
     CK(cudaMemset(arena, 0, bytes));
-    stagingBytes = std::max(sizeof(bepugpu_body) * B, sizeof(bepugpu_manifold) * M);
+    // body records, then manifold records: bepugpu_step_host stages both at once
+    stagingManifoldsAt = Align(sizeof(bepugpu_body) * B);
+    stagingBytes = stagingManifoldsAt + sizeof(bepugpu_manifold) * M;
     CK(cudaMalloc(&staging, stagingBytes));
     CK(cudaMalloc(&counter, kScratchBytes));
     CK(cudaMemset(counter, 0, kScratchBytes));
@@ -1376,6 +1378,83 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
         return BEPUGPU_INVALID_ARGUMENT;
     }
     return UploadManifoldRecords(ctx, s, man, n, true);
+}
+
+bepugpu_status bepugpu_step_host(bepugpu_context* c, int32_t id, bepugpu_body* bodies, uint32_t nb,
+                                 bepugpu_manifold* man, uint32_t nm, float dt, uint32_t flags) {
+    NvtxRange range("bepugpu_step_host");
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    if (nb != (uint32_t)s->b.count || nm != (uint32_t)s->m.count || (nb && !bodies) || (nm && !man)) {
+        ctx->SetError("step_host needs the %d bodies and %d manifolds of the last uploads", s->b.count, s->m.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->jointCount) {
+        ctx->SetError("step_host takes scenes without joints; use the update, step and download calls");
+        return BEPUGPU_INVALID_OPERATION;
+    }
+    if (!(dt > 0) || !std::isfinite(dt)) {
+        ctx->SetError("dt must be positive and finite");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->asyncPending) {  // an earlier step may still read the staging buffer's neighbours
+        CK(cudaStreamSynchronize(s->stream));
+        s->asyncPending = false;
+    }
+    // Both record arrays up, both checked on the device; one round trip for
+    // the verdict, so nothing changes when a record is refused.
+    bepugpu_body* sb = (bepugpu_body*)s->staging;
+    bepugpu_manifold* sm = (bepugpu_manifold*)((char*)s->staging + s->stagingManifoldsAt);
+    int* check = s->CheckWords();
+    if (nb) CK(cudaMemcpyAsync(sb, bodies, sizeof(bepugpu_body) * nb, cudaMemcpyHostToDevice, s->stream));
+    if (nm) CK(cudaMemcpyAsync(sm, man, sizeof(bepugpu_manifold) * nm, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(check, 0x7f, sizeof(int), s->stream));
+    CK(cudaMemsetAsync(check + 1, 0, sizeof(int), s->stream));
+    CK(cudaMemsetAsync(check + 2, 0x7f, sizeof(int), s->stream));
+    if (nb) k_check_body_records<<<Blocks(nb, 256), 256, 0, s->stream>>>(sb, s->bodyRecords, (int)nb, check);
+    if (nm) k_check_manifold_records<<<Blocks(nm, 256), 256, 0, s->stream>>>(sm, s->slotOf, (int)nm, s->m, check + 2);
+    CK(cudaGetLastError());
+    int h[3];
+    CK(cudaMemcpyAsync(h, check, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (h[0] != 0x7f7f7f7f) {
+        ctx->SetError("body %d changed more than its state (position, orientation, velocities); use "
+                      "bepugpu_upload_bodies", h[0]);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (h[2] != 0x7f7f7f7f) {
+        ctx->SetError("manifold %d changed its bodies or its GENERATED flag, has a contact count outside 0..4 or a "
+                      "contact_order that is no permutation; use bepugpu_upload_constraints", h[2]);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (nb) {
+        k_update_body_state<<<Blocks(nb, 256), 256, 0, s->stream>>>(sb, (int)nb, s->b, s->bodyRecords);
+        k_world_inertia<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, s->localM33);
+    }
+    if (nm) k_unpack_manifolds<<<Blocks(nm, 256), 256, 0, s->stream>>>(sm, s->slotOf, (int)nm, s->m);
+    CK(cudaGetLastError());
+    if ((h[1] != 0) != s->kinematicMoving) {
+        s->kinematicMoving = h[1] != 0;
+        s->version++;
+    }
+    bepugpu_status st = s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
+    if (st != BEPUGPU_OK) return st;
+    // whole records back into the caller's arrays
+    if (nb) {
+        k_patch_body_records<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, s->bodyRecords);
+        CK(cudaMemcpyAsync(bodies, s->bodyRecords, sizeof(bepugpu_body) * nb, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (nm) {
+        k_pack_manifold_records<<<Blocks(nm, kRecordBlock), kRecordBlock, 0, s->stream>>>(s->m, s->slotOf, (int)nm,
+                                                                                        (uint2*)sm);
+        CK(cudaMemcpyAsync(man, sm, sizeof(bepugpu_manifold) * nm, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s->stream));
+    s->asyncPending = false;
+    return BEPUGPU_OK;
 }
 
 bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {

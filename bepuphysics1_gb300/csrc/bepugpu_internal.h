@@ -196,6 +196,7 @@ struct Scene {
     size_t DeviceBytes() const { return arenaBytes + stagingBytes; }
     void* staging = nullptr;
     size_t stagingBytes = 0;
+    size_t stagingManifoldsAt = 0;  // manifold records start here in staging (body records first)
     void* counter = nullptr;  // grid barrier counter / generation / error word
     BodySoA b{};
     ManifoldSoA m{};

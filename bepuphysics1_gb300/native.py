@@ -123,6 +123,7 @@ GPU_EXPORTS = {
     "bepugpu_scene_destroy": (_I, [_P, _I]),
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
+    "bepugpu_step_host": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
     "bepugpu_update_bodies": (_I, [_P, _I, _P, _U]),

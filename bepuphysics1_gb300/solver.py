@@ -152,6 +152,14 @@ class GpuSpace:
         self.ctx.check(self.ctx.lib.bepugpu_update_manifolds(self.ctx.handle, self.id, N.ptr(manifolds),
                                                              len(manifolds)))
 
+    def step_host(self, bodies: np.ndarray, manifolds: np.ndarray, dt: float, flags: int = N.STEP_ALL):
+        """bepugpu_step_host: new body state and manifold records up, one step,
+        whole records back into the same (ideally pinned) arrays."""
+        assert bodies.dtype == N.BODY_DTYPE and manifolds.dtype == N.MANIFOLD_DTYPE
+        assert bodies.flags.c_contiguous and manifolds.flags.c_contiguous
+        self.ctx.check(self.ctx.lib.bepugpu_step_host(self.ctx.handle, self.id, N.ptr(bodies), len(bodies),
+                                                      N.ptr(manifolds), len(manifolds), float(dt), flags))
+
     def set_mode(self, mode: int):
         self.ctx.check(self.ctx.lib.bepugpu_set_solve_mode(self.ctx.handle, self.id, mode))
 

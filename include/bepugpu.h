@@ -261,6 +261,15 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* ctx, int32_t scene,
 bepugpu_status bepugpu_update_bodies(bepugpu_context* ctx, int32_t scene, const bepugpu_body* bodies,
                                      uint32_t count);
 
+/* One step on host records in one call, for scenes without joints: the
+ * bodies' state and the manifold records go up and are checked on the device
+ * as bepugpu_update_bodies / bepugpu_update_manifolds check them (nothing
+ * changes when one is refused), the scene steps with `flags`, and whole body
+ * and manifold records come back into the same arrays, as the downloads write
+ * them.  Two host synchronisations per call instead of one per stage. */
+bepugpu_status bepugpu_step_host(bepugpu_context* ctx, int32_t scene, bepugpu_body* bodies, uint32_t body_count,
+                                 bepugpu_manifold* manifolds, uint32_t manifold_count, float dt, uint32_t flags);
+
 /* Checks every body's position, orientation and velocities for NaN or
  * infinity (the reference's CHECKMATH validation, Toolbox.Validate, off there
  * by default): NAN_DETECTED with *first_bad set to the lowest such body, else

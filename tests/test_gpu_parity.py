@@ -270,6 +270,44 @@ def test_update_bodies_and_manifolds_per_step(gpu_context):
     fast.close()
 
 
+def test_step_host_equals_separate_calls(gpu_context):
+    """bepugpu_step_host gives the bits of update, step and download done
+    separately, refuses a bad record with nothing changed, and takes no scene
+    with joints."""
+    gpu_context.set_settings(default_settings())
+    b, m, _ = scenes.pile_1k()
+    calls = GpuSpace(gpu_context, b, m)
+    one = GpuSpace(gpu_context, b, m)
+    hb, hm = b.copy(), m.copy()
+    ob, om = b.copy(), m.copy()
+    for _ in range(4):
+        calls.update_bodies(hb)
+        calls.update_manifolds(hm)
+        calls.step(DT)
+        hb = calls.download_bodies(hb)
+        hm = calls.download_constraints(hm)[0]
+        one.step_host(ob, om, DT)
+        assert ob.tobytes() == hb.tobytes() and om.tobytes() == hm.tobytes()
+    before = one.download_bodies(ob.copy())
+    bad = ob.copy()
+    bad["inverse_mass"][3] *= 2
+    with pytest.raises(N.ArgumentException):
+        one.step_host(bad, om.copy(), DT)
+    badm = om.copy()
+    badm["contact_count"][2] = 7
+    with pytest.raises(N.ArgumentException):
+        one.step_host(ob.copy(), badm, DT)
+    assert one.download_bodies(ob.copy()).tobytes() == before.tobytes()
+    calls.close()
+    one.close()
+    cb, cm, cj = scenes.make_chain(chains=2, links=4, loose_bodies=2, seed=4,
+                                   region=np.array([6.0, 4.0, 6.0], np.float32))
+    sj = GpuSpace(gpu_context, cb, cm, cj)
+    with pytest.raises(N.InvalidOperationException):
+        sj.step_host(cb.copy(), cm.copy(), DT)
+    sj.close()
+
+
 def test_check_finite_and_bounded_wait(gpu_context):
     """NaN state is reported as NAN_DETECTED with the body's index; a device
     wait on a flag nothing sets gives up with TIMEOUT and the context keeps
