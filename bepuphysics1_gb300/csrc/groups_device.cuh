@@ -16,6 +16,7 @@ namespace bepugpu {
 struct GroupBodies {
     float4 *pos, *quat, *vlin, *vang, *inv0, *inv1;
     BodySoA g;
+    const int32_t* globalOf;  // the group's bodies' global indices
     __device__ __forceinline__ float4 Pos(int r) const { return r >= 0 ? pos[r] : g.pos[-2 - r]; }
     __device__ __forceinline__ float4 Quat(int r) const { return r >= 0 ? quat[r] : g.quat[-2 - r]; }
     __device__ __forceinline__ float4 Vlin(int r) const { return r >= 0 ? vlin[r] : g.vlin[-2 - r]; }
@@ -24,6 +25,10 @@ struct GroupBodies {
     __device__ __forceinline__ float4 Inv1(int r) const { return r >= 0 ? inv1[r] : g.inv1[-2 - r]; }
     __device__ __forceinline__ void SetVelocity(int r, float4 v, float4 w) const {
         if (r >= 0) { vlin[r] = v; vang[r] = w; }  // only a group's own (dynamic) bodies are written
+    }
+    __device__ __forceinline__ void LocalInertia(int r, float4& l0, float4& l1, float& m33) const {
+        const int gi = r >= 0 ? globalOf[r] : -2 - r;
+        l0 = g.loc0[gi]; l1 = g.loc1[gi]; m33 = g.damp[gi].z;
     }
 };
 
@@ -54,6 +59,7 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
     bv.inv0 = bv.vang + Bc;
     bv.inv1 = bv.inv0 + Bc;
     bv.g = b;
+    bv.globalOf = t.bodies + g.bBegin;
     // Solve lanes: in shared memory at local slot j, or the global lanes at
     // slot mBegin + j.
     ManifoldSoA ml = m;

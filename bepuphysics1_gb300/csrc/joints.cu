@@ -43,6 +43,10 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_SWING_LIMIT:
         case BEPUGPU_JOINT_REVOLUTE_LIMIT: return kJChildLimit;
         case BEPUGPU_JOINT_REVOLUTE: return kJChildBall | kJChildAngular | kJChildLimit;
+        case BEPUGPU_JOINT_NO_ROTATION: return kJChildAngular;
+        case BEPUGPU_JOINT_WELD: return kJChildBall | kJChildAngular;
+        case BEPUGPU_JOINT_DISTANCE:
+        case BEPUGPU_JOINT_DISTANCE_LIMIT: return kJChildBall;
         default: return 0;
     }
 }
@@ -69,6 +73,15 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
         // SpringSettings.ComputeErrorReductionAndSoftness throws on this (SpringSettings.cs:104-105)
         if (r.spring_stiffness == 0 && r.spring_damping == 0) {
             ctx->SetError("joint %u: constraints cannot have both 0 stiffness and 0 damping", u);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        // DistanceJoint.Distance, DistanceLimit.MinimumLength / MaximumLength setters keep these
+        if (r.type == BEPUGPU_JOINT_DISTANCE && !(r.limit_min >= 0)) {
+            ctx->SetError("joint %u: distance %g must be non-negative", u, r.limit_min);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if (r.type == BEPUGPU_JOINT_DISTANCE_LIMIT && !(r.limit_min >= 0 && r.limit_min <= r.limit_max)) {
+            ctx->SetError("joint %u: lengths need 0 <= minimum <= maximum", u);
             return BEPUGPU_INVALID_ARGUMENT;
         }
     }
@@ -114,6 +127,17 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
         at(kJBX, slot) = F4(r.basis_x, r.type == BEPUGPU_JOINT_SWING_LIMIT ? r.limit_min : 0.f);
         at(kJTA, slot) = F4(r.test_axis, maxCorrSq);
         at(kJTRIG, slot) = make_float4(sinMin, omcMin, sinMax, omcMax);
+        if (r.type == BEPUGPU_JOINT_NO_ROTATION || r.type == BEPUGPU_JOINT_WELD) {
+            // the initial orientations' conjugates (NoRotationJoint.cs:48-63)
+            const float* qa = r.orientation_a;
+            const float* qb = r.orientation_b;
+            at(kJC1, slot) = make_float4(-qa[0], -qa[1], -qa[2], qa[3]);
+            at(kJC2, slot) = make_float4(-qb[0], -qb[1], -qb[2], qb[3]);
+        }
+        if (r.type == BEPUGPU_JOINT_DISTANCE || r.type == BEPUGPU_JOINT_DISTANCE_LIMIT) {
+            at(kJAXA, slot) = make_float4(r.limit_min, r.limit_max, 0.f, maxCorr);
+            at(kJBP, slot) = make_float4(0.f, 0.f, 0.f, 0.f);  // the limit's last jLinearA
+        }
         // impulses: ball xyz | angular x, angular y | limit x | limit y
         float ball[3] = {0, 0, 0}, ang[2] = {0, 0}, lim[2] = {0, 0};
         switch (r.type) {
@@ -125,6 +149,17 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 std::memcpy(ball, r.impulse, 12);
                 std::memcpy(ang, r.impulse + 3, 8);
                 std::memcpy(lim, r.impulse + 5, 8);
+                break;
+            case BEPUGPU_JOINT_NO_ROTATION:  // angular x, y and (in the limit's first lane) z
+                ang[0] = r.impulse[0]; ang[1] = r.impulse[1]; lim[0] = r.impulse[2];
+                break;
+            case BEPUGPU_JOINT_WELD:
+                std::memcpy(ball, r.impulse, 12);
+                ang[0] = r.impulse[3]; ang[1] = r.impulse[4]; lim[0] = r.impulse[5];
+                break;
+            case BEPUGPU_JOINT_DISTANCE:
+            case BEPUGPU_JOINT_DISTANCE_LIMIT:
+                ball[0] = r.impulse[0];
                 break;
         }
         at(kJACC0, slot) = make_float4(ball[0], ball[1], ball[2], ang[0]);
@@ -180,6 +215,17 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
                 r.impulse[3] = a0.w; r.impulse[4] = a1.x;
                 r.impulse[5] = a1.y; r.impulse[6] = a1.z;
+                break;
+            case BEPUGPU_JOINT_NO_ROTATION:
+                r.impulse[0] = a0.w; r.impulse[1] = a1.x; r.impulse[2] = a1.y;
+                break;
+            case BEPUGPU_JOINT_WELD:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                r.impulse[3] = a0.w; r.impulse[4] = a1.x; r.impulse[5] = a1.y;
+                break;
+            case BEPUGPU_JOINT_DISTANCE:
+            case BEPUGPU_JOINT_DISTANCE_LIMIT:
+                r.impulse[0] = a0.x;
                 break;
         }
     }

@@ -11,6 +11,10 @@
 //   RevoluteAngularJoint  TwoEntity/Joints/RevoluteAngularJoint.cs:226-365
 //   SwingLimit            TwoEntity/JointLimits/SwingLimit.cs:211-347
 //   RevoluteLimit         TwoEntity/JointLimits/RevoluteLimit.cs:285-649
+//   NoRotationJoint       TwoEntity/Joints/NoRotationJoint.cs:160-262 (the angular child of
+//                         NO_ROTATION and WELD records; WeldJoint.cs:15-55 is ball socket + it)
+//   DistanceJoint         TwoEntity/Joints/DistanceJoint.cs:226-380 (the first child slot)
+//   DistanceLimit         TwoEntity/JointLimits/DistanceLimit.cs:260-457 (the first child slot)
 //   SpringSettings        Constraints/SpringSettings.cs:95-110
 // A connection of -1 is TwoEntityConstraint.WorldEntity: kinematic, at the
 // origin, identity orientation, zero velocity.  Its zeros go through the same
@@ -74,14 +78,20 @@ enum : uint32_t {
 };
 // State word x: kGroupActive (bit 0), child isActiveInSolver bits 1-3,
 // limit minIsActive / maxIsActive bits 4-5, kDynA / kDynB (bits 7-8), the
-// record type (bits 9-11), iterations << 16.  Word y: 4-bit zero-impulse
+// record type (bits 9-12), iterations << 16.  Word y: 4-bit zero-impulse
 // streaks of the three children.
 enum : uint32_t {
     kJMinActive = 1u << 4,
     kJMaxActive = 1u << 5,
     kJTypeShift = 9,
 };
-__device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 7u); }
+__device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 15u); }
+__device__ __forceinline__ bool IsDistanceType(int type) {
+    return type == BEPUGPU_JOINT_DISTANCE || type == BEPUGPU_JOINT_DISTANCE_LIMIT;
+}
+__device__ __forceinline__ bool IsNoRotationType(int type) {
+    return type == BEPUGPU_JOINT_NO_ROTATION || type == BEPUGPU_JOINT_WELD;
+}
 
 struct JointSoA {
     int4* head;     // body A, body B, type | flags, source record index
@@ -187,6 +197,7 @@ __device__ __forceinline__ float JBounce(float impactVelocity, float threshold, 
 struct JointBody {
     BodyState s;
     float3 pos;
+    float4 q;
     JM3 R;
     bool dynamic;
 };
@@ -197,6 +208,7 @@ __device__ __forceinline__ void LoadJointBodyV(const V& bv, int r, JointBody& o)
         o.s.wx = o.s.wy = o.s.wz = 0.f;
         o.s.I11 = o.s.I12 = o.s.I13 = o.s.I21 = o.s.I22 = o.s.I23 = o.s.I31 = o.s.I32 = o.s.I33 = 0.f;
         o.pos = make_float3(0.f, 0.f, 0.f);
+        o.q = make_float4(0.f, 0.f, 0.f, 1.f);
         o.R = {1, 0, 0, 0, 1, 0, 0, 0, 1};
         o.dynamic = false;
         return;
@@ -204,8 +216,46 @@ __device__ __forceinline__ void LoadJointBodyV(const V& bv, int r, JointBody& o)
     LoadBodyV(bv, r, o.s);
     float4 p = bv.Pos(r);
     o.pos = make_float3(p.x, p.y, p.z);
-    o.R = JRotation(bv.Quat(r));
+    o.q = bv.Quat(r);
+    o.R = JRotation(o.q);
     o.dynamic = p.w != 0.f;
+}
+// A connection's local inverse inertia (the distance joints' effective mass
+// reads it, DistanceJoint.cs:301-333); only asked for dynamic connections.
+template <class V>
+__device__ __forceinline__ JM3 LoadLocalInertiaV(const V& bv, int r) {
+    float4 l0, l1;
+    float m33;
+    bv.LocalInertia(r, l0, l1, m33);
+    return {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w, m33};
+}
+// Quaternion.Multiply (Quaternion.cs)
+__device__ __forceinline__ float4 JQMul(float4 a, float4 b) {
+    float4 r;
+    r.x = a.x * b.w + b.x * a.w + a.y * b.z - a.z * b.y;
+    r.y = a.y * b.w + b.y * a.w + a.z * b.x - a.x * b.z;
+    r.z = a.z * b.w + b.z * a.w + a.x * b.y - a.y * b.x;
+    r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+    return r;
+}
+// Quaternion.GetAxisAngleFromQuaternion (Quaternion.cs:756-787); Math.Acos in double.
+__device__ __forceinline__ void JAxisAngle(float4 q, float3& axis, float& angle) {
+    float qw = q.w;
+    if (qw > 0) {
+        axis = make_float3(q.x, q.y, q.z);
+    } else {
+        axis = make_float3(-q.x, -q.y, -q.z);
+        qw = -qw;
+    }
+    float lengthSquared = axis.x * axis.x + axis.y * axis.y + axis.z * axis.z;
+    if (lengthSquared > 1e-14f) {
+        float inverse = 1 / SqrtOfFloat(lengthSquared);  // Vector3.Divide
+        axis = make_float3(axis.x * inverse, axis.y * inverse, axis.z * inverse);
+        angle = 2 * (float)acos((double)Clampf(qw, -1, 1));
+    } else {
+        axis = make_float3(0.f, 1.f, 0.f);
+        angle = 0;
+    }
 }
 // Velocity-only view for the warm start and the solve.
 template <class V>
@@ -249,7 +299,87 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
     const float maxCorrSq = ji.L(kJTA, si).w;
     uint32_t active = present & childIsActive;
-    if (active & kJChildBall) {
+    if ((active & kJChildBall) && IsDistanceType(type)) {
+        // DistanceJoint.Update (DistanceJoint.cs:275-352) / DistanceLimit.Update (DistanceLimit.cs:312-430).
+        // Lanes: kJM0 jLinearA + velocityToImpulse, kJM1 jAngularA + bias, kJM2 jAngularB
+        // (jLinearB = -jLinearA); kJOA.w softness.  A limit keeps its last jLinearA in kJBP.
+        const bool isLimit = type == BEPUGPU_JOINT_DISTANCE_LIMIT;
+        const float3 offA = JTransform(JXYZ(la), A.R), offB = JTransform(JXYZ(lb), B.R);
+        const float anx = A.pos.x + offA.x, any = A.pos.y + offA.y, anz = A.pos.z + offA.z;
+        const float bnx = B.pos.x + offB.x, bny = B.pos.y + offB.y, bnz = B.pos.z + offB.z;
+        const float3 sep = make_float3(bnx - anx, bny - any, bnz - anz);
+        const float dist = SqrtOfFloat(sep.x * sep.x + sep.y * sep.y + sep.z * sep.z);
+        const float minL = axa.x, maxL = axa.y;
+        bool on = true;
+        float3 jA, jAngA, jAngB;
+        if (isLimit && dist <= maxL && dist >= minL) {
+            on = false;
+            acc0.x = 0.f;
+        } else if (isLimit && dist > maxL) {
+            jA = JXYZ(ji.L(kJBP, si));  // a degenerate separation keeps the last jLinearA
+            if (dist > 1e-7f) jA = make_float3(sep.x / dist, sep.y / dist, sep.z / dist);
+            jAngA = JCross(jA, offA);
+            jAngB = JCross(jA, offB);
+        } else {
+            float3 jB = make_float3(0.f, 0.f, 0.f);
+            if (dist > 1e-7f) jB = make_float3(sep.x / dist, sep.y / dist, sep.z / dist);
+            jA = make_float3(-jB.x, -jB.y, -jB.z);
+            jAngA = JCross(offA, jB);
+            jAngB = JCross(offB, jB);
+        }
+        if (on) {
+            if (isLimit) {
+                const float4 last = ji.L(kJBP, si);
+                ji.L(kJBP, si) = make_float4(jA.x, jA.y, jA.z, last.w);
+            }
+            const float3 jB = make_float3(-jA.x, -jA.y, -jA.z);
+            float vti;
+            if (A.dynamic && B.dynamic) {
+                float3 aAng = JCross(JTransform(jAngA, LoadLocalInertiaV(bv, ra)), offA);
+                float3 bAng = JCross(JTransform(jAngB, LoadLocalInertiaV(bv, rb)), offB);
+                aAng = make_float3(aAng.x + bAng.x, aAng.y + bAng.y, aAng.z + bAng.z);
+                vti = JDot(aAng, jB);
+                vti += A.s.invMass + B.s.invMass;
+            } else if (A.dynamic) {
+                float3 aAng = JCross(JTransform(jAngA, LoadLocalInertiaV(bv, ra)), offA);
+                vti = JDot(aAng, jB);
+                vti += A.s.invMass;
+            } else {
+                float3 bAng = JCross(JTransform(jAngB, LoadLocalInertiaV(bv, rb)), offB);
+                vti = JDot(bAng, jB);
+                vti += B.s.invMass;
+            }
+            float erp, softness;
+            JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+            vti = 1 / (softness + vti);
+            jAngA = make_float3(-jAngA.x, -jAngA.y, -jAngA.z);
+            float bias;
+            if (!isLimit) {
+                float error = minL - dist;  // Distance - currentDistance
+                bias = Clampf(error * erp, -maxCorr, maxCorr);
+            } else {
+                float error = dist > maxL ? Maxf(0, dist - maxL - margin) : Maxf(0, minL - margin - dist);
+                bias = Minf(erp * error, maxCorr);
+                const float bounciness = ji.L(kJC1, si).w, threshold = ji.L(kJC2, si).w;
+                if (bounciness > 0) {
+                    float rel = jA.x * A.s.vx + jA.y * A.s.vy + jA.z * A.s.vz;
+                    float dot = jAngA.x * A.s.wx + jAngA.y * A.s.wy + jAngA.z * A.s.wz;
+                    rel += dot;
+                    dot = jB.x * B.s.vx + jB.y * B.s.vy + jB.z * B.s.vz;
+                    rel += dot;
+                    dot = jAngB.x * B.s.wx + jAngB.y * B.s.wy + jAngB.z * B.s.wz;
+                    rel += dot;
+                    bias = Maxf(bias, JBounce(-rel, threshold, bounciness));
+                }
+            }
+            j.L(kJOA, s) = make_float4(0.f, 0.f, 0.f, softness);
+            j.L(kJM0, s) = make_float4(jA.x, jA.y, jA.z, vti);
+            j.L(kJM1, s) = make_float4(jAngA.x, jAngA.y, jAngA.z, bias);
+            j.L(kJM2, s) = make_float4(jAngB.x, jAngB.y, jAngB.z, 0.f);
+            st |= 1u << (kChildShift + 0);
+        }
+        j.L(kJACC0, s) = acc0;
+    } else if (active & kJChildBall) {
         // BallSocketJoint.Update (BallSocketJoint.cs:210-278)
         float3 offA = JTransform(JXYZ(la), A.R), offB = JTransform(JXYZ(lb), B.R);
         float erp, softness;
@@ -294,7 +424,40 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM2, s) = make_float4(mass.M33, bx, by, bz);
         st |= 1u << (kChildShift + 0);
     }
-    if (active & kJChildAngular) {
+    if ((active & kJChildAngular) && IsNoRotationType(type)) {
+        // NoRotationJoint.Update (NoRotationJoint.cs:194-243).  Inputs: kJC1 / kJC2 the
+        // initial orientations' conjugates; lanes kJL0..kJL2 the 3x3 effective mass and
+        // the bias, kJOB.w the softness.
+        float4 quaternionA = JQMul(A.q, ji.L(kJC1, si));
+        float4 quaternionB = JQMul(B.q, ji.L(kJC2, si));
+        quaternionB = make_float4(-quaternionB.x, -quaternionB.y, -quaternionB.z, quaternionB.w);
+        float4 intermediate = JQMul(quaternionA, quaternionB);
+        float3 axis;
+        float angle;
+        JAxisAngle(intermediate, axis, angle);
+        float ex = axis.x * angle, ey = axis.y * angle, ez = axis.z * angle;
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        erp = -erp;
+        float bx = erp * ex, by = erp * ey, bz = erp * ez;
+        float length = bx * bx + by * by + bz * bz;
+        if (length > maxCorrSq) {
+            float multiplier = maxCorr / SqrtOfFloat(length);
+            bx *= multiplier; by *= multiplier; bz *= multiplier;
+        }
+        const JM3 ia = JInertia(A.s), ib = JInertia(B.s);  // Matrix3x3.Add, whatever the connections
+        JM3 k = {ia.M11 + ib.M11, ia.M12 + ib.M12, ia.M13 + ib.M13, ia.M21 + ib.M21, ia.M22 + ib.M22,
+                 ia.M23 + ib.M23, ia.M31 + ib.M31, ia.M32 + ib.M32, ia.M33 + ib.M33};
+        k.M11 += softness;
+        k.M22 += softness;
+        k.M33 += softness;
+        JM3 mass = JInvert(k);
+        j.L(kJOB, s).w = softness;
+        j.L(kJL0, s) = make_float4(mass.M11, mass.M12, mass.M13, mass.M21);
+        j.L(kJL1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
+        j.L(kJL2, s) = make_float4(mass.M33, bx, by, bz);
+        st |= 1u << (kChildShift + 1);
+    } else if (active & kJChildAngular) {
         // RevoluteAngularJoint.Update (RevoluteAngularJoint.cs:226-289)
         float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
         float3 c1 = JTransform(JXYZ(ji.L(kJC1, si)), A.R), c2 = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
@@ -493,7 +656,19 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
                                           int type) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
     const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if (st & (1u << kChildShift)) {
+    if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+        // DistanceJoint / DistanceLimit.ExclusiveUpdate (DistanceJoint.cs:354-380)
+        const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
+        const float a = acc0.x;
+        if (dynA) {
+            ApplyLinear(A, m0.x * a, m0.y * a, m0.z * a);
+            ApplyAngular(A, m1.x * a, m1.y * a, m1.z * a);
+        }
+        if (dynB) {
+            ApplyLinear(B, -m0.x * a, -m0.y * a, -m0.z * a);
+            ApplyAngular(B, m2.x * a, m2.y * a, m2.z * a);
+        }
+    } else if (st & (1u << kChildShift)) {
         // BallSocketJoint.ExclusiveUpdate (BallSocketJoint.cs:285-311)
         const float3 offA = JXYZ(j.L(kJOA, s)), offB = JXYZ(j.L(kJOB, s));
         const float3 acc = make_float3(acc0.x, acc0.y, acc0.z);
@@ -509,7 +684,11 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
             ApplyAngular(B, t.x, t.y, t.z);
         }
     }
-    if (st & (2u << kChildShift)) {
+    if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+        // NoRotationJoint.ExclusiveUpdate (NoRotationJoint.cs:245-259)
+        if (dynA) ApplyAngular(A, acc0.w, acc1.x, acc1.y);
+        if (dynB) ApplyAngular(B, -acc0.w, -acc1.x, -acc1.y);
+    } else if (st & (2u << kChildShift)) {
         // RevoluteAngularJoint.ExclusiveUpdate (RevoluteAngularJoint.cs:291-310)
         const float3 c1 = JXYZ(j.L(kJW1, s)), c2 = JXYZ(j.L(kJW2, s));
         float ix = c1.x * acc0.w + c2.x * acc1.x, iy = c1.y * acc0.w + c2.y * acc1.x,
@@ -571,7 +750,38 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
     float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if (st & (1u << kChildShift)) {
+    if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+        // DistanceJoint.SolveIteration (DistanceJoint.cs:226-268) /
+        // DistanceLimit.SolveIteration (DistanceLimit.cs:260-305)
+        const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
+        const float softness = j.L(kJOA, s).w;
+        const float bx = -m0.x, by = -m0.y, bz = -m0.z;  // jLinearB
+        float lambda = m0.x * A.vx + m0.y * A.vy + m0.z * A.vz;
+        float dot = m1.x * A.wx + m1.y * A.wy + m1.z * A.wz;
+        lambda += dot;
+        dot = bx * B.vx + by * B.vy + bz * B.vz;
+        lambda += dot;
+        dot = m2.x * B.wx + m2.y * B.wy + m2.z * B.wz;
+        lambda += dot;
+        lambda = -lambda + m1.w - softness * acc0.x;
+        lambda *= m0.w;
+        if (type == BEPUGPU_JOINT_DISTANCE) {
+            acc0.x += lambda;
+        } else {
+            float previous = acc0.x;
+            acc0.x = Maxf(acc0.x + lambda, 0);
+            lambda = acc0.x - previous;
+        }
+        if (dynA) {
+            ApplyLinear(A, m0.x * lambda, m0.y * lambda, m0.z * lambda);
+            ApplyAngular(A, m1.x * lambda, m1.y * lambda, m1.z * lambda);
+        }
+        if (dynB) {
+            ApplyLinear(B, bx * lambda, by * lambda, bz * lambda);
+            ApplyAngular(B, m2.x * lambda, m2.y * lambda, m2.z * lambda);
+        }
+        account(0, fabsf(lambda));
+    } else if (st & (1u << kChildShift)) {
         // BallSocketJoint.SolveIteration (BallSocketJoint.cs:318-372)
         const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
                      m2 = j.L(kJM2, s);
@@ -601,7 +811,25 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         }
         account(0, fabsf(tx) + fabsf(ty) + fabsf(tz));
     }
-    if (st & (2u << kChildShift)) {
+    if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+        // NoRotationJoint.SolveIteration (NoRotationJoint.cs:160-187)
+        const float4 l0 = j.L(kJL0, s), l1 = j.L(kJL1, s), l2 = j.L(kJL2, s);
+        const float softness = j.L(kJOB, s).w;
+        float lx = B.wx - A.wx, ly = B.wy - A.wy, lz = B.wz - A.wz;
+        float sx = acc0.w * softness, sy = acc1.x * softness, sz = acc1.y * softness;
+        lx = lx + l2.y; ly = ly + l2.z; lz = lz + l2.w;
+        lx = lx - sx; ly = ly - sy; lz = lz - sz;
+        // Matrix3x3.Transform by the effective mass (M11 M12 M13 M21 | M22 M23 M31 M32 | M33)
+        float tx = lx * l0.x + ly * l0.w + lz * l1.z;
+        float ty = lx * l0.y + ly * l1.x + lz * l1.w;
+        float tz = lx * l0.z + ly * l1.y + lz * l2.x;
+        acc0.w = tx + acc0.w;
+        acc1.x = ty + acc1.x;
+        acc1.y = tz + acc1.y;
+        if (dynA) ApplyAngular(A, tx, ty, tz);
+        if (dynB) ApplyAngular(B, -tx, -ty, -tz);
+        account(1, fabsf(tx) + fabsf(ty) + fabsf(tz));
+    } else if (st & (2u << kChildShift)) {
         // RevoluteAngularJoint.SolveIteration (RevoluteAngularJoint.cs:313-356)
         const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s), e = j.L(kJE, s);
         const float softness = j.L(kJOB, s).w;

@@ -107,6 +107,10 @@ struct GlobalBodies {
     __device__ __forceinline__ float4 Inv0(int r) const { return b.inv0[r]; }
     __device__ __forceinline__ float4 Inv1(int r) const { return b.inv1[r]; }
     __device__ __forceinline__ void SetVelocity(int r, float4 v, float4 w) const { b.vlin[r] = v; b.vang[r] = w; }
+    // local inverse inertia: M11 M12 M13 M21, M22 M23 M31 M32, M33
+    __device__ __forceinline__ void LocalInertia(int r, float4& l0, float4& l1, float& m33) const {
+        l0 = b.loc0[r]; l1 = b.loc1[r]; m33 = b.damp[r].z;
+    }
 };
 
 template <class V>

@@ -47,7 +47,7 @@ JOINT_DTYPE = np.dtype([
     ("constrained_1", "<f4", 3), ("constrained_2", "<f4", 3), ("basis_primary", "<f4", 3), ("basis_x", "<f4", 3),
     ("test_axis", "<f4", 3), ("limit_min", "<f4"), ("limit_max", "<f4"), ("margin", "<f4"), ("bounciness", "<f4"),
     ("bounce_velocity_threshold", "<f4"), ("max_corrective_velocity", "<f4"), ("spring_stiffness", "<f4"),
-    ("spring_damping", "<f4"), ("impulse", "<f4", 8),
+    ("spring_damping", "<f4"), ("impulse", "<f4", 8), ("orientation_a", "<f4", 4), ("orientation_b", "<f4", 4),
 ])
 
 PILE_PARAMS_DTYPE = np.dtype([
@@ -102,6 +102,7 @@ NOALLOC_MAX_BODIES, NOALLOC_MAX_MANIFOLDS = 1024, 2048  # bepugpu_step_noalloc l
 MODE_GRAPH, MODE_PERSISTENT = 0, 1
 MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE, MANIFOLD_GENERATED = 1, 2, 4
 JOINT_BALL_SOCKET, JOINT_REVOLUTE_ANGULAR, JOINT_SWING_LIMIT, JOINT_REVOLUTE_LIMIT, JOINT_REVOLUTE = 1, 2, 3, 4, 5
+JOINT_NO_ROTATION, JOINT_WELD, JOINT_DISTANCE, JOINT_DISTANCE_LIMIT = 6, 7, 8, 9
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE = 1, 2
 
 _P = ctypes.c_void_p

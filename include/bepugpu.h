@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 3
+#define BEPUGPU_ABI_VERSION 4
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -140,7 +140,11 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_REVOLUTE_ANGULAR = 2, /* RevoluteAngularJoint.cs:226-365 */
     BEPUGPU_JOINT_SWING_LIMIT = 3,      /* SwingLimit.cs:211-347 */
     BEPUGPU_JOINT_REVOLUTE_LIMIT = 4,   /* RevoluteLimit.cs:285-649 */
-    BEPUGPU_JOINT_REVOLUTE = 5          /* RevoluteJoint group: ball socket + angular + limit */
+    BEPUGPU_JOINT_REVOLUTE = 5,         /* RevoluteJoint group: ball socket + angular + limit */
+    BEPUGPU_JOINT_NO_ROTATION = 6,      /* NoRotationJoint.cs:160-262 */
+    BEPUGPU_JOINT_WELD = 7,             /* WeldJoint group: ball socket + no rotation (WeldJoint.cs:15-55) */
+    BEPUGPU_JOINT_DISTANCE = 8,         /* DistanceJoint.cs:226-380 */
+    BEPUGPU_JOINT_DISTANCE_LIMIT = 9    /* DistanceLimit.cs:260-457 */
 } bepugpu_joint_type;
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
@@ -149,21 +153,26 @@ typedef enum bepugpu_joint_type {
 /* Joint record: the state each reference object keeps between steps.  Body -1
  * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic
  * entity at the origin with identity orientation and zero velocity.
- *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE)
+ *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE, WELD),
+ *                     DistanceJoint / DistanceLimit.localAnchorA/B (DISTANCE, DISTANCE_LIMIT)
  *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
  *                     SwingLimit.localAxisA/B (SWING_LIMIT)
  *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame
  *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame
  *   test_axis         RevoluteLimit.localTestAxis, in B's frame
- *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine
- *   limit_max         RevoluteLimit.maximumAngle
+ *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine;
+ *                     DistanceJoint.Distance; DistanceLimit.MinimumLength
+ *   limit_max         RevoluteLimit.maximumAngle; DistanceLimit.MaximumLength
+ *   orientation_a/b   NoRotationJoint.InitialOrientationA/B (NO_ROTATION, WELD), quaternions x y z w
  *   margin, bounciness, bounce_velocity_threshold   JointLimit fields (0.005, 0, 1)
  *   max_corrective_velocity   Joint.MaxCorrectiveVelocity (FLT_MAX = unlimited)
  *   spring_stiffness/damping  SpringSettings (600000, 90000)
  * The last three apply to every child of a REVOLUTE record.
  *   impulse           accumulated impulses, in/out: BALL_SOCKET [0..2];
  *                     REVOLUTE_ANGULAR [0..1]; SWING_LIMIT [0]; REVOLUTE_LIMIT [0..1];
- *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit. */
+ *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit;
+ *                     NO_ROTATION [0..2]; WELD [0..2] ball socket, [3..5] no rotation;
+ *                     DISTANCE [0]; DISTANCE_LIMIT [0]. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */
     int32_t body_a;
@@ -187,6 +196,8 @@ typedef struct bepugpu_joint {
     float spring_stiffness;
     float spring_damping;
     float impulse[8];
+    float orientation_a[4];
+    float orientation_b[4];
 } bepugpu_joint;
 
 typedef struct bepugpu_context bepugpu_context;

@@ -172,3 +172,90 @@ def test_chains_in_island_groups(gpu_context, policy):
         # chains and loose stacks are small islands: the step is the group launch alone
         assert p.gpu.last_step_launches() <= 2
     p.close()
+
+
+NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT)
+
+
+def _rows(q):
+    x, y, z, w = (float(v) for v in q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y + z * w), 2 * (x * z - y * w)],
+                     [2 * (x * y - z * w), 1 - 2 * (x * x + z * z), 2 * (y * z + x * w)],
+                     [2 * (x * z + y * w), 2 * (y * z - x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def _convert(b, j, types, seed):
+    """The chain joints re-typed: welds and no-rotation joints keep the pose
+    they are made in (the constructors' initial orientations), distance joints
+    keep the anchors' current distance, distance limits bracket it."""
+    j = j.copy()
+    rng = np.random.default_rng(seed)
+    ident = np.array([0, 0, 0, 1], np.float32)
+    for k in range(len(j)):
+        t = types[rng.integers(len(types))]
+        a, bb = int(j["body_a"][k]), int(j["body_b"][k])
+        qa = b["orientation"][a] if a >= 0 else ident
+        qb = b["orientation"][bb] if bb >= 0 else ident
+        wa = (b["position"][a] + j["anchor_a"][k] @ _rows(qa)) if a >= 0 else j["anchor_a"][k]
+        wb = (b["position"][bb] + j["anchor_b"][k] @ _rows(qb)) if bb >= 0 else j["anchor_b"][k]
+        d = float(np.linalg.norm(wb - wa))
+        j["type"][k] = t
+        j["impulse"][k] = 0
+        j["orientation_a"][k] = qa
+        j["orientation_b"][k] = qb
+        if t == N.JOINT_DISTANCE:
+            j["limit_min"][k] = d * rng.uniform(0.95, 1.05)
+        elif t == N.JOINT_DISTANCE_LIMIT:
+            lo = d * rng.uniform(0.7, 1.02)
+            j["limit_min"][k], j["limit_max"][k] = lo, lo + d * rng.uniform(0.0, 0.2)
+            j["bounciness"][k] = rng.choice([0.0, 0.5])
+    return j
+
+
+def test_weld_no_rotation_distance_every_step(gpu_context):
+    b, m, j = _small_chains(seed=21)
+    j = _convert(b, j, NEW_TYPES, 21)
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    for step in range(8):
+        p.step()
+        errs, exact = p.compare()
+        assert exact, (step, errs)
+    p.close()
+
+
+@pytest.mark.parametrize("jtype", NEW_TYPES)
+def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
+    b, m, j = _small_chains(seed=22, chains=16, loose=60)
+    j = _convert(b, j, (jtype,), 22)
+    j["impulse"] = np.random.default_rng(5).uniform(0, 0.05, j["impulse"].shape).astype(np.float32)
+    p = Pair(gpu_context, b, m, j, settings=_settings())
+    for step in range(5):
+        p.step()
+        errs, exact = p.compare()
+        assert exact, (jtype, step, errs)
+    p.close()
+
+
+@pytest.mark.parametrize("policy,mode", [(None, N.MODE_GRAPH), ((0, 1024, 4096, 64, 0), N.MODE_GRAPH),
+                                         (None, N.MODE_PERSISTENT)])
+def test_new_types_sixty_steps_every_path(gpu_context, policy, mode):
+    b, m, j = _small_chains(seed=23, chains=20)
+    j = _convert(b, j, NEW_TYPES, 23)
+    p = Pair(gpu_context, b, m, j, settings=_settings(), group_policy=policy, mode=mode)
+    p.step(steps=60)
+    errs, exact = p.compare()
+    assert exact, (policy, mode, errs)
+    p.close()
+
+
+def test_new_type_records_checked(gpu_context):
+    b, m, j = _small_chains(seed=24, chains=2, loose=0)
+    j = _convert(b, j, (N.JOINT_DISTANCE_LIMIT,), 24)
+    bad = j.copy()
+    bad["limit_min"][0], bad["limit_max"][0] = 2.0, 1.0
+    with pytest.raises(N.BepuError):
+        GpuSpace(gpu_context, b, m, bad)
+    bad = _convert(b, j, (N.JOINT_DISTANCE,), 25)
+    bad["limit_min"][1] = -1.0
+    with pytest.raises(N.BepuError):
+        GpuSpace(gpu_context, b, m, bad)

@@ -149,3 +149,72 @@ def test_revolute_limit_planes(phi_deg, active):
     # the correction turns B back toward the allowed range about the free axis
     wz = ob["angular_velocity"][0][2]
     assert np.sign(wz) == -np.sign(phi)
+
+
+def test_no_rotation_to_world_closed_form():
+    """NoRotationJoint.Update / SolveIteration (NoRotationJoint.cs:160-243):
+    body B turned by phi about z against the world; one solve from rest turns
+    it back about z with lambda = erp * phi / (I_zz + softness)."""
+    phi = np.radians(10.0)
+    b = _body((0, 0, 0), quat=_rot_z(phi))
+    j = _joint(N.JOINT_NO_ROTATION, -1, 0)
+    j["orientation_a"] = (0, 0, 0, 1)
+    j["orientation_b"] = (0, 0, 0, 1)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    # error = axis * angle of conj(qB): (0, 0, -phi); bias = -erp * error
+    lam_z = erp * phi / (4.0 + soft)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam_z), rtol=1e-4, atol=1e-9)
+    # B takes the negated impulse: w = -lambda * I_zz
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam_z), rtol=1e-4, atol=1e-8)
+
+
+def test_distance_joint_to_world_closed_form():
+    """DistanceJoint (DistanceJoint.cs:226-352): B 0.1 beyond its distance of 2
+    from a world anchor is pulled back along the line, no angular part."""
+    b = _body((2.1, 0, 0))
+    j = _joint(N.JOINT_DISTANCE, -1, 0)
+    j["limit_min"] = 2.0
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    vti = 1 / (soft + 1.0)
+    lam = (-0.1 * erp) * vti  # error = distance - current
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-5)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (lam, 0, 0), rtol=1e-5, atol=1e-9)
+    assert np.all(ob["angular_velocity"][0] == 0)
+
+
+@pytest.mark.parametrize("x,active", [(1.5, False), (2.3, True), (0.7, True)])
+def test_distance_limit_switch(x, active):
+    """DistanceLimit (DistanceLimit.cs:260-430): inside [1, 2] nothing acts and
+    a stale impulse is cleared; beyond either end a non-negative impulse
+    pushes back by the error less the margin."""
+    b = _body((x, 0, 0))
+    j = _joint(N.JOINT_DISTANCE_LIMIT, -1, 0)
+    j["limit_min"], j["limit_max"] = 1.0, 2.0
+    j["impulse"][0, 0] = 0.0 if active else 0.3
+    ob, oj = _step(b, j)
+    if not active:
+        assert oj["impulse"][0, 0] == 0 and np.all(ob["linear_velocity"][0] == 0)
+        return
+    erp, soft = _spring(float(DT))
+    error = (x - 2.0 - 0.005) if x > 2 else (1.0 - 0.005 - x)
+    lam = erp * error / (soft + 1.0)
+    assert oj["impulse"][0, 0] > 0
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(abs(ob["linear_velocity"][0, 0]), lam, rtol=1e-4)
+    assert np.sign(ob["linear_velocity"][0, 0]) == (-1 if x > 2 else 1)
+
+
+def test_weld_is_ball_socket_then_no_rotation():
+    """WeldJoint (WeldJoint.cs:15-55) solves its ball socket, then its
+    no-rotation joint, as one SolverGroup: the impulses land in [0..2] and
+    [3..5], each one nonzero for an offset and turned body."""
+    b = _body((0.05, -1, 0), quat=_rot_z(np.radians(5.0)))
+    j = _joint(N.JOINT_WELD, -1, 0)
+    j["anchor_b"] = (0, 1, 0)
+    j["orientation_a"] = (0, 0, 0, 1)
+    j["orientation_b"] = (0, 0, 0, 1)
+    _, oj = _step(b, j)
+    assert np.abs(oj["impulse"][0, :3]).max() > 0 and np.abs(oj["impulse"][0, 3:6]).max() > 0
+    assert np.all(oj["impulse"][0, 6:] == 0)
