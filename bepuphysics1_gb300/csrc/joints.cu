@@ -46,7 +46,9 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_NO_ROTATION: return kJChildAngular;
         case BEPUGPU_JOINT_WELD: return kJChildBall | kJChildAngular;
         case BEPUGPU_JOINT_DISTANCE:
-        case BEPUGPU_JOINT_DISTANCE_LIMIT: return kJChildBall;
+        case BEPUGPU_JOINT_DISTANCE_LIMIT:
+        case BEPUGPU_JOINT_POINT_ON_PLANE: return kJChildBall;
+        case BEPUGPU_JOINT_TWIST: return kJChildAngular;
         default: return 0;
     }
 }
@@ -159,7 +161,11 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 break;
             case BEPUGPU_JOINT_DISTANCE:
             case BEPUGPU_JOINT_DISTANCE_LIMIT:
+            case BEPUGPU_JOINT_POINT_ON_PLANE:
                 ball[0] = r.impulse[0];
+                break;
+            case BEPUGPU_JOINT_TWIST:
+                ang[0] = r.impulse[0];
                 break;
         }
         at(kJACC0, slot) = make_float4(ball[0], ball[1], ball[2], ang[0]);
@@ -225,7 +231,11 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_DISTANCE:
             case BEPUGPU_JOINT_DISTANCE_LIMIT:
+            case BEPUGPU_JOINT_POINT_ON_PLANE:
                 r.impulse[0] = a0.x;
+                break;
+            case BEPUGPU_JOINT_TWIST:
+                r.impulse[0] = a0.w;
                 break;
         }
     }

@@ -15,6 +15,8 @@
 //                         NO_ROTATION and WELD records; WeldJoint.cs:15-55 is ball socket + it)
 //   DistanceJoint         TwoEntity/Joints/DistanceJoint.cs:226-380 (the first child slot)
 //   DistanceLimit         TwoEntity/JointLimits/DistanceLimit.cs:260-457 (the first child slot)
+//   PointOnPlaneJoint     TwoEntity/Joints/PointOnPlaneJoint.cs:212-330 (the first child slot)
+//   TwistJoint            TwoEntity/Joints/TwistJoint.cs:204-365 (the angular child slot)
 //   SpringSettings        Constraints/SpringSettings.cs:95-110
 // A connection of -1 is TwoEntityConstraint.WorldEntity: kinematic, at the
 // origin, identity orientation, zero velocity.  Its zeros go through the same
@@ -257,6 +259,26 @@ __device__ __forceinline__ void JAxisAngle(float4 q, float3& axis, float& angle)
         angle = 0;
     }
 }
+// Quaternion.Normalize: the reciprocal square root in double.
+__device__ __forceinline__ float4 JQNormalize(float4 q) {
+    float inverse = (float)(1.0 / sqrt((double)(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w)));
+    return make_float4(q.x * inverse, q.y * inverse, q.z * inverse, q.w * inverse);
+}
+// Quaternion.GetQuaternionBetweenNormalizedVectors (Quaternion.cs:795-823)
+__device__ __forceinline__ float4 JQuatBetween(float3 v1, float3 v2) {
+    float dot = JDot(v1, v2);
+    float4 q;
+    if (dot < -0.9999f) {
+        float absX = fabsf(v1.x), absY = fabsf(v1.y), absZ = fabsf(v1.z);
+        if (absX < absY && absX < absZ) q = make_float4(0.f, -v1.z, v1.y, 0.f);
+        else if (absY < absZ) q = make_float4(-v1.z, 0.f, v1.x, 0.f);
+        else q = make_float4(-v1.y, v1.x, 0.f, 0.f);
+    } else {
+        float3 axis = JCross(v1, v2);
+        q = make_float4(axis.x, axis.y, axis.z, dot + 1);
+    }
+    return JQNormalize(q);
+}
 // Velocity-only view for the warm start and the solve.
 template <class V>
 __device__ __forceinline__ void LoadJointVelocityV(const V& bv, int r, BodyState& s) {
@@ -299,7 +321,50 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
     const float maxCorrSq = ji.L(kJTA, si).w;
     uint32_t active = present & childIsActive;
-    if ((active & kJChildBall) && IsDistanceType(type)) {
+    if ((active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+        // PointOnPlaneJoint.Update (PointOnPlaneJoint.cs:250-306).  Lanes: kJOA rA + softness,
+        // kJOB.xyz rB, kJM0 normal + negative effective mass, kJM1 rA x n + bias, kJM2 -(rB x n).
+        const float3 n = JTransform(JXYZ(axa), A.R);
+        float3 wpa = JTransform(JXYZ(la), A.R);
+        wpa = make_float3(wpa.x + A.pos.x, wpa.y + A.pos.y, wpa.z + A.pos.z);
+        const float3 rB = JTransform(JXYZ(lb), B.R);
+        const float3 wpt = make_float3(rB.x + B.pos.x, rB.y + B.pos.y, rB.z + B.pos.z);
+        const float pointDistance = JDot(wpt, n), planeDistance = JDot(wpa, n);
+        const float distanceChange = planeDistance - pointDistance;
+        float3 closest = make_float3(n.x * distanceChange, n.y * distanceChange, n.z * distanceChange);
+        closest = make_float3(closest.x + wpt.x, closest.y + wpt.y, closest.z + wpt.z);
+        const float3 rA = make_float3(closest.x - A.pos.x, closest.y - A.pos.y, closest.z - A.pos.z);
+        const float3 raxn = JCross(rA, n);
+        float3 rbxn = JCross(rB, n);
+        rbxn = make_float3(-rbxn.x, -rbxn.y, -rbxn.z);
+        const float error = JDot(make_float3(wpt.x - closest.x, wpt.y - closest.y, wpt.z - closest.z), n);
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        const float bias = Clampf(-erp * error, -maxCorr, maxCorr);
+        float nem;
+        if (A.dynamic && B.dynamic) {
+            float angularA = JDot(raxn, JTransform(raxn, JInertia(A.s)));
+            float angularB = JDot(rbxn, JTransform(rbxn, JInertia(B.s)));
+            nem = A.s.invMass + B.s.invMass + angularA + angularB;
+            nem = -1 / (nem + softness);
+        } else if (A.dynamic) {
+            float angularA = JDot(raxn, JTransform(raxn, JInertia(A.s)));
+            nem = A.s.invMass + angularA;
+            nem = -1 / (nem + softness);
+        } else {
+            float angularB = JDot(rbxn, JTransform(rbxn, JInertia(B.s)));
+            nem = B.s.invMass + angularB;
+            nem = -1 / (nem + softness);
+        }
+        j.L(kJOA, s) = make_float4(rA.x, rA.y, rA.z, softness);
+        j.L(kJOB, s).x = rB.x;
+        j.L(kJOB, s).y = rB.y;
+        j.L(kJOB, s).z = rB.z;
+        j.L(kJM0, s) = make_float4(n.x, n.y, n.z, nem);
+        j.L(kJM1, s) = make_float4(raxn.x, raxn.y, raxn.z, bias);
+        j.L(kJM2, s) = make_float4(rbxn.x, rbxn.y, rbxn.z, 0.f);
+        st |= 1u << (kChildShift + 0);
+    } else if ((active & kJChildBall) && IsDistanceType(type)) {
         // DistanceJoint.Update (DistanceJoint.cs:275-352) / DistanceLimit.Update (DistanceLimit.cs:312-430).
         // Lanes: kJM0 jLinearA + velocityToImpulse, kJM1 jAngularA + bias, kJM2 jAngularB
         // (jLinearB = -jLinearA); kJOA.w softness.  A limit keeps its last jLinearA in kJBP.
@@ -424,7 +489,34 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM2, s) = make_float4(mass.M33, bx, by, bz);
         st |= 1u << (kChildShift + 0);
     }
-    if ((active & kJChildAngular) && IsNoRotationType(type)) {
+    if ((active & kJChildAngular) && type == BEPUGPU_JOINT_TWIST) {
+        // TwistJoint.Update (TwistJoint.cs:235-300).  Inputs: axes A / B, A's local y and z
+        // (kJC1, kJC2) and B's local y (kJBX).  Lanes: kJW1 jacobianB + velocityToImpulse,
+        // kJW2.x bias, kJOB.w softness (jacobianA = -jacobianB).
+        const float3 worldAxisA = JTransform(JXYZ(axa), A.R);
+        const float3 aAxisY = JTransform(JXYZ(ji.L(kJC1, si)), A.R), aAxisZ = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
+        const float3 worldAxisB = JTransform(JXYZ(axb), B.R);
+        const float3 bAxisY = JTransform(JXYZ(ji.L(kJBX, si)), B.R);
+        const float4 rotation = JQuatBetween(worldAxisB, worldAxisA);
+        const float3 twistMeasure = QTransform(bAxisY.x, bAxisY.y, bAxisY.z, rotation);
+        const float y = JDot(twistMeasure, aAxisZ), x = JDot(twistMeasure, aAxisY);
+        const float error = (float)atan2((double)y, (double)x);
+        float3 jB = make_float3(worldAxisA.x + worldAxisB.x, worldAxisA.y + worldAxisB.y, worldAxisA.z + worldAxisB.z);
+        if (JDot(jB, jB) >= 1e-7f) {  // else the child leaves the solver this step, impulse kept
+            jB = JNormalize(jB);
+            const float3 jA = make_float3(-jB.x, -jB.y, -jB.z);
+            float erp, softness;
+            JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+            const float bias = Clampf(-error * erp, -maxCorr, maxCorr);
+            const float entryA = A.dynamic ? JDot(JTransform(jA, JInertia(A.s)), jA) : 0.f;
+            const float entryB = B.dynamic ? JDot(JTransform(jB, JInertia(B.s)), jB) : 0.f;
+            const float vti = 1 / (softness + entryA + entryB);
+            j.L(kJOB, s).w = softness;
+            j.L(kJW1, s) = make_float4(jB.x, jB.y, jB.z, vti);
+            j.L(kJW2, s) = make_float4(bias, 0.f, 0.f, 0.f);
+            st |= 1u << (kChildShift + 1);
+        }
+    } else if ((active & kJChildAngular) && IsNoRotationType(type)) {
         // NoRotationJoint.Update (NoRotationJoint.cs:194-243).  Inputs: kJC1 / kJC2 the
         // initial orientations' conjugates; lanes kJL0..kJL2 the 3x3 effective mass and
         // the bias, kJOB.w the softness.
@@ -656,7 +748,20 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
                                           int type) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
     const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+    if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+        // PointOnPlaneJoint.ExclusiveUpdate (PointOnPlaneJoint.cs:308-328)
+        const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
+        const float a = acc0.x;
+        const float ix = m0.x * a, iy = m0.y * a, iz = m0.z * a;
+        if (dynA) {
+            ApplyLinear(A, ix, iy, iz);
+            ApplyAngular(A, m1.x * a, m1.y * a, m1.z * a);
+        }
+        if (dynB) {
+            ApplyLinear(B, -ix, -iy, -iz);
+            ApplyAngular(B, m2.x * a, m2.y * a, m2.z * a);
+        }
+    } else if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
         // DistanceJoint / DistanceLimit.ExclusiveUpdate (DistanceJoint.cs:354-380)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
         const float a = acc0.x;
@@ -684,7 +789,13 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
             ApplyAngular(B, t.x, t.y, t.z);
         }
     }
-    if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+    if ((st & (2u << kChildShift)) && type == BEPUGPU_JOINT_TWIST) {
+        // TwistJoint.ExclusiveUpdate (TwistJoint.cs:302-317)
+        const float4 w1 = j.L(kJW1, s);
+        const float a = acc0.w;
+        if (dynA) ApplyAngular(A, -w1.x * a, -w1.y * a, -w1.z * a);
+        if (dynB) ApplyAngular(B, w1.x * a, w1.y * a, w1.z * a);
+    } else if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
         // NoRotationJoint.ExclusiveUpdate (NoRotationJoint.cs:245-259)
         if (dynA) ApplyAngular(A, acc0.w, acc1.x, acc1.y);
         if (dynB) ApplyAngular(B, -acc0.w, -acc1.x, -acc1.y);
@@ -750,7 +861,29 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
     float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+    if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+        // PointOnPlaneJoint.SolveIteration (PointOnPlaneJoint.cs:212-243)
+        const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
+                     m2 = j.L(kJM2, s);
+        float ax = A.wy * oa.z - A.wz * oa.y, ay = A.wz * oa.x - A.wx * oa.z, az = A.wx * oa.y - A.wy * oa.x;
+        ax = ax + A.vx; ay = ay + A.vy; az = az + A.vz;
+        float bx = B.wy * ob.z - B.wz * ob.y, by = B.wz * ob.x - B.wx * ob.z, bz = B.wx * ob.y - B.wy * ob.x;
+        bx = bx + B.vx; by = by + B.vy; bz = bz + B.vz;
+        const float dvx = ax - bx, dvy = ay - by, dvz = az - bz;
+        const float vd = dvx * m0.x + dvy * m0.y + dvz * m0.z;
+        const float lambda = m0.w * (vd + m1.w + oa.w * acc0.x);
+        acc0.x += lambda;
+        const float ix = m0.x * lambda, iy = m0.y * lambda, iz = m0.z * lambda;
+        if (dynA) {
+            ApplyLinear(A, ix, iy, iz);
+            ApplyAngular(A, m1.x * lambda, m1.y * lambda, m1.z * lambda);
+        }
+        if (dynB) {
+            ApplyLinear(B, -ix, -iy, -iz);
+            ApplyAngular(B, m2.x * lambda, m2.y * lambda, m2.z * lambda);
+        }
+        account(0, lambda);  // signed, as the reference returns it
+    } else if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
         // DistanceJoint.SolveIteration (DistanceJoint.cs:226-268) /
         // DistanceLimit.SolveIteration (DistanceLimit.cs:260-305)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
@@ -811,7 +944,20 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         }
         account(0, fabsf(tx) + fabsf(ty) + fabsf(tz));
     }
-    if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+    if ((st & (2u << kChildShift)) && type == BEPUGPU_JOINT_TWIST) {
+        // TwistJoint.SolveIteration (TwistJoint.cs:204-228)
+        const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s);
+        const float softness = j.L(kJOB, s).w;
+        const float jax = -w1.x, jay = -w1.y, jaz = -w1.z;
+        const float velocityA = A.wx * jax + A.wy * jay + A.wz * jaz;
+        const float velocityB = B.wx * w1.x + B.wy * w1.y + B.wz * w1.z;
+        float lambda = -(velocityA + velocityB) + w2.x - softness * acc0.w;
+        lambda *= w1.w;
+        acc0.w += lambda;
+        if (dynA) ApplyAngular(A, jax * lambda, jay * lambda, jaz * lambda);
+        if (dynB) ApplyAngular(B, w1.x * lambda, w1.y * lambda, w1.z * lambda);
+        account(1, fabsf(lambda));
+    } else if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
         // NoRotationJoint.SolveIteration (NoRotationJoint.cs:160-187)
         const float4 l0 = j.L(kJL0, s), l1 = j.L(kJL1, s), l2 = j.L(kJL2, s);
         const float softness = j.L(kJOB, s).w;

@@ -144,7 +144,9 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_NO_ROTATION = 6,      /* NoRotationJoint.cs:160-262 */
     BEPUGPU_JOINT_WELD = 7,             /* WeldJoint group: ball socket + no rotation (WeldJoint.cs:15-55) */
     BEPUGPU_JOINT_DISTANCE = 8,         /* DistanceJoint.cs:226-380 */
-    BEPUGPU_JOINT_DISTANCE_LIMIT = 9    /* DistanceLimit.cs:260-457 */
+    BEPUGPU_JOINT_DISTANCE_LIMIT = 9,   /* DistanceLimit.cs:260-457 */
+    BEPUGPU_JOINT_POINT_ON_PLANE = 10,  /* PointOnPlaneJoint.cs:212-330 */
+    BEPUGPU_JOINT_TWIST = 11            /* TwistJoint.cs:204-365 */
 } bepugpu_joint_type;
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
@@ -154,11 +156,15 @@ typedef enum bepugpu_joint_type {
  * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic
  * entity at the origin with identity orientation and zero velocity.
  *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE, WELD),
- *                     DistanceJoint / DistanceLimit.localAnchorA/B (DISTANCE, DISTANCE_LIMIT)
+ *                     DistanceJoint / DistanceLimit.localAnchorA/B (DISTANCE, DISTANCE_LIMIT),
+ *                     PointOnPlaneJoint.localPlaneAnchor / localPointAnchor (POINT_ON_PLANE)
  *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
- *                     SwingLimit.localAxisA/B (SWING_LIMIT)
- *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame
- *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame
+ *                     SwingLimit.localAxisA/B (SWING_LIMIT), TwistJoint.localAxisA/B (TWIST),
+ *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE)
+ *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame;
+ *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST)
+ *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame;
+ *                     basis_x: TwistJoint.bLocalAxisY (TWIST)
  *   test_axis         RevoluteLimit.localTestAxis, in B's frame
  *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine;
  *                     DistanceJoint.Distance; DistanceLimit.MinimumLength
@@ -172,7 +178,7 @@ typedef enum bepugpu_joint_type {
  *                     REVOLUTE_ANGULAR [0..1]; SWING_LIMIT [0]; REVOLUTE_LIMIT [0..1];
  *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit;
  *                     NO_ROTATION [0..2]; WELD [0..2] ball socket, [3..5] no rotation;
- *                     DISTANCE [0]; DISTANCE_LIMIT [0]. */
+ *                     DISTANCE [0]; DISTANCE_LIMIT [0]; POINT_ON_PLANE [0]; TWIST [0]. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */
     int32_t body_a;

@@ -174,7 +174,8 @@ def test_chains_in_island_groups(gpu_context, policy):
     p.close()
 
 
-NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT)
+NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
+             N.JOINT_TWIST)
 
 
 def _rows(q):
@@ -209,6 +210,24 @@ def _convert(b, j, types, seed):
             lo = d * rng.uniform(0.7, 1.02)
             j["limit_min"][k], j["limit_max"][k] = lo, lo + d * rng.uniform(0.0, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        elif t == N.JOINT_POINT_ON_PLANE:
+            n = rng.normal(size=3)
+            j["axis_a"][k] = n / np.linalg.norm(n)
+        elif t == N.JOINT_TWIST:
+            # TwistJoint.Initialize (TwistJoint.cs:340-365) for a shared world axis
+            ax = rng.normal(size=3)
+            ax /= np.linalg.norm(ax)
+            ra, rb = _rows(qa), _rows(qb)
+            y = np.cross(ax, (0, 1, 0))
+            if y @ y < 1e-7:
+                y = np.cross(ax, (1, 0, 0))
+            y /= np.linalg.norm(y)
+            la = ax @ ra.T
+            j["axis_a"][k] = la
+            j["axis_b"][k] = ax @ rb.T
+            j["constrained_1"][k] = y @ ra.T
+            j["constrained_2"][k] = np.cross(la, y @ ra.T)
+            j["basis_x"][k] = y @ rb.T
     return j
 
 

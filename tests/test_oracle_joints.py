@@ -218,3 +218,34 @@ def test_weld_is_ball_socket_then_no_rotation():
     _, oj = _step(b, j)
     assert np.abs(oj["impulse"][0, :3]).max() > 0 and np.abs(oj["impulse"][0, 3:6]).max() > 0
     assert np.all(oj["impulse"][0, 6:] == 0)
+
+
+def test_point_on_plane_to_world_closed_form():
+    """PointOnPlaneJoint (PointOnPlaneJoint.cs:212-306): B's centre 0.1 above the
+    world's y = 0 plane is pushed down; the solve returns the signed lambda."""
+    b = _body((0.3, 0.1, -0.2))
+    j = _joint(N.JOINT_POINT_ON_PLANE, -1, 0)
+    j["axis_a"] = (0, 1, 0)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = (erp * 0.1) / (1.0 + soft)  # negative effective mass times the bias
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (0, -lam, 0), rtol=1e-4, atol=1e-9)
+
+
+def test_twist_to_world_closed_form():
+    """TwistJoint (TwistJoint.cs:204-300): B twisted by phi about the shared x
+    axis; the error is atan2 of the measured y axis, the jacobian x."""
+    phi = np.radians(12.0)
+    b = _body((0, 0, 0), quat=(np.sin(phi / 2), 0, 0, np.cos(phi / 2)))
+    j = _joint(N.JOINT_TWIST, -1, 0)
+    j["axis_a"] = j["axis_b"] = (1, 0, 0)
+    j["constrained_1"] = (0, 0, -1)  # A's local y: cross(x, up) normalised
+    j["constrained_2"] = (0, 1, 0)   # A's local z: cross(axis, y)
+    j["basis_x"] = (0, 0, -1)        # B's local y
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    # B's y axis turned by phi about x, measured in A's (y, z) frame: error = phi
+    lam = (-phi * erp) / (soft + 2.0)  # I_xx = 2, jacobianB = x
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (2.0 * lam, 0, 0), rtol=1e-4, atol=1e-8)
