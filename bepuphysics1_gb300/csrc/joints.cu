@@ -49,6 +49,10 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_DISTANCE_LIMIT:
         case BEPUGPU_JOINT_POINT_ON_PLANE: return kJChildBall;
         case BEPUGPU_JOINT_TWIST: return kJChildAngular;
+        case BEPUGPU_JOINT_POINT_ON_LINE: return kJChildBall;
+        case BEPUGPU_JOINT_PRISMATIC:
+        case BEPUGPU_JOINT_LINE_SLIDER:
+        case BEPUGPU_JOINT_UNIVERSAL: return kJChildBall | kJChildAngular;
         default: return 0;
     }
 }
@@ -129,7 +133,8 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
         at(kJBX, slot) = F4(r.basis_x, r.type == BEPUGPU_JOINT_SWING_LIMIT ? r.limit_min : 0.f);
         at(kJTA, slot) = F4(r.test_axis, maxCorrSq);
         at(kJTRIG, slot) = make_float4(sinMin, omcMin, sinMax, omcMax);
-        if (r.type == BEPUGPU_JOINT_NO_ROTATION || r.type == BEPUGPU_JOINT_WELD) {
+        if (r.type == BEPUGPU_JOINT_NO_ROTATION || r.type == BEPUGPU_JOINT_WELD ||
+            r.type == BEPUGPU_JOINT_PRISMATIC) {
             // the initial orientations' conjugates (NoRotationJoint.cs:48-63)
             const float* qa = r.orientation_a;
             const float* qb = r.orientation_b;
@@ -166,6 +171,21 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 break;
             case BEPUGPU_JOINT_TWIST:
                 ang[0] = r.impulse[0];
+                break;
+            case BEPUGPU_JOINT_POINT_ON_LINE:
+                ball[0] = r.impulse[0]; ball[1] = r.impulse[1];
+                break;
+            case BEPUGPU_JOINT_PRISMATIC:
+                ball[0] = r.impulse[0]; ball[1] = r.impulse[1];
+                ang[0] = r.impulse[2]; ang[1] = r.impulse[3]; lim[0] = r.impulse[4];
+                break;
+            case BEPUGPU_JOINT_LINE_SLIDER:
+                ball[0] = r.impulse[0]; ball[1] = r.impulse[1];
+                ang[0] = r.impulse[2]; ang[1] = r.impulse[3];
+                break;
+            case BEPUGPU_JOINT_UNIVERSAL:
+                std::memcpy(ball, r.impulse, 12);
+                ang[0] = r.impulse[3];
                 break;
         }
         at(kJACC0, slot) = make_float4(ball[0], ball[1], ball[2], ang[0]);
@@ -236,6 +256,21 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_TWIST:
                 r.impulse[0] = a0.w;
+                break;
+            case BEPUGPU_JOINT_POINT_ON_LINE:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y;
+                break;
+            case BEPUGPU_JOINT_PRISMATIC:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y;
+                r.impulse[2] = a0.w; r.impulse[3] = a1.x; r.impulse[4] = a1.y;
+                break;
+            case BEPUGPU_JOINT_LINE_SLIDER:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y;
+                r.impulse[2] = a0.w; r.impulse[3] = a1.x;
+                break;
+            case BEPUGPU_JOINT_UNIVERSAL:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                r.impulse[3] = a0.w;
                 break;
         }
     }

@@ -17,6 +17,9 @@
 //   DistanceLimit         TwoEntity/JointLimits/DistanceLimit.cs:260-457 (the first child slot)
 //   PointOnPlaneJoint     TwoEntity/Joints/PointOnPlaneJoint.cs:212-330 (the first child slot)
 //   TwistJoint            TwoEntity/Joints/TwistJoint.cs:204-365 (the angular child slot)
+//   PointOnLineJoint      TwoEntity/Joints/PointOnLineJoint.cs:247-463 (the first child slot)
+// and the groups PrismaticJoint (point on line + no rotation), LineSliderJoint
+// (point on line + revolute angular), UniversalJoint (ball socket + twist).
 //   SpringSettings        Constraints/SpringSettings.cs:95-110
 // A connection of -1 is TwoEntityConstraint.WorldEntity: kinematic, at the
 // origin, identity orientation, zero velocity.  Its zeros go through the same
@@ -92,7 +95,14 @@ __device__ __forceinline__ bool IsDistanceType(int type) {
     return type == BEPUGPU_JOINT_DISTANCE || type == BEPUGPU_JOINT_DISTANCE_LIMIT;
 }
 __device__ __forceinline__ bool IsNoRotationType(int type) {
-    return type == BEPUGPU_JOINT_NO_ROTATION || type == BEPUGPU_JOINT_WELD;
+    return type == BEPUGPU_JOINT_NO_ROTATION || type == BEPUGPU_JOINT_WELD || type == BEPUGPU_JOINT_PRISMATIC;
+}
+__device__ __forceinline__ bool IsPointOnLineType(int type) {
+    return type == BEPUGPU_JOINT_POINT_ON_LINE || type == BEPUGPU_JOINT_PRISMATIC ||
+           type == BEPUGPU_JOINT_LINE_SLIDER;
+}
+__device__ __forceinline__ bool IsTwistType(int type) {
+    return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
 }
 
 struct JointSoA {
@@ -291,6 +301,26 @@ __device__ __forceinline__ void LoadJointVelocityV(const V& bv, int r, BodyState
     LoadBodyV(bv, r, s);
 }
 
+// PointOnLineJoint's impulse on both connections (SolveIteration and
+// ExclusiveUpdate, PointOnLineJoint.cs:318-355, 440-463).  Lanes: kJOA rA,
+// kJOB rB, kJM0 / kJM1 the world restricted axes; the angular jacobians are
+// their cross products with rA and rB, recomputed as the reference computed them.
+__device__ __forceinline__ void ApplyPointOnLine(float4 oa, float4 ob, float4 m0, float4 m1, float x, float y,
+                                                 bool dynA, bool dynB, BodyState& A, BodyState& B) {
+    const float3 rA = JXYZ(oa), rB = JXYZ(ob), ax1 = JXYZ(m0), ax2 = JXYZ(m1);
+    float ix = ax1.x * x + ax2.x * y, iy = ax1.y * x + ax2.y * y, iz = ax1.z * x + ax2.z * y;
+    if (dynA) {
+        const float3 a1 = JCross(rA, ax1), a2 = JCross(rA, ax2);
+        ApplyLinear(A, ix, iy, iz);
+        ApplyAngular(A, x * a1.x + y * a2.x, x * a1.y + y * a2.y, x * a1.z + y * a2.z);
+    }
+    if (dynB) {
+        const float3 b1 = JCross(ax1, rB), b2 = JCross(ax2, rB);
+        ApplyLinear(B, -ix, -iy, -iz);
+        ApplyAngular(B, x * b1.x + y * b2.x, x * b1.y + y * b2.y, x * b1.z + y * b2.z);
+    }
+}
+
 // ------------------------------------------------------------- prestep --
 // Solver.UnsafePrestep (Solver.cs:265-275) of one joint: UpdateSolverActivity,
 // then Update of every active child (SolverGroup.cs:94-100).
@@ -321,7 +351,69 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
     const float maxCorrSq = ji.L(kJTA, si).w;
     uint32_t active = present & childIsActive;
-    if ((active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    if ((active & kJChildBall) && IsPointOnLineType(type)) {
+        // PointOnLineJoint.Update (PointOnLineJoint.cs:362-438).  Inputs: kJLA line anchor
+        // (A), kJLB point (B), kJBP line direction, kJBX / kJTA restricted axes (A's frame).
+        // Lanes: kJOA rA + softness, kJOB.xyz rB, kJM0 axis 1 + M11, kJM1 axis 2 + M12,
+        // kJM2 M21 M22 bias x y of the negative effective mass.
+        const float3 ax1 = JTransform(JXYZ(ji.L(kJBX, si)), A.R), ax2 = JTransform(JXYZ(ji.L(kJTA, si)), A.R);
+        float3 lineAnchor = JTransform(JXYZ(la), A.R);
+        lineAnchor = make_float3(lineAnchor.x + A.pos.x, lineAnchor.y + A.pos.y, lineAnchor.z + A.pos.z);
+        const float3 lineDir = JTransform(JXYZ(ji.L(kJBP, si)), A.R);
+        const float3 rB = JTransform(JXYZ(lb), B.R);
+        const float3 point = make_float3(rB.x + B.pos.x, rB.y + B.pos.y, rB.z + B.pos.z);
+        float3 off = make_float3(point.x - lineAnchor.x, point.y - lineAnchor.y, point.z - lineAnchor.z);
+        const float along = JDot(off, lineDir);
+        off = make_float3(lineDir.x * along, lineDir.y * along, lineDir.z * along);
+        const float3 nearPoint = make_float3(lineAnchor.x + off.x, lineAnchor.y + off.y, lineAnchor.z + off.z);
+        const float3 rA = make_float3(nearPoint.x - A.pos.x, nearPoint.y - A.pos.y, nearPoint.z - A.pos.z);
+        const float3 e3 = make_float3(point.x - nearPoint.x, point.y - nearPoint.y, point.z - nearPoint.z);
+        const float ex = JDot(e3, ax1), ey = JDot(e3, ax2);
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        const float bias = -erp;
+        float bx = bias * ex, by = bias * ey;
+        const float length = bx * bx + by * by;
+        if (length > maxCorrSq) {
+            float multiplier = maxCorr / SqrtOfFloat(length);
+            bx *= multiplier; by *= multiplier;
+        }
+        const float3 a1 = JCross(rA, ax1), b1 = JCross(ax1, rB), a2 = JCross(rA, ax2), b2 = JCross(ax2, rB);
+        float m11 = 0, m22 = 0, m1221 = 0;
+        if (A.dynamic) {
+            const JM3 ia = JInertia(A.s);
+            float3 t = JTransform(a1, ia);
+            m11 = JDot(t, a1);
+            m11 += A.s.invMass;
+            m1221 = JDot(t, a2);
+            t = JTransform(a2, ia);
+            m22 = JDot(t, a2);
+            m22 += A.s.invMass;
+        }
+        if (B.dynamic) {
+            const JM3 ib = JInertia(B.s);
+            float3 t = JTransform(b1, ib);
+            float extra = JDot(t, b1);
+            m11 += B.s.invMass + extra;
+            extra = JDot(t, b2);
+            m1221 += extra;
+            t = JTransform(b2, ib);
+            extra = JDot(t, b2);
+            m22 += B.s.invMass + extra;
+        }
+        // Matrix2x2.Invert (Matrix2x2.cs:160-174), then Negate (:259-273)
+        const float k11 = m11 + softness, k12 = m1221, k21 = m1221, k22 = m22 + softness;
+        const float d = 1 / (k11 * k22 - k12 * k21);
+        const float i11 = k22 * d, i12 = -k12 * d, i21 = -k21 * d, i22 = k11 * d;
+        j.L(kJOA, s) = make_float4(rA.x, rA.y, rA.z, softness);
+        j.L(kJOB, s).x = rB.x;
+        j.L(kJOB, s).y = rB.y;
+        j.L(kJOB, s).z = rB.z;
+        j.L(kJM0, s) = make_float4(ax1.x, ax1.y, ax1.z, -i11);
+        j.L(kJM1, s) = make_float4(ax2.x, ax2.y, ax2.z, -i12);
+        j.L(kJM2, s) = make_float4(-i21, -i22, bx, by);
+        st |= 1u << (kChildShift + 0);
+    } else if ((active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.Update (PointOnPlaneJoint.cs:250-306).  Lanes: kJOA rA + softness,
         // kJOB.xyz rB, kJM0 normal + negative effective mass, kJM1 rA x n + bias, kJM2 -(rB x n).
         const float3 n = JTransform(JXYZ(axa), A.R);
@@ -489,7 +581,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM2, s) = make_float4(mass.M33, bx, by, bz);
         st |= 1u << (kChildShift + 0);
     }
-    if ((active & kJChildAngular) && type == BEPUGPU_JOINT_TWIST) {
+    if ((active & kJChildAngular) && IsTwistType(type)) {
         // TwistJoint.Update (TwistJoint.cs:235-300).  Inputs: axes A / B, A's local y and z
         // (kJC1, kJC2) and B's local y (kJBX).  Lanes: kJW1 jacobianB + velocityToImpulse,
         // kJW2.x bias, kJOB.w softness (jacobianA = -jacobianB).
@@ -748,7 +840,10 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
                                           int type) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
     const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    if ((st & (1u << kChildShift)) && IsPointOnLineType(type)) {
+        // PointOnLineJoint.ExclusiveUpdate (PointOnLineJoint.cs:440-463)
+        ApplyPointOnLine(j.L(kJOA, s), j.L(kJOB, s), j.L(kJM0, s), j.L(kJM1, s), acc0.x, acc0.y, dynA, dynB, A, B);
+    } else if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.ExclusiveUpdate (PointOnPlaneJoint.cs:308-328)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
         const float a = acc0.x;
@@ -789,7 +884,7 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
             ApplyAngular(B, t.x, t.y, t.z);
         }
     }
-    if ((st & (2u << kChildShift)) && type == BEPUGPU_JOINT_TWIST) {
+    if ((st & (2u << kChildShift)) && IsTwistType(type)) {
         // TwistJoint.ExclusiveUpdate (TwistJoint.cs:302-317)
         const float4 w1 = j.L(kJW1, s);
         const float a = acc0.w;
@@ -861,7 +956,25 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
     float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    if ((st & (1u << kChildShift)) && IsPointOnLineType(type)) {
+        // PointOnLineJoint.SolveIteration (PointOnLineJoint.cs:247-355)
+        const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
+                     m2 = j.L(kJM2, s);
+        float ax = A.wy * oa.z - A.wz * oa.y, ay = A.wz * oa.x - A.wx * oa.z, az = A.wx * oa.y - A.wy * oa.x;
+        ax = ax + A.vx; ay = ay + A.vy; az = az + A.vz;
+        float bx = B.wy * ob.z - B.wz * ob.y, by = B.wz * ob.x - B.wx * ob.z, bz = B.wx * ob.y - B.wy * ob.x;
+        bx = bx + B.vx; by = by + B.vy; bz = bz + B.vz;
+        const float dvx = ax - bx, dvy = ay - by, dvz = az - bz;
+        float lx = dvx * m0.x + dvy * m0.y + dvz * m0.z;
+        float ly = dvx * m1.x + dvy * m1.y + dvz * m1.z;
+        lx += m2.z + oa.w * acc0.x;
+        ly += m2.w + oa.w * acc0.y;
+        const float x = lx * m0.w + ly * m2.x, y = lx * m1.w + ly * m2.y;  // Matrix2x2.Transform
+        acc0.x = x + acc0.x;
+        acc0.y = y + acc0.y;
+        ApplyPointOnLine(oa, ob, m0, m1, x, y, dynA, dynB, A, B);
+        account(0, fabsf(x) + fabsf(y));
+    } else if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.SolveIteration (PointOnPlaneJoint.cs:212-243)
         const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
                      m2 = j.L(kJM2, s);
@@ -944,7 +1057,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         }
         account(0, fabsf(tx) + fabsf(ty) + fabsf(tz));
     }
-    if ((st & (2u << kChildShift)) && type == BEPUGPU_JOINT_TWIST) {
+    if ((st & (2u << kChildShift)) && IsTwistType(type)) {
         // TwistJoint.SolveIteration (TwistJoint.cs:204-228)
         const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s);
         const float softness = j.L(kJOB, s).w;

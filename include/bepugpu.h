@@ -146,8 +146,15 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_DISTANCE = 8,         /* DistanceJoint.cs:226-380 */
     BEPUGPU_JOINT_DISTANCE_LIMIT = 9,   /* DistanceLimit.cs:260-457 */
     BEPUGPU_JOINT_POINT_ON_PLANE = 10,  /* PointOnPlaneJoint.cs:212-330 */
-    BEPUGPU_JOINT_TWIST = 11            /* TwistJoint.cs:204-365 */
+    BEPUGPU_JOINT_TWIST = 11,           /* TwistJoint.cs:204-365 */
+    BEPUGPU_JOINT_POINT_ON_LINE = 12,   /* PointOnLineJoint.cs:247-463 */
+    BEPUGPU_JOINT_PRISMATIC = 13,       /* PrismaticJoint group: point on line + no rotation */
+    BEPUGPU_JOINT_LINE_SLIDER = 14,     /* LineSliderJoint group: point on line + revolute angular */
+    BEPUGPU_JOINT_UNIVERSAL = 15        /* UniversalJoint group: ball socket + twist */
 } bepugpu_joint_type;
+/* The groups' limit and motor children are inactive, as their constructors
+ * leave them (PrismaticJoint.cs:57-58, LineSliderJoint.cs:53-54,
+ * UniversalJoint.cs:52-53); active ones are not carried. */
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
 #define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE: RevoluteJoint.Limit.IsActive */
@@ -157,14 +164,17 @@ typedef enum bepugpu_joint_type {
  * entity at the origin with identity orientation and zero velocity.
  *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE, WELD),
  *                     DistanceJoint / DistanceLimit.localAnchorA/B (DISTANCE, DISTANCE_LIMIT),
- *                     PointOnPlaneJoint.localPlaneAnchor / localPointAnchor (POINT_ON_PLANE)
+ *                     PointOnPlaneJoint.localPlaneAnchor / localPointAnchor (POINT_ON_PLANE),
+ *                     PointOnLineJoint.localAxisAnchor / localPoint (POINT_ON_LINE, PRISMATIC, LINE_SLIDER)
  *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
  *                     SwingLimit.localAxisA/B (SWING_LIMIT), TwistJoint.localAxisA/B (TWIST),
  *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE)
  *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame;
  *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST)
  *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame;
- *                     basis_x: TwistJoint.bLocalAxisY (TWIST)
+ *                     basis_x: TwistJoint.bLocalAxisY (TWIST, UNIVERSAL);
+ *                     PointOnLineJoint: basis_primary localLineDirection, basis_x / test_axis
+ *                     localRestrictedAxis1 / 2 (POINT_ON_LINE, PRISMATIC, LINE_SLIDER)
  *   test_axis         RevoluteLimit.localTestAxis, in B's frame
  *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine;
  *                     DistanceJoint.Distance; DistanceLimit.MinimumLength
@@ -178,7 +188,11 @@ typedef enum bepugpu_joint_type {
  *                     REVOLUTE_ANGULAR [0..1]; SWING_LIMIT [0]; REVOLUTE_LIMIT [0..1];
  *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit;
  *                     NO_ROTATION [0..2]; WELD [0..2] ball socket, [3..5] no rotation;
- *                     DISTANCE [0]; DISTANCE_LIMIT [0]; POINT_ON_PLANE [0]; TWIST [0]. */
+ *                     DISTANCE [0]; DISTANCE_LIMIT [0]; POINT_ON_PLANE [0]; TWIST [0];
+ *                     POINT_ON_LINE [0..1]; PRISMATIC [0..1] point on line, [2..4] no rotation;
+ *                     LINE_SLIDER [0..1] point on line, [2..3] angular; UNIVERSAL [0..2] ball
+ *                     socket, [3] twist.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
+ *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */
     int32_t body_a;

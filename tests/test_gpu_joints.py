@@ -175,7 +175,20 @@ def test_chains_in_island_groups(gpu_context, policy):
 
 
 NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
-             N.JOINT_TWIST)
+             N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL)
+
+
+def _unit(v):
+    return v / np.linalg.norm(v)
+
+
+def _perpendicular_pair(d):
+    """PointOnLineJoint.UpdateRestrictedAxes (PointOnLineJoint.cs:465-474) in float64."""
+    r1 = np.cross((0, 1, 0), d)
+    if r1 @ r1 < .001:
+        r1 = np.cross((1, 0, 0), d)
+    r2 = np.cross(d, r1)
+    return _unit(r1), _unit(r2)
 
 
 def _rows(q):
@@ -213,7 +226,17 @@ def _convert(b, j, types, seed):
         elif t == N.JOINT_POINT_ON_PLANE:
             n = rng.normal(size=3)
             j["axis_a"][k] = n / np.linalg.norm(n)
-        elif t == N.JOINT_TWIST:
+        elif t in (N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER):
+            ra, rb = _rows(qa), _rows(qb)
+            d = _unit(rng.normal(size=3))  # the line direction in A's frame
+            r1, r2 = _perpendicular_pair(d)
+            j["basis_primary"][k], j["basis_x"][k], j["test_axis"][k] = d, r1, r2
+            if t == N.JOINT_LINE_SLIDER:  # RevoluteAngularJoint about the line
+                wd = d @ ra
+                c1, c2 = _perpendicular_pair(wd)
+                j["axis_a"][k], j["axis_b"][k] = d, wd @ rb.T
+                j["constrained_1"][k], j["constrained_2"][k] = c1 @ ra.T, c2 @ ra.T
+        if t in (N.JOINT_TWIST, N.JOINT_UNIVERSAL):
             # TwistJoint.Initialize (TwistJoint.cs:340-365) for a shared world axis
             ax = rng.normal(size=3)
             ax /= np.linalg.norm(ax)

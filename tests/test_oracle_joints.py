@@ -249,3 +249,18 @@ def test_twist_to_world_closed_form():
     lam = (-phi * erp) / (soft + 2.0)  # I_xx = 2, jacobianB = x
     np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
     np.testing.assert_allclose(ob["angular_velocity"][0], (2.0 * lam, 0, 0), rtol=1e-4, atol=1e-8)
+
+
+def test_point_on_line_to_world_closed_form():
+    """PointOnLineJoint (PointOnLineJoint.cs:247-438): B's centre 0.1 off the
+    world's x axis is pulled back along the restricted axis (0, 1, 0)."""
+    b = _body((0.5, 0.1, 0))
+    j = _joint(N.JOINT_POINT_ON_LINE, -1, 0)
+    j["basis_primary"] = (1, 0, 0)  # line direction
+    j["basis_x"] = (0, 0, -1)       # restricted axes of UpdateRestrictedAxes for x
+    j["test_axis"] = (0, 1, 0)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    y = erp * 0.1 / (1.0 + soft)
+    np.testing.assert_allclose(oj["impulse"][0, :2], (0, y), rtol=1e-4, atol=1e-9)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (0, -y, 0), rtol=1e-4, atol=1e-9)
