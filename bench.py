@@ -63,11 +63,11 @@ def parse_args():
     ap.add_argument("--group-threads", type=int, default=0, help="threads per group CTA (0 = from the plan)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-sample-seconds", type=float, default=10.0)
     ap.add_argument("--no-batch", action="store_true", help="skip the many-scene batching section")
     ap.add_argument("--batch-scenes", type=int, default=4096)
     ap.add_argument("--batch-rounds", type=int, default=5, help="timed rounds of the plain and batched paths")
-    ap.add_argument("--tune-seconds", type=float, default=45.0, help="autotuner time limit")
+    ap.add_argument("--tune-seconds", type=float, default=20.0, help="autotuner time limit")
     ap.add_argument("--tune-out", default=None, help="write the autotuner's trials to this JSON file")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
@@ -76,10 +76,10 @@ def parse_args():
     ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
-    ap.add_argument("--serve-rates", default="1000,5000,20000,50000,100000,200000",
+    ap.add_argument("--serve-rates", default="1000,20000,100000,200000",
                     help="Poisson arrival rates (requests/s)")
-    ap.add_argument("--serve-plain-rates", default="1000,5000,20000")
-    ap.add_argument("--serve-spill-rates", default="1000,5000,20000",
+    ap.add_argument("--serve-plain-rates", default="1000,20000")
+    ap.add_argument("--serve-spill-rates", default="1000,20000",
                     help="arrival rates under a device budget of half the served bytes")
     ap.add_argument("--chain-cpu-seconds", type=float, default=8.0)
     return ap.parse_args()
@@ -594,7 +594,8 @@ def serve_level(srv, ids, rate, seconds, seed):
             "restores": int(s1["restores"] - s0["restores"]), "submit_ring_full": int(full),
             "spill_ms": (int(s1["spill_us"]) - int(s0["spill_us"])) / 1e3,
             "restore_ms": (int(s1["restore_us"]) - int(s0["restore_us"])) / 1e3,
-            "room_waits": int(s1["room_waits"] - s0["room_waits"])}
+            "room_waits": int(s1["room_waits"] - s0["room_waits"]),
+            "failed": int(len(done) - len(ok)), "last_error": srv.last_error() if len(done) > len(ok) else None}
 
 
 def serve_section(args, local, rank, world, pg):
@@ -624,6 +625,7 @@ def serve_section(args, local, rank, world, pg):
                       "setup_s": setup_s, "latency": "submit to completion seen by the server, steady clock"}}
 
     def run(mode_rates, **kw):
+        t_run = time.perf_counter()
         srv = Server(ctx, dt=float(DT), **kw)
         t_add = time.perf_counter()
         for sp in spaces:
@@ -636,11 +638,16 @@ def serve_section(args, local, rank, world, pg):
         srv.drain(600000)
         while len(srv.poll()):
             pass
+        t_warm = time.perf_counter() - t_add - t_run
         st = srv.stats()
+        warm = {"s": t_warm, "waves": int(st["waves"]), "spills": int(st["spills"]), "restores": int(st["restores"]),
+                "spill_ms": int(st["spill_us"]) / 1e3, "restore_ms": int(st["restore_us"]) / 1e3}
+        if rank == 0:
+            print(f"bench: serve {kw} warm-up {warm}", file=sys.stderr, flush=True)
         levels = [serve_level(srv, ids, r, args.serve_seconds, 17 + i) for i, r in enumerate(mode_rates)]
         res = {"levels": levels, "resident_bytes": int(st["resident_bytes"]),
                "resident_scenes": int(st["resident_scenes"]), "pinned_spill_bytes": int(st["pinned_bytes"]),
-               "add_scenes_s": t_add}
+               "add_scenes_s": t_add, "warmup": warm, "run_s": time.perf_counter() - t_run}
         srv.close()
         return res
 
@@ -708,6 +715,15 @@ def main():
 
     import torch
     import __graft_entry__
+    t_start = time.perf_counter()
+    section_s = {}
+
+    def mark(name, since):
+        section_s[name] = round(time.perf_counter() - since, 2)
+        if rank == 0:
+            print(f"bench: {name} {section_s[name]:.1f} s", file=sys.stderr, flush=True)
+        return time.perf_counter()
+
     __graft_entry__.build()
     from bepuphysics1_gb300 import native as N
     from bepuphysics1_gb300 import scenes
@@ -720,6 +736,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
         pg = dist
 
+    t_sec = mark("build", t_start)
     bodies, manifolds, _ = scenes.pile_64k()
     settings = default_settings()
     iters = int(settings["iteration_limit"])
@@ -812,6 +829,7 @@ def main():
                         "frac": step_achieved / peak, "ms_per_step": total_ms / args.steps,
                         "what": "the whole step (every kernel, launch gaps included) against the same bytes"}
 
+    t_sec = mark("headline", t_sec)
     # e2e through the C ABI with pinned host records
     e2e = None
     if not args.no_e2e:
@@ -848,26 +866,33 @@ def main():
                                   "path": "update_bodies, update_manifolds, step, download_bodies, "
                                           "download_constraints"}}
 
+    t_sec = mark("e2e", t_sec)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(bodies, manifolds, cips, args.cpu_sample_seconds, os.cpu_count() or 1)
+    t_sec = mark("cpu_baseline", t_sec)
 
     batch = None
     if not args.no_batch:
         space.close()
         batch = batch_section(args, local, rank, world, pg)
+        t_sec = mark("batch", t_sec)
     chains = None
     if not args.no_chains:
         space.close()
         chains = chain_section(args, local, rank, world, pg)
+        t_sec = mark("chains", t_sec)
     collide = None
     if not args.no_collide:
         space.close()
         collide = collide_section(args, local, rank, world, pg)
+        t_sec = mark("collide", t_sec)
     serve = None
     if not args.no_serve:
         space.close()
         serve = serve_section(args, local, rank, world, pg)
+        t_sec = mark("serve", t_sec)
+    section_s["total"] = round(time.perf_counter() - t_start, 2)
 
     if rank == 0:
         line = {
@@ -892,6 +917,7 @@ def main():
             "chains": chains,
             "collide": collide,
             "serve": serve,
+            "section_seconds": section_s,
         }
         print(json.dumps(line), flush=True)
     space.close()

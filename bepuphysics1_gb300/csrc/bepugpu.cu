@@ -349,6 +349,9 @@ __global__ void k_solve(ManifoldSoA m, BodySoA b, StepParams p, int begin, int e
 
 // Joints (joints_device.cuh).  A colour's joints and manifolds touch different
 // dynamic bodies, so one launch runs both: threads [0, joints) take the joints.
+// kAdded false builds the variant for scenes whose joints are all of the
+// classic types (1-5), without the added types' branches.
+template <bool kAdded>
 __device__ __forceinline__ void WarmJointSlot(const JointSoA& j, const BodySoA& b, int s) {
     uint2 st = j.state[s];
     if (!(st.x & kGroupActive)) return;
@@ -356,10 +359,11 @@ __device__ __forceinline__ void WarmJointSlot(const JointSoA& j, const BodySoA& 
     BodyState A, B;
     LoadJointVelocityV(GlobalBodies{b}, h.x, A);
     LoadJointVelocityV(GlobalBodies{b}, h.y, B);
-    WarmJoint(j, s, A, B, st.x, h.z & 0xff);
+    WarmJoint<kAdded>(j, s, A, B, st.x, h.z & 0xff);
     if (st.x & kDynA) StoreVelocity(b, h.x, A);
     if (st.x & kDynB) StoreVelocity(b, h.y, B);
 }
+template <bool kAdded>
 __device__ __forceinline__ void SolveJointSlot(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
     uint2 st = j.state[s];
     if (!(st.x & kGroupActive)) return;
@@ -367,24 +371,27 @@ __device__ __forceinline__ void SolveJointSlot(const JointSoA& j, const BodySoA&
     BodyState A, B;
     LoadJointVelocityV(GlobalBodies{b}, h.x, A);
     LoadJointVelocityV(GlobalBodies{b}, h.y, B);
-    SolveJoint(j, s, A, B, st, h.z & 0xff, p);
+    SolveJoint<kAdded>(j, s, A, B, st, h.z & 0xff, p);
     if (st.x & kDynA) StoreVelocity(b, h.x, A);
     if (st.x & kDynB) StoreVelocity(b, h.y, B);
     j.state[s] = st;
 }
+template <bool kAdded>
 __global__ void k_prestep_mixed(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < j.count) PrestepJoint(j, b, t, p);
+    if (t < j.count) PrestepJoint<kAdded>(j, b, t, p);
     else if (t - j.count < m.count) PrestepManifold(m, b, t - j.count, p);
 }
+template <bool kAdded>
 __global__ void k_warm_mixed(ManifoldSoA m, BodySoA b, JointSoA j, int mb, int me, int jb, int je) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < je - jb) WarmJointSlot(j, b, jb + t);
+    if (t < je - jb) WarmJointSlot<kAdded>(j, b, jb + t);
     else if (mb + t - (je - jb) < me) WarmSlot(m, b, mb + t - (je - jb));
 }
+template <bool kAdded>
 __global__ void k_solve_mixed(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, int mb, int me, int jb, int je) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < je - jb) SolveJointSlot(j, b, jb + t, p);
+    if (t < je - jb) SolveJointSlot<kAdded>(j, b, jb + t, p);
     else if (mb + t - (je - jb) < me) SolveSlot(m, b, mb + t - (je - jb), p);
 }
 
@@ -442,6 +449,7 @@ __device__ __forceinline__ unsigned long long GlobalTimer() {
     return t;
 }
 
+template <bool kAdded>
 __global__ void k_persistent(PersistentArgs a) {
     unsigned int localGen = *(volatile unsigned int*)a.generation;
     const int stride = gridDim.x * blockDim.x;
@@ -459,12 +467,12 @@ __global__ void k_persistent(PersistentArgs a) {
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
     }
     if (a.flags & BEPUGPU_STEP_SOLVE) {
-        for (int s = tid; s < a.j.count; s += stride) PrestepJoint(a.j, a.b, s, a.p);
+        for (int s = tid; s < a.j.count; s += stride) PrestepJoint<kAdded>(a.j, a.b, s, a.p);
         for (int s = tid; s < a.m.count; s += stride) PrestepManifold(a.m, a.b, s, a.p);
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
         for (int c = 0; c < a.colours; c++) {
             if (a.j.count)
-                for (int s = a.jointOffsets[c] + tid; s < a.jointOffsets[c + 1]; s += stride) WarmJointSlot(a.j, a.b, s);
+                for (int s = a.jointOffsets[c] + tid; s < a.jointOffsets[c + 1]; s += stride) WarmJointSlot<kAdded>(a.j, a.b, s);
             for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride) WarmSlot(a.m, a.b, s);
             if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
         }
@@ -473,7 +481,7 @@ __global__ void k_persistent(PersistentArgs a) {
             for (int c = 0; c < a.colours; c++) {
                 if (a.j.count)
                     for (int s = a.jointOffsets[c] + tid; s < a.jointOffsets[c + 1]; s += stride)
-                        SolveJointSlot(a.j, a.b, s, a.p);
+                        SolveJointSlot<kAdded>(a.j, a.b, s, a.p);
                 for (int s = a.colourOffsets[c] + tid; s < a.colourOffsets[c + 1]; s += stride)
                     SolveSlot(a.m, a.b, s, a.p);
                 if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
@@ -539,11 +547,14 @@ static size_t Align(size_t x) { return (x + 255) & ~(size_t)255; }
 
 Scene::~Scene() {
     if (graphExec) cudaGraphExecDestroy(graphExec);
-    if (arena) cudaFree(arena);
+    if ((arena || staging) && stream) cudaStreamSynchronize(stream);  // no work reads the blocks any more
+    if (heap) {
+        heap->Free(arena);
+        heap->Free(staging);
+    }
     if (spillHost && !spillHostBorrowed) cudaFreeHost(spillHost);
     if (evSpill) cudaEventDestroy(evSpill);
     if (evRestore) cudaEventDestroy(evRestore);
-    if (staging) cudaFree(staging);
     if (counter) cudaFree(counter);
     if (evStart) cudaEventDestroy(evStart);
     if (evStop) cudaEventDestroy(evStop);
@@ -632,7 +643,10 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     L.bodyRecords = take(sizeof(bepugpu_body) * B);
     L.shape = take(16 * B); L.genSlots = take(4 * M);
     arenaBytes = bytes;
-    cudaError_t e = cudaMalloc(&arena, bytes);
+    // The arena and the staging buffer are blocks of the context's heap, like
+    // the ones a restore takes after a spill.
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    cudaError_t e = heap->Alloc(bytes, &arena);
     if (e != cudaSuccess) {
         arena = nullptr;
         ctx->SetError("scene arena of %zu bytes: %s", bytes, cudaGetErrorString(e));
@@ -644,14 +658,14 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     j.count = 0;
     j.capacity = (int)J;
     Rebase();
-    CK(cudaMemset(arena, 0, bytes));
+    CK(cudaMemsetAsync(arena, 0, bytes, stream));
     // body records, then manifold records: bepugpu_step_host stages both at once
     stagingManifoldsAt = Align(sizeof(bepugpu_body) * B);
     stagingBytes = stagingManifoldsAt + sizeof(bepugpu_manifold) * M;
-    CK(cudaMalloc(&staging, stagingBytes));
+    CK(heap->Alloc(stagingBytes, &staging));
+    CK(cudaStreamSynchronize(stream));
     CK(cudaMalloc(&counter, kScratchBytes));
     CK(cudaMemset(counter, 0, kScratchBytes));
-    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&evStart));
     CK(cudaEventCreate(&evStop));
     for (auto& e : evPhase) CK(cudaEventCreate(&e));
@@ -692,15 +706,14 @@ void Scene::Rebase() {
     genSlotsDev = (int32_t*)(base + L.genSlots);
 }
 
-// Moves the arena to pinned host memory and releases the scene's device
-// memory but the 1 KiB scratch block.  The scene's step graph is dropped: it
-// holds device addresses.
-// Stream-ordered frees and allocations (cudaFreeAsync / cudaMallocAsync) keep
-// a spill or restore from synchronising the device with work of other scenes.
-// Without `wait` neither call blocks: the spill's copy and frees are ordered
-// on the scene's stream and marked by evSpill; a restore waits for that mark
-// on the stream it is given, copies there, and the scene's stream waits for
-// the copy (evRestore).  `host` (optional) is a pinned buffer of arenaBytes
+// Moves the arena to pinned host memory and gives the scene's heap blocks
+// back (all of its device memory but the 1 KiB scratch block).  The scene's
+// step graph is dropped: it holds device addresses.
+// Neither call synchronises the device with other scenes' work, and without
+// `wait` neither blocks: the spill's copy is ordered on the scene's stream and
+// marked by evSpill, and its blocks become reusable once that copy is done; a
+// restore takes blocks from the heap, waits for the mark on the stream it is
+// given, copies there, and the scene's stream waits for the copy (evRestore).  `host` (optional) is a pinned buffer of arenaBytes
 // for the first spill, owned by the caller.
 bepugpu_status Scene::Spill(Context* ctx, bool wait, void* host) {
     if (!arena) return BEPUGPU_OK;
@@ -715,9 +728,9 @@ bepugpu_status Scene::Spill(Context* ctx, bool wait, void* host) {
     }
     if (!evSpill) CK(cudaEventCreateWithFlags(&evSpill, cudaEventDisableTiming));
     CK(cudaMemcpyAsync(spillHost, arena, arenaBytes, cudaMemcpyDeviceToHost, stream));
-    CK(cudaFreeAsync(arena, stream));
+    CK(heap->FreeAfter(arena, stream));
     arena = nullptr;
-    if (staging) CK(cudaFreeAsync(staging, stream));
+    if (staging) CK(heap->FreeAfter(staging, stream));
     staging = nullptr;
     CK(cudaEventRecord(evSpill, stream));
     if (wait) CK(cudaStreamSynchronize(stream));
@@ -730,11 +743,11 @@ bepugpu_status Scene::Spill(Context* ctx, bool wait, void* host) {
 bepugpu_status Scene::Restore(Context* ctx, cudaStream_t q, bool wait) {
     if (arena) return BEPUGPU_OK;
     if (!q) q = stream;
-    cudaError_t e = cudaMallocAsync(&arena, arenaBytes, q);
+    cudaError_t e = heap->Alloc(arenaBytes, &arena);
     if (e == cudaSuccess) {
-        e = cudaMallocAsync(&staging, stagingBytes, q);
+        e = heap->Alloc(stagingBytes, &staging);
         if (e != cudaSuccess) {
-            cudaFreeAsync(arena, q);
+            heap->Free(arena);
             arena = nullptr;
             staging = nullptr;
         }
@@ -882,8 +895,11 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     const JointSoA js = SweepJoints();
     const int nj = js.count;
     bool solve = (flags & BEPUGPU_STEP_SOLVE) && (nm || nj);
+    const auto prestepMixed = addedJointTypes ? k_prestep_mixed<true> : k_prestep_mixed<false>;
+    const auto warmMixed = addedJointTypes ? k_warm_mixed<true> : k_warm_mixed<false>;
+    const auto solveMixed = addedJointTypes ? k_solve_mixed<true> : k_solve_mixed<false>;
     if (solve) {
-        if (nj) k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, stream>>>(ms, b, js, p);
+        if (nj) prestepMixed<<<Blocks(nm + nj, T), T, 0, stream>>>(ms, b, js, p);
         else k_prestep<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p);
         launchesPerStep++;
     }
@@ -893,7 +909,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
             int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
             int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
             if (j1 > j0) {
-                k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, b0, b1, j0, j1);
+                warmMixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, b0, b1, j0, j1);
                 launchesPerStep++;
             } else if (b1 > b0) {
                 k_warm<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, b0, b1);
@@ -908,7 +924,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
                 int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
                 int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
                 if (j1 > j0) {
-                    k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, p, b0, b1, j0, j1);
+                    solveMixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, p, b0, b1, j0, j1);
                     launchesPerStep++;
                 } else if (b1 > b0) {
                     k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1);
@@ -947,14 +963,16 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
 
 bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t flags) {
     const int T = 256;
-    if (persistentBlocks == 0) {
+    void* kernel = addedJointTypes ? (void*)k_persistent<true> : (void*)k_persistent<false>;
+    if (persistentBlocks == 0 || persistentAdded != addedJointTypes) {
         int perSm = 0;
-        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, k_persistent, T, 0));
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kernel, T, 0));
         if (perSm < 1) {
             ctx->SetError("persistent kernel cannot be resident");
             return BEPUGPU_CUDA_ERROR;
         }
         persistentBlocks = std::min(perSm, persistentBlocksPerSm) * ctx->smCount;
+        persistentAdded = addedJointTypes;
     }
     launchesPerStep = 0;
     if ((flags & BEPUGPU_STEP_COLLIDE) && generatedCount) {
@@ -982,7 +1000,7 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
     CK(cudaMemsetAsync(BarrierCounter(), 0, sizeof(unsigned int), stream));
     CK(cudaMemsetAsync(ErrorWord(), 0, sizeof(int), stream));
     void* args[] = {&a};
-    CK(cudaLaunchCooperativeKernel((void*)k_persistent, dim3(persistentBlocks), dim3(T), args, 0, stream));
+    CK(cudaLaunchCooperativeKernel(kernel, dim3(persistentBlocks), dim3(T), args, 0, stream));
     launchesPerStep++;
     return BEPUGPU_OK;
 }
@@ -1130,6 +1148,7 @@ bepugpu_status bepugpu_create(int32_t device, const bepugpu_settings* settings, 
     if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return BEPUGPU_CUDA_ERROR;
     auto* ctx = new Context();
     ctx->device = device;
+    ctx->heap = std::make_unique<DeviceHeap>();
     if (settings) ctx->settings = *settings;
     else bepugpu_default_settings(&ctx->settings);
     if (ValidateSettings(ctx, &ctx->settings) != BEPUGPU_OK) { delete ctx; return BEPUGPU_INVALID_ARGUMENT; }
@@ -1147,6 +1166,15 @@ void bepugpu_destroy(bepugpu_context* c) {
     ctx->batch.reset();
     ctx->scenes.clear();
     delete ctx;
+}
+
+bepugpu_status bepugpu_memory_usage(bepugpu_context* c, uint64_t* reserved, uint64_t* in_use) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (!reserved || !in_use) return BEPUGPU_INVALID_ARGUMENT;
+    *reserved = ctx->heap->Reserved();
+    *in_use = ctx->heap->InUse();
+    return BEPUGPU_OK;
 }
 
 const char* bepugpu_last_error(bepugpu_context* c) {
@@ -1193,6 +1221,7 @@ bepugpu_status bepugpu_scene_create(bepugpu_context* c, uint32_t nb, uint32_t nm
         return BEPUGPU_INVALID_ARGUMENT;
     }
     auto s = std::make_unique<Scene>();
+    s->heap = ctx->heap.get();
     bepugpu_status st = s->Allocate(ctx, nb, nm, nj);
     if (st != BEPUGPU_OK) return st;
     int32_t id = ctx->nextScene++;
@@ -1772,14 +1801,16 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     const int nj = js.count;
     if ((flags & BEPUGPU_STEP_SOLVE) && (nm || nj)) {
         cudaEvent_t a = mark();
-        k_prestep_mixed<<<Blocks(nm + nj, T), T, 0, q>>>(ms, s->b, js, p);
+        const bool added = s->addedJointTypes;
+        (added ? k_prestep_mixed<true> : k_prestep_mixed<false>)<<<Blocks(nm + nj, T), T, 0, q>>>(ms, s->b, js, p);
         spans.push_back({a, mark(), &out->prestep_ms});
         for (int cc = 0; cc < colours; cc++) {
             int b0 = s->manifoldOffsets[cc], b1 = s->manifoldOffsets[cc + 1];
             int j0 = nj ? s->jointOffsets[cc] : 0, j1 = nj ? s->jointOffsets[cc + 1] : 0;
             if (b1 - b0 + j1 - j0 <= 0) continue;
             cudaEvent_t e0 = mark();
-            k_warm_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, js, b0, b1, j0, j1);
+            (added ? k_warm_mixed<true> : k_warm_mixed<false>)<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(
+                ms, s->b, js, b0, b1, j0, j1);
             spans.push_back({e0, mark(), &out->warm_ms});
             out->warm_launches++;
         }
@@ -1790,7 +1821,8 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
                 if (b1 - b0 + j1 - j0 <= 0) continue;
                 if (b1 > b0) k_census<<<Blocks(b1 - b0, T), T, 0, q>>>(ms, b0, b1, acc);
                 cudaEvent_t e0 = mark();
-                k_solve_mixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(ms, s->b, js, p, b0, b1, j0, j1);
+                (added ? k_solve_mixed<true> : k_solve_mixed<false>)<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, q>>>(
+                    ms, s->b, js, p, b0, b1, j0, j1);
                 spans.push_back({e0, mark(), &out->solve_ms});
                 out->solve_launches++;
             }

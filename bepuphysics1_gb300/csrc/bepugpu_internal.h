@@ -5,7 +5,10 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
+#include <deque>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -20,6 +23,59 @@ namespace bepugpu {
 struct Context;
 struct BatchEngine;
 struct Scene;
+
+// Device memory of a context's scene arenas and staging buffers, carved from
+// large cudaMalloc slabs (heap.cu).  Thread-safe: a server's worker spills and
+// restores while the caller's thread creates and destroys scenes.
+class DeviceHeap {
+  public:
+    DeviceHeap() = default;
+    DeviceHeap(const DeviceHeap&) = delete;
+    DeviceHeap& operator=(const DeviceHeap&) = delete;
+    ~DeviceHeap();
+    cudaError_t Alloc(size_t bytes, void** out);
+    // The caller has finished every use of the block (its stream drained).
+    void Free(void* p);
+    // Reusable once the work queued on `stream` so far has completed.
+    cudaError_t FreeAfter(void* p, cudaStream_t stream);
+    // While held (live servers), empty slabs stay mapped for restores.
+    void Hold(bool hold);
+    size_t Reserved() const;
+    size_t InUse() const;
+
+  private:
+    struct Slab {
+        char* base = nullptr;
+        size_t bytes = 0;
+    };
+    struct FreeRange {
+        size_t bytes;
+        int slab;
+    };
+    struct LiveBlock {
+        size_t bytes;
+        int slab;
+    };
+    struct Pending {
+        char* p;
+        cudaEvent_t done;
+    };
+    void InsertFree(char* p, size_t bytes, int slab);
+    void EraseSized(char* p, size_t bytes);
+    void Reclaim(bool wait);
+    void ReleaseBlock(char* p);
+    void TrimEmptySlabs();
+
+    mutable std::mutex mu_;
+    std::vector<Slab> slabs_;
+    std::map<char*, FreeRange> free_;           // by address: coalescing
+    std::multimap<size_t, char*> bySize_;       // by size: best fit
+    std::unordered_map<char*, LiveBlock> live_;
+    std::deque<Pending> pending_;
+    std::vector<cudaEvent_t> spareEvents_;
+    size_t reserved_ = 0, inUse_ = 0;
+    int holds_ = 0;
+};
 
 StepParams MakeParams(const bepugpu_settings& s, float dt);
 
@@ -174,6 +230,7 @@ struct Scene {
     }
     int SweepColours() const { return manifoldOffsets.empty() ? 0 : (int)manifoldOffsets.size() - 1; }
     uint32_t maxBodies = 0, maxManifolds = 0, maxJoints = 0;
+    DeviceHeap* heap = nullptr;     // the owning context's heap: arena and staging blocks
     void* arena = nullptr;          // null while spilled
     size_t arenaBytes = 0;
     ArenaLayout layout{};
@@ -204,6 +261,7 @@ struct Scene {
     int32_t* slotOf = nullptr;           // device: manifold record -> slot
     int32_t* colourOffsetsDev = nullptr; // device: manifold slot range per colour
     uint32_t jointCount = 0;
+    bool addedJointTypes = false;         // a joint of type 6 or above: kernels with every joint branch
     JointSoA j{};                         // joint slots in colour order (joints.cu)
     std::vector<int32_t> jointOffsets;    // joint slot range per sweep colour
     std::vector<int32_t> hostJointSlotOf; // joint record -> slot
@@ -230,6 +288,7 @@ struct Scene {
     int graphIterations = -1;
     uint32_t launchesPerStep = 0;
     int persistentBlocks = 0;
+    bool persistentAdded = false;  // the persistent variant persistentBlocks was sized for
 
     ~Scene();
     bepugpu_status Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj);
@@ -259,6 +318,7 @@ struct Context {
     int smCount = 0;
     bepugpu_settings settings{};
     std::string lastError;
+    std::unique_ptr<DeviceHeap> heap;  // declared before the scenes: it outlives them
     std::unordered_map<int32_t, std::unique_ptr<Scene>> scenes;
     int32_t nextScene = 1;
     std::unique_ptr<BatchEngine> batch;

@@ -26,7 +26,7 @@
 
 namespace bepugpu {
 
-template <bool kCensus, bool kShared, bool kJoints>
+template <bool kCensus, bool kShared, int kJoints>
 __global__ void k_groups(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, uint32_t flags, GroupTables t,
                          int groupBase, int Bc, int Lc, int Jc, unsigned long long* census) {
     extern __shared__ float4 smem[];
@@ -254,7 +254,7 @@ int ClassThreads(const GroupClass& c, int override_) {
     return std::min(std::max(t, 32), 256);
 }
 
-template <bool kShared, bool kJoints>
+template <bool kShared, int kJoints>
 bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const StepParams& p, uint32_t flags,
                            bool count, GroupTables t) {
     if (c.end <= c.begin) return BEPUGPU_OK;
@@ -274,6 +274,8 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
     }
     const int threads = ClassThreads(c, s->groupThreadsOverride);
     const unsigned blocks = (unsigned)(c.end - c.begin);
+    // the thread's last error must be this launch's own
+    const cudaError_t earlier = cudaGetLastError();
     if (count)
         k_groups<true, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
             s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census());
@@ -282,7 +284,9 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
             s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
-        ctx->SetError("group kernel launch: %s", cudaGetErrorString(e));
+        ctx->SetError("group kernel launch (%u CTAs of %d threads, %zu bytes of shared memory): %s%s%s", blocks,
+                      threads, smemBytes, cudaGetErrorString(e), earlier != cudaSuccess ? "; earlier error: " : "",
+                      earlier != cudaSuccess ? cudaGetErrorString(earlier) : "");
         return BEPUGPU_CUDA_ERROR;
     }
     return BEPUGPU_OK;
@@ -307,8 +311,13 @@ bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_
     t.jointColourOffsets = s->groupJointColourOffsetsDev;
     bepugpu_status st = LaunchClass<true, false>(ctx, s, g.shared, p, flags, count, t);
     if (st == BEPUGPU_OK) st = LaunchClass<false, false>(ctx, s, g.global, p, flags, count, t);
-    if (st == BEPUGPU_OK) st = LaunchClass<true, true>(ctx, s, g.sharedJoints, p, flags, count, t);
-    if (st == BEPUGPU_OK) st = LaunchClass<false, true>(ctx, s, g.globalJoints, p, flags, count, t);
+    if (s->addedJointTypes) {
+        if (st == BEPUGPU_OK) st = LaunchClass<true, 2>(ctx, s, g.sharedJoints, p, flags, count, t);
+        if (st == BEPUGPU_OK) st = LaunchClass<false, 2>(ctx, s, g.globalJoints, p, flags, count, t);
+    } else {
+        if (st == BEPUGPU_OK) st = LaunchClass<true, 1>(ctx, s, g.sharedJoints, p, flags, count, t);
+        if (st == BEPUGPU_OK) st = LaunchClass<false, 1>(ctx, s, g.globalJoints, p, flags, count, t);
+    }
     return st;
 }
 

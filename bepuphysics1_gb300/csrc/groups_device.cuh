@@ -45,7 +45,9 @@ __host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int
 // the manifolds into shared-memory solve lanes (Jc per lane) and swept colour
 // by colour with them -- a colour's joints and manifolds share no dynamic
 // body -- and their impulses go back to the joint lanes after the sweeps.
-template <bool kCensus, bool kShared, bool kJoints>
+// kJoints: 0 no joints, 1 the classic joint types (1-5) only, 2 any type; the
+// classic variant leaves the added types' branches out of the kernel.
+template <bool kCensus, bool kShared, int kJoints>
 __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const JointSoA& jt,
                                           const StepParams& p, uint32_t flags, const GroupTables& t,
                                           const GroupDesc& g, int Bc, int Lc, int Jc, float4* smem,
@@ -142,7 +144,7 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
         for (int q = tid; q < nj; q += T) {
             const int2 r = t.jointRefs[g.jBegin + q];
             jRefs[q] = r;
-            PrestepJointIO(jt, g.jBegin + q, jl, q, bv, r.x, r.y, p);
+            PrestepJointIO<kJoints == 2>(jt, g.jBegin + q, jl, q, bv, r.x, r.y, p);
         }
     if (kCensus && tid == 0) atomicAdd(census + 3, 208ull * (unsigned long long)nLocal);  // 7 lanes in, 6 out
     __syncthreads();
@@ -158,7 +160,7 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
                     BodyState A, B;
                     LoadJointVelocityV(bv, r.x, A);
                     LoadJointVelocityV(bv, r.y, B);
-                    WarmJoint(jl, q, A, B, st.x, JointType(st.x));
+                    WarmJoint<kJoints == 2>(jl, q, A, B, st.x, JointType(st.x));
                     if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
                     if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
                 }
@@ -186,7 +188,7 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
                         BodyState A, B;
                         LoadJointVelocityV(bv, r.x, A);
                         LoadJointVelocityV(bv, r.y, B);
-                        SolveJoint(jl, q, A, B, st, JointType(st.x), p);
+                        SolveJoint<kJoints == 2>(jl, q, A, B, st, JointType(st.x), p);
                         if (st.x & kDynA) StoreVelocityV(bv, r.x, A);
                         if (st.x & kDynB) StoreVelocityV(bv, r.y, B);
                         jl.state[q] = st;

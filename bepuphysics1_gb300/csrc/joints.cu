@@ -98,6 +98,8 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
 // lanes (kJACC0, kJACC1), heads and a cleared state.
 bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints, uint32_t nj) {
     s->j.count = (int)nj;
+    s->addedJointTypes = false;
+    for (uint32_t u = 0; u < nj; u++) s->addedJointTypes |= joints[u].type > BEPUGPU_JOINT_REVOLUTE;
     if (!nj) return BEPUGPU_OK;
     constexpr int kIn = kJointLanes - kJLA;
     std::vector<float4> lanes((size_t)kIn * nj), acc(2 * (size_t)nj);

@@ -328,7 +328,7 @@ __device__ __forceinline__ void ApplyPointOnLine(float4 oa, float4 ob, float4 m0
 // prestep products and state at (jo, so): the same slot on the sweep path, the
 // group's shared-memory lanes in a group kernel.  ra, rb: the connections'
 // refs in the body view.
-template <class V>
+template <bool kAdded, class V>
 __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const JointSoA& jo, int so, const V& bv,
                                                int ra, int rb, const StepParams& p) {
     const JointSoA& j = jo;
@@ -351,7 +351,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     const float stiffness = la.w, damping = lb.w, maxCorr = axa.w, margin = axb.w;
     const float maxCorrSq = ji.L(kJTA, si).w;
     uint32_t active = present & childIsActive;
-    if ((active & kJChildBall) && IsPointOnLineType(type)) {
+    if (kAdded && (active & kJChildBall) && IsPointOnLineType(type)) {
         // PointOnLineJoint.Update (PointOnLineJoint.cs:362-438).  Inputs: kJLA line anchor
         // (A), kJLB point (B), kJBP line direction, kJBX / kJTA restricted axes (A's frame).
         // Lanes: kJOA rA + softness, kJOB.xyz rB, kJM0 axis 1 + M11, kJM1 axis 2 + M12,
@@ -413,7 +413,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM1, s) = make_float4(ax2.x, ax2.y, ax2.z, -i12);
         j.L(kJM2, s) = make_float4(-i21, -i22, bx, by);
         st |= 1u << (kChildShift + 0);
-    } else if ((active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.Update (PointOnPlaneJoint.cs:250-306).  Lanes: kJOA rA + softness,
         // kJOB.xyz rB, kJM0 normal + negative effective mass, kJM1 rA x n + bias, kJM2 -(rB x n).
         const float3 n = JTransform(JXYZ(axa), A.R);
@@ -456,7 +456,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM1, s) = make_float4(raxn.x, raxn.y, raxn.z, bias);
         j.L(kJM2, s) = make_float4(rbxn.x, rbxn.y, rbxn.z, 0.f);
         st |= 1u << (kChildShift + 0);
-    } else if ((active & kJChildBall) && IsDistanceType(type)) {
+    } else if (kAdded && (active & kJChildBall) && IsDistanceType(type)) {
         // DistanceJoint.Update (DistanceJoint.cs:275-352) / DistanceLimit.Update (DistanceLimit.cs:312-430).
         // Lanes: kJM0 jLinearA + velocityToImpulse, kJM1 jAngularA + bias, kJM2 jAngularB
         // (jLinearB = -jLinearA); kJOA.w softness.  A limit keeps its last jLinearA in kJBP.
@@ -581,7 +581,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM2, s) = make_float4(mass.M33, bx, by, bz);
         st |= 1u << (kChildShift + 0);
     }
-    if ((active & kJChildAngular) && IsTwistType(type)) {
+    if (kAdded && (active & kJChildAngular) && IsTwistType(type)) {
         // TwistJoint.Update (TwistJoint.cs:235-300).  Inputs: axes A / B, A's local y and z
         // (kJC1, kJC2) and B's local y (kJBX).  Lanes: kJW1 jacobianB + velocityToImpulse,
         // kJW2.x bias, kJOB.w softness (jacobianA = -jacobianB).
@@ -608,7 +608,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
             j.L(kJW2, s) = make_float4(bias, 0.f, 0.f, 0.f);
             st |= 1u << (kChildShift + 1);
         }
-    } else if ((active & kJChildAngular) && IsNoRotationType(type)) {
+    } else if (kAdded && (active & kJChildAngular) && IsNoRotationType(type)) {
         // NoRotationJoint.Update (NoRotationJoint.cs:194-243).  Inputs: kJC1 / kJC2 the
         // initial orientations' conjugates; lanes kJL0..kJL2 the 3x3 effective mass and
         // the bias, kJOB.w the softness.
@@ -829,21 +829,23 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     j.state[s] = make_uint2(st, 0u);
 }
 
+template <bool kAdded>
 __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b, int s, const StepParams& p) {
     const int4 h = j.head[s];
-    PrestepJointIO(j, s, j, s, GlobalBodies{b}, h.x, h.y, p);
+    PrestepJointIO<kAdded>(j, s, j, s, GlobalBodies{b}, h.x, h.y, p);
 }
 
 // ---------------------------------------------------------- warm start --
 // ExclusiveUpdate of every active child in order.
+template <bool kAdded>
 __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint32_t st,
                                           int type) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
     const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && IsPointOnLineType(type)) {
+    if (kAdded && (st & (1u << kChildShift)) && IsPointOnLineType(type)) {
         // PointOnLineJoint.ExclusiveUpdate (PointOnLineJoint.cs:440-463)
         ApplyPointOnLine(j.L(kJOA, s), j.L(kJOB, s), j.L(kJM0, s), j.L(kJM1, s), acc0.x, acc0.y, dynA, dynB, A, B);
-    } else if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.ExclusiveUpdate (PointOnPlaneJoint.cs:308-328)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
         const float a = acc0.x;
@@ -856,7 +858,7 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
             ApplyLinear(B, -ix, -iy, -iz);
             ApplyAngular(B, m2.x * a, m2.y * a, m2.z * a);
         }
-    } else if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+    } else if (kAdded && (st & (1u << kChildShift)) && IsDistanceType(type)) {
         // DistanceJoint / DistanceLimit.ExclusiveUpdate (DistanceJoint.cs:354-380)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
         const float a = acc0.x;
@@ -884,13 +886,13 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
             ApplyAngular(B, t.x, t.y, t.z);
         }
     }
-    if ((st & (2u << kChildShift)) && IsTwistType(type)) {
+    if (kAdded && (st & (2u << kChildShift)) && IsTwistType(type)) {
         // TwistJoint.ExclusiveUpdate (TwistJoint.cs:302-317)
         const float4 w1 = j.L(kJW1, s);
         const float a = acc0.w;
         if (dynA) ApplyAngular(A, -w1.x * a, -w1.y * a, -w1.z * a);
         if (dynB) ApplyAngular(B, w1.x * a, w1.y * a, w1.z * a);
-    } else if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+    } else if (kAdded && (st & (2u << kChildShift)) && IsNoRotationType(type)) {
         // NoRotationJoint.ExclusiveUpdate (NoRotationJoint.cs:245-259)
         if (dynA) ApplyAngular(A, acc0.w, acc1.x, acc1.y);
         if (dynB) ApplyAngular(B, -acc0.w, -acc1.x, -acc1.y);
@@ -932,6 +934,7 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
 // -------------------------------------------------------------- solve --
 // Solver.UnsafeSolveIteration (Solver.cs:285-314) on the joint, then
 // SolverGroup.SolveUpdateable (SolverGroup.cs:117-150) on each child.
+template <bool kAdded>
 __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint2& state,
                                            int type, const StepParams& p) {
     uint32_t st = state.x, zeros = state.y;
@@ -956,7 +959,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
     float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
-    if ((st & (1u << kChildShift)) && IsPointOnLineType(type)) {
+    if (kAdded && (st & (1u << kChildShift)) && IsPointOnLineType(type)) {
         // PointOnLineJoint.SolveIteration (PointOnLineJoint.cs:247-355)
         const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
                      m2 = j.L(kJM2, s);
@@ -974,7 +977,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         acc0.y = y + acc0.y;
         ApplyPointOnLine(oa, ob, m0, m1, x, y, dynA, dynB, A, B);
         account(0, fabsf(x) + fabsf(y));
-    } else if ((st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
         // PointOnPlaneJoint.SolveIteration (PointOnPlaneJoint.cs:212-243)
         const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
                      m2 = j.L(kJM2, s);
@@ -996,7 +999,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
             ApplyAngular(B, m2.x * lambda, m2.y * lambda, m2.z * lambda);
         }
         account(0, lambda);  // signed, as the reference returns it
-    } else if ((st & (1u << kChildShift)) && IsDistanceType(type)) {
+    } else if (kAdded && (st & (1u << kChildShift)) && IsDistanceType(type)) {
         // DistanceJoint.SolveIteration (DistanceJoint.cs:226-268) /
         // DistanceLimit.SolveIteration (DistanceLimit.cs:260-305)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
@@ -1057,7 +1060,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         }
         account(0, fabsf(tx) + fabsf(ty) + fabsf(tz));
     }
-    if ((st & (2u << kChildShift)) && IsTwistType(type)) {
+    if (kAdded && (st & (2u << kChildShift)) && IsTwistType(type)) {
         // TwistJoint.SolveIteration (TwistJoint.cs:204-228)
         const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s);
         const float softness = j.L(kJOB, s).w;
@@ -1070,7 +1073,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         if (dynA) ApplyAngular(A, jax * lambda, jay * lambda, jaz * lambda);
         if (dynB) ApplyAngular(B, w1.x * lambda, w1.y * lambda, w1.z * lambda);
         account(1, fabsf(lambda));
-    } else if ((st & (2u << kChildShift)) && IsNoRotationType(type)) {
+    } else if (kAdded && (st & (2u << kChildShift)) && IsNoRotationType(type)) {
         // NoRotationJoint.SolveIteration (NoRotationJoint.cs:160-187)
         const float4 l0 = j.L(kJL0, s), l1 = j.L(kJL1, s), l2 = j.L(kJL2, s);
         const float softness = j.L(kJOB, s).w;

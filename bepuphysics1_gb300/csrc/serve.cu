@@ -102,30 +102,6 @@ class HostPool {
     size_t left_ = 0, pinned_ = 0;
 };
 
-// While a server lives, the device's stream-ordered pool keeps the memory that
-// spills free instead of handing it back to the driver at the next
-// synchronisation: a restore then reuses mapped memory (tens of microseconds)
-// rather than mapping new pages.  The pool's own threshold is put back when
-// the last server of the device goes.
-void HoldPoolMemory(int device, bool hold) {
-    static std::mutex mu;
-    static std::unordered_map<int, std::pair<int, uint64_t>> held;  // device -> servers, saved threshold
-    std::lock_guard<std::mutex> g(mu);
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return;
-    auto& h = held[device];
-    if (hold) {
-        if (h.first++ == 0) {
-            cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &h.second);
-            uint64_t keep = UINT64_MAX;
-            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-        }
-    } else if (h.first > 0 && --h.first == 0) {
-        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &h.second);
-        cudaMemPoolTrimTo(pool, 0);
-    }
-}
-
 }  // namespace
 
 struct Server {
@@ -269,11 +245,12 @@ struct Server {
         return ok;
     }
 
-    void EnsureViewCapacity() {
-        if (viewsCap >= viewsHost.size()) return;
+    cudaError_t EnsureViewCapacity() {
+        if (viewsCap >= viewsHost.size()) return cudaSuccess;
         size_t want = std::max<size_t>(viewsHost.size(), viewsCap * 2);
         SceneView* d = nullptr;
-        if (cudaMalloc(&d, sizeof(SceneView) * want) != cudaSuccess) return;
+        const cudaError_t e = cudaMalloc(&d, sizeof(SceneView) * want);
+        if (e != cudaSuccess) return e;
         if (viewsDev) {
             cudaDeviceSynchronize();  // no wave reads the old table any more
             cudaFree(viewsDev);
@@ -282,6 +259,7 @@ struct Server {
         viewsCap = want;
         dirtyViews.clear();
         for (int i = 0; i < (int)viewsHost.size(); i++) dirtyViews.push_back(i);
+        return cudaSuccess;
     }
 
     bool FinishWaves() {
@@ -439,10 +417,17 @@ struct Server {
         }
         for (auto it = keep.rbegin(); it != keep.rend(); ++it) ready.push_front(*it);
         cudaError_t e = cudaSuccess;
+        const char* failedAt = "";
+        auto check = [&](cudaError_t r, const char* at) {
+            if (e == cudaSuccess && r != cudaSuccess) {
+                e = r;
+                failedAt = at;
+            }
+        };
         if (!restored.empty()) {
             const double t0 = NowUs();
             for (Scene* s : restored)
-                if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+                if (e == cudaSuccess) check(cudaStreamSynchronize(s->stream), "restore copy");
             usRestore += NowUs() - t0;
         }
         if (w.slotIds.empty()) return false;
@@ -453,16 +438,17 @@ struct Server {
             gMem = std::max(gMem, sMem);
             shared.clear();
         }
-        EnsureViewCapacity();
-        if (e == cudaSuccess && !viewsDev) e = cudaErrorMemoryAllocation;
+        if (e == cudaSuccess) check(EnsureViewCapacity(), "scene table allocation");
         // Synchronous copies: any later wave, on any stream, may read these entries.
         if (dirtyViews.size() > 32) {
             if (e == cudaSuccess)
-                e = cudaMemcpy(viewsDev, viewsHost.data(), sizeof(SceneView) * viewsHost.size(), cudaMemcpyHostToDevice);
+                check(cudaMemcpy(viewsDev, viewsHost.data(), sizeof(SceneView) * viewsHost.size(),
+                                 cudaMemcpyHostToDevice), "scene table copy");
         } else {
             for (int id : dirtyViews)
                 if (e == cudaSuccess)
-                    e = cudaMemcpy(viewsDev + id, &viewsHost[id], sizeof(SceneView), cudaMemcpyHostToDevice);
+                    check(cudaMemcpy(viewsDev + id, &viewsHost[id], sizeof(SceneView), cudaMemcpyHostToDevice),
+                          "scene table copy");
         }
         dirtyViews.clear();
         size_t nWork = shared.size() + global.size();
@@ -472,8 +458,9 @@ struct Server {
             w.workDev = nullptr;
             w.workHost = nullptr;
             size_t want = std::max(nWork, w.workCap * 2);
-            if ((e = cudaMalloc(&w.workDev, sizeof(int4) * want)) == cudaSuccess &&
-                (e = cudaMallocHost(&w.workHost, sizeof(int4) * want)) == cudaSuccess)
+            check(cudaMalloc(&w.workDev, sizeof(int4) * want), "work list allocation");
+            if (e == cudaSuccess) check(cudaMallocHost(&w.workHost, sizeof(int4) * want), "work list allocation");
+            if (e == cudaSuccess)
                 w.workCap = want;
             else
                 w.workCap = 0;
@@ -483,35 +470,40 @@ struct Server {
         if (e == cudaSuccess && nWork) {
             std::copy(shared.begin(), shared.end(), w.workHost);
             std::copy(global.begin(), global.end(), w.workHost + shared.size());
-            e = cudaMemcpyAsync(w.workDev, w.workHost, sizeof(int4) * nWork, cudaMemcpyHostToDevice, w.stream);
+            check(cudaMemcpyAsync(w.workDev, w.workHost, sizeof(int4) * nWork, cudaMemcpyHostToDevice, w.stream),
+                  "work list copy");
             if (e == cudaSuccess && !shared.empty()) {
-                e = LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc, sMem, 0,
-                                        passes, w.stream);
+                check(LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc, sMem,
+                                          0, passes, w.stream),
+                      "group launch");
                 statLaunches += passes;
             }
             if (e == cudaSuccess && !global.empty()) {
-                e = LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p, cfg.flags,
-                                        gBc, 1, gMem, 0, passes, w.stream);
+                check(LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p,
+                                          cfg.flags, gBc, 1, gMem, 0, passes, w.stream),
+                      "group launch");
                 statLaunches += passes;
             }
         }
         // one-scene path: each scene's own stream, joined into the wave's event
+        bool stepFailed = false;
         for (int k : plain) {
             if (e != cudaSuccess) break;
             Scene* s = slots[w.slotIds[k]].s;
             for (uint32_t st = 0; st < w.reqs[k].steps; st++) {
                 if (s->Step(&sink, cfg.dt, cfg.flags) != BEPUGPU_OK) {
-                    SetError(sink.lastError);
-                    e = cudaErrorUnknown;
+                    SetError("wave step: " + sink.lastError);
+                    stepFailed = true;
+                    check(cudaErrorUnknown, "step");
                     break;
                 }
                 statLaunches += s->launchesPerStep;
             }
-            if (e == cudaSuccess) e = cudaStreamWaitEvent(w.stream, s->evStop, 0);
+            if (e == cudaSuccess) check(cudaStreamWaitEvent(w.stream, s->evStop, 0), "wave join");
         }
-        if (e == cudaSuccess) e = cudaEventRecord(w.done, w.stream);
+        if (e == cudaSuccess) check(cudaEventRecord(w.done, w.stream), "wave event");
         if (e != cudaSuccess) {
-            SetError(std::string("wave launch: ") + cudaGetErrorString(e));
+            if (!stepFailed) SetError(std::string("wave launch (") + failedAt + "): " + cudaGetErrorString(e));
             for (size_t k = 0; k < w.slotIds.size(); k++) {
                 Slot& sl = slots[w.slotIds[k]];
                 sl.inFlight = false;
@@ -583,7 +575,7 @@ bepugpu_status Shutdown(Server* s) {
         cudaStreamDestroy(w.stream);
     }
     if (s->viewsDev) cudaFree(s->viewsDev);
-    HoldPoolMemory(s->ctx->device, false);
+    s->ctx->heap->Hold(false);
     delete s;
     return st;
 }
@@ -640,7 +632,7 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
     s->cfg = *config;
     s->cfg.flags &= BEPUGPU_STEP_ALL;
     s->p = MakeParams(ctx->settings, config->dt);
-    HoldPoolMemory(ctx->device, true);
+    ctx->heap->Hold(true);
     s->waves.resize(config->max_waves_in_flight);
     for (auto& w : s->waves) {
         if (cudaStreamCreateWithFlags(&w.stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -650,7 +642,7 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
                 if (x.stream) cudaStreamDestroy(x.stream);
                 if (x.done) cudaEventDestroy(x.done);
             }
-            HoldPoolMemory(ctx->device, false);
+            ctx->heap->Hold(false);
             delete s;
             return BEPUGPU_CUDA_ERROR;
         }

@@ -122,6 +122,7 @@ GPU_EXPORTS = {
     "bepugpu_last_error": (ctypes.c_char_p, [_P]),
     "bepugpu_set_settings": (_I, [_P, _P]),
     "bepugpu_synchronize": (_I, [_P]),
+    "bepugpu_memory_usage": (_I, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]),
     "bepugpu_scene_create": (_I, [_P, _U, _U, _U, ctypes.POINTER(_I)]),
     "bepugpu_scene_destroy": (_I, [_P, _I]),
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),

@@ -57,6 +57,10 @@ class Server:
             msg = self.lib.bepugpu_server_last_error(self.handle)
             N.raise_for(status, msg.decode() if msg else "")
 
+    def last_error(self) -> str:
+        msg = self.lib.bepugpu_server_last_error(self.handle)
+        return msg.decode() if msg else ""
+
     def add(self, space: GpuSpace):
         self.check(self.lib.bepugpu_server_add_scene(self.handle, space.id))
 

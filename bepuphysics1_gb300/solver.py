@@ -45,6 +45,12 @@ class Context:
     def synchronize(self):
         self.check(self.lib.bepugpu_synchronize(self.handle))
 
+    def memory_usage(self) -> tuple[int, int]:
+        """(reserved, in_use) bytes of the device heap that holds scene arenas."""
+        r, u = ctypes.c_uint64(), ctypes.c_uint64()
+        self.check(self.lib.bepugpu_memory_usage(self.handle, ctypes.byref(r), ctypes.byref(u)))
+        return r.value, u.value
+
     def close(self):
         if getattr(self, "handle", None):
             self.lib.bepugpu_destroy(self.handle)

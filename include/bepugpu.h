@@ -255,6 +255,11 @@ void bepugpu_destroy(bepugpu_context* ctx);
 const char* bepugpu_last_error(bepugpu_context* ctx);
 bepugpu_status bepugpu_set_settings(bepugpu_context* ctx, const bepugpu_settings* settings);
 bepugpu_status bepugpu_synchronize(bepugpu_context* ctx);
+/* Device memory of the context's scenes: `reserved` the slabs mapped for them,
+ * `in_use` the arena and staging blocks of resident scenes.  Slabs that no
+ * scene uses go back to the device when their last scene goes, unless a
+ * server is live (it keeps them for restores). */
+bepugpu_status bepugpu_memory_usage(bepugpu_context* ctx, uint64_t* reserved, uint64_t* in_use);
 
 /* Scenes.  A scene is one Space's body set and solver list.  Capacities are
  * fixed at creation; uploads may use any count up to them. */

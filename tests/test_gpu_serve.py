@@ -220,3 +220,52 @@ def test_context_destroyed_under_a_live_server():
     with pytest.raises(N.BepuError):
         srv.drain(1000)
     srv.close()
+
+
+def test_device_heap_reuses_and_returns_memory(gpu_context):
+    """Scene arenas are heap blocks: freed blocks are taken again by scenes of
+    the same sizes, and slabs no scene uses go back to the device."""
+    gpu_context.set_settings(default_settings())
+    r0, u0 = gpu_context.memory_usage()
+    pool = _pool(40, 71)
+    spaces = [GpuSpace(gpu_context, b, m) for b, m in pool]
+    r1, u1 = gpu_context.memory_usage()
+    assert u1 > u0 and r1 >= u1 and r1 >= r0
+    for sp in spaces[::2]:
+        sp.close()
+    _, u2 = gpu_context.memory_usage()
+    assert u0 < u2 < u1
+    again = [GpuSpace(gpu_context, b, m) for b, m in pool[::2]]
+    r3, u3 = gpu_context.memory_usage()
+    assert u3 == u1 and r3 == r1
+    for sp in again:
+        sp.step(DT)
+    for sp in again + spaces[1::2]:
+        sp.close()
+    assert gpu_context.memory_usage() == (r0, u0)
+
+
+def test_served_scenes_spill_into_held_heap(gpu_context):
+    """While a server lives its spills keep the heap's slabs; they go back when
+    the server and the scenes are gone."""
+    gpu_context.set_settings(default_settings())
+    r0, u0 = gpu_context.memory_usage()
+    pool = _pool(12, 72)
+    spaces = [GpuSpace(gpu_context, b, m) for b, m in pool]
+    _, u1 = gpu_context.memory_usage()
+    srv = Server(gpu_context, budget_bytes=(u1 - u0) // 3, dt=float(DT))
+    for sp in spaces:
+        srv.add(sp)
+    for k in range(3):
+        for sp in spaces:
+            while srv.submit(sp.id, 1, k) == N.QUEUE_FULL:
+                srv.poll()
+    srv.drain()
+    st = srv.stats()
+    assert st["spills"] > 0 and st["restores"] > 0
+    r2, u2 = gpu_context.memory_usage()
+    assert u2 < u1 and r2 >= r0
+    srv.close()
+    for sp in spaces:
+        sp.close()
+    assert gpu_context.memory_usage() == (r0, u0)
