@@ -23,9 +23,10 @@ namespace bepugpu {
 
 namespace {
 
-constexpr float kHostTwoPi = 6.28318548f, kHostPiOver2 = 1.57079637f;  // MathHelper.cs:13-33
+constexpr float kHostPi = 3.14159274f, kHostTwoPi = 6.28318548f, kHostPiOver2 = 1.57079637f;  // MathHelper.cs:13-33
 
-// RevoluteLimit.GetDistanceFromMinimum (RevoluteLimit.cs:622-646)
+// RevoluteLimit.GetDistanceFromMinimum (RevoluteLimit.cs:622-646); TwistLimit's
+// (TwistLimit.cs:341-357) is the same function.
 float DistanceFromMinimum(float minimumAngle, float angle) {
     if (minimumAngle > 0) {
         if (angle >= minimumAngle) return angle - minimumAngle;
@@ -51,8 +52,10 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_TWIST: return kJChildAngular;
         case BEPUGPU_JOINT_POINT_ON_LINE: return kJChildBall;
         case BEPUGPU_JOINT_PRISMATIC:
-        case BEPUGPU_JOINT_LINE_SLIDER:
+        case BEPUGPU_JOINT_LINE_SLIDER: return kJChildBall | kJChildAngular | kJChildLimit;
         case BEPUGPU_JOINT_UNIVERSAL: return kJChildBall | kJChildAngular;
+        case BEPUGPU_JOINT_TWIST_LIMIT:
+        case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT: return kJChildLimit;
         default: return 0;
     }
 }
@@ -112,8 +115,9 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
         const int slot = s->hostJointSlotOf[u];
         const uint32_t present = ChildrenOf(r.type);
         uint32_t childIsActive = present;
-        if (r.type == BEPUGPU_JOINT_REVOLUTE && !(r.flags & BEPUGPU_JOINT_LIMIT_ACTIVE))
-            childIsActive &= ~kJChildLimit;
+        const bool groupLimit = r.type == BEPUGPU_JOINT_REVOLUTE || r.type == BEPUGPU_JOINT_PRISMATIC ||
+                                r.type == BEPUGPU_JOINT_LINE_SLIDER;
+        if (groupLimit && !(r.flags & BEPUGPU_JOINT_LIMIT_ACTIVE)) childIsActive &= ~kJChildLimit;
         uint32_t z = (uint32_t)r.type | (present << kJPresentShift) | (childIsActive << kJChildActiveShift) |
                      ((r.flags & BEPUGPU_JOINT_ACTIVE) ? kJGroupIsActive : 0u);
         head[slot] = make_int4(r.body_a, r.body_b, (int)z, (int)u);
@@ -147,8 +151,22 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             at(kJAXA, slot) = make_float4(r.limit_min, r.limit_max, 0.f, maxCorr);
             at(kJBP, slot) = make_float4(0.f, 0.f, 0.f, 0.f);  // the limit's last jLinearA
         }
-        // impulses: ball xyz | angular x, angular y | limit x | limit y
-        float ball[3] = {0, 0, 0}, ang[2] = {0, 0}, lim[2] = {0, 0};
+        if (r.type == BEPUGPU_JOINT_TWIST_LIMIT) {
+            // MinimumAngle / MaximumAngle setters (TwistLimit.cs:50-75): the maximum's
+            // setter wraps the minimum a second time, which changes nothing.
+            float minimumAngle = std::fmod(r.limit_min, kHostTwoPi);
+            if (minimumAngle > kHostPi) minimumAngle -= kHostTwoPi;
+            if (minimumAngle <= -kHostPi) minimumAngle += kHostTwoPi;
+            const float maximumAngle = std::fmod(r.limit_max, kHostTwoPi);
+            at(kJBX, slot) = F4(r.basis_x, 0.f);
+            at(kJTRIG, slot) = make_float4(minimumAngle, DistanceFromMinimum(minimumAngle, maximumAngle), 0.f, 0.f);
+        }
+        if (r.type == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || r.type == BEPUGPU_JOINT_PRISMATIC ||
+            r.type == BEPUGPU_JOINT_LINE_SLIDER)
+            // a prismatic joint's kJC1 / kJC2 hold orientations: the limit's bounce settings go here
+            at(kJTRIG, slot) = make_float4(r.limit_min, r.limit_max, r.bounciness, r.bounce_velocity_threshold);
+        // impulses: ball xyz | angular x, angular y | limit x | limit y | twist limit error
+        float ball[3] = {0, 0, 0}, ang[2] = {0, 0}, lim[2] = {0, 0}, last = 0;
         switch (r.type) {
             case BEPUGPU_JOINT_BALL_SOCKET: std::memcpy(ball, r.impulse, 12); break;
             case BEPUGPU_JOINT_REVOLUTE_ANGULAR: std::memcpy(ang, r.impulse, 8); break;
@@ -180,10 +198,19 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_PRISMATIC:
                 ball[0] = r.impulse[0]; ball[1] = r.impulse[1];
                 ang[0] = r.impulse[2]; ang[1] = r.impulse[3]; lim[0] = r.impulse[4];
+                lim[1] = r.impulse[5];
                 break;
             case BEPUGPU_JOINT_LINE_SLIDER:
                 ball[0] = r.impulse[0]; ball[1] = r.impulse[1];
                 ang[0] = r.impulse[2]; ang[1] = r.impulse[3];
+                lim[1] = r.impulse[4];
+                break;
+            case BEPUGPU_JOINT_TWIST_LIMIT:
+                lim[0] = r.impulse[0];
+                last = r.impulse[1];
+                break;
+            case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
+                lim[1] = r.impulse[0];
                 break;
             case BEPUGPU_JOINT_UNIVERSAL:
                 std::memcpy(ball, r.impulse, 12);
@@ -191,7 +218,7 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 break;
         }
         at(kJACC0, slot) = make_float4(ball[0], ball[1], ball[2], ang[0]);
-        at(kJACC1, slot) = make_float4(ang[1], lim[0], lim[1], 0.f);
+        at(kJACC1, slot) = make_float4(ang[1], lim[0], lim[1], last);
     }
     cudaError_t e;
     if ((e = cudaMemcpy2DAsync(s->j.lanes + (size_t)kJLA * s->j.capacity, sizeof(float4) * s->j.capacity,
@@ -265,10 +292,18 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
             case BEPUGPU_JOINT_PRISMATIC:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y;
                 r.impulse[2] = a0.w; r.impulse[3] = a1.x; r.impulse[4] = a1.y;
+                r.impulse[5] = a1.z;
                 break;
             case BEPUGPU_JOINT_LINE_SLIDER:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y;
                 r.impulse[2] = a0.w; r.impulse[3] = a1.x;
+                r.impulse[4] = a1.z;
+                break;
+            case BEPUGPU_JOINT_TWIST_LIMIT:
+                r.impulse[0] = a1.y; r.impulse[1] = a1.w;
+                break;
+            case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
+                r.impulse[0] = a1.z;
                 break;
             case BEPUGPU_JOINT_UNIVERSAL:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;

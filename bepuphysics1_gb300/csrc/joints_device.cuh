@@ -18,6 +18,10 @@
 //   PointOnPlaneJoint     TwoEntity/Joints/PointOnPlaneJoint.cs:212-330 (the first child slot)
 //   TwistJoint            TwoEntity/Joints/TwistJoint.cs:204-365 (the angular child slot)
 //   PointOnLineJoint      TwoEntity/Joints/PointOnLineJoint.cs:247-463 (the first child slot)
+//   TwistLimit            TwoEntity/JointLimits/TwistLimit.cs:200-383 (the limit slot; its
+//                         last error, which picks the next jacobian's sign, in kJACC1.w)
+//   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
+//                         also the limit child of PRISMATIC and LINE_SLIDER records)
 // and the groups PrismaticJoint (point on line + no rotation), LineSliderJoint
 // (point on line + revolute angular), UniversalJoint (ball socket + twist).
 //   SpringSettings        Constraints/SpringSettings.cs:95-110
@@ -82,15 +86,16 @@ enum : uint32_t {
     kJGroupIsActive = 1u << 14,
 };
 // State word x: kGroupActive (bit 0), child isActiveInSolver bits 1-3,
-// limit minIsActive / maxIsActive bits 4-5, kDynA / kDynB (bits 7-8), the
-// record type (bits 9-12), iterations << 16.  Word y: 4-bit zero-impulse
+// limit minIsActive / maxIsActive bits 4-5 (a linear axis limit: bit 4 =
+// violated below its minimum), kDynA / kDynB (bits 7-8), the record type
+// (bits 9-13), iterations << 16.  Word y: 4-bit zero-impulse
 // streaks of the three children.
 enum : uint32_t {
     kJMinActive = 1u << 4,
     kJMaxActive = 1u << 5,
     kJTypeShift = 9,
 };
-__device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 15u); }
+__device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 31u); }
 __device__ __forceinline__ bool IsDistanceType(int type) {
     return type == BEPUGPU_JOINT_DISTANCE || type == BEPUGPU_JOINT_DISTANCE_LIMIT;
 }
@@ -103,6 +108,16 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+__device__ __forceinline__ bool IsLinearLimitType(int type) {
+    return type == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || type == BEPUGPU_JOINT_PRISMATIC ||
+           type == BEPUGPU_JOINT_LINE_SLIDER;
+}
+// The linear axis limit's three solve lanes (jacobian linear A + softness,
+// angular A + bias, angular B + mass): a prismatic joint's no-rotation child
+// holds kJL0..kJL2, so its limit takes the revolute angular lanes.
+__device__ __forceinline__ int LinearLimitLane(int type) {
+    return type == BEPUGPU_JOINT_PRISMATIC ? (int)kJW1 : (int)kJL0;
 }
 
 struct JointSoA {
@@ -688,7 +703,117 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         const float bounciness = ji.L(kJC1, si).w, threshold = ji.L(kJC2, si).w;
         float erp, softness;
         bool on = true;
-        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+        if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
+            // TwistLimit.Update (TwistLimit.cs:238-366).  Inputs: basis A primary / x / y
+            // (kJAXA, kJC1, kJC2), basis B primary / x (kJAXB, kJBX), kJTRIG.x the minimum
+            // angle and .y GetDistanceFromMinimum(maximum).  Lanes: kJL0 jacobianA +
+            // softness, kJL2 bias, -, velocityToImpulse; impulse kJACC1.y, error kJACC1.w.
+            const float4 trig = ji.L(kJTRIG, si);
+            const float minimumAngle = trig.x, distanceFromMaximum = trig.y;
+            const float3 pA = JTransform(JXYZ(axa), A.R), xA = JTransform(JXYZ(ji.L(kJC1, si)), A.R);
+            const float3 yA = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
+            const float3 pB = JTransform(JXYZ(axb), B.R), xB = JTransform(JXYZ(ji.L(kJBX, si)), B.R);
+            const float4 rotation = JQuatBetween(pB, pA);
+            const float3 twistMeasure = QTransform(xB.x, xB.y, xB.z, rotation);
+            const float y = JDot(twistMeasure, yA), x = JDot(twistMeasure, xA);
+            const float angle = (float)atan2((double)y, (double)x);
+            // GetDistanceFromMinimum (:341-357)
+            float distanceFromCurrent;
+            if (minimumAngle > 0)
+                distanceFromCurrent = angle >= minimumAngle ? angle - minimumAngle : 6.28318548f - minimumAngle + angle;
+            else
+                distanceFromCurrent = angle < minimumAngle ? 6.28318548f - minimumAngle + angle : angle - minimumAngle;
+            if (distanceFromCurrent < distanceFromMaximum) {
+                on = false;
+                acc1.y = 0.f;
+                acc1.w = 0.f;
+            } else {
+                float3 jv = make_float3(pA.x + pB.x, pA.y + pB.y, pA.z + pB.z);
+                if (JDot(jv, jv) < 1e-7f) {
+                    on = false;  // aligned axes: impulse and error stay
+                } else {
+                    jv = JNormalize(jv);
+                    const float3 nv = make_float3(-jv.x, -jv.y, -jv.z);
+                    const float3 jA = acc1.w > 0 ? nv : jv, jB = acc1.w > 0 ? jv : nv;
+                    const float errorFromMin = 6.28318548f - distanceFromCurrent;
+                    const float errorFromMax = distanceFromCurrent - distanceFromMaximum;
+                    const float error = errorFromMax > errorFromMin ? errorFromMin : -errorFromMax;
+                    acc1.w = error;
+                    JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+                    float bias = Minf(Maxf(0, fabsf(error) - margin) * erp, maxCorr);
+                    if (bounciness > 0) {
+                        float rel = A.s.wx * jA.x + A.s.wy * jA.y + A.s.wz * jA.z;
+                        const float dot = B.s.wx * jB.x + B.s.wy * jB.y + B.s.wz * jB.z;
+                        rel += dot;
+                        bias = Maxf(bias, JBounce(-rel, threshold, bounciness));
+                    }
+                    const float entryA = A.dynamic ? JDot(JTransform(jA, JInertia(A.s)), jA) : 0.f;
+                    const float entryB = B.dynamic ? JDot(JTransform(jB, JInertia(B.s)), jB) : 0.f;
+                    const float v2i = 1 / (softness + entryA + entryB);
+                    j.L(kJL0, s) = make_float4(jA.x, jA.y, jA.z, softness);
+                    j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
+                }
+            }
+        } else if (kAdded && IsLinearLimitType(type)) {
+            // LinearAxisLimit.Update (LinearAxisLimit.cs:338-447).  Inputs: anchors kJLA / kJLB,
+            // axis kJBP (A's frame), kJTRIG minimum, maximum, bounciness, bounce velocity
+            // threshold.  Lanes at
+            // LinearLimitLane: jLinearA + softness, jAngularA + bias, jAngularB + mass;
+            // impulse kJACC1.z; state bit kJMinActive when violated below the minimum.
+            const float4 trig = ji.L(kJTRIG, si);
+            const float limitBounciness = trig.z, limitThreshold = trig.w;
+            const float3 offA = JTransform(JXYZ(la), A.R), offB = JTransform(JXYZ(lb), B.R);
+            const float3 anchorA = make_float3(offA.x + A.pos.x, offA.y + A.pos.y, offA.z + A.pos.z);
+            const float3 anchorB = make_float3(offB.x + B.pos.x, offB.y + B.pos.y, offB.z + B.pos.z);
+            const float3 rA = make_float3(anchorB.x - A.pos.x, anchorB.y - A.pos.y, anchorB.z - A.pos.z);
+            const float3 axis = JTransform(JXYZ(ji.L(kJBP, si)), A.R);
+            const float3 sep = make_float3(anchorB.x - anchorA.x, anchorB.y - anchorA.y, anchorB.z - anchorA.z);
+            float u = JDot(sep, axis);
+            if (u < trig.x) {
+                u = trig.x - u;
+            } else if (u > trig.y) {
+                u = trig.y - u;
+            } else {
+                on = false;
+                acc1.z = 0.f;
+            }
+            if (on) {
+                u = -u;
+                const float error = u > 0 ? Maxf(0, u - margin) : Minf(0, u + margin);  // u is never 0 here
+                const float3 jlb = make_float3(-axis.x, -axis.y, -axis.z);
+                const float3 jaa = JCross(rA, axis), jab = JCross(offB, jlb);
+                JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+                float bias = Clampf(erp * error, -maxCorr, maxCorr);
+                if (limitBounciness > 0) {
+                    float rel = axis.x * A.s.vx + axis.y * A.s.vy + axis.z * A.s.vz;
+                    float dot = jaa.x * A.s.wx + jaa.y * A.s.wy + jaa.z * A.s.wz;
+                    rel += dot;
+                    dot = jlb.x * B.s.vx + jlb.y * B.s.vy + jlb.z * B.s.vz;
+                    rel += dot;
+                    dot = jab.x * B.s.wx + jab.y * B.s.wy + jab.z * B.s.wz;
+                    rel += dot;
+                    if (u > 0 && -rel > limitThreshold)
+                        bias = Maxf(bias, JBounce(-rel, limitThreshold, limitBounciness));
+                    else if (u < 0 && rel > limitThreshold)
+                        bias = Minf(bias, -JBounce(rel, limitThreshold, limitBounciness));
+                }
+                float entryA = 0, entryB = 0;
+                if (A.dynamic) {
+                    entryA = JDot(JTransform(jaa, JInertia(A.s)), jaa);
+                    entryA += A.s.invMass;
+                }
+                if (B.dynamic) {
+                    entryB = JDot(JTransform(jab, JInertia(B.s)), jab);
+                    entryB += B.s.invMass;
+                }
+                const float mass = 1 / (entryA + entryB + softness);
+                const int k0 = LinearLimitLane(type);
+                j.L(k0, s) = make_float4(axis.x, axis.y, axis.z, softness);
+                j.L(k0 + 1, s) = make_float4(jaa.x, jaa.y, jaa.z, bias);
+                j.L(k0 + 2, s) = make_float4(jab.x, jab.y, jab.z, mass);
+                if (u < 0) st |= kJMinActive;
+            }
+        } else if (type == BEPUGPU_JOINT_SWING_LIMIT) {
             // SwingLimit.Update (SwingLimit.cs:249-331)
             float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
             float dot = JDot(wA, wB);
@@ -906,7 +1031,25 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+        if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
+            // TwistLimit.ExclusiveUpdate (TwistLimit.cs:368-383)
+            const float a = acc1.y;
+            if (dynA) ApplyAngular(A, l0.x * a, l0.y * a, l0.z * a);
+            if (dynB) ApplyAngular(B, -l0.x * a, -l0.y * a, -l0.z * a);
+        } else if (kAdded && IsLinearLimitType(type)) {
+            // LinearAxisLimit.ExclusiveUpdate (LinearAxisLimit.cs:449-466)
+            const int k0 = LinearLimitLane(type);
+            const float4 ja = j.L(k0, s), jaa = j.L(k0 + 1, s), jab = j.L(k0 + 2, s);
+            const float a = acc1.z;
+            if (dynA) {
+                ApplyLinear(A, ja.x * a, ja.y * a, ja.z * a);
+                ApplyAngular(A, jaa.x * a, jaa.y * a, jaa.z * a);
+            }
+            if (dynB) {
+                ApplyLinear(B, -ja.x * a, -ja.y * a, -ja.z * a);
+                ApplyAngular(B, jab.x * a, jab.y * a, jab.z * a);
+            }
+        } else if (type == BEPUGPU_JOINT_SWING_LIMIT) {
             // SwingLimit.ExclusiveUpdate (SwingLimit.cs:333-347)
             float ix = l0.x * acc1.y, iy = l0.y * acc1.y, iz = l0.z * acc1.y;
             if (dynA) ApplyAngular(A, ix, iy, iz);
@@ -1112,10 +1255,49 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         if (dynB) ApplyAngular(B, -ix, -iy, -iz);
         account(1, fabsf(tx) + fabsf(ty));
     }
-    if (st & (4u << kChildShift)) {
+    if (kAdded && (st & (4u << kChildShift)) && IsLinearLimitType(type)) {
+        // LinearAxisLimit.SolveIteration (LinearAxisLimit.cs:290-336)
+        const int k0 = LinearLimitLane(type);
+        const float4 ja = j.L(k0, s), jaa = j.L(k0 + 1, s), jab = j.L(k0 + 2, s);
+        const float bx = -ja.x, by = -ja.y, bz = -ja.z;  // jLinearB
+        float lambda = ja.x * A.vx + ja.y * A.vy + ja.z * A.vz;
+        float dot = jaa.x * A.wx + jaa.y * A.wy + jaa.z * A.wz;
+        lambda += dot;
+        dot = bx * B.vx + by * B.vy + bz * B.vz;
+        lambda += dot;
+        dot = jab.x * B.wx + jab.y * B.wy + jab.z * B.wz;
+        lambda += dot;
+        lambda = -lambda + jaa.w - ja.w * acc1.z;
+        lambda *= jab.w;
+        const float previous = acc1.z;
+        acc1.z = (st & kJMinActive) ? Minf(acc1.z + lambda, 0) : Maxf(acc1.z + lambda, 0);
+        lambda = acc1.z - previous;
+        if (dynA) {
+            ApplyLinear(A, ja.x * lambda, ja.y * lambda, ja.z * lambda);
+            ApplyAngular(A, jaa.x * lambda, jaa.y * lambda, jaa.z * lambda);
+        }
+        if (dynB) {
+            ApplyLinear(B, bx * lambda, by * lambda, bz * lambda);
+            ApplyAngular(B, jab.x * lambda, jab.y * lambda, jab.z * lambda);
+        }
+        account(2, fabsf(lambda));
+    } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (type == BEPUGPU_JOINT_SWING_LIMIT) {
+        if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
+            // TwistLimit.SolveIteration (TwistLimit.cs:200-236)
+            const float nx = -l0.x, ny = -l0.y, nz = -l0.z;  // jacobianB
+            const float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;
+            const float velocityB = B.wx * nx + B.wy * ny + B.wz * nz;
+            float lambda = -(velocityA + velocityB) + l2.x - softness * acc1.y;
+            lambda *= l2.z;
+            const float previous = acc1.y;
+            acc1.y = Maxf(acc1.y + lambda, 0);
+            lambda = acc1.y - previous;
+            if (dynA) ApplyAngular(A, l0.x * lambda, l0.y * lambda, l0.z * lambda);
+            if (dynB) ApplyAngular(B, nx * lambda, ny * lambda, nz * lambda);
+            account(2, fabsf(lambda));
+        } else if (type == BEPUGPU_JOINT_SWING_LIMIT) {
             // SwingLimit.SolveIteration (SwingLimit.cs:211-243)
             float rx = A.wx - B.wx, ry = A.wy - B.wy, rz = A.wz - B.wz;
             float lambda = rx * l0.x + ry * l0.y + rz * l0.z;

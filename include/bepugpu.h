@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 4
+#define BEPUGPU_ABI_VERSION 5
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -150,14 +150,18 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_POINT_ON_LINE = 12,   /* PointOnLineJoint.cs:247-463 */
     BEPUGPU_JOINT_PRISMATIC = 13,       /* PrismaticJoint group: point on line + no rotation */
     BEPUGPU_JOINT_LINE_SLIDER = 14,     /* LineSliderJoint group: point on line + revolute angular */
-    BEPUGPU_JOINT_UNIVERSAL = 15        /* UniversalJoint group: ball socket + twist */
+    BEPUGPU_JOINT_UNIVERSAL = 15,       /* UniversalJoint group: ball socket + twist */
+    BEPUGPU_JOINT_TWIST_LIMIT = 16,     /* TwistLimit.cs:200-383 */
+    BEPUGPU_JOINT_LINEAR_AXIS_LIMIT = 17 /* LinearAxisLimit.cs:290-466 */
 } bepugpu_joint_type;
-/* The groups' limit and motor children are inactive, as their constructors
- * leave them (PrismaticJoint.cs:57-58, LineSliderJoint.cs:53-54,
- * UniversalJoint.cs:52-53); active ones are not carried. */
+/* The groups' motor children are inactive, as their constructors leave them
+ * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
+ * is UniversalJoint's twist limit (:52).  The limits of REVOLUTE, PRISMATIC and
+ * LINE_SLIDER records (a LinearAxisLimit on the line's anchors and direction
+ * for the last two) follow BEPUGPU_JOINT_LIMIT_ACTIVE. */
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
-#define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE: RevoluteJoint.Limit.IsActive */
+#define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE, PRISMATIC, LINE_SLIDER: the group's Limit.IsActive */
 
 /* Joint record: the state each reference object keeps between steps.  Body -1
  * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic
@@ -165,20 +169,28 @@ typedef enum bepugpu_joint_type {
  *   anchor_a/b        BallSocketJoint.localAnchorA/B (BALL_SOCKET, REVOLUTE, WELD),
  *                     DistanceJoint / DistanceLimit.localAnchorA/B (DISTANCE, DISTANCE_LIMIT),
  *                     PointOnPlaneJoint.localPlaneAnchor / localPointAnchor (POINT_ON_PLANE),
- *                     PointOnLineJoint.localAxisAnchor / localPoint (POINT_ON_LINE, PRISMATIC, LINE_SLIDER)
+ *                     PointOnLineJoint.localAxisAnchor / localPoint (POINT_ON_LINE, PRISMATIC, LINE_SLIDER),
+ *                     LinearAxisLimit.localAnchorA/B (LINEAR_AXIS_LIMIT; the groups' limits take the line's)
  *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
  *                     SwingLimit.localAxisA/B (SWING_LIMIT), TwistJoint.localAxisA/B (TWIST),
- *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE)
+ *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE),
+ *                     TwistLimit basis A / basis B local primary axes (TWIST_LIMIT)
  *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame;
- *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST)
+ *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST, UNIVERSAL);
+ *                     TwistLimit basis A local x / y axes (TWIST_LIMIT)
  *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame;
- *                     basis_x: TwistJoint.bLocalAxisY (TWIST, UNIVERSAL);
+ *                     basis_x: TwistJoint.bLocalAxisY (TWIST, UNIVERSAL), TwistLimit basis B
+ *                     local x axis (TWIST_LIMIT); basis_primary: LinearAxisLimit.localAxis
+ *                     (LINEAR_AXIS_LIMIT);
  *                     PointOnLineJoint: basis_primary localLineDirection, basis_x / test_axis
  *                     localRestrictedAxis1 / 2 (POINT_ON_LINE, PRISMATIC, LINE_SLIDER)
  *   test_axis         RevoluteLimit.localTestAxis, in B's frame
  *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine;
- *                     DistanceJoint.Distance; DistanceLimit.MinimumLength
- *   limit_max         RevoluteLimit.maximumAngle; DistanceLimit.MaximumLength
+ *                     DistanceJoint.Distance; DistanceLimit.MinimumLength;
+ *                     TwistLimit.MinimumAngle (the setter's wrap applied at upload);
+ *                     LinearAxisLimit.Minimum (LINEAR_AXIS_LIMIT, PRISMATIC, LINE_SLIDER)
+ *   limit_max         RevoluteLimit.maximumAngle; DistanceLimit.MaximumLength;
+ *                     TwistLimit.MaximumAngle; LinearAxisLimit.Maximum
  *   orientation_a/b   NoRotationJoint.InitialOrientationA/B (NO_ROTATION, WELD), quaternions x y z w
  *   margin, bounciness, bounce_velocity_threshold   JointLimit fields (0.005, 0, 1)
  *   max_corrective_velocity   Joint.MaxCorrectiveVelocity (FLT_MAX = unlimited)
@@ -189,9 +201,11 @@ typedef enum bepugpu_joint_type {
  *                     REVOLUTE [0..2] ball socket, [3..4] angular, [5..6] limit;
  *                     NO_ROTATION [0..2]; WELD [0..2] ball socket, [3..5] no rotation;
  *                     DISTANCE [0]; DISTANCE_LIMIT [0]; POINT_ON_PLANE [0]; TWIST [0];
- *                     POINT_ON_LINE [0..1]; PRISMATIC [0..1] point on line, [2..4] no rotation;
- *                     LINE_SLIDER [0..1] point on line, [2..3] angular; UNIVERSAL [0..2] ball
- *                     socket, [3] twist.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
+ *                     POINT_ON_LINE [0..1]; PRISMATIC [0..1] point on line, [2..4] no rotation,
+ *                     [5] limit; LINE_SLIDER [0..1] point on line, [2..3] angular, [4] limit;
+ *                     UNIVERSAL [0..2] ball socket, [3] twist; TWIST_LIMIT [0], and [1] the
+ *                     error its last Update left (the sign of the next jacobian follows it,
+ *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0].  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
  *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */

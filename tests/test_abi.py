@@ -37,7 +37,7 @@ def test_binding_covers_header():
 
 def test_record_sizes():
     lib = N.load_gpu_library()
-    assert lib.bepugpu_abi_version() == 4
+    assert lib.bepugpu_abi_version() == 5
     assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 108
     assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 64
     assert lib.bepugpu_record_size(3) == N.MANIFOLD_DTYPE.itemsize

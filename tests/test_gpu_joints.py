@@ -175,7 +175,8 @@ def test_chains_in_island_groups(gpu_context, policy):
 
 
 NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
-             N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL)
+             N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL,
+             N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT)
 
 
 def _unit(v):
@@ -236,6 +237,29 @@ def _convert(b, j, types, seed):
                 c1, c2 = _perpendicular_pair(wd)
                 j["axis_a"][k], j["axis_b"][k] = d, wd @ rb.T
                 j["constrained_1"][k], j["constrained_2"][k] = c1 @ ra.T, c2 @ ra.T
+        if t in (N.JOINT_LINEAR_AXIS_LIMIT, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER):
+            # limits around the anchors' separation along the axis (zero for chain links)
+            if t == N.JOINT_LINEAR_AXIS_LIMIT:
+                j["basis_primary"][k] = _unit(rng.normal(size=3))
+            lo = rng.uniform(-0.03, 0.005)
+            j["limit_min"][k], j["limit_max"][k] = lo, lo + rng.uniform(0.0, 0.03)
+            j["bounciness"][k] = rng.choice([0.0, 0.5])
+            if t != N.JOINT_LINEAR_AXIS_LIMIT and rng.random() < 0.6:
+                j["flags"][k] |= N.JOINT_LIMIT_ACTIVE
+        if t == N.JOINT_TWIST_LIMIT:
+            # TwistLimit.SetupJointTransforms (TwistLimit.cs:165-197) for a shared world axis
+            ax = _unit(rng.normal(size=3))
+            ra, rb = _rows(qa), _rows(qb)
+            x = np.cross(ax, (0, 1, 0))
+            if x @ x < 1e-7:
+                x = np.cross(ax, (1, 0, 0))
+            x = _unit(x)
+            y = _unit(np.cross(ax, x))
+            j["axis_a"][k], j["constrained_1"][k], j["constrained_2"][k] = ax @ ra.T, x @ ra.T, y @ ra.T
+            j["axis_b"][k], j["basis_x"][k] = ax @ rb.T, x @ rb.T
+            lo = rng.uniform(-0.3, 0.02)
+            j["limit_min"][k], j["limit_max"][k] = lo, lo + rng.uniform(0.0, 0.3)
+            j["bounciness"][k] = rng.choice([0.0, 0.5])
         if t in (N.JOINT_TWIST, N.JOINT_UNIVERSAL):
             # TwistJoint.Initialize (TwistJoint.cs:340-365) for a shared world axis
             ax = rng.normal(size=3)
@@ -275,6 +299,12 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
         p.step()
         errs, exact = p.compare()
         assert exact, (jtype, step, errs)
+    limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_PRISMATIC: 5,
+                   N.JOINT_LINE_SLIDER: 4}
+    if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
+        e = limit_entry[jtype]
+        got = p.oracle.get_constraints()[1]["impulse"][:, e]
+        assert np.count_nonzero((got != j["impulse"][:, e]) & (got != 0)) > 0
     p.close()
 
 

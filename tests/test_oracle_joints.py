@@ -264,3 +264,107 @@ def test_point_on_line_to_world_closed_form():
     y = erp * 0.1 / (1.0 + soft)
     np.testing.assert_allclose(oj["impulse"][0, :2], (0, y), rtol=1e-4, atol=1e-9)
     np.testing.assert_allclose(ob["linear_velocity"][0], (0, -y, 0), rtol=1e-4, atol=1e-9)
+
+
+def _twist_limit_z(phi, lo, hi, error=0.0):
+    """B turned by phi about the world z axis, a twist limit about z to the world."""
+    b = _body((0, 0, 0), quat=_rot_z(phi))
+    j = _joint(N.JOINT_TWIST_LIMIT, -1, 0)
+    j["axis_a"] = j["axis_b"] = (0, 0, 1)   # basis primaries
+    j["constrained_1"] = (1, 0, 0)           # basis A x
+    j["constrained_2"] = (0, 1, 0)           # basis A y
+    j["basis_x"] = (1, 0, 0)                 # basis B x
+    j["limit_min"], j["limit_max"] = lo, hi
+    j["impulse"][0, 1] = error
+    return b, j
+
+
+@pytest.mark.parametrize("phi", [0.1, -0.15])
+def test_twist_limit_inside_clears_impulse_and_error(phi):
+    """TwistLimit (TwistLimit.cs:238-260): an angle inside [min, max] turns the
+    limit off and zeroes its impulse and its error."""
+    b, j = _twist_limit_z(phi, -0.2, 0.2, error=0.3)
+    j["impulse"][0, 0] = 0.4
+    ob, oj = _step(b, j)
+    assert oj["impulse"][0, 0] == 0 and oj["impulse"][0, 1] == 0
+    assert np.all(ob["angular_velocity"][0] == 0)
+
+
+def test_twist_limit_beyond_maximum_closed_form():
+    """Past the maximum by 0.3 rad: error -0.3 (TwistLimit.cs:334-339), the
+    jacobian A = z (the previous error was 0), B pushed back about -z."""
+    b, j = _twist_limit_z(0.5, -0.2, 0.2)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = (0.3 - 0.005) * erp / (soft + 4.0)  # I_zz = 4, jacobianB = -z
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(oj["impulse"][0, 1], -0.3, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def test_twist_limit_jacobian_follows_previous_error():
+    """Past the minimum the error is positive (+0.3), but the jacobian of that
+    step still follows the previous error (0): B is pushed further about -z.
+    With the error +0.3 kept, the next step's jacobian flips and B is pushed
+    back about +z (TwistLimit.cs:284-312)."""
+    erp, soft = _spring(float(DT))
+    lam = (0.3 - 0.005) * erp / (soft + 4.0)
+    b, j = _twist_limit_z(-0.5, -0.2, 0.2, error=0.0)
+    ob, oj = _step(b, j)
+    np.testing.assert_allclose(oj["impulse"][0, 1], 0.3, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+    b, j = _twist_limit_z(-0.5, -0.2, 0.2, error=0.3)
+    ob, oj = _step(b, j)
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, 4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def test_twist_limit_angle_setters_wrap_the_minimum():
+    """MinimumAngle wraps into (-pi, pi]; MaximumAngle is only reduced modulo
+    2 pi (TwistLimit.cs:50-75): a minimum of 2 pi - 0.2 acts as -0.2."""
+    b, j = _twist_limit_z(0.5, 2 * np.pi - 0.2, 0.2)
+    ob, oj = _step(b, j)
+    b2, j2 = _twist_limit_z(0.5, -0.2, 0.2)
+    ob2, oj2 = _step(b2, j2)
+    np.testing.assert_allclose(oj["impulse"][0, :2], oj2["impulse"][0, :2], rtol=1e-5)
+
+
+@pytest.mark.parametrize("x,side", [(0.5, 0), (1.5, 1), (-0.4, -1)])
+def test_linear_axis_limit_closed_form(x, side):
+    """LinearAxisLimit (LinearAxisLimit.cs:290-447): B's centre at x along the
+    world's x axis with limits [0, 1].  Inside nothing acts and a stale impulse
+    is cleared; above the maximum the impulse is non-negative, below the
+    minimum non-positive, and B is pushed back either way."""
+    b = _body((x, 0, 0))
+    j = _joint(N.JOINT_LINEAR_AXIS_LIMIT, -1, 0)
+    j["basis_primary"] = (1, 0, 0)
+    j["limit_min"], j["limit_max"] = 0.0, 1.0
+    j["impulse"][0, 0] = 0.2 if side == 0 else 0.0
+    ob, oj = _step(b, j)
+    if side == 0:
+        assert oj["impulse"][0, 0] == 0 and np.all(ob["linear_velocity"][0] == 0)
+        return
+    erp, soft = _spring(float(DT))
+    over = x - 1.0 if side > 0 else -x
+    lam = side * (over - 0.005) * erp / (1.0 + soft)  # unadjustedError > 0 above the maximum
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (-lam, 0, 0), rtol=1e-4, atol=1e-9)
+    assert np.sign(ob["linear_velocity"][0, 0]) == -side
+
+
+def test_prismatic_limit_follows_the_flag():
+    """PrismaticJoint's LinearAxisLimit (PrismaticJoint.cs:53-60) acts only when
+    the record's LIMIT_ACTIVE flag is set; its impulse is record entry 5."""
+    b = _body((1.5, 0, 0))
+    j = _joint(N.JOINT_PRISMATIC, -1, 0)
+    j["basis_primary"] = (1, 0, 0)
+    j["basis_x"], j["test_axis"] = (0, 0, -1), (0, 1, 0)
+    j["orientation_a"] = j["orientation_b"] = (0, 0, 0, 1)
+    j["limit_min"], j["limit_max"] = 0.0, 1.0
+    _, off = _step(b, j)
+    assert off["impulse"][0, 5] == 0
+    j["flags"] |= N.JOINT_LIMIT_ACTIVE
+    ob, on = _step(b, j)
+    erp, soft = _spring(float(DT))
+    np.testing.assert_allclose(on["impulse"][0, 5], (0.5 - 0.005) * erp / (1.0 + soft), rtol=1e-4)
+    assert ob["linear_velocity"][0, 0] < 0
