@@ -55,7 +55,8 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_LINE_SLIDER: return kJChildBall | kJChildAngular | kJChildLimit;
         case BEPUGPU_JOINT_UNIVERSAL: return kJChildBall | kJChildAngular;
         case BEPUGPU_JOINT_TWIST_LIMIT:
-        case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT: return kJChildLimit;
+        case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
+        case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT: return kJChildLimit;
         default: return 0;
     }
 }
@@ -161,6 +162,11 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             at(kJBX, slot) = F4(r.basis_x, 0.f);
             at(kJTRIG, slot) = make_float4(minimumAngle, DistanceFromMinimum(minimumAngle, maximumAngle), 0.f, 0.f);
         }
+        if (r.type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
+            // MaximumAngleX / Y setters (EllipseSwingLimit.cs:57-68): MathHelper.Clamp to [BigEpsilon, Pi]
+            auto clamp = [](float v) { return v < 1e-5f ? 1e-5f : (v > kHostPi ? kHostPi : v); };
+            at(kJTRIG, slot) = make_float4(clamp(r.limit_min), clamp(r.limit_max), 0.f, 0.f);
+        }
         if (r.type == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || r.type == BEPUGPU_JOINT_PRISMATIC ||
             r.type == BEPUGPU_JOINT_LINE_SLIDER)
             // a prismatic joint's kJC1 / kJC2 hold orientations: the limit's bounce settings go here
@@ -208,6 +214,9 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_TWIST_LIMIT:
                 lim[0] = r.impulse[0];
                 last = r.impulse[1];
+                break;
+            case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT:
+                lim[0] = r.impulse[0];
                 break;
             case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
                 lim[1] = r.impulse[0];
@@ -304,6 +313,9 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
                 r.impulse[0] = a1.z;
+                break;
+            case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT:
+                r.impulse[0] = a1.y;
                 break;
             case BEPUGPU_JOINT_UNIVERSAL:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;

@@ -20,6 +20,7 @@
 //   PointOnLineJoint      TwoEntity/Joints/PointOnLineJoint.cs:247-463 (the first child slot)
 //   TwistLimit            TwoEntity/JointLimits/TwistLimit.cs:200-383 (the limit slot; its
 //                         last error, which picks the next jacobian's sign, in kJACC1.w)
+//   EllipseSwingLimit     TwoEntity/JointLimits/EllipseSwingLimit.cs:162-357 (the limit slot)
 //   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
 //                         also the limit child of PRISMATIC and LINE_SLIDER records)
 // and the groups PrismaticJoint (point on line + no rotation), LineSliderJoint
@@ -754,6 +755,48 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                     j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
                 }
             }
+        } else if (kAdded && type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
+            // EllipseSwingLimit.Update (EllipseSwingLimit.cs:162-308).  Inputs: basis primary /
+            // x / y (kJAXA, kJC1, kJC2, A's frame), B's twist axis (kJAXB), kJTRIG.x / .y the
+            // maximum angles.  Lanes: kJL0 jacobianA + softness, kJL2 bias, -,
+            // velocityToImpulse; impulse (non-positive) kJACC1.y.
+            const float4 trig = ji.L(kJTRIG, si);
+            const float3 primary = JTransform(JXYZ(axa), A.R), xAxis = JTransform(JXYZ(ji.L(kJC1, si)), A.R);
+            const float3 yAxis = JTransform(JXYZ(ji.L(kJC2, si)), A.R), twistB = JTransform(JXYZ(axb), B.R);
+            const float4 rel = JQuatBetween(twistB, primary);
+            float3 axis;
+            float angle;
+            JAxisAngle(rel, axis, angle);
+            const float3 axisAngle = make_float3(axis.x * angle, axis.y * angle, axis.z * angle);
+            const float angleX = JDot(axisAngle, xAxis), angleY = JDot(axisAngle, yAxis);
+            const float maxX2 = trig.x * trig.x, maxY2 = trig.y * trig.y;
+            float error = angleX * angleX * maxY2 + angleY * angleY * maxX2 - maxX2 * maxY2;
+            if (error < 0) {
+                on = false;
+                acc1.y = 0.f;
+            } else {
+                const float tangentX = 2 * angleX / maxX2, tangentY = 2 * angleY / maxY2;
+                const float4 conj = make_float4(-rel.x, -rel.y, -rel.z, rel.w);
+                const float3 stX = QTransform(xAxis.x, xAxis.y, xAxis.z, conj);
+                const float3 stY = QTransform(yAxis.x, yAxis.y, yAxis.z, conj);
+                const float3 jA = make_float3(stX.x * tangentX + stY.x * tangentY, stX.y * tangentX + stY.y * tangentY,
+                                              stX.z * tangentX + stY.z * tangentY);
+                const float3 jB = make_float3(-jA.x, -jA.y, -jA.z);
+                JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+                error = error - margin;
+                float bias = Minf(Maxf(error, 0) * erp, maxCorr);
+                if (bounciness > 0) {
+                    float rv = A.s.wx * jA.x + A.s.wy * jA.y + A.s.wz * jA.z;
+                    const float dot = B.s.wx * jB.x + B.s.wy * jB.y + B.s.wz * jB.z;
+                    rv += dot;
+                    bias = Maxf(bias, JBounce(rv, threshold, bounciness));
+                }
+                const float entryA = A.dynamic ? JDot(JTransform(jA, JInertia(A.s)), jA) : 0.f;
+                const float entryB = B.dynamic ? JDot(JTransform(jB, JInertia(B.s)), jB) : 0.f;
+                const float v2i = 1 / (softness + entryA + entryB);
+                j.L(kJL0, s) = make_float4(jA.x, jA.y, jA.z, softness);
+                j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
+            }
         } else if (kAdded && IsLinearLimitType(type)) {
             // LinearAxisLimit.Update (LinearAxisLimit.cs:338-447).  Inputs: anchors kJLA / kJLB,
             // axis kJBP (A's frame), kJTRIG minimum, maximum, bounciness, bounce velocity
@@ -1031,8 +1074,8 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
-            // TwistLimit.ExclusiveUpdate (TwistLimit.cs:368-383)
+        if (kAdded && (type == BEPUGPU_JOINT_TWIST_LIMIT || type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT)) {
+            // TwistLimit.ExclusiveUpdate (TwistLimit.cs:368-383), EllipseSwingLimit's (:310-325)
             const float a = acc1.y;
             if (dynA) ApplyAngular(A, l0.x * a, l0.y * a, l0.z * a);
             if (dynB) ApplyAngular(B, -l0.x * a, -l0.y * a, -l0.z * a);
@@ -1284,7 +1327,20 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
+        if (kAdded && type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
+            // EllipseSwingLimit.SolveIteration (EllipseSwingLimit.cs:327-357)
+            const float nx = -l0.x, ny = -l0.y, nz = -l0.z;  // jacobianB
+            const float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;
+            const float velocityB = B.wx * nx + B.wy * ny + B.wz * nz;
+            float lambda = (-velocityA - velocityB) - l2.x - softness * acc1.y;
+            lambda *= l2.z;
+            const float previous = acc1.y;
+            acc1.y = Minf(acc1.y + lambda, 0);
+            lambda = acc1.y - previous;
+            if (dynA) ApplyAngular(A, l0.x * lambda, l0.y * lambda, l0.z * lambda);
+            if (dynB) ApplyAngular(B, nx * lambda, ny * lambda, nz * lambda);
+            account(2, fabsf(lambda));
+        } else if (kAdded && type == BEPUGPU_JOINT_TWIST_LIMIT) {
             // TwistLimit.SolveIteration (TwistLimit.cs:200-236)
             const float nx = -l0.x, ny = -l0.y, nz = -l0.z;  // jacobianB
             const float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;

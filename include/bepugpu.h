@@ -152,7 +152,8 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_LINE_SLIDER = 14,     /* LineSliderJoint group: point on line + revolute angular */
     BEPUGPU_JOINT_UNIVERSAL = 15,       /* UniversalJoint group: ball socket + twist */
     BEPUGPU_JOINT_TWIST_LIMIT = 16,     /* TwistLimit.cs:200-383 */
-    BEPUGPU_JOINT_LINEAR_AXIS_LIMIT = 17 /* LinearAxisLimit.cs:290-466 */
+    BEPUGPU_JOINT_LINEAR_AXIS_LIMIT = 17, /* LinearAxisLimit.cs:290-466 */
+    BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT = 18 /* EllipseSwingLimit.cs:162-357 */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
@@ -174,10 +175,12 @@ typedef enum bepugpu_joint_type {
  *   axis_a/b          RevoluteAngularJoint.localAxisA/B (REVOLUTE_ANGULAR, REVOLUTE),
  *                     SwingLimit.localAxisA/B (SWING_LIMIT), TwistJoint.localAxisA/B (TWIST),
  *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE),
- *                     TwistLimit basis A / basis B local primary axes (TWIST_LIMIT)
+ *                     TwistLimit basis A / basis B local primary axes (TWIST_LIMIT),
+ *                     EllipseSwingLimit basis primary / localTwistAxisB (ELLIPSE_SWING_LIMIT)
  *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame;
  *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST, UNIVERSAL);
- *                     TwistLimit basis A local x / y axes (TWIST_LIMIT)
+ *                     TwistLimit basis A local x / y axes (TWIST_LIMIT), EllipseSwingLimit
+ *                     basis x / y axes (ELLIPSE_SWING_LIMIT)
  *   basis_primary/x   RevoluteLimit.Basis localPrimaryAxis / localXAxis, in A's frame;
  *                     basis_x: TwistJoint.bLocalAxisY (TWIST, UNIVERSAL), TwistLimit basis B
  *                     local x axis (TWIST_LIMIT); basis_primary: LinearAxisLimit.localAxis
@@ -188,9 +191,11 @@ typedef enum bepugpu_joint_type {
  *   limit_min         RevoluteLimit.minimumAngle; SwingLimit.minimumCosine;
  *                     DistanceJoint.Distance; DistanceLimit.MinimumLength;
  *                     TwistLimit.MinimumAngle (the setter's wrap applied at upload);
- *                     LinearAxisLimit.Minimum (LINEAR_AXIS_LIMIT, PRISMATIC, LINE_SLIDER)
+ *                     LinearAxisLimit.Minimum (LINEAR_AXIS_LIMIT, PRISMATIC, LINE_SLIDER);
+ *                     EllipseSwingLimit.MaximumAngleX (its setter's clamp applied at upload)
  *   limit_max         RevoluteLimit.maximumAngle; DistanceLimit.MaximumLength;
- *                     TwistLimit.MaximumAngle; LinearAxisLimit.Maximum
+ *                     TwistLimit.MaximumAngle; LinearAxisLimit.Maximum;
+ *                     EllipseSwingLimit.MaximumAngleY
  *   orientation_a/b   NoRotationJoint.InitialOrientationA/B (NO_ROTATION, WELD), quaternions x y z w
  *   margin, bounciness, bounce_velocity_threshold   JointLimit fields (0.005, 0, 1)
  *   max_corrective_velocity   Joint.MaxCorrectiveVelocity (FLT_MAX = unlimited)
@@ -205,7 +210,7 @@ typedef enum bepugpu_joint_type {
  *                     [5] limit; LINE_SLIDER [0..1] point on line, [2..3] angular, [4] limit;
  *                     UNIVERSAL [0..2] ball socket, [3] twist; TWIST_LIMIT [0], and [1] the
  *                     error its last Update left (the sign of the next jacobian follows it,
- *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0].  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
+ *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0]; ELLIPSE_SWING_LIMIT [0].  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
  *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */

@@ -176,7 +176,7 @@ def test_chains_in_island_groups(gpu_context, policy):
 
 NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
              N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL,
-             N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT)
+             N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT, N.JOINT_ELLIPSE_SWING_LIMIT)
 
 
 def _unit(v):
@@ -260,6 +260,21 @@ def _convert(b, j, types, seed):
             lo = rng.uniform(-0.3, 0.02)
             j["limit_min"][k], j["limit_max"][k] = lo, lo + rng.uniform(0.0, 0.3)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        if t == N.JOINT_ELLIPSE_SWING_LIMIT:
+            # EllipseSwingLimit.SetupJointTransforms (EllipseSwingLimit.cs:138-160)
+            ax = _unit(rng.normal(size=3))
+            ra, rb = _rows(qa), _rows(qb)
+            x = np.cross(ax, (0, 1, 0))
+            if x @ x < 1e-7:
+                x = np.cross(ax, (1, 0, 0))
+            y = np.cross(ax, x)
+            j["axis_a"][k], j["constrained_1"][k], j["constrained_2"][k] = ax @ ra.T, _unit(x) @ ra.T, _unit(y) @ ra.T
+            # B's twist axis tilted off A's primary by up to 0.3 rad: some limits start violated
+            tilt = _unit(np.cross(ax, rng.normal(size=3)))
+            ang = rng.uniform(0.0, 0.3)
+            j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
+            j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
+            j["bounciness"][k] = rng.choice([0.0, 0.5])
         if t in (N.JOINT_TWIST, N.JOINT_UNIVERSAL):
             # TwistJoint.Initialize (TwistJoint.cs:340-365) for a shared world axis
             ax = rng.normal(size=3)
@@ -299,8 +314,8 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
         p.step()
         errs, exact = p.compare()
         assert exact, (jtype, step, errs)
-    limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_PRISMATIC: 5,
-                   N.JOINT_LINE_SLIDER: 4}
+    limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_ELLIPSE_SWING_LIMIT: 0,
+                   N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
         got = p.oracle.get_constraints()[1]["impulse"][:, e]

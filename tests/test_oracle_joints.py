@@ -368,3 +368,47 @@ def test_prismatic_limit_follows_the_flag():
     erp, soft = _spring(float(DT))
     np.testing.assert_allclose(on["impulse"][0, 5], (0.5 - 0.005) * erp / (1.0 + soft), rtol=1e-4)
     assert ob["linear_velocity"][0, 0] < 0
+
+
+def _ellipse_swing_x(theta, max_x=0.3, max_y=0.5):
+    """B turned by theta about the world x axis; its twist axis is its local z.
+    A is the world, with the basis z (primary), x, y."""
+    b = _body((0, 0, 0), quat=(np.sin(theta / 2), 0, 0, np.cos(theta / 2)))
+    j = _joint(N.JOINT_ELLIPSE_SWING_LIMIT, -1, 0)
+    j["axis_a"], j["constrained_1"], j["constrained_2"] = (0, 0, 1), (1, 0, 0), (0, 1, 0)
+    j["axis_b"] = (0, 0, 1)
+    j["limit_min"], j["limit_max"] = max_x, max_y
+    return b, j
+
+
+def test_ellipse_swing_limit_inside_is_off():
+    b, j = _ellipse_swing_x(0.2)
+    j["impulse"][0, 0] = -0.3
+    ob, oj = _step(b, j)
+    assert oj["impulse"][0, 0] == 0 and np.all(ob["angular_velocity"][0] == 0)
+
+
+def test_ellipse_swing_limit_closed_form():
+    """EllipseSwingLimit (EllipseSwingLimit.cs:162-357): swung 0.4 rad about x
+    against a 0.3 rad x-semi-axis: error maxY^2 (theta^2 - maxX^2), jacobian
+    A = (2 angleX / maxX^2) x with angleX = -theta, a non-positive impulse
+    that turns B back about -x."""
+    theta, mx, my = 0.4, 0.3, 0.5
+    b, j = _ellipse_swing_x(theta, mx, my)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    error = my * my * (theta * theta - mx * mx) - 0.005
+    t = 2 * theta / (mx * mx)  # |jacobian|
+    lam = -(error * erp) / (soft + 2.0 * t * t)  # I_xx = 2
+    assert oj["impulse"][0, 0] < 0
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (2.0 * t * lam, 0, 0), rtol=1e-4, atol=1e-8)
+
+
+def test_ellipse_swing_limit_clamps_its_angles():
+    """MaximumAngleX / Y setters clamp to [BigEpsilon, pi] (EllipseSwingLimit.cs:57-68)."""
+    b, j = _ellipse_swing_x(0.4, 5.0, 0.5)
+    _, oj = _step(b, j)
+    b, j2 = _ellipse_swing_x(0.4, np.pi, 0.5)
+    _, oj2 = _step(b, j2)
+    assert oj["impulse"][0, 0] == oj2["impulse"][0, 0] == 0
