@@ -57,6 +57,8 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_TWIST_LIMIT:
         case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
         case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT: return kJChildLimit;
+        case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR: return kJChildAngular;
+        case BEPUGPU_JOINT_SWIVEL_HINGE: return kJChildBall | kJChildAngular;
         default: return 0;
     }
 }
@@ -218,6 +220,13 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT:
                 lim[0] = r.impulse[0];
                 break;
+            case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR:
+                ang[0] = r.impulse[0];
+                break;
+            case BEPUGPU_JOINT_SWIVEL_HINGE:
+                std::memcpy(ball, r.impulse, 12);
+                ang[0] = r.impulse[3];
+                break;
             case BEPUGPU_JOINT_LINEAR_AXIS_LIMIT:
                 lim[1] = r.impulse[0];
                 break;
@@ -316,6 +325,13 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT:
                 r.impulse[0] = a1.y;
+                break;
+            case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR:
+                r.impulse[0] = a0.w;
+                break;
+            case BEPUGPU_JOINT_SWIVEL_HINGE:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                r.impulse[3] = a0.w;
                 break;
             case BEPUGPU_JOINT_UNIVERSAL:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;

@@ -21,6 +21,8 @@
 //   TwistLimit            TwoEntity/JointLimits/TwistLimit.cs:200-383 (the limit slot; its
 //                         last error, which picks the next jacobian's sign, in kJACC1.w)
 //   EllipseSwingLimit     TwoEntity/JointLimits/EllipseSwingLimit.cs:162-357 (the limit slot)
+//   SwivelHingeAngularJoint  TwoEntity/Joints/SwivelHingeAngularJoint.cs:193-287 (the angular
+//                         slot; SWIVEL_HINGE is the group of a ball socket and it)
 //   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
 //                         also the limit child of PRISMATIC and LINE_SLIDER records)
 // and the groups PrismaticJoint (point on line + no rotation), LineSliderJoint
@@ -109,6 +111,9 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+__device__ __forceinline__ bool IsSwivelType(int type) {
+    return type == BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR || type == BEPUGPU_JOINT_SWIVEL_HINGE;
 }
 __device__ __forceinline__ bool IsLinearLimitType(int type) {
     return type == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || type == BEPUGPU_JOINT_PRISMATIC ||
@@ -657,6 +662,31 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJL1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
         j.L(kJL2, s) = make_float4(mass.M33, bx, by, bz);
         st |= 1u << (kChildShift + 1);
+    } else if (kAdded && (active & kJChildAngular) && IsSwivelType(type)) {
+        // SwivelHingeAngularJoint.Update (SwivelHingeAngularJoint.cs:222-270).  Inputs: the
+        // hinge axis (kJAXA, A's frame) and the twist axis (kJAXB, B's frame).  Lanes: kJW1
+        // jacobianA + velocityToImpulse, kJW2.x bias, kJOB.w softness (jacobianB = -jacobianA).
+        const float3 hinge = JTransform(JXYZ(axa), A.R), twist = JTransform(JXYZ(axb), B.R);
+        const float error = JDot(hinge, twist);
+        float erp, softness;
+        JSpring(stiffness, damping, p.dt, p.updateRate, erp, softness);
+        const float bias = Clampf(error * erp, -maxCorr, maxCorr);
+        float3 jA = JCross(hinge, twist);
+        const float length = JDot(jA, jA);
+        if (length > 1e-7f) {
+            const float inverse = 1 / SqrtOfFloat(length);  // Vector3.Divide (Vector3.cs:175-181)
+            jA = make_float3(jA.x * inverse, jA.y * inverse, jA.z * inverse);
+        } else {
+            jA = make_float3(0.f, 0.f, 0.f);
+        }
+        const float3 jB = make_float3(-jA.x, -jA.y, -jA.z);
+        const float entryA = A.dynamic ? JDot(JTransform(jA, JInertia(A.s)), jA) : 0.f;
+        const float entryB = B.dynamic ? JDot(JTransform(jB, JInertia(B.s)), jB) : 0.f;
+        const float vti = 1 / (softness + entryA + entryB);
+        j.L(kJOB, s).w = softness;
+        j.L(kJW1, s) = make_float4(jA.x, jA.y, jA.z, vti);
+        j.L(kJW2, s) = make_float4(bias, 0.f, 0.f, 0.f);
+        st |= 1u << (kChildShift + 1);
     } else if (active & kJChildAngular) {
         // RevoluteAngularJoint.Update (RevoluteAngularJoint.cs:226-289)
         float3 wA = JTransform(JXYZ(axa), A.R), wB = JTransform(JXYZ(axb), B.R);
@@ -1064,6 +1094,12 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
         // NoRotationJoint.ExclusiveUpdate (NoRotationJoint.cs:245-259)
         if (dynA) ApplyAngular(A, acc0.w, acc1.x, acc1.y);
         if (dynB) ApplyAngular(B, -acc0.w, -acc1.x, -acc1.y);
+    } else if (kAdded && (st & (2u << kChildShift)) && IsSwivelType(type)) {
+        // SwivelHingeAngularJoint.ExclusiveUpdate (SwivelHingeAngularJoint.cs:272-287)
+        const float4 w1 = j.L(kJW1, s);
+        const float a = acc0.w;
+        if (dynA) ApplyAngular(A, w1.x * a, w1.y * a, w1.z * a);
+        if (dynB) ApplyAngular(B, -w1.x * a, -w1.y * a, -w1.z * a);
     } else if (st & (2u << kChildShift)) {
         // RevoluteAngularJoint.ExclusiveUpdate (RevoluteAngularJoint.cs:291-310)
         const float3 c1 = JXYZ(j.L(kJW1, s)), c2 = JXYZ(j.L(kJW2, s));
@@ -1277,6 +1313,19 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         if (dynA) ApplyAngular(A, tx, ty, tz);
         if (dynB) ApplyAngular(B, -tx, -ty, -tz);
         account(1, fabsf(tx) + fabsf(ty) + fabsf(tz));
+    } else if (kAdded && (st & (2u << kChildShift)) && IsSwivelType(type)) {
+        // SwivelHingeAngularJoint.SolveIteration (SwivelHingeAngularJoint.cs:193-220)
+        const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s);
+        const float softness = j.L(kJOB, s).w;
+        const float jbx = -w1.x, jby = -w1.y, jbz = -w1.z;
+        const float velocityA = A.wx * w1.x + A.wy * w1.y + A.wz * w1.z;
+        const float velocityB = B.wx * jbx + B.wy * jby + B.wz * jbz;
+        float lambda = -(velocityA + velocityB) - w2.x - softness * acc0.w;
+        lambda *= w1.w;
+        acc0.w += lambda;
+        if (dynA) ApplyAngular(A, w1.x * lambda, w1.y * lambda, w1.z * lambda);
+        if (dynB) ApplyAngular(B, jbx * lambda, jby * lambda, jbz * lambda);
+        account(1, fabsf(lambda));
     } else if (st & (2u << kChildShift)) {
         // RevoluteAngularJoint.SolveIteration (RevoluteAngularJoint.cs:313-356)
         const float4 w1 = j.L(kJW1, s), w2 = j.L(kJW2, s), e = j.L(kJE, s);

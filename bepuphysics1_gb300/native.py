@@ -106,6 +106,7 @@ JOINT_NO_ROTATION, JOINT_WELD, JOINT_DISTANCE, JOINT_DISTANCE_LIMIT = 6, 7, 8, 9
 JOINT_POINT_ON_PLANE, JOINT_TWIST = 10, 11
 JOINT_POINT_ON_LINE, JOINT_PRISMATIC, JOINT_LINE_SLIDER, JOINT_UNIVERSAL = 12, 13, 14, 15
 JOINT_TWIST_LIMIT, JOINT_LINEAR_AXIS_LIMIT, JOINT_ELLIPSE_SWING_LIMIT = 16, 17, 18
+JOINT_SWIVEL_HINGE_ANGULAR, JOINT_SWIVEL_HINGE = 19, 20
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE = 1, 2
 
 _P = ctypes.c_void_p

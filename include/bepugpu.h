@@ -153,11 +153,14 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_UNIVERSAL = 15,       /* UniversalJoint group: ball socket + twist */
     BEPUGPU_JOINT_TWIST_LIMIT = 16,     /* TwistLimit.cs:200-383 */
     BEPUGPU_JOINT_LINEAR_AXIS_LIMIT = 17, /* LinearAxisLimit.cs:290-466 */
-    BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT = 18 /* EllipseSwingLimit.cs:162-357 */
+    BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT = 18, /* EllipseSwingLimit.cs:162-357 */
+    BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR = 19, /* SwivelHingeAngularJoint.cs:193-287 */
+    BEPUGPU_JOINT_SWIVEL_HINGE = 20     /* SwivelHingeJoint group: ball socket + swivel hinge angular */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
- * is UniversalJoint's twist limit (:52).  The limits of REVOLUTE, PRISMATIC and
+ * are UniversalJoint's twist limit (:52) and SwivelHingeJoint's hinge and twist
+ * limits (SwivelHingeJoint.cs:59-62).  The limits of REVOLUTE, PRISMATIC and
  * LINE_SLIDER records (a LinearAxisLimit on the line's anchors and direction
  * for the last two) follow BEPUGPU_JOINT_LIMIT_ACTIVE. */
 
@@ -176,7 +179,9 @@ typedef enum bepugpu_joint_type {
  *                     SwingLimit.localAxisA/B (SWING_LIMIT), TwistJoint.localAxisA/B (TWIST),
  *                     PointOnPlaneJoint.localPlaneNormal (axis_a, POINT_ON_PLANE),
  *                     TwistLimit basis A / basis B local primary axes (TWIST_LIMIT),
- *                     EllipseSwingLimit basis primary / localTwistAxisB (ELLIPSE_SWING_LIMIT)
+ *                     EllipseSwingLimit basis primary / localTwistAxisB (ELLIPSE_SWING_LIMIT),
+ *                     SwivelHingeAngularJoint.localHingeAxis (A) / localTwistAxis (B)
+ *                     (SWIVEL_HINGE_ANGULAR, SWIVEL_HINGE)
  *   constrained_1/2   RevoluteAngularJoint.localConstrainedAxis1/2, in A's frame;
  *                     TwistJoint.aLocalAxisY / aLocalAxisZ (TWIST, UNIVERSAL);
  *                     TwistLimit basis A local x / y axes (TWIST_LIMIT), EllipseSwingLimit
@@ -210,7 +215,8 @@ typedef enum bepugpu_joint_type {
  *                     [5] limit; LINE_SLIDER [0..1] point on line, [2..3] angular, [4] limit;
  *                     UNIVERSAL [0..2] ball socket, [3] twist; TWIST_LIMIT [0], and [1] the
  *                     error its last Update left (the sign of the next jacobian follows it,
- *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0]; ELLIPSE_SWING_LIMIT [0].  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
+ *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0]; ELLIPSE_SWING_LIMIT [0];
+ *                     SWIVEL_HINGE_ANGULAR [0]; SWIVEL_HINGE [0..2] ball socket, [3] angular.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
  *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */

@@ -176,7 +176,8 @@ def test_chains_in_island_groups(gpu_context, policy):
 
 NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
              N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL,
-             N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT, N.JOINT_ELLIPSE_SWING_LIMIT)
+             N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT, N.JOINT_ELLIPSE_SWING_LIMIT,
+             N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE)
 
 
 def _unit(v):
@@ -275,6 +276,13 @@ def _convert(b, j, types, seed):
             j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
             j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        if t in (N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE):
+            # a hinge axis on A and a twist axis on B, perpendicular up to 0.1 rad
+            ra, rb = _rows(qa), _rows(qb)
+            h = _unit(rng.normal(size=3))
+            t0 = _unit(np.cross(h, rng.normal(size=3)))
+            e = rng.uniform(-0.1, 0.1)
+            j["axis_a"][k], j["axis_b"][k] = h @ ra.T, _unit(t0 * np.cos(e) + h * np.sin(e)) @ rb.T
         if t in (N.JOINT_TWIST, N.JOINT_UNIVERSAL):
             # TwistJoint.Initialize (TwistJoint.cs:340-365) for a shared world axis
             ax = rng.normal(size=3)

@@ -412,3 +412,23 @@ def test_ellipse_swing_limit_clamps_its_angles():
     b, j2 = _ellipse_swing_x(0.4, np.pi, 0.5)
     _, oj2 = _step(b, j2)
     assert oj["impulse"][0, 0] == oj2["impulse"][0, 0] == 0
+
+
+def test_swivel_hinge_angular_to_world_closed_form():
+    """SwivelHingeAngularJoint (SwivelHingeAngularJoint.cs:193-270): the world's
+    hinge axis x against B's twist axis y turned by phi about z: error
+    -sin(phi), jacobian A = z, an unclamped impulse whose bias is subtracted."""
+    phi = 0.1
+    b = _body((0, 0, 0), quat=_rot_z(phi))
+    j = _joint(N.JOINT_SWIVEL_HINGE_ANGULAR, -1, 0)
+    j["axis_a"], j["axis_b"] = (1, 0, 0), (0, 1, 0)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = np.sin(phi) * erp / (soft + 4.0)  # I_zz = 4, jacobianB = -z
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+    g = _joint(N.JOINT_SWIVEL_HINGE, -1, 0)  # ball socket at B's centre first: it does nothing here
+    g["axis_a"], g["axis_b"] = (1, 0, 0), (0, 1, 0)
+    _, og = _step(b, g)
+    assert np.all(og["impulse"][0, :3] == 0)
+    assert og["impulse"][0, 3] == oj["impulse"][0, 0]
