@@ -59,6 +59,9 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT: return kJChildLimit;
         case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR: return kJChildAngular;
         case BEPUGPU_JOINT_SWIVEL_HINGE: return kJChildBall | kJChildAngular;
+        case BEPUGPU_JOINT_REVOLUTE_MOTOR:
+        case BEPUGPU_JOINT_TWIST_MOTOR:
+        case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR: return kJChildLimit;
         default: return 0;
     }
 }
@@ -169,6 +172,22 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             auto clamp = [](float v) { return v < 1e-5f ? 1e-5f : (v > kHostPi ? kHostPi : v); };
             at(kJTRIG, slot) = make_float4(clamp(r.limit_min), clamp(r.limit_max), 0.f, 0.f);
         }
+        if (r.type >= BEPUGPU_JOINT_REVOLUTE_MOTOR && r.type <= BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+            // MotorSettings1D through its setters (MotorSettings.cs): the angular motors' goal
+            // wrapped by MathHelper.WrapAngle (MathHelper.cs:35-49), as GetDistanceFromGoal does
+            float goal = r.limit_min;
+            if (r.type != BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+                goal = (float)std::remainder((double)goal, (double)kHostTwoPi);
+                if (goal < -kHostPi) goal += kHostTwoPi;
+                else if (goal >= kHostPi) goal -= kHostTwoPi;
+            }
+            const float softness = r.margin < 0 ? 0.f : r.margin;
+            const float base = r.bounciness < 0 ? 0.f : r.bounciness;
+            const float maxForce = r.bounce_velocity_threshold >= 0 ? r.bounce_velocity_threshold : 0.f;
+            at(kJTRIG, slot) = make_float4(goal, r.limit_max, softness, base);
+            at(kJBX, slot) = F4(r.basis_x, maxForce);
+            at(kJAXB, slot) = F4(r.axis_b, (r.flags & BEPUGPU_JOINT_SERVO) ? 1.f : 0.f);
+        }
         if (r.type == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || r.type == BEPUGPU_JOINT_PRISMATIC ||
             r.type == BEPUGPU_JOINT_LINE_SLIDER)
             // a prismatic joint's kJC1 / kJC2 hold orientations: the limit's bounce settings go here
@@ -222,6 +241,11 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR:
                 ang[0] = r.impulse[0];
+                break;
+            case BEPUGPU_JOINT_REVOLUTE_MOTOR:
+            case BEPUGPU_JOINT_TWIST_MOTOR:
+            case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
+                lim[0] = r.impulse[0];
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
                 std::memcpy(ball, r.impulse, 12);
@@ -328,6 +352,11 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR:
                 r.impulse[0] = a0.w;
+                break;
+            case BEPUGPU_JOINT_REVOLUTE_MOTOR:
+            case BEPUGPU_JOINT_TWIST_MOTOR:
+            case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
+                r.impulse[0] = a1.y;
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;

@@ -21,6 +21,7 @@
 //   TwistLimit            TwoEntity/JointLimits/TwistLimit.cs:200-383 (the limit slot; its
 //                         last error, which picks the next jacobian's sign, in kJACC1.w)
 //   EllipseSwingLimit     TwoEntity/JointLimits/EllipseSwingLimit.cs:162-357 (the limit slot)
+//   RevoluteMotor, TwistMotor, LinearAxisMotor  TwoEntity/Motors/*.cs (the limit slot)
 //   SwivelHingeAngularJoint  TwoEntity/Joints/SwivelHingeAngularJoint.cs:193-287 (the angular
 //                         slot; SWIVEL_HINGE is the group of a ball socket and it)
 //   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
@@ -111,6 +112,19 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+__device__ __forceinline__ bool IsMotorType(int type) {
+    return type >= BEPUGPU_JOINT_REVOLUTE_MOTOR && type <= BEPUGPU_JOINT_LINEAR_AXIS_MOTOR;
+}
+// Math.Sign of a float, as the motors' servo bias multiplies it
+__device__ __forceinline__ float JSign(float v) { return v > 0 ? 1.f : (v < 0 ? -1.f : 0.f); }
+// RevoluteMotor / TwistMotor.GetDistanceFromGoal (RevoluteMotor.cs:345-371); the
+// goal arrives wrapped by MathHelper.WrapAngle.
+__device__ __forceinline__ float JDistanceFromGoal(float angle, float goalAngle) {
+    float forward;
+    if (goalAngle > 0) forward = angle > goalAngle ? angle - goalAngle : 6.28318548f - goalAngle + angle;
+    else forward = angle < goalAngle ? 6.28318548f - goalAngle + angle : angle - goalAngle;
+    return forward > 3.14159274f ? 6.28318548f - forward : -forward;
 }
 __device__ __forceinline__ bool IsSwivelType(int type) {
     return type == BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR || type == BEPUGPU_JOINT_SWIVEL_HINGE;
@@ -785,6 +799,114 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                     j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
                 }
             }
+        } else if (kAdded && IsMotorType(type)) {
+            // RevoluteMotor.Update (RevoluteMotor.cs:243-290), TwistMotor.Update (TwistMotor.cs:182-224),
+            // LinearAxisMotor.Update (LinearAxisMotor.cs:285-368).  Inputs: kJTRIG wrapped servo
+            // goal (the linear motor's as given), goal velocity, velocity softness, base corrective
+            // speed; kJBX.w maximum force; kJAXB.w 1 in servo mode; axes as the limits of the same
+            // kind take them.  Lanes: kJL0 jacobian (linear A) + used softness; angular motors
+            // kJL2 = signed bias (the revolute motor's negated: its solve subtracts it), -,
+            // velocityToImpulse, maxForceDt; the linear motor kJL1 jAngularA + bias, kJL2
+            // jAngularB + mass, kJOA.x maxForceDt.  Impulse kJACC1.y.
+            const float4 trig = ji.L(kJTRIG, si);
+            const bool servo = axb.w != 0.f;
+            const float maxForce = ji.L(kJBX, si).w;
+            const float updateRate = p.updateRate;
+            const float maxForceDt = maxForce < 3.40282347e+38f ? maxForce * p.dt : 3.40282347e+38f;
+            auto servoBias = [&](float error, float absErrorOverDt, float errorReduction) {
+                float bias = JSign(error) * Minf(trig.w, absErrorOverDt) + error * errorReduction;
+                return Clampf(bias, -maxCorr, maxCorr);
+            };
+            float usedSoftness, bias;
+            if (type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+                const float3 offA = JTransform(JXYZ(la), A.R), offB = JTransform(JXYZ(lb), B.R);
+                const float3 anchorA = make_float3(offA.x + A.pos.x, offA.y + A.pos.y, offA.z + A.pos.z);
+                const float3 anchorB = make_float3(offB.x + B.pos.x, offB.y + B.pos.y, offB.z + B.pos.z);
+                const float3 rA = make_float3(anchorB.x - A.pos.x, anchorB.y - A.pos.y, anchorB.z - A.pos.z);
+                const float3 axis = JTransform(JXYZ(ji.L(kJBP, si)), A.R);
+                if (servo) {
+                    const float3 sep = make_float3(anchorB.x - anchorA.x, anchorB.y - anchorA.y, anchorB.z - anchorA.z);
+                    float error = JDot(sep, axis);
+                    error = error - trig.x;
+                    const float absErrorOverDt = fabsf(error * updateRate);
+                    JSpring(stiffness, damping, p.dt, updateRate, erp, usedSoftness);
+                    bias = servoBias(error, absErrorOverDt, erp);
+                } else {
+                    bias = -trig.y;
+                    usedSoftness = trig.z * updateRate;
+                }
+                const float3 jlb = make_float3(-axis.x, -axis.y, -axis.z);
+                const float3 jaa = JCross(rA, axis), jab = JCross(offB, jlb);
+                float entryA = 0, entryB = 0;
+                if (A.dynamic) {
+                    entryA = JDot(JTransform(jaa, JInertia(A.s)), jaa);
+                    entryA += A.s.invMass;
+                }
+                if (B.dynamic) {
+                    entryB = JDot(JTransform(jab, JInertia(B.s)), jab);
+                    entryB += B.s.invMass;
+                }
+                const float mass = 1 / (entryA + entryB + usedSoftness);
+                j.L(kJL0, s) = make_float4(axis.x, axis.y, axis.z, usedSoftness);
+                j.L(kJL1, s) = make_float4(jaa.x, jaa.y, jaa.z, bias);
+                j.L(kJL2, s) = make_float4(jab.x, jab.y, jab.z, mass);
+                j.L(kJOA, s).x = maxForceDt;
+            } else {
+                float3 jA;
+                float signedBias;
+                if (type == BEPUGPU_JOINT_REVOLUTE_MOTOR) {
+                    const float3 primary = JTransform(JXYZ(ji.L(kJBP, si)), A.R);
+                    const float3 xAxis = JTransform(JXYZ(ji.L(kJBX, si)), A.R);
+                    const float3 test = JTransform(JXYZ(ji.L(kJTA, si)), B.R);
+                    if (servo) {
+                        const float3 yAxis = JCross(primary, xAxis);
+                        const float y = JDot(test, yAxis), x = JDot(test, xAxis);
+                        const float angle = (float)atan2((double)y, (double)x);
+                        const float error = JDistanceFromGoal(angle, trig.x);
+                        const float absErrorOverDt = fabsf(error * updateRate);
+                        JSpring(stiffness, damping, p.dt, updateRate, erp, usedSoftness);
+                        bias = servoBias(error, absErrorOverDt, erp);
+                    } else {
+                        bias = trig.y;
+                        usedSoftness = trig.z * updateRate;
+                    }
+                    jA = primary;
+                    signedBias = -bias;
+                } else {
+                    const float3 pA = JTransform(JXYZ(axa), A.R), xA = JTransform(JXYZ(ji.L(kJC1, si)), A.R);
+                    const float3 yA = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
+                    const float3 pB = JTransform(JXYZ(axb), B.R), xB = JTransform(JXYZ(ji.L(kJBX, si)), B.R);
+                    if (servo) {
+                        const float4 rotation = JQuatBetween(pB, pA);
+                        const float3 tm = QTransform(xB.x, xB.y, xB.z, rotation);
+                        const float y = JDot(tm, yA), x = JDot(tm, xA);
+                        const float angle = (float)atan2((double)y, (double)x);
+                        const float error = JDistanceFromGoal(angle, trig.x);
+                        const float absErrorOverDt = fabsf(error / p.dt);
+                        JSpring(stiffness, damping, p.dt, updateRate, erp, usedSoftness);
+                        bias = servoBias(error, absErrorOverDt, erp);
+                    } else {
+                        bias = trig.y;
+                        usedSoftness = trig.z / p.dt;
+                    }
+                    float3 jv = make_float3(pA.x + pB.x, pA.y + pB.y, pA.z + pB.z);
+                    if (JDot(jv, jv) < 1e-7f) {
+                        on = false;  // aligned axes: the motor leaves the solver this step
+                    } else {
+                        jv = JNormalize(jv);
+                        jA = make_float3(-jv.x, -jv.y, -jv.z);
+                    }
+                    signedBias = bias;
+                }
+                if (on) {
+                    const float3 jB = make_float3(-jA.x, -jA.y, -jA.z);
+                    const float entryA = A.dynamic ? JDot(JTransform(jA, JInertia(A.s)), jA) : 0.f;
+                    const float entryB = B.dynamic ? JDot(JTransform(jB, JInertia(B.s)), jB) : 0.f;
+                    const float vti = 1 / (usedSoftness + entryA + entryB);
+                    j.L(kJL0, s) = make_float4(jA.x, jA.y, jA.z, usedSoftness);
+                    j.L(kJL2, s) = make_float4(signedBias, 0.f, vti, maxForceDt);
+                }
+            }
         } else if (kAdded && type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
             // EllipseSwingLimit.Update (EllipseSwingLimit.cs:162-308).  Inputs: basis primary /
             // x / y (kJAXA, kJC1, kJC2, A's frame), B's twist axis (kJAXB), kJTRIG.x / .y the
@@ -1110,8 +1232,22 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && (type == BEPUGPU_JOINT_TWIST_LIMIT || type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT)) {
-            // TwistLimit.ExclusiveUpdate (TwistLimit.cs:368-383), EllipseSwingLimit's (:310-325)
+        if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+            // LinearAxisMotor.ExclusiveUpdate (LinearAxisMotor.cs:370-390)
+            const float4 jaa = j.L(kJL1, s), jab = j.L(kJL2, s);
+            const float a = acc1.y;
+            if (dynA) {
+                ApplyLinear(A, l0.x * a, l0.y * a, l0.z * a);
+                ApplyAngular(A, jaa.x * a, jaa.y * a, jaa.z * a);
+            }
+            if (dynB) {
+                ApplyLinear(B, -l0.x * a, -l0.y * a, -l0.z * a);
+                ApplyAngular(B, jab.x * a, jab.y * a, jab.z * a);
+            }
+        } else if (kAdded && (type == BEPUGPU_JOINT_TWIST_LIMIT || type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT ||
+                              type == BEPUGPU_JOINT_REVOLUTE_MOTOR || type == BEPUGPU_JOINT_TWIST_MOTOR)) {
+            // TwistLimit.ExclusiveUpdate (TwistLimit.cs:368-383), EllipseSwingLimit's (:310-325),
+            // RevoluteMotor's (RevoluteMotor.cs:292-307), TwistMotor's (TwistMotor.cs:255-270)
             const float a = acc1.y;
             if (dynA) ApplyAngular(A, l0.x * a, l0.y * a, l0.z * a);
             if (dynB) ApplyAngular(B, -l0.x * a, -l0.y * a, -l0.z * a);
@@ -1376,7 +1512,46 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
+        if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+            // LinearAxisMotor.SolveIteration (LinearAxisMotor.cs:244-283)
+            const float4 jaa = j.L(kJL1, s), jab = j.L(kJL2, s);
+            const float maxForceDt = j.L(kJOA, s).x;
+            const float bx = -l0.x, by = -l0.y, bz = -l0.z;  // jLinearB
+            float lambda = l0.x * A.vx + l0.y * A.vy + l0.z * A.vz;
+            float dot = jaa.x * A.wx + jaa.y * A.wy + jaa.z * A.wz;
+            lambda += dot;
+            dot = bx * B.vx + by * B.vy + bz * B.vz;
+            lambda += dot;
+            dot = jab.x * B.wx + jab.y * B.wy + jab.z * B.wz;
+            lambda += dot;
+            lambda = -lambda + jaa.w - softness * acc1.y;
+            lambda *= jab.w;
+            const float previous = acc1.y;
+            acc1.y = Clampf(acc1.y + lambda, -maxForceDt, maxForceDt);
+            lambda = acc1.y - previous;
+            if (dynA) {
+                ApplyLinear(A, l0.x * lambda, l0.y * lambda, l0.z * lambda);
+                ApplyAngular(A, jaa.x * lambda, jaa.y * lambda, jaa.z * lambda);
+            }
+            if (dynB) {
+                ApplyLinear(B, bx * lambda, by * lambda, bz * lambda);
+                ApplyAngular(B, jab.x * lambda, jab.y * lambda, jab.z * lambda);
+            }
+            account(2, fabsf(lambda));
+        } else if (kAdded && (type == BEPUGPU_JOINT_REVOLUTE_MOTOR || type == BEPUGPU_JOINT_TWIST_MOTOR)) {
+            // RevoluteMotor.SolveIteration (RevoluteMotor.cs:309-340), TwistMotor's (TwistMotor.cs:226-253)
+            const float nx = -l0.x, ny = -l0.y, nz = -l0.z;  // jacobianB
+            const float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;
+            const float velocityB = B.wx * nx + B.wy * ny + B.wz * nz;
+            float lambda = -(velocityA + velocityB) + l2.x - softness * acc1.y;
+            lambda *= l2.z;
+            const float previous = acc1.y;
+            acc1.y = Clampf(acc1.y + lambda, -l2.w, l2.w);
+            lambda = acc1.y - previous;
+            if (dynA) ApplyAngular(A, l0.x * lambda, l0.y * lambda, l0.z * lambda);
+            if (dynB) ApplyAngular(B, nx * lambda, ny * lambda, nz * lambda);
+            account(2, fabsf(lambda));
+        } else if (kAdded && type == BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT) {
             // EllipseSwingLimit.SolveIteration (EllipseSwingLimit.cs:327-357)
             const float nx = -l0.x, ny = -l0.y, nz = -l0.z;  // jacobianB
             const float velocityA = A.wx * l0.x + A.wy * l0.y + A.wz * l0.z;

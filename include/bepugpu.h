@@ -155,7 +155,10 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_LINEAR_AXIS_LIMIT = 17, /* LinearAxisLimit.cs:290-466 */
     BEPUGPU_JOINT_ELLIPSE_SWING_LIMIT = 18, /* EllipseSwingLimit.cs:162-357 */
     BEPUGPU_JOINT_SWIVEL_HINGE_ANGULAR = 19, /* SwivelHingeAngularJoint.cs:193-287 */
-    BEPUGPU_JOINT_SWIVEL_HINGE = 20     /* SwivelHingeJoint group: ball socket + swivel hinge angular */
+    BEPUGPU_JOINT_SWIVEL_HINGE = 20,    /* SwivelHingeJoint group: ball socket + swivel hinge angular */
+    BEPUGPU_JOINT_REVOLUTE_MOTOR = 21,  /* RevoluteMotor.cs:243-340 */
+    BEPUGPU_JOINT_TWIST_MOTOR = 22,     /* TwistMotor.cs:182-253 */
+    BEPUGPU_JOINT_LINEAR_AXIS_MOTOR = 23 /* LinearAxisMotor.cs:244-390 */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
@@ -166,6 +169,7 @@ typedef enum bepugpu_joint_type {
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
 #define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE, PRISMATIC, LINE_SLIDER: the group's Limit.IsActive */
+#define BEPUGPU_JOINT_SERVO         4u  /* motors: MotorMode.Servomechanism (else VelocityMotor) */
 
 /* Joint record: the state each reference object keeps between steps.  Body -1
  * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic
@@ -216,7 +220,18 @@ typedef enum bepugpu_joint_type {
  *                     UNIVERSAL [0..2] ball socket, [3] twist; TWIST_LIMIT [0], and [1] the
  *                     error its last Update left (the sign of the next jacobian follows it,
  *                     TwistLimit.cs:284-312); LINEAR_AXIS_LIMIT [0]; ELLIPSE_SWING_LIMIT [0];
- *                     SWIVEL_HINGE_ANGULAR [0]; SWIVEL_HINGE [0..2] ball socket, [3] angular.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
+ *                     SWIVEL_HINGE_ANGULAR [0]; SWIVEL_HINGE [0..2] ball socket, [3] angular;
+ *                     the motors [0].
+ * Motors (REVOLUTE_MOTOR, TWIST_MOTOR, LINEAR_AXIS_MOTOR) take their axes as the
+ * limit of the same kind does (REVOLUTE_LIMIT's basis and test axis, TWIST_LIMIT's
+ * bases, LINEAR_AXIS_LIMIT's anchors and axis) and their MotorSettings1D from:
+ *   limit_min  servo goal          limit_max  velocity motor goal velocity
+ *   margin     velocity motor softness (default 0.0001)
+ *   bounciness servo base corrective speed (0)
+ *   bounce_velocity_threshold  maximum force (FLT_MAX)
+ *   max_corrective_velocity    servo max corrective velocity
+ *   spring_stiffness/damping   servo spring settings
+ *   flags & BEPUGPU_JOINT_SERVO  servomechanism mode.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
  *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */

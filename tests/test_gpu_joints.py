@@ -177,7 +177,9 @@ def test_chains_in_island_groups(gpu_context, policy):
 NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTANCE_LIMIT, N.JOINT_POINT_ON_PLANE,
              N.JOINT_TWIST, N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER, N.JOINT_UNIVERSAL,
              N.JOINT_TWIST_LIMIT, N.JOINT_LINEAR_AXIS_LIMIT, N.JOINT_ELLIPSE_SWING_LIMIT,
-             N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE)
+             N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE, N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR,
+             N.JOINT_LINEAR_AXIS_MOTOR)
+MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
 
 
 def _unit(v):
@@ -276,6 +278,29 @@ def _convert(b, j, types, seed):
             j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
             j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        if t in MOTORS:
+            servo = rng.random() < 0.5
+            j["flags"][k] |= N.JOINT_SERVO if servo else 0
+            linear = t == N.JOINT_LINEAR_AXIS_MOTOR
+            j["limit_min"][k] = rng.uniform(-0.05, 0.05) if linear else rng.uniform(-np.pi, np.pi)
+            j["limit_max"][k] = rng.uniform(-1.0, 1.0)
+            j["margin"][k] = 0.0001
+            j["bounciness"][k] = rng.choice([0.0, 0.3])
+            j["bounce_velocity_threshold"][k] = rng.choice([np.finfo(np.float32).max, 5.0])
+            ra, rb = _rows(qa), _rows(qb)
+            ax = _unit(rng.normal(size=3))
+            if t == N.JOINT_REVOLUTE_MOTOR:
+                x = _unit(np.cross(ax, rng.normal(size=3)))
+                ang = rng.uniform(-np.pi, np.pi)
+                xt = x * np.cos(ang) + np.cross(ax, x) * np.sin(ang)
+                j["basis_primary"][k], j["basis_x"][k], j["test_axis"][k] = ax @ ra.T, x @ ra.T, xt @ rb.T
+            elif t == N.JOINT_TWIST_MOTOR:
+                x = _unit(np.cross(ax, rng.normal(size=3)))
+                y = _unit(np.cross(ax, x))
+                j["axis_a"][k], j["constrained_1"][k], j["constrained_2"][k] = ax @ ra.T, x @ ra.T, y @ ra.T
+                j["axis_b"][k], j["basis_x"][k] = ax @ rb.T, x @ rb.T
+            else:
+                j["basis_primary"][k] = ax @ ra.T
         if t in (N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE):
             # a hinge axis on A and a twist axis on B, perpendicular up to 0.1 rad
             ra, rb = _rows(qa), _rows(qb)
@@ -323,7 +348,8 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
         errs, exact = p.compare()
         assert exact, (jtype, step, errs)
     limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_ELLIPSE_SWING_LIMIT: 0,
-                   N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4}
+                   N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4, N.JOINT_REVOLUTE_MOTOR: 0,
+                   N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
         got = p.oracle.get_constraints()[1]["impulse"][:, e]

@@ -432,3 +432,65 @@ def test_swivel_hinge_angular_to_world_closed_form():
     _, og = _step(b, g)
     assert np.all(og["impulse"][0, :3] == 0)
     assert og["impulse"][0, 3] == oj["impulse"][0, 0]
+
+
+def _motor(jtype, servo=False, goal=0.0, goal_velocity=0.0, max_force=np.finfo(np.float32).max):
+    j = _joint(jtype, -1, 0)
+    j["flags"] |= N.JOINT_SERVO if servo else 0
+    j["limit_min"], j["limit_max"] = goal, goal_velocity
+    j["margin"] = 0.0001                 # velocity motor softness
+    j["bounciness"] = 0.0                # servo base corrective speed
+    j["bounce_velocity_threshold"] = max_force
+    return j
+
+
+@pytest.mark.parametrize("max_force,expect", [(np.finfo(np.float32).max, None), (12.0, 0.2)])
+def test_revolute_velocity_motor_closed_form(max_force, expect):
+    """RevoluteMotor in velocity mode (RevoluteMotor.cs:243-340): goal 2 rad/s
+    about z; its bias is subtracted, its softness is 0.0001 / dt, and the
+    impulse is clamped to the maximum force times dt."""
+    b = _body((0, 0, 0))
+    j = _motor(N.JOINT_REVOLUTE_MOTOR, goal_velocity=2.0, max_force=max_force)
+    j["basis_primary"], j["basis_x"], j["test_axis"] = (0, 0, 1), (1, 0, 0), (1, 0, 0)
+    ob, oj = _step(b, j)
+    lam = -2.0 / (0.0001 * 60 + 4.0)  # I_zz = 4, jacobian B = -z
+    if expect is not None:
+        lam = -expect                    # 12 * dt
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def test_linear_axis_motors_closed_form():
+    """LinearAxisMotor (LinearAxisMotor.cs:244-368): the velocity motor's bias
+    is the negated goal velocity; the servo's is the error (separation less
+    the goal) times the error reduction, pushing B back to the goal."""
+    b = _body((0, 0, 0))
+    j = _motor(N.JOINT_LINEAR_AXIS_MOTOR, goal_velocity=3.0)
+    j["basis_primary"] = (1, 0, 0)
+    ob, oj = _step(b, j)
+    lam = -3.0 / (1.0 + 0.0001 * 60)
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (-lam, 0, 0), rtol=1e-4, atol=1e-9)
+    b = _body((1.2, 0, 0))
+    j = _motor(N.JOINT_LINEAR_AXIS_MOTOR, servo=True, goal=1.0)
+    j["basis_primary"] = (1, 0, 0)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = 0.2 * erp / (1.0 + soft)
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (-lam, 0, 0), rtol=1e-4, atol=1e-9)
+
+
+def test_twist_servo_motor_closed_form():
+    """TwistMotor as a servo (TwistMotor.cs:182-253): turned 0.3 about z with
+    goal 0, the distance from the goal is -0.3; jacobian B = z, and the
+    positive-bias solve turns B back."""
+    b, j0 = _twist_limit_z(0.3, 0, 0)
+    j = _motor(N.JOINT_TWIST_MOTOR, servo=True, goal=2 * np.pi)  # wraps to 0
+    for f in ("axis_a", "axis_b", "constrained_1", "constrained_2", "basis_x"):
+        j[f] = j0[f]
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = -0.3 * erp / (soft + 4.0)
+    np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, 4.0 * lam), rtol=1e-4, atol=1e-8)
