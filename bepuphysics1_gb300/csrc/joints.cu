@@ -61,7 +61,9 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_SWIVEL_HINGE: return kJChildBall | kJChildAngular;
         case BEPUGPU_JOINT_REVOLUTE_MOTOR:
         case BEPUGPU_JOINT_TWIST_MOTOR:
-        case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR: return kJChildLimit;
+        case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
+        case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
+        case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED: return kJChildLimit;
         default: return 0;
     }
 }
@@ -93,6 +95,11 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
         // DistanceJoint.Distance, DistanceLimit.MinimumLength / MaximumLength setters keep these
         if (r.type == BEPUGPU_JOINT_DISTANCE && !(r.limit_min >= 0)) {
             ctx->SetError("joint %u: distance %g must be non-negative", u, r.limit_min);
+            return BEPUGPU_INVALID_ARGUMENT;
+        }
+        if ((r.type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || r.type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED) &&
+            r.body_b != -1) {
+            ctx->SetError("joint %u: a single-entity constraint acts on body_a alone (body_b must be -1)", u);
             return BEPUGPU_INVALID_ARGUMENT;
         }
         if (r.type == BEPUGPU_JOINT_DISTANCE_LIMIT && !(r.limit_min >= 0 && r.limit_min <= r.limit_max)) {
@@ -172,6 +179,12 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             auto clamp = [](float v) { return v < 1e-5f ? 1e-5f : (v > kHostPi ? kHostPi : v); };
             at(kJTRIG, slot) = make_float4(clamp(r.limit_min), clamp(r.limit_max), 0.f, 0.f);
         }
+        if (r.type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || r.type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED) {
+            // MaximumSpeed, MaximumForce and Softness setters (MaximumLinearVelocityConstraint.cs:32-59)
+            const float speed = 0 > r.limit_min ? 0.f : r.limit_min;
+            const float force = r.limit_max >= 0 ? r.limit_max : 0.f;
+            at(kJTRIG, slot) = make_float4(speed, force, std::max(0.f, r.margin), 0.f);
+        }
         if (r.type >= BEPUGPU_JOINT_REVOLUTE_MOTOR && r.type <= BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
             // MotorSettings1D through its setters (MotorSettings.cs): the angular motors' goal
             // wrapped by MathHelper.WrapAngle (MathHelper.cs:35-49), as GetDistanceFromGoal does
@@ -246,6 +259,10 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_TWIST_MOTOR:
             case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
                 lim[0] = r.impulse[0];
+                break;
+            case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
+            case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
+                std::memcpy(ball, r.impulse, 12);
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
                 std::memcpy(ball, r.impulse, 12);
@@ -357,6 +374,10 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
             case BEPUGPU_JOINT_TWIST_MOTOR:
             case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
                 r.impulse[0] = a1.y;
+                break;
+            case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
+            case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;

@@ -22,6 +22,8 @@
 //                         last error, which picks the next jacobian's sign, in kJACC1.w)
 //   EllipseSwingLimit     TwoEntity/JointLimits/EllipseSwingLimit.cs:162-357 (the limit slot)
 //   RevoluteMotor, TwistMotor, LinearAxisMotor  TwoEntity/Motors/*.cs (the limit slot)
+//   MaximumLinearSpeedConstraint, MaximumAngularSpeedConstraint
+//                         SingleEntity/Maximum*VelocityConstraint.cs (the limit slot, body B the world)
 //   SwivelHingeAngularJoint  TwoEntity/Joints/SwivelHingeAngularJoint.cs:193-287 (the angular
 //                         slot; SWIVEL_HINGE is the group of a ball socket and it)
 //   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
@@ -112,6 +114,9 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+__device__ __forceinline__ bool IsSpeedLimitType(int type) {
+    return type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED;
 }
 __device__ __forceinline__ bool IsMotorType(int type) {
     return type >= BEPUGPU_JOINT_REVOLUTE_MOTOR && type <= BEPUGPU_JOINT_LINEAR_AXIS_MOTOR;
@@ -799,6 +804,36 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                     j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
                 }
             }
+        } else if (kAdded && IsSpeedLimitType(type)) {
+            // MaximumLinearSpeedConstraint / MaximumAngularSpeedConstraint.Update
+            // (MaximumLinearVelocityConstraint.cs:177-193 and the angular file's).  Inputs: kJTRIG
+            // maximum speed, maximum force, softness.  Lanes (linear): kJL0 effective mass, used
+            // softness, maxForceDt, its square; kJL1 maximum speed, its square.  (Angular): kJL0
+            // used softness, maxForceDt, its square, maximum speed; kJL1 / kJL2 / kJOA.x the
+            // effective mass matrix; kJOA.y the maximum speed squared.  Impulse kJACC0.xyz.
+            const float4 trig = ji.L(kJTRIG, si);
+            const float usedSoftness = trig.z / p.dt;
+            float maxForceDt = 3.40282347e+38f, maxForceDtSquared = 3.40282347e+38f;
+            if (trig.y < 3.40282347e+38f) {
+                maxForceDt = trig.y * p.dt;
+                maxForceDtSquared = maxForceDt * maxForceDt;
+            }
+            const float maxSpeedSquared = trig.x * trig.x;
+            if (type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED) {
+                const float mass = 1 / (A.s.invMass + usedSoftness);
+                j.L(kJL0, s) = make_float4(mass, usedSoftness, maxForceDt, maxForceDtSquared);
+                j.L(kJL1, s) = make_float4(trig.x, maxSpeedSquared, 0.f, 0.f);
+            } else {
+                JM3 m = JInertia(A.s);
+                m.M11 += usedSoftness;
+                m.M22 += usedSoftness;
+                m.M33 += usedSoftness;
+                const JM3 inv = JInvert(m);
+                j.L(kJL0, s) = make_float4(usedSoftness, maxForceDt, maxForceDtSquared, trig.x);
+                j.L(kJL1, s) = make_float4(inv.M11, inv.M12, inv.M13, inv.M21);
+                j.L(kJL2, s) = make_float4(inv.M22, inv.M23, inv.M31, inv.M32);
+                j.L(kJOA, s) = make_float4(inv.M33, maxSpeedSquared, 0.f, 0.f);
+            }
         } else if (kAdded && IsMotorType(type)) {
             // RevoluteMotor.Update (RevoluteMotor.cs:243-290), TwistMotor.Update (TwistMotor.cs:182-224),
             // LinearAxisMotor.Update (LinearAxisMotor.cs:285-368).  Inputs: kJTRIG wrapped servo
@@ -1232,7 +1267,11 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+        if (kAdded && IsSpeedLimitType(type)) {
+            // ExclusiveUpdate (MaximumLinearVelocityConstraint.cs:195-199): no warm start, the
+            // accumulated impulse starts the iterations from zero
+            j.L(kJACC0, s) = make_float4(0.f, 0.f, 0.f, acc0.w);
+        } else if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
             // LinearAxisMotor.ExclusiveUpdate (LinearAxisMotor.cs:370-390)
             const float4 jaa = j.L(kJL1, s), jab = j.L(kJL2, s);
             const float a = acc1.y;
@@ -1512,7 +1551,58 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
+        if (kAdded && IsSpeedLimitType(type)) {
+            // MaximumLinearSpeedConstraint / MaximumAngularSpeedConstraint.SolveIteration
+            // (MaximumLinearVelocityConstraint.cs:138-175 and the angular file's)
+            const bool angular = type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED;
+            const float4 l1 = j.L(kJL1, s);
+            float usedSoftness, maxForceDt, maxForceDtSquared, maxSpeed, maxSpeedSquared;
+            if (angular) {
+                const float4 oa = j.L(kJOA, s);
+                usedSoftness = l0.x; maxForceDt = l0.y; maxForceDtSquared = l0.z; maxSpeed = l0.w;
+                maxSpeedSquared = oa.y;
+            } else {
+                usedSoftness = l0.y; maxForceDt = l0.z; maxForceDtSquared = l0.w; maxSpeed = l1.x;
+                maxSpeedSquared = l1.y;
+            }
+            const float vx = angular ? A.wx : A.vx, vy = angular ? A.wy : A.vy, vz = angular ? A.wz : A.vz;
+            float speed = vx * vx + vy * vy + vz * vz;
+            float result = 0;
+            if (speed > maxSpeedSquared) {
+                speed = SqrtOfFloat(speed);
+                const float f = -(speed - maxSpeed) / speed;
+                float ix = vx * f, iy = vy * f, iz = vz * f;
+                ix = ix - acc0.x * usedSoftness;
+                iy = iy - acc0.y * usedSoftness;
+                iz = iz - acc0.z * usedSoftness;
+                if (angular) {
+                    const float4 oa = j.L(kJOA, s);
+                    const JM3 m = {l1.x, l1.y, l1.z, l1.w, l2.x, l2.y, l2.z, l2.w, oa.x};
+                    const float3 t = JTransform(make_float3(ix, iy, iz), m);
+                    ix = t.x; iy = t.y; iz = t.z;
+                } else {
+                    ix *= l0.x; iy *= l0.x; iz *= l0.x;
+                }
+                const float px = acc0.x, py = acc0.y, pz = acc0.z;
+                acc0.x = acc0.x + ix;
+                acc0.y = acc0.y + iy;
+                acc0.z = acc0.z + iz;
+                const float forceMagnitude = acc0.x * acc0.x + acc0.y * acc0.y + acc0.z * acc0.z;
+                if (forceMagnitude > maxForceDtSquared) {
+                    const float multiplier = maxForceDt / SqrtOfFloat(forceMagnitude);
+                    acc0.x *= multiplier;
+                    acc0.y *= multiplier;
+                    acc0.z *= multiplier;
+                    ix = acc0.x - px;
+                    iy = acc0.y - py;
+                    iz = acc0.z - pz;
+                }
+                if (angular) ApplyAngular(A, ix, iy, iz);
+                else ApplyLinear(A, ix, iy, iz);
+                result = fabsf(ix) + fabsf(iy) + fabsf(iz);
+            }
+            account(2, result);
+        } else if (kAdded && type == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR) {
             // LinearAxisMotor.SolveIteration (LinearAxisMotor.cs:244-283)
             const float4 jaa = j.L(kJL1, s), jab = j.L(kJL2, s);
             const float maxForceDt = j.L(kJOA, s).x;

@@ -158,7 +158,9 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_SWIVEL_HINGE = 20,    /* SwivelHingeJoint group: ball socket + swivel hinge angular */
     BEPUGPU_JOINT_REVOLUTE_MOTOR = 21,  /* RevoluteMotor.cs:243-340 */
     BEPUGPU_JOINT_TWIST_MOTOR = 22,     /* TwistMotor.cs:182-253 */
-    BEPUGPU_JOINT_LINEAR_AXIS_MOTOR = 23 /* LinearAxisMotor.cs:244-390 */
+    BEPUGPU_JOINT_LINEAR_AXIS_MOTOR = 23, /* LinearAxisMotor.cs:244-390 */
+    BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED = 24, /* MaximumLinearSpeedConstraint (SingleEntity/MaximumLinearVelocityConstraint.cs:138-199) */
+    BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25 /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
@@ -231,8 +233,13 @@ typedef enum bepugpu_joint_type {
  *   bounce_velocity_threshold  maximum force (FLT_MAX)
  *   max_corrective_velocity    servo max corrective velocity
  *   spring_stiffness/damping   servo spring settings
- *   flags & BEPUGPU_JOINT_SERVO  servomechanism mode.  axis_a/b and constrained_1/2 of a LINE_SLIDER are its
- *                     RevoluteAngularJoint's; orientation_a/b of a PRISMATIC its NoRotationJoint's. */
+ *   flags & BEPUGPU_JOINT_SERVO  servomechanism mode.
+ * The single-entity speed limits (MAXIMUM_LINEAR_SPEED, MAXIMUM_ANGULAR_SPEED) act on
+ * body_a; body_b must be -1.  limit_min = MaximumSpeed, limit_max = MaximumForce
+ * (FLT_MAX = unlimited), margin = Softness (0.00001); impulse [0..2] is the
+ * accumulated impulse of the current step (no warm start: it starts from zero).
+ * axis_a/b and constrained_1/2 of a LINE_SLIDER are its RevoluteAngularJoint's;
+ * orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {
     int32_t type;                    /* bepugpu_joint_type */
     int32_t body_a;

@@ -180,6 +180,8 @@ NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTAN
              N.JOINT_SWIVEL_HINGE_ANGULAR, N.JOINT_SWIVEL_HINGE, N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR,
              N.JOINT_LINEAR_AXIS_MOTOR)
 MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
+SPEED_LIMITS = (N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED)
+NEW_TYPES = NEW_TYPES + SPEED_LIMITS
 
 
 def _unit(v):
@@ -278,6 +280,11 @@ def _convert(b, j, types, seed):
             j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
             j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        if t in SPEED_LIMITS:  # single-entity: on the link, the world as body B
+            j["body_a"][k], j["body_b"][k] = (bb if a < 0 else a), -1
+            j["limit_min"][k] = rng.uniform(0.0, 0.2) if t == N.JOINT_MAXIMUM_LINEAR_SPEED else rng.uniform(0.0, 0.5)
+            j["limit_max"][k] = rng.choice([np.finfo(np.float32).max, 2.0])
+            j["margin"][k] = 0.00001
         if t in MOTORS:
             servo = rng.random() < 0.5
             j["flags"][k] |= N.JOINT_SERVO if servo else 0
@@ -342,18 +349,26 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
     b, m, j = _small_chains(seed=22, chains=16, loose=60)
     j = _convert(b, j, (jtype,), 22)
     j["impulse"] = np.random.default_rng(5).uniform(0, 0.05, j["impulse"].shape).astype(np.float32)
+    if jtype in SPEED_LIMITS:  # spinning links, so the angular speed limits have work too
+        b = b.copy()
+        dyn = b["is_dynamic"] == 1
+        b["angular_velocity"][dyn] = np.random.default_rng(6).uniform(-2, 2, (int(dyn.sum()), 3))
     p = Pair(gpu_context, b, m, j, settings=_settings())
     for step in range(5):
         p.step()
         errs, exact = p.compare()
         assert exact, (jtype, step, errs)
+        if step == 0:  # speed limits start from zero each step: the first one shows their work
+            first = p.oracle.get_constraints()[1]["impulse"]
     limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_ELLIPSE_SWING_LIMIT: 0,
                    N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4, N.JOINT_REVOLUTE_MOTOR: 0,
-                   N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0}
+                   N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0, N.JOINT_MAXIMUM_LINEAR_SPEED: 0,
+                   N.JOINT_MAXIMUM_ANGULAR_SPEED: 2}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
-        got = p.oracle.get_constraints()[1]["impulse"][:, e]
-        assert np.count_nonzero((got != j["impulse"][:, e]) & (got != 0)) > 0
+        e = slice(0, 3) if jtype in SPEED_LIMITS else slice(e, e + 1)
+        got = (first if jtype in SPEED_LIMITS else p.oracle.get_constraints()[1]["impulse"])[:, e]
+        assert np.count_nonzero(np.any((got != j["impulse"][:, e]) & (got != 0), axis=1)) > 0
     p.close()
 
 

@@ -494,3 +494,43 @@ def test_twist_servo_motor_closed_form():
     lam = -0.3 * erp / (soft + 4.0)
     np.testing.assert_allclose(oj["impulse"][0, 0], lam, rtol=1e-4)
     np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, 4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def _speed_limit(jtype, max_speed, max_force=np.finfo(np.float32).max):
+    j = _joint(jtype, 0, -1)
+    j["limit_min"], j["limit_max"], j["margin"] = max_speed, max_force, 0.00001
+    return j
+
+
+@pytest.mark.parametrize("max_force,scale", [(np.finfo(np.float32).max, None), (60.0, 1.0)])
+def test_maximum_linear_speed_closed_form(max_force, scale):
+    """MaximumLinearSpeedConstraint (MaximumLinearVelocityConstraint.cs:138-193):
+    speed 5 against a maximum of 2 is cut by (5 - 2) / 5 of the velocity times
+    the effective mass 1 / (1/m + softness/dt); a maximum force scales the
+    accumulated impulse to force * dt."""
+    b = _body((0, 0, 0))
+    b["linear_velocity"] = (3.0, 4.0, 0.0)
+    ob, oj = _step(b, _speed_limit(N.JOINT_MAXIMUM_LINEAR_SPEED, 2.0, max_force))
+    imp = np.array([3.0, 4.0, 0.0]) * (-3.0 / 5.0) / (1.0 + 0.00001 * 60)
+    if scale is not None:
+        imp = imp / np.linalg.norm(imp) * scale  # 60 * dt
+    np.testing.assert_allclose(oj["impulse"][0, :3], imp, rtol=1e-4, atol=1e-7)
+    np.testing.assert_allclose(ob["linear_velocity"][0], np.array([3.0, 4.0, 0.0]) + imp, rtol=1e-4)
+
+
+def test_maximum_speeds_below_limit_and_angular():
+    """Below the maximum nothing acts and the stale impulse is cleared (no warm
+    start, :195-199); the angular form uses the inverse of (I^-1 + softness/dt)."""
+    b = _body((0, 0, 0))
+    b["linear_velocity"] = (1.0, 0.0, 0.0)
+    j = _speed_limit(N.JOINT_MAXIMUM_LINEAR_SPEED, 2.0)
+    j["impulse"][0, :3] = (0.5, 0.5, 0.5)
+    ob, oj = _step(b, j)
+    assert np.all(oj["impulse"][0, :3] == 0)
+    np.testing.assert_array_equal(ob["linear_velocity"][0], (1.0, 0.0, 0.0))
+    b = _body((0, 0, 0))
+    b["angular_velocity"] = (0.0, 0.0, 10.0)
+    ob, oj = _step(b, _speed_limit(N.JOINT_MAXIMUM_ANGULAR_SPEED, 4.0))
+    imp_z = -6.0 / (4.0 + 0.00001 * 60)
+    np.testing.assert_allclose(oj["impulse"][0, 2], imp_z, rtol=1e-4)
+    np.testing.assert_allclose(ob["angular_velocity"][0, 2], 10.0 + 4.0 * imp_z, rtol=1e-4)
