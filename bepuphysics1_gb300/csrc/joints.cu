@@ -48,7 +48,8 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_WELD: return kJChildBall | kJChildAngular;
         case BEPUGPU_JOINT_DISTANCE:
         case BEPUGPU_JOINT_DISTANCE_LIMIT:
-        case BEPUGPU_JOINT_POINT_ON_PLANE: return kJChildBall;
+        case BEPUGPU_JOINT_POINT_ON_PLANE:
+        case BEPUGPU_JOINT_PLANE_SLIDER: return kJChildBall;
         case BEPUGPU_JOINT_TWIST: return kJChildAngular;
         case BEPUGPU_JOINT_POINT_ON_LINE: return kJChildBall;
         case BEPUGPU_JOINT_PRISMATIC:
@@ -227,6 +228,7 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_DISTANCE:
             case BEPUGPU_JOINT_DISTANCE_LIMIT:
             case BEPUGPU_JOINT_POINT_ON_PLANE:
+            case BEPUGPU_JOINT_PLANE_SLIDER:
                 ball[0] = r.impulse[0];
                 break;
             case BEPUGPU_JOINT_TWIST:
@@ -340,6 +342,7 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
             case BEPUGPU_JOINT_DISTANCE:
             case BEPUGPU_JOINT_DISTANCE_LIMIT:
             case BEPUGPU_JOINT_POINT_ON_PLANE:
+            case BEPUGPU_JOINT_PLANE_SLIDER:
                 r.impulse[0] = a0.x;
                 break;
             case BEPUGPU_JOINT_TWIST:

@@ -24,6 +24,8 @@
 //   RevoluteMotor, TwistMotor, LinearAxisMotor  TwoEntity/Motors/*.cs (the limit slot)
 //   MaximumLinearSpeedConstraint, MaximumAngularSpeedConstraint
 //                         SingleEntity/Maximum*VelocityConstraint.cs (the limit slot, body B the world)
+//   PlaneSliderJoint      SolverGroups/PlaneSliderJoint.cs: its point on plane joint (its limits
+//                         and motors are constructed inactive)
 //   SwivelHingeAngularJoint  TwoEntity/Joints/SwivelHingeAngularJoint.cs:193-287 (the angular
 //                         slot; SWIVEL_HINGE is the group of a ball socket and it)
 //   LinearAxisLimit       TwoEntity/JointLimits/LinearAxisLimit.cs:290-466 (the limit slot;
@@ -114,6 +116,9 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+__device__ __forceinline__ bool IsPointOnPlaneType(int type) {
+    return type == BEPUGPU_JOINT_POINT_ON_PLANE || type == BEPUGPU_JOINT_PLANE_SLIDER;
 }
 __device__ __forceinline__ bool IsSpeedLimitType(int type) {
     return type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED;
@@ -453,7 +458,7 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         j.L(kJM1, s) = make_float4(ax2.x, ax2.y, ax2.z, -i12);
         j.L(kJM2, s) = make_float4(-i21, -i22, bx, by);
         st |= 1u << (kChildShift + 0);
-    } else if (kAdded && (active & kJChildBall) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (active & kJChildBall) && IsPointOnPlaneType(type)) {
         // PointOnPlaneJoint.Update (PointOnPlaneJoint.cs:250-306).  Lanes: kJOA rA + softness,
         // kJOB.xyz rB, kJM0 normal + negative effective mass, kJM1 rA x n + bias, kJM2 -(rB x n).
         const float3 n = JTransform(JXYZ(axa), A.R);
@@ -1200,7 +1205,7 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     if (kAdded && (st & (1u << kChildShift)) && IsPointOnLineType(type)) {
         // PointOnLineJoint.ExclusiveUpdate (PointOnLineJoint.cs:440-463)
         ApplyPointOnLine(j.L(kJOA, s), j.L(kJOB, s), j.L(kJM0, s), j.L(kJM1, s), acc0.x, acc0.y, dynA, dynB, A, B);
-    } else if (kAdded && (st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (st & (1u << kChildShift)) && IsPointOnPlaneType(type)) {
         // PointOnPlaneJoint.ExclusiveUpdate (PointOnPlaneJoint.cs:308-328)
         const float4 m0 = j.L(kJM0, s), m1 = j.L(kJM1, s), m2 = j.L(kJM2, s);
         const float a = acc0.x;
@@ -1374,7 +1379,7 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
         acc0.y = y + acc0.y;
         ApplyPointOnLine(oa, ob, m0, m1, x, y, dynA, dynB, A, B);
         account(0, fabsf(x) + fabsf(y));
-    } else if (kAdded && (st & (1u << kChildShift)) && type == BEPUGPU_JOINT_POINT_ON_PLANE) {
+    } else if (kAdded && (st & (1u << kChildShift)) && IsPointOnPlaneType(type)) {
         // PointOnPlaneJoint.SolveIteration (PointOnPlaneJoint.cs:212-243)
         const float4 oa = j.L(kJOA, s), ob = j.L(kJOB, s), m0 = j.L(kJM0, s), m1 = j.L(kJM1, s),
                      m2 = j.L(kJM2, s);

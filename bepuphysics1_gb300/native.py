@@ -108,7 +108,7 @@ JOINT_POINT_ON_LINE, JOINT_PRISMATIC, JOINT_LINE_SLIDER, JOINT_UNIVERSAL = 12, 1
 JOINT_TWIST_LIMIT, JOINT_LINEAR_AXIS_LIMIT, JOINT_ELLIPSE_SWING_LIMIT = 16, 17, 18
 JOINT_SWIVEL_HINGE_ANGULAR, JOINT_SWIVEL_HINGE = 19, 20
 JOINT_REVOLUTE_MOTOR, JOINT_TWIST_MOTOR, JOINT_LINEAR_AXIS_MOTOR = 21, 22, 23
-JOINT_MAXIMUM_LINEAR_SPEED, JOINT_MAXIMUM_ANGULAR_SPEED = 24, 25
+JOINT_MAXIMUM_LINEAR_SPEED, JOINT_MAXIMUM_ANGULAR_SPEED, JOINT_PLANE_SLIDER = 24, 25, 26
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE, JOINT_SERVO = 1, 2, 4
 
 _P = ctypes.c_void_p

@@ -160,12 +160,14 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_TWIST_MOTOR = 22,     /* TwistMotor.cs:182-253 */
     BEPUGPU_JOINT_LINEAR_AXIS_MOTOR = 23, /* LinearAxisMotor.cs:244-390 */
     BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED = 24, /* MaximumLinearSpeedConstraint (SingleEntity/MaximumLinearVelocityConstraint.cs:138-199) */
-    BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25 /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
+    BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25, /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
+    BEPUGPU_JOINT_PLANE_SLIDER = 26     /* PlaneSliderJoint group: point on plane (POINT_ON_PLANE's fields) */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
- * are UniversalJoint's twist limit (:52) and SwivelHingeJoint's hinge and twist
- * limits (SwivelHingeJoint.cs:59-62).  The limits of REVOLUTE, PRISMATIC and
+ * are UniversalJoint's twist limit (:52), SwivelHingeJoint's hinge and twist
+ * limits (SwivelHingeJoint.cs:59-62) and PlaneSliderJoint's two limits
+ * (PlaneSliderJoint.cs:60-63).  The limits of REVOLUTE, PRISMATIC and
  * LINE_SLIDER records (a LinearAxisLimit on the line's anchors and direction
  * for the last two) follow BEPUGPU_JOINT_LIMIT_ACTIVE. */
 

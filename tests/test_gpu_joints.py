@@ -181,7 +181,7 @@ NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTAN
              N.JOINT_LINEAR_AXIS_MOTOR)
 MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
 SPEED_LIMITS = (N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED)
-NEW_TYPES = NEW_TYPES + SPEED_LIMITS
+NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER,)
 
 
 def _unit(v):
@@ -229,7 +229,7 @@ def _convert(b, j, types, seed):
             lo = d * rng.uniform(0.7, 1.02)
             j["limit_min"][k], j["limit_max"][k] = lo, lo + d * rng.uniform(0.0, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
-        elif t == N.JOINT_POINT_ON_PLANE:
+        elif t in (N.JOINT_POINT_ON_PLANE, N.JOINT_PLANE_SLIDER):
             n = rng.normal(size=3)
             j["axis_a"][k] = n / np.linalg.norm(n)
         elif t in (N.JOINT_POINT_ON_LINE, N.JOINT_PRISMATIC, N.JOINT_LINE_SLIDER):

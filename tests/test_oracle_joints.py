@@ -534,3 +534,17 @@ def test_maximum_speeds_below_limit_and_angular():
     imp_z = -6.0 / (4.0 + 0.00001 * 60)
     np.testing.assert_allclose(oj["impulse"][0, 2], imp_z, rtol=1e-4)
     np.testing.assert_allclose(ob["angular_velocity"][0, 2], 10.0 + 4.0 * imp_z, rtol=1e-4)
+
+
+def test_plane_slider_is_its_point_on_plane_joint():
+    """PlaneSliderJoint (PlaneSliderJoint.cs:48-69) with its limits and motors
+    inactive, as constructed: a group of its point on plane joint alone."""
+    b = _body((0.3, 0.1, -0.2))
+    j = _joint(N.JOINT_POINT_ON_PLANE, -1, 0)
+    j["axis_a"] = (0, 1, 0)
+    g = j.copy()
+    g["type"] = N.JOINT_PLANE_SLIDER
+    ob, oj = _step(b, j)
+    og_b, og = _step(b, g)
+    assert og["impulse"][0, 0] == oj["impulse"][0, 0] != 0
+    np.testing.assert_array_equal(og_b["linear_velocity"], ob["linear_velocity"])
