@@ -64,7 +64,8 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_TWIST_MOTOR:
         case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
         case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
-        case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED: return kJChildLimit;
+        case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
+        case BEPUGPU_JOINT_ANGULAR_MOTOR: return kJChildLimit;
         default: return 0;
     }
 }
@@ -180,6 +181,16 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             auto clamp = [](float v) { return v < 1e-5f ? 1e-5f : (v > kHostPi ? kHostPi : v); };
             at(kJTRIG, slot) = make_float4(clamp(r.limit_min), clamp(r.limit_max), 0.f, 0.f);
         }
+        if (r.type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
+            // MotorSettings3D / ServoSettingsOrientation through their setters (MotorSettings.cs)
+            const float softness = r.margin < 0 ? 0.f : r.margin;
+            const float base = r.bounciness < 0 ? 0.f : r.bounciness;
+            const float maxForce = r.bounce_velocity_threshold >= 0 ? r.bounce_velocity_threshold : 0.f;
+            at(kJTRIG, slot) = make_float4(softness, base, maxForce, maxCorrSq);
+            at(kJTA, slot) = make_float4(r.orientation_a[0], r.orientation_a[1], r.orientation_a[2],
+                                         r.orientation_a[3]);
+            at(kJAXB, slot) = F4(r.axis_b, (r.flags & BEPUGPU_JOINT_SERVO) ? 1.f : 0.f);
+        }
         if (r.type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || r.type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED) {
             // MaximumSpeed, MaximumForce and Softness setters (MaximumLinearVelocityConstraint.cs:32-59)
             const float speed = 0 > r.limit_min ? 0.f : r.limit_min;
@@ -264,6 +275,7 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
                 break;
             case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
             case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
+            case BEPUGPU_JOINT_ANGULAR_MOTOR:
                 std::memcpy(ball, r.impulse, 12);
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
@@ -380,6 +392,7 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
                 break;
             case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
             case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
+            case BEPUGPU_JOINT_ANGULAR_MOTOR:
                 r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:

@@ -22,6 +22,7 @@
 //                         last error, which picks the next jacobian's sign, in kJACC1.w)
 //   EllipseSwingLimit     TwoEntity/JointLimits/EllipseSwingLimit.cs:162-357 (the limit slot)
 //   RevoluteMotor, TwistMotor, LinearAxisMotor  TwoEntity/Motors/*.cs (the limit slot)
+//   AngularMotor          TwoEntity/Motors/AngularMotor.cs:203-326 (the limit slot)
 //   MaximumLinearSpeedConstraint, MaximumAngularSpeedConstraint
 //                         SingleEntity/Maximum*VelocityConstraint.cs (the limit slot, body B the world)
 //   PlaneSliderJoint      SolverGroups/PlaneSliderJoint.cs: its point on plane joint (its limits
@@ -116,6 +117,30 @@ __device__ __forceinline__ bool IsPointOnLineType(int type) {
 }
 __device__ __forceinline__ bool IsTwistType(int type) {
     return type == BEPUGPU_JOINT_TWIST || type == BEPUGPU_JOINT_UNIVERSAL;
+}
+// Quaternion.Concatenate (BEPUutilities/Quaternion.cs:101-117)
+__device__ __forceinline__ float4 JQConcat(float4 a, float4 b) {
+    return make_float4(a.w * b.x + a.x * b.w + a.z * b.y - a.y * b.z, a.w * b.y + a.y * b.w + a.x * b.z - a.z * b.x,
+                       a.w * b.z + a.z * b.w + a.y * b.x - a.x * b.y, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z);
+}
+// Quaternion.CreateFromRotationMatrix (BEPUutilities/Quaternion.cs:152-194) of the
+// matrix with rows Right r, Up u, Backward k.
+__device__ __forceinline__ float4 JQFromRows(float3 r, float3 u, float3 k) {
+    const float trace = r.x + u.y + k.z;
+    if (trace >= 0) {
+        const float S = (float)sqrt((double)trace + 1.0) * 2, inverseS = 1 / S;
+        return make_float4((u.z - k.y) * inverseS, (k.x - r.z) * inverseS, (r.y - u.x) * inverseS, 0.25f * S);
+    }
+    if ((r.x > u.y) & (r.x > k.z)) {
+        const float S = (float)sqrt(1.0 + (double)r.x - (double)u.y - (double)k.z) * 2, inverseS = 1 / S;
+        return make_float4(0.25f * S, (u.x + r.y) * inverseS, (k.x + r.z) * inverseS, (u.z - k.y) * inverseS);
+    }
+    if (u.y > k.z) {
+        const float S = (float)sqrt(1.0 + (double)u.y - (double)r.x - (double)k.z) * 2, inverseS = 1 / S;
+        return make_float4((u.x + r.y) * inverseS, 0.25f * S, (k.y + u.z) * inverseS, (k.x - r.z) * inverseS);
+    }
+    const float S = (float)sqrt(1.0 + (double)k.z - (double)r.x - (double)u.y) * 2, inverseS = 1 / S;
+    return make_float4((k.x + r.z) * inverseS, (k.y + u.z) * inverseS, 0.25f * S, (r.y - u.x) * inverseS);
 }
 __device__ __forceinline__ bool IsPointOnPlaneType(int type) {
     return type == BEPUGPU_JOINT_POINT_ON_PLANE || type == BEPUGPU_JOINT_PLANE_SLIDER;
@@ -809,6 +834,62 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                     j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
                 }
             }
+        } else if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
+            // AngularMotor.Update (AngularMotor.cs:248-312).  Inputs: basis primary / x / y
+            // (kJAXA, kJC1, kJC2), the servo goal kJTA (x y z w), the goal velocity kJLA.xyz,
+            // kJTRIG velocity softness, base corrective speed, maximum force, servo max corrective
+            // velocity squared; kJAXB.w 1 in servo mode.  Lanes: kJL0..kJL2 the effective mass
+            // and the bias velocity, kJOA used softness, maxForceDt, its square.  Impulse kJACC0.xyz.
+            const float4 trig = ji.L(kJTRIG, si);
+            const bool servo = axb.w != 0.f;
+            const float3 primary = JTransform(JXYZ(axa), A.R), xAxis = JTransform(JXYZ(ji.L(kJC1, si)), A.R);
+            const float3 yAxis = JTransform(JXYZ(ji.L(kJC2, si)), A.R);
+            const float inverseDt = 1 / p.dt;
+            float usedSoftness;
+            float3 bias;
+            if (servo) {
+                const float4 worldBasis = JQFromRows(xAxis, yAxis, primary);
+                const float4 bTarget = JQConcat(ji.L(kJTA, si), worldBasis);
+                const float4 conj = make_float4(-bTarget.x, -bTarget.y, -bTarget.z, bTarget.w);
+                const float4 error = JQConcat(conj, B.q);
+                JSpring(stiffness, damping, p.dt, inverseDt, erp, usedSoftness);
+                float3 axis;
+                float angle;
+                JAxisAngle(error, axis, angle);
+                if (angle > 1e-5f) {
+                    const float velocity = -(Minf(trig.y, angle * inverseDt) + angle * erp);
+                    bias = make_float3(axis.x * velocity, axis.y * velocity, axis.z * velocity);
+                    const float length = bias.x * bias.x + bias.y * bias.y + bias.z * bias.z;
+                    if (length > trig.w) {
+                        const float multiplier = maxCorr / SqrtOfFloat(length);
+                        bias = make_float3(bias.x * multiplier, bias.y * multiplier, bias.z * multiplier);
+                    }
+                } else {
+                    bias = make_float3(0.f, 0.f, 0.f);
+                }
+            } else {
+                usedSoftness = trig.x * inverseDt;
+                const float3 g = JXYZ(la);
+                bias = make_float3(g.x * xAxis.x + g.y * yAxis.x + g.z * primary.x,
+                                   g.x * xAxis.y + g.y * yAxis.y + g.z * primary.y,
+                                   g.x * xAxis.z + g.y * yAxis.z + g.z * primary.z);
+            }
+            const JM3 ia = JInertia(A.s), ib = JInertia(B.s);  // Matrix3x3.Add, whatever the connections
+            JM3 k = {ia.M11 + ib.M11, ia.M12 + ib.M12, ia.M13 + ib.M13, ia.M21 + ib.M21, ia.M22 + ib.M22,
+                     ia.M23 + ib.M23, ia.M31 + ib.M31, ia.M32 + ib.M32, ia.M33 + ib.M33};
+            k.M11 += usedSoftness;
+            k.M22 += usedSoftness;
+            k.M33 += usedSoftness;
+            const JM3 mass = JInvert(k);
+            float maxForceDt = 3.40282347e+38f, maxForceDtSquared = 3.40282347e+38f;
+            if (trig.z < 3.40282347e+38f) {
+                maxForceDt = trig.z * p.dt;
+                maxForceDtSquared = maxForceDt * maxForceDt;
+            }
+            j.L(kJL0, s) = make_float4(mass.M11, mass.M12, mass.M13, mass.M21);
+            j.L(kJL1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
+            j.L(kJL2, s) = make_float4(mass.M33, bias.x, bias.y, bias.z);
+            j.L(kJOA, s) = make_float4(usedSoftness, maxForceDt, maxForceDtSquared, 0.f);
         } else if (kAdded && IsSpeedLimitType(type)) {
             // MaximumLinearSpeedConstraint / MaximumAngularSpeedConstraint.Update
             // (MaximumLinearVelocityConstraint.cs:177-193 and the angular file's).  Inputs: kJTRIG
@@ -1272,7 +1353,11 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && IsSpeedLimitType(type)) {
+        if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
+            // AngularMotor.ExclusiveUpdate (AngularMotor.cs:314-326)
+            if (dynA) ApplyAngular(A, acc0.x, acc0.y, acc0.z);
+            if (dynB) ApplyAngular(B, -acc0.x, -acc0.y, -acc0.z);
+        } else if (kAdded && IsSpeedLimitType(type)) {
             // ExclusiveUpdate (MaximumLinearVelocityConstraint.cs:195-199): no warm start, the
             // accumulated impulse starts the iterations from zero
             j.L(kJACC0, s) = make_float4(0.f, 0.f, 0.f, acc0.w);
@@ -1556,7 +1641,34 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && IsSpeedLimitType(type)) {
+        if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
+            // AngularMotor.SolveIteration (AngularMotor.cs:203-246)
+            const float4 l1 = j.L(kJL1, s), oa = j.L(kJOA, s);
+            const float us = oa.x;
+            float lx = B.wx - A.wx - l2.y - us * acc0.x;
+            float ly = B.wy - A.wy - l2.z - us * acc0.y;
+            float lz = B.wz - A.wz - l2.w - us * acc0.z;
+            const JM3 m = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w, l2.x};
+            const float3 t = JTransform(make_float3(lx, ly, lz), m);
+            lx = t.x; ly = t.y; lz = t.z;
+            const float px = acc0.x, py = acc0.y, pz = acc0.z;
+            acc0.x += lx;
+            acc0.y += ly;
+            acc0.z += lz;
+            const float sumLengthSquared = acc0.x * acc0.x + acc0.y * acc0.y + acc0.z * acc0.z;
+            if (sumLengthSquared > oa.z) {
+                const float multiplier = oa.y / SqrtOfFloat(sumLengthSquared);
+                acc0.x *= multiplier;
+                acc0.y *= multiplier;
+                acc0.z *= multiplier;
+                lx = acc0.x - px;
+                ly = acc0.y - py;
+                lz = acc0.z - pz;
+            }
+            if (dynA) ApplyAngular(A, lx, ly, lz);
+            if (dynB) ApplyAngular(B, -lx, -ly, -lz);
+            account(2, fabsf(lx) + fabsf(ly) + fabsf(lz));
+        } else if (kAdded && IsSpeedLimitType(type)) {
             // MaximumLinearSpeedConstraint / MaximumAngularSpeedConstraint.SolveIteration
             // (MaximumLinearVelocityConstraint.cs:138-175 and the angular file's)
             const bool angular = type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED;

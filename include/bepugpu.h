@@ -161,7 +161,8 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_LINEAR_AXIS_MOTOR = 23, /* LinearAxisMotor.cs:244-390 */
     BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED = 24, /* MaximumLinearSpeedConstraint (SingleEntity/MaximumLinearVelocityConstraint.cs:138-199) */
     BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25, /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
-    BEPUGPU_JOINT_PLANE_SLIDER = 26     /* PlaneSliderJoint group: point on plane (POINT_ON_PLANE's fields) */
+    BEPUGPU_JOINT_PLANE_SLIDER = 26,    /* PlaneSliderJoint group: point on plane (POINT_ON_PLANE's fields) */
+    BEPUGPU_JOINT_ANGULAR_MOTOR = 27    /* AngularMotor.cs:203-326 */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
@@ -240,6 +241,10 @@ typedef enum bepugpu_joint_type {
  * body_a; body_b must be -1.  limit_min = MaximumSpeed, limit_max = MaximumForce
  * (FLT_MAX = unlimited), margin = Softness (0.00001); impulse [0..2] is the
  * accumulated impulse of the current step (no warm start: it starts from zero).
+ * An ANGULAR_MOTOR takes its basis from axis_a (primary), constrained_1 (x) and
+ * constrained_2 (y) in A's frame, the servo goal (a relative orientation) from
+ * orientation_a, the velocity goal (in the basis) from anchor_a, its other
+ * MotorSettings as the 1-D motors do; impulse [0..2].
  * axis_a/b and constrained_1/2 of a LINE_SLIDER are its RevoluteAngularJoint's;
  * orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {

@@ -181,7 +181,7 @@ NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTAN
              N.JOINT_LINEAR_AXIS_MOTOR)
 MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
 SPEED_LIMITS = (N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED)
-NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER,)
+NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER, N.JOINT_ANGULAR_MOTOR)
 
 
 def _unit(v):
@@ -280,6 +280,21 @@ def _convert(b, j, types, seed):
             j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
             j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
+        if t == N.JOINT_ANGULAR_MOTOR:
+            ra = _rows(qa)
+            ax = _unit(rng.normal(size=3))
+            x = _unit(np.cross(ax, rng.normal(size=3)))
+            y = np.cross(ax, x)
+            j["axis_a"][k], j["constrained_1"][k], j["constrained_2"][k] = ax @ ra.T, x @ ra.T, y @ ra.T
+            servo = rng.random() < 0.5
+            j["flags"][k] |= N.JOINT_SERVO if servo else 0
+            g = _unit(rng.normal(size=4))
+            j["orientation_a"][k] = g if g[3] >= 0 else -g
+            j["anchor_a"][k] = rng.uniform(-1, 1, 3)
+            j["margin"][k] = 0.0001
+            j["bounciness"][k] = rng.choice([0.0, 0.3])
+            j["bounce_velocity_threshold"][k] = rng.choice([np.finfo(np.float32).max, 5.0])
+            j["max_corrective_velocity"][k] = rng.choice([np.finfo(np.float32).max, 2.0])
         if t in SPEED_LIMITS:  # single-entity: on the link, the world as body B
             j["body_a"][k], j["body_b"][k] = (bb if a < 0 else a), -1
             j["limit_min"][k] = rng.uniform(0.0, 0.2) if t == N.JOINT_MAXIMUM_LINEAR_SPEED else rng.uniform(0.0, 0.5)
@@ -363,10 +378,10 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
     limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_ELLIPSE_SWING_LIMIT: 0,
                    N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4, N.JOINT_REVOLUTE_MOTOR: 0,
                    N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0, N.JOINT_MAXIMUM_LINEAR_SPEED: 0,
-                   N.JOINT_MAXIMUM_ANGULAR_SPEED: 2}
+                   N.JOINT_MAXIMUM_ANGULAR_SPEED: 2, N.JOINT_ANGULAR_MOTOR: 0}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
-        e = slice(0, 3) if jtype in SPEED_LIMITS else slice(e, e + 1)
+        e = slice(0, 3) if jtype in SPEED_LIMITS + (N.JOINT_ANGULAR_MOTOR,) else slice(e, e + 1)
         got = (first if jtype in SPEED_LIMITS else p.oracle.get_constraints()[1]["impulse"])[:, e]
         assert np.count_nonzero(np.any((got != j["impulse"][:, e]) & (got != 0), axis=1)) > 0
     p.close()

@@ -548,3 +548,34 @@ def test_plane_slider_is_its_point_on_plane_joint():
     og_b, og = _step(b, g)
     assert og["impulse"][0, 0] == oj["impulse"][0, 0] != 0
     np.testing.assert_array_equal(og_b["linear_velocity"], ob["linear_velocity"])
+
+
+def _angular_motor(servo=False):
+    j = _motor(N.JOINT_ANGULAR_MOTOR, servo=servo)
+    j["axis_a"], j["constrained_1"], j["constrained_2"] = (0, 0, 1), (1, 0, 0), (0, 1, 0)
+    j["orientation_a"] = (0, 0, 0, 1)  # servo goal: the identity relative orientation
+    return j
+
+
+def test_angular_velocity_motor_closed_form():
+    """AngularMotor in velocity mode (AngularMotor.cs:203-312): goal (0, 0, 2)
+    in the basis; the impulse is (I_A^-1 + I_B^-1 + softness/dt)^-1 times
+    (w_B - w_A - bias), applied to A and negated on B."""
+    b = _body((0, 0, 0))
+    j = _angular_motor()
+    j["anchor_a"] = (0, 0, 2.0)
+    ob, oj = _step(b, j)
+    lam = -2.0 / (4.0 + 0.0001 * 60)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam), rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def test_angular_servo_motor_closed_form():
+    """AngularMotor as a servo: B turned 0.2 about z from the goal (identity in
+    a world basis) gets the bias -(0.2 erp) about z and turns back."""
+    b = _body((0, 0, 0), quat=_rot_z(0.2))
+    ob, oj = _step(b, _angular_motor(servo=True))
+    erp, soft = _spring(float(DT))
+    lam = 0.2 * erp / (4.0 + soft)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam), rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
