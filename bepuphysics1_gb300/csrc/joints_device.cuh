@@ -145,6 +145,9 @@ __device__ __forceinline__ float4 JQFromRows(float3 r, float3 u, float3 k) {
 __device__ __forceinline__ bool IsPointOnPlaneType(int type) {
     return type == BEPUGPU_JOINT_POINT_ON_PLANE || type == BEPUGPU_JOINT_PLANE_SLIDER;
 }
+__device__ __forceinline__ bool IsAngularMotorType(int type) {
+    return type == BEPUGPU_JOINT_ANGULAR_MOTOR || type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR;
+}
 __device__ __forceinline__ bool IsSpeedLimitType(int type) {
     return type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED;
 }
@@ -834,8 +837,10 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                     j.L(kJL2, s) = make_float4(bias, 0.f, v2i, 0.f);
                 }
             }
-        } else if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
-            // AngularMotor.Update (AngularMotor.cs:248-312).  Inputs: basis primary / x / y
+        } else if (kAdded && IsAngularMotorType(type)) {
+            // AngularMotor.Update (AngularMotor.cs:248-312); SingleEntityAngularMotor.Update
+            // (SingleEntityAngularMotor.cs:150-213) on body A alone: its servo error is
+            // goal * conjugate(basis), its corrective velocity positive.  Inputs: basis primary / x / y
             // (kJAXA, kJC1, kJC2), the servo goal kJTA (x y z w), the goal velocity kJLA.xyz,
             // kJTRIG velocity softness, base corrective speed, maximum force, servo max corrective
             // velocity squared; kJAXB.w 1 in servo mode.  Lanes: kJL0..kJL2 the effective mass
@@ -847,17 +852,24 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
             const float inverseDt = 1 / p.dt;
             float usedSoftness;
             float3 bias;
+            const bool single = type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR;
             if (servo) {
                 const float4 worldBasis = JQFromRows(xAxis, yAxis, primary);
-                const float4 bTarget = JQConcat(ji.L(kJTA, si), worldBasis);
-                const float4 conj = make_float4(-bTarget.x, -bTarget.y, -bTarget.z, bTarget.w);
-                const float4 error = JQConcat(conj, B.q);
+                float4 error;
+                if (single) {
+                    error = JQMul(ji.L(kJTA, si), make_float4(-worldBasis.x, -worldBasis.y, -worldBasis.z, worldBasis.w));
+                } else {
+                    const float4 bTarget = JQConcat(ji.L(kJTA, si), worldBasis);
+                    const float4 conj = make_float4(-bTarget.x, -bTarget.y, -bTarget.z, bTarget.w);
+                    error = JQConcat(conj, B.q);
+                }
                 JSpring(stiffness, damping, p.dt, inverseDt, erp, usedSoftness);
                 float3 axis;
                 float angle;
                 JAxisAngle(error, axis, angle);
                 if (angle > 1e-5f) {
-                    const float velocity = -(Minf(trig.y, angle * inverseDt) + angle * erp);
+                    float velocity = Minf(trig.y, angle * inverseDt) + angle * erp;
+                    if (!single) velocity = -velocity;
                     bias = make_float3(axis.x * velocity, axis.y * velocity, axis.z * velocity);
                     const float length = bias.x * bias.x + bias.y * bias.y + bias.z * bias.z;
                     if (length > trig.w) {
@@ -874,9 +886,12 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
                                    g.x * xAxis.y + g.y * yAxis.y + g.z * primary.y,
                                    g.x * xAxis.z + g.y * yAxis.z + g.z * primary.z);
             }
-            const JM3 ia = JInertia(A.s), ib = JInertia(B.s);  // Matrix3x3.Add, whatever the connections
-            JM3 k = {ia.M11 + ib.M11, ia.M12 + ib.M12, ia.M13 + ib.M13, ia.M21 + ib.M21, ia.M22 + ib.M22,
-                     ia.M23 + ib.M23, ia.M31 + ib.M31, ia.M32 + ib.M32, ia.M33 + ib.M33};
+            JM3 k = JInertia(A.s);  // Matrix3x3.Add of both connections' (whatever they are) for two
+            if (!single) {
+                const JM3 ib = JInertia(B.s);
+                k = {k.M11 + ib.M11, k.M12 + ib.M12, k.M13 + ib.M13, k.M21 + ib.M21, k.M22 + ib.M22,
+                     k.M23 + ib.M23, k.M31 + ib.M31, k.M32 + ib.M32, k.M33 + ib.M33};
+            }
             k.M11 += usedSoftness;
             k.M22 += usedSoftness;
             k.M33 += usedSoftness;
@@ -1353,8 +1368,9 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
-            // AngularMotor.ExclusiveUpdate (AngularMotor.cs:314-326)
+        if (kAdded && IsAngularMotorType(type)) {
+            // AngularMotor.ExclusiveUpdate (AngularMotor.cs:314-326), SingleEntityAngularMotor's
+            // (:215-218; B is the world there)
             if (dynA) ApplyAngular(A, acc0.x, acc0.y, acc0.z);
             if (dynB) ApplyAngular(B, -acc0.x, -acc0.y, -acc0.z);
         } else if (kAdded && IsSpeedLimitType(type)) {
@@ -1641,13 +1657,21 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && type == BEPUGPU_JOINT_ANGULAR_MOTOR) {
-            // AngularMotor.SolveIteration (AngularMotor.cs:203-246)
+        if (kAdded && IsAngularMotorType(type)) {
+            // AngularMotor.SolveIteration (AngularMotor.cs:203-246); SingleEntityAngularMotor's
+            // (SingleEntityAngularMotor.cs:117-148) adds its bias to -w_A
             const float4 l1 = j.L(kJL1, s), oa = j.L(kJOA, s);
             const float us = oa.x;
-            float lx = B.wx - A.wx - l2.y - us * acc0.x;
-            float ly = B.wy - A.wy - l2.z - us * acc0.y;
-            float lz = B.wz - A.wz - l2.w - us * acc0.z;
+            float lx, ly, lz;
+            if (type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR) {
+                lx = -A.wx + l2.y - us * acc0.x;
+                ly = -A.wy + l2.z - us * acc0.y;
+                lz = -A.wz + l2.w - us * acc0.z;
+            } else {
+                lx = B.wx - A.wx - l2.y - us * acc0.x;
+                ly = B.wy - A.wy - l2.z - us * acc0.y;
+                lz = B.wz - A.wz - l2.w - us * acc0.z;
+            }
             const JM3 m = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w, l2.x};
             const float3 t = JTransform(make_float3(lx, ly, lz), m);
             lx = t.x; ly = t.y; lz = t.z;

@@ -162,7 +162,8 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED = 24, /* MaximumLinearSpeedConstraint (SingleEntity/MaximumLinearVelocityConstraint.cs:138-199) */
     BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25, /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
     BEPUGPU_JOINT_PLANE_SLIDER = 26,    /* PlaneSliderJoint group: point on plane (POINT_ON_PLANE's fields) */
-    BEPUGPU_JOINT_ANGULAR_MOTOR = 27    /* AngularMotor.cs:203-326 */
+    BEPUGPU_JOINT_ANGULAR_MOTOR = 27,   /* AngularMotor.cs:203-326 */
+    BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR = 28 /* SingleEntityAngularMotor.cs:117-226: body_b -1, ANGULAR_MOTOR's fields */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so

@@ -181,7 +181,8 @@ NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTAN
              N.JOINT_LINEAR_AXIS_MOTOR)
 MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
 SPEED_LIMITS = (N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED)
-NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER, N.JOINT_ANGULAR_MOTOR)
+NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER, N.JOINT_ANGULAR_MOTOR,
+                                       N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR)
 
 
 def _unit(v):
@@ -280,7 +281,11 @@ def _convert(b, j, types, seed):
             j["axis_b"][k] = _unit(ax * np.cos(ang) + tilt * np.sin(ang)) @ rb.T
             j["limit_min"][k], j["limit_max"][k] = rng.uniform(0.005, 0.2), rng.uniform(0.005, 0.2)
             j["bounciness"][k] = rng.choice([0.0, 0.5])
-        if t == N.JOINT_ANGULAR_MOTOR:
+        if t == N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR:  # on the link, the world as body B
+            if a < 0:
+                a, qa = bb, qb
+            j["body_a"][k], j["body_b"][k] = a, -1
+        if t in (N.JOINT_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR):
             ra = _rows(qa)
             ax = _unit(rng.normal(size=3))
             x = _unit(np.cross(ax, rng.normal(size=3)))
@@ -378,10 +383,12 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
     limit_entry = {N.JOINT_TWIST_LIMIT: 0, N.JOINT_LINEAR_AXIS_LIMIT: 0, N.JOINT_ELLIPSE_SWING_LIMIT: 0,
                    N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4, N.JOINT_REVOLUTE_MOTOR: 0,
                    N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0, N.JOINT_MAXIMUM_LINEAR_SPEED: 0,
-                   N.JOINT_MAXIMUM_ANGULAR_SPEED: 2, N.JOINT_ANGULAR_MOTOR: 0}
+                   N.JOINT_MAXIMUM_ANGULAR_SPEED: 2, N.JOINT_ANGULAR_MOTOR: 0,
+                   N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR: 0}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
-        e = slice(0, 3) if jtype in SPEED_LIMITS + (N.JOINT_ANGULAR_MOTOR,) else slice(e, e + 1)
+        e = slice(0, 3) if jtype in SPEED_LIMITS + (N.JOINT_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR) \
+            else slice(e, e + 1)
         got = (first if jtype in SPEED_LIMITS else p.oracle.get_constraints()[1]["impulse"])[:, e]
         assert np.count_nonzero(np.any((got != j["impulse"][:, e]) & (got != 0), axis=1)) > 0
     p.close()

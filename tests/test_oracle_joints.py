@@ -579,3 +579,23 @@ def test_angular_servo_motor_closed_form():
     lam = 0.2 * erp / (4.0 + soft)
     np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam), rtol=1e-4, atol=1e-8)
     np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, -4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+@pytest.mark.parametrize("servo", [False, True])
+def test_single_entity_angular_motor_closed_form(servo):
+    """SingleEntityAngularMotor (SingleEntityAngularMotor.cs:117-218) on body A:
+    velocity goal (0, 0, 2) in its basis, or a servo back from 0.2 rad about z
+    to the identity goal; lambda = (I^-1 + softness/dt)^-1 (bias - w)."""
+    b = _body((0, 0, 0), quat=_rot_z(0.2) if servo else (0, 0, 0, 1))
+    j = _angular_motor(servo=servo)
+    j["type"], j["body_a"], j["body_b"] = N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR, 0, -1
+    j["axis_a"], j["constrained_1"], j["constrained_2"] = (0, 0, 1), (1, 0, 0), (0, 1, 0)
+    j["anchor_a"] = (0, 0, 2.0)
+    ob, oj = _step(b, j)
+    if servo:
+        erp, soft = _spring(float(DT))
+        lam = -0.2 * erp / (4.0 + soft)
+    else:
+        lam = 2.0 / (4.0 + 0.0001 * 60)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam), rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, 4.0 * lam), rtol=1e-4, atol=1e-8)
