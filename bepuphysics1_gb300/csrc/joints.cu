@@ -66,7 +66,8 @@ uint32_t ChildrenOf(int32_t type) {
         case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
         case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:
         case BEPUGPU_JOINT_ANGULAR_MOTOR:
-        case BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR: return kJChildLimit;
+        case BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR:
+        case BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR: return kJChildLimit;
         default: return 0;
     }
 }
@@ -101,7 +102,7 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
             return BEPUGPU_INVALID_ARGUMENT;
         }
         if ((r.type == BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED || r.type == BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED ||
-             r.type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR) &&
+             r.type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR || r.type == BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR) &&
             r.body_b != -1) {
             ctx->SetError("joint %u: a single-entity constraint acts on body_a alone (body_b must be -1)", u);
             return BEPUGPU_INVALID_ARGUMENT;
@@ -183,7 +184,8 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             auto clamp = [](float v) { return v < 1e-5f ? 1e-5f : (v > kHostPi ? kHostPi : v); };
             at(kJTRIG, slot) = make_float4(clamp(r.limit_min), clamp(r.limit_max), 0.f, 0.f);
         }
-        if (r.type == BEPUGPU_JOINT_ANGULAR_MOTOR || r.type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR) {
+        if (r.type == BEPUGPU_JOINT_ANGULAR_MOTOR || r.type == BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR ||
+            r.type == BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR) {
             // MotorSettings3D / ServoSettingsOrientation through their setters (MotorSettings.cs)
             const float softness = r.margin < 0 ? 0.f : r.margin;
             const float base = r.bounciness < 0 ? 0.f : r.bounciness;
@@ -280,6 +282,10 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
             case BEPUGPU_JOINT_ANGULAR_MOTOR:
             case BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR:
                 std::memcpy(ball, r.impulse, 12);
+                break;
+            case BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR:  // and the used softness it keeps
+                std::memcpy(ball, r.impulse, 12);
+                ang[1] = r.impulse[3];
                 break;
             case BEPUGPU_JOINT_SWIVEL_HINGE:
                 std::memcpy(ball, r.impulse, 12);
@@ -392,6 +398,10 @@ bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uin
             case BEPUGPU_JOINT_TWIST_MOTOR:
             case BEPUGPU_JOINT_LINEAR_AXIS_MOTOR:
                 r.impulse[0] = a1.y;
+                break;
+            case BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR:  // and the used softness it keeps
+                r.impulse[0] = a0.x; r.impulse[1] = a0.y; r.impulse[2] = a0.z;
+                r.impulse[3] = a1.x;
                 break;
             case BEPUGPU_JOINT_MAXIMUM_LINEAR_SPEED:
             case BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED:

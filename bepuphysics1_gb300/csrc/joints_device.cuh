@@ -905,6 +905,57 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
             j.L(kJL1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
             j.L(kJL2, s) = make_float4(mass.M33, bias.x, bias.y, bias.z);
             j.L(kJOA, s) = make_float4(usedSoftness, maxForceDt, maxForceDtSquared, 0.f);
+        } else if (kAdded && type == BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR) {
+            // SingleEntityLinearMotor.Update (SingleEntityLinearMotor.cs:210-268).  Inputs: the
+            // local point kJLA, the servo goal kJLB.xyz, the goal velocity kJAXA.xyz, kJTRIG and
+            // kJAXB.w as the angular motor's.  Lanes: kJL0..kJL2 effective mass and bias, kJOA
+            // used softness, maxForceDt, its square, kJOB.xyz r.  Impulse kJACC0.xyz; the used
+            // softness is kept in kJACC1.x (the servo leaves it while the point is at its goal).
+            const float4 trig = ji.L(kJTRIG, si);
+            const bool servo = axb.w != 0.f;
+            const float3 r = JTransform(JXYZ(la), A.R);
+            const float3 wp = make_float3(r.x + A.pos.x, r.y + A.pos.y, r.z + A.pos.z);
+            const float updateRate = 1 / p.dt;
+            float usedSoftness = acc1.x;
+            float3 bias;
+            if (servo) {
+                const float3 goal = JXYZ(lb);
+                const float3 error = make_float3(goal.x - wp.x, goal.y - wp.y, goal.z - wp.z);
+                const float sep = SqrtOfFloat(error.x * error.x + error.y * error.y + error.z * error.z);
+                if (sep > 1e-5f) {
+                    JSpring(stiffness, damping, p.dt, updateRate, erp, usedSoftness);
+                    const float cs = Minf(trig.y, sep * updateRate) + sep * erp;
+                    const float f = cs / sep;
+                    bias = make_float3(error.x * f, error.y * f, error.z * f);
+                    const float length = bias.x * bias.x + bias.y * bias.y + bias.z * bias.z;
+                    if (length > trig.w) {
+                        const float multiplier = maxCorr / SqrtOfFloat(length);
+                        bias = make_float3(bias.x * multiplier, bias.y * multiplier, bias.z * multiplier);
+                    }
+                } else {
+                    bias = make_float3(0.f, 0.f, 0.f);
+                }
+            } else {
+                usedSoftness = trig.x * updateRate;
+                bias = JXYZ(axa);
+            }
+            acc1.x = usedSoftness;
+            float maxForceDt = 3.40282347e+38f, maxForceDtSquared = 3.40282347e+38f;
+            if (trig.z < 3.40282347e+38f) {
+                maxForceDt = trig.z * p.dt;
+                maxForceDtSquared = maxForceDt * maxForceDt;
+            }
+            const JM3 rx = JCrossMatrix(r);
+            JM3 k = JSub(JScale(A.s.invMass), JMul(JMul(rx, JInertia(A.s)), rx));
+            k.M11 += usedSoftness;
+            k.M22 += usedSoftness;
+            k.M33 += usedSoftness;
+            const JM3 mass = JInvert(k);
+            j.L(kJL0, s) = make_float4(mass.M11, mass.M12, mass.M13, mass.M21);
+            j.L(kJL1, s) = make_float4(mass.M22, mass.M23, mass.M31, mass.M32);
+            j.L(kJL2, s) = make_float4(mass.M33, bias.x, bias.y, bias.z);
+            j.L(kJOA, s) = make_float4(usedSoftness, maxForceDt, maxForceDtSquared, 0.f);
+            j.L(kJOB, s) = make_float4(r.x, r.y, r.z, 0.f);
         } else if (kAdded && IsSpeedLimitType(type)) {
             // MaximumLinearSpeedConstraint / MaximumAngularSpeedConstraint.Update
             // (MaximumLinearVelocityConstraint.cs:177-193 and the angular file's).  Inputs: kJTRIG
@@ -1368,7 +1419,13 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
     if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s);
-        if (kAdded && IsAngularMotorType(type)) {
+        if (kAdded && type == BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR) {
+            // SingleEntityLinearMotor.ExclusiveUpdate (SingleEntityLinearMotor.cs:270-276)
+            const float3 r = JXYZ(j.L(kJOB, s)), a = make_float3(acc0.x, acc0.y, acc0.z);
+            ApplyLinear(A, a.x, a.y, a.z);
+            const float3 t = JCross(r, a);
+            ApplyAngular(A, t.x, t.y, t.z);
+        } else if (kAdded && IsAngularMotorType(type)) {
             // AngularMotor.ExclusiveUpdate (AngularMotor.cs:314-326), SingleEntityAngularMotor's
             // (:215-218; B is the world there)
             if (dynA) ApplyAngular(A, acc0.x, acc0.y, acc0.z);
@@ -1657,7 +1714,33 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
     } else if (st & (4u << kChildShift)) {
         const float4 l0 = j.L(kJL0, s), l2 = j.L(kJL2, s);
         const float softness = l0.w;
-        if (kAdded && IsAngularMotorType(type)) {
+        if (kAdded && type == BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR) {
+            // SingleEntityLinearMotor.SolveIteration (SingleEntityLinearMotor.cs:180-208)
+            const float4 l1 = j.L(kJL1, s), oa = j.L(kJOA, s);
+            const float3 r = JXYZ(j.L(kJOB, s));
+            float3 l = JCross(r, make_float3(A.wx, A.wy, A.wz));
+            l = make_float3(l.x - A.vx, l.y - A.vy, l.z - A.vz);
+            l = make_float3(l2.y + l.x, l2.z + l.y, l2.w + l.z);
+            l = make_float3(l.x - acc0.x * oa.x, l.y - acc0.y * oa.x, l.z - acc0.z * oa.x);
+            const JM3 m = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w, l2.x};
+            l = JTransform(l, m);
+            const float px = acc0.x, py = acc0.y, pz = acc0.z;
+            acc0.x = acc0.x + l.x;
+            acc0.y = acc0.y + l.y;
+            acc0.z = acc0.z + l.z;
+            const float sq = acc0.x * acc0.x + acc0.y * acc0.y + acc0.z * acc0.z;
+            if (sq > oa.z) {
+                const float f = oa.y / SqrtOfFloat(sq);
+                acc0.x = acc0.x * f;
+                acc0.y = acc0.y * f;
+                acc0.z = acc0.z * f;
+                l = make_float3(acc0.x - px, acc0.y - py, acc0.z - pz);
+            }
+            ApplyLinear(A, l.x, l.y, l.z);
+            const float3 t = JCross(r, l);
+            ApplyAngular(A, t.x, t.y, t.z);
+            account(2, fabsf(l.x) + fabsf(l.y) + fabsf(l.z));
+        } else if (kAdded && IsAngularMotorType(type)) {
             // AngularMotor.SolveIteration (AngularMotor.cs:203-246); SingleEntityAngularMotor's
             // (SingleEntityAngularMotor.cs:117-148) adds its bias to -w_A
             const float4 l1 = j.L(kJL1, s), oa = j.L(kJOA, s);

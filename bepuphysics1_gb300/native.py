@@ -109,7 +109,7 @@ JOINT_TWIST_LIMIT, JOINT_LINEAR_AXIS_LIMIT, JOINT_ELLIPSE_SWING_LIMIT = 16, 17, 
 JOINT_SWIVEL_HINGE_ANGULAR, JOINT_SWIVEL_HINGE = 19, 20
 JOINT_REVOLUTE_MOTOR, JOINT_TWIST_MOTOR, JOINT_LINEAR_AXIS_MOTOR = 21, 22, 23
 JOINT_MAXIMUM_LINEAR_SPEED, JOINT_MAXIMUM_ANGULAR_SPEED, JOINT_PLANE_SLIDER = 24, 25, 26
-JOINT_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_ANGULAR_MOTOR = 27, 28
+JOINT_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_LINEAR_MOTOR = 27, 28, 29
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE, JOINT_SERVO = 1, 2, 4
 
 _P = ctypes.c_void_p

@@ -163,7 +163,8 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_MAXIMUM_ANGULAR_SPEED = 25, /* MaximumAngularSpeedConstraint (SingleEntity/MaximumAngularVelocityConstraint.cs:138-199) */
     BEPUGPU_JOINT_PLANE_SLIDER = 26,    /* PlaneSliderJoint group: point on plane (POINT_ON_PLANE's fields) */
     BEPUGPU_JOINT_ANGULAR_MOTOR = 27,   /* AngularMotor.cs:203-326 */
-    BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR = 28 /* SingleEntityAngularMotor.cs:117-226: body_b -1, ANGULAR_MOTOR's fields */
+    BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR = 28, /* SingleEntityAngularMotor.cs:117-226: body_b -1, ANGULAR_MOTOR's fields */
+    BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR = 29 /* SingleEntityLinearMotor.cs:180-276: body_b -1 */
 } bepugpu_joint_type;
 /* The groups' motor children are inactive, as their constructors leave them
  * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
@@ -245,7 +246,10 @@ typedef enum bepugpu_joint_type {
  * An ANGULAR_MOTOR takes its basis from axis_a (primary), constrained_1 (x) and
  * constrained_2 (y) in A's frame, the servo goal (a relative orientation) from
  * orientation_a, the velocity goal (in the basis) from anchor_a, its other
- * MotorSettings as the 1-D motors do; impulse [0..2].
+ * MotorSettings as the 1-D motors do; impulse [0..2].  A SINGLE_ENTITY_LINEAR_MOTOR
+ * drives the point anchor_a (body_a's frame) at the velocity axis_a or, as a
+ * servo, towards the world point anchor_b; impulse [0..2], and [3] the used
+ * softness it keeps while the point sits at its goal (SingleEntityLinearMotor.cs:214-241).
  * axis_a/b and constrained_1/2 of a LINE_SLIDER are its RevoluteAngularJoint's;
  * orientation_a/b of a PRISMATIC its NoRotationJoint's. */
 typedef struct bepugpu_joint {

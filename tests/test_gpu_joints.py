@@ -182,7 +182,7 @@ NEW_TYPES = (N.JOINT_WELD, N.JOINT_NO_ROTATION, N.JOINT_DISTANCE, N.JOINT_DISTAN
 MOTORS = (N.JOINT_REVOLUTE_MOTOR, N.JOINT_TWIST_MOTOR, N.JOINT_LINEAR_AXIS_MOTOR)
 SPEED_LIMITS = (N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED)
 NEW_TYPES = NEW_TYPES + SPEED_LIMITS + (N.JOINT_PLANE_SLIDER, N.JOINT_ANGULAR_MOTOR,
-                                       N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR)
+                                       N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR)
 
 
 def _unit(v):
@@ -285,6 +285,20 @@ def _convert(b, j, types, seed):
             if a < 0:
                 a, qa = bb, qb
             j["body_a"][k], j["body_b"][k] = a, -1
+        if t == N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR:  # the link's anchor point towards a nearby goal
+            if a < 0:
+                a, qa = bb, qb
+                j["anchor_a"][k] = j["anchor_b"][k]
+            j["body_a"][k], j["body_b"][k] = a, -1
+            servo = rng.random() < 0.5
+            j["flags"][k] |= N.JOINT_SERVO if servo else 0
+            wp = b["position"][a] + j["anchor_a"][k] @ _rows(qa)
+            j["anchor_b"][k] = wp + rng.uniform(-0.05, 0.05, 3) * (rng.random() < 0.8)
+            j["axis_a"][k] = rng.uniform(-0.5, 0.5, 3)
+            j["margin"][k] = 0.0001
+            j["bounciness"][k] = rng.choice([0.0, 0.3])
+            j["bounce_velocity_threshold"][k] = rng.choice([np.finfo(np.float32).max, 5.0])
+            j["max_corrective_velocity"][k] = rng.choice([np.finfo(np.float32).max, 1.0])
         if t in (N.JOINT_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR):
             ra = _rows(qa)
             ax = _unit(rng.normal(size=3))
@@ -384,10 +398,11 @@ def test_each_new_type_alone_with_stale_impulses(gpu_context, jtype):
                    N.JOINT_PRISMATIC: 5, N.JOINT_LINE_SLIDER: 4, N.JOINT_REVOLUTE_MOTOR: 0,
                    N.JOINT_TWIST_MOTOR: 0, N.JOINT_LINEAR_AXIS_MOTOR: 0, N.JOINT_MAXIMUM_LINEAR_SPEED: 0,
                    N.JOINT_MAXIMUM_ANGULAR_SPEED: 2, N.JOINT_ANGULAR_MOTOR: 0,
-                   N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR: 0}
+                   N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR: 0, N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR: 0}
     if jtype in limit_entry:  # some limits pushed: impulses that are new and nonzero
         e = limit_entry[jtype]
-        e = slice(0, 3) if jtype in SPEED_LIMITS + (N.JOINT_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR) \
+        e = slice(0, 3) if jtype in SPEED_LIMITS + (N.JOINT_ANGULAR_MOTOR, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR,
+                                                    N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR) \
             else slice(e, e + 1)
         got = (first if jtype in SPEED_LIMITS else p.oracle.get_constraints()[1]["impulse"])[:, e]
         assert np.count_nonzero(np.any((got != j["impulse"][:, e]) & (got != 0), axis=1)) > 0

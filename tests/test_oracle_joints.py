@@ -599,3 +599,35 @@ def test_single_entity_angular_motor_closed_form(servo):
         lam = 2.0 / (4.0 + 0.0001 * 60)
     np.testing.assert_allclose(oj["impulse"][0, :3], (0, 0, lam), rtol=1e-4, atol=1e-8)
     np.testing.assert_allclose(ob["angular_velocity"][0], (0, 0, 4.0 * lam), rtol=1e-4, atol=1e-8)
+
+
+def _linear_motor(servo=False):
+    j = _motor(N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR, servo=servo)
+    j["body_a"], j["body_b"] = 0, -1
+    return j
+
+
+def test_single_entity_linear_motor_closed_form():
+    """SingleEntityLinearMotor (SingleEntityLinearMotor.cs:180-268): the centre
+    driven at 1 m/s along x, then as a servo towards (0.5, 0, 0); at the goal
+    the servo keeps the softness its record carries (impulse [3])."""
+    b = _body((0, 0, 0))
+    j = _linear_motor()
+    j["axis_a"] = (1.0, 0, 0)
+    ob, oj = _step(b, j)
+    lam = 1.0 / (1.0 + 0.0001 * 60)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (lam, 0, 0), rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(ob["linear_velocity"][0], (lam, 0, 0), rtol=1e-4, atol=1e-8)
+    j = _linear_motor(servo=True)
+    j["anchor_b"] = (0.5, 0, 0)
+    ob, oj = _step(b, j)
+    erp, soft = _spring(float(DT))
+    lam = 0.5 * erp / (1.0 + soft)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (lam, 0, 0), rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(oj["impulse"][0, 3], soft, rtol=1e-5)
+    b["linear_velocity"] = (1.0, 0, 0)
+    j = _linear_motor(servo=True)
+    j["impulse"][0, 3] = 0.5  # at the goal: this softness stays
+    ob, oj = _step(b, j)
+    np.testing.assert_allclose(oj["impulse"][0, :3], (-1.0 / 1.5, 0, 0), rtol=1e-4, atol=1e-8)
+    assert oj["impulse"][0, 3] == np.float32(0.5)
