@@ -432,3 +432,32 @@ def test_new_type_records_checked(gpu_context):
     bad["limit_min"][1] = -1.0
     with pytest.raises(N.BepuError):
         GpuSpace(gpu_context, b, m, bad)
+
+
+@pytest.mark.parametrize("jtype", [N.JOINT_TWIST_LIMIT, N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR, N.JOINT_PRISMATIC,
+                                   N.JOINT_ANGULAR_MOTOR, N.JOINT_REVOLUTE_MOTOR])
+def test_added_types_resume_from_records(gpu_context, jtype):
+    """Stepping, downloading the records (bodies and joints: impulses, a twist
+    limit's last error, a linear motor's kept softness), uploading them into a
+    new scene and stepping on continues bit for bit like the uninterrupted run."""
+    b, m, j = _small_chains(seed=31, chains=12, loose=40)
+    j = _convert(b, j, (jtype,), 31)
+    gpu_context.set_settings(_settings())
+    ref = GpuSpace(gpu_context, b, m, j)
+    for _ in range(6):
+        ref.step(float(DT))
+    cut = GpuSpace(gpu_context, b, m, j)
+    for _ in range(3):
+        cut.step(float(DT))
+    mb = cut.download_bodies(b.copy())
+    mm, mj = cut.download_constraints(m.copy(), j.copy())
+    again = GpuSpace(gpu_context, mb, mm, mj)
+    for _ in range(3):
+        again.step(float(DT))
+    rb, ab = ref.download_bodies(b.copy()), again.download_bodies(b.copy())
+    for f in ("position", "orientation", "linear_velocity", "angular_velocity"):
+        np.testing.assert_array_equal(rb[f], ab[f], err_msg=f)
+    np.testing.assert_array_equal(ref.download_constraints(m.copy(), j.copy())[1]["impulse"],
+                                  again.download_constraints(m.copy(), j.copy())[1]["impulse"])
+    for s in (ref, cut, again):
+        s.close()
