@@ -406,10 +406,51 @@ def chain_section(args, local, rank, world, pg):
         "parity": "bit-exact vs the colour-ordered oracle (tests/test_gpu_joints.py)",
     }
     sp.close()
+
+    # the same scene with its joints re-typed as ten of the added joint, limit and motor types
+    mixed = scenes.with_added_joint_types(bodies, joints)
+    sp = GpuSpace(ctx, bodies, manifolds, mixed)
+    for _ in range(max(args.warmup, 3)):
+        sp.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    mixed_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        sp.step(DT, N.STEP_ALL)
+        mixed_ms.append(sp.last_step_ms())
+    mixed_total = float(sum(mixed_ms))
+    if pg:
+        t = torch.tensor([mixed_total], device=f"cuda:{local}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        mixed_total = float(t.item())
+    out["added_types"] = {
+        "value": world * n_upd * CHAIN_ITERATIONS * args.steps / (mixed_total / 1000.0), "unit": "updateable-iters/s",
+        "steps_per_s": world * args.steps / (mixed_total / 1000.0), "ms_per_step": mixed_total / args.steps,
+        "gpu_launches_per_step": int(sp.last_step_launches()),
+        "joint_types": sorted({int(t) for t in mixed["type"]}),
+        "what": "chains_8k with its joints re-typed in turn as weld, distance, prismatic with its limit, revolute "
+                "motor, linear servo motor, maximum speed, twist limit, swivel hinge, ellipse swing limit and "
+                "point on plane (scenes.with_added_joint_types)",
+    }
+    sp.close()
     ctx.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
         threads = os.cpu_count() or 1
+        o = oracle.OracleSpace(settings, bodies, manifolds, mixed)
+        o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+        o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+        steps, t0 = 0, time.perf_counter()
+        while True:
+            o.step_multithreaded(DT, N.STEP_ALL, 1, threads)
+            steps += 1
+            if time.perf_counter() - t0 >= args.chain_cpu_seconds / 2:
+                break
+        el = time.perf_counter() - t0
+        o.close()
+        out["added_types"]["cpu_baseline"] = {"steps_per_s": steps / el, "cores": threads, "kind": "port",
+                                              "sample": f"{steps} steps of the oracle port, {threads} threads"}
         o = oracle.OracleSpace(settings, bodies, manifolds, joints)
         o.set_order_mode(oracle.ORDER_PERMUTED, 0)
         o.step_multithreaded(DT, N.STEP_ALL, 1, threads)

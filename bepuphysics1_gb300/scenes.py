@@ -78,6 +78,75 @@ def chains_8k(seed: int = 3):
     return make_chain(seed=seed)
 
 
+def _rows(q) -> np.ndarray:
+    """Matrix3x3.CreateFromQuaternion (row-vector convention: world = local @ R), float64."""
+    x, y, z, w = (float(v) for v in q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y + z * w), 2 * (x * z - y * w)],
+                     [2 * (x * y - z * w), 1 - 2 * (x * x + z * z), 2 * (y * z + x * w)],
+                     [2 * (x * z + y * w), 2 * (y * z - x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def with_added_joint_types(bodies: np.ndarray, joints: np.ndarray) -> np.ndarray:
+    """The joints of a chain scene re-typed in turn as ten of the added types,
+    each set up from the current poses: weld, distance (the anchors' distance),
+    prismatic with its linear limit, revolute velocity motor, linear servo
+    motor, single-entity maximum speed, twist limit, swivel hinge, ellipse
+    swing limit and point on plane.  Anchors stay the chain's."""
+    j = joints.copy()
+    ident = np.array([0, 0, 0, 1], np.float32)
+    fmax = np.finfo(np.float32).max
+    for k in range(len(j)):
+        a, c = int(j["body_a"][k]), int(j["body_b"][k])
+        qa = bodies["orientation"][a] if a >= 0 else ident
+        qb = bodies["orientation"][c] if c >= 0 else ident
+        j["orientation_a"][k], j["orientation_b"][k] = qa, qb
+        j["impulse"][k] = 0
+        j["flags"][k] = N.JOINT_ACTIVE
+        kind = k % 10
+        if kind == 0:
+            j["type"][k] = N.JOINT_WELD
+        elif kind == 1:
+            wa = (bodies["position"][a] + j["anchor_a"][k] @ _rows(qa)) if a >= 0 else j["anchor_a"][k]
+            wb = (bodies["position"][c] + j["anchor_b"][k] @ _rows(qb)) if c >= 0 else j["anchor_b"][k]
+            j["type"][k] = N.JOINT_DISTANCE
+            j["limit_min"][k] = float(np.linalg.norm(wb - wa))
+        elif kind == 2:
+            j["type"][k] = N.JOINT_PRISMATIC
+            j["flags"][k] |= N.JOINT_LIMIT_ACTIVE
+            j["limit_min"][k], j["limit_max"][k] = -0.01, 0.01
+            j["basis_primary"][k], j["basis_x"][k], j["test_axis"][k] = (1, 0, 0), (0, 0, -1), (0, 1, 0)
+        elif kind == 3:
+            j["type"][k] = N.JOINT_REVOLUTE_MOTOR
+            j["limit_max"][k], j["margin"][k], j["bounce_velocity_threshold"][k] = 1.0, 0.0001, fmax
+            j["basis_primary"][k], j["basis_x"][k], j["test_axis"][k] = (1, 0, 0), (0, 0, -1), (0, 0, -1)
+        elif kind == 4:
+            j["type"][k] = N.JOINT_LINEAR_AXIS_MOTOR
+            j["flags"][k] |= N.JOINT_SERVO
+            j["limit_min"][k], j["margin"][k], j["bounce_velocity_threshold"][k] = 0.05, 0.0001, 50.0
+            j["basis_primary"][k] = (0, 1, 0)
+        elif kind == 5:
+            j["type"][k] = N.JOINT_MAXIMUM_LINEAR_SPEED
+            j["body_a"][k], j["body_b"][k] = (c if a < 0 else a), -1
+            j["limit_min"][k], j["limit_max"][k], j["margin"][k] = 0.5, fmax, 0.00001
+        elif kind == 6:
+            j["type"][k] = N.JOINT_TWIST_LIMIT
+            j["axis_a"][k] = j["axis_b"][k] = (1, 0, 0)
+            j["constrained_1"][k], j["constrained_2"][k], j["basis_x"][k] = (0, 0, -1), (0, 1, 0), (0, 0, -1)
+            j["limit_min"][k], j["limit_max"][k] = -0.5, 0.5
+        elif kind == 7:
+            j["type"][k] = N.JOINT_SWIVEL_HINGE
+            j["axis_a"][k], j["axis_b"][k] = (1, 0, 0), (0, 1, 0)
+        elif kind == 8:
+            j["type"][k] = N.JOINT_ELLIPSE_SWING_LIMIT
+            j["axis_a"][k], j["constrained_1"][k], j["constrained_2"][k] = (0, 1, 0), (1, 0, 0), (0, 0, 1)
+            j["axis_b"][k] = (0, 1, 0)
+            j["limit_min"][k], j["limit_max"][k] = 0.5, 0.3
+        else:
+            j["type"][k] = N.JOINT_POINT_ON_PLANE
+            j["axis_a"][k] = (0, 1, 0)
+    return j
+
+
 def pile_1k(seed: int = 1234):
     return make_pile(seed=seed)
 

@@ -461,3 +461,17 @@ def test_added_types_resume_from_records(gpu_context, jtype):
                                   again.download_constraints(m.copy(), j.copy())[1]["impulse"])
     for s in (ref, cut, again):
         s.close()
+
+
+def test_added_type_mix_of_the_bench(gpu_context):
+    """scenes.with_added_joint_types (the bench's added-types chains) against the
+    oracle, on the island-group path and the sweep path."""
+    b, m, j = _small_chains(seed=41, chains=30, loose=80)
+    mixed = scenes.with_added_joint_types(b, j)
+    assert len(set(mixed["type"].tolist())) == 10
+    for policy in (None, (0, 1024, 4096, 64, 0)):
+        p = Pair(gpu_context, b, m, mixed, settings=_settings(), group_policy=policy)
+        p.step(steps=20)
+        errs, exact = p.compare()
+        assert exact, (policy, errs)
+        p.close()
