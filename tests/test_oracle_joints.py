@@ -631,3 +631,32 @@ def test_single_entity_linear_motor_closed_form():
     ob, oj = _step(b, j)
     np.testing.assert_allclose(oj["impulse"][0, :3], (-1.0 / 1.5, 0, 0), rtol=1e-4, atol=1e-8)
     assert oj["impulse"][0, 3] == np.float32(0.5)
+
+
+SINGLE_ENTITY = {N.JOINT_MAXIMUM_LINEAR_SPEED, N.JOINT_MAXIMUM_ANGULAR_SPEED, N.JOINT_SINGLE_ENTITY_ANGULAR_MOTOR,
+                 N.JOINT_SINGLE_ENTITY_LINEAR_MOTOR}
+
+
+@pytest.mark.parametrize("jtype", range(1, 30))
+def test_every_joint_type_steps_in_the_oracle(jtype):
+    """Every record type of the header builds its oracle object and steps: two
+    moving bodies (or one, for the single-entity types) and the impulses stay
+    finite."""
+    a = _body((0, 0, 0))
+    b = _body((0.1, -0.9, 0.05), quat=_rot_z(0.3))
+    a["linear_velocity"], b["angular_velocity"] = (0.5, 0, 0), (0, 1.0, 2.0)
+    bodies = np.concatenate([a, b])
+    j = _joint(jtype, 0, -1 if jtype in SINGLE_ENTITY else 1)
+    j["anchor_a"], j["anchor_b"] = (0, -0.5, 0), (0, 0.4, 0)
+    j["axis_a"] = j["axis_b"] = j["basis_primary"] = (1, 0, 0)
+    j["constrained_1"], j["constrained_2"] = (0, 1, 0), (0, 0, 1)
+    j["basis_x"], j["test_axis"] = (0, 1, 0), (0, 1, 0)
+    j["orientation_a"] = j["orientation_b"] = (0, 0, 0, 1)
+    j["limit_min"], j["limit_max"] = 0.1, 0.3
+    j["impulse"][0, :4] = 0.01
+    o = oracle.OracleSpace(_settings(5), bodies, np.zeros(0, N.MANIFOLD_DTYPE), j)
+    o.step(DT, N.STEP_ALL, 3)
+    ob, oj = o.get_bodies(), o.get_constraints()[1]
+    o.close()
+    assert np.all(np.isfinite(ob["linear_velocity"])) and np.all(np.isfinite(ob["angular_velocity"]))
+    assert np.all(np.isfinite(oj["impulse"]))
