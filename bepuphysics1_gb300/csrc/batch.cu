@@ -11,8 +11,10 @@
 //
 // A scene joins the batched launch when its whole step is island groups: no
 // constraints on the colour-sweep path, no joints, no dynamic body outside a
-// group and no moving kinematic body.  Other listed scenes are stepped with
-// their own one-scene path, after the batched launch.
+// group, and no kinematic body whose candidacy or position stage would change
+// it (a moving or always-active one, or one settling in the first steps after
+// an upload).  Other listed scenes are stepped with their own one-scene path,
+// after the batched launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -69,6 +71,7 @@ struct Batch : BatchEngine {
     std::vector<int32_t> keyScenes;
     std::vector<uint32_t> keySteps;
     std::vector<uint64_t> keyVersions;
+    std::vector<uint8_t> keyReady;
     float keyDt = 0.f;
     uint32_t keyFlags = 0;
     int keyThreads = 0;
@@ -145,7 +148,9 @@ SceneView MakeView(const Scene& s) {
     return v;
 }
 
-bool Scene::BatchReady() const { return SweepEmpty() && jointCount == 0 && generatedCount == 0; }
+bool Scene::BatchReady(uint32_t flags) const {
+    return SweepEmpty() && jointCount == 0 && generatedCount == 0 && !kin.Needed(flags);
+}
 
 }  // namespace bepugpu
 
@@ -182,6 +187,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         ~EpochBump() { c->batchEpoch++; }
     } bump{ctx};
     std::vector<uint64_t> versions(count);
+    std::vector<uint8_t> ready(count);  // joins the batched launch
     for (uint32_t i = 0; i < count; i++) {
         auto it = ctx->scenes.find(scenes[i]);
         if (it == ctx->scenes.end()) {
@@ -211,6 +217,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         list[i] = s;
         stepCount[i] = k;
         versions[i] = s->version;
+        ready[i] = s->BatchReady(flags) ? 1 : 0;
         if (s->asyncPending) {  // a one-scene step may still run on the scene's stream
             if (cudaStreamSynchronize(s->stream) != cudaSuccess) {
                 ctx->SetError("batch: scene %d stream failed", scenes[i]);
@@ -225,7 +232,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
     bool same = bt.graph && bt.keyDt == dt && bt.keyFlags == flags && bt.keyThreads == ctx->batchThreads &&
                 std::memcmp(&bt.keySettings, &ctx->settings, sizeof(bepugpu_settings)) == 0 &&
                 bt.keyScenes.size() == count && std::equal(scenes, scenes + count, bt.keyScenes.begin()) &&
-                bt.keySteps == stepCount && bt.keyVersions == versions;
+                bt.keySteps == stepCount && bt.keyVersions == versions && bt.keyReady == ready;
     cudaError_t e = cudaSuccess;
     if (!same) {
         if (bt.graph) {
@@ -238,7 +245,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         bt.global = ClassLaunch{{}, 1, 1, 0, bt.global.dev, bt.global.cap};
         for (uint32_t i = 0; i < count; i++) {
             Scene* s = list[i];
-            if (!s->BatchReady() || stepCount[i] == 0) continue;
+            if (!ready[i] || stepCount[i] == 0) continue;
             passes = std::max(passes, (int)stepCount[i]);
             const GroupPlan& g = s->groupPlan;
             const int vi = (int)views.size();
@@ -305,6 +312,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         bt.keyScenes.assign(scenes, scenes + count);
         bt.keySteps = stepCount;
         bt.keyVersions = versions;
+        bt.keyReady = ready;
         bt.keyDt = dt;
         bt.keyFlags = flags;
         bt.keyThreads = ctx->batchThreads;
@@ -319,7 +327,10 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
     // Scenes outside the batched launch take their own path, step by step.
     for (uint32_t i = 0; i < count; i++) {
         Scene* s = list[i];
-        if (s->BatchReady()) continue;
+        if (ready[i]) {
+            for (uint32_t k = 0; k < stepCount[i]; k++) s->kin.Advance(flags);
+            continue;
+        }
         for (uint32_t k = 0; k < stepCount[i]; k++) {
             bepugpu_status st = s->Step(ctx, dt, flags);
             if (st != BEPUGPU_OK) return st;

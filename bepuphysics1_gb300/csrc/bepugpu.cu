@@ -43,6 +43,7 @@ __global__ void k_unpack_bodies(const bepugpu_body* __restrict__ rec, int n, Bod
     b.loc1[i] = make_float4(l[4], l[5], l[6], l[7]);
     b.inv0[i] = make_float4(0, 0, 0, 0);
     b.inv1[i] = make_float4(0, 0, 0, 0);
+    b.act[i] = make_float4(r.previous_velocity, r.velocity_time_below_limit, __uint_as_float(r.activity), 0.f);
 }
 
 // World inverse inertia at upload (Entity orientation setter: R^T L R), so a
@@ -96,6 +97,10 @@ __global__ void k_patch_body_records(BodySoA b, bepugpu_body* __restrict__ rec) 
     r.orientation[0] = q.x; r.orientation[1] = q.y; r.orientation[2] = q.z; r.orientation[3] = q.w;
     r.linear_velocity[0] = v.x; r.linear_velocity[1] = v.y; r.linear_velocity[2] = v.z;
     r.angular_velocity[0] = w.x; r.angular_velocity[1] = w.y; r.angular_velocity[2] = w.z;
+    const float4 a = b.act[i];
+    r.previous_velocity = a.x;
+    r.velocity_time_below_limit = a.y;
+    r.activity = __float_as_uint(a.z);
 }
 
 // Lowest body with a non-finite position, orientation or velocity.
@@ -124,8 +129,8 @@ __global__ void k_bounded_wait_probe(volatile unsigned int* flag, unsigned int l
 }
 
 // Checks of the update calls, before anything is written: check[0] receives
-// the lowest offending record index (stays INT_MAX when none), check[1] is set
-// when a kinematic body has a velocity.
+// the lowest offending record index (stays INT_MAX when none), check[1] the
+// KinematicState bits of the kinematic bodies.
 __device__ __forceinline__ bool SameWord(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
 __global__ void k_check_body_records(const bepugpu_body* __restrict__ in, const bepugpu_body* __restrict__ kept, int n,
                                      int* check) {
@@ -136,9 +141,14 @@ __global__ void k_check_body_records(const bepugpu_body* __restrict__ in, const 
                 SameWord(r.linear_damping, k.linear_damping) && SameWord(r.angular_damping, k.angular_damping);
     for (int q = 0; q < 9; q++) same = same && SameWord(r.local_inverse_inertia[q], k.local_inverse_inertia[q]);
     if (!same) atomicMin(check, i);
-    if (!r.is_dynamic && (r.linear_velocity[0] != 0 || r.linear_velocity[1] != 0 || r.linear_velocity[2] != 0 ||
-                          r.angular_velocity[0] != 0 || r.angular_velocity[1] != 0 || r.angular_velocity[2] != 0))
-        atomicOr(check + 1, 1);
+    if (!r.is_dynamic) {
+        KinematicState k{};
+        k.Add(r.linear_velocity[0] != 0 || r.linear_velocity[1] != 0 || r.linear_velocity[2] != 0 ||
+                  r.angular_velocity[0] != 0 || r.angular_velocity[1] != 0 || r.angular_velocity[2] != 0,
+              r.activity, r.previous_velocity, r.velocity_time_below_limit);
+        const uint32_t bits = k.Bits();
+        if (bits) atomicOr(check + 1, (int)bits);
+    }
 }
 // The state fields of checked records into the body lanes and the kept records.
 __global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, BodySoA b, bepugpu_body* kept) {
@@ -151,6 +161,10 @@ __global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, 
     b.quat[i] = make_float4(r.orientation[0], r.orientation[1], r.orientation[2], r.orientation[3]);
     b.vlin[i] = make_float4(r.linear_velocity[0], r.linear_velocity[1], r.linear_velocity[2], v.w);
     b.vang[i] = make_float4(r.angular_velocity[0], r.angular_velocity[1], r.angular_velocity[2], w.w);
+    b.act[i] = make_float4(r.previous_velocity, r.velocity_time_below_limit, __uint_as_float(r.activity), 0.f);
+    k.previous_velocity = r.previous_velocity;
+    k.velocity_time_below_limit = r.velocity_time_below_limit;
+    k.activity = r.activity;
     for (int q = 0; q < 3; q++) {
         k.position[q] = r.position[q];
         k.linear_velocity[q] = r.linear_velocity[q];
@@ -276,14 +290,16 @@ __global__ void k_refresh(ManifoldSoA m, BodySoA b, StepParams p) {
 __device__ __forceinline__ bool OwnedByGroup(const BodySoA& b, int i) {
     return __float_as_uint(b.damp[i].w) & kOwnedByGroup;
 }
-__global__ void k_refresh_force(ManifoldSoA m, BodySoA b, StepParams p) {
+// The body stages at the start of a step (candidacy and force update) touch
+// velocities, inertia and activity only, so they share the refresh's launch.
+constexpr uint32_t kStartStages = BEPUGPU_STEP_FORCES | BEPUGPU_STEP_DEACTIVATION;
+__global__ void k_refresh_force(ManifoldSoA m, BodySoA b, StepParams p, uint32_t flags) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < m.count) RefreshManifold(m, b, t, p);
-    else if (t - m.count < b.count && !OwnedByGroup(b, t - m.count)) ForceUpdateBody(b, t - m.count, p);
-}
-__global__ void k_force(BodySoA b, StepParams p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < b.count && !OwnedByGroup(b, i)) ForceUpdateBody(b, i, p);
+    if (t < m.count) {
+        if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifold(m, b, t, p);
+    } else if (t - m.count < b.count && !OwnedByGroup(b, t - m.count)) {
+        StartBodyStep(b, t - m.count, p, flags);
+    }
 }
 // Body stages over the bodies no group kernel steps (the scene has groups).
 __global__ void k_refresh_force_list(ManifoldSoA m, BodySoA b, StepParams p, const int32_t* __restrict__ list, int n,
@@ -292,8 +308,19 @@ __global__ void k_refresh_force_list(ManifoldSoA m, BodySoA b, StepParams p, con
     if (t < m.count) {
         if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifold(m, b, t, p);
     } else if (t - m.count < n) {
-        if (flags & BEPUGPU_STEP_FORCES) ForceUpdateBody(b, list[t - m.count], p);
+        if (flags & kStartStages) StartBodyStep(b, list[t - m.count], p, flags);
     }
+}
+// The kinematic bodies of a scene whose step is otherwise island groups
+// alone, after the group launch: their candidacy update and, while active,
+// their position update.  A kinematic body's velocity does not change during
+// the step, so its candidacy reads the same values here as at the start.
+__global__ void k_kinematic_tail(BodySoA b, StepParams p, const int32_t* __restrict__ list, int n, uint32_t flags) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int i = list[t];
+    if (flags & BEPUGPU_STEP_DEACTIVATION) StartBodyStep(b, i, p, BEPUGPU_STEP_DEACTIVATION);
+    if (flags & BEPUGPU_STEP_POSITIONS) PositionUpdateBody(b, i, p);
 }
 __global__ void k_position_list(BodySoA b, StepParams p, const int32_t* __restrict__ list, int n) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -458,12 +485,12 @@ __global__ void k_persistent(PersistentArgs a) {
     __syncthreads();
     // The refresh reads poses only and the force update writes velocities and
     // inertia only, so the two share one phase.
-    if (a.flags & (BEPUGPU_STEP_REFRESH_CONTACTS | BEPUGPU_STEP_FORCES)) {
+    if (a.flags & (BEPUGPU_STEP_REFRESH_CONTACTS | kStartStages)) {
         if (a.flags & BEPUGPU_STEP_REFRESH_CONTACTS)
             for (int s = tid; s < a.m.count; s += stride) RefreshManifold(a.m, a.b, s, a.p);
-        if (a.flags & BEPUGPU_STEP_FORCES)
+        if (a.flags & kStartStages)
             for (int i = tid; i < a.b.count; i += stride)
-                if (!OwnedByGroup(a.b, i)) ForceUpdateBody(a.b, i, a.p);
+                if (!OwnedByGroup(a.b, i)) StartBodyStep(a.b, i, a.p, a.flags);
         if (!GridBarrier(a.counter, a.generation, localGen, err)) return;
     }
     if (a.flags & BEPUGPU_STEP_SOLVE) {
@@ -585,6 +612,10 @@ StepParams MakeParams(const bepugpu_settings& s, float dt) {
     p.allowedPenetration = s.allowed_penetration;
     p.invalidationLengthSquared = s.contact_invalidation_length_squared;
     p.maximumContactDistance = s.maximum_contact_distance;
+    p.useStabilization = s.use_stabilization != 0 ? 1 : 0;
+    p.velocityLowerLimit = s.velocity_lower_limit;
+    p.velocityLowerLimitSquared = s.velocity_lower_limit * s.velocity_lower_limit;
+    p.lowVelocityTimeMinimum = s.low_velocity_time_minimum;
     return p;
 }
 
@@ -625,7 +656,7 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     ArenaLayout& L = layout;
     L.pos = take(16 * B); L.quat = take(16 * B); L.vlin = take(16 * B); L.vang = take(16 * B);
     L.inv0 = take(16 * B); L.inv1 = take(16 * B); L.loc0 = take(16 * B); L.loc1 = take(16 * B);
-    L.damp = take(16 * B); L.m33 = take(4 * B);
+    L.damp = take(16 * B); L.m33 = take(4 * B); L.act = take(16 * B); L.rawDamp = take(8 * B);
     L.head = take(16 * M); L.cpos = take(64 * M); L.cnrm = take(64 * M); L.offA = take(64 * M);
     L.offB = take(64 * M); L.mat = take(16 * M); L.pen = take(16 * M); L.fric = take(16 * M);
     L.axis = take(16 * M); L.pj0 = take(64 * M); L.pj1 = take(64 * M); L.pj2 = take(64 * M);
@@ -680,6 +711,7 @@ void Scene::Rebase() {
     b.pos = (float4*)(base + L.pos); b.quat = (float4*)(base + L.quat); b.vlin = (float4*)(base + L.vlin);
     b.vang = (float4*)(base + L.vang); b.inv0 = (float4*)(base + L.inv0); b.inv1 = (float4*)(base + L.inv1);
     b.loc0 = (float4*)(base + L.loc0); b.loc1 = (float4*)(base + L.loc1); b.damp = (float4*)(base + L.damp);
+    b.act = (float4*)(base + L.act); b.rawDamp = (float2*)(base + L.rawDamp);
     localM33 = (float*)(base + L.m33);
     m.head = (int4*)(base + L.head); m.cpos = (float4*)(base + L.cpos); m.cnrm = (float4*)(base + L.cnrm);
     m.offA = (float4*)(base + L.offA); m.offB = (float4*)(base + L.offB); m.mat = (float4*)(base + L.mat);
@@ -853,7 +885,15 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     // path: no sweep manifolds or joints, no dynamic body outside the groups,
     // no moving kinematic body.  Its graph is the group launch alone.
     phaseEvents = !SweepEmpty();
+    graphTail = false;
     if (!phaseEvents) {
+        // the kinematic bodies' candidacy and position stages, while they change anything
+        if (kin.Needed(flags) && sweepBodyCount) {
+            k_kinematic_tail<<<Blocks((int)sweepBodyCount, T), T, 0, stream>>>(b, p, sweepBodiesDev,
+                                                                               (int)sweepBodyCount, flags);
+            launchesPerStep++;
+            graphTail = true;
+        }
         cudaGraph_t graph;
         cudaError_t e = cudaStreamEndCapture(stream, &graph);
         if (e != cudaSuccess) {
@@ -876,7 +916,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     // Phase events become event-record nodes of the graph: their elapsed times
     // are the device time of each phase of every launched step.
     CK(cudaEventRecordWithFlags(evPhase[0], stream, cudaEventRecordExternal));
-    bool refresh = (flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm, force = (flags & BEPUGPU_STEP_FORCES) && nb;
+    bool refresh = (flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm, force = (flags & kStartStages) && nb;
     const bool listed = !groupPlan.groups.empty();  // body stages over the sweep path's own bodies
     const int nl = (int)sweepBodyCount;
     if (listed) {
@@ -885,11 +925,13 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
             launchesPerStep++;
         }
     } else if (refresh && force) {
-        k_refresh_force<<<Blocks(nm + nb, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
+        k_refresh_force<<<Blocks(nm + nb, T), T, 0, stream>>>(ms, b, p, flags); launchesPerStep++;
     } else if (refresh) {
         k_refresh<<<Blocks(nm, T), T, 0, stream>>>(ms, b, p); launchesPerStep++;
     } else if (force) {
-        k_force<<<Blocks(nb, T), T, 0, stream>>>(b, p); launchesPerStep++;
+        ManifoldSoA none = ms;
+        none.count = 0;
+        k_refresh_force<<<Blocks(nb, T), T, 0, stream>>>(none, b, p, flags & kStartStages); launchesPerStep++;
     }
     CK(cudaEventRecordWithFlags(evPhase[1], stream, cudaEventRecordExternal));
     const JointSoA js = SweepJoints();
@@ -1031,14 +1073,16 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
         st = RunPersistent(ctx, p, flags);
         if (st != BEPUGPU_OK) return st;
     } else {
+        const bool tail = SweepEmpty() && kin.Needed(flags) && sweepBodyCount;
         if (!graphExec || graphDt != dt || graphFlags != flags || graphVersion != version ||
-            graphIterations != p.iterationLimit) {
+            graphIterations != p.iterationLimit || graphTail != tail) {
             st = BuildGraph(ctx, p, flags);
             if (st != BEPUGPU_OK) return st;
         }
         CK(cudaGraphLaunch(graphExec, stream));
     }
     CK(cudaEventRecord(evStop, stream));
+    kin.Advance(flags);
     stepped = true;
     asyncPending = true;
     return BEPUGPU_OK;
@@ -1127,6 +1171,9 @@ void bepugpu_default_settings(bepugpu_settings* s) {
     s->allowed_penetration = .01f;
     s->contact_invalidation_length_squared = .01f;
     s->maximum_contact_distance = .1f;
+    s->use_stabilization = 1;
+    s->velocity_lower_limit = .26f;
+    s->low_velocity_time_minimum = 1.f;
 }
 
 static bepugpu_status ValidateSettings(Context* ctx, const bepugpu_settings* s) {
@@ -1136,6 +1183,16 @@ static bepugpu_status ValidateSettings(Context* ctx, const bepugpu_settings* s) 
     }
     if (s->minimum_iteration_count < 0 || s->minimum_iteration_count > 14) {
         ctx->SetError("minimum_iteration_count must be in [0, 14]");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    // DeactivationManager.VelocityLowerLimit clamps to >= 0 and LowVelocityTimeMinimum
+    // throws ArgumentException for values <= 0 (DeactivationManager.cs:36,54-55).
+    if (!(s->velocity_lower_limit >= 0) || !std::isfinite(s->velocity_lower_limit)) {
+        ctx->SetError("velocity_lower_limit must be finite and >= 0");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (!(s->low_velocity_time_minimum > 0)) {
+        ctx->SetError("low_velocity_time_minimum must be positive");
         return BEPUGPU_INVALID_ARGUMENT;
     }
     return BEPUGPU_OK;
@@ -1250,24 +1307,26 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         return BEPUGPU_INVALID_ARGUMENT;
     }
     s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);
-    const bool wasMoving = s->kinematicMoving;
     bool dynamicChanged = s->hostDynamic.size() != n;
     s->hostDynamic.resize(n);
-    s->kinematicMoving = false;
+    s->hostRawDamp.resize(n);
+    s->kin.Clear();
     for (uint32_t i = 0; i < n; i++) {
         if (!dynamicChanged && s->hostDynamic[i] != (bodies[i].is_dynamic ? 1 : 0)) dynamicChanged = true;
         if (!bodies[i].is_dynamic) {
             const float* v = bodies[i].linear_velocity;
             const float* w = bodies[i].angular_velocity;
-            if (v[0] != 0 || v[1] != 0 || v[2] != 0 || w[0] != 0 || w[1] != 0 || w[2] != 0) s->kinematicMoving = true;
+            s->kin.Add(v[0] != 0 || v[1] != 0 || v[2] != 0 || w[0] != 0 || w[1] != 0 || w[2] != 0,
+                       bodies[i].activity, bodies[i].previous_velocity, bodies[i].velocity_time_below_limit);
         }
+        s->hostRawDamp[i] = make_float2(bodies[i].linear_damping, bodies[i].angular_damping);
         s->hostLinDamp[i] = bodies[i].linear_damping;
         s->hostAngDamp[i] = bodies[i].angular_damping;
         s->hostDynamic[i] = bodies[i].is_dynamic ? 1 : 0;
         s->hostLocalM33[i] = bodies[i].is_dynamic ? bodies[i].local_inverse_inertia[8] : 0.f;
     }
     const bool resized = n != (uint32_t)s->b.count;
-    if (resized || wasMoving != s->kinematicMoving) s->version++;
+    if (resized) s->version++;
     // The colouring and the island groups depend on which bodies are dynamic.
     if (dynamicChanged && (s->m.count || s->jointCount)) s->planStale = true;
     s->b.count = (int)n;
@@ -1280,6 +1339,8 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         CK(cudaMemcpyAsync(s->bodyRecords, bodies, sizeof(bepugpu_body) * n, cudaMemcpyHostToDevice, s->stream));
         k_unpack_bodies<<<Blocks(n, 256), 256, 0, s->stream>>>(s->bodyRecords, (int)n, s->b);
         CK(cudaMemcpyAsync(s->localM33, s->hostLocalM33.data(), sizeof(float) * n, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->b.rawDamp, s->hostRawDamp.data(), sizeof(float2) * n, cudaMemcpyHostToDevice,
+                           s->stream));
         k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
         CK(cudaGetLastError());
         // The staging buffer and host vectors are reused by the next call: wait.
@@ -1464,10 +1525,7 @@ bepugpu_status bepugpu_step_host(bepugpu_context* c, int32_t id, bepugpu_body* b
     }
     if (nm) k_unpack_manifolds<<<Blocks(nm, 256), 256, 0, s->stream>>>(sm, s->slotOf, (int)nm, s->m);
     CK(cudaGetLastError());
-    if ((h[1] != 0) != s->kinematicMoving) {
-        s->kinematicMoving = h[1] != 0;
-        s->version++;
-    }
+    s->kin.FromBits((uint32_t)h[1]);
     bepugpu_status st = s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
     if (st != BEPUGPU_OK) return st;
     // whole records back into the caller's arrays
@@ -1497,7 +1555,7 @@ bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepug
         return BEPUGPU_INVALID_ARGUMENT;
     }
     if (!n) return BEPUGPU_OK;
-    int bad = -1, moving = 0;
+    int bad = -1, moving = 0;  // moving: the kinematic bodies' KinematicState bits
     bepugpu_status st = CheckRecords(ctx, s, bodies, sizeof(bepugpu_body) * n, [&](int* check) {
         k_check_body_records<<<Blocks(n, 256), 256, 0, s->stream>>>((const bepugpu_body*)s->staging,
                                                                      s->bodyRecords, (int)n, check);
@@ -1512,10 +1570,7 @@ bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepug
                                                                  s->bodyRecords);
     k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
     CK(cudaGetLastError());
-    if ((moving != 0) != s->kinematicMoving) {
-        s->kinematicMoving = moving != 0;
-        s->version++;
-    }
+    s->kin.FromBits((uint32_t)moving);
     return BEPUGPU_OK;
 }
 
@@ -1794,8 +1849,12 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && nm) {
         cudaEvent_t a = mark(); k_refresh<<<Blocks(nm, T), T, 0, q>>>(ms, s->b, p); spans.push_back({a, mark(), &out->refresh_ms});
     }
-    if ((flags & BEPUGPU_STEP_FORCES) && nb) {
-        cudaEvent_t a = mark(); k_force<<<Blocks(nb, T), T, 0, q>>>(s->b, p); spans.push_back({a, mark(), &out->force_ms});
+    if ((flags & kStartStages) && nb) {
+        ManifoldSoA none = ms;
+        none.count = 0;
+        cudaEvent_t a = mark();
+        k_refresh_force<<<Blocks(nb, T), T, 0, q>>>(none, s->b, p, flags & kStartStages);
+        spans.push_back({a, mark(), &out->force_ms});
     }
     const JointSoA js = s->SweepJoints();
     const int nj = js.count;

@@ -147,6 +147,46 @@ int GroupLaunchCount(const GroupPlan& g);
 // Damping flags bit 2 marks a body stepped by a group kernel.
 constexpr uint32_t kOwnedByGroup = 4u;
 
+// The host's account of a scene's kinematic bodies, from the records it
+// uploaded and the stages it has run since: whether their candidacy and
+// position stages change anything.  A kinematic body's velocity does not
+// change on the device, so its stages follow from its record.  A "still"
+// body (zero velocity, not always active) settles within two candidacy
+// updates: velocity_time_below_limit < 0 becomes 0, 0 becomes 1, and from then
+// on the body is inactive and its stages leave it as it is
+// (SimulationIslandMember.cs:102-122).
+struct KinematicState {
+    bool live = false;   // a kinematic body moves or is always active: stages every step
+    bool neg = false;    // a still body with velocity_time_below_limit < 0
+    bool zero = false;   // a still body with velocity_time_below_limit == 0
+    bool prev = false;   // a still, inactive body whose previous_velocity is not yet 0
+    void Clear() { live = neg = zero = prev = false; }
+    // Adds one kinematic body from its record fields.
+    __host__ __device__ void Add(bool moving, uint32_t activity, float previousVelocity, float timeBelowLimit) {
+        if (moving || (activity & BEPUGPU_BODY_ALWAYS_ACTIVE)) live = true;
+        else if (timeBelowLimit < 0.f) neg = true;
+        else if (timeBelowLimit == 0.f) zero = true;
+        else if (previousVelocity != 0.f) prev = true;
+    }
+    // Whether a step with `flags` changes a kinematic body.
+    bool Needed(uint32_t flags) const {
+        if (live) return (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_POSITIONS)) != 0;
+        return ((flags & BEPUGPU_STEP_DEACTIVATION) && (neg || zero || prev)) ||
+               ((flags & BEPUGPU_STEP_POSITIONS) && (neg || zero));
+    }
+    // The state after a step with `flags`.
+    void Advance(uint32_t flags) {
+        if (flags & BEPUGPU_STEP_DEACTIVATION) {
+            zero = neg;
+            neg = false;
+            prev = false;
+        }
+    }
+    // Record-check word bits (k_check_body_records) and back.
+    __host__ __device__ uint32_t Bits() const { return (live ? 1u : 0u) | (neg ? 2u : 0u) | (zero ? 4u : 0u) | (prev ? 8u : 0u); }
+    void FromBits(uint32_t b) { live = b & 1u; neg = b & 2u; zero = b & 4u; prev = b & 8u; }
+};
+
 // Layout of a scene's device scratch block (kScratchBytes): grid barrier
 // arrival counter, barrier generation, error word, record-check words, census
 // accumulators, timer stamps -- each on its own 128-byte line.
@@ -156,7 +196,7 @@ constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 2
 
 // Byte offsets of a scene's device arrays inside its arena.
 struct ArenaLayout {
-    size_t pos, quat, vlin, vang, inv0, inv1, loc0, loc1, damp, m33;
+    size_t pos, quat, vlin, vang, inv0, inv1, loc0, loc1, damp, m33, act, rawDamp;
     size_t head, cpos, cnrm, offA, offB, mat, pen, fric, axis, pj0, pj1, pj2, s0, s1, s3, s4, s5, s6, s7, lev,
         state, slot, offs;
     size_t jhead, jlanes, jstate, joffs;
@@ -191,17 +231,19 @@ struct Scene {
     int32_t* sweepBodiesDev = nullptr;  // bodies no group steps (valid when groups exist)
     uint32_t sweepBodyCount = 0;
     uint32_t sweepDynamicCount = 0;     // dynamic bodies among them
-    bool kinematicMoving = false;       // a kinematic body has a velocity
+    KinematicState kin;                 // what the kinematic bodies' stages still have to do
     bool asyncPending = false;          // a one-scene step may still run on `stream`
     // Nothing is left for the colour-sweep path: every constraint and dynamic
-    // body is in an island group and no kinematic body moves.
+    // body is in an island group.  (Kinematic bodies may still need their
+    // stages: KinematicState.)
     bool SweepEmpty() const {
         return !groupPlan.groups.empty() && groupPlan.globalCount == 0 && groupPlan.jointGlobalCount == 0 &&
-               sweepDynamicCount == 0 && !kinematicMoving;
+               sweepDynamicCount == 0;
     }
-    // The whole step is island groups without joints or narrow-phase manifolds,
-    // so a batched launch can run it (batch.cu).
-    bool BatchReady() const;
+    // The whole step of `flags` is island groups without joints or
+    // narrow-phase manifolds, and no kinematic body has a stage to run, so a
+    // batched launch can run it (batch.cu).
+    bool BatchReady(uint32_t flags) const;
     // Narrow phase (collide.cu): one shape per body once uploaded, and the
     // slots of GENERATED manifolds.
     std::vector<bepugpu_shape> hostShapes;
@@ -272,6 +314,7 @@ struct Scene {
     std::vector<int32_t> manifoldOffsets;
     std::vector<int32_t> hostSlotOf;
     std::vector<float> hostLinDamp, hostAngDamp, hostLocalM33;
+    std::vector<float2> hostRawDamp;
     std::vector<uint8_t> hostDynamic;
     std::vector<float4> hostDamp;
     bool dampDirty = true;
@@ -285,6 +328,7 @@ struct Scene {
     float graphDt = 0.f;
     uint32_t graphFlags = 0;
     uint64_t version = 1, graphVersion = 0;
+    bool graphTail = false;  // the graph ends with the kinematic bodies' stages
     int graphIterations = -1;
     uint32_t launchesPerStep = 0;
     int persistentBlocks = 0;

@@ -102,12 +102,19 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
     const int tid = threadIdx.x, T = blockDim.x;
     const int lbase = kShared ? 0 : g.mBegin;  // slot of local manifold 0 in ml
 
-    // Bodies into shared memory, through the force update (EntityBase.cs:911-975).
+    // Bodies into shared memory, through the candidacy update
+    // (SimulationIslandMember.cs:53-164) and the force update (EntityBase.cs:911-975).
     for (int i = tid; i < nLocal; i += T) {
         int gi = t.bodies[g.bBegin + i];
         float4 v = b.vlin[gi], w = b.vang[gi], q = b.quat[gi], a, c;
+        float4 act = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_FORCES)) act = b.act[gi];
+        if (flags & BEPUGPU_STEP_DEACTIVATION) {
+            CandidacyMath(v, w, true, act, p);  // a group's bodies are dynamic
+            b.act[gi] = act;
+        }
         if (flags & BEPUGPU_STEP_FORCES) {
-            ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], a, c, p);
+            ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], act, b.rawDamp + gi, a, c, p);
         } else {
             a = b.inv0[gi];
             c = b.inv1[gi];
@@ -233,11 +240,10 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
     for (int i = tid; i < nLocal; i += T) {
         int gi = t.bodies[g.bBegin + i];
         float4 pos = bv.pos[i], q = bv.quat[i], v = bv.vlin[i], w = bv.vang[i];
-        if (flags & BEPUGPU_STEP_POSITIONS) {
-            if (PositionMath(pos, q, v, w, p)) {
-                b.pos[gi] = pos;
-                b.quat[gi] = q;
-            }
+        if (flags & BEPUGPU_STEP_POSITIONS) {  // a group's bodies are dynamic, so active
+            PositionMath(pos, q, v, w, p);
+            b.pos[gi] = pos;
+            b.quat[gi] = q;
         }
         b.vlin[gi] = v;
         b.vang[gi] = w;

@@ -42,8 +42,8 @@ constexpr size_t A(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kBodyArray = A(16 * (size_t)kMaxBodies);       // one float4 per body
 constexpr size_t kLaneArray = A(16 * (size_t)kMaxManifolds);    // one float4 per manifold
 constexpr size_t kLane4Array = A(64 * (size_t)kMaxManifolds);   // four float4 per manifold
-constexpr size_t kBodiesAt = 0;                                  // 9 body arrays
-constexpr size_t kHeadAt = kBodiesAt + 9 * kBodyArray;
+constexpr size_t kBodiesAt = 0;                                  // 11 body arrays
+constexpr size_t kHeadAt = kBodiesAt + 11 * kBodyArray;
 constexpr size_t kLane4At = kHeadAt + kLaneArray;               // cpos cnrm offA offB pj0 pj1 pj2
 constexpr size_t kLaneAt = kLane4At + 7 * kLane4Array;          // mat penacc fricacc saxis s0 s1 s3..s7 lever
 constexpr size_t kStateAt = kLaneAt + 14 * kLaneArray;
@@ -73,10 +73,11 @@ struct Views {
 
 __device__ Views Carve(unsigned char* s, int nb, int nm) {
     Views v;
-    float4* body[9];
-    for (int k = 0; k < 9; k++) body[k] = (float4*)(s + kBodiesAt + k * kBodyArray);
+    float4* body[11];
+    for (int k = 0; k < 11; k++) body[k] = (float4*)(s + kBodiesAt + k * kBodyArray);
     v.b.pos = body[0]; v.b.quat = body[1]; v.b.vlin = body[2]; v.b.vang = body[3]; v.b.inv0 = body[4];
-    v.b.inv1 = body[5]; v.b.loc0 = body[6]; v.b.loc1 = body[7]; v.b.damp = body[8];
+    v.b.inv1 = body[5]; v.b.loc0 = body[6]; v.b.loc1 = body[7]; v.b.damp = body[8]; v.b.act = body[9];
+    v.b.rawDamp = (float2*)body[10];
     v.b.count = nb;
     float4* l4[7];
     for (int k = 0; k < 7; k++) l4[k] = (float4*)(s + kLane4At + k * kLane4Array);
@@ -146,6 +147,8 @@ __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies,
         uint32_t dflags = (lin > 0 ? 1u : 0u) | (ang > 0 ? 2u : 0u);
         v.b.damp[i] = make_float4(DeviceDampingFactor(lin, p.dt), DeviceDampingFactor(ang, p.dt), l[8],
                                   __uint_as_float(dflags));
+        v.b.rawDamp[i] = make_float2(r.linear_damping, r.angular_damping);
+        v.b.act[i] = make_float4(r.previous_velocity, r.velocity_time_below_limit, __uint_as_float(r.activity), 0.f);
         // Matrix3x3.CreateFromQuaternion then MultiplyTransposed / Multiply, as in the force update.
         float qX2 = q.x + q.x, qY2 = q.y + q.y, qZ2 = q.z + q.z;
         float XX = qX2 * q.x, YY = qY2 * q.y, ZZ = qZ2 * q.z;
@@ -235,8 +238,8 @@ __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies,
 
     if (flags & BEPUGPU_STEP_REFRESH_CONTACTS)
         for (int s = t; s < nm; s += kThreads) RefreshManifold(v.m, v.b, s, p);
-    if (flags & BEPUGPU_STEP_FORCES)
-        for (int i = t; i < nb; i += kThreads) ForceUpdateBody(v.b, i, p);
+    if (flags & (BEPUGPU_STEP_FORCES | BEPUGPU_STEP_DEACTIVATION))
+        for (int i = t; i < nb; i += kThreads) StartBodyStep(v.b, i, p, flags);
     __syncthreads();
     if (flags & BEPUGPU_STEP_SOLVE) {
         for (int s = t; s < nm; s += kThreads) PrestepManifold(v.m, v.b, s, p);
@@ -284,6 +287,10 @@ __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies,
         r.orientation[0] = q.x; r.orientation[1] = q.y; r.orientation[2] = q.z; r.orientation[3] = q.w;
         r.linear_velocity[0] = lv.x; r.linear_velocity[1] = lv.y; r.linear_velocity[2] = lv.z;
         r.angular_velocity[0] = av.x; r.angular_velocity[1] = av.y; r.angular_velocity[2] = av.z;
+        const float4 a = v.b.act[i];
+        r.previous_velocity = a.x;
+        r.velocity_time_below_limit = a.y;
+        r.activity = __float_as_uint(a.z);
     }
     for (int i = t; i < nm; i += kThreads) {
         int s = v.slotOf[i], cap = kMaxManifolds;
@@ -313,10 +320,54 @@ __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies,
     }
 }
 
-// Device address of g_stepScratch, looked up once per device with that device
-// current (the first call on each device does it).
+// Device address of g_stepScratch in each CUDA context that has called: the
+// first call made under a context (the device's primary context, or a
+// context the caller created and made current) looks the address up with
+// cudaGetSymbolAddress, which loads the library's module into that context.
+// An address is valid only in the context it was looked up in, so the cache
+// is keyed by the current context (cuCtxGetCurrent, reached through
+// cudaGetDriverEntryPointByVersion so the library does not link the driver).
+typedef int (*CtxGetCurrentFn)(void**);
 std::mutex g_setupLock;
-void* g_scratchAddress[64] = {nullptr};
+CtxGetCurrentFn g_ctxGetCurrent = nullptr;
+bool g_ctxLookedUp = false;
+struct ScratchEntry {
+    void* context;
+    void* address;
+};
+ScratchEntry g_scratchAddress[64];
+int g_scratchEntries = 0;
+
+void* CurrentContext() {
+    void* c = nullptr;
+    if (g_ctxGetCurrent && g_ctxGetCurrent(&c) != 0) c = nullptr;
+    return c;
+}
+
+// The scratch array's address in the current context (null on failure).
+void* ScratchAddress() {
+    std::lock_guard<std::mutex> lock(g_setupLock);
+    if (!g_ctxLookedUp) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctxGetCurrent = (CtxGetCurrentFn)fn;
+        g_ctxLookedUp = true;
+    }
+    void* ctx = CurrentContext();
+    if (ctx)
+        for (int i = 0; i < g_scratchEntries; i++)
+            if (g_scratchAddress[i].context == ctx) return g_scratchAddress[i].address;
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_stepScratch) != cudaSuccess || !ptr) return nullptr;
+    ctx = CurrentContext();  // the runtime has made its context current if none was
+    if (ctx) {
+        if (g_scratchEntries == 64) g_scratchEntries = 0;  // a full table starts over
+        g_scratchAddress[g_scratchEntries++] = {ctx, ptr};
+    }
+    return ptr;
+}
 
 }  // namespace
 
@@ -328,21 +379,14 @@ extern "C" bepugpu_status bepugpu_step_noalloc(const bepugpu_settings* settings,
     if (body_count > (uint32_t)kMaxBodies || manifold_count > (uint32_t)kMaxManifolds)
         return BEPUGPU_INVALID_ARGUMENT;  // beyond the fixed scratch: at most 1024 bodies, 2048 manifolds
     if (!(dt > 0) || !std::isfinite(dt)) return BEPUGPU_INVALID_ARGUMENT;
-    if (settings->iteration_limit < 0 || settings->minimum_iteration_count < 0 ||
-        settings->minimum_iteration_count > 14)
+    // the bounds bepugpu_create and bepugpu_set_settings apply
+    if (settings->iteration_limit < 0 || settings->iteration_limit > 65535 ||
+        settings->minimum_iteration_count < 0 || settings->minimum_iteration_count > 14 ||
+        !(settings->velocity_lower_limit >= 0) || !std::isfinite(settings->velocity_lower_limit) ||
+        !(settings->low_velocity_time_minimum > 0))
         return BEPUGPU_INVALID_ARGUMENT;
-    int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= 64) return BEPUGPU_CUDA_ERROR;
-    void* scratch;
-    {
-        std::lock_guard<std::mutex> lock(g_setupLock);
-        if (!g_scratchAddress[device]) {
-            void* ptr = nullptr;
-            if (cudaGetSymbolAddress(&ptr, g_stepScratch) != cudaSuccess || !ptr) return BEPUGPU_CUDA_ERROR;
-            g_scratchAddress[device] = ptr;
-        }
-        scratch = g_scratchAddress[device];
-    }
+    void* scratch = ScratchAddress();
+    if (!scratch) return BEPUGPU_CUDA_ERROR;
     cudaStream_t s = (cudaStream_t)stream;
     StepParams p = MakeParams(*settings, dt);
     k_step_noalloc<<<1, kThreads, 0, s>>>(bodies, (int)body_count, manifolds, (int)manifold_count, p,

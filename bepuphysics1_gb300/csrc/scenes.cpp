@@ -67,6 +67,10 @@ bepugpu_body MakeRecord(const Body& b) {
     r.angular_damping = .15f;  // EntityBase.cs:1164
     if (b.mass > 0) {
         r.is_dynamic = 1;
+        // Dynamic bodies are always active, as DeterminismTestDemo.cs:84 makes its
+        // boxes: no island of them would go to sleep in the reference either.  The
+        // static bodies keep the default and go inactive after their first step.
+        r.activity = BEPUGPU_BODY_ALWAYS_ACTIVE;
         r.inverse_mass = 1.f / b.mass;
         const float scale = b.mass * 2.5f;  // InertiaHelper.InertiaTensorScale (InertiaHelper.cs:20)
         float i0, i1, i2;

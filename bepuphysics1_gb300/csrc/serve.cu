@@ -397,7 +397,8 @@ struct Server {
             sl.inFlight = true;
             w.slotIds.push_back(id);
             w.reqs.push_back(r);
-            if (cfg.batching && s->BatchReady()) {
+            if (cfg.batching && s->BatchReady(cfg.flags)) {
+                for (uint32_t k = 0; k < r.steps; k++) s->kin.Advance(cfg.flags);
                 const GroupPlan& gp = s->groupPlan;
                 passes = std::max(passes, (int)r.steps);
                 for (int k = gp.shared.begin; k < gp.shared.end; k++) shared.push_back(make_int4(id, k, (int)r.steps, 0));

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/bepugpu.h"
+
 namespace bepugpu {
 
 // Per-step constants (CollisionResponseSettings, CollisionDetectionSettings,
@@ -31,6 +33,10 @@ struct StepParams {
     float minimumImpulse;
     float softness, recoveryStiffness, maxRecoverySpeed, staticThreshold, twistFactor;
     float bounceThreshold, allowedPenetration, invalidationLengthSquared, maximumContactDistance;
+    // DeactivationManager: useStabilization, velocityLowerLimit (and its square, as the
+    // setter computes it), lowVelocityTimeMinimum (DeactivationManager.cs:18-20,36-37,60)
+    int useStabilization;
+    float velocityLowerLimit, velocityLowerLimitSquared, lowVelocityTimeMinimum;
 };
 
 struct BodySoA {
@@ -43,7 +49,17 @@ struct BodySoA {
     float4* loc0;  // local inverse inertia M11 M12 M13 M21
     float4* loc1;  // local inverse inertia M22 M23 M31 M32
     float4* damp;  // linear damping factor, angular damping factor, local M33, flags
+    float4* act;   // activity: previousVelocity, velocityTimeBelowLimit, BEPUGPU_BODY_* bits, 0
+    float2* rawDamp;  // LinearDamping, AngularDamping (read when the stabilization boost applies)
     int count;
+};
+
+// Activity bits in act.z, the ABI's BEPUGPU_BODY_* values.
+enum : uint32_t {
+    kAlwaysActive = 1u,
+    kNoStabilization = 2u,
+    kSlowing = 4u,
+    kCandidate = 8u
 };
 
 // Manifold state bits (word x of the uint2 state).
@@ -142,17 +158,101 @@ __device__ __forceinline__ void ApplyAngular(BodyState& s, float x, float y, flo
     s.wz += x * s.I13 + y * s.I23 + z * s.I33;
 }
 
-// Entity.UpdateForForces (EntityBase.cs:911-975), stabilization boost off.
-// The arithmetic on one body's lanes: v and w in/out, world inverse inertia to
-// a (M11 M12 M13 M21), c (M22 M23 M31 M32) and w.w (M33).
-__device__ __forceinline__ void ForceMath(float4& v, float4& w, float4 q, float4 l0, float4 l1, float4 d, float4& a,
-                                          float4& c, const StepParams& p) {
+// SimulationIslandMember.UpdateDeactivationCandidacy (SimulationIslandMember.cs:53-164)
+// for a body whose island is awake (every dynamic body's: islands are not put
+// to sleep here).  v and w are the body's velocities at the start of the step;
+// act holds previousVelocity, velocityTimeBelowLimit and the activity bits and
+// is rewritten.  The island bookkeeping of the reference (path compression,
+// waking islands next to an active kinematic body) has nothing to do when
+// every island is awake.
+__device__ __forceinline__ void CandidacyMath(float4 v, float4 w, bool dynamic, float4& act, const StepParams& p) {
+    uint32_t f = __float_as_uint(act.z);
+    // velocity = linearVelocity.LengthSquared() + angularVelocity.LengthSquared() (Vector3.cs:64-67)
+    float velocity = (v.x * v.x + v.y * v.y + v.z * v.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
+    float t = act.y;
+    // IsActive (:225-248): the island's state for a dynamic body, the time flag for a kinematic one
+    const bool isActive = dynamic || t <= 0.f;
+    if (isActive) {
+        const bool slowing = velocity <= act.x;
+        f = slowing ? (f | kSlowing) : (f & ~kSlowing);
+        if (dynamic) {
+            if (velocity < p.velocityLowerLimitSquared) t = t + p.dt;
+            else t = 0.f;
+            if (!(f & kAlwaysActive)) {
+                if (!(f & kCandidate)) {
+                    if (t > p.lowVelocityTimeMinimum && slowing) f |= kCandidate;
+                } else if (t <= p.lowVelocityTimeMinimum) {
+                    f &= ~kCandidate;  // the IsDeactivationCandidate setter resets the time (:186-189)
+                    t = 0.f;
+                }
+            } else {
+                f &= ~kCandidate;
+                t = 0.f;
+            }
+        } else {
+            const bool candidate = velocity == 0.f && !(f & kAlwaysActive);
+            if (!candidate) t = 0.f;  // the setter, then the time flag below
+            f = candidate ? (f | kCandidate) : (f & ~kCandidate);
+            if (candidate) {
+                if (t == 0.f) t = 1.f;
+                else if (t < 0.f) t = 0.f;
+            } else {
+                t = -1.f;
+            }
+        }
+    }
+    act.x = velocity;
+    act.y = t;
+    act.z = __uint_as_float(f);
+}
+
+// (float)Math.Pow(MathHelper.Clamp(1 - d, 0, 1), dt) of a boosted damping
+// (EntityBase.cs:943,952), in double like System.Math.Pow.
+__device__ __forceinline__ float BoostedDampingFactor(float d, float dt) {
+    float c = 1 - d;
+    c = c < 0.f ? 0.f : (c > 1.f ? 1.f : c);
+    return (float)pow((double)c, (double)dt);
+}
+
+// Entity.UpdateForForces (EntityBase.cs:911-975).  The arithmetic on one
+// body's lanes: v and w in/out, world inverse inertia to a (M11 M12 M13 M21),
+// c (M22 M23 M31 M32) and w.w (M33).  d.x / d.y are the damping factors of
+// the entity's own damping, computed on the host; act carries the activity
+// state the stabilization boost reads (:926-936), raw the entity's
+// LinearDamping and AngularDamping, read only when the boost applies.
+__device__ __forceinline__ void ForceMath(float4& v, float4& w, float4 q, float4 l0, float4 l1, float4 d, float4 act,
+                                          const float2* raw, float4& a, float4& c, const StepParams& p) {
     uint32_t flags = __float_as_uint(d.w);
     v.x = p.gravityDt[0] + v.x;
     v.y = p.gravityDt[1] + v.y;
     v.z = p.gravityDt[2] + v.z;
-    if (flags & 1u) { v.x = v.x * d.x; v.y = v.y * d.x; v.z = v.z * d.x; }
-    if (flags & 2u) { w.x = w.x * d.y; w.y = w.y * d.y; w.z = w.z * d.y; }
+    const uint32_t af = __float_as_uint(act.z);
+    bool boosted = false;
+    if (p.useStabilization && !(af & kNoStabilization) && ((af & kSlowing) || act.y > p.lowVelocityTimeMinimum)) {
+        float energy = (v.x * v.x + v.y * v.y + v.z * v.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
+        if (energy < p.velocityLowerLimitSquared) {
+            float boost = 1 - (float)(sqrt((double)energy) / (double)(2.f * p.velocityLowerLimit));
+            const float2 r = *raw;
+            // ModifyAngularDamping(boost), then ModifyLinearDamping(boost) (:1205-1221), from zero boosts
+            float angularBoost = 0.f + boost * (1 - (r.y + 0.f));
+            float linearBoost = 0.f + boost * (1 - (r.x + 0.f));
+            float linear = r.x + linearBoost;
+            if (linear > 0) {
+                float f = BoostedDampingFactor(linear, p.dt);
+                v.x = v.x * f; v.y = v.y * f; v.z = v.z * f;
+            }
+            float angular = r.y + angularBoost;
+            if (angular > 0) {
+                float f = BoostedDampingFactor(angular, p.dt);
+                w.x = w.x * f; w.y = w.y * f; w.z = w.z * f;
+            }
+            boosted = true;
+        }
+    }
+    if (!boosted) {
+        if (flags & 1u) { v.x = v.x * d.x; v.y = v.y * d.x; v.z = v.z * d.x; }
+        if (flags & 2u) { w.x = w.x * d.y; w.y = w.y * d.y; w.z = w.z * d.y; }
+    }
     // orientationMatrix = Matrix3x3.CreateFromQuaternion(orientation) (Matrix3x3.cs:1303-1328)
     float qX2 = q.x + q.x, qY2 = q.y + q.y, qZ2 = q.z + q.z;
     float XX = qX2 * q.x, YY = qY2 * q.y, ZZ = qZ2 * q.z;
@@ -184,24 +284,33 @@ __device__ __forceinline__ void ForceMath(float4& v, float4& w, float4 q, float4
     c.w = m31 * R12 + m32 * R22 + m33 * R32;
     w.w = m31 * R13 + m32 * R23 + m33 * R33;
 }
-__device__ __forceinline__ void ForceUpdateBody(const BodySoA& b, int i, const StepParams& p) {
-    float4 pos = b.pos[i];
-    if (pos.w == 0.f) return;  // ForceUpdater only holds dynamic entities
+// The body stages of one body at the start of a step: the candidacy update
+// (BEPUGPU_STEP_DEACTIVATION, every body) and the force update
+// (BEPUGPU_STEP_FORCES, dynamic bodies: ForceUpdater only holds those).
+__device__ __forceinline__ void StartBodyStep(const BodySoA& b, int i, const StepParams& p, uint32_t stages) {
+    const float4 pos = b.pos[i];
+    const bool dynamic = pos.w != 0.f;
+    float4 act = b.act[i];
+    if (stages & BEPUGPU_STEP_DEACTIVATION) {
+        CandidacyMath(b.vlin[i], b.vang[i], dynamic, act, p);
+        b.act[i] = act;
+    }
+    if (!dynamic || !(stages & BEPUGPU_STEP_FORCES)) return;
     float4 v = b.vlin[i], w = b.vang[i], q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i], d = b.damp[i];
     float4 a, c;
-    ForceMath(v, w, q, l0, l1, d, a, c, p);
+    ForceMath(v, w, q, l0, l1, d, act, b.rawDamp + i, a, c, p);
     b.vlin[i] = v;
     b.vang[i] = w;
     b.inv0[i] = a;
     b.inv1[i] = c;
 }
 
-// Entity.PreUpdatePosition, Discrete mode (EntityBase.cs:1124-1160).  Returns
-// false for a body that does not move this step.
-__device__ __forceinline__ bool PositionMath(float4& pos, float4& q, float4 v, float4 w, const StepParams& p) {
-    // Kinematic entities are integrated while they move (SimulationIslandMember.cs:225-248).
-    if (pos.w == 0.f && v.x == 0.f && v.y == 0.f && v.z == 0.f && w.x == 0.f && w.y == 0.f && w.z == 0.f)
-        return false;
+// Entity.PreUpdatePosition, Discrete mode (EntityBase.cs:1124-1160), for an
+// active body (the position updater skips inactive ones,
+// ContinuousPositionUpdater.cs:71): every dynamic body, and a kinematic body
+// while its velocityTimeBelowLimit flag is <= 0 (SimulationIslandMember.cs:225-248).
+__device__ __forceinline__ bool BodyActive(float4 pos, float4 act) { return pos.w != 0.f || act.y <= 0.f; }
+__device__ __forceinline__ void PositionMath(float4& pos, float4& q, float4 v, float4 w, const StepParams& p) {
     float h = p.dt * .5f;
     float ix = w.x * h, iy = w.y * h, iz = w.z * h;
     // Quaternion.Multiply(multiplier = (ix, iy, iz, 0), orientation) (Quaternion.cs:66-79)
@@ -217,11 +326,11 @@ __device__ __forceinline__ bool PositionMath(float4& pos, float4& q, float4 v, f
     pos.x = pos.x + v.x * p.dt;
     pos.y = pos.y + v.y * p.dt;
     pos.z = pos.z + v.z * p.dt;
-    return true;
 }
 __device__ __forceinline__ void PositionUpdateBody(const BodySoA& b, int i, const StepParams& p) {
     float4 pos = b.pos[i], q = b.quat[i];
-    if (!PositionMath(pos, q, b.vlin[i], b.vang[i], p)) return;
+    if (!BodyActive(pos, b.act[i])) return;
+    PositionMath(pos, q, b.vlin[i], b.vang[i], p);
     b.quat[i] = q;
     b.pos[i] = pos;
 }

@@ -22,12 +22,14 @@ SETTINGS_DTYPE = np.dtype([
     ("static_friction_velocity_threshold", "<f4"), ("twist_friction_factor", "<f4"),
     ("bounciness_velocity_threshold", "<f4"), ("allowed_penetration", "<f4"),
     ("contact_invalidation_length_squared", "<f4"), ("maximum_contact_distance", "<f4"),
-    ("reserved", "<i4", 4),
+    ("use_stabilization", "<i4"), ("velocity_lower_limit", "<f4"), ("low_velocity_time_minimum", "<f4"),
+    ("reserved", "<i4"),
 ])
 BODY_DTYPE = np.dtype([
     ("position", "<f4", 3), ("orientation", "<f4", 4), ("linear_velocity", "<f4", 3),
     ("angular_velocity", "<f4", 3), ("inverse_mass", "<f4"), ("local_inverse_inertia", "<f4", 9),
-    ("linear_damping", "<f4"), ("angular_damping", "<f4"), ("is_dynamic", "<i4"), ("reserved", "<i4"),
+    ("linear_damping", "<f4"), ("angular_damping", "<f4"), ("is_dynamic", "<i4"), ("activity", "<u4"),
+    ("previous_velocity", "<f4"), ("velocity_time_below_limit", "<f4"),
 ])
 CONTACT_DTYPE = np.dtype([
     ("position", "<f4", 3), ("normal", "<f4", 3), ("penetration_depth", "<f4"), ("id", "<i4"),
@@ -96,7 +98,9 @@ OK, INVALID_ARGUMENT, OUT_OF_MEMORY, ADMISSION_REFUSED, CUDA_ERROR, TIMEOUT, NAN
 STATUS_NAMES = ["OK", "INVALID_ARGUMENT", "OUT_OF_MEMORY", "ADMISSION_REFUSED", "CUDA_ERROR", "TIMEOUT",
                 "NAN_DETECTED", "NOT_FOUND", "QUEUE_FULL", "INVALID_OPERATION"]
 
-STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_COLLIDE, STEP_ALL = 1, 2, 4, 8, 16, 31
+STEP_REFRESH_CONTACTS, STEP_FORCES, STEP_SOLVE, STEP_POSITIONS, STEP_COLLIDE = 1, 2, 4, 8, 16
+STEP_DEACTIVATION, STEP_ALL = 32, 63
+BODY_ALWAYS_ACTIVE, BODY_NO_STABILIZATION, BODY_SLOWING, BODY_DEACTIVATION_CANDIDATE = 1, 2, 4, 8
 SHAPE_NONE, SHAPE_BOX, SHAPE_SPHERE = 0, 1, 2
 NOALLOC_MAX_BODIES, NOALLOC_MAX_MANIFOLDS = 1024, 2048  # bepugpu_step_noalloc limits
 MODE_GRAPH, MODE_PERSISTENT = 0, 1

@@ -173,6 +173,11 @@ class GpuSpace:
         """Space.Update's velocity and integration stages in pipeline order."""
         self.ctx.check(self.ctx.lib.bepugpu_step(self.ctx.handle, self.id, float(dt), flags))
 
+    def deactivation_update(self, dt: float):
+        """DeactivationManager.Update's per-member part: every body's
+        UpdateDeactivationCandidacy (SimulationIslandMember.cs:53-164)."""
+        self.step(dt, N.STEP_DEACTIVATION)
+
     def force_update(self, dt: float):
         self.step(dt, N.STEP_FORCES)
 

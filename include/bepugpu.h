@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 5
+#define BEPUGPU_ABI_VERSION 6
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -63,12 +63,29 @@ typedef struct bepugpu_settings {
     float allowed_penetration;             /* CollisionDetectionSettings.AllowedPenetration, :74 (.01) */
     float contact_invalidation_length_squared; /* CollisionDetectionSettings, :11 (.01) */
     float maximum_contact_distance;        /* CollisionDetectionSettings, :82 (.1) */
-    int32_t reserved[4];
+    int32_t use_stabilization;             /* DeactivationManager.UseStabilization,
+                                              DeactivationManager.cs:60,67 (1): the force update's
+                                              low-velocity damping boost, EntityBase.cs:926-936 */
+    float velocity_lower_limit;            /* DeactivationManager.VelocityLowerLimit, :18,28 (.26) */
+    float low_velocity_time_minimum;       /* DeactivationManager.LowVelocityTimeMinimum, :20,46 (1) */
+    int32_t reserved;
 } bepugpu_settings;
 
+/* Body activity flags: the state of the entity's SimulationIslandMember
+ * (DeactivationManagement/SimulationIslandMember.cs) that the step reads and
+ * writes.  0 is the reference's default for a new entity. */
+#define BEPUGPU_BODY_ALWAYS_ACTIVE        1u  /* IsAlwaysActive (:284-297) */
+#define BEPUGPU_BODY_NO_STABILIZATION     2u  /* AllowStabilization = false (:305-315; default true) */
+#define BEPUGPU_BODY_SLOWING              4u  /* isSlowing (:19), written by the candidacy update */
+#define BEPUGPU_BODY_DEACTIVATION_CANDIDATE 8u /* IsDeactivationCandidate (:171-190), written likewise */
+
 /* One rigid body, as the C# shim reads it from an Entity (EntityBase.cs:35-43,
- * 303-347, 1164-1165).  Kinematic bodies have is_dynamic = 0; their inverse
- * mass and inverse inertia are ignored by the solver, as in the reference. */
+ * 303-347, 1164-1165) and its activity information.  Kinematic bodies have
+ * is_dynamic = 0; their inverse mass and inverse inertia are ignored by the
+ * solver, as in the reference.  A kinematic body takes part in the position
+ * update while it is active: velocity_time_below_limit <= 0
+ * (SimulationIslandMember.IsActive, :225-248).  Every dynamic body's island is
+ * awake: the library does not put islands to sleep. */
 typedef struct bepugpu_body {
     float position[3];
     float orientation[4];            /* quaternion x, y, z, w */
@@ -79,7 +96,9 @@ typedef struct bepugpu_body {
     float linear_damping;            /* Entity.LinearDamping (.03) */
     float angular_damping;           /* Entity.AngularDamping (.15) */
     int32_t is_dynamic;
-    int32_t reserved;
+    uint32_t activity;               /* BEPUGPU_BODY_*, in/out */
+    float previous_velocity;         /* SimulationIslandMember.previousVelocity (:17), in/out */
+    float velocity_time_below_limit; /* SimulationIslandMember.velocityTimeBelowLimit (:18), in/out */
 } bepugpu_body;
 
 /* One contact of a convex manifold (Contact.cs:15-31) together with the
@@ -281,13 +300,16 @@ typedef struct bepugpu_joint {
 
 typedef struct bepugpu_context bepugpu_context;
 
-/* Step flags: which stages bepugpu_step runs, in pipeline order. */
+/* Step flags: which stages bepugpu_step runs. */
 #define BEPUGPU_STEP_REFRESH_CONTACTS 1u  /* ContactRefresher on every manifold */
 #define BEPUGPU_STEP_FORCES           2u  /* ForceUpdater */
 #define BEPUGPU_STEP_SOLVE            4u  /* Solver */
 #define BEPUGPU_STEP_POSITIONS        8u  /* PositionUpdater (Discrete) */
 #define BEPUGPU_STEP_COLLIDE         16u  /* narrow phase of GENERATED manifolds (NarrowPhase) */
-#define BEPUGPU_STEP_ALL              31u
+#define BEPUGPU_STEP_DEACTIVATION    32u  /* DeactivationManager.Update's per-member part: every
+                                             body's UpdateDeactivationCandidacy
+                                             (SimulationIslandMember.cs:53-164), before the forces */
+#define BEPUGPU_STEP_ALL              63u
 
 /* Collision shapes, one per body, for the narrow phase. */
 #define BEPUGPU_SHAPE_NONE   0
@@ -502,16 +524,25 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float d
  * and BEPUGPU_NOALLOC_MAX_MANIFOLDS manifolds and returns
  * BEPUGPU_INVALID_ARGUMENT above that.  The step runs on the current device, on
  * `stream` (a cudaStream_t, NULL = legacy default stream), in one thread block,
- * and the call returns when it is done.  The first call on a device looks up
- * the scratch array's device address; make that first call before any stream
- * capture.  Calls share the scratch array: calls whose work overlaps on the GPU
- * (other host threads, other streams) race and must be serialised by the
- * caller.  Damping factors are computed with the device's double pow.  There
- * is no narrow phase here: GENERATED manifolds are stepped with the contacts
- * they hold (and not refreshed). */
+ * and the call returns when it is done.  The first call made under a CUDA
+ * context (the device's primary context, or one the caller created and made
+ * current) looks up the scratch array's address in that context and keeps it
+ * for later calls under the same context; make that first call before any
+ * stream capture.  Calls share the scratch array: calls whose work overlaps
+ * on the GPU (other host threads, other streams) race and must be serialised
+ * by the caller.  The manifold list is coloured in the call with at most 128
+ * colours (two 64-bit masks per body): a list that needs more returns
+ * BEPUGPU_INVALID_OPERATION with the records unchanged, where
+ * bepugpu_upload_constraints has no colour limit.  Records whose manifolds
+ * name bodies out of range, the same body twice or a contact count outside
+ * 0..4 return BEPUGPU_INVALID_ARGUMENT, found on the device before anything is
+ * written.  Settings are bounded as bepugpu_create bounds them.  Damping
+ * factors are computed with the device's double pow.  There is no narrow
+ * phase here: GENERATED manifolds are stepped with the contacts they hold
+ * (and not refreshed). */
 #define BEPUGPU_NOALLOC_MAX_BODIES 1024
 #define BEPUGPU_NOALLOC_MAX_MANIFOLDS 2048
-#define BEPUGPU_NOALLOC_SCRATCH_BYTES 1606656
+#define BEPUGPU_NOALLOC_SCRATCH_BYTES 1639424
 bepugpu_status bepugpu_step_noalloc(const bepugpu_settings* settings, bepugpu_body* bodies,
                                     uint32_t body_count, bepugpu_manifold* manifolds,
                                     uint32_t manifold_count, float dt, uint32_t flags, void* stream);

@@ -104,10 +104,10 @@ class OracleSpace:
     def set_order_mode(self, mode: int, permutation_index: int = 0):
         self.lib.oracle_set_order_mode(self.h, mode, permutation_index)
 
-    def step(self, dt: float, flags: int = 31, steps: int = 1):
+    def step(self, dt: float, flags: int = 63, steps: int = 1):
         self.lib.oracle_step(self.h, dt, flags, steps)
 
-    def step_multithreaded(self, dt: float, flags: int = 31, steps: int = 1, threads: int = 8):
+    def step_multithreaded(self, dt: float, flags: int = 63, steps: int = 1, threads: int = 8):
         self.lib.oracle_step_multithreaded(self.h, dt, flags, steps, threads)
 
     def get_bodies(self):

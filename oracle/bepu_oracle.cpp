@@ -36,6 +36,9 @@ struct Settings {
     int maximumIterationCount;
     float softness, recoveryStiffness, maxRecoverySpeed, staticThreshold, twistFactor,
         bounceThreshold, allowedPenetration, invalidationLengthSquared, maximumContactDistance;
+    // DeactivationManager (DeactivationManager.cs:18-20,60)
+    bool useStabilization = true;
+    float velocityLowerLimit = .26f, velocityLowerLimitSquared = .26f * .26f, lowVelocityTimeMinimum = 1;
 };
 
 // ---------------------------------------------------------------- PermutationMapper --
@@ -85,6 +88,61 @@ struct Entity {
     float linearDamping = .03f, angularDamping = .15f;
     bool isDynamic = false;
     SpinLock locker;
+    // activityInformation (SimulationIslandMember.cs:17-19, 278-312).  Every
+    // dynamic body's simulation island is awake here.
+    float previousVelocity = 0, velocityTimeBelowLimit = 0;
+    bool isSlowing = false, isDeactivationCandidate = false, isAlwaysActive = false, allowStabilization = true;
+    float linearDampingBoost = 0, angularDampingBoost = 0;
+
+    // SimulationIslandMember.IsActive (:225-248)
+    bool IsActive() const { return isDynamic || velocityTimeBelowLimit <= 0; }
+    // The IsDeactivationCandidate setter (:171-190)
+    void SetDeactivationCandidate(bool value) {
+        isDeactivationCandidate = value;
+        if (!value) velocityTimeBelowLimit = 0;
+    }
+    // SimulationIslandMember.UpdateDeactivationCandidacy (:53-164), island awake.
+    void UpdateDeactivationCandidacy(float dt, const Settings& s) {
+        float velocity = LengthSquared(linearVelocity) + LengthSquared(angularVelocity);
+        bool isActive = IsActive();
+        if (isActive) {
+            isSlowing = velocity <= previousVelocity;
+            if (isDynamic) {
+                if (velocity < s.velocityLowerLimitSquared) velocityTimeBelowLimit += dt;
+                else velocityTimeBelowLimit = 0;
+                if (!isAlwaysActive) {
+                    if (!isDeactivationCandidate) {
+                        if (velocityTimeBelowLimit > s.lowVelocityTimeMinimum && isSlowing)
+                            SetDeactivationCandidate(true);
+                    } else {
+                        if (velocityTimeBelowLimit <= s.lowVelocityTimeMinimum) SetDeactivationCandidate(false);
+                    }
+                } else {
+                    SetDeactivationCandidate(false);
+                }
+            } else {
+                SetDeactivationCandidate(velocity == 0 && !isAlwaysActive);
+                if (isDeactivationCandidate) {
+                    if (velocityTimeBelowLimit == 0) velocityTimeBelowLimit = 1;
+                    else if (velocityTimeBelowLimit < 0) velocityTimeBelowLimit = 0;
+                } else {
+                    velocityTimeBelowLimit = -1;
+                }
+            }
+        }
+        previousVelocity = velocity;
+    }
+    // EntityBase.ModifyLinearDamping / ModifyAngularDamping (EntityBase.cs:1205-1221)
+    void ModifyLinearDamping(float damping) {
+        float totalDamping = linearDamping + linearDampingBoost;
+        float remainder = 1 - totalDamping;
+        linearDampingBoost += damping * remainder;
+    }
+    void ModifyAngularDamping(float damping) {
+        float totalDamping = angularDamping + angularDampingBoost;
+        float remainder = 1 - totalDamping;
+        angularDampingBoost += damping * remainder;
+    }
 
     // EntityBase.cs:754-761
     void ApplyLinearImpulse(const Vec3& impulse) {
@@ -99,16 +157,27 @@ struct Entity {
         angularVelocity.Y += impulse.X * I.M12 + impulse.Y * I.M22 + impulse.Z * I.M32;
         angularVelocity.Z += impulse.X * I.M13 + impulse.Y * I.M23 + impulse.Z * I.M33;
     }
-    // EntityBase.cs:911-975 (stabilization off: DeactivationManager.useStabilization
-    // is not modelled; the boost terms are zero).
-    void UpdateForForces(float dt, const Vec3& gravityDt) {
+    // EntityBase.cs:911-975
+    void UpdateForForces(float dt, const Vec3& gravityDt, const Settings& s) {
         linearVelocity = Add(gravityDt, linearVelocity);
-        float linear = linearDamping + 0.f;
+        // Boost damping at very low velocities (:926-936).
+        if (s.useStabilization && allowStabilization &&
+            (isSlowing || velocityTimeBelowLimit > s.lowVelocityTimeMinimum)) {
+            float energy = LengthSquared(linearVelocity) + LengthSquared(angularVelocity);
+            if (energy < s.velocityLowerLimitSquared) {
+                float boost = 1 - (float)(std::sqrt((double)energy) / (double)(2.f * s.velocityLowerLimit));
+                ModifyAngularDamping(boost);
+                ModifyLinearDamping(boost);
+            }
+        }
+        float linear = linearDamping + linearDampingBoost;
         if (linear > 0)
             linearVelocity = Multiply(linearVelocity, (float)std::pow((double)Clamp(1 - linear, 0, 1), (double)dt));
-        float angular = angularDamping + 0.f;
+        float angular = angularDamping + angularDampingBoost;
         if (angular > 0)
             angularVelocity = Multiply(angularVelocity, (float)std::pow((double)Clamp(1 - angular, 0, 1), (double)dt));
+        linearDampingBoost = 0;
+        angularDampingBoost = 0;
         Mat3 multiplied = MultiplyTransposed(orientationMatrix, localInertiaTensorInverse);
         inertiaTensorInverse = Multiply(multiplied, orientationMatrix);
     }
@@ -1049,11 +1118,16 @@ static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
             if (!m->generated) RefreshManifold(*m, sp.s);
         }
     }
-    if (flags & BEPUGPU_STEP_FORCES) {  // ForceUpdater.cs:85-92
+    if (flags & BEPUGPU_STEP_DEACTIVATION) {  // DeactivationManager.cs:206-224, the candidacy loop
+        auto body = [&](long long i) { sp.entities[i].UpdateDeactivationCandidacy(dt, sp.s); };
+        if (threads > 1) ForLoop(threads, 0, (long long)sp.entities.size(), body);
+        else for (size_t i = 0; i < sp.entities.size(); i++) body((long long)i);
+    }
+    if (flags & BEPUGPU_STEP_FORCES) {  // ForceUpdater.cs:73-92
         Vec3 gravityDt = Multiply(sp.s.gravity, dt);
         auto body = [&](long long i) {
             Entity& e = sp.entities[i];
-            if (e.isDynamic) e.UpdateForForces(dt, gravityDt);
+            if (e.isDynamic && e.IsActive()) e.UpdateForForces(dt, gravityDt, sp.s);
         };
         if (threads > 1) ForLoop(threads, 0, (long long)sp.entities.size(), body);
         else for (size_t i = 0; i < sp.entities.size(); i++) body((long long)i);
@@ -1064,13 +1138,12 @@ static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
         if (threads > 1) SolverUpdateMultithreaded(sp, dt, threads);
         else SolverUpdateSingleThreaded(sp, dt);
     }
-    if (flags & BEPUGPU_STEP_POSITIONS) {  // ContinuousPositionUpdater.cs:134-154, Discrete bodies
-        // Kinematic entities take part while they move (SimulationIslandMember.cs:225-248).
+    if (flags & BEPUGPU_STEP_POSITIONS) {  // ContinuousPositionUpdater.cs:49-74,134-154, Discrete bodies
+        // Active entities only (:71): kinematic ones while their time flag is <= 0
+        // (SimulationIslandMember.cs:225-248).
         auto body = [&](long long i) {
             Entity& e = sp.entities[i];
-            const Vec3 &v = e.linearVelocity, &w = e.angularVelocity;
-            bool moving = v.X != 0 || v.Y != 0 || v.Z != 0 || w.X != 0 || w.Y != 0 || w.Z != 0;
-            if (e.isDynamic || moving) e.PreUpdatePosition(dt);
+            if (e.IsActive()) e.PreUpdatePosition(dt);
         };
         if (threads > 1) ForLoop(threads, 0, (long long)sp.entities.size(), body);
         else for (size_t i = 0; i < sp.entities.size(); i++) body((long long)i);
@@ -1110,6 +1183,10 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
     S.allowedPenetration = st->allowed_penetration;
     S.invalidationLengthSquared = st->contact_invalidation_length_squared;
     S.maximumContactDistance = st->maximum_contact_distance;
+    S.useStabilization = st->use_stabilization != 0;
+    S.velocityLowerLimit = std::max(0.f, st->velocity_lower_limit);  // DeactivationManager.cs:36-37
+    S.velocityLowerLimitSquared = S.velocityLowerLimit * S.velocityLowerLimit;
+    S.lowVelocityTimeMinimum = st->low_velocity_time_minimum;
 
     sp.entities = std::vector<Entity>(nb);
     for (int i = 0; i < nb; i++) {
@@ -1130,6 +1207,12 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
         e.inertiaTensorInverse = Multiply(mult, e.orientationMatrix);
         e.linearDamping = b.linear_damping;
         e.angularDamping = b.angular_damping;
+        e.previousVelocity = b.previous_velocity;
+        e.velocityTimeBelowLimit = b.velocity_time_below_limit;
+        e.isAlwaysActive = (b.activity & BEPUGPU_BODY_ALWAYS_ACTIVE) != 0;
+        e.allowStabilization = (b.activity & BEPUGPU_BODY_NO_STABILIZATION) == 0;
+        e.isSlowing = (b.activity & BEPUGPU_BODY_SLOWING) != 0;
+        e.isDeactivationCandidate = (b.activity & BEPUGPU_BODY_DEACTIVATION_CANDIDATE) != 0;
     }
     sp.world.index = -1;
     sp.world.orientationMatrix = CreateFromQuaternion(sp.world.orientation);
@@ -1244,6 +1327,12 @@ void oracle_get_bodies(oracle_space* s, bepugpu_body* out) {
         b.orientation[2] = e.orientation.Z; b.orientation[3] = e.orientation.W;
         P3(b.linear_velocity, e.linearVelocity);
         P3(b.angular_velocity, e.angularVelocity);
+        b.previous_velocity = e.previousVelocity;
+        b.velocity_time_below_limit = e.velocityTimeBelowLimit;
+        b.activity = (e.isAlwaysActive ? BEPUGPU_BODY_ALWAYS_ACTIVE : 0u) |
+                     (e.allowStabilization ? 0u : BEPUGPU_BODY_NO_STABILIZATION) |
+                     (e.isSlowing ? BEPUGPU_BODY_SLOWING : 0u) |
+                     (e.isDeactivationCandidate ? BEPUGPU_BODY_DEACTIVATION_CANDIDATE : 0u);
     }
 }
 

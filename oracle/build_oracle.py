@@ -13,7 +13,8 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "liboracle.so"
 SOURCES = [HERE / "bepu_oracle.cpp"]
 DEPS = SOURCES + [HERE / "bepu_oracle.h", HERE / "bepu_math.h", HERE / "bepu_oracle_joints.inc",
-                  HERE / "permutation_primes.inc", HERE.parent / "include" / "bepugpu.h"]
+                  HERE / "bepu_oracle_collide.inc", HERE / "permutation_primes.inc",
+                  HERE.parent / "include" / "bepugpu.h"]
 
 
 def build() -> str:

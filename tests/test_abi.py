@@ -37,8 +37,9 @@ def test_binding_covers_header():
 
 def test_record_sizes():
     lib = N.load_gpu_library()
-    assert lib.bepugpu_abi_version() == 5
-    assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 108
+    assert lib.bepugpu_abi_version() == 6
+    assert lib.bepugpu_record_size(0) == N.SETTINGS_DTYPE.itemsize
+    assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 116
     assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 64
     assert lib.bepugpu_record_size(3) == N.MANIFOLD_DTYPE.itemsize
     assert lib.bepugpu_record_size(4) == N.JOINT_DTYPE.itemsize
@@ -57,6 +58,9 @@ def test_default_settings_are_the_reference_defaults():
     assert s["static_friction_velocity_threshold"] == np.float32(0.2)
     assert s["allowed_penetration"] == np.float32(0.01)     # CollisionDetectionSettings.cs:74
     assert tuple(s["gravity"]) == (0, np.float32(-9.81), 0)
+    assert s["use_stabilization"] == 1                      # DeactivationManager.cs:60
+    assert s["velocity_lower_limit"] == np.float32(0.26)    # DeactivationManager.cs:18
+    assert s["low_velocity_time_minimum"] == 1              # DeactivationManager.cs:20
 
 
 def test_create_without_device_fails_cleanly():
