@@ -128,6 +128,29 @@ __global__ void k_bounded_wait_probe(volatile unsigned int* flag, unsigned int l
     *status = BEPUGPU_OK;
 }
 
+// The device's float results of the reference's double expressions
+// (double_rounding.cuh) over n inputs; `fast` counts the inputs the FP32
+// path decided.
+__global__ void k_probe_double_rounding(int kind, const float* __restrict__ a, const float* __restrict__ b, int n,
+                                        float* __restrict__ out, unsigned int* fast) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float r = 0.f;
+    bool f = false;
+    if (kind == 0) {
+        f = dr::TryInvSqrt(a[i], r);
+        if (!f) r = dr::InvSqrtAsDouble(a[i]);
+    } else if (kind == 1) {
+        f = dr::TrySqrtQuotient(a[i], b[i], r);
+        if (!f) r = dr::SqrtQuotientAsDouble(a[i], b[i]);
+    } else {
+        f = dr::TryPow(a[i], b[i], r);
+        if (!f) r = dr::PowAsDouble(a[i], b[i]);
+    }
+    out[i] = r;
+    if (f) atomicAdd(fast, 1u);
+}
+
 // Checks of the update calls, before anything is written: check[0] receives
 // the lowest offending record index (stays INT_MAX when none), check[1] the
 // KinematicState bits of the kinematic bodies.
@@ -1571,6 +1594,46 @@ bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepug
     k_world_inertia<<<Blocks(n, 256), 256, 0, s->stream>>>(s->b, s->localM33);
     CK(cudaGetLastError());
     s->kin.FromBits((uint32_t)moving);
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_probe_double_rounding(bepugpu_context* c, int32_t kind, const float* a, const float* b,
+                                             uint32_t n, float* out, uint32_t* fast) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    if (kind < 0 || kind > 2 || (n && (!a || !out || (kind > 0 && !b))) || n > (1u << 26)) {
+        ctx->SetError("probe_double_rounding: kind 0..2, inputs and output given, at most 2^26 values");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (fast) *fast = 0;
+    if (!n) return BEPUGPU_OK;
+    float *da = nullptr, *db = nullptr, *dout = nullptr;
+    unsigned int* dfast = nullptr;
+    auto release = [&]() {
+        cudaFree(da);
+        cudaFree(db);
+        cudaFree(dout);
+        cudaFree(dfast);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&da, 4ull * n)) || (e = cudaMalloc(&db, 4ull * n)) || (e = cudaMalloc(&dout, 4ull * n)) ||
+        (e = cudaMalloc(&dfast, 4)) || (e = cudaMemcpy(da, a, 4ull * n, cudaMemcpyHostToDevice)) ||
+        (e = cudaMemset(db, 0, 4ull * n)) || (kind > 0 && (e = cudaMemcpy(db, b, 4ull * n, cudaMemcpyHostToDevice))) ||
+        (e = cudaMemset(dfast, 0, 4))) {
+        release();
+        ctx->SetError("probe_double_rounding: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    k_probe_double_rounding<<<Blocks((int)n, 256), 256>>>(kind, da, db, (int)n, dout, dfast);
+    unsigned int h = 0;
+    if ((e = cudaGetLastError()) || (e = cudaMemcpy(out, dout, 4ull * n, cudaMemcpyDeviceToHost)) ||
+        (e = cudaMemcpy(&h, dfast, 4, cudaMemcpyDeviceToHost))) {
+        release();
+        ctx->SetError("probe_double_rounding: %s", cudaGetErrorString(e));
+        return BEPUGPU_CUDA_ERROR;
+    }
+    release();
+    if (fast) *fast = h;
     return BEPUGPU_OK;
 }
 

@@ -246,7 +246,7 @@ __device__ __forceinline__ ClipEdge EdgeOf(const Face& f, int i) {
     c.b = f.v[ib];
     c.id = EdgeId(f.id[i], f.id[ib]);
     V3 dir = c.b - c.a;
-    float inverse = (float)(1.0 / sqrt((double)(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z)));
+    float inverse = dr::InvSqrtAsDouble(dir.x * dir.x + dir.y * dir.y + dir.z * dir.z);
     dir = mk(dir.x * inverse, dir.y * inverse, dir.z * inverse);
     c.perp = cross(dir, f.normal);
     if (dot(c.perp, f.v[in] - c.a) > 0) c.perp = -c.perp;

@@ -255,7 +255,7 @@ __device__ __forceinline__ float JDot(float3 a, float3 b) { return a.x * b.x + a
 __device__ __forceinline__ float3 JXYZ(float4 v) { return make_float3(v.x, v.y, v.z); }
 // Vector3.Normalize (Vector3.cs:81-87): the reciprocal square root in double.
 __device__ __forceinline__ float3 JNormalize(float3 v) {
-    float inverse = (float)(1.0 / sqrt((double)(v.x * v.x + v.y * v.y + v.z * v.z)));
+    float inverse = dr::InvSqrtAsDouble(v.x * v.x + v.y * v.y + v.z * v.z);
     return make_float3(v.x * inverse, v.y * inverse, v.z * inverse);
 }
 __device__ __forceinline__ JM3 JInertia(const BodyState& s) {
@@ -344,7 +344,7 @@ __device__ __forceinline__ void JAxisAngle(float4 q, float3& axis, float& angle)
 }
 // Quaternion.Normalize: the reciprocal square root in double.
 __device__ __forceinline__ float4 JQNormalize(float4 q) {
-    float inverse = (float)(1.0 / sqrt((double)(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w)));
+    float inverse = dr::InvSqrtAsDouble(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
     return make_float4(q.x * inverse, q.y * inverse, q.z * inverse, q.w * inverse);
 }
 // Quaternion.GetQuaternionBetweenNormalizedVectors (Quaternion.cs:795-823)

@@ -100,12 +100,12 @@ __device__ Views Carve(unsigned char* s, int nb, int nm) {
     return v;
 }
 
-// (float)Math.Pow(Clamp(1 - d, 0, 1), dt) (EntityBase.cs:943,952), here with
-// CUDA's double pow on the device.
+// (float)Math.Pow(Clamp(1 - d, 0, 1), dt) (EntityBase.cs:943,952), here on
+// the device: the float the double result rounds to.
 __device__ float DeviceDampingFactor(float d, float dt) {
     float c = 1 - d;
     c = c < 0 ? 0 : (c > 1 ? 1 : c);
-    return (float)pow((double)c, (double)dt);
+    return dr::PowAsDouble(c, dt);
 }
 
 __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies, int nb, bepugpu_manifold* man,

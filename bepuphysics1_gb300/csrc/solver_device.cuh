@@ -18,6 +18,7 @@
 #include <stdint.h>
 
 #include "../../include/bepugpu.h"
+#include "double_rounding.cuh"
 
 namespace bepugpu {
 
@@ -207,11 +208,11 @@ __device__ __forceinline__ void CandidacyMath(float4 v, float4 w, bool dynamic, 
 }
 
 // (float)Math.Pow(MathHelper.Clamp(1 - d, 0, 1), dt) of a boosted damping
-// (EntityBase.cs:943,952), in double like System.Math.Pow.
+// (EntityBase.cs:943,952): the float System.Math.Pow's double result rounds to.
 __device__ __forceinline__ float BoostedDampingFactor(float d, float dt) {
     float c = 1 - d;
     c = c < 0.f ? 0.f : (c > 1.f ? 1.f : c);
-    return (float)pow((double)c, (double)dt);
+    return dr::PowAsDouble(c, dt);
 }
 
 // Entity.UpdateForForces (EntityBase.cs:911-975).  The arithmetic on one
@@ -231,7 +232,7 @@ __device__ __forceinline__ void ForceMath(float4& v, float4& w, float4 q, float4
     if (p.useStabilization && !(af & kNoStabilization) && ((af & kSlowing) || act.y > p.lowVelocityTimeMinimum)) {
         float energy = (v.x * v.x + v.y * v.y + v.z * v.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
         if (energy < p.velocityLowerLimitSquared) {
-            float boost = 1 - (float)(sqrt((double)energy) / (double)(2.f * p.velocityLowerLimit));
+            float boost = 1 - dr::SqrtQuotientAsDouble(energy, 2.f * p.velocityLowerLimit);
             const float2 r = *raw;
             // ModifyAngularDamping(boost), then ModifyLinearDamping(boost) (:1205-1221), from zero boosts
             float angularBoost = 0.f + boost * (1 - (r.y + 0.f));
@@ -321,7 +322,7 @@ __device__ __forceinline__ void PositionMath(float4& pos, float4& q, float4 v, f
     float mw = ww * q.w - x * q.x - y * q.y - z * q.z;
     q.x = q.x + mx; q.y = q.y + my; q.z = q.z + mz; q.w = q.w + mw;
     // Quaternion.Normalize (Quaternion.cs:262-269)
-    float inverse = (float)(1.0 / sqrt((double)(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w)));
+    float inverse = dr::InvSqrtAsDouble(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w);
     q.x *= inverse; q.y *= inverse; q.z *= inverse; q.w *= inverse;
     pos.x = pos.x + v.x * p.dt;
     pos.y = pos.y + v.y * p.dt;
@@ -638,7 +639,7 @@ __device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si,
             } else {
                 // Vector3.Cross(normal, Toolbox.UpVector), then Normalize
                 x1 = ny * 0.f - nz * 1.f; y1 = nz * 0.f - nx * 0.f; z1 = nx * 1.f - ny * 0.f;
-                float inv = (float)(1.0 / sqrt((double)(x1 * x1 + y1 * y1 + z1 * z1)));
+                float inv = dr::InvSqrtAsDouble(x1 * x1 + y1 * y1 + z1 * z1);
                 l11 = x1 * inv; l12 = y1 * inv; l13 = z1 * inv;
             }
         }

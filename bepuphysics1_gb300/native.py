@@ -123,6 +123,7 @@ _F = ctypes.c_float
 
 # name: (restype, argtypes)
 GPU_EXPORTS = {
+    "bepugpu_probe_double_rounding": (_I, [_P, _I, _P, _P, _U, _P, _P]),
     "bepugpu_abi_version": (_I, []),
     "bepugpu_record_size": (_U, [_I]),
     "bepugpu_default_settings": (None, [_P]),

@@ -400,6 +400,18 @@ bepugpu_status bepugpu_check_finite(bepugpu_context* ctx, int32_t scene, int32_t
  * context stays usable.  No reference counterpart. */
 bepugpu_status bepugpu_probe_bounded_wait(bepugpu_context* ctx, uint32_t spin_limit);
 
+/* Self-test of the device's float results of the reference's double-precision
+ * expressions, which the step computes in double-float FP32 arithmetic and
+ * falls back to FP64 only where that cannot decide the rounding:
+ * kind 0 (float)(1 / Math.Sqrt(a)) (Vector3.Normalize, Vector3.cs:575-581;
+ * Quaternion.Normalize), kind 1 (float)(Math.Sqrt(a) / b) (the stabilization
+ * boost, EntityBase.cs:931), kind 2 (float)Math.Pow(a, b) (the damping
+ * factors, EntityBase.cs:943,952).  `out` receives n results; `fast` (optional)
+ * how many the FP32 path decided.  Allocates device memory for the call.  No
+ * reference counterpart. */
+bepugpu_status bepugpu_probe_double_rounding(bepugpu_context* ctx, int32_t kind, const float* a, const float* b,
+                                             uint32_t n, float* out, uint32_t* fast);
+
 /* Writes whole body records: the fields as last uploaded, with position,
  * orientation and velocities as they are now (one copy of the scene's device
  * copy of the records). */
