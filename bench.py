@@ -10,15 +10,19 @@ One step = ContactRefresher -> ForceUpdater -> Solver (prestep, warm start,
               each graph launch), inputs resident in HBM, L2 flushed between
               steps by writing a 512 MiB buffer (the step's working set is
               below L2 size).
-  e2e         the same metric through the C ABI with host records: every step
-              sends the bodies' state and the manifolds from pinned host memory
-              (bepugpu_update_bodies / bepugpu_update_manifolds, checked on the
-              device), steps, and downloads whole body and manifold records;
-              host wall clock.
-  roofline    the solve kernel (k_solve): algorithmic bytes of the executed
-              manifold visits (76 d + 136 + 48 c per visit, counted by a census
-              before every sweep) / solve-phase device time from events captured
-              in the step graph; peak = measured HBM copy bandwidth.
+  e2e         the same metric through the C ABI with host buffers
+              (bepugpu_step_state): every step sends every body's state from
+              pinned host memory, steps, and brings back every body's state and
+              every manifold's contact ids and impulses; host wall clock.  The
+              whole-record path (bepugpu_step_host) and the separate calls are
+              reported beside it.
+  roofline    the dominant kernel: k_groups when island groups run the step
+              (algorithmic bytes of the units one launch processes: executed
+              solve visits counted by a census, warm start, prestep, bodies),
+              else k_solve (76 d + 136 + 48 c per executed manifold visit);
+              divided by the kernel's device time from events captured in the
+              step graph; peak = measured HBM copy bandwidth.  `sweep` adds
+              the colour-sweep path's k_solve on the same pile, groups off.
   cpu_baseline the oracle port of Solver.UpdateMultithreaded (per-body spin
               locks, chunked parallel loop) on all host cores, on a bounded
               sample of steps of the same pile.
@@ -73,6 +77,7 @@ def parse_args():
     ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--no-collide", action="store_true", help="skip the narrow-phase section")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the colour-sweep path section")
     ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
@@ -204,6 +209,77 @@ def cpu_baseline(bodies, manifolds, contact_iters_per_step, seconds, threads):
             "kind": "port", "steps": steps,
             "sample": f"{steps} full steps of the 65,536-box pile after 1 warm-up step "
                       f"(oracle port of Solver.UpdateMultithreaded, {threads} threads, {dt:.1f} s)"}
+
+
+def timed_steps(space, steps, flush, flags):
+    """Device ms of `steps` steps (events in the step graph) and of their
+    solve phase, with L2 flushed before each."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    step_ms, solve_ms = [], []
+    for _ in range(steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        space.step(DT, flags)
+        step_ms.append(space.last_step_ms())
+        solve_ms.append(float(space.last_step_phase_ms()[3]))
+    torch.cuda.synchronize()
+    return step_ms, solve_ms
+
+
+def solve_roofline(prof, solve_ms, peak, peak_kind):
+    """k_solve: the executed manifold visits' algorithmic bytes (census) over
+    the solve phase's device time, one launch per colour sweep."""
+    bytes_per_step = float(prof["solve_algorithmic_bytes"])
+    launches = int(prof["solve_launches"])
+    mean_s = statistics.mean(solve_ms) / 1000.0
+    achieved = bytes_per_step / mean_s / 1e9 if mean_s > 0 else 0.0
+    return {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": bytes_per_step / max(launches, 1),
+            "algorithmic": "76 d + 136 + 48 c per executed manifold visit",
+            "launch_ms_avg": 1000.0 * mean_s / max(launches, 1), "solve_launches_per_step": launches,
+            "solve_ms_per_step": 1000.0 * mean_s,
+            "manifold_visits_per_step": float(prof["solve_manifold_visits"])}
+
+
+def sweep_section(args, ctx, local, pg, peak, peak_kind):
+    """The colour-sweep path (one launch per colour, one thread per manifold):
+    the 65,536-box pile with island groups off, and the pile packed as config
+    1 packs its 1,000 boxes (unit boxes at 1.05 m, +-0.05 m jitter) scaled to
+    64 x 16 x 64, whose touching columns make one island too large for a
+    group, so the default policy sweeps it."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import GpuSpace, profile_step
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    out = {}
+    cases = [("pile_64k_groups_off", scenes.pile_64k, (0, 1024, 4096, 64, 0)),
+             ("pile_64k_packed", lambda: scenes.make_pile(nx=64, ny=16, nz=64, spacing=1.05, size_min=1.0,
+                                                         size_max=1.0, jitter=0.05, friction_min=0.6,
+                                                         friction_max=0.6, seed=11), None)]
+    for name, make, policy in cases:
+        bodies, manifolds, _ = make()
+        space = GpuSpace(ctx, bodies, manifolds, group_policy=policy) if policy else GpuSpace(ctx, bodies, manifolds)
+        for _ in range(max(args.warmup, 3)):
+            space.step(DT, N.STEP_ALL)
+        ctx.synchronize()
+        live_m, _ = space.download_constraints()
+        cips = int(live_m["contact_count"].sum()) * int(ctx.settings["iteration_limit"])
+        if pg:
+            pg.barrier()
+        step_ms, solve_ms = timed_steps(space, args.steps, flush, N.STEP_ALL)
+        prof = profile_step(space, DT, N.STEP_ALL)
+        ms = statistics.mean(step_ms)
+        out[name] = {"value": cips / (ms / 1000.0), "unit": "contact-iters/s", "ms_per_step": ms,
+                     "bodies": int(len(bodies)), "manifolds": int(len(manifolds)),
+                     "contacts": int(live_m["contact_count"].sum()), "colours": int(space.colouring()[2]),
+                     "group_ctas": int(prof["groups"]), "gpu_launches_per_step": int(space.last_step_launches()),
+                     "roofline": solve_roofline(prof, solve_ms, peak, peak_kind)}
+        space.close()
+    out["l2"] = "flushed between timed steps (512 MiB write)"
+    return out
 
 
 BATCH_WORKLOAD = "towers_4096"
@@ -883,6 +959,22 @@ def main():
         space.download_constraints(hm)
         ctx.synchronize()
         k = max(3, min(args.steps, 10))
+        # state records: the bodies' state up, one step, the bodies' state and
+        # the manifolds' impulses down (bepugpu_step_state)
+        sb = torch.empty(len(bodies) * N.BODY_STATE_DTYPE.itemsize, dtype=torch.uint8,
+                         pin_memory=True).numpy().view(N.BODY_STATE_DTYPE)
+        sm = torch.empty(len(manifolds) * N.MANIFOLD_STATE_DTYPE.itemsize, dtype=torch.uint8,
+                         pin_memory=True).numpy().view(N.MANIFOLD_STATE_DTYPE)
+        space.download_state(sb, sm)
+        space.step_state(sb, sm, DT, N.STEP_ALL)  # untimed: first call of the path
+        if pg:
+            pg.barrier()
+        t2 = time.perf_counter()
+        for _ in range(k):
+            space.step_state(sb, sm, DT, N.STEP_ALL)
+        el_state = time.perf_counter() - t2
+        space.download_bodies(hb)
+        space.download_constraints(hm)
         if pg:
             pg.barrier()
         t0 = time.perf_counter()
@@ -900,9 +992,15 @@ def main():
         el_calls = time.perf_counter() - t1
         h2d = hb.nbytes + hm.nbytes
         d2h = hb.nbytes + hm.nbytes  # whole body and manifold records come back
-        e2e = {"value": world * cips * k / el, "unit": "contact-iters/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "steps": k, "ms_per_step": 1000 * el / k,
-               "path": "bepugpu_step_host (records up, checked, one step, whole records down; host wall clock)",
+        e2e = {"value": world * cips * k / el_state, "unit": "contact-iters/s",
+               "h2d_bytes_per_step": int(sb.nbytes), "d2h_bytes_per_step": int(sb.nbytes + sm.nbytes),
+               "steps": k, "ms_per_step": 1000 * el_state / k,
+               "path": "bepugpu_step_state (every body's state up from pinned host memory, one step, every "
+                       "body's state and every manifold's contact ids and impulses down; host wall clock)",
+               "whole_records": {"value": world * cips * k / el, "ms_per_step": 1000 * el / k,
+                                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                                 "path": "bepugpu_step_host (body and manifold records up, checked, one step, "
+                                         "whole records down)"},
                "separate_calls": {"value": world * cips * k / el_calls, "ms_per_step": 1000 * el_calls / k,
                                   "path": "update_bodies, update_manifolds, step, download_bodies, "
                                           "download_constraints"}}
@@ -913,6 +1011,17 @@ def main():
         cpu = cpu_baseline(bodies, manifolds, cips, args.cpu_sample_seconds, os.cpu_count() or 1)
     t_sec = mark("cpu_baseline", t_sec)
 
+    sweep = None
+    if not args.no_sweep:
+        space.close()
+        sweep = sweep_section(args, ctx, local, pg, peak, peak_kind)
+        off = sweep["pile_64k_groups_off"]
+        roofline["sweep"] = {"kernel": "k_solve", "workload": "pile_64k, island groups off",
+                             "frac": off["roofline"]["frac"], "achieved": off["roofline"]["achieved"],
+                             "ms_per_step": off["ms_per_step"],
+                             "solve_ms_per_step": off["roofline"]["solve_ms_per_step"],
+                             "packed_pile_frac": sweep["pile_64k_packed"]["roofline"]["frac"]}
+        t_sec = mark("sweep", t_sec)
     batch = None
     if not args.no_batch:
         space.close()
@@ -951,6 +1060,7 @@ def main():
                        "l2": "flushed between timed steps (512 MiB write)"},
             "gpu_launches": int(launches),
             "roofline": roofline,
+            "sweep": sweep,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

@@ -195,6 +195,57 @@ __global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, 
     }
     for (int q = 0; q < 4; q++) k.orientation[q] = r.orientation[q];
 }
+// State records into the body lanes and the kept records (bepugpu_step_state).
+__global__ void k_update_body_state_records(const bepugpu_body_state* __restrict__ in, int n, BodySoA b,
+                                            bepugpu_body* kept) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4* w4 = (const float4*)(in + i);  // 64-byte records: four 16-byte loads
+    const float4 r0 = w4[0], r1 = w4[1], r2 = w4[2], r3 = w4[3];
+    // r0 = p.xyz q.x, r1 = q.yzw v.x, r2 = v.yz w.xy, r3 = w.z activity previous timeBelow
+    const float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i];
+    b.pos[i] = make_float4(r0.x, r0.y, r0.z, p.w);
+    b.quat[i] = make_float4(r0.w, r1.x, r1.y, r1.z);
+    b.vlin[i] = make_float4(r1.w, r2.x, r2.y, v.w);
+    b.vang[i] = make_float4(r2.z, r2.w, r3.x, w.w);
+    b.act[i] = make_float4(r3.z, r3.w, r3.y, 0.f);
+    bepugpu_body& k = kept[i];
+    k.position[0] = r0.x; k.position[1] = r0.y; k.position[2] = r0.z;
+    k.orientation[0] = r0.w; k.orientation[1] = r1.x; k.orientation[2] = r1.y; k.orientation[3] = r1.z;
+    k.linear_velocity[0] = r1.w; k.linear_velocity[1] = r2.x; k.linear_velocity[2] = r2.y;
+    k.angular_velocity[0] = r2.z; k.angular_velocity[1] = r2.w; k.angular_velocity[2] = r3.x;
+    k.activity = __float_as_uint(r3.y);
+    k.previous_velocity = r3.z;
+    k.velocity_time_below_limit = r3.w;
+}
+// Body lanes -> state records.
+__global__ void k_pack_body_state(BodySoA b, bepugpu_body_state* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.count) return;
+    const float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i], a = b.act[i];
+    float4* o = (float4*)(out + i);
+    o[0] = make_float4(p.x, p.y, p.z, q.x);
+    o[1] = make_float4(q.y, q.z, q.w, v.x);
+    o[2] = make_float4(v.y, v.z, w.x, w.y);
+    o[3] = make_float4(w.z, a.z, a.x, a.y);
+}
+// Manifold slots -> state records, in record order.
+__global__ void k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__ slot_of, int n,
+                                      bepugpu_manifold_state* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int s = slot_of[i], cap = m.capacity;
+    const int count = m.head[s].z & 0xff;
+    const float4 pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
+    int id[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) id[k] = k < count ? __float_as_int(m.cnrm[k * cap + s].w) : 0;
+    float4* o = (float4*)(out + i);
+    o[0] = make_float4(__int_as_float(count), __int_as_float(id[0]), __int_as_float(id[1]), __int_as_float(id[2]));
+    o[1] = make_float4(__int_as_float(id[3]), count > 0 ? pa.x : 0.f, count > 1 ? pa.y : 0.f, count > 2 ? pa.z : 0.f);
+    o[2] = make_float4(count > 3 ? pa.w : 0.f, f.x, f.y, f.z);
+    o[3] = make_float4(ax.x, ax.y, ax.z, 0.f);
+}
 __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
                                          int n, ManifoldSoA m, int* check) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1174,6 +1225,8 @@ uint32_t bepugpu_record_size(int32_t kind) {
         case 2: return sizeof(bepugpu_contact);
         case 3: return sizeof(bepugpu_manifold);
         case 4: return sizeof(bepugpu_joint);
+        case 5: return sizeof(bepugpu_body_state);
+        case 6: return sizeof(bepugpu_manifold_state);
         default: return 0;
     }
 }
@@ -1334,9 +1387,11 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
     s->hostDynamic.resize(n);
     s->hostRawDamp.resize(n);
     s->kin.Clear();
+    s->hostKinematic.clear();
     for (uint32_t i = 0; i < n; i++) {
         if (!dynamicChanged && s->hostDynamic[i] != (bodies[i].is_dynamic ? 1 : 0)) dynamicChanged = true;
         if (!bodies[i].is_dynamic) {
+            s->hostKinematic.push_back((int32_t)i);
             const float* v = bodies[i].linear_velocity;
             const float* w = bodies[i].angular_velocity;
             s->kin.Add(v[0] != 0 || v[1] != 0 || v[2] != 0 || w[0] != 0 || w[1] != 0 || w[2] != 0,
@@ -1565,6 +1620,106 @@ bepugpu_status bepugpu_step_host(bepugpu_context* c, int32_t id, bepugpu_body* b
     CK(cudaStreamSynchronize(s->stream));
     s->asyncPending = false;
     return BEPUGPU_OK;
+}
+
+namespace {
+// Argument checks shared by bepugpu_step_state and bepugpu_download_state.
+bepugpu_status CheckStateArrays(Context* ctx, Scene* s, const void* bodies, uint32_t nb, bool bodiesRequired,
+                                const void* man, uint32_t nm) {
+    if ((bodiesRequired || nb) && (nb != (uint32_t)s->b.count || (nb && !bodies))) {
+        ctx->SetError("state calls take the %d bodies of the last upload", s->b.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (nm && (nm != (uint32_t)s->m.count || !man)) {
+        ctx->SetError("state calls take all %d manifolds of the last upload, or none", s->m.count);
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    return BEPUGPU_OK;
+}
+// Packs the scene's state into the staging buffer and copies it into the
+// caller's arrays (asynchronous on the scene's stream).
+bepugpu_status QueueStateDownload(Context* ctx, Scene* s, bepugpu_body_state* bodies, uint32_t nb,
+                                  bepugpu_manifold_state* man, uint32_t nm) {
+    auto* sb = (bepugpu_body_state*)s->staging;
+    auto* sm = (bepugpu_manifold_state*)((char*)s->staging + s->stagingManifoldsAt);
+    if (nb) {
+        k_pack_body_state<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, sb);
+        CK(cudaMemcpyAsync(bodies, sb, sizeof(bepugpu_body_state) * nb, cudaMemcpyDeviceToHost, s->stream));
+    }
+    if (nm) {
+        k_pack_manifold_state<<<Blocks(nm, 256), 256, 0, s->stream>>>(s->m, s->slotOf, (int)nm, sm);
+        CK(cudaMemcpyAsync(man, sm, sizeof(bepugpu_manifold_state) * nm, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaGetLastError());
+    return BEPUGPU_OK;
+}
+}  // namespace
+
+static_assert(sizeof(bepugpu_body_state) == 64 && sizeof(bepugpu_manifold_state) == 64,
+              "state records are four 16-byte words");
+
+bepugpu_status bepugpu_step_state(bepugpu_context* c, int32_t id, bepugpu_body_state* bodies, uint32_t nb,
+                                  bepugpu_manifold_state* man, uint32_t nm, float dt, uint32_t flags) {
+    NvtxRange range("bepugpu_step_state");
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    bepugpu_status st = CheckStateArrays(ctx, s, bodies, nb, true, man, nm);
+    if (st != BEPUGPU_OK) return st;
+    if (!(dt > 0) || !std::isfinite(dt)) {
+        ctx->SetError("dt must be positive and finite");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->asyncPending) {  // an earlier step may still read the staging buffer
+        CK(cudaStreamSynchronize(s->stream));
+        s->asyncPending = false;
+    }
+    // What the kinematic bodies' stages have to do, from their new state on
+    // the host (the rest of their records cannot change here).
+    s->kin.Clear();
+    for (int32_t i : s->hostKinematic) {
+        const bepugpu_body_state& r = bodies[i];
+        const float* v = r.linear_velocity;
+        const float* w = r.angular_velocity;
+        s->kin.Add(v[0] != 0 || v[1] != 0 || v[2] != 0 || w[0] != 0 || w[1] != 0 || w[2] != 0, r.activity,
+                   r.previous_velocity, r.velocity_time_below_limit);
+    }
+    auto* sb = (bepugpu_body_state*)s->staging;
+    if (nb) {
+        CK(cudaMemcpyAsync(sb, bodies, sizeof(bepugpu_body_state) * nb, cudaMemcpyHostToDevice, s->stream));
+        k_update_body_state_records<<<Blocks(nb, 256), 256, 0, s->stream>>>(sb, (int)nb, s->b, s->bodyRecords);
+        k_world_inertia<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, s->localM33);
+        CK(cudaGetLastError());
+    }
+    st = s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
+    if (st != BEPUGPU_OK) {
+        cudaStreamSynchronize(s->stream);  // the caller may reuse its arrays after an error
+        s->asyncPending = false;
+        return st;
+    }
+    st = QueueStateDownload(ctx, s, bodies, nb, man, nm);
+    CK(cudaStreamSynchronize(s->stream));
+    s->asyncPending = false;
+    return st;
+}
+
+bepugpu_status bepugpu_download_state(bepugpu_context* c, int32_t id, bepugpu_body_state* bodies, uint32_t nb,
+                                      bepugpu_manifold_state* man, uint32_t nm) {
+    NvtxRange range("bepugpu_download_state");
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    bepugpu_status st = CheckStateArrays(ctx, s, bodies, nb, false, man, nm);
+    if (st != BEPUGPU_OK) return st;
+    if (s->asyncPending) {
+        CK(cudaStreamSynchronize(s->stream));
+        s->asyncPending = false;
+    }
+    st = QueueStateDownload(ctx, s, bodies, nb, man, nm);
+    CK(cudaStreamSynchronize(s->stream));
+    return st;
 }
 
 bepugpu_status bepugpu_update_bodies(bepugpu_context* c, int32_t id, const bepugpu_body* bodies, uint32_t n) {

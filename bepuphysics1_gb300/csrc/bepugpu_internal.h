@@ -316,6 +316,7 @@ struct Scene {
     std::vector<float> hostLinDamp, hostAngDamp, hostLocalM33;
     std::vector<float2> hostRawDamp;
     std::vector<uint8_t> hostDynamic;
+    std::vector<int32_t> hostKinematic;  // indices of the bodies uploaded with is_dynamic = 0
     std::vector<float4> hostDamp;
     bool dampDirty = true;
     float dampDt = 0.f;

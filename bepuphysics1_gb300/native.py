@@ -42,6 +42,15 @@ MANIFOLD_DTYPE = np.dtype([
     ("sliding_impulse", "<f4", 2), ("sliding_axis", "<f4", 3), ("twist_impulse", "<f4"), ("contact_order", "<i4"),
     ("contacts", CONTACT_DTYPE, 4),
 ])
+BODY_STATE_DTYPE = np.dtype([
+    ("position", "<f4", 3), ("orientation", "<f4", 4), ("linear_velocity", "<f4", 3),
+    ("angular_velocity", "<f4", 3), ("activity", "<u4"), ("previous_velocity", "<f4"),
+    ("velocity_time_below_limit", "<f4"),
+])
+MANIFOLD_STATE_DTYPE = np.dtype([
+    ("contact_count", "<i4"), ("contact_id", "<i4", 4), ("penetration_impulse", "<f4", 4),
+    ("sliding_impulse", "<f4", 2), ("twist_impulse", "<f4"), ("sliding_axis", "<f4", 3), ("reserved", "<i4"),
+])
 SHAPE_DTYPE = np.dtype([("type", "<i4"), ("size", "<f4", 3)])
 JOINT_DTYPE = np.dtype([
     ("type", "<i4"), ("body_a", "<i4"), ("body_b", "<i4"), ("flags", "<u4"),
@@ -138,6 +147,8 @@ GPU_EXPORTS = {
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
     "bepugpu_step_host": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
+    "bepugpu_step_state": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
+    "bepugpu_download_state": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_upload_constraints": (_I, [_P, _I, _P, _U, _P, _U]),
     "bepugpu_update_manifolds": (_I, [_P, _I, _P, _U]),
     "bepugpu_update_bodies": (_I, [_P, _I, _P, _U]),
@@ -210,7 +221,8 @@ def load_gpu_library(path: str | None = None):
         raise RuntimeError(f"{p} is missing: build it with __graft_entry__.build() "
                            "(the solver has no CPU fallback)")
     lib = _bind(ctypes.CDLL(str(p)), GPU_EXPORTS)
-    sizes = {0: SETTINGS_DTYPE, 1: BODY_DTYPE, 2: CONTACT_DTYPE, 3: MANIFOLD_DTYPE, 4: JOINT_DTYPE}
+    sizes = {0: SETTINGS_DTYPE, 1: BODY_DTYPE, 2: CONTACT_DTYPE, 3: MANIFOLD_DTYPE, 4: JOINT_DTYPE,
+             5: BODY_STATE_DTYPE, 6: MANIFOLD_STATE_DTYPE}
     for kind, dt in sizes.items():
         got = lib.bepugpu_record_size(kind)
         if got != dt.itemsize:

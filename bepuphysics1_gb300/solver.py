@@ -166,6 +166,27 @@ class GpuSpace:
         self.ctx.check(self.ctx.lib.bepugpu_step_host(self.ctx.handle, self.id, N.ptr(bodies), len(bodies),
                                                       N.ptr(manifolds), len(manifolds), float(dt), flags))
 
+    def step_state(self, bodies: np.ndarray, manifolds: np.ndarray | None, dt: float, flags: int = N.STEP_ALL):
+        """bepugpu_step_state: body state up, one step, body state back into
+        `bodies` and the manifolds' impulses into `manifolds` (None: skipped)."""
+        assert bodies.dtype == N.BODY_STATE_DTYPE and bodies.flags.c_contiguous
+        nm = 0
+        if manifolds is not None:
+            assert manifolds.dtype == N.MANIFOLD_STATE_DTYPE and manifolds.flags.c_contiguous
+            nm = len(manifolds)
+        self.ctx.check(self.ctx.lib.bepugpu_step_state(self.ctx.handle, self.id, N.ptr(bodies), len(bodies),
+                                                       N.ptr(manifolds), nm, float(dt), flags))
+
+    def download_state(self, bodies: np.ndarray | None = None, manifolds: np.ndarray | None = None):
+        """bepugpu_download_state into the given state arrays (either may be None)."""
+        nb = 0 if bodies is None else len(bodies)
+        nm = 0 if manifolds is None else len(manifolds)
+        assert bodies is None or bodies.dtype == N.BODY_STATE_DTYPE
+        assert manifolds is None or manifolds.dtype == N.MANIFOLD_STATE_DTYPE
+        self.ctx.check(self.ctx.lib.bepugpu_download_state(self.ctx.handle, self.id, N.ptr(bodies), nb,
+                                                           N.ptr(manifolds), nm))
+        return bodies, manifolds
+
     def set_mode(self, mode: int):
         self.ctx.check(self.ctx.lib.bepugpu_set_solve_mode(self.ctx.handle, self.id, mode))
 
@@ -235,6 +256,15 @@ class GpuSpace:
         if getattr(self, "id", None) is not None and self.ctx.handle:
             self.ctx.lib.bepugpu_scene_destroy(self.ctx.handle, self.id)
             self.id = None
+
+
+def body_states(bodies: np.ndarray, out: np.ndarray | None = None) -> np.ndarray:
+    """The state fields of body records as bepugpu_body_state records."""
+    if out is None:
+        out = np.zeros(len(bodies), N.BODY_STATE_DTYPE)
+    for f in N.BODY_STATE_DTYPE.names:
+        out[f] = bodies[f]
+    return out
 
 
 def colour_list(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | None = None):

@@ -326,7 +326,8 @@ typedef struct bepugpu_shape {
 
 int32_t bepugpu_abi_version(void);
 /* sizeof of the record types, so a binding can check its marshalling:
- * kind 0 settings, 1 body, 2 contact, 3 manifold, 4 joint. */
+ * kind 0 settings, 1 body, 2 contact, 3 manifold, 4 joint, 5 body state,
+ * 6 manifold state. */
 uint32_t bepugpu_record_size(int32_t kind);
 void bepugpu_default_settings(bepugpu_settings* out);
 
@@ -386,6 +387,56 @@ bepugpu_status bepugpu_update_bodies(bepugpu_context* ctx, int32_t scene, const 
  * them.  Two host synchronisations per call instead of one per stage. */
 bepugpu_status bepugpu_step_host(bepugpu_context* ctx, int32_t scene, bepugpu_body* bodies, uint32_t body_count,
                                  bepugpu_manifold* manifolds, uint32_t manifold_count, float dt, uint32_t flags);
+
+/* The per-step state of a body: the fields a step reads and writes
+ * (Entity position, orientation, linear and angular velocity,
+ * EntityBase.cs:35-43, and the SimulationIslandMember activity fields). */
+typedef struct bepugpu_body_state {
+    float position[3];
+    float orientation[4];
+    float linear_velocity[3];
+    float angular_velocity[3];
+    uint32_t activity;
+    float previous_velocity;
+    float velocity_time_below_limit;
+} bepugpu_body_state;
+
+/* The per-step result of a manifold: its contacts' ids and warm-start
+ * impulses in the solver's contact order (the penetration constraints'
+ * accumulatedImpulse, ContactPenetrationConstraint.cs:21), the sliding and
+ * twist friction impulses and the sliding axis (SlidingFrictionTwoAxis.cs,
+ * TwistFrictionConstraint.cs).  Contact slots at and above contact_count are
+ * zero. */
+typedef struct bepugpu_manifold_state {
+    int32_t contact_count;
+    int32_t contact_id[4];
+    float penetration_impulse[4];
+    float sliding_impulse[2];
+    float twist_impulse;
+    float sliding_axis[3];
+    int32_t reserved;
+} bepugpu_manifold_state;
+
+/* One step on state records, for a C# host that keeps its records on the
+ * host and steps every frame: `bodies` (all of the scene's bodies, in upload
+ * order) goes up as the new position, orientation, velocities and activity,
+ * the scene steps with `flags`, and the stepped state comes back into the same
+ * array.  `manifolds` receives each manifold's state in upload order
+ * (manifold_count = the scene's count), or nothing (manifold_count = 0).
+ * Everything else -- masses, inertia, damping, the manifold set and its
+ * contacts, joints -- stays as the last uploads and the device's own steps
+ * left it, so a step moves 64 bytes a body each way and 64 bytes a manifold
+ * down, against whole records in bepugpu_step_host.  One host
+ * synchronisation.  No reference counterpart: the reference's stages share
+ * the entities' memory. */
+bepugpu_status bepugpu_step_state(bepugpu_context* ctx, int32_t scene, bepugpu_body_state* bodies,
+                                  uint32_t body_count, bepugpu_manifold_state* manifolds, uint32_t manifold_count,
+                                  float dt, uint32_t flags);
+/* The scene's current body and manifold state without stepping (either
+ * count may be 0 to skip that part; otherwise it must be the scene's). */
+bepugpu_status bepugpu_download_state(bepugpu_context* ctx, int32_t scene, bepugpu_body_state* bodies,
+                                      uint32_t body_count, bepugpu_manifold_state* manifolds,
+                                      uint32_t manifold_count);
 
 /* Checks every body's position, orientation and velocities for NaN or
  * infinity (the reference's CHECKMATH validation, Toolbox.Validate, off there

@@ -2,10 +2,10 @@
 PermutationMapper (BEPUutilities/PermutationMapper.cs:49-104).
 
 The table is data the reference-order mode must reproduce exactly, so it is
-extracted from the reference source rather than retyped.  Run in a checkout
-that has the reference mounted:
+extracted from the reference source rather than retyped.  Give it the root
+of a bepuphysics1 checkout:
 
-    python oracle/extract_primes.py /root/reference
+    python oracle/extract_primes.py <path to the bepuphysics1 checkout>
 """
 import re
 import sys
@@ -13,7 +13,9 @@ from pathlib import Path
 
 
 def main() -> None:
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python oracle/extract_primes.py <path to the bepuphysics1 checkout>")
+    ref = Path(sys.argv[1])
     src = (ref / "BEPUutilities" / "PermutationMapper.cs").read_text(encoding="utf-8-sig")
     body = src[src.index("static long[] primes"):]
     body = body[body.index("{") + 1: body.index("};")]

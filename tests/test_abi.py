@@ -43,6 +43,8 @@ def test_record_sizes():
     assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 64
     assert lib.bepugpu_record_size(3) == N.MANIFOLD_DTYPE.itemsize
     assert lib.bepugpu_record_size(4) == N.JOINT_DTYPE.itemsize
+    assert lib.bepugpu_record_size(5) == N.BODY_STATE_DTYPE.itemsize == 64
+    assert lib.bepugpu_record_size(6) == N.MANIFOLD_STATE_DTYPE.itemsize == 64
     assert lib.bepugpu_record_size(99) == 0
 
 

@@ -92,6 +92,36 @@ def test_pile_64k_full_size(gpu_context):
     p.close()
 
 
+def test_pile_64k_full_size_colour_sweeps(gpu_context):
+    """The colour-sweep path (k_prestep / k_warm / k_solve, one launch per
+    colour) on the whole 65,536-box pile, island groups off."""
+    b, m, _ = scenes.pile_64k()
+    p = Pair(gpu_context, b, m, group_policy=(0, 1024, 4096, 64, 0))
+    for _ in range(2):
+        p.step()
+        errs, exact = p.compare()
+        assert exact, errs
+    assert p.gpu.last_step_launches() > 2 * p.colours  # swept, not grouped
+    p.close()
+
+
+def test_packed_pile_64k_one_island(gpu_context):
+    """The 1.05 m packing of the 1,000-box pile scaled to 64 x 16 x 64: its
+    columns touch, so the pile is one island too large for a group and the
+    default policy runs it as colour sweeps."""
+    b, m, _ = scenes.make_pile(nx=64, ny=16, nz=64, spacing=1.05, size_min=1.0, size_max=1.0, jitter=0.05,
+                               friction_min=0.6, friction_max=0.6, seed=11)
+    assert len(m) > 150000
+    p = Pair(gpu_context, b, m)
+    assert p.colours >= 8
+    p.step()
+    errs, exact = p.compare()
+    assert exact, errs
+    prof = p.gpu.last_step_launches()
+    assert prof > p.colours
+    p.close()
+
+
 def test_towers(gpu_context):
     b, m, _ = scenes.make_tower(900, seed=11)
     p = Pair(gpu_context, b, m)
