@@ -78,6 +78,8 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving section")
     ap.add_argument("--no-collide", action="store_true", help="skip the narrow-phase section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the colour-sweep path section")
+    ap.add_argument("--no-pile1k", action="store_true", help="skip the 1,000-box pile section")
+    ap.add_argument("--pile1k-cpu-seconds", type=float, default=2.0)
     ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
@@ -282,6 +284,61 @@ def sweep_section(args, ctx, local, pg, peak, peak_kind):
     return out
 
 
+def pile1k_section(args, ctx, local, pg):
+    """The 1,000-box pile (unit boxes at 1.05 m, +-0.05 m jitter, I = 10): the
+    one-scene GPU step beside the oracle port's single-threaded
+    (Solver.UpdateSingleThreaded, PermutationMapper order) and multithreaded
+    (Solver.UpdateMultithreaded, all host cores) steps, each CPU leg a bounded
+    sample of whole steps."""
+    import torch
+    import oracle
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import GpuSpace, default_settings
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    bodies, manifolds, _ = scenes.pile_1k()
+    space = GpuSpace(ctx, bodies, manifolds)
+    for _ in range(max(args.warmup, 3)):
+        space.step(DT, N.STEP_ALL)
+    ctx.synchronize()
+    live_m, _ = space.download_constraints()
+    cips = int(live_m["contact_count"].sum()) * int(ctx.settings["iteration_limit"])
+    if pg:
+        pg.barrier()
+    step_ms, _ = timed_steps(space, args.steps, flush, N.STEP_ALL)
+    ms = statistics.mean(step_ms)
+    space.close()
+    out = {"workload": "pile_1k", "bodies": int(len(bodies)), "manifolds": int(len(manifolds)),
+           "contacts": int(live_m["contact_count"].sum()),
+           "gpu": {"value": cips / (ms / 1000.0), "unit": "contact-iters/s", "ms_per_step": ms,
+                   "path": "bepugpu_step, one scene, island groups (device time, L2 flushed)"}}
+    if args.no_cpu_baseline:
+        return out
+    threads = os.cpu_count() or 1
+    for name, nthreads in (("cpu_single_thread", 1), ("cpu_multithreaded", threads)):
+        o = oracle.OracleSpace(default_settings(), bodies, manifolds)
+        o.set_order_mode(oracle.ORDER_PERMUTED, 0)
+
+        def one_step():
+            if nthreads > 1:
+                o.step_multithreaded(DT, N.STEP_ALL, 1, nthreads)
+            else:
+                o.step(DT, N.STEP_ALL, 1)
+
+        one_step()  # warm-up step (MultithreadedScalingTestDemo.cs:223)
+        steps, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < args.pile1k_cpu_seconds:
+            one_step()
+            steps += 1
+        el = time.perf_counter() - t0
+        o.close()
+        out[name] = {"value": cips * steps / el, "unit": "contact-iters/s", "cores": nthreads, "kind": "port",
+                     "ms_per_step": 1000 * el / steps,
+                     "sample": f"{steps} steps after 1 warm-up step (oracle port of Solver.Update"
+                               f"{'Multithreaded' if nthreads > 1 else 'SingleThreaded'}, {el:.1f} s)"}
+    return out
+
+
 BATCH_WORKLOAD = "towers_4096"
 BATCH_ITERATIONS = 8
 
@@ -395,6 +452,27 @@ def batch_section(args, local, rank, world, pg):
     plain_rate = whole(n * args.batch_rounds / plain_s)
     batched_rate = whole(tb.scene_steps_per_s)
     batched_1 = whole(t1.scene_steps_per_s)
+
+    # roofline of the batched launches: the step formula's algorithmic bytes of
+    # every scene (solve visits from a census of one instrumented step each)
+    # per scene-step, times the scene-steps of a call, over its device time
+    from bepuphysics1_gb300.solver import profile_step
+    step_bytes = 0.0
+    for sp, (b, _) in zip(spaces, records):
+        prof = profile_step(sp, DT, N.STEP_ALL)
+        live_m, _ = sp.download_constraints()
+        warm_b, prestep_b, body_b = step_static_bytes(b, live_m)
+        step_bytes += float(prof["solve_algorithmic_bytes"]) + float(prof["group_solve_algorithmic_bytes"]) + \
+            warm_b + prestep_b + body_b
+    peak, peak_kind = measured_hbm_peak()
+    call_bytes = step_bytes * best.steps_per_launch
+    achieved = call_bytes / (tb.device_ms_per_launch / 1000.0) / 1e9 if tb.device_ms_per_launch > 0 else 0.0
+    batch_roofline = {"bound": "hbm", "kernel": "k_batch_groups", "achieved": achieved, "peak": peak,
+                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                      "algorithmic_bytes_per_call": call_bytes, "device_ms_per_call": tb.device_ms_per_launch,
+                      "launches_per_call": tb.launches,
+                      "algorithmic": "per scene-step: 76 d + 136 + 48 c per executed solve visit (census), one "
+                                     "warm-start visit and one prestep per active manifold, 152 per dynamic body"}
     out = {
         "metric": "scene-steps/s", "workload": BATCH_WORKLOAD,
         "config": {"scenes": args.batch_scenes, "bodies": bodies, "manifolds": manifolds, "contacts": contacts,
@@ -410,6 +488,7 @@ def batch_section(args, local, rank, world, pg):
         "batched_1_step_per_launch": {"value": batched_1, "unit": "scene-steps/s",
                                       "device_ms_per_call": t1.device_ms_per_launch,
                                       "gpu_launches_per_call": t1.launches},
+        "roofline": batch_roofline,
         "speedup_vs_plain": batched_rate / plain_rate,
         "speedup_vs_plain_1_step_per_launch": batched_1 / plain_rate,
         "contact_iters_per_s_batched": contacts * BATCH_ITERATIONS * batched_rate / max(args.batch_scenes, 1),
@@ -481,6 +560,29 @@ def chain_section(args, local, rank, world, pg):
                    "l2": "flushed between timed steps (512 MiB write)"},
         "parity": "bit-exact vs the colour-ordered oracle (tests/test_gpu_joints.py)",
     }
+    # roofline of the step (its launches are the joint-island group kernels):
+    # manifold visits from a census, joint visits counted as joints x
+    # iterations (an upper bound: joints that early-out are counted), each
+    # 76 d + 256 bytes (its 13 solve lanes and state read, 2 impulse lanes and
+    # state written, each moving body's velocities and inertia); warm start,
+    # prestep and body terms as the step formula has them
+    from bepuphysics1_gb300.solver import profile_step
+    prof = profile_step(sp, DT, N.STEP_ALL)
+    live_m, _ = sp.download_constraints()
+    warm_b, prestep_b, body_b = step_static_bytes(bodies, live_m)
+    dyn = np.asarray(bodies["is_dynamic"]) != 0
+    ja, jb = np.asarray(joints["body_a"]), np.asarray(joints["body_b"])
+    jd = ((ja >= 0) & dyn[np.clip(ja, 0, None)]).astype(np.int64) + ((jb >= 0) & dyn[np.clip(jb, 0, None)])
+    joint_visit_bytes = float((76 * jd + 256).sum())
+    step_bytes = float(prof["solve_algorithmic_bytes"]) + float(prof["group_solve_algorithmic_bytes"]) + \
+        warm_b + prestep_b + body_b + joint_visit_bytes * (CHAIN_ITERATIONS + 2)  # + warm start and prestep
+    peak, peak_kind = measured_hbm_peak()
+    achieved = step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": "k_groups (joint islands)", "achieved": achieved, "peak": peak,
+                       "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                       "algorithmic_bytes_per_step": step_bytes,
+                       "algorithmic": "manifolds: the step formula with a census of solve visits; joints: "
+                                      "76 d + 256 per visit, joints x (iterations + 2) visits (upper bound)"}
     sp.close()
 
     # the same scene with its joints re-typed as ten of the added joint, limit and motor types
@@ -1022,6 +1124,11 @@ def main():
                              "solve_ms_per_step": off["roofline"]["solve_ms_per_step"],
                              "packed_pile_frac": sweep["pile_64k_packed"]["roofline"]["frac"]}
         t_sec = mark("sweep", t_sec)
+    pile1k = None
+    if not args.no_pile1k:
+        space.close()
+        pile1k = pile1k_section(args, ctx, local, pg)
+        t_sec = mark("pile1k", t_sec)
     batch = None
     if not args.no_batch:
         space.close()
@@ -1061,6 +1168,7 @@ def main():
             "gpu_launches": int(launches),
             "roofline": roofline,
             "sweep": sweep,
+            "pile_1k": pile1k,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

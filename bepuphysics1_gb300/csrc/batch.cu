@@ -36,7 +36,7 @@ namespace bepugpu {
 // iterations and pushes the kernel past the register file into spills.
 template <bool kShared>
 __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
-                               uint32_t flags, int Bc, int Lc, int pass) {
+                               uint32_t flags, int Bc, int Lc, int pass, bool nonConvex) {
     extern __shared__ float4 smem[];
     __shared__ SceneView sv;
     const int4 w = work[blockIdx.x];  // scene view, group, steps
@@ -48,7 +48,7 @@ __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* 
     }
     __syncthreads();
     const GroupDesc g = sv.t.groups[w.y];
-    GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr);
+    GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr, nonConvex);
 }
 
 namespace {
@@ -56,6 +56,7 @@ namespace {
 struct ClassLaunch {
     std::vector<int4> work;
     int Bc = 1, Lc = 1, members = 0;
+    bool nonConvex = false;  // shared lanes with room for NONCONVEX manifolds' contact friction
     int4* dev = nullptr;
     size_t cap = 0;
 };
@@ -112,23 +113,24 @@ cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uin
     if (c.work.empty()) return cudaSuccess;
     bt.launches += passes;
     return LaunchBatchedGroups(kShared, bt.viewsDev, c.dev, (int)c.work.size(), p, flags, c.Bc, c.Lc, c.members,
-                               threads, passes, bt.stream);
+                               threads, passes, bt.stream, c.nonConvex);
 }
 
 }  // namespace
 
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
                                 uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, bool nonConvex) {
     if (n <= 0) return cudaSuccess;
-    size_t smemBytes = GroupSmemBytes(shared, Bc, Lc);
+    size_t smemBytes = GroupSmemBytes(shared, Bc, Lc, 0, nonConvex);
     auto kernel = shared ? k_batch_groups<true> : k_batch_groups<false>;
     if (smemBytes > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
         if (e != cudaSuccess) return e;
     }
     for (int pass = 0; pass < passes; pass++) {
-        kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass);
+        kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass,
+                                                                                  nonConvex);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
@@ -241,8 +243,8 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         }
         std::vector<SceneView> views;
         int passes = 0;  // launches per class: the most steps any batched scene asked for
-        bt.shared = ClassLaunch{{}, 1, 1, 0, bt.shared.dev, bt.shared.cap};
-        bt.global = ClassLaunch{{}, 1, 1, 0, bt.global.dev, bt.global.cap};
+        bt.shared = ClassLaunch{{}, 1, 1, 0, false, bt.shared.dev, bt.shared.cap};
+        bt.global = ClassLaunch{{}, 1, 1, 0, false, bt.global.dev, bt.global.cap};
         for (uint32_t i = 0; i < count; i++) {
             Scene* s = list[i];
             if (!ready[i] || stepCount[i] == 0) continue;
@@ -258,6 +260,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
                 bt.shared.Bc = std::max(bt.shared.Bc, g.shared.maxLocal);
                 bt.shared.Lc = std::max(bt.shared.Lc, g.shared.maxManifolds);
                 bt.shared.members = std::max(bt.shared.members, g.shared.maxColourMembers);
+                bt.shared.nonConvex = bt.shared.nonConvex || g.nonConvexLanes;
             }
             if (g.global.end > g.global.begin) {
                 bt.global.Bc = std::max(bt.global.Bc, g.global.maxLocal);
@@ -265,9 +268,9 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             }
         }
         // the shared-lane groups of different scenes must fit one launch's budget together
-        if (GroupSmemBytes(true, bt.shared.Bc, bt.shared.Lc) > kGroupSmemBudget + 16 * 1024) {
-            ctx->SetError("batch: shared-lane groups need %zu bytes of shared memory",
-                          GroupSmemBytes(true, bt.shared.Bc, bt.shared.Lc));
+        const size_t sharedBytes = GroupSmemBytes(true, bt.shared.Bc, bt.shared.Lc, 0, bt.shared.nonConvex);
+        if (sharedBytes > kGroupSmemBudget + 16 * 1024) {
+            ctx->SetError("batch: shared-lane groups need %zu bytes of shared memory", sharedBytes);
             return BEPUGPU_INVALID_OPERATION;
         }
         if ((e = Ensure(bt.viewsDev, bt.viewsCap, std::max<size_t>(views.size(), 1))) ||

@@ -238,13 +238,18 @@ __global__ void k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__
     const int count = m.head[s].z & 0xff;
     const float4 pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
     int id[4];
+    float fi[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) id[k] = k < count ? __float_as_int(m.cnrm[k * cap + s].w) : 0;
+    for (int k = 0; k < 4; k++) {
+        id[k] = k < count ? __float_as_int(m.cnrm[k * cap + s].w) : 0;
+        fi[k] = k < count ? m.cfr[k * cap + s].w : 0.f;
+    }
     float4* o = (float4*)(out + i);
     o[0] = make_float4(__int_as_float(count), __int_as_float(id[0]), __int_as_float(id[1]), __int_as_float(id[2]));
     o[1] = make_float4(__int_as_float(id[3]), count > 0 ? pa.x : 0.f, count > 1 ? pa.y : 0.f, count > 2 ? pa.z : 0.f);
     o[2] = make_float4(count > 3 ? pa.w : 0.f, f.x, f.y, f.z);
-    o[3] = make_float4(ax.x, ax.y, ax.z, 0.f);
+    o[3] = make_float4(ax.x, ax.y, ax.z, fi[0]);
+    o[4] = make_float4(fi[1], fi[2], fi[3], 0.f);
 }
 __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
                                          int n, ManifoldSoA m, int* check) {
@@ -254,7 +259,7 @@ __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ re
     int4 h = m.head[slot_of[i]];
     const uint32_t was = (uint32_t)h.z >> 8;
     bool bad = r.body_a != h.x || r.body_b != h.y || r.contact_count < 0 || r.contact_count > 4 ||
-               ((r.flags ^ was) & BEPUGPU_MANIFOLD_GENERATED);
+               ((r.flags ^ was) & (BEPUGPU_MANIFOLD_GENERATED | BEPUGPU_MANIFOLD_NONCONVEX));
     if (!bad && (r.flags & BEPUGPU_MANIFOLD_GENERATED)) {  // contact_order: a permutation of the contacts
         const uint32_t code = (uint32_t)r.contact_order ^ 0xE4u;
         uint32_t seen = 0;
@@ -281,6 +286,11 @@ __global__ void k_unpack_manifolds(const bepugpu_manifold* __restrict__ rec, con
         m.offA[k * cap + s] = make_float4(c.local_offset_a[0], c.local_offset_a[1], c.local_offset_a[2],
                                           c.base_penetration_depth);
         m.offB[k * cap + s] = make_float4(c.local_offset_b[0], c.local_offset_b[1], c.local_offset_b[2], 0.f);
+        // contact friction state: NONCONVEX manifolds only (zero in a convex one's records)
+        m.cfr[k * cap + s] = k < count && (r.flags & BEPUGPU_MANIFOLD_NONCONVEX)
+                                 ? make_float4(c.friction_direction[0], c.friction_direction[1],
+                                               c.friction_direction[2], c.friction_impulse)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     float pa[4];
     for (int k = 0; k < 4; k++) pa[k] = k < count ? r.contacts[k].penetration_impulse : 0.f;
@@ -331,7 +341,7 @@ __global__ void __launch_bounds__(kRecordBlock) k_pack_manifold_records(Manifold
             bepugpu_contact& c = r.contacts[k];
             if (k < count) {
                 const float4 cp = m.cpos[k * cap + s], cn = m.cnrm[k * cap + s], oa = m.offA[k * cap + s],
-                             ob = m.offB[k * cap + s];
+                             ob = m.offB[k * cap + s], fr = m.cfr[k * cap + s];
                 c.position[0] = cp.x; c.position[1] = cp.y; c.position[2] = cp.z;
                 c.normal[0] = cn.x; c.normal[1] = cn.y; c.normal[2] = cn.z;
                 c.penetration_depth = cp.w;
@@ -340,6 +350,8 @@ __global__ void __launch_bounds__(kRecordBlock) k_pack_manifold_records(Manifold
                 c.local_offset_b[0] = ob.x; c.local_offset_b[1] = ob.y; c.local_offset_b[2] = ob.z;
                 c.base_penetration_depth = oa.w;
                 c.penetration_impulse = acc[k];
+                c.friction_impulse = fr.w;
+                c.friction_direction[0] = fr.x; c.friction_direction[1] = fr.y; c.friction_direction[2] = fr.z;
             } else {
                 uint32_t* w = (uint32_t*)&c;
                 for (int q = 0; q < (int)(sizeof(bepugpu_contact) / 4); q++) w[q] = 0u;
@@ -735,7 +747,8 @@ bepugpu_status Scene::Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t 
     L.offB = take(64 * M); L.mat = take(16 * M); L.pen = take(16 * M); L.fric = take(16 * M);
     L.axis = take(16 * M); L.pj0 = take(64 * M); L.pj1 = take(64 * M); L.pj2 = take(64 * M);
     L.s0 = take(16 * M); L.s1 = take(16 * M); L.s3 = take(16 * M); L.s4 = take(16 * M); L.s5 = take(16 * M);
-    L.s6 = take(16 * M); L.s7 = take(16 * M); L.lev = take(16 * M); L.state = take(8 * M);
+    L.s6 = take(16 * M); L.s7 = take(16 * M); L.lev = take(16 * M);
+    L.cfr = take(64 * M); L.cfa = take(64 * M); L.cfb = take(64 * M); L.state = take(8 * M);
     L.slot = take(4 * M); L.offs = take(4 * (M + J + 2));
     L.jhead = take(16 * J); L.jlanes = take(16 * (size_t)kJointLanes * J); L.jstate = take(8 * J);
     L.joffs = take(4 * (M + J + 2));
@@ -794,6 +807,7 @@ void Scene::Rebase() {
     m.s0 = (float4*)(base + L.s0); m.s1 = (float4*)(base + L.s1); m.s3 = (float4*)(base + L.s3);
     m.s4 = (float4*)(base + L.s4); m.s5 = (float4*)(base + L.s5); m.s6 = (float4*)(base + L.s6);
     m.s7 = (float4*)(base + L.s7); m.lever = (float4*)(base + L.lev); m.state = (uint2*)(base + L.state);
+    m.cfr = (float4*)(base + L.cfr); m.cfa = (float4*)(base + L.cfa); m.cfb = (float4*)(base + L.cfb);
     slotOf = (int32_t*)(base + L.slot);
     colourOffsetsDev = (int32_t*)(base + L.offs);
     groupDescDev = (GroupDesc*)(base + L.groups);
@@ -1456,6 +1470,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         if (jst != BEPUGPU_OK) return jst;
     }
     std::vector<int32_t> a(nm + nj), bb(nm + nj);
+    std::vector<uint8_t> nonConvex(nm);
     for (uint32_t u = 0; u < nj; u++) {
         a[u] = joints[u].body_a;
         bb[u] = joints[u].body_b;
@@ -1463,6 +1478,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     for (uint32_t i = 0; i < nm; i++) {
         a[nj + i] = man[i].body_a;
         bb[nj + i] = man[i].body_b;
+        nonConvex[i] = (man[i].flags & BEPUGPU_MANIFOLD_NONCONVEX) != 0;
         if (man[i].contact_count < 0 || man[i].contact_count > 4) {
             ctx->SetError("manifold %u has contact_count %d (0..4 allowed)", i, man[i].contact_count);
             return BEPUGPU_INVALID_ARGUMENT;
@@ -1482,7 +1498,7 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     GroupPolicy pol = s->policy;
     if (s->mode == BEPUGPU_MODE_PERSISTENT) pol.enabled = false;
     PlanGroups(pol, a.data(), bb.data(), s->colouring.colour.data(), (int32_t)nj, (int32_t)nm,
-               s->hostDynamic.data(), nb, s->colouring.colours, s->groupPlan);
+               s->hostDynamic.data(), nb, s->colouring.colours, s->groupPlan, nonConvex.data());
     const GroupPlan& plan = s->groupPlan;
     s->manifoldOffsets = plan.globalOffsets;
     s->jointOffsets = plan.jointGlobalOffsets;
@@ -1541,7 +1557,7 @@ bepugpu_status bepugpu_update_manifolds(bepugpu_context* c, int32_t id, const be
     }, bad, flag);
     if (st != BEPUGPU_OK) return st;
     if (bad >= 0) {
-        ctx->SetError("manifold %d changed its bodies or its GENERATED flag, has a contact count outside "
+        ctx->SetError("manifold %d changed its bodies or its GENERATED or NONCONVEX flag, has a contact count outside "
                       "0..4 or a contact_order that is no permutation; use bepugpu_upload_constraints", bad);
         return BEPUGPU_INVALID_ARGUMENT;
     }
@@ -1593,8 +1609,8 @@ bepugpu_status bepugpu_step_host(bepugpu_context* c, int32_t id, bepugpu_body* b
         return BEPUGPU_INVALID_ARGUMENT;
     }
     if (h[2] != 0x7f7f7f7f) {
-        ctx->SetError("manifold %d changed its bodies or its GENERATED flag, has a contact count outside 0..4 or a "
-                      "contact_order that is no permutation; use bepugpu_upload_constraints", h[2]);
+        ctx->SetError("manifold %d changed its bodies or its GENERATED or NONCONVEX flag, has a contact count "
+                      "outside 0..4 or a contact_order that is no permutation; use bepugpu_upload_constraints", h[2]);
         return BEPUGPU_INVALID_ARGUMENT;
     }
     if (nb) {
@@ -1655,8 +1671,8 @@ bepugpu_status QueueStateDownload(Context* ctx, Scene* s, bepugpu_body_state* bo
 }
 }  // namespace
 
-static_assert(sizeof(bepugpu_body_state) == 64 && sizeof(bepugpu_manifold_state) == 64,
-              "state records are four 16-byte words");
+static_assert(sizeof(bepugpu_body_state) == 64 && sizeof(bepugpu_manifold_state) == 80,
+              "state records are four and five 16-byte words");
 
 bepugpu_status bepugpu_step_state(bepugpu_context* c, int32_t id, bepugpu_body_state* bodies, uint32_t nb,
                                   bepugpu_manifold_state* man, uint32_t nm, float dt, uint32_t flags) {

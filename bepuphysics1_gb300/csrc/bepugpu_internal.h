@@ -131,12 +131,14 @@ struct GroupPlan {
     std::vector<int2> jointRefs;
     int32_t jointGlobalCount = 0;
     bool groupJoints = false;  // some group holds joints
+    bool nonConvexLanes = false;  // some group holds a NONCONVEX manifold: shared lanes have room for its friction
 };
 // Shared memory a group may use: 96 bytes per body, plus 400 per manifold when
 // its solve lanes live there.
 constexpr size_t kGroupSmemBudget = 200 * 1024;
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
-                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan);
+                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan,
+                const uint8_t* nonConvex = nullptr);
 bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
 // Joints (joints.cu): record checks, upload into the scene's joint slots, and
 // the accumulated impulses back into records.
@@ -198,7 +200,7 @@ constexpr size_t kBarrierCounterAt = 0, kBarrierGenerationAt = 128, kErrorAt = 2
 struct ArenaLayout {
     size_t pos, quat, vlin, vang, inv0, inv1, loc0, loc1, damp, m33, act, rawDamp;
     size_t head, cpos, cnrm, offA, offB, mat, pen, fric, axis, pj0, pj1, pj2, s0, s1, s3, s4, s5, s6, s7, lev,
-        state, slot, offs;
+        cfr, cfa, cfb, state, slot, offs;
     size_t jhead, jlanes, jstate, joffs;
     size_t groups, groupBodies, groupRefs, groupOffsets, sweepBodies;
     size_t groupJointRefs, groupJointOffsets;
@@ -356,7 +358,7 @@ struct SceneView {
 SceneView MakeView(const Scene& s);
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
                                 uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
-                                cudaStream_t stream);
+                                cudaStream_t stream, bool nonConvex = false);
 
 struct Context {
     int device = 0;

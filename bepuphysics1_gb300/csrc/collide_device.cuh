@@ -514,6 +514,7 @@ __device__ __forceinline__ bool BoxSphere(V3 h, float r, V3 pa, float4 qa, V3 pb
 // list) plus the manifold's own list order.
 struct Kept {
     float4 cp[4], cn[4], oa[4], ob[4];
+    float4 cf[4];  // NONCONVEX: each contact's friction direction and impulse
     float acc[4];
     int n;
     int list[4];  // list position -> solver index
@@ -521,12 +522,13 @@ struct Kept {
 
 // ContactManifold.Remove of list entry i: the list moves its last entry into
 // the gap (RawList.FastRemoveAt); the constraint removes its penetration child
-// keeping order (RawList.RemoveAt).
+// (and, NONCONVEX, the contact's friction child) keeping order (RawList.RemoveAt).
 __device__ __forceinline__ void RemoveListAt(Kept& k, int i) {
     const int p = k.list[i];
     k.list[i] = k.list[k.n - 1];
     for (int q = p; q + 1 < k.n; q++) {
         k.cp[q] = k.cp[q + 1]; k.cn[q] = k.cn[q + 1]; k.oa[q] = k.oa[q + 1]; k.ob[q] = k.ob[q + 1];
+        k.cf[q] = k.cf[q + 1];
         k.acc[q] = k.acc[q + 1];
     }
     k.n--;
@@ -541,6 +543,7 @@ __device__ __forceinline__ void AddContact(Kept& k, V3 p, V3 n, float depth, int
     k.cn[s] = make_float4(n.x, n.y, n.z, __int_as_float(id));
     k.oa[s] = make_float4(0, 0, 0, 0);
     k.ob[s] = make_float4(0, 0, 0, 0);
+    k.cf[s] = make_float4(0, 0, 0, 0);  // ContactFrictionConstraint.Setup: linearA = 0, impulse 0
     k.acc[s] = 0.f;
     k.list[s] = s;
     k.n++;
@@ -562,12 +565,14 @@ __device__ __forceinline__ void CollideManifold(const ManifoldSoA& m, const Body
     const uint32_t code = (uint32_t)__float_as_int(fr.w) ^ 0xE4u;
     const float4 pen = m.penacc[s];
     const float accs[4] = {pen.x, pen.y, pen.z, pen.w};
+    const bool nonConvex = ((uint32_t)h.z >> 8) & kManifoldNonConvex;
     for (int q = 0; q < 4; q++) {
         if (q < k.n) {
             k.cp[q] = m.cpos[q * cap + s];
             k.cn[q] = m.cnrm[q * cap + s];
             k.oa[q] = m.offA[q * cap + s];
             k.ob[q] = m.offB[q * cap + s];
+            k.cf[q] = nonConvex ? m.cfr[q * cap + s] : make_float4(0, 0, 0, 0);
             k.acc[q] = accs[q];
             k.list[q] = (int)((code >> (2 * q)) & 3u);
         }
@@ -637,6 +642,8 @@ __device__ __forceinline__ void CollideManifold(const ManifoldSoA& m, const Body
             m.offA[q * cap + s] = k.oa[q];
             m.offB[q * cap + s] = k.ob[q];
         }
+        if (nonConvex && q < (k.n > before ? k.n : before))
+            m.cfr[q * cap + s] = q < k.n ? k.cf[q] : make_float4(0, 0, 0, 0);
     }
     m.penacc[s] = make_float4(k.n > 0 ? k.acc[0] : 0.f, k.n > 1 ? k.acc[1] : 0.f, k.n > 2 ? k.acc[2] : 0.f,
                               k.n > 3 ? k.acc[3] : 0.f);

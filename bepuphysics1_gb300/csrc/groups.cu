@@ -28,10 +28,10 @@ namespace bepugpu {
 
 template <bool kCensus, bool kShared, int kJoints>
 __global__ void k_groups(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, uint32_t flags, GroupTables t,
-                         int groupBase, int Bc, int Lc, int Jc, unsigned long long* census) {
+                         int groupBase, int Bc, int Lc, int Jc, unsigned long long* census, bool nonConvex) {
     extern __shared__ float4 smem[];
     const GroupDesc g = t.groups[groupBase + blockIdx.x];
-    GroupStep<kCensus, kShared, kJoints>(m, b, j, p, flags, t, g, Bc, Lc, Jc, smem, census);
+    GroupStep<kCensus, kShared, kJoints>(m, b, j, p, flags, t, g, Bc, Lc, Jc, smem, census, nonConvex);
 }
 
 // ------------------------------------------------------------------ host side --
@@ -59,9 +59,12 @@ struct UnionFind {
 // colouring (joints first, u < nj).  The sweep part takes manifold slots
 // [0, globalCount) and joint slots [0, jointGlobalCount) in colour-major
 // order; each group takes a contiguous manifold range and a contiguous joint
-// range, each in colour-major order.
+// range, each in colour-major order.  When a group holds a NONCONVEX manifold
+// (nonConvex[i] != 0; null: none), every group's shared manifold lanes have
+// room for contact friction (plan.nonConvexLanes, GroupManifoldLanes).
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
-                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan) {
+                int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan,
+                const uint8_t* nonConvex) {
     plan = GroupPlan();
     const int32_t n = nj + nm;
     std::vector<int32_t> groupOf(n, -1);  // per updateable
@@ -135,9 +138,15 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
     std::vector<int32_t> order(G);
     std::iota(order.begin(), order.end(), 0);
     std::vector<uint8_t> fits(G), kind(G);
+    // Shared manifold lanes have room for contact friction when any group
+    // holds a NONCONVEX manifold (one layout for all of the scene's groups).
+    if (nonConvex)
+        for (int32_t gId = 0; gId < G && !plan.nonConvexLanes; gId++)
+            for (int32_t u : mMembers[gId]) plan.nonConvexLanes = plan.nonConvexLanes || nonConvex[u - nj];
     for (int32_t gId = 0; gId < G; gId++) {
         fits[gId] = GroupSmemBytes(true, (int)gBodies[gId].size(), (int)mMembers[gId].size(),
-                                   (int)jMembers[gId].size()) <= std::min<size_t>(pol.sharedLanesBudget, kGroupSmemBudget);
+                                   (int)jMembers[gId].size(), plan.nonConvexLanes) <=
+                    std::min<size_t>(pol.sharedLanesBudget, kGroupSmemBudget);
         kind[gId] = (uint8_t)((jMembers[gId].empty() ? 0 : 2) + (fits[gId] ? 0 : 1));
     }
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return kind[x] < kind[y]; });
@@ -259,7 +268,8 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
                            bool count, GroupTables t) {
     if (c.end <= c.begin) return BEPUGPU_OK;
     const int Bc = std::max(c.maxLocal, 1), Lc = std::max(c.maxManifolds, 1), Jc = std::max(c.maxJoints, 1);
-    size_t smemBytes = GroupSmemBytes(kShared, Bc, Lc, kJoints ? Jc : 0);
+    const bool nonConvex = s->groupPlan.nonConvexLanes;
+    size_t smemBytes = GroupSmemBytes(kShared, Bc, Lc, kJoints ? Jc : 0, nonConvex);
     cudaError_t e = cudaSuccess;
     if (smemBytes > 48 * 1024) {
         e = cudaFuncSetAttribute(k_groups<false, kShared, kJoints>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -278,10 +288,10 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
     const cudaError_t earlier = cudaGetLastError();
     if (count)
         k_groups<true, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
-            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census());
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census(), nonConvex);
     else
         k_groups<false, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
-            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr);
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr, nonConvex);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         ctx->SetError("group kernel launch (%u CTAs of %d threads, %zu bytes of shared memory): %s%s%s", blocks,

@@ -33,10 +33,14 @@ struct GroupBodies {
 };
 
 // Shared memory of one CTA: 6 body lanes per body; with kShared also 24 float4
-// lanes, a state word and a ref pair per manifold (400 bytes); with joints the
-// joints' solve lanes, state and refs (kJointSmemBytes each).
-__host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int manifolds, int joints = 0) {
-    return 96 * (size_t)bodies + (shared ? 400 * (size_t)manifolds : 0) + (size_t)kJointSmemBytes * joints;
+// lanes, a state word and a ref pair per manifold (400 bytes), plus 4 lanes
+// when the groups hold NONCONVEX manifolds (nonConvex: 464 bytes); with joints
+// the joints' solve lanes, state and refs (kJointSmemBytes each).
+__host__ __device__ constexpr int GroupManifoldLanes(bool nonConvex) { return nonConvex ? 29 : 25; }
+__host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int manifolds, int joints = 0,
+                                                    bool nonConvex = false) {
+    return 96 * (size_t)bodies + (shared ? 16 * (size_t)GroupManifoldLanes(nonConvex) * (size_t)manifolds : 0) +
+           (size_t)kJointSmemBytes * joints;
 }
 
 // One step of group g by the calling CTA (the body of the group kernels).
@@ -47,11 +51,15 @@ __host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int
 // body -- and their impulses go back to the joint lanes after the sweeps.
 // kJoints: 0 no joints, 1 the classic joint types (1-5) only, 2 any type; the
 // classic variant leaves the added types' branches out of the kernel.
+// nonConvex: the launch's shared lanes have room for NONCONVEX manifolds'
+// contact friction lanes (GroupManifoldLanes); a NONCONVEX manifold keeps its
+// friction direction and impulse in lanes 12-15 (the sliding lanes it does not
+// use), its prestep angular A in lanes 16-19 and angular B in lanes 25-28.
 template <bool kCensus, bool kShared, int kJoints>
 __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const JointSoA& jt,
                                           const StepParams& p, uint32_t flags, const GroupTables& t,
                                           const GroupDesc& g, int Bc, int Lc, int Jc, float4* smem,
-                                          unsigned long long* census) {
+                                          unsigned long long* census, bool nonConvex = false) {
     const int nLocal = g.bEnd - g.bBegin, nm = g.mEnd - g.mBegin;
     GroupBodies bv;
     bv.pos = smem;
@@ -86,13 +94,16 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
         ml.state = (uint2*)(lanes + 24 * Lc);
         sRefs = (int2*)(ml.state + Lc);
         ml.capacity = Lc;
+        ml.cfr = nonConvex ? lanes + 12 * Lc : nullptr;
+        ml.cfa = nonConvex ? lanes + 16 * Lc : nullptr;
+        ml.cfb = nonConvex ? lanes + 25 * Lc : nullptr;
     }
     // Joint solve lanes after the bodies and manifold lanes.
     JointSoA jl{};
     int2* jRefs = nullptr;
     const int nj = g.jEnd - g.jBegin;
     if (kJoints) {
-        float4* jbase = smem + 6 * Bc + (kShared ? 25 * Lc : 0);
+        float4* jbase = smem + 6 * Bc + (kShared ? GroupManifoldLanes(nonConvex) * Lc : 0);
         jl.lanes = jbase;
         jl.capacity = Jc;
         jl.state = (uint2*)(jbase + kJSolveLanes * Jc);
@@ -227,12 +238,17 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
                 jt.L(kJACC0, g.jBegin + q) = jl.L(kJACC0, q);
                 jt.L(kJACC1, g.jBegin + q) = jl.L(kJACC1, q);
             }
-        if (kShared) {  // impulses and sliding axis back to the manifold records
+        if (kShared) {  // impulses and sliding axis (NONCONVEX: contact friction) back to the manifold records
             for (int j = tid; j < nm; j += T) {
                 const int s = g.mBegin + j;
                 m.penacc[s] = ml.penacc[j];
                 m.fricacc[s] = ml.fricacc[j];
-                m.saxis[s] = ml.saxis[j];
+                const int4 h = ml.head[j];
+                if (nonConvex && (((uint32_t)h.z >> 8) & kManifoldNonConvex)) {
+                    for (int k = 0; k < (h.z & 0xff); k++) m.cfr[k * m.capacity + s] = ml.cfr[k * Lc + j];
+                } else {
+                    m.saxis[s] = ml.saxis[j];
+                }
             }
         }
     }

@@ -89,6 +89,7 @@ __device__ Views Carve(unsigned char* s, int nb, int nm) {
     v.m.mat = l1[0]; v.m.penacc = l1[1]; v.m.fricacc = l1[2]; v.m.saxis = l1[3];
     v.m.s0 = l1[4]; v.m.s1 = l1[5]; v.m.s3 = l1[6]; v.m.s4 = l1[7]; v.m.s5 = l1[8]; v.m.s6 = l1[9];
     v.m.s7 = l1[10]; v.m.lever = l1[11];
+    v.m.cfr = v.m.cfa = v.m.cfb = nullptr;  // NONCONVEX manifolds are refused
     v.m.state = (uint2*)(s + kStateAt);
     v.m.count = nm;
     v.m.capacity = kMaxManifolds;
@@ -120,7 +121,8 @@ __global__ void __launch_bounds__(kThreads) k_step_noalloc(bepugpu_body* bodies,
         int err = BEPUGPU_OK;
         for (int i = 0; i < nm && !err; i++) {
             int a = man[i].body_a, b = man[i].body_b, c = man[i].contact_count;
-            if (a < -1 || a >= nb || b < -1 || b >= nb || (a >= 0 && a == b) || c < 0 || c > 4)
+            if (a < -1 || a >= nb || b < -1 || b >= nb || (a >= 0 && a == b) || c < 0 || c > 4 ||
+                (man[i].flags & BEPUGPU_MANIFOLD_NONCONVEX))
                 err = BEPUGPU_INVALID_ARGUMENT;
         }
         sErr = err;

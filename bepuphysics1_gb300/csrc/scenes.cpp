@@ -248,8 +248,17 @@ struct Generator {
             }
         }
         bepugpu_manifold m = NewManifold(a, b);
+        if (SpherePairIsNonConvex(A, B)) m.flags |= BEPUGPU_MANIFOLD_NONCONVEX;
         AddContact(m, p, n, depth, 0);
         manifolds.push_back(m);
+    }
+
+    // The reference's sphere-sphere and box-sphere pair handlers carry a
+    // NonConvexContactManifoldConstraint (SpherePairHandler.cs:28,
+    // BoxSpherePairHandler.cs:28); pairs with a capsule are convex pairs.
+    static bool SpherePairIsNonConvex(const Body& A, const Body& B) {
+        return (A.shape == kSphere && (B.shape == kSphere || B.shape == kBox)) ||
+               (B.shape == kSphere && A.shape == kBox);
     }
 
     // Uniform-grid broad phase over all bodies except the ground (index 0,
@@ -298,6 +307,7 @@ struct Generator {
         if (A.shape == kSphere && B.shape == kBox) std::swap(a, b);  // box-sphere pairs put the box first
         bepugpu_manifold m = NewManifold(a, b);
         m.flags |= BEPUGPU_MANIFOLD_GENERATED;
+        if (SpherePairIsNonConvex(bodies[a], bodies[b])) m.flags |= BEPUGPU_MANIFOLD_NONCONVEX;
         manifolds.push_back(m);
     }
 

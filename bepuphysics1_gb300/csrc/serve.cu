@@ -321,6 +321,7 @@ struct Server {
         w.reqs.clear();
         std::vector<int4> shared, global;
         int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0, passes = 0;
+        bool sNonConvex = false;  // a shared-lane group holds a NONCONVEX manifold
         std::vector<int> plain;
         std::deque<int> keep;
         std::vector<Scene*> restored;  // copies in flight on their scenes' streams
@@ -407,6 +408,7 @@ struct Server {
                     sBc = std::max(sBc, gp.shared.maxLocal);
                     sLc = std::max(sLc, gp.shared.maxManifolds);
                     sMem = std::max(sMem, gp.shared.maxColourMembers);
+                    sNonConvex = sNonConvex || gp.nonConvexLanes;
                 }
                 if (gp.global.end > gp.global.begin) {
                     gBc = std::max(gBc, gp.global.maxLocal);
@@ -433,7 +435,7 @@ struct Server {
         }
         if (w.slotIds.empty()) return false;
         // one launch's shared-lane groups must fit a CTA's shared memory together
-        if (GroupSmemBytes(true, sBc, sLc) > kGroupSmemBudget + 16 * 1024) {
+        if (GroupSmemBytes(true, sBc, sLc, 0, sNonConvex) > kGroupSmemBudget + 16 * 1024) {
             for (auto& it : shared) global.push_back(it);
             gBc = std::max(gBc, sBc);
             gMem = std::max(gMem, sMem);
@@ -475,7 +477,7 @@ struct Server {
                   "work list copy");
             if (e == cudaSuccess && !shared.empty()) {
                 check(LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc, sMem,
-                                          0, passes, w.stream),
+                                          0, passes, w.stream, sNonConvex),
                       "group launch");
                 statLaunches += passes;
             }

@@ -73,9 +73,12 @@ enum : uint32_t {
     kDynB = 1u << 8,
     kHasA = 1u << 9,              // entity A is not null
     kHasB = 1u << 10,
+    kFricShift = 11,              // NONCONVEX: bits 11..14, contact friction 0..3 isActiveInSolver
     kIterShift = 16               // bits 16..31: group currentIterations
 };
-// Word y: 4-bit iterationsAtZeroImpulse per child (pen0..3, sliding, twist).
+// Word y: 4-bit iterationsAtZeroImpulse per child: pen0..3, then sliding and
+// twist (convex) or contact friction 0..3 (NONCONVEX).
+constexpr uint32_t kManifoldNonConvex = 8u;  // BEPUGPU_MANIFOLD_NONCONVEX, in head.z >> 8
 
 struct ManifoldSoA {
     int4* head;      // body A, body B, contact count | flags << 8, source index
@@ -99,6 +102,11 @@ struct ManifoldSoA {
     float4* s6;      // sliding angularB row 1, w = twist friction
     float4* s7;      // sliding angularB row 2
     float4* lever;   // twist lever arms
+    // NONCONVEX manifolds: one ContactFrictionConstraint per contact, in
+    // global memory only (a group with such a manifold keeps its lanes there)
+    float4* cfr;     // [4][cap] linearA (the friction direction, kept between steps), w = accumulatedImpulse
+    float4* cfa;     // [4][cap] prestep: angularA, w = velocityToImpulse
+    float4* cfb;     // [4][cap] prestep: angularB, w = friction
     uint2* state;
     int count;
     int capacity;
@@ -440,6 +448,20 @@ __device__ __forceinline__ void RefreshManifoldV(const ManifoldSoA& m, const V& 
             float4 f = m.fricacc[s];
             m.fricacc[s] = make_float4(0.f, 0.f, 0.f, f.w);
         }
+        if (((uint32_t)h.z >> 8) & kManifoldNonConvex) {
+            // NonConvexContactManifoldConstraint.RemoveContact (:139-166): each
+            // removed contact's friction child goes with it (CleanUp: impulse 0,
+            // and Setup clears the direction when the slot is reused).
+            int q = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (k >= count) break;
+                if (!keep[k]) continue;
+                if (q != k) m.cfr[q * cap + s] = m.cfr[k * cap + s];
+                q++;
+            }
+            for (int k = kept; k < count; k++) m.cfr[k * cap + s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 __device__ __forceinline__ void RefreshManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
@@ -487,11 +509,21 @@ __device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si,
     uint32_t st = 0;
     // BEPUGPU_MANIFOLD_ACTIVE = 1, BEPUGPU_MANIFOLD_SOLVER_RULE = 2
     bool groupActive = (mflags & 1u) && (mflags & 2u) && ((hasA && A.dynamic) || (hasB && B.dynamic));
-    // A manifold the sliding update skips keeps its axis; lanes staged in
-    // shared memory must carry it too (they are written back whole).
+    const bool nonConvex = mflags & kManifoldNonConvex;
+    // A manifold the sliding update skips keeps its axis, a NONCONVEX one its
+    // contacts' friction state; lanes staged in shared memory must carry them
+    // too (they are written back whole).
+    auto carryState = [&]() {
+        if (nonConvex) {
+            if (mo.cfr != mi.cfr)
+                for (int k = 0; k < count; k++) mo.cfr[k * capo + so] = mi.cfr[k * cap + si];
+        } else if (mo.saxis != mi.saxis) {
+            mo.saxis[so] = mi.saxis[si];
+        }
+    };
     if (!groupActive) {
         mo.state[so] = make_uint2(0u, 0u);
-        if (mo.saxis != mi.saxis) mo.saxis[so] = mi.saxis[si];
+        carryState();
         return;
     }
     st |= kGroupActive;
@@ -566,7 +598,77 @@ __device__ __forceinline__ void PrestepManifoldIO(const ManifoldSoA& mi, int si,
     }
     if (count == 0) {
         mo.state[so] = make_uint2(st, 0u);
-        if (mo.saxis != mi.saxis) mo.saxis[so] = mi.saxis[si];
+        carryState();
+        return;
+    }
+    if (nonConvex) {
+        // NonConvexContactManifoldConstraint.Update (NonConvexContactManifoldConstraint.cs:180-186):
+        // after the penetration children, each contact's ContactFrictionConstraint.Update
+        // (ContactFrictionConstraint.cs:147-256).  The friction direction and impulse come
+        // from mi; they go to mo with the prestep products.
+        st &= ~(kSlidingBit | kTwistBit);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= count) break;
+            const float4 cp = mi.cpos[k * cap + si], cn = mi.cnrm[k * cap + si];
+            float4 fr = mi.cfr[k * cap + si];
+            float rax = 0, ray = 0, raz = 0, rbx = 0, rby = 0, rbz = 0;  // the penetration child's ra, rb
+            float vAx = 0, vAy = 0, vAz = 0, vBx = 0, vBy = 0, vBz = 0;
+            if (hasA) {
+                rax = cp.x - A.px; ray = cp.y - A.py; raz = cp.z - A.pz;
+                vAx = A.wy * raz - A.wz * ray;  // Vector3.Cross(angularVelocity, ra)
+                vAy = A.wz * rax - A.wx * raz;
+                vAz = A.wx * ray - A.wy * rax;
+                vAx = vAx + A.vx; vAy = vAy + A.vy; vAz = vAz + A.vz;
+            }
+            if (hasB) {
+                rbx = cp.x - B.px; rby = cp.y - B.py; rbz = cp.z - B.pz;
+                vBx = B.wy * rbz - B.wz * rby;
+                vBy = B.wz * rbx - B.wx * rbz;
+                vBz = B.wx * rby - B.wy * rbx;
+                vBx = vBx + B.vx; vBy = vBy + B.vy; vBz = vBz + B.vz;
+            }
+            float rvx = vAx - vBx, rvy = vAy - vBy, rvz = vAz - vBz;
+            const float nvs = cn.x * rvx + cn.y * rvy + cn.z * rvz;
+            rvx -= nvs * cn.x;
+            rvy -= nvs * cn.y;
+            rvz -= nvs * cn.z;
+            float length = rvx * rvx + rvy * rvy + rvz * rvz;
+            float friction;
+            if (length > 1e-7f) {  // Toolbox.Epsilon
+                length = SqrtOfFloat(length);
+                fr.x = rvx / length;
+                fr.y = rvy / length;
+                fr.z = rvz / length;
+                friction = length > p.staticThreshold ? kinetic : staticF;
+            } else if (fr.x != 0 || fr.y != 0 || fr.z != 0) {
+                friction = staticF;  // the previous step's direction
+            } else {
+                mo.cfr[k * capo + so] = fr;
+                continue;  // no direction: isActiveInSolver = false for this step
+            }
+            st |= 1u << (kFricShift + k);
+            const float lx = fr.x, ly = fr.y, lz = fr.z;
+            const float aAx = (ray * lz) - (raz * ly), aAy = (raz * lx) - (rax * lz), aAz = (rax * ly) - (ray * lx);
+            const float aBx = (ly * rbz) - (lz * rby), aBy = (lz * rbx) - (lx * rbz), aBz = (lx * rby) - (ly * rbx);
+            float entryA, entryB, tX, tY, tZ;
+            if (dynA) {
+                tX = aAx * A.I11 + aAy * A.I21 + aAz * A.I31;
+                tY = aAx * A.I12 + aAy * A.I22 + aAz * A.I32;
+                tZ = aAx * A.I13 + aAy * A.I23 + aAz * A.I33;
+                entryA = tX * aAx + tY * aAy + tZ * aAz + A.invMass;
+            } else entryA = 0;
+            if (dynB) {
+                tX = aBx * B.I11 + aBy * B.I21 + aBz * B.I31;
+                tY = aBx * B.I12 + aBy * B.I22 + aBz * B.I32;
+                tZ = aBx * B.I13 + aBy * B.I23 + aBz * B.I33;
+                entryB = tX * aBx + tY * aBy + tZ * aBz + B.invMass;
+            } else entryB = 0;
+            mo.cfr[k * capo + so] = fr;
+            mo.cfa[k * capo + so] = make_float4(aAx, aAy, aAz, -1 / (entryA + entryB));
+            mo.cfb[k * capo + so] = make_float4(aBx, aBy, aBz, friction);
+        }
+        mo.state[so] = make_uint2(st, 0u);
         return;
     }
 
@@ -780,6 +882,28 @@ __device__ __forceinline__ void WarmStartManifold(const ManifoldSoA& m, int s, B
             ApplyAngular(B, acc * j2.x, acc * j2.y, acc * j2.z);
         }
     }
+    if (st & (0xfu << kFricShift)) {
+        // ContactFrictionConstraint.ExclusiveUpdate (ContactFrictionConstraint.cs:258-289)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= count) break;
+            if (!(st & (1u << (kFricShift + k)))) continue;
+            const float4 fr = m.cfr[k * cap + s];
+            const float acc = fr.w;
+            const float lx = acc * fr.x, ly = acc * fr.y, lz = acc * fr.z;
+            if (dynA) {
+                const float4 fa = m.cfa[k * cap + s];
+                ApplyLinear(A, lx, ly, lz);
+                ApplyAngular(A, acc * fa.x, acc * fa.y, acc * fa.z);
+            }
+            if (dynB) {
+                const float4 fb = m.cfb[k * cap + s];
+                ApplyLinear(B, -lx, -ly, -lz);
+                ApplyAngular(B, acc * fb.x, acc * fb.y, acc * fb.z);
+            }
+        }
+        return;
+    }
     if (count == 0) return;
     float4 f = m.fricacc[s];
     if (st & kSlidingBit) {
@@ -847,12 +971,13 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
         A1 = m.s4[s]; A2 = m.s5[s]; B1 = m.s6[s]; B2 = m.s7[s];
         LEV = m.lever[s];
     }
-    // SolveUpdateable bookkeeping for child c given its |impulse|.
-    auto account = [&](int c, float r) {
+    // SolveUpdateable bookkeeping for child c (its zero-impulse nibble) given
+    // its |impulse|; `bit` is its activity bit.
+    auto accountBit = [&](int c, uint32_t bit, float r) {
         uint32_t z = (zeros >> (4 * c)) & 0xfu;
         if (r < p.minimumImpulse) {
             z++;
-            if ((int)z > p.minimumIterationCount) st &= ~(1u << (kChildShift + c));
+            if ((int)z > p.minimumIterationCount) st &= ~bit;
             else activeConstraints++;
         } else {
             z = 0;
@@ -860,6 +985,7 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
         }
         zeros = (zeros & ~(0xfu << (4 * c))) | ((z & 0xfu) << (4 * c));
     };
+    auto account = [&](int c, float r) { accountBit(c, 1u << (kChildShift + c), r); };
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         if (k >= count) break;
@@ -884,6 +1010,38 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
             ApplyAngular(B, lambda * j2.x, lambda * j2.y, lambda * j2.z);
         }
         account(k, fabsf(lambda));
+    }
+    if (st & (0xfu << kFricShift)) {
+        // NONCONVEX: each contact's ContactFrictionConstraint.SolveIteration
+        // (ContactFrictionConstraint.cs:95-143), after every penetration child.
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (k >= count) break;
+            const uint32_t bit = 1u << (kFricShift + k);
+            if (!(st & bit)) continue;
+            float4 fr = m.cfr[k * cap + s];
+            const float4 fa = m.cfa[k * cap + s], fb = m.cfb[k * cap + s];
+            float velocity = 0;
+            if (hasA)
+                velocity += A.vx * fr.x + A.vy * fr.y + A.vz * fr.z + A.wx * fa.x + A.wy * fa.y + A.wz * fa.z;
+            if (hasB)
+                velocity += -B.vx * fr.x - B.vy * fr.y - B.vz * fr.z + B.wx * fb.x + B.wy * fb.y + B.wz * fb.z;
+            float lambda = velocity * fa.w;
+            const float prev = fr.w, maxForce = fb.w * accs[k];
+            fr.w = Clampf(fr.w + lambda, -maxForce, maxForce);
+            lambda = fr.w - prev;
+            const float ix = lambda * fr.x, iy = lambda * fr.y, iz = lambda * fr.z;
+            if (dynA) {
+                ApplyLinear(A, ix, iy, iz);
+                ApplyAngular(A, lambda * fa.x, lambda * fa.y, lambda * fa.z);
+            }
+            if (dynB) {
+                ApplyLinear(B, -ix, -iy, -iz);
+                ApplyAngular(B, lambda * fb.x, lambda * fb.y, lambda * fb.z);
+            }
+            accountBit(4 + k, bit, fabsf(lambda));
+            m.cfr[k * cap + s] = fr;
+        }
     }
     if (st & kSlidingBit) {
         // SlidingFrictionTwoAxis.SolveIteration (SlidingFrictionTwoAxis.cs:155-234)

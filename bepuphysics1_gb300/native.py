@@ -34,7 +34,7 @@ BODY_DTYPE = np.dtype([
 CONTACT_DTYPE = np.dtype([
     ("position", "<f4", 3), ("normal", "<f4", 3), ("penetration_depth", "<f4"), ("id", "<i4"),
     ("local_offset_a", "<f4", 3), ("local_offset_b", "<f4", 3), ("base_penetration_depth", "<f4"),
-    ("penetration_impulse", "<f4"),
+    ("penetration_impulse", "<f4"), ("friction_impulse", "<f4"), ("friction_direction", "<f4", 3),
 ])
 MANIFOLD_DTYPE = np.dtype([
     ("body_a", "<i4"), ("body_b", "<i4"), ("contact_count", "<i4"), ("flags", "<u4"),
@@ -49,7 +49,8 @@ BODY_STATE_DTYPE = np.dtype([
 ])
 MANIFOLD_STATE_DTYPE = np.dtype([
     ("contact_count", "<i4"), ("contact_id", "<i4", 4), ("penetration_impulse", "<f4", 4),
-    ("sliding_impulse", "<f4", 2), ("twist_impulse", "<f4"), ("sliding_axis", "<f4", 3), ("reserved", "<i4"),
+    ("sliding_impulse", "<f4", 2), ("twist_impulse", "<f4"), ("sliding_axis", "<f4", 3),
+    ("friction_impulse", "<f4", 4), ("reserved", "<i4"),
 ])
 SHAPE_DTYPE = np.dtype([("type", "<i4"), ("size", "<f4", 3)])
 JOINT_DTYPE = np.dtype([
@@ -113,7 +114,7 @@ BODY_ALWAYS_ACTIVE, BODY_NO_STABILIZATION, BODY_SLOWING, BODY_DEACTIVATION_CANDI
 SHAPE_NONE, SHAPE_BOX, SHAPE_SPHERE = 0, 1, 2
 NOALLOC_MAX_BODIES, NOALLOC_MAX_MANIFOLDS = 1024, 2048  # bepugpu_step_noalloc limits
 MODE_GRAPH, MODE_PERSISTENT = 0, 1
-MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE, MANIFOLD_GENERATED = 1, 2, 4
+MANIFOLD_ACTIVE, MANIFOLD_SOLVER_RULE, MANIFOLD_GENERATED, MANIFOLD_NONCONVEX = 1, 2, 4, 8
 JOINT_BALL_SOCKET, JOINT_REVOLUTE_ANGULAR, JOINT_SWING_LIMIT, JOINT_REVOLUTE_LIMIT, JOINT_REVOLUTE = 1, 2, 3, 4, 5
 JOINT_NO_ROTATION, JOINT_WELD, JOINT_DISTANCE, JOINT_DISTANCE_LIMIT = 6, 7, 8, 9
 JOINT_POINT_ON_PLANE, JOINT_TWIST = 10, 11

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 6
+#define BEPUGPU_ABI_VERSION 7
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -101,9 +101,12 @@ typedef struct bepugpu_body {
     float velocity_time_below_limit; /* SimulationIslandMember.velocityTimeBelowLimit (:18), in/out */
 } bepugpu_body;
 
-/* One contact of a convex manifold (Contact.cs:15-31) together with the
- * ContactSupplementData the refresher reads and the warm-start impulse of its
- * ContactPenetrationConstraint (ContactPenetrationConstraint.cs:21). */
+/* One contact of a manifold (Contact.cs:15-31) together with the
+ * ContactSupplementData the refresher reads, the warm-start impulse of its
+ * ContactPenetrationConstraint (ContactPenetrationConstraint.cs:21) and, in a
+ * NONCONVEX manifold, the state of its ContactFrictionConstraint
+ * (ContactFrictionConstraint.cs:49-58: accumulatedImpulse, and linearA, the
+ * friction direction a contact keeps while its sliding velocity is zero). */
 typedef struct bepugpu_contact {
     float position[3];
     float normal[3];
@@ -113,6 +116,8 @@ typedef struct bepugpu_contact {
     float local_offset_b[3];         /* ContactSupplementData.LocalOffsetB */
     float base_penetration_depth;    /* ContactSupplementData.BasePenetrationDepth */
     float penetration_impulse;       /* accumulated impulse, in/out */
+    float friction_impulse;          /* NONCONVEX: ContactFrictionConstraint.accumulatedImpulse, in/out */
+    float friction_direction[3];     /* NONCONVEX: ContactFrictionConstraint.linearA, in/out */
 } bepugpu_contact;
 
 /* Manifold flags. */
@@ -126,10 +131,21 @@ typedef struct bepugpu_contact {
  * contacts keep their warm-start impulse, new ones start at zero.  The
  * refresher skips such manifolds. */
 #define BEPUGPU_MANIFOLD_GENERATED   4u
+/* The manifold is a NonConvexContactManifoldConstraint
+ * (NonConvexContactManifoldConstraint.cs:12-216): each contact's penetration
+ * constraint, in contact-add order, then each contact's
+ * ContactFrictionConstraint (ContactFrictionConstraint.cs:95-299) in the same
+ * order; no sliding or twist friction (their record fields stay zero).  The
+ * reference builds these for sphere-sphere and box-sphere pairs
+ * (SpherePairHandler.cs:28, BoxSpherePairHandler.cs:28) and for mesh and
+ * terrain pairs.  Without the flag a manifold is a
+ * ConvexContactManifoldConstraint. */
+#define BEPUGPU_MANIFOLD_NONCONVEX   8u
 
-/* One ConvexContactManifoldConstraint (ConvexContactManifoldConstraint.cs:12-212):
+/* One ContactManifoldConstraint.  Convex (ConvexContactManifoldConstraint.cs:12-212):
  * up to four penetration children in contact-add order, then one
- * SlidingFrictionTwoAxis and one TwistFrictionConstraint. */
+ * SlidingFrictionTwoAxis and one TwistFrictionConstraint.  NONCONVEX: up to
+ * four penetration children, then one ContactFrictionConstraint per contact. */
 typedef struct bepugpu_manifold {
     int32_t body_a;                  /* index into the body array, -1 = no entity */
     int32_t body_b;
@@ -405,8 +421,11 @@ typedef struct bepugpu_body_state {
  * impulses in the solver's contact order (the penetration constraints'
  * accumulatedImpulse, ContactPenetrationConstraint.cs:21), the sliding and
  * twist friction impulses and the sliding axis (SlidingFrictionTwoAxis.cs,
- * TwistFrictionConstraint.cs).  Contact slots at and above contact_count are
- * zero. */
+ * TwistFrictionConstraint.cs) of a convex manifold, and the contacts'
+ * friction impulses (ContactFrictionConstraint.accumulatedImpulse) of a
+ * NONCONVEX one.  Contact slots at and above contact_count are zero; the
+ * NONCONVEX friction directions stay on the device (whole-record downloads
+ * carry them). */
 typedef struct bepugpu_manifold_state {
     int32_t contact_count;
     int32_t contact_id[4];
@@ -414,6 +433,7 @@ typedef struct bepugpu_manifold_state {
     float sliding_impulse[2];
     float twist_impulse;
     float sliding_axis[3];
+    float friction_impulse[4];
     int32_t reserved;
 } bepugpu_manifold_state;
 
@@ -425,7 +445,7 @@ typedef struct bepugpu_manifold_state {
  * (manifold_count = the scene's count), or nothing (manifold_count = 0).
  * Everything else -- masses, inertia, damping, the manifold set and its
  * contacts, joints -- stays as the last uploads and the device's own steps
- * left it, so a step moves 64 bytes a body each way and 64 bytes a manifold
+ * left it, so a step moves 64 bytes a body each way and 80 bytes a manifold
  * down, against whole records in bepugpu_step_host.  One host
  * synchronisation.  No reference counterpart: the reference's stages share
  * the entities' memory. */
@@ -598,9 +618,11 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* ctx, int32_t scene, float d
  * BEPUGPU_INVALID_OPERATION with the records unchanged, where
  * bepugpu_upload_constraints has no colour limit.  Records whose manifolds
  * name bodies out of range, the same body twice or a contact count outside
- * 0..4 return BEPUGPU_INVALID_ARGUMENT, found on the device before anything is
- * written.  Settings are bounded as bepugpu_create bounds them.  Damping
- * factors are computed with the device's double pow.  There is no narrow
+ * 0..4, and NONCONVEX manifolds (their contact friction lanes are not in the
+ * scratch), return BEPUGPU_INVALID_ARGUMENT, found on the device before
+ * anything is written.  Settings are bounded as bepugpu_create bounds them
+ * (iteration_limit 0..65535).  Damping factors are the float of the
+ * reference's double pow, computed on the device.  There is no narrow
  * phase here: GENERATED manifolds are stepped with the contacts they hold
  * (and not refreshed). */
 #define BEPUGPU_NOALLOC_MAX_BODIES 1024

@@ -496,7 +496,85 @@ struct TwistFriction : SolverUpdateable {
     }
 };
 
-// ConvexContactManifoldConstraint.cs:12-212 over ContactManifoldConstraint.cs:15-174
+// ContactFrictionConstraint.cs:10-299: one per contact of a nonconvex manifold.
+struct ContactFriction : SolverUpdateable {
+    ConvexManifold* m = nullptr;
+    PenetrationConstraint* penetration = nullptr;
+    float accumulatedImpulse = 0;
+    float angularAX = 0, angularAY = 0, angularAZ = 0;
+    float angularBX = 0, angularBY = 0, angularBZ = 0;
+    float friction = 0;
+    float linearAX = 0, linearAY = 0, linearAZ = 0;
+    Entity *entityA = nullptr, *entityB = nullptr;
+    bool entityAIsDynamic = false, entityBIsDynamic = false;
+    float velocityToImpulse = 0;
+
+    float RelativeVelocity() const {  // :85-97
+        float velocity = 0;
+        if (entityA)
+            velocity += entityA->linearVelocity.X * linearAX + entityA->linearVelocity.Y * linearAY +
+                        entityA->linearVelocity.Z * linearAZ + entityA->angularVelocity.X * angularAX +
+                        entityA->angularVelocity.Y * angularAY + entityA->angularVelocity.Z * angularAZ;
+        if (entityB)
+            velocity += -entityB->linearVelocity.X * linearAX - entityB->linearVelocity.Y * linearAY -
+                        entityB->linearVelocity.Z * linearAZ + entityB->angularVelocity.X * angularBX +
+                        entityB->angularVelocity.Y * angularBY + entityB->angularVelocity.Z * angularBZ;
+        return velocity;
+    }
+    float SolveIteration() override {  // :100-143
+        float lambda = RelativeVelocity() * velocityToImpulse;
+        float previousAccumulatedImpulse = accumulatedImpulse;
+        float maxForce = friction * penetration->accumulatedImpulse;
+        accumulatedImpulse = Clamp(accumulatedImpulse + lambda, -maxForce, maxForce);
+        lambda = accumulatedImpulse - previousAccumulatedImpulse;
+        Vec3 linear, angular;
+        linear.X = lambda * linearAX;
+        linear.Y = lambda * linearAY;
+        linear.Z = lambda * linearAZ;
+        if (entityAIsDynamic) {
+            angular.X = lambda * angularAX;
+            angular.Y = lambda * angularAY;
+            angular.Z = lambda * angularAZ;
+            entityA->ApplyLinearImpulse(linear);
+            entityA->ApplyAngularImpulse(angular);
+        }
+        if (entityBIsDynamic) {
+            linear.X = -linear.X; linear.Y = -linear.Y; linear.Z = -linear.Z;
+            angular.X = lambda * angularBX;
+            angular.Y = lambda * angularBY;
+            angular.Z = lambda * angularBZ;
+            entityB->ApplyLinearImpulse(linear);
+            entityB->ApplyAngularImpulse(angular);
+        }
+        return std::fabs(lambda);
+    }
+    void Update(float dt) override;
+    void ExclusiveUpdate() override {  // :258-289
+        Vec3 linear, angular;
+        linear.X = accumulatedImpulse * linearAX;
+        linear.Y = accumulatedImpulse * linearAY;
+        linear.Z = accumulatedImpulse * linearAZ;
+        if (entityAIsDynamic) {
+            angular.X = accumulatedImpulse * angularAX;
+            angular.Y = accumulatedImpulse * angularAY;
+            angular.Z = accumulatedImpulse * angularAZ;
+            entityA->ApplyLinearImpulse(linear);
+            entityA->ApplyAngularImpulse(angular);
+        }
+        if (entityBIsDynamic) {
+            linear.X = -linear.X; linear.Y = -linear.Y; linear.Z = -linear.Z;
+            angular.X = accumulatedImpulse * angularBX;
+            angular.Y = accumulatedImpulse * angularBY;
+            angular.Z = accumulatedImpulse * angularBZ;
+            entityB->ApplyLinearImpulse(linear);
+            entityB->ApplyAngularImpulse(angular);
+        }
+    }
+};
+
+// ConvexContactManifoldConstraint.cs:12-212 over ContactManifoldConstraint.cs:15-174,
+// or, with nonConvex, NonConvexContactManifoldConstraint.cs:12-216: one
+// ContactFriction per contact in place of the sliding and twist friction.
 struct ConvexManifold : SolverGroup {
     Entity *entityA = nullptr, *entityB = nullptr;
     float kineticFriction = 0, staticFriction = 0, bounciness = 0;
@@ -509,14 +587,20 @@ struct ConvexManifold : SolverGroup {
     bool generated = false;  // contacts come from the narrow phase each step
     SlidingFriction slidingFriction;
     TwistFriction twistFriction;
+    bool nonConvex = false;
+    ContactFriction fpool[4];
+    std::vector<ContactFriction*> frictionConstraints;  // nonConvex: one per contact, in contact-add order
     int sourceIndex = 0;
 
     ConvexManifold() {
         // ConvexContactManifoldConstraint.cs:75-84: four penetration children,
-        // then sliding, then twist, all initially inactive.
+        // then sliding, then twist, all initially inactive.  The contact
+        // friction children (NonConvexContactManifoldConstraint.cs:64-74) stay
+        // inactive unless the manifold is nonconvex.
         for (auto& p : pool) { p.isActive = false; p.m = this; children.push_back(&p); }
         slidingFriction.isActive = false; slidingFriction.m = this; children.push_back(&slidingFriction);
         twistFriction.isActive = false; twistFriction.m = this; children.push_back(&twistFriction);
+        for (auto& f : fpool) { f.isActive = false; f.m = this; children.push_back(&f); }
     }
     // ContactManifoldConstraint.cs:128-145 with every entity awake
     void UpdateSolverActivity() override {
@@ -527,26 +611,40 @@ struct ConvexManifold : SolverGroup {
             isActiveInSolver = false;
         }
     }
-    void Update(float dt) override {  // :171-177
+    void Update(float dt) override {  // :171-177; NonConvexContactManifoldConstraint.cs:180-186
         for (auto* p : penetrationConstraints) UpdateUpdateable(p, dt);
+        if (nonConvex) {
+            for (auto* f : frictionConstraints) UpdateUpdateable(f, dt);
+            return;
+        }
         UpdateUpdateable(&slidingFriction, dt);
         UpdateUpdateable(&twistFriction, dt);
     }
-    void ExclusiveUpdate() override {  // :186-192
+    void ExclusiveUpdate() override {  // :186-192; NonConvexContactManifoldConstraint.cs:189-195
         for (auto* p : penetrationConstraints) ExclusiveUpdateUpdateable(p);
+        if (nonConvex) {
+            for (auto* f : frictionConstraints) ExclusiveUpdateUpdateable(f);
+            return;
+        }
         ExclusiveUpdateUpdateable(&slidingFriction);
         ExclusiveUpdateUpdateable(&twistFriction);
     }
-    float SolveIteration() override {  // :199-212
+    float SolveIteration() override {  // :199-212; NonConvexContactManifoldConstraint.cs:198-207
         int activeConstraints = 0;
         for (auto* p : penetrationConstraints) SolveUpdateable(p, activeConstraints);
-        SolveUpdateable(&slidingFriction, activeConstraints);
-        SolveUpdateable(&twistFriction, activeConstraints);
+        if (nonConvex) {
+            for (auto* f : frictionConstraints) SolveUpdateable(f, activeConstraints);
+        } else {
+            SolveUpdateable(&slidingFriction, activeConstraints);
+            SolveUpdateable(&twistFriction, activeConstraints);
+        }
         isActiveInSolver = activeConstraints > 0;
         return solverSettings.minimumImpulse + 1;
     }
     // AddContact (:117-129): the first contact sets up sliding and twist.
-    void AddContact(const Contact& c, float impulse) {
+    // Nonconvex (NonConvexContactManifoldConstraint.cs:115-126): a penetration
+    // and a friction child per contact, the friction child Setup (linearA = 0).
+    void AddContact(const Contact& c, float impulse, float frictionImpulse = 0, Vec3 frictionDirection = Vec3()) {
         PenetrationConstraint* p = nullptr;
         for (auto& q : pool)
             if (!q.isActive) { p = &q; break; }
@@ -556,6 +654,18 @@ struct ConvexManifold : SolverGroup {
         p->accumulatedImpulse = impulse;
         penetrationConstraints.push_back(p);
         contactList.push_back(p);
+        if (nonConvex) {
+            ContactFriction* f = nullptr;
+            for (auto& q : fpool)
+                if (!q.isActive) { f = &q; break; }
+            f->penetration = p;
+            f->isActive = true;
+            f->entityA = entityA; f->entityB = entityB;
+            f->linearAX = frictionDirection.X; f->linearAY = frictionDirection.Y; f->linearAZ = frictionDirection.Z;
+            f->accumulatedImpulse = frictionImpulse;
+            frictionConstraints.push_back(f);
+            return;
+        }
         if (!twistFriction.isActive) {
             twistFriction.isActive = true;
             twistFriction.entityA = entityA; twistFriction.entityB = entityB;
@@ -585,6 +695,19 @@ struct ConvexManifold : SolverGroup {
         p->isActive = false;
         p->entityA = p->entityB = nullptr;
         penetrationConstraints.erase(penetrationConstraints.begin() + i);
+        // NonConvexContactManifoldConstraint.RemoveContact (:139-166): the
+        // contact's friction child, found from the end, CleanUp and RemoveAt.
+        for (int k = (int)frictionConstraints.size() - 1; k >= 0; k--) {
+            ContactFriction* f = frictionConstraints[k];
+            if (f->penetration == p) {
+                f->accumulatedImpulse = 0;
+                f->isActive = false;
+                f->penetration = nullptr;
+                f->entityA = f->entityB = nullptr;
+                frictionConstraints.erase(frictionConstraints.begin() + k);
+                break;
+            }
+        }
         if (penetrationConstraints.empty()) {
             twistFriction.accumulatedImpulse = 0; twistFriction.isActive = false;
             twistFriction.entityA = twistFriction.entityB = nullptr;
@@ -648,6 +771,66 @@ void PenetrationConstraint::Update(float dt) {  // ContactPenetrationConstraint.
     } else {
         bias = contact.PenetrationDepth * updateRate;
     }
+}
+
+void ContactFriction::Update(float dt) {  // ContactFrictionConstraint.cs:147-256
+    (void)dt;
+    entityAIsDynamic = entityA != nullptr && entityA->isDynamic;
+    entityBIsDynamic = entityB != nullptr && entityB->isDynamic;
+    Vec3 velocityA, velocityB;
+    const Vec3 ra = penetration->ra, rb = penetration->rb;
+    if (entityA) {
+        velocityA = Cross(entityA->angularVelocity, ra);
+        velocityA = Add(velocityA, entityA->linearVelocity);
+    }
+    if (entityB) {
+        velocityB = Cross(entityB->angularVelocity, rb);
+        velocityB = Add(velocityB, entityB->linearVelocity);
+    }
+    Vec3 relativeVelocity = Subtract(velocityA, velocityB);
+    const Vec3 normal = penetration->contact.Normal;
+    float normalVelocityScalar =
+        normal.X * relativeVelocity.X + normal.Y * relativeVelocity.Y + normal.Z * relativeVelocity.Z;
+    relativeVelocity.X -= normalVelocityScalar * normal.X;
+    relativeVelocity.Y -= normalVelocityScalar * normal.Y;
+    relativeVelocity.Z -= normalVelocityScalar * normal.Z;
+    float length = LengthSquared(relativeVelocity);
+    if (length > 1e-7f) {  // Toolbox.Epsilon
+        length = (float)std::sqrt((double)length);
+        linearAX = relativeVelocity.X / length;
+        linearAY = relativeVelocity.Y / length;
+        linearAZ = relativeVelocity.Z / length;
+        friction = length > m->space->s.staticThreshold ? m->kineticFriction : m->staticFriction;
+    } else {
+        if (linearAX != 0 || linearAY != 0 || linearAZ != 0) {
+            friction = m->staticFriction;
+        } else {
+            isActiveInSolver = false;
+            return;
+        }
+    }
+    angularAX = (ra.Y * linearAZ) - (ra.Z * linearAY);
+    angularAY = (ra.Z * linearAX) - (ra.X * linearAZ);
+    angularAZ = (ra.X * linearAY) - (ra.Y * linearAX);
+    angularBX = (linearAY * rb.Z) - (linearAZ * rb.Y);
+    angularBY = (linearAZ * rb.X) - (linearAX * rb.Z);
+    angularBZ = (linearAX * rb.Y) - (linearAY * rb.X);
+    float entryA, entryB, tX, tY, tZ;
+    if (entityAIsDynamic) {
+        const Mat3& I = entityA->inertiaTensorInverse;
+        tX = angularAX * I.M11 + angularAY * I.M21 + angularAZ * I.M31;
+        tY = angularAX * I.M12 + angularAY * I.M22 + angularAZ * I.M32;
+        tZ = angularAX * I.M13 + angularAY * I.M23 + angularAZ * I.M33;
+        entryA = tX * angularAX + tY * angularAY + tZ * angularAZ + entityA->inverseMass;
+    } else entryA = 0;
+    if (entityBIsDynamic) {
+        const Mat3& I = entityB->inertiaTensorInverse;
+        tX = angularBX * I.M11 + angularBY * I.M21 + angularBZ * I.M31;
+        tY = angularBX * I.M12 + angularBY * I.M22 + angularBZ * I.M32;
+        tZ = angularBX * I.M13 + angularBY * I.M23 + angularBZ * I.M33;
+        entryB = tX * angularBX + tY * angularBY + tZ * angularBZ + entityB->inverseMass;
+    } else entryB = 0;
+    velocityToImpulse = -1 / (entryA + entryB);
 }
 
 float SlidingFriction::SolveIteration() {  // SlidingFrictionTwoAxis.cs:155-234
@@ -1234,6 +1417,7 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
         m->SetInvolved(m->entityA, m->entityB);
         m->isActive = (mr.flags & BEPUGPU_MANIFOLD_ACTIVE) != 0;
         m->generated = (mr.flags & BEPUGPU_MANIFOLD_GENERATED) != 0;
+        m->nonConvex = (mr.flags & BEPUGPU_MANIFOLD_NONCONVEX) != 0;
         m->solverRule = (mr.flags & BEPUGPU_MANIFOLD_SOLVER_RULE) != 0;
         m->kineticFriction = mr.kinetic_friction;
         m->staticFriction = mr.static_friction;
@@ -1257,7 +1441,7 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
             c.LocalOffsetA = V3(cr.local_offset_a);
             c.LocalOffsetB = V3(cr.local_offset_b);
             c.BasePenetrationDepth = cr.base_penetration_depth;
-            m->AddContact(c, cr.penetration_impulse);
+            m->AddContact(c, cr.penetration_impulse, cr.friction_impulse, V3(cr.friction_direction));
         }
         if (m->generated && cc > 0) {  // the list order carried in contact_order
             std::vector<PenetrationConstraint*> list(cc);
@@ -1357,6 +1541,15 @@ void oracle_get_constraints(oracle_space* s, bepugpu_manifold* manifolds, bepugp
             P3(cr.local_offset_b, p->contact.LocalOffsetB);
             cr.base_penetration_depth = p->contact.BasePenetrationDepth;
             cr.penetration_impulse = p->accumulatedImpulse;
+            cr.friction_impulse = 0;
+            cr.friction_direction[0] = cr.friction_direction[1] = cr.friction_direction[2] = 0;
+            if (m->nonConvex) {
+                const ContactFriction* f = m->frictionConstraints[k];
+                cr.friction_impulse = f->accumulatedImpulse;
+                cr.friction_direction[0] = f->linearAX;
+                cr.friction_direction[1] = f->linearAY;
+                cr.friction_direction[2] = f->linearAZ;
+            }
         }
         for (int k = cc; k < 4; k++) std::memset(&mr.contacts[k], 0, sizeof(bepugpu_contact));
         mr.sliding_impulse[0] = m->slidingFriction.accX;

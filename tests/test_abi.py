@@ -37,14 +37,14 @@ def test_binding_covers_header():
 
 def test_record_sizes():
     lib = N.load_gpu_library()
-    assert lib.bepugpu_abi_version() == 6
+    assert lib.bepugpu_abi_version() == 7
     assert lib.bepugpu_record_size(0) == N.SETTINGS_DTYPE.itemsize
     assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 116
-    assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 64
+    assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 80
     assert lib.bepugpu_record_size(3) == N.MANIFOLD_DTYPE.itemsize
     assert lib.bepugpu_record_size(4) == N.JOINT_DTYPE.itemsize
     assert lib.bepugpu_record_size(5) == N.BODY_STATE_DTYPE.itemsize == 64
-    assert lib.bepugpu_record_size(6) == N.MANIFOLD_STATE_DTYPE.itemsize == 64
+    assert lib.bepugpu_record_size(6) == N.MANIFOLD_STATE_DTYPE.itemsize == 80
     assert lib.bepugpu_record_size(99) == 0
 
 

@@ -169,8 +169,9 @@ def test_chains_in_island_groups(gpu_context, policy):
     errs, exact = p.compare()
     assert exact, (policy, errs)
     if policy[0]:
-        # chains and loose stacks are small islands: the step is the group launch alone
-        assert p.gpu.last_step_launches() <= 2
+        # chains and loose stacks are small islands: the step is group launches alone,
+        # one per group kind (shared or global lanes, with or without joints)
+        assert p.gpu.last_step_launches() <= 4
     p.close()
 
 

@@ -26,6 +26,8 @@ def _same_manifolds(state: np.ndarray, records: np.ndarray):
     imp = np.where(live, records["contacts"]["penetration_impulse"], np.float32(0))
     assert state["contact_id"].tobytes() == ids.astype(np.int32).tobytes()
     assert state["penetration_impulse"].tobytes() == imp.astype(np.float32).tobytes()
+    fimp = np.where(live, records["contacts"]["friction_impulse"], np.float32(0))
+    assert state["friction_impulse"].tobytes() == fimp.astype(np.float32).tobytes()
     for f in ("sliding_impulse", "twist_impulse", "sliding_axis"):
         assert state[f].tobytes() == np.ascontiguousarray(records[f]).tobytes(), f
     assert not state["reserved"].any()

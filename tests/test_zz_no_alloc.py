@@ -165,7 +165,8 @@ def test_noalloc_colour_limit():
             assert _host(dev_m, N.MANIFOLD_DTYPE).tobytes() == m.tobytes()
 
 
-@pytest.mark.parametrize("field,value", [("body_b", 10 ** 6), ("contact_count", 5), ("body_a", -2), ("same", 0)])
+@pytest.mark.parametrize("field,value", [("body_b", 10 ** 6), ("contact_count", 5), ("body_a", -2), ("same", 0),
+                                         ("flags", N.MANIFOLD_ACTIVE | N.MANIFOLD_SOLVER_RULE | N.MANIFOLD_NONCONVEX)])
 def test_noalloc_device_side_validation(field, value):
     """A bad manifold record is caught on the device (the host only checks
     sizes): INVALID_ARGUMENT, the caller's records untouched, and the next
