@@ -715,6 +715,19 @@ def collide_section(args, local, rank, world, pg):
                    "l2": "flushed between timed steps (512 MiB write)"},
         "parity": "bit-exact vs the oracle's narrow phase and solver (tests/test_gpu_collide.py)",
     }
+    # the broad phase over the same bodies: the overlapping pairs, sorted
+    sp.broad_phase(DT)  # first call sizes its buffers
+    bp_ms = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        bp_pairs = sp.broad_phase(DT)
+        bp_ms.append(1000 * (time.perf_counter() - t0))
+    out["broad_phase"] = {"ms_per_call": statistics.median(bp_ms), "pairs": int(len(bp_pairs)),
+                          "bodies_per_s": len(bodies) / (statistics.median(bp_ms) / 1000.0),
+                          "path": "bepugpu_broad_phase: boxes, uniform-grid cell entries sorted on the device, "
+                                  "pairs within cells, pairs sorted on the device and copied back; host clock "
+                                  "per call",
+                          "parity": "the oracle's brute-force pair set (tests/test_gpu_broad_phase.py)"}
     sp.close()
     ctx.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

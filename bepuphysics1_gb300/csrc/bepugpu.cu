@@ -675,6 +675,7 @@ Scene::~Scene() {
         if (e) cudaEventDestroy(e);
     for (auto e : evGroup)
         if (e) cudaEventDestroy(e);
+    ReleaseBroadPhase(this);
     if (stream) cudaStreamDestroy(stream);
 }
 

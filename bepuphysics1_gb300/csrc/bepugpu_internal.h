@@ -23,6 +23,8 @@ namespace bepugpu {
 struct Context;
 struct BatchEngine;
 struct Scene;
+struct BroadPhaseBuffers;
+void ReleaseBroadPhase(Scene* s);  // broadphase.cu
 
 // Device memory of a context's scene arenas and staging buffers, carved from
 // large cudaMalloc slabs (heap.cu).  Thread-safe: a server's worker spills and
@@ -336,6 +338,7 @@ struct Scene {
     uint32_t launchesPerStep = 0;
     int persistentBlocks = 0;
     bool persistentAdded = false;  // the persistent variant persistentBlocks was sized for
+    BroadPhaseBuffers* broadPhase = nullptr;  // device buffers of bepugpu_broad_phase (broadphase.cu)
 
     ~Scene();
     bepugpu_status Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj);

@@ -147,6 +147,7 @@ GPU_EXPORTS = {
     "bepugpu_scene_destroy": (_I, [_P, _I]),
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
+    "bepugpu_broad_phase": (_I, [_P, _I, _F, _P, _U, ctypes.POINTER(_U)]),
     "bepugpu_step_host": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_step_state": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_download_state": (_I, [_P, _I, _P, _U, _P, _U]),

@@ -177,6 +177,21 @@ class GpuSpace:
         self.ctx.check(self.ctx.lib.bepugpu_step_state(self.ctx.handle, self.id, N.ptr(bodies), len(bodies),
                                                        N.ptr(manifolds), nm, float(dt), flags))
 
+    def broad_phase(self, dt: float, max_pairs: int | None = None) -> np.ndarray:
+        """bepugpu_broad_phase: the overlapping pairs of shaped bodies as an
+        (n, 2) int32 array, ascending; grows the buffer once when max_pairs is
+        too small (None: start at four pairs a body)."""
+        cap = 4 * self.body_count if max_pairs is None else max_pairs
+        for _ in range(2):
+            out = np.zeros((max(cap, 1), 2), np.int32)
+            n = ctypes.c_uint32()
+            self.ctx.check(self.ctx.lib.bepugpu_broad_phase(self.ctx.handle, self.id, float(dt), N.ptr(out), cap,
+                                                            ctypes.byref(n)))
+            if n.value <= cap:
+                return out[:n.value]
+            cap = n.value
+        raise RuntimeError("broad phase pair count kept growing")
+
     def download_state(self, bodies: np.ndarray | None = None, manifolds: np.ndarray | None = None):
         """bepugpu_download_state into the given state arrays (either may be None)."""
         nb = 0 if bodies is None else len(bodies)

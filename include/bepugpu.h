@@ -381,6 +381,24 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* ctx, int32_t scene,
  * sphere-sphere); bepugpu_upload_constraints checks it. */
 bepugpu_status bepugpu_upload_shapes(bepugpu_context* ctx, int32_t scene, const bepugpu_shape* shapes,
                                      uint32_t count);
+
+/* Broad phase (the pair set the reference's DynamicHierarchy reports,
+ * BroadPhaseSystems/Hierarchies/DynamicHierarchy.cs): every pair of shaped
+ * bodies whose bounding boxes overlap, from the bodies' current state.  A
+ * body's box is its shape's (BoxShape.GetBoundingBox, BoxShape.cs:149-174;
+ * SphereShape.GetBoundingBox, SphereShape.cs:75-86) expanded by its linear
+ * velocity times dt (EntityCollidable.ExpandBoundingBox,
+ * EntityCollidable.cs:195-216, discrete bodies; dt = 0: no expansion); boxes
+ * overlap as BoundingBox.Intersects (BoundingBox.cs:58-66) has it; two
+ * kinematic bodies make no pair (the default kinematic group's NoBroadPhase
+ * rule, CollisionRules.cs:177); bodies of shape NONE take no part.  Pairs are
+ * written as (lower index, higher index) in ascending order, at most
+ * max_pairs of them (2 int32 each); *pair_count receives how many there are,
+ * which may exceed max_pairs.  Needs bepugpu_upload_shapes.  The hierarchy's
+ * own traversal order is not reproduced.  Allocates device buffers on first
+ * use and when the pair count grows. */
+bepugpu_status bepugpu_broad_phase(bepugpu_context* ctx, int32_t scene, float dt, int32_t* pairs,
+                                   uint32_t max_pairs, uint32_t* pair_count);
 /* Rewrites manifold records in place without recolouring.  Body pairs and the
  * manifold count must be those of the last bepugpu_upload_constraints (checked
  * on the device before anything changes; INVALID_ARGUMENT otherwise). */

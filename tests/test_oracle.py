@@ -152,10 +152,31 @@ def test_colouring_edge_cases():
         colour_list(b, bad)
 
 
-def test_identity_order_matches_permutation_invariants():
-    """Reference order and colour order are both Gauss-Seidel sweeps over the
-    same constraints; after 60 steps the pile's kinetic state agrees to the
-    level the orders' different sequences allow."""
+def _approach_residual(bodies, manifolds):
+    """RMS over contacts of the approach speed along the normal left after a
+    step (the velocity residual of the penetration constraints: relative
+    velocity of B against A at the contact, negative when approaching)."""
+    v = bodies["linear_velocity"].astype(np.float64)
+    w = bodies["angular_velocity"].astype(np.float64)
+    p = bodies["position"].astype(np.float64)
+    out = []
+    for mi in manifolds:
+        a, bb = mi["body_a"], mi["body_b"]
+        for k in range(mi["contact_count"]):
+            c = mi["contacts"][k]
+            x, n = c["position"].astype(np.float64), c["normal"].astype(np.float64)
+            va = v[a] + np.cross(w[a], x - p[a]) if a >= 0 else np.zeros(3)
+            vb = v[bb] + np.cross(w[bb], x - p[bb]) if bb >= 0 else np.zeros(3)
+            out.append(min(float(np.dot(vb - va, n)), 0.0))
+    return float(np.sqrt(np.mean(np.square(out))))
+
+
+def test_reference_order_and_colour_order_reach_equal_residual():
+    """Reference order (PermutationMapper) and colour order are both
+    Gauss-Seidel sweeps over the same constraints but in different orders, so
+    their states differ; after 60 steps both leave the pile with the same
+    small velocity residual (approach speed at the contacts within 25 % of
+    each other and below 1 cm/s) and poses within 2 cm."""
     s = default_settings()
     b, m, _ = scenes.pile_1k()
     col, order, _ = colour_list(b, m)
@@ -163,13 +184,15 @@ def test_identity_order_matches_permutation_invariants():
     ref.set_order_mode(oracle.ORDER_PERMUTED, 0)
     colr = oracle.OracleSpace(s, b, m)
     colr.set_list_order(order)
-    ref.step(DT, N.STEP_ALL, 20)
-    colr.step(DT, N.STEP_ALL, 20)
-    v1 = ref.get_bodies()["linear_velocity"]
-    v2 = colr.get_bodies()["linear_velocity"]
-    # both settle: velocities stay small and close
-    assert np.abs(v1).max() < 1.0 and np.abs(v2).max() < 1.0
-    assert np.abs(v1 - v2).max() < 0.25
+    ref.step(DT, N.STEP_ALL, 60)
+    colr.step(DT, N.STEP_ALL, 60)
+    b1, b2 = ref.get_bodies(), colr.get_bodies()
+    r1 = _approach_residual(b1, ref.get_constraints()[0])
+    r2 = _approach_residual(b2, colr.get_constraints()[0])
+    assert r1 < 0.01 and r2 < 0.01, (r1, r2)
+    assert abs(r1 - r2) <= 0.25 * max(r1, r2), (r1, r2)
+    assert np.abs(b1["position"] - b2["position"]).max() < 0.02
+    assert np.abs(b1["linear_velocity"]).max() < 1.0 and np.abs(b2["linear_velocity"]).max() < 1.0
 
 
 def test_multithreaded_baseline_runs():
