@@ -1471,10 +1471,11 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
         if (jst != BEPUGPU_OK) return jst;
     }
     std::vector<int32_t> a(nm + nj), bb(nm + nj);
-    std::vector<uint8_t> nonConvex(nm);
+    std::vector<uint8_t> nonConvex(nm), follows(nm + nj, 0);
     for (uint32_t u = 0; u < nj; u++) {
         a[u] = joints[u].body_a;
         bb[u] = joints[u].body_b;
+        follows[u] = (joints[u].flags & BEPUGPU_JOINT_GROUP_CONTINUATION) != 0;
     }
     for (uint32_t i = 0; i < nm; i++) {
         a[nj + i] = man[i].body_a;
@@ -1489,7 +1490,8 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
             return BEPUGPU_INVALID_ARGUMENT;
         }
     }
-    if (!ColourSolverList(a.data(), bb.data(), (int32_t)(nm + nj), s->hostDynamic.data(), nb, s->colouring)) {
+    if (!ColourSolverList(a.data(), bb.data(), (int32_t)(nm + nj), s->hostDynamic.data(), nb, s->colouring,
+                          follows.data())) {
         ctx->SetError("a constraint references a body outside [0, %d)", nb);
         return BEPUGPU_INVALID_ARGUMENT;
     }

@@ -5,7 +5,7 @@
 namespace bepugpu {
 
 bool ColourSolverList(const int32_t* a, const int32_t* b, int32_t n, const uint8_t* dynamic, int32_t bodies,
-                      Colouring& out) {
+                      Colouring& out, const uint8_t* follows) {
     out.colour.assign(n, 0);
     out.order.assign(n, 0);
     out.colours = 0;
@@ -16,6 +16,10 @@ bool ColourSolverList(const int32_t* a, const int32_t* b, int32_t n, const uint8
         int32_t ends[2] = {a[u], b[u]};
         for (int32_t e : ends)
             if (e < -1 || e >= bodies) return false;
+        if (follows && follows[u] && u > 0) {
+            out.colour[u] = out.colour[u - 1];
+            continue;
+        }
         const std::vector<uint64_t>* sets[2] = {nullptr, nullptr};
         int ns = 0;
         for (int32_t e : ends)

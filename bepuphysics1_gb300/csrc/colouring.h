@@ -22,8 +22,11 @@ struct Colouring {
 };
 
 // a[i], b[i]: body indices of updateable i (-1 = none); dynamic[k] != 0 for
-// dynamic bodies.  Returns false if an index is out of range.
+// dynamic bodies.  follows[i] != 0 (null: none) marks an entry that is part of
+// entry i - 1's visit (a group's continuation record): it takes i - 1's colour
+// and claims nothing, so the rest of the colouring is the one of the list
+// without it.  Returns false if an index is out of range.
 bool ColourSolverList(const int32_t* a, const int32_t* b, int32_t n, const uint8_t* dynamic, int32_t bodies,
-                      Colouring& out);
+                      Colouring& out, const uint8_t* follows = nullptr);
 
 }  // namespace bepugpu

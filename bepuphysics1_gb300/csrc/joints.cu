@@ -74,6 +74,22 @@ uint32_t ChildrenOf(int32_t type) {
 
 float4 F4(const float* v, float w) { return make_float4(v[0], v[1], v[2], w); }
 
+// The children a group record may be continued with (BEPUGPU_JOINT_GROUP_CONTINUATION).
+bool ContinuationAllowed(int32_t group, int32_t child) {
+    switch (group) {
+        case BEPUGPU_JOINT_REVOLUTE: return child == BEPUGPU_JOINT_REVOLUTE_MOTOR;
+        case BEPUGPU_JOINT_PRISMATIC:
+        case BEPUGPU_JOINT_LINE_SLIDER: return child == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR;
+        case BEPUGPU_JOINT_UNIVERSAL: return child == BEPUGPU_JOINT_TWIST_LIMIT || child == BEPUGPU_JOINT_TWIST_MOTOR;
+        case BEPUGPU_JOINT_SWIVEL_HINGE:
+            return child == BEPUGPU_JOINT_REVOLUTE_LIMIT || child == BEPUGPU_JOINT_REVOLUTE_MOTOR ||
+                   child == BEPUGPU_JOINT_TWIST_LIMIT || child == BEPUGPU_JOINT_TWIST_MOTOR;
+        case BEPUGPU_JOINT_PLANE_SLIDER:
+            return child == BEPUGPU_JOINT_LINEAR_AXIS_LIMIT || child == BEPUGPU_JOINT_LINEAR_AXIS_MOTOR;
+        default: return false;
+    }
+}
+
 }  // namespace
 
 bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint32_t nj, int32_t bodies) {
@@ -111,6 +127,27 @@ bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint
             ctx->SetError("joint %u: lengths need 0 <= minimum <= maximum", u);
             return BEPUGPU_INVALID_ARGUMENT;
         }
+        if (r.flags & BEPUGPU_JOINT_GROUP_CONTINUATION) {
+            uint32_t g = u, children = 0;
+            while (g > 0 && (joints[g].flags & BEPUGPU_JOINT_GROUP_CONTINUATION)) {
+                g--;
+                children++;
+            }
+            const bepugpu_joint& head = joints[g];
+            if (head.flags & BEPUGPU_JOINT_GROUP_CONTINUATION || !ContinuationAllowed(head.type, r.type)) {
+                ctx->SetError("joint %u: a GROUP_CONTINUATION record of type %d does not follow a group that takes it",
+                              u, r.type);
+                return BEPUGPU_INVALID_ARGUMENT;
+            }
+            if (children > 4) {
+                ctx->SetError("joint %u: a group takes at most four continuation records", u);
+                return BEPUGPU_INVALID_ARGUMENT;
+            }
+            if (r.body_a != head.body_a || r.body_b != head.body_b) {
+                ctx->SetError("joint %u: a GROUP_CONTINUATION record connects its group's bodies", u);
+                return BEPUGPU_INVALID_ARGUMENT;
+            }
+        }
     }
     return BEPUGPU_OK;
 }
@@ -136,8 +173,23 @@ bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints,
         const bool groupLimit = r.type == BEPUGPU_JOINT_REVOLUTE || r.type == BEPUGPU_JOINT_PRISMATIC ||
                                 r.type == BEPUGPU_JOINT_LINE_SLIDER;
         if (groupLimit && !(r.flags & BEPUGPU_JOINT_LIMIT_ACTIVE)) childIsActive &= ~kJChildLimit;
+        // a continuation is active when it and its group are; the group's
+        // visit solves it right after the slot before it (same colour, next slot)
+        const bool continuation = (r.flags & BEPUGPU_JOINT_GROUP_CONTINUATION) != 0;
+        bool isActive = (r.flags & BEPUGPU_JOINT_ACTIVE) != 0;
+        if (continuation) {
+            uint32_t g = u;
+            while (g > 0 && (joints[g].flags & BEPUGPU_JOINT_GROUP_CONTINUATION)) g--;
+            isActive = isActive && (joints[g].flags & BEPUGPU_JOINT_ACTIVE);
+        }
+        const bool hasNext = u + 1 < nj && (joints[u + 1].flags & BEPUGPU_JOINT_GROUP_CONTINUATION);
+        if (hasNext && s->hostJointSlotOf[u + 1] != slot + 1) {
+            ctx->SetError("joint %u: its continuation record did not get the next slot", u);
+            return BEPUGPU_INVALID_OPERATION;
+        }
         uint32_t z = (uint32_t)r.type | (present << kJPresentShift) | (childIsActive << kJChildActiveShift) |
-                     ((r.flags & BEPUGPU_JOINT_ACTIVE) ? kJGroupIsActive : 0u);
+                     (isActive ? kJGroupIsActive : 0u) | (continuation ? kJHeadContinuation : 0u) |
+                     (hasNext ? kJHeadHasNext : 0u);
         head[slot] = make_int4(r.body_a, r.body_b, (int)z, (int)u);
         // Joint.MaxCorrectiveVelocity setter (Joint.cs:23-36)
         float maxCorr = std::max(0.f, r.max_corrective_velocity);

@@ -85,7 +85,8 @@ enum JointLane : int {
 constexpr int kJointSmemBytes = 16 * kJSolveLanes + 8 + 8;
 
 // head.z: type (bits 0-7), children present (8-10), children IsActive (11-13),
-// joint / group IsActive (14).
+// joint / group IsActive (14), the record continues the group before it (15),
+// the next slot continues this one's group (16).
 enum : uint32_t {
     kJChildBall = 1u,
     kJChildAngular = 2u,
@@ -93,16 +94,21 @@ enum : uint32_t {
     kJPresentShift = 8,
     kJChildActiveShift = 11,
     kJGroupIsActive = 1u << 14,
+    kJHeadContinuation = 1u << 15,
+    kJHeadHasNext = 1u << 16,
 };
 // State word x: kGroupActive (bit 0), child isActiveInSolver bits 1-3,
 // limit minIsActive / maxIsActive bits 4-5 (a linear axis limit: bit 4 =
 // violated below its minimum), kDynA / kDynB (bits 7-8), the record type
-// (bits 9-13), iterations << 16.  Word y: 4-bit zero-impulse
-// streaks of the three children.
+// (bits 9-13), continuation (14) and has-next (15) as in the head,
+// iterations << 16.  Word y: 4-bit zero-impulse streaks of the three
+// children.
 enum : uint32_t {
     kJMinActive = 1u << 4,
     kJMaxActive = 1u << 5,
     kJTypeShift = 9,
+    kJIsContinuation = 1u << 14,
+    kJHasNext = 1u << 15,
 };
 __device__ __forceinline__ int JointType(uint32_t stx) { return (int)((stx >> kJTypeShift) & 31u); }
 __device__ __forceinline__ bool IsDistanceType(int type) {
@@ -414,7 +420,8 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
     LoadJointBodyV(bv, rb, B);
     float4 acc0 = ji.L(kJACC0, si), acc1 = ji.L(kJACC1, si);
     j.L(kJACC0, s) = acc0;
-    uint32_t st = (A.dynamic ? kDynA : 0u) | (B.dynamic ? kDynB : 0u) | ((uint32_t)type << kJTypeShift);
+    uint32_t st = (A.dynamic ? kDynA : 0u) | (B.dynamic ? kDynB : 0u) | ((uint32_t)type << kJTypeShift) |
+                  ((h.z & kJHeadContinuation) ? kJIsContinuation : 0u) | ((h.z & kJHeadHasNext) ? kJHasNext : 0u);
     if (!(h.z & kJGroupIsActive) || !(A.dynamic || B.dynamic)) {
         j.L(kJACC1, s) = acc1;
         j.state[s] = make_uint2(st, 0u);
@@ -1332,7 +1339,11 @@ __device__ __forceinline__ void PrestepJointIO(const JointSoA& ji, int si, const
         if (on) st |= 1u << (kChildShift + 2);
     }
     j.L(kJACC1, s) = acc1;
-    if (st & (7u << kChildShift)) st |= kGroupActive;
+    // A continuation's visits belong to its group's record: its own slot never
+    // carries kGroupActive, so the sweeps pass over it.  The group's first child
+    // is active whenever the group is (the constructors' IsActive = true), so the
+    // group record's kGroupActive already stands for the whole group here.
+    if ((st & (7u << kChildShift)) && !(st & kJIsContinuation)) st |= kGroupActive;
     j.state[s] = make_uint2(st, 0u);
 }
 
@@ -1343,10 +1354,10 @@ __device__ __forceinline__ void PrestepJoint(const JointSoA& j, const BodySoA& b
 }
 
 // ---------------------------------------------------------- warm start --
-// ExclusiveUpdate of every active child in order.
+// ExclusiveUpdate of every active child of one record in order.
 template <bool kAdded>
-__device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint32_t st,
-                                          int type) {
+__device__ __forceinline__ void WarmJointChildren(const JointSoA& j, int s, BodyState& A, BodyState& B, uint32_t st,
+                                                  int type) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
     const float4 acc0 = j.L(kJACC0, s), acc1 = j.L(kJACC1, s);
     if (kAdded && (st & (1u << kChildShift)) && IsPointOnLineType(type)) {
@@ -1491,21 +1502,32 @@ __device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A
     }
 }
 
-// -------------------------------------------------------------- solve --
-// Solver.UnsafeSolveIteration (Solver.cs:285-314) on the joint, then
-// SolverGroup.SolveUpdateable (SolverGroup.cs:117-150) on each child.
+// SolverGroup.ExclusiveUpdate (SolverGroup.cs:103-109) over the group's
+// children in Add order: the record's own, then those of its continuation
+// records in the slots after it.
 template <bool kAdded>
-__device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint2& state,
-                                           int type, const StepParams& p) {
-    uint32_t st = state.x, zeros = state.y;
-    uint32_t iter = (st >> kIterShift) + 1;
-    st = (st & 0xffffu) | (iter << kIterShift);
-    if (!((int)iter <= p.iterationLimit && (int)iter <= p.maximumIterationCount)) {
-        state = make_uint2(st & ~kGroupActive, zeros);
-        return;
-    }
+__device__ __forceinline__ void WarmJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint32_t st,
+                                          int type) {
+    WarmJointChildren<kAdded>(j, s, A, B, st, type);
+    if (kAdded && (st & kJHasNext))
+        for (int u = s + 1;; u++) {
+            const uint32_t cst = j.state[u].x;
+            WarmJointChildren<kAdded>(j, u, A, B, cst, JointType(cst));
+            if (!(cst & kJHasNext)) break;
+        }
+}
+
+// -------------------------------------------------------------- solve --
+// SolverGroup.SolveUpdateable (SolverGroup.cs:117-150) on each active child of
+// one record: st / zeros are the record's state words, activeConstraints the
+// group's count.  A child's currentIterations equals the group's while the
+// child stays active (both restart at the Update, SolverGroup.cs:70-76), so
+// the group's iteration check covers the child's.
+template <bool kAdded>
+__device__ __forceinline__ void SolveJointChildren(const JointSoA& j, int s, BodyState& A, BodyState& B,
+                                                   uint32_t& st, uint32_t& zeros, int& activeConstraints, int type,
+                                                   const StepParams& p) {
     const bool dynA = st & kDynA, dynB = st & kDynB;
-    int activeConstraints = 0;
     auto account = [&](int c, float r) {
         uint32_t z = (zeros >> (4 * c)) & 0xfu;
         if (r < p.minimumImpulse) {
@@ -1937,9 +1959,33 @@ __device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& 
             account(2, lambdaTotal);
         }
     }
-    if (activeConstraints <= 0) st &= ~kGroupActive;
     j.L(kJACC0, s) = acc0;
     j.L(kJACC1, s) = acc1;
+}
+
+// Solver.UnsafeSolveIteration (Solver.cs:285-314) on the joint or group, then
+// SolverGroup.SolveIteration (SolverGroup.cs:156-165): the record's children,
+// then its continuation records' in the slots after it.
+template <bool kAdded>
+__device__ __forceinline__ void SolveJoint(const JointSoA& j, int s, BodyState& A, BodyState& B, uint2& state,
+                                           int type, const StepParams& p) {
+    uint32_t st = state.x, zeros = state.y;
+    uint32_t iter = (st >> kIterShift) + 1;
+    st = (st & 0xffffu) | (iter << kIterShift);
+    if (!((int)iter <= p.iterationLimit && (int)iter <= p.maximumIterationCount)) {
+        state = make_uint2(st & ~kGroupActive, zeros);
+        return;
+    }
+    int activeConstraints = 0;
+    SolveJointChildren<kAdded>(j, s, A, B, st, zeros, activeConstraints, type, p);
+    if (kAdded && (st & kJHasNext))
+        for (int u = s + 1;; u++) {
+            uint2 cs = j.state[u];
+            SolveJointChildren<kAdded>(j, u, A, B, cs.x, cs.y, activeConstraints, JointType(cs.x), p);
+            j.state[u] = cs;
+            if (!(cs.x & kJHasNext)) break;
+        }
+    if (activeConstraints <= 0) st &= ~kGroupActive;
     state = make_uint2(st, zeros);
 }
 

@@ -124,7 +124,7 @@ JOINT_SWIVEL_HINGE_ANGULAR, JOINT_SWIVEL_HINGE = 19, 20
 JOINT_REVOLUTE_MOTOR, JOINT_TWIST_MOTOR, JOINT_LINEAR_AXIS_MOTOR = 21, 22, 23
 JOINT_MAXIMUM_LINEAR_SPEED, JOINT_MAXIMUM_ANGULAR_SPEED, JOINT_PLANE_SLIDER = 24, 25, 26
 JOINT_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_LINEAR_MOTOR = 27, 28, 29
-JOINT_ACTIVE, JOINT_LIMIT_ACTIVE, JOINT_SERVO = 1, 2, 4
+JOINT_ACTIVE, JOINT_LIMIT_ACTIVE, JOINT_SERVO, JOINT_GROUP_CONTINUATION = 1, 2, 4, 8
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int32

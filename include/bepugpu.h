@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 7
+#define BEPUGPU_ABI_VERSION 8
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -201,17 +201,35 @@ typedef enum bepugpu_joint_type {
     BEPUGPU_JOINT_SINGLE_ENTITY_ANGULAR_MOTOR = 28, /* SingleEntityAngularMotor.cs:117-226: body_b -1, ANGULAR_MOTOR's fields */
     BEPUGPU_JOINT_SINGLE_ENTITY_LINEAR_MOTOR = 29 /* SingleEntityLinearMotor.cs:180-276: body_b -1 */
 } bepugpu_joint_type;
-/* The groups' motor children are inactive, as their constructors leave them
- * (PrismaticJoint.cs:56, LineSliderJoint.cs:54, UniversalJoint.cs:53), and so
- * are UniversalJoint's twist limit (:52), SwivelHingeJoint's hinge and twist
- * limits (SwivelHingeJoint.cs:59-62) and PlaneSliderJoint's two limits
- * (PlaneSliderJoint.cs:60-63).  The limits of REVOLUTE, PRISMATIC and
- * LINE_SLIDER records (a LinearAxisLimit on the line's anchors and direction
- * for the last two) follow BEPUGPU_JOINT_LIMIT_ACTIVE. */
+/* A group record holds the group's first children: REVOLUTE its ball socket,
+ * angular joint and limit; PRISMATIC and LINE_SLIDER their point on line,
+ * angular joint and limit; UNIVERSAL its ball socket and twist joint;
+ * SWIVEL_HINGE its ball socket and swivel hinge angular joint; PLANE_SLIDER
+ * its point on plane joint.  The limits of REVOLUTE, PRISMATIC and LINE_SLIDER
+ * records (a LinearAxisLimit on the line's anchors and direction for the last
+ * two) follow BEPUGPU_JOINT_LIMIT_ACTIVE.  The group's other children -- its
+ * motors, UniversalJoint's twist limit, SwivelHingeJoint's hinge and twist
+ * limits, PlaneSliderJoint's two limits -- are records of their own type
+ * (REVOLUTE_MOTOR, TWIST_MOTOR, LINEAR_AXIS_MOTOR, TWIST_LIMIT, REVOLUTE_LIMIT,
+ * LINEAR_AXIS_LIMIT) flagged BEPUGPU_JOINT_GROUP_CONTINUATION, right after the
+ * group record (and its earlier continuations) in the joint list, with the
+ * group's two bodies, in the order the group adds its children
+ * (RevoluteJoint.cs:88-91, UniversalJoint.cs:54-57, PrismaticJoint.cs:57-60,
+ * LineSliderJoint.cs:55-58, SwivelHingeJoint.cs:96-101,
+ * PlaneSliderJoint.cs:64-68).  A child the group leaves inactive (as the
+ * constructors leave the motors and these limits) is simply not listed: an
+ * inactive child takes no part in the group's steps.  A continuation is solved
+ * inside its group's visit, after the group's earlier children, and counts
+ * toward the group's activity; it is active when both its own ACTIVE flag and
+ * the group's are set.  Allowed: REVOLUTE: REVOLUTE_MOTOR; PRISMATIC and
+ * LINE_SLIDER: LINEAR_AXIS_MOTOR; UNIVERSAL: TWIST_LIMIT, TWIST_MOTOR;
+ * SWIVEL_HINGE: REVOLUTE_LIMIT, REVOLUTE_MOTOR, TWIST_LIMIT, TWIST_MOTOR;
+ * PLANE_SLIDER: LINEAR_AXIS_LIMIT, LINEAR_AXIS_MOTOR; at most four a group. */
 
 #define BEPUGPU_JOINT_ACTIVE        1u  /* SolverUpdateable.IsActive of the joint (or group) */
 #define BEPUGPU_JOINT_LIMIT_ACTIVE  2u  /* REVOLUTE, PRISMATIC, LINE_SLIDER: the group's Limit.IsActive */
 #define BEPUGPU_JOINT_SERVO         4u  /* motors: MotorMode.Servomechanism (else VelocityMotor) */
+#define BEPUGPU_JOINT_GROUP_CONTINUATION 8u /* a further child of the group record before it (see above) */
 
 /* Joint record: the state each reference object keeps between steps.  Body -1
  * is TwoEntityConstraint.WorldEntity (TwoEntityConstraint.cs:17): a kinematic

@@ -1401,7 +1401,16 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
     sp.world.orientationMatrix = CreateFromQuaternion(sp.world.orientation);
     auto ent = [&](int idx) -> Entity* { return idx >= 0 && idx < nb ? &sp.entities[idx] : nullptr; };
     for (int j = 0; j < nj; j++) {
-        SolverUpdateable* u = CreateJoint(sp, joints[j], ent(joints[j].body_a), ent(joints[j].body_b));
+        SolverUpdateable* u;
+        if (joints[j].flags & BEPUGPU_JOINT_GROUP_CONTINUATION) {
+            int h = j;
+            while (h > 0 && (joints[h].flags & BEPUGPU_JOINT_GROUP_CONTINUATION)) h--;
+            u = h < j ? CreateContinuation(sp, joints[j], ent(joints[j].body_a), ent(joints[j].body_b),
+                                           sp.updateables[h].get())
+                      : nullptr;
+        } else {
+            u = CreateJoint(sp, joints[j], ent(joints[j].body_a), ent(joints[j].body_b));
+        }
         if (!u) { delete o; return nullptr; }
         sp.updateables.emplace_back(u);
     }
@@ -1588,13 +1597,19 @@ int64_t oracle_permutation_map(int64_t permutation_index, int64_t index, int32_t
 int32_t oracle_prime_count(void) { return kPrimeCount; }
 
 // Restatement of the library's colouring (deterministic greedy in list order,
-// conflicts only through dynamic bodies; colour-sorted order is stable).
+// conflicts only through dynamic bodies; colour-sorted order is stable).  A
+// GROUP_CONTINUATION record is solved inside its group's visit: it takes the
+// colour of the record before it and claims nothing.
 int32_t oracle_colour(const bepugpu_body* bodies, int32_t nb, const bepugpu_manifold* manifolds, int32_t nm,
                       const bepugpu_joint* joints, int32_t nj, int32_t* colour_out, int32_t* order_out) {
     int n = nj + nm;
     std::vector<std::vector<int>> used(nb);  // colours taken at each dynamic body
     int colours = 0;
     for (int u = 0; u < n; u++) {
+        if (u > 0 && u < nj && (joints[u].flags & BEPUGPU_JOINT_GROUP_CONTINUATION)) {
+            colour_out[u] = colour_out[u - 1];
+            continue;
+        }
         int a = u < nj ? joints[u].body_a : manifolds[u - nj].body_a;
         int b = u < nj ? joints[u].body_b : manifolds[u - nj].body_b;
         int ends[2] = {a, b};
