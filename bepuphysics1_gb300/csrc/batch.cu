@@ -151,7 +151,7 @@ SceneView MakeView(const Scene& s) {
 }
 
 bool Scene::BatchReady(uint32_t flags) const {
-    return SweepEmpty() && jointCount == 0 && generatedCount == 0 && !kin.Needed(flags);
+    return SweepEmpty() && jointCount == 0 && generatedCount == 0 && !kin.Needed(flags) && !islands;
 }
 
 }  // namespace bepugpu

@@ -676,6 +676,7 @@ Scene::~Scene() {
     for (auto e : evGroup)
         if (e) cudaEventDestroy(e);
     ReleaseBroadPhase(this);
+    ReleaseIslands(this);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -800,6 +801,7 @@ void Scene::Rebase() {
     b.vang = (float4*)(base + L.vang); b.inv0 = (float4*)(base + L.inv0); b.inv1 = (float4*)(base + L.inv1);
     b.loc0 = (float4*)(base + L.loc0); b.loc1 = (float4*)(base + L.loc1); b.damp = (float4*)(base + L.damp);
     b.act = (float4*)(base + L.act); b.rawDamp = (float2*)(base + L.rawDamp);
+    ApplyIslandViews(this);
     localM33 = (float*)(base + L.m33);
     m.head = (int4*)(base + L.head); m.cpos = (float4*)(base + L.cpos); m.cnrm = (float4*)(base + L.cnrm);
     m.offA = (float4*)(base + L.offA); m.offB = (float4*)(base + L.offB); m.mat = (float4*)(base + L.mat);
@@ -938,7 +940,21 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     if (graphExec) { cudaGraphExecDestroy(graphExec); graphExec = nullptr; }
     const int T = 128;
     launchesPerStep = 0;
+    const uint32_t requested = flags;
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    // DeactivationManager.Update before everything else (Space.cs:502): the
+    // narrow phase, the refresher and the body stages read the islands' state.
+    if (islands && (flags & BEPUGPU_STEP_DEACTIVATION)) {
+        cudaError_t ie = LaunchIslandStage(this, p, ctx->settings.maximum_deactivation_attempts_per_frame, stream);
+        if (ie != cudaSuccess) {
+            cudaGraph_t dropped;
+            cudaStreamEndCapture(stream, &dropped);
+            if (dropped) cudaGraphDestroy(dropped);
+            ctx->SetError("island stage launch: %s", cudaGetErrorString(ie));
+            return BEPUGPU_CUDA_ERROR;
+        }
+    }
+    flags = StageFlags(flags);
     // The narrow phase first: it rewrites the GENERATED manifolds' contacts
     // from the poses the rest of the step starts from.
     if ((flags & BEPUGPU_STEP_COLLIDE) && generatedCount) {
@@ -997,7 +1013,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
             return BEPUGPU_CUDA_ERROR;
         }
         graphDt = p.dt;
-        graphFlags = flags;
+        graphFlags = requested;
         graphVersion = version;
         graphIterations = p.iterationLimit;
         return BEPUGPU_OK;
@@ -1086,7 +1102,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
         return BEPUGPU_CUDA_ERROR;
     }
     graphDt = p.dt;
-    graphFlags = flags;
+    graphFlags = requested;
     graphVersion = version;
     graphIterations = p.iterationLimit;
     return BEPUGPU_OK;
@@ -1106,6 +1122,9 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
         persistentAdded = addedJointTypes;
     }
     launchesPerStep = 0;
+    if (islands && (flags & BEPUGPU_STEP_DEACTIVATION))
+        CK(LaunchIslandStage(this, p, ctx->settings.maximum_deactivation_attempts_per_frame, stream));
+    flags = StageFlags(flags);
     if ((flags & BEPUGPU_STEP_COLLIDE) && generatedCount) {
         CK(LaunchCollide(this, p, stream));
         launchesPerStep++;
@@ -1162,7 +1181,7 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
         st = RunPersistent(ctx, p, flags);
         if (st != BEPUGPU_OK) return st;
     } else {
-        const bool tail = SweepEmpty() && kin.Needed(flags) && sweepBodyCount;
+        const bool tail = SweepEmpty() && kin.Needed(StageFlags(flags)) && sweepBodyCount;
         if (!graphExec || graphDt != dt || graphFlags != flags || graphVersion != version ||
             graphIterations != p.iterationLimit || graphTail != tail) {
             st = BuildGraph(ctx, p, flags);
@@ -1265,6 +1284,7 @@ void bepugpu_default_settings(bepugpu_settings* s) {
     s->use_stabilization = 1;
     s->velocity_lower_limit = .26f;
     s->low_velocity_time_minimum = 1.f;
+    s->maximum_deactivation_attempts_per_frame = 100;
 }
 
 static bepugpu_status ValidateSettings(Context* ctx, const bepugpu_settings* s) {
@@ -1284,6 +1304,10 @@ static bepugpu_status ValidateSettings(Context* ctx, const bepugpu_settings* s) 
     }
     if (!(s->low_velocity_time_minimum > 0)) {
         ctx->SetError("low_velocity_time_minimum must be positive");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->maximum_deactivation_attempts_per_frame < 0) {
+        ctx->SetError("maximum_deactivation_attempts_per_frame must be >= 0");
         return BEPUGPU_INVALID_ARGUMENT;
     }
     return BEPUGPU_OK;
@@ -1397,6 +1421,12 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         ctx->SetError("body count %u exceeds scene capacity %u", n, s->maxBodies);
         return BEPUGPU_INVALID_ARGUMENT;
     }
+    if (s->islands) {  // the islands are set again for the new bodies
+        if (s->asyncPending) CK(cudaStreamSynchronize(s->stream));
+        s->asyncPending = false;
+        ReleaseIslands(s);
+        s->version++;
+    }
     s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);
     bool dynamicChanged = s->hostDynamic.size() != n;
     s->hostDynamic.resize(n);
@@ -1464,6 +1494,11 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     if (nm > s->maxManifolds || nj > s->maxJoints || (nm && !man) || (nj && !joints)) {
         ctx->SetError("constraint counts exceed scene capacity");
         return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->islands) {  // the islands are set again for the new connections
+        if (s->asyncPending) CK(cudaStreamSynchronize(s->stream));
+        s->asyncPending = false;
+        ReleaseIslands(s);
     }
     int nb = s->b.count;
     if (nj) {
@@ -2071,6 +2106,12 @@ bepugpu_status bepugpu_profile_step(bepugpu_context* c, int32_t id, float dt, ui
     std::vector<Span> spans;
     unsigned long long* acc = s->Census();
     CK(cudaMemsetAsync(acc, 0, 8 * sizeof(unsigned long long), q));
+    if (s->islands && (flags & BEPUGPU_STEP_DEACTIVATION)) {  // the island stage first, timed with the forces
+        cudaEvent_t a = mark();
+        CK(LaunchIslandStage(s, p, ctx->settings.maximum_deactivation_attempts_per_frame, q));
+        spans.push_back({a, mark(), &out->force_ms});
+    }
+    flags = s->StageFlags(flags);
     if (!s->groupPlan.groups.empty()) {  // the census variant of the group kernel counts its visits
         cudaEvent_t a = mark();
         bepugpu_status gs = LaunchGroups(ctx, s, p, flags, true);

@@ -25,6 +25,11 @@ struct BatchEngine;
 struct Scene;
 struct BroadPhaseBuffers;
 void ReleaseBroadPhase(Scene* s);  // broadphase.cu
+struct IslandBuffers;               // islands.cu
+struct StepParams;
+void ReleaseIslands(Scene* s);
+void ApplyIslandViews(Scene* s);    // the body view's island pointers after a rebase
+cudaError_t LaunchIslandStage(Scene* s, const StepParams& p, int maxAttempts, cudaStream_t q);
 
 // Device memory of a context's scene arenas and staging buffers, carved from
 // large cudaMalloc slabs (heap.cu).  Thread-safe: a server's worker spills and
@@ -339,6 +344,12 @@ struct Scene {
     int persistentBlocks = 0;
     bool persistentAdded = false;  // the persistent variant persistentBlocks was sized for
     BroadPhaseBuffers* broadPhase = nullptr;  // device buffers of bepugpu_broad_phase (broadphase.cu)
+    IslandBuffers* islands = nullptr;         // bepugpu_set_islands (islands.cu); null: every island awake
+    // With islands the deactivation stage runs first, in its own launches
+    // (LaunchIslandStage); the other stages then run without it.
+    uint32_t StageFlags(uint32_t flags) const {
+        return islands ? flags & ~(uint32_t)BEPUGPU_STEP_DEACTIVATION : flags;
+    }
 
     ~Scene();
     bepugpu_status Allocate(Context* ctx, uint32_t nb, uint32_t nm, uint32_t nj);

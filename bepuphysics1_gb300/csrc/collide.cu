@@ -24,7 +24,12 @@ namespace bepugpu {
 __global__ void __launch_bounds__(64) k_collide(ManifoldSoA m, BodySoA b, const float4* __restrict__ shape,
                                                  const int32_t* __restrict__ slots, int n, StepParams p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) nphase::CollideManifold(m, b, shape, slots[i], p);
+    if (i >= n) return;
+    if (b.islandOf) {  // with islands, a pair between two inactive entries keeps its contacts (NarrowPhase.cs:300-332)
+        const int4 h = m.head[slots[i]];
+        if (!EntryActive(b, h.x) && !EntryActive(b, h.y)) return;
+    }
+    nphase::CollideManifold(m, b, shape, slots[i], p);
 }
 
 cudaError_t LaunchCollide(Scene* s, const StepParams& p, cudaStream_t stream) {

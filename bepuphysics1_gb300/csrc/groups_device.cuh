@@ -115,34 +115,50 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
 
     // Bodies into shared memory, through the candidacy update
     // (SimulationIslandMember.cs:53-164) and the force update (EntityBase.cs:911-975).
+    // With islands (the candidacy update ran before this launch) a body of a
+    // sleeping island skips the force update and reads as not dynamic for the
+    // rest of the step: pos.w = 0 in shared memory.
+    int asleepAll = b.islandOf != nullptr;
     for (int i = tid; i < nLocal; i += T) {
         int gi = t.bodies[g.bBegin + i];
         float4 v = b.vlin[gi], w = b.vang[gi], q = b.quat[gi], a, c;
         float4 act = make_float4(0.f, 0.f, 0.f, 0.f);
+        const bool asleep = IslandAsleep(b, gi);
+        asleepAll &= asleep ? 1 : 0;
         if (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_FORCES)) act = b.act[gi];
         if (flags & BEPUGPU_STEP_DEACTIVATION) {
             CandidacyMath(v, w, true, act, p);  // a group's bodies are dynamic
             b.act[gi] = act;
         }
-        if (flags & BEPUGPU_STEP_FORCES) {
+        if ((flags & BEPUGPU_STEP_FORCES) && !asleep) {
             ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], act, b.rawDamp + gi, a, c, p);
         } else {
             a = b.inv0[gi];
             c = b.inv1[gi];
         }
-        bv.pos[i] = b.pos[gi];
+        float4 pos = b.pos[gi];
+        if (asleep) pos.w = 0.f;
+        bv.pos[i] = pos;
         bv.quat[i] = q;
         bv.vlin[i] = v;
         bv.vang[i] = w;
         bv.inv0[i] = a;
         bv.inv1[i] = c;
     }
-    __syncthreads();
+    // A group whose islands all sleep has nothing to do: no active constraint,
+    // no manifold with an active entry (an active kinematic body touching one
+    // of its islands would have woken it), no body to move.
+    if (__syncthreads_and(asleepAll)) return;
     // Refresh, lanes in, prestep: a thread keeps the same manifolds throughout.
     for (int j = tid; j < nm; j += T) {
         const int s = g.mBegin + j;
         int2 r = t.refs[s];
-        if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifoldV(m, bv, s, r.x, r.y, p);
+        // with islands, a pair between two inactive entries is not refreshed (NarrowPhase.cs:300-332)
+        auto entryActive = [&](int ref) {
+            return ref >= 0 ? bv.pos[ref].w != 0.f : (ref <= -2 && b.act[-2 - ref].y <= 0.f);
+        };
+        if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && (!b.islandOf || entryActive(r.x) || entryActive(r.y)))
+            RefreshManifoldV(m, bv, s, r.x, r.y, p);
         if (kShared) {
             ml.penacc[j] = m.penacc[s];  // after the refresh, which may compact them
             ml.fricacc[j] = m.fricacc[s];
@@ -252,10 +268,12 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
             }
         }
     }
-    // Position update (EntityBase.cs:1124-1160) and write-back.
+    // Position update (EntityBase.cs:1124-1160) and write-back; a sleeping
+    // body (pos.w = 0 here) is left as it was.
     for (int i = tid; i < nLocal; i += T) {
         int gi = t.bodies[g.bBegin + i];
         float4 pos = bv.pos[i], q = bv.quat[i], v = bv.vlin[i], w = bv.vang[i];
+        if (pos.w == 0.f) continue;
         if (flags & BEPUGPU_STEP_POSITIONS) {  // a group's bodies are dynamic, so active
             PositionMath(pos, q, v, w, p);
             b.pos[gi] = pos;

@@ -78,6 +78,8 @@ __device__ Views Carve(unsigned char* s, int nb, int nm) {
     v.b.pos = body[0]; v.b.quat = body[1]; v.b.vlin = body[2]; v.b.vang = body[3]; v.b.inv0 = body[4];
     v.b.inv1 = body[5]; v.b.loc0 = body[6]; v.b.loc1 = body[7]; v.b.damp = body[8]; v.b.act = body[9];
     v.b.rawDamp = (float2*)body[10];
+    v.b.islandOf = nullptr;  // every island awake
+    v.b.islandFlags = nullptr;
     v.b.count = nb;
     float4* l4[7];
     for (int k = 0; k < 7; k++) l4[k] = (float4*)(s + kLane4At + k * kLane4Array);

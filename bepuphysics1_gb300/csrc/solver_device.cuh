@@ -52,8 +52,20 @@ struct BodySoA {
     float4* damp;  // linear damping factor, angular damping factor, local M33, flags
     float4* act;   // activity: previousVelocity, velocityTimeBelowLimit, BEPUGPU_BODY_* bits, 0
     float2* rawDamp;  // LinearDamping, AngularDamping (read when the stabilization boost applies)
+    // Simulation islands (islands.cu; null without them): each body's island
+    // (-1 kinematic) and the islands' BEPUGPU_ISLAND_* flags.
+    const int32_t* islandOf;
+    const uint32_t* islandFlags;
     int count;
 };
+
+// A dynamic body whose island sleeps (SimulationIslandMember.IsActive,
+// SimulationIslandMember.cs:225-248, is its island's state).
+__device__ __forceinline__ bool IslandAsleep(const BodySoA& b, int i) {
+    if (!b.islandOf) return false;
+    const int k = b.islandOf[i];
+    return k >= 0 && !(b.islandFlags[k] & 1u);
+}
 
 // Activity bits in act.z, the ABI's BEPUGPU_BODY_* values.
 enum : uint32_t {
@@ -125,7 +137,14 @@ struct BodyState {
 // routines are templated on the view, so both paths run the same arithmetic.
 struct GlobalBodies {
     BodySoA b;
-    __device__ __forceinline__ float4 Pos(int r) const { return b.pos[r]; }
+    // A sleeping body reads as not dynamic: nothing of the step may move it, and
+    // a constraint with no active dynamic body is not active in the solver
+    // (SolverUpdateable.cs:202-219, ContactManifoldConstraint.cs:125-141).
+    __device__ __forceinline__ float4 Pos(int r) const {
+        float4 p = b.pos[r];
+        if (b.islandOf && p.w != 0.f && IslandAsleep(b, r)) p.w = 0.f;
+        return p;
+    }
     __device__ __forceinline__ float4 Quat(int r) const { return b.quat[r]; }
     __device__ __forceinline__ float4 Vlin(int r) const { return b.vlin[r]; }
     __device__ __forceinline__ float4 Vang(int r) const { return b.vang[r]; }
@@ -174,13 +193,14 @@ __device__ __forceinline__ void ApplyAngular(BodyState& s, float x, float y, flo
 // is rewritten.  The island bookkeeping of the reference (path compression,
 // waking islands next to an active kinematic body) has nothing to do when
 // every island is awake.
-__device__ __forceinline__ void CandidacyMath(float4 v, float4 w, bool dynamic, float4& act, const StepParams& p) {
+__device__ __forceinline__ void CandidacyMath(float4 v, float4 w, bool dynamic, float4& act, const StepParams& p,
+                                              bool islandActive = true) {
     uint32_t f = __float_as_uint(act.z);
     // velocity = linearVelocity.LengthSquared() + angularVelocity.LengthSquared() (Vector3.cs:64-67)
     float velocity = (v.x * v.x + v.y * v.y + v.z * v.z) + (w.x * w.x + w.y * w.y + w.z * w.z);
     float t = act.y;
     // IsActive (:225-248): the island's state for a dynamic body, the time flag for a kinematic one
-    const bool isActive = dynamic || t <= 0.f;
+    const bool isActive = dynamic ? islandActive : t <= 0.f;
     if (isActive) {
         const bool slowing = velocity <= act.x;
         f = slowing ? (f | kSlowing) : (f & ~kSlowing);
@@ -304,7 +324,7 @@ __device__ __forceinline__ void StartBodyStep(const BodySoA& b, int i, const Ste
         CandidacyMath(b.vlin[i], b.vang[i], dynamic, act, p);
         b.act[i] = act;
     }
-    if (!dynamic || !(stages & BEPUGPU_STEP_FORCES)) return;
+    if (!dynamic || !(stages & BEPUGPU_STEP_FORCES) || IslandAsleep(b, i)) return;  // ForceUpdater.cs:73-76
     float4 v = b.vlin[i], w = b.vang[i], q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i], d = b.damp[i];
     float4 a, c;
     ForceMath(v, w, q, l0, l1, d, act, b.rawDamp + i, a, c, p);
@@ -338,7 +358,7 @@ __device__ __forceinline__ void PositionMath(float4& pos, float4& q, float4 v, f
 }
 __device__ __forceinline__ void PositionUpdateBody(const BodySoA& b, int i, const StepParams& p) {
     float4 pos = b.pos[i], q = b.quat[i];
-    if (!BodyActive(pos, b.act[i])) return;
+    if (!BodyActive(pos, b.act[i]) || IslandAsleep(b, i)) return;
     PositionMath(pos, q, b.vlin[i], b.vang[i], p);
     b.quat[i] = q;
     b.pos[i] = pos;
@@ -464,8 +484,18 @@ __device__ __forceinline__ void RefreshManifoldV(const ManifoldSoA& m, const V& 
         }
     }
 }
+// An entry of the narrow phase is active (NarrowPhase.cs:300-332 updates a
+// pair while one of its entries is): a dynamic body while its island is
+// awake, a kinematic one while its time flag is <= 0; no entity is a static
+// entry, inactive.  Only asked with islands.
+__device__ __forceinline__ bool EntryActive(const BodySoA& b, int r) {
+    if (r < 0) return false;
+    if (b.pos[r].w != 0.f) return !IslandAsleep(b, r);
+    return b.act[r].y <= 0.f;
+}
 __device__ __forceinline__ void RefreshManifold(const ManifoldSoA& m, const BodySoA& b, int s, const StepParams& p) {
     int4 h = m.head[s];
+    if (b.islandOf && !EntryActive(b, h.x) && !EntryActive(b, h.y)) return;
     RefreshManifoldV(m, GlobalBodies{b}, s, h.x, h.y, p);
 }
 

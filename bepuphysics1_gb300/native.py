@@ -23,7 +23,7 @@ SETTINGS_DTYPE = np.dtype([
     ("bounciness_velocity_threshold", "<f4"), ("allowed_penetration", "<f4"),
     ("contact_invalidation_length_squared", "<f4"), ("maximum_contact_distance", "<f4"),
     ("use_stabilization", "<i4"), ("velocity_lower_limit", "<f4"), ("low_velocity_time_minimum", "<f4"),
-    ("reserved", "<i4"),
+    ("maximum_deactivation_attempts_per_frame", "<i4"),
 ])
 BODY_DTYPE = np.dtype([
     ("position", "<f4", 3), ("orientation", "<f4", 4), ("linear_velocity", "<f4", 3),
@@ -125,6 +125,7 @@ JOINT_REVOLUTE_MOTOR, JOINT_TWIST_MOTOR, JOINT_LINEAR_AXIS_MOTOR = 21, 22, 23
 JOINT_MAXIMUM_LINEAR_SPEED, JOINT_MAXIMUM_ANGULAR_SPEED, JOINT_PLANE_SLIDER = 24, 25, 26
 JOINT_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_ANGULAR_MOTOR, JOINT_SINGLE_ENTITY_LINEAR_MOTOR = 27, 28, 29
 JOINT_ACTIVE, JOINT_LIMIT_ACTIVE, JOINT_SERVO, JOINT_GROUP_CONTINUATION = 1, 2, 4, 8
+ISLAND_ACTIVE, ISLAND_ALLOW_DEACTIVATION = 1, 2
 
 _P = ctypes.c_void_p
 _I = ctypes.c_int32
@@ -148,6 +149,8 @@ GPU_EXPORTS = {
     "bepugpu_upload_bodies": (_I, [_P, _I, _P, _U]),
     "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
     "bepugpu_broad_phase": (_I, [_P, _I, _F, _P, _U, ctypes.POINTER(_U)]),
+    "bepugpu_set_islands": (_I, [_P, _I, _P, _U, _P, _U, _I]),
+    "bepugpu_get_islands": (_I, [_P, _I, _P, _U, ctypes.POINTER(_I)]),
     "bepugpu_step_host": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_step_state": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_download_state": (_I, [_P, _I, _P, _U, _P, _U]),

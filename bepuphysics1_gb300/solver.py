@@ -223,6 +223,27 @@ class GpuSpace:
     def refresh_contacts(self, dt: float):
         self.step(dt, N.STEP_REFRESH_CONTACTS)
 
+    def set_islands(self, island_of_body: np.ndarray, island_flags: np.ndarray | None = None,
+                    deactivation_index: int = 0):
+        """bepugpu_set_islands: the island list (one entry per island, BEPUGPU_ISLAND_*
+        flags; default awake and allowed to deactivate) and each body's island
+        (-1 for kinematic bodies)."""
+        of = np.ascontiguousarray(island_of_body, np.int32)
+        n = int(of.max(initial=-1)) + 1 if island_flags is None else len(island_flags)
+        flags = (np.full(n, N.ISLAND_ACTIVE | N.ISLAND_ALLOW_DEACTIVATION, np.uint32) if island_flags is None
+                 else np.ascontiguousarray(island_flags, np.uint32))
+        self.ctx.check(self.ctx.lib.bepugpu_set_islands(self.ctx.handle, self.id, N.ptr(of), len(of), N.ptr(flags),
+                                                        len(flags), int(deactivation_index)))
+        self.island_count = len(flags)
+
+    def get_islands(self):
+        """(island flags, deactivation index) as the last step left them."""
+        flags = np.zeros(getattr(self, "island_count", 0), np.uint32)
+        idx = ctypes.c_int32()
+        self.ctx.check(self.ctx.lib.bepugpu_get_islands(self.ctx.handle, self.id, N.ptr(flags), len(flags),
+                                                        ctypes.byref(idx)))
+        return flags, idx.value
+
     def download_bodies(self, into: np.ndarray | None = None) -> np.ndarray:
         out = np.zeros(self.body_count, N.BODY_DTYPE) if into is None else into
         self.ctx.check(self.ctx.lib.bepugpu_download_bodies(self.ctx.handle, self.id, N.ptr(out), len(out)))
@@ -298,6 +319,42 @@ def colour_list(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | 
                                  ctypes.byref(k))
     N.raise_for(st, "bepugpu_colour_list: a constraint references a body outside the body array")
     return colour, order, k.value
+
+
+def islands_of(bodies: np.ndarray, manifolds: np.ndarray, joints: np.ndarray | None = None) -> np.ndarray:
+    """A partition for bepugpu_set_islands when no DeactivationManager keeps one:
+    dynamic bodies joined through every joint and every manifold with contacts
+    (the SimulationIslandConnections of the constraints in the solver),
+    islands numbered in the order of their first member.  -1 for kinematic
+    bodies."""
+    nb = len(bodies)
+    parent = np.arange(nb)
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    dyn = bodies["is_dynamic"] != 0
+    pairs = []
+    if joints is not None and len(joints):
+        pairs.append(np.stack([joints["body_a"], joints["body_b"]], 1))
+    if len(manifolds):
+        has = manifolds["contact_count"] > 0
+        pairs.append(np.stack([manifolds["body_a"][has], manifolds["body_b"][has]], 1))
+    for a, b in (np.concatenate(pairs) if pairs else np.zeros((0, 2), np.int64)):
+        if a >= 0 and b >= 0 and dyn[a] and dyn[b]:
+            ra, rb = find(int(a)), find(int(b))
+            if ra != rb:
+                parent[max(ra, rb)] = min(ra, rb)
+    out = np.full(nb, -1, np.int32)
+    ids = {}
+    for i in range(nb):
+        if dyn[i]:
+            r = find(i)
+            out[i] = ids.setdefault(r, len(ids))
+    return out
 
 
 def scene_ids(spaces) -> np.ndarray:

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 8
+#define BEPUGPU_ABI_VERSION 9
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -68,7 +68,9 @@ typedef struct bepugpu_settings {
                                               low-velocity damping boost, EntityBase.cs:926-936 */
     float velocity_lower_limit;            /* DeactivationManager.VelocityLowerLimit, :18,28 (.26) */
     float low_velocity_time_minimum;       /* DeactivationManager.LowVelocityTimeMinimum, :20,46 (1) */
-    int32_t reserved;
+    int32_t maximum_deactivation_attempts_per_frame; /* DeactivationManager, :15,89 (100): members of
+                                              the islands DeactivateObjects looks at in one step
+                                              (scenes with bepugpu_set_islands) */
 } bepugpu_settings;
 
 /* Body activity flags: the state of the entity's SimulationIslandMember
@@ -417,6 +419,51 @@ bepugpu_status bepugpu_upload_shapes(bepugpu_context* ctx, int32_t scene, const 
  * use and when the pair count grows. */
 bepugpu_status bepugpu_broad_phase(bepugpu_context* ctx, int32_t scene, float dt, int32_t* pairs,
                                    uint32_t max_pairs, uint32_t* pair_count);
+/* Simulation islands (DeactivationManagement/SimulationIsland.cs,
+ * DeactivationManager.cs): the host's island partition and list order, after
+ * which steps put islands to sleep and skip their work as the reference's
+ * DeactivationManager does.  island_of_body[i] is body i's index in the
+ * island list (`islands` entries): >= 0 for every dynamic body, -1 for
+ * kinematic ones; every island needs a member, and every constraint's dynamic
+ * bodies share one island (a SimulationIslandConnection's members do; merging
+ * and splitting islands stays with the host, DeactivationManager.cs:345-700).
+ * island_flags[k]: BEPUGPU_ISLAND_* of island k.  deactivation_index is
+ * DeactivationManager.deactivationIslandIndex, the island DeactivateObjects
+ * looked at last.  Body records are the member list in order
+ * (DeactivationManager.simulationIslandMembers).
+ *
+ * With islands set, BEPUGPU_STEP_DEACTIVATION runs DeactivationManager.Update
+ * minus the splits (DeactivationManager.cs:216-224) before the other stages:
+ * each member's UpdateDeactivationCandidacy in member order
+ * (SimulationIslandMember.cs:53-164; an island woken by an active kinematic
+ * body is active, and not allowed to deactivate at its next attempt, from that
+ * kinematic member on), then DeactivateObjects (:310-336): from the island
+ * after deactivation_index, round robin, TryToDeactivate
+ * (SimulationIsland.cs:94-118) on islands until their members add up to
+ * maximum_deactivation_attempts_per_frame or every island was looked at.  The
+ * connections of a kinematic body are its joints and its manifolds with
+ * contacts.  A dynamic body is then active when its island is: the force and
+ * position updates skip inactive bodies (ForceUpdater.cs:73-76,
+ * ContinuousPositionUpdater.cs:71), a constraint with no active dynamic body
+ * is not active in the solver (SolverUpdateable.cs:202-219,
+ * ContactManifoldConstraint.cs:125-141) and keeps its impulses, and a manifold
+ * neither of whose bodies is active is not refreshed or regenerated
+ * (NarrowPhase.cs:300-332; world-anchored ends count as inactive).
+ *
+ * bepugpu_upload_bodies and bepugpu_upload_constraints clear the islands (the
+ * scene is stepped with every island awake until they are set again); so does
+ * islands = 0.  Scenes with islands are stepped one at a time (batch and
+ * serve refuse them). */
+#define BEPUGPU_ISLAND_ACTIVE             1u  /* SimulationIsland.isActive */
+#define BEPUGPU_ISLAND_ALLOW_DEACTIVATION 2u  /* SimulationIsland.allowDeactivation (default true) */
+bepugpu_status bepugpu_set_islands(bepugpu_context* ctx, int32_t scene, const int32_t* island_of_body,
+                                   uint32_t body_count, const uint32_t* island_flags, uint32_t islands,
+                                   int32_t deactivation_index);
+/* The islands' flags and the deactivation index as the last step left them
+ * (synchronises the scene's stream). */
+bepugpu_status bepugpu_get_islands(bepugpu_context* ctx, int32_t scene, uint32_t* island_flags,
+                                   uint32_t islands, int32_t* deactivation_index);
+
 /* Rewrites manifold records in place without recolouring.  Body pairs and the
  * manifold count must be those of the last bepugpu_upload_constraints (checked
  * on the device before anything changes; INVALID_ARGUMENT otherwise). */

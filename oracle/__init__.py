@@ -38,6 +38,8 @@ def _load():
             "oracle_prime_count": (I, []),
             "oracle_colour": (I, [P, I, P, I, P, I, P, P]),
             "oracle_set_shapes": (I, [P, P, I]),
+            "oracle_set_islands": (I, [P, P, P, I, I]),
+            "oracle_get_islands": (I, [P, P, I, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -120,6 +122,26 @@ class OracleSpace:
         j = self.joints.copy()
         self.lib.oracle_get_constraints(self.h, _ptr(m), _ptr(j))
         return m, j
+
+    def set_islands(self, island_of_body, island_flags=None, deactivation_index: int = 0):
+        """The island list as bepugpu_set_islands takes it (flags default: awake,
+        allowed to deactivate)."""
+        from bepuphysics1_gb300 import native as N
+        of = np.ascontiguousarray(island_of_body, np.int32)
+        n = int(of.max(initial=-1)) + 1 if island_flags is None else len(island_flags)
+        flags = (np.full(n, N.ISLAND_ACTIVE | N.ISLAND_ALLOW_DEACTIVATION, np.uint32) if island_flags is None
+                 else np.ascontiguousarray(island_flags, np.uint32))
+        self._island_of, self._island_flags = of, flags
+        if self.lib.oracle_set_islands(self.h, _ptr(of), _ptr(flags), len(flags), int(deactivation_index)) != 0:
+            raise ValueError("bad island partition")
+        self.island_count = len(flags)
+
+    def get_islands(self):
+        flags = np.zeros(getattr(self, "island_count", 0), np.uint32)
+        idx = ctypes.c_int32()
+        if self.lib.oracle_get_islands(self.h, _ptr(flags), len(flags), ctypes.byref(idx)) != 0:
+            raise ValueError("island count")
+        return flags, idx.value
 
     def last_child_solves(self) -> int:
         return self.lib.oracle_last_child_solves(self.h)

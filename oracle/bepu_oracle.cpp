@@ -39,6 +39,7 @@ struct Settings {
     // DeactivationManager (DeactivationManager.cs:18-20,60)
     bool useStabilization = true;
     float velocityLowerLimit = .26f, velocityLowerLimitSquared = .26f * .26f, lowVelocityTimeMinimum = 1;
+    int maximumDeactivationAttemptsPerFrame = 100;  // DeactivationManager.cs:15
 };
 
 // ---------------------------------------------------------------- PermutationMapper --
@@ -77,8 +78,17 @@ struct SpinLock {
     void Exit() { owner.store(-1, std::memory_order_release); }
 };
 
+// SimulationIsland.cs:12-56: the state DeactivateObjects reads and writes.
+struct Island {
+    bool isActive = true, allowDeactivation = true;
+    int memberCount = 0, candidates = 0;  // candidates: members that are deactivation candidates
+    int deactivationCandidateCount() const { return candidates; }
+};
+
 struct Entity {
     int index = 0;
+    Island* island = nullptr;  // SimulationIslandMember.SimulationIsland: null for kinematic bodies
+                               // and for every body of a space without islands (all awake)
     Vec3 position;
     Quat orientation;
     Mat3 orientationMatrix;
@@ -94,17 +104,25 @@ struct Entity {
     bool isSlowing = false, isDeactivationCandidate = false, isAlwaysActive = false, allowStabilization = true;
     float linearDampingBoost = 0, angularDampingBoost = 0;
 
-    // SimulationIslandMember.IsActive (:225-248)
-    bool IsActive() const { return isDynamic || velocityTimeBelowLimit <= 0; }
+    // SimulationIslandMember.IsActive (:225-248): the island's state, or the
+    // time flag without an island (kinematic bodies).  A dynamic body of a
+    // space without islands counts as awake.
+    bool IsActive() const {
+        if (island) return island->isActive;
+        return isDynamic || velocityTimeBelowLimit <= 0;
+    }
     // The IsDeactivationCandidate setter (:171-190)
     void SetDeactivationCandidate(bool value) {
         isDeactivationCandidate = value;
         if (!value) velocityTimeBelowLimit = 0;
     }
-    // SimulationIslandMember.UpdateDeactivationCandidacy (:53-164), island awake.
-    void UpdateDeactivationCandidacy(float dt, const Settings& s) {
+    // SimulationIslandMember.UpdateDeactivationCandidacy (:53-164).  Returns
+    // whether an active kinematic body wakes its connections' islands
+    // (:135-159); the caller does the waking.
+    bool UpdateDeactivationCandidacy(float dt, const Settings& s) {
         float velocity = LengthSquared(linearVelocity) + LengthSquared(angularVelocity);
         bool isActive = IsActive();
+        bool wakes = false;
         if (isActive) {
             isSlowing = velocity <= previousVelocity;
             if (isDynamic) {
@@ -128,9 +146,11 @@ struct Entity {
                 } else {
                     velocityTimeBelowLimit = -1;
                 }
+                wakes = velocityTimeBelowLimit <= 0;
             }
         }
         previousVelocity = velocity;
+        return wakes;
     }
     // EntityBase.ModifyLinearDamping / ModifyAngularDamping (EntityBase.cs:1205-1221)
     void ModifyLinearDamping(float damping) {
@@ -214,12 +234,12 @@ struct SolverUpdateable {
     int involvedCount = 0;
 
     virtual ~SolverUpdateable() = default;
-    // SolverUpdateable.cs:202-219 with every simulation island awake: an island
-    // exists (and is active) exactly for dynamic entities.
+    // SolverUpdateable.cs:202-219: active while a connected member's island
+    // is; islands exist for dynamic entities only.
     virtual void UpdateSolverActivity() {
         if (isActive) {
             for (int i = 0; i < involvedCount; i++)
-                if (involved[i]->isDynamic) { isActiveInSolver = true; return; }
+                if (involved[i]->isDynamic && involved[i]->IsActive()) { isActiveInSolver = true; return; }
         }
         isActiveInSolver = false;
     }
@@ -256,6 +276,11 @@ struct Space {
     size_t jointCount = 0;
     std::vector<bepugpu_shape> shapes;  // one per entity, for GENERATED manifolds
     Entity world;  // TwoEntityConstraint.WorldEntity: kinematic, at the origin, identity orientation
+    // DeactivationManager.simulationIslands (in list order) and deactivationIslandIndex;
+    // empty: every island awake, no deactivation.
+    std::vector<Island> islands;
+    int deactivationIslandIndex = 0;
+    std::vector<std::vector<SolverUpdateable*>> connectionsOf;  // per entity: the constraints touching it
 };
 
 // SolverGroup.cs:52-165
@@ -605,7 +630,8 @@ struct ConvexManifold : SolverGroup {
     // ContactManifoldConstraint.cs:128-145 with every entity awake
     void UpdateSolverActivity() override {
         if (isActive) {
-            isActiveInSolver = solverRule && ((entityA && entityA->isDynamic) || (entityB && entityB->isDynamic));
+            isActiveInSolver = solverRule && ((entityA && entityA->isDynamic && entityA->IsActive()) ||
+                                              (entityB && entityB->isDynamic && entityB->IsActive()));
             for (auto* c : children) c->isActiveInSolver = c->isActive && isActiveInSolver;
         } else {
             isActiveInSolver = false;
@@ -1283,13 +1309,75 @@ static void SolverUpdateMultithreaded(Space& sp, float dt, int threads) {
     });
 }
 
+// DeactivationManager.DeactivateObjects (DeactivationManager.cs:310-336) over
+// islands that all have members, with SimulationIsland.TryToDeactivate
+// (SimulationIsland.cs:94-118).
+static void DeactivateObjects(Space& sp) {
+    int numberOfEntitiesDeactivated = 0, numberOfIslandsChecked = 0;
+    const int originalIslandCount = (int)sp.islands.size();
+    while (numberOfEntitiesDeactivated < sp.s.maximumDeactivationAttemptsPerFrame && !sp.islands.empty() &&
+           numberOfIslandsChecked < originalIslandCount) {
+        sp.deactivationIslandIndex = (sp.deactivationIslandIndex + 1) % (int)sp.islands.size();
+        Island& island = sp.islands[sp.deactivationIslandIndex];
+        if (island.allowDeactivation) {
+            if (island.isActive && island.deactivationCandidateCount() == island.memberCount) island.isActive = false;
+        } else {
+            island.allowDeactivation = true;
+        }
+        numberOfEntitiesDeactivated += island.memberCount;
+        ++numberOfIslandsChecked;
+    }
+}
+
+// DeactivationManager.UpdateSingleThreaded (DeactivationManager.cs:216-224)
+// without the split flush: the candidacy loop in member order, an active
+// kinematic member waking its connections' islands as it goes, then
+// DeactivateObjects.  A manifold is a connection while it has contacts (the
+// pair handler keeps its constraint in the solver only then).
+static void DeactivationUpdate(Space& sp, float dt) {
+    for (auto& e : sp.entities) {
+        if (!e.UpdateDeactivationCandidacy(dt, sp.s)) continue;
+        for (SolverUpdateable* c : sp.connectionsOf[(size_t)e.index]) {
+            if (auto* m = dynamic_cast<ConvexManifold*>(c))
+                if (m->penetrationConstraints.empty()) continue;
+            for (int k = 0; k < c->involvedCount; k++)
+                if (Island* isl = c->involved[k]->island) {
+                    isl->isActive = true;
+                    isl->allowDeactivation = false;
+                }
+        }
+    }
+    for (auto& isl : sp.islands) isl.candidates = 0;
+    for (auto& e : sp.entities)
+        if (e.island && e.isDeactivationCandidate) e.island->candidates++;
+    DeactivateObjects(sp);
+}
+
+// An entry of the narrow phase is active (NarrowPhase.cs:300-332 updates a pair
+// while one of its entries is); a missing entity is a static entry, inactive.
+static bool EntryActive(const Entity* e) { return e && e->IsActive(); }
+
 static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
-    // The narrow phase and the refresher read poses only, so they run before
-    // the force update here (the reference runs them after it, Space.cs:504-513).
+    // DeactivationManager.Update comes first (Space.cs:502); the narrow phase
+    // and the refresher read poses only, so they run before the force update
+    // here (the reference runs them after it, Space.cs:504-513).
+    const bool islands = !sp.islands.empty();
+    if (flags & BEPUGPU_STEP_DEACTIVATION) {  // DeactivationManager.cs:206-224, the candidacy loop
+        if (islands) {
+            DeactivationUpdate(sp, dt);  // member order matters: sequential
+        } else {
+            auto body = [&](long long i) { sp.entities[i].UpdateDeactivationCandidacy(dt, sp.s); };
+            if (threads > 1) ForLoop(threads, 0, (long long)sp.entities.size(), body);
+            else for (size_t i = 0; i < sp.entities.size(); i++) body((long long)i);
+        }
+    }
+    auto pairActive = [&](const ConvexManifold* m) {
+        return !islands || EntryActive(m->entityA) || EntryActive(m->entityB);
+    };
     if (flags & BEPUGPU_STEP_COLLIDE) {  // pairs are independent: the narrow phase's pair loop
         auto pair = [&](long long i) {
             auto* m = static_cast<ConvexManifold*>(sp.updateables[sp.jointCount + (size_t)i].get());
-            if (m->generated) CollideManifold(sp, *m);
+            if (m->generated && pairActive(m)) CollideManifold(sp, *m);
         };
         const long long n = (long long)(sp.updateables.size() - sp.jointCount);
         if (threads > 1) ForLoop(threads, 0, n, pair);
@@ -1298,13 +1386,8 @@ static void StepOnce(Space& sp, float dt, uint32_t flags, int threads) {
     if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) {
         for (size_t i = sp.jointCount; i < sp.updateables.size(); i++) {
             auto* m = static_cast<ConvexManifold*>(sp.updateables[i].get());
-            if (!m->generated) RefreshManifold(*m, sp.s);
+            if (!m->generated && pairActive(m)) RefreshManifold(*m, sp.s);
         }
-    }
-    if (flags & BEPUGPU_STEP_DEACTIVATION) {  // DeactivationManager.cs:206-224, the candidacy loop
-        auto body = [&](long long i) { sp.entities[i].UpdateDeactivationCandidacy(dt, sp.s); };
-        if (threads > 1) ForLoop(threads, 0, (long long)sp.entities.size(), body);
-        else for (size_t i = 0; i < sp.entities.size(); i++) body((long long)i);
     }
     if (flags & BEPUGPU_STEP_FORCES) {  // ForceUpdater.cs:73-92
         Vec3 gravityDt = Multiply(sp.s.gravity, dt);
@@ -1370,6 +1453,7 @@ oracle_space* oracle_create(const bepugpu_settings* st, const bepugpu_body* bodi
     S.velocityLowerLimit = std::max(0.f, st->velocity_lower_limit);  // DeactivationManager.cs:36-37
     S.velocityLowerLimitSquared = S.velocityLowerLimit * S.velocityLowerLimit;
     S.lowVelocityTimeMinimum = st->low_velocity_time_minimum;
+    S.maximumDeactivationAttemptsPerFrame = st->maximum_deactivation_attempts_per_frame;
 
     sp.entities = std::vector<Entity>(nb);
     for (int i = 0; i < nb; i++) {
@@ -1509,6 +1593,63 @@ int32_t oracle_step_multithreaded(oracle_space* s, float dt, uint32_t flags, int
 }
 
 int64_t oracle_last_child_solves(oracle_space* s) { return s->sp.childSolves.load(); }
+
+// The island list as bepugpu_set_islands takes it: island_of[i] per body (-1
+// for kinematic bodies), flags per island.  count 0 clears the islands.
+// Returns -1 when a dynamic body has no island, an island has no member or a
+// constraint's dynamic bodies lie in two islands.
+int32_t oracle_set_islands(oracle_space* s, const int32_t* island_of, const uint32_t* flags, int32_t count,
+                           int32_t deactivation_index) {
+    Space& sp = s->sp;
+    for (auto& e : sp.entities) e.island = nullptr;
+    sp.islands.clear();
+    sp.connectionsOf.clear();
+    if (count <= 0) return 0;
+    std::vector<Island> islands((size_t)count);
+    for (int k = 0; k < count; k++) {
+        islands[k].isActive = (flags[k] & BEPUGPU_ISLAND_ACTIVE) != 0;
+        islands[k].allowDeactivation = (flags[k] & BEPUGPU_ISLAND_ALLOW_DEACTIVATION) != 0;
+    }
+    const int nb = (int)sp.entities.size();
+    for (int i = 0; i < nb; i++) {
+        const int k = island_of[i];
+        if (!sp.entities[i].isDynamic) {
+            if (k != -1) return -1;
+            continue;
+        }
+        if (k < 0 || k >= count) return -1;
+        islands[k].memberCount++;
+    }
+    for (auto& isl : islands)
+        if (isl.memberCount == 0) return -1;
+    sp.connectionsOf.assign((size_t)nb, {});
+    for (auto& u : sp.updateables) {
+        int shared = -1;
+        for (int k = 0; k < u->involvedCount; k++) {
+            Entity* e = u->involved[k];
+            if (e->index < 0) continue;  // the world entity
+            sp.connectionsOf[(size_t)e->index].push_back(u.get());
+            if (!e->isDynamic) continue;
+            if (shared >= 0 && island_of[e->index] != shared) return -1;
+            shared = island_of[e->index];
+        }
+    }
+    sp.islands = std::move(islands);
+    for (int i = 0; i < nb; i++)
+        if (sp.entities[i].isDynamic) sp.entities[i].island = &sp.islands[(size_t)island_of[i]];
+    sp.deactivationIslandIndex = deactivation_index;
+    return 0;
+}
+
+int32_t oracle_get_islands(oracle_space* s, uint32_t* flags, int32_t count, int32_t* deactivation_index) {
+    Space& sp = s->sp;
+    if (count != (int32_t)sp.islands.size()) return -1;
+    for (int k = 0; k < count; k++)
+        flags[k] = (sp.islands[k].isActive ? BEPUGPU_ISLAND_ACTIVE : 0u) |
+                   (sp.islands[k].allowDeactivation ? BEPUGPU_ISLAND_ALLOW_DEACTIVATION : 0u);
+    if (deactivation_index) *deactivation_index = sp.deactivationIslandIndex;
+    return 0;
+}
 
 void oracle_get_bodies(oracle_space* s, bepugpu_body* out) {
     Space& sp = s->sp;

@@ -35,6 +35,10 @@ int32_t oracle_step_multithreaded(oracle_space* s, float dt, uint32_t flags, int
                                   int32_t threads);
 /* One shape per body, for manifolds flagged BEPUGPU_MANIFOLD_GENERATED. */
 int32_t oracle_set_shapes(oracle_space* s, const bepugpu_shape* shapes, int32_t count);
+/* Simulation islands as bepugpu_set_islands takes them; count 0 clears them. */
+int32_t oracle_set_islands(oracle_space* s, const int32_t* island_of, const uint32_t* flags, int32_t count,
+                           int32_t deactivation_index);
+int32_t oracle_get_islands(oracle_space* s, uint32_t* flags, int32_t count, int32_t* deactivation_index);
 void oracle_get_bodies(oracle_space* s, bepugpu_body* out);
 void oracle_get_constraints(oracle_space* s, bepugpu_manifold* manifolds, bepugpu_joint* joints);
 /* Counts of solves executed by the last step (manifold-children and joints). */
