@@ -26,6 +26,11 @@ One step = ContactRefresher -> ForceUpdater -> Solver (prestep, warm start,
   cpu_baseline the oracle port of Solver.UpdateMultithreaded (per-body spin
               locks, chunked parallel loop) on all host cores, on a bounded
               sample of steps of the same pile.
+  dropped     the same pile dropped from a 2 m grid and settled for 120 steps
+              with the device broad phase, narrow phase and solver, then its
+              captured manifold set timed like the headline.
+  islands     device ms of a step of the pile's 4,096 column islands awake and
+              asleep (DeactivationManager on the device).
 
 `--impl reference` times that CPU port alone (the reference is C# and no .NET
 runtime exists on these machines).  Under torchrun every rank steps its own
@@ -79,6 +84,9 @@ def parse_args():
     ap.add_argument("--no-collide", action="store_true", help="skip the narrow-phase section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the colour-sweep path section")
     ap.add_argument("--no-pile1k", action="store_true", help="skip the 1,000-box pile section")
+    ap.add_argument("--no-dropped", action="store_true", help="skip the dropped-and-settled pile section")
+    ap.add_argument("--dropped-steps", type=int, default=240, help="settling steps of the dropped pile")
+    ap.add_argument("--no-islands", action="store_true", help="skip the simulation-islands section")
     ap.add_argument("--pile1k-cpu-seconds", type=float, default=2.0)
     ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
@@ -281,6 +289,140 @@ def sweep_section(args, ctx, local, pg, peak, peak_kind):
                      "roofline": solve_roofline(prof, solve_ms, peak, peak_kind)}
         space.close()
     out["l2"] = "flushed between timed steps (512 MiB write)"
+    return out
+
+
+def dropped_section(args, ctx, local, pg):
+    """Config 2 as written: pile_64k's 65,536 boxes on a 64 x 16 x 64 grid
+    with 2 m between layers too, dropped onto the ground and settled with the
+    device broad phase, the pair records (bepuphysics1_gb300/pairs.py), the
+    device narrow phase and the solver.  120 steps (2 s) are not enough for
+    the top layers, which fall about 16 m, to land: the state after 120 steps
+    is reported and the pile settles for --dropped-steps in all.  Then the
+    settled heap's pair set, its contacts regenerated by the narrow phase each
+    step, timed like the headline (contact-iters/s, I = 10)."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.pairs import PairRecords
+    from bepuphysics1_gb300.solver import GpuSpace, islands_of
+    bodies, shapes, friction = scenes.dropped_pile()
+    nb = len(bodies)
+    space = GpuSpace(ctx, bodies, None, capacity=(nb, 8 * nb, 0), shapes=shapes)
+    records = PairRecords(friction, shapes)
+    flags = N.STEP_ALL | N.STEP_COLLIDE
+    loop_ms, changes, after120 = [], 0, None
+    t0 = time.perf_counter()
+    for step in range(args.dropped_steps):
+        if step == 120:
+            b120 = space.download_bodies(bodies.copy())
+            d120 = b120["is_dynamic"] == 1
+            sp120 = np.linalg.norm(b120["linear_velocity"][d120], axis=1)
+            after120 = {"speed_p50": float(np.median(sp120)), "speed_p99": float(np.percentile(sp120, 99)),
+                        "top": float(b120["position"][d120][:, 1].max())}
+        ts = time.perf_counter()
+        pairs = space.broad_phase(DT)
+        current = space.download_constraints(records.manifolds.copy())[0] if len(records.manifolds) else None
+        if records.update(pairs, current):
+            changes += 1
+            space.upload_constraints(records.manifolds)
+        space.step(DT, flags)
+        ctx.synchronize()
+        loop_ms.append(1000.0 * (time.perf_counter() - ts))
+    settle_s = time.perf_counter() - t0
+    gb = space.download_bodies(bodies.copy())
+    gm, _ = space.download_constraints(records.manifolds.copy())
+    space.close()
+    dyn = gb["is_dynamic"] == 1
+    speed = np.linalg.norm(gb["linear_velocity"][dyn], axis=1)
+    # the settled heap's pair set kept, its contacts regenerated every step by the narrow phase
+    isl = islands_of(gb, gm)
+    sizes = np.bincount(isl[isl >= 0]) if (isl >= 0).any() else np.zeros(1, np.int64)
+    solved = GpuSpace(ctx, gb, gm, shapes=shapes)
+    for _ in range(max(args.warmup, 3)):
+        solved.step(DT, flags)
+    ctx.synchronize()
+    live_m, _ = solved.download_constraints()
+    contacts = int(live_m["contact_count"].sum())
+    cips = contacts * int(ctx.settings["iteration_limit"])
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    if pg:
+        pg.barrier()
+    step_ms, _ = timed_steps(solved, args.steps, flush, flags)
+    from bepuphysics1_gb300.solver import profile_step
+    prof = profile_step(solved, DT, flags)
+    ms = statistics.mean(step_ms)
+    out = {"workload": "pile_64k dropped from a 64 x 16 x 64 grid (2 m spacing) and settled for "
+                       f"{args.dropped_steps} steps on the device",
+           "value": cips / (ms / 1000.0), "unit": "contact-iters/s", "ms_per_step": ms,
+           "step": "collide+refresh+forces+solve+positions on the settled heap's pair set",
+           "bodies": int(nb), "manifolds": int(len(gm)), "contacts": contacts,
+           "colours": int(solved.colouring()[2]), "islands": int(isl.max() + 1) if (isl >= 0).any() else 0,
+           "largest_island": int(sizes.max()), "group_ctas": int(prof["groups"]),
+           "gpu_launches_per_step": int(solved.last_step_launches()),
+           "settle": {"steps": args.dropped_steps, "seconds": settle_s, "pair_set_changes": changes,
+                      "loop_ms_median": statistics.median(loop_ms),
+                      "loop_ms_last20_median": statistics.median(loop_ms[-20:]),
+                      "after_120_steps": after120,
+                      "what": "per step: device broad phase, pair records (download, diff, upload and "
+                              "recolour when the set changed), narrow phase + solver step; host wall clock",
+                      "speed_p50_after": float(np.median(speed)), "speed_p99_after": float(np.percentile(speed, 99)),
+                      "top_after": float(gb["position"][dyn][:, 1].max())},
+           "parity": "the same loop bit-exact against the oracle on a 5 x 4 x 5 drop (tests/test_gpu_settle.py)",
+           "l2": "flushed between timed steps (512 MiB write)"}
+    solved.close()
+    return out
+
+
+def islands_section(args, ctx, local, pg):
+    """Simulation islands on the device: 4,096 columns of 16 unit cubes as
+    islands (IsAlwaysActive cleared), stepped until every island sleeps (the
+    round robin looks at 100 members' worth of islands a step); device ms of
+    a step with every island awake and with every island asleep."""
+    import torch
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import GpuSpace, islands_of
+    # unit cubes, so that every column stands (pile_64k's random sizes topple
+    # some columns, which never come to rest on a frozen manifold set)
+    bodies, manifolds, _ = scenes.make_pile(nx=64, ny=16, nz=64, spacing=2.0, size_min=1.0, size_max=1.0,
+                                            jitter=0.02, friction_min=0.6, friction_max=0.6,
+                                            ground_size=(140.0, 1.0, 140.0), seed=5)
+    bodies = bodies.copy()
+    bodies["activity"] &= ~np.uint32(N.BODY_ALWAYS_ACTIVE)
+    space = GpuSpace(ctx, bodies, manifolds)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    for _ in range(3):
+        space.step(DT, N.STEP_ALL)
+    plain_ms, _ = timed_steps(space, args.steps, flush, N.STEP_ALL)  # no islands: every island awake
+    space.upload_bodies(bodies)
+    isl = islands_of(bodies, manifolds)
+    space.set_islands(isl)
+    awake_ms, _ = timed_steps(space, args.steps, flush, N.STEP_ALL)
+    steps = args.steps
+    asleep_at = None
+    for k in range(4000):
+        space.step(DT, N.STEP_ALL)
+        steps += 1
+        if k % 50 == 49:
+            f, _ = space.get_islands()
+            if not np.any(f & N.ISLAND_ACTIVE):
+                asleep_at = steps
+                break
+    if pg:
+        pg.barrier()
+    asleep_ms, _ = timed_steps(space, args.steps, flush, N.STEP_ALL)
+    f, idx = space.get_islands()
+    out = {"workload": "64 x 16 x 64 unit cubes in 4,096 column islands", "islands": int(len(f)),
+           "without_islands_ms_per_step": statistics.mean(plain_ms),
+           "awake_ms_per_step": statistics.mean(awake_ms), "asleep_ms_per_step": statistics.mean(asleep_ms),
+           "all_asleep_after_steps": asleep_at, "asleep_now": int(np.count_nonzero((f & N.ISLAND_ACTIVE) == 0)),
+           "launches_per_step": int(space.last_step_launches()),
+           "what": "DeactivationManager.Update on the device (1 launch without moving kinematic bodies, 2 with) "
+                   "before the group step; a group whose "
+                   "islands all sleep returns after loading its bodies",
+           "l2": "flushed between timed steps (512 MiB write)"}
+    space.close()
     return out
 
 
@@ -1142,6 +1284,16 @@ def main():
         space.close()
         pile1k = pile1k_section(args, ctx, local, pg)
         t_sec = mark("pile1k", t_sec)
+    dropped = None
+    if not args.no_dropped:
+        space.close()
+        dropped = dropped_section(args, ctx, local, pg)
+        t_sec = mark("dropped", t_sec)
+    islands = None
+    if not args.no_islands:
+        space.close()
+        islands = islands_section(args, ctx, local, pg)
+        t_sec = mark("islands", t_sec)
     batch = None
     if not args.no_batch:
         space.close()
@@ -1182,6 +1334,8 @@ def main():
             "roofline": roofline,
             "sweep": sweep,
             "pile_1k": pile1k,
+            "dropped": dropped,
+            "islands": islands,
             "e2e": e2e,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),

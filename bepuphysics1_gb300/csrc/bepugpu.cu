@@ -944,6 +944,7 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
     // DeactivationManager.Update before everything else (Space.cs:502): the
     // narrow phase, the refresher and the body stages read the islands' state.
+    graphWakes = islands && IslandWakesPossible(this);
     if (islands && (flags & BEPUGPU_STEP_DEACTIVATION)) {
         cudaError_t ie = LaunchIslandStage(this, p, ctx->settings.maximum_deactivation_attempts_per_frame, stream);
         if (ie != cudaSuccess) {
@@ -1182,8 +1183,9 @@ bepugpu_status Scene::Step(Context* ctx, float dt, uint32_t flags) {
         if (st != BEPUGPU_OK) return st;
     } else {
         const bool tail = SweepEmpty() && kin.Needed(StageFlags(flags)) && sweepBodyCount;
+        const bool wakes = islands && IslandWakesPossible(this);
         if (!graphExec || graphDt != dt || graphFlags != flags || graphVersion != version ||
-            graphIterations != p.iterationLimit || graphTail != tail) {
+            graphIterations != p.iterationLimit || graphTail != tail || graphWakes != wakes) {
             st = BuildGraph(ctx, p, flags);
             if (st != BEPUGPU_OK) return st;
         }

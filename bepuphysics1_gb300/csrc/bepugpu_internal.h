@@ -30,6 +30,7 @@ struct StepParams;
 void ReleaseIslands(Scene* s);
 void ApplyIslandViews(Scene* s);    // the body view's island pointers after a rebase
 cudaError_t LaunchIslandStage(Scene* s, const StepParams& p, int maxAttempts, cudaStream_t q);
+bool IslandWakesPossible(const Scene* s);
 
 // Device memory of a context's scene arenas and staging buffers, carved from
 // large cudaMalloc slabs (heap.cu).  Thread-safe: a server's worker spills and
@@ -339,6 +340,7 @@ struct Scene {
     uint32_t graphFlags = 0;
     uint64_t version = 1, graphVersion = 0;
     bool graphTail = false;  // the graph ends with the kinematic bodies' stages
+    bool graphWakes = false; // the graph's island stage looks for kinematic wakes
     int graphIterations = -1;
     uint32_t launchesPerStep = 0;
     int persistentBlocks = 0;

@@ -5,15 +5,17 @@
 // The reference's candidacy loop runs member by member; the only coupling
 // between members is an active kinematic member waking its connections'
 // islands (SimulationIslandMember.cs:135-159), which decides whether a later
-// member of such an island is updated as active.  Three launches restate the
+// member of such an island is updated as active.  Two launches restate the
 // loop: every connection of an active kinematic body records, per island, the
-// lowest member index that wakes it (k_island_wakes); every member then runs
-// its candidacy update with its island's state at its own turn -- awake from
-// the start, or woken by a member before it -- and counts the island's
-// candidates (k_island_members); one block applies the wakes and runs
-// DeactivateObjects' round robin (k_deactivate_objects).
+// lowest member index that wakes it (k_island_wakes, only while a kinematic
+// body can wake anything); every member then runs its candidacy update with
+// its island's state at its own turn -- awake from the start, or woken by a
+// member before it -- and counts the island's candidates, and the launch's
+// last block applies the wakes and runs DeactivateObjects' round robin
+// (k_island_members).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <vector>
 
@@ -34,6 +36,7 @@ struct IslandBuffers {
     int32_t* candidates = nullptr; // [n] members that are deactivation candidates (scratch, zero between steps)
     int32_t* wakeAt = nullptr;     // [n] lowest waking kinematic member (scratch, INT_MAX between steps)
     int32_t* index = nullptr;      // [1] deactivationIslandIndex
+    unsigned int* done = nullptr;  // [1] blocks of k_island_members finished (zero between steps)
     ~IslandBuffers() { cudaFree(block); }
 };
 
@@ -68,52 +71,121 @@ __global__ void k_island_wakes(ManifoldSoA m, JointSoA j, BodySoA b, StepParams 
     WakeThrough(b, h.y, h.x, p, wakeAt);
 }
 
-// UpdateDeactivationCandidacy of every member (SimulationIslandMember.cs:53-164).
-__global__ void k_island_members(BodySoA b, StepParams p, const int32_t* __restrict__ wakeAt, int32_t* candidates) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.count) return;
-    const bool dynamic = b.pos[i].w != 0.f;
-    float4 act = b.act[i];
-    if (dynamic) {
-        const int island = b.islandOf[i];
-        const bool awake = (b.islandFlags[island] & BEPUGPU_ISLAND_ACTIVE) || wakeAt[island] < i;
-        CandidacyMath(b.vlin[i], b.vang[i], true, act, p, awake);
-        if (__float_as_uint(act.z) & kCandidate) atomicAdd(candidates + island, 1);
-    } else {
-        CandidacyMath(b.vlin[i], b.vang[i], false, act, p);
+// Inclusive sum over the block (blockDim.x a multiple of 32, at most 1,024).
+__device__ __forceinline__ int BlockInclusiveSum(int v, int* warpSums) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
     }
-    b.act[i] = act;
+    if (lane == 31) warpSums[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < warps ? warpSums[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        if (lane < warps) warpSums[lane] = w;
+    }
+    __syncthreads();
+    const int before = warp ? warpSums[warp - 1] : 0;
+    __syncthreads();
+    return v + before;
 }
 
 // The wakes (island.IsActive = true, allowDeactivation = false), then
 // DeactivateObjects (DeactivationManager.cs:310-336) with TryToDeactivate
-// (SimulationIsland.cs:94-118) on thread 0, then the scratch cleared.
-__global__ void k_deactivate_objects(uint32_t* flags, const int32_t* __restrict__ members, int32_t* candidates,
-                                     int32_t* wakeAt, int32_t* index, int n, int maxAttempts) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x)
-        if (wakeAt[k] != INT_MAX) {
-            flags[k] = (flags[k] | BEPUGPU_ISLAND_ACTIVE) & ~BEPUGPU_ISLAND_ALLOW_DEACTIVATION;
-            wakeAt[k] = INT_MAX;
+// (SimulationIsland.cs:94-118), then the scratch cleared; by one block.  The
+// round robin looks at a run of islands after the index, each while the
+// members of the run's islands before it add up to less than the budget and
+// the run is shorter than the list; TryToDeactivate of one island reads only
+// that island, so the run is decided a block-wide chunk at a time from a
+// prefix sum of member counts.  The counts other blocks added are read from L2.
+__device__ void DeactivateObjects(uint32_t* flags, const int32_t* __restrict__ members, int32_t* candidates,
+                                  int32_t* wakeAt, int32_t* index, int n, int maxAttempts, bool wakes) {
+    __shared__ int warpSums[32];
+    __shared__ int lastLooked, counted;
+    if (wakes) {  // eight loads in flight a thread, then their islands
+        constexpr int kBatch = 8;
+        for (int k0 = threadIdx.x; k0 < n; k0 += kBatch * blockDim.x) {
+            int w[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int k = k0 + u * (int)blockDim.x;
+                w[u] = k < n ? __ldcg(wakeAt + k) : INT_MAX;
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int k = k0 + u * (int)blockDim.x;
+                if (w[u] != INT_MAX) {
+                    flags[k] = (flags[k] | BEPUGPU_ISLAND_ACTIVE) & ~BEPUGPU_ISLAND_ALLOW_DEACTIVATION;
+                    wakeAt[k] = INT_MAX;
+                }
+            }
         }
-    __syncthreads();
+    }
     if (threadIdx.x == 0) {
-        int counted = 0, checked = 0, idx = *index;
-        while (counted < maxAttempts && n > 0 && checked < n) {
-            idx = (idx + 1) % n;
-            uint32_t f = flags[idx];
+        lastLooked = -1;
+        counted = 0;
+    }
+    __syncthreads();
+    const int start = *index;
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int k = base + (int)threadIdx.x;  // position in the run
+        const int island = (start + 1 + k) % n;
+        const int m = k < n ? members[island] : 0;
+        const int before = counted;  // members of the run before this chunk
+        const int incl = BlockInclusiveSum(m, warpSums);
+        const bool looked = k < n && before + (incl - m) < maxAttempts;
+        if (looked) {
+            uint32_t f = flags[island];
             if (f & BEPUGPU_ISLAND_ALLOW_DEACTIVATION) {
-                if ((f & BEPUGPU_ISLAND_ACTIVE) && candidates[idx] == members[idx]) f &= ~BEPUGPU_ISLAND_ACTIVE;
+                if ((f & BEPUGPU_ISLAND_ACTIVE) && __ldcg(candidates + island) == m) f &= ~BEPUGPU_ISLAND_ACTIVE;
             } else {
                 f |= BEPUGPU_ISLAND_ALLOW_DEACTIVATION;
             }
-            flags[idx] = f;
-            counted += members[idx];
-            checked++;
+            flags[island] = f;
+            atomicMax(&lastLooked, k);
         }
-        *index = idx;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) counted = before + incl;
+        __syncthreads();
+        if (counted >= maxAttempts || lastLooked < base + (int)blockDim.x - 1) break;
     }
+    if (threadIdx.x == 0 && lastLooked >= 0) *index = (start + 1 + lastLooked) % n;
     __syncthreads();
     for (int k = threadIdx.x; k < n; k += blockDim.x) candidates[k] = 0;
+}
+
+// UpdateDeactivationCandidacy of every member (SimulationIslandMember.cs:53-164);
+// the last block to finish then runs DeactivateObjects.
+__global__ void k_island_members(BodySoA b, StepParams p, int32_t* wakeAt, int32_t* candidates, uint32_t* flags,
+                                 const int32_t* __restrict__ members, int32_t* index, int n, int maxAttempts,
+                                 unsigned int* done, bool wakes) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < b.count) {
+        const bool dynamic = b.pos[i].w != 0.f;
+        float4 act = b.act[i];
+        if (dynamic) {
+            const int island = b.islandOf[i];
+            const bool awake = (b.islandFlags[island] & BEPUGPU_ISLAND_ACTIVE) || (wakes && wakeAt[island] < i);
+            CandidacyMath(b.vlin[i], b.vang[i], true, act, p, awake);
+            if (__float_as_uint(act.z) & kCandidate) atomicAdd(candidates + island, 1);
+        } else {
+            CandidacyMath(b.vlin[i], b.vang[i], false, act, p);
+        }
+        b.act[i] = act;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    DeactivateObjects(flags, members, candidates, wakeAt, index, n, maxAttempts, wakes);
+    if (threadIdx.x == 0) *done = 0u;
 }
 
 // Every joint and every manifold with contacts keeps its dynamic bodies in
@@ -156,19 +228,26 @@ void ApplyIslandViews(Scene* s) {
     s->b.islandFlags = s->islands ? s->islands->flags : nullptr;
 }
 
+// Kinematic members can wake islands in this step: one moves or is always
+// active (its update leaves its time flag at -1), or a still one's flag is
+// below 0 (the update takes it to 0).
+bool IslandWakesPossible(const Scene* s) {
+    return !s->hostKinematic.empty() && (s->kin.live || s->kin.neg);
+}
+
 cudaError_t LaunchIslandStage(Scene* s, const StepParams& p, int maxAttempts, cudaStream_t q) {
     IslandBuffers& I = *s->islands;
     const int T = 128;
     const int nc = s->m.count + s->j.count;
-    if (!s->hostKinematic.empty() && nc > 0) {
+    const bool wakes = IslandWakesPossible(s) && nc > 0;  // else every wakeAt stays INT_MAX
+    if (wakes) {
         k_island_wakes<<<(nc + T - 1) / T, T, 0, q>>>(s->m, s->j, s->b, p, I.wakeAt);
         s->launchesPerStep++;
     }
-    if (s->b.count > 0) {
-        k_island_members<<<(s->b.count + T - 1) / T, T, 0, q>>>(s->b, p, I.wakeAt, I.candidates);
-        s->launchesPerStep++;
-    }
-    k_deactivate_objects<<<1, 256, 0, q>>>(I.flags, I.members, I.candidates, I.wakeAt, I.index, I.n, maxAttempts);
+    // at least one block: its last one runs DeactivateObjects
+    const int blocks = std::max(1, (s->b.count + 255) / 256);
+    k_island_members<<<blocks, 256, 0, q>>>(s->b, p, I.wakeAt, I.candidates, I.flags, I.members, I.index, I.n,
+                                            maxAttempts, I.done, wakes);
     s->launchesPerStep++;
     return cudaGetLastError();
 }
@@ -233,7 +312,7 @@ extern "C" bepugpu_status bepugpu_set_islands(bepugpu_context* c, int32_t id, co
     auto* I = new IslandBuffers();
     I->n = (int32_t)islands;
     I->nb = nb;
-    const size_t bytes = 4 * ((size_t)nb + 5 * (size_t)islands + 1);
+    const size_t bytes = 4 * ((size_t)nb + 5 * (size_t)islands + 2);
     cudaError_t e = cudaMalloc(&I->block, bytes);
     if (e != cudaSuccess) {
         delete I;
@@ -247,6 +326,7 @@ extern "C" bepugpu_status bepugpu_set_islands(bepugpu_context* c, int32_t id, co
     I->candidates = w + nb + 2 * (size_t)islands;
     I->wakeAt = w + nb + 3 * (size_t)islands;
     I->index = w + nb + 4 * (size_t)islands;
+    I->done = (unsigned int*)(I->index + 1);
     std::vector<int32_t> wake(islands, INT_MAX);
     auto fail = [&](cudaError_t err) {
         delete I;
@@ -258,7 +338,8 @@ extern "C" bepugpu_status bepugpu_set_islands(bepugpu_context* c, int32_t id, co
         (e = cudaMemcpyAsync(I->members, members.data(), 4 * (size_t)islands, cudaMemcpyHostToDevice, s->stream)) ||
         (e = cudaMemsetAsync(I->candidates, 0, 4 * (size_t)islands, s->stream)) ||
         (e = cudaMemcpyAsync(I->wakeAt, wake.data(), 4 * (size_t)islands, cudaMemcpyHostToDevice, s->stream)) ||
-        (e = cudaMemcpyAsync(I->index, &deactivation_index, 4, cudaMemcpyHostToDevice, s->stream)))
+        (e = cudaMemcpyAsync(I->index, &deactivation_index, 4, cudaMemcpyHostToDevice, s->stream)) ||
+        (e = cudaMemsetAsync(I->done, 0, 4, s->stream)))
         return fail(e);
     // every connection inside one island, checked against the scene's current contacts
     BodySoA bv = s->b;

@@ -322,6 +322,7 @@ struct Generator {
 }  // namespace
 
 struct bepuscene {
+    std::vector<float> friction;  // per body
     std::vector<bepugpu_shape> shapes;
     std::vector<bepugpu_body> bodies;
     std::vector<bepugpu_manifold> manifolds;
@@ -333,6 +334,7 @@ static bepuscene* Finish(Generator& g) {
     s->bodies.reserve(g.bodies.size());
     for (const Body& b : g.bodies) {
         s->bodies.push_back(MakeRecord(b));
+        s->friction.push_back(b.friction);
         bepugpu_shape sh;
         std::memset(&sh, 0, sizeof(sh));
         if (b.shape == kBox) {
@@ -408,14 +410,18 @@ int32_t bepuscene_make_pile(const bepuscene_pile_params* p, bepuscene** out) {
                 b.c[0] = x0 + ix * p->spacing + rng.uniform(-p->jitter, p->jitter);
                 b.c[2] = z0 + iz * p->spacing + rng.uniform(-p->jitter, p->jitter);
                 float pen = rng.uniform(0.f, p->settle_penetration);
-                b.c[1] = top + b.h[1] - pen;
-                top = b.c[1] + b.h[1];
+                if (p->drop_spacing > 0) {
+                    b.c[1] = .05f + .5f * p->size_max + iy * p->drop_spacing;
+                } else {
+                    b.c[1] = top + b.h[1] - pen;
+                    top = b.c[1] + b.h[1];
+                }
                 b.mass = p->density > 0 ? p->density * (8.f * b.h[0] * b.h[1] * b.h[2]) : p->mass;
                 b.friction = rng.uniform(p->friction_min, p->friction_max);
                 g.bodies.push_back(b);
             }
         }
-    g.Collide(0.f);
+    if (!(p->drop_spacing > 0)) g.Collide(0.f);
     *out = Finish(g);
     return BEPUGPU_OK;
 }
@@ -691,6 +697,10 @@ uint32_t bepuscene_params_size(int32_t kind) {
         case 2: return sizeof(bepuscene_chain_params);
         default: return 0;
     }
+}
+
+void bepuscene_body_friction(const bepuscene* s, float* friction) {
+    if (friction && !s->friction.empty()) std::memcpy(friction, s->friction.data(), s->friction.size() * sizeof(float));
 }
 
 void bepuscene_shapes(const bepuscene* s, bepugpu_shape* shapes) {

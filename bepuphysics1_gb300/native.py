@@ -66,7 +66,7 @@ PILE_PARAMS_DTYPE = np.dtype([
     ("nx", "<i4"), ("ny", "<i4"), ("nz", "<i4"), ("spacing", "<f4"), ("size_min", "<f4"), ("size_max", "<f4"),
     ("density", "<f4"), ("mass", "<f4"), ("jitter", "<f4"), ("friction_min", "<f4"), ("friction_max", "<f4"),
     ("ground_friction", "<f4"), ("ground_size", "<f4", 3), ("settle_penetration", "<f4"),
-    ("contact_distance", "<f4"), ("seed", "<u8"), ("narrow_phase", "<i4"),
+    ("contact_distance", "<f4"), ("seed", "<u8"), ("narrow_phase", "<i4"), ("drop_spacing", "<f4"),
 ], align=True)
 TOWER_PARAMS_DTYPE = np.dtype([
     ("body_count", "<i4"), ("tower_min", "<i4"), ("tower_max", "<i4"), ("sphere_fraction", "<f4"),
@@ -200,6 +200,7 @@ SCENE_EXPORTS = {
     "bepuscene_counts": (None, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "bepuscene_copy": (None, [_P, _P, _P, _P]),
     "bepuscene_shapes": (None, [_P, _P]),
+    "bepuscene_body_friction": (None, [_P, _P]),
     "bepuscene_params_size": (_U, [_I]),
     "bepuscene_free": (None, [_P]),
 }

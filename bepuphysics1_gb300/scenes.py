@@ -16,7 +16,7 @@ import numpy as np
 from . import native as N
 
 
-def _collect(handle, with_shapes: bool = False):
+def _collect(handle, with_shapes: bool = False, with_friction: bool = False):
     lib = N.load_scene_library()
     nb, nm, nj = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
     lib.bepuscene_counts(handle, ctypes.byref(nb), ctypes.byref(nm), ctypes.byref(nj))
@@ -26,7 +26,11 @@ def _collect(handle, with_shapes: bool = False):
     lib.bepuscene_copy(handle, N.ptr(bodies), N.ptr(manifolds), N.ptr(joints))
     shapes = np.zeros(nb.value, N.SHAPE_DTYPE)
     lib.bepuscene_shapes(handle, N.ptr(shapes))
+    friction = np.zeros(nb.value, np.float32)
+    lib.bepuscene_body_friction(handle, N.ptr(friction))
     lib.bepuscene_free(handle)
+    if with_friction:
+        return bodies, shapes, friction
     if with_shapes:
         return bodies, manifolds, joints, shapes
     return bodies, manifolds, joints
@@ -154,6 +158,25 @@ def pile_1k(seed: int = 1234):
 def pile_64k(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):
     return make_pile(nx=nx, ny=ny, nz=nz, spacing=2.0, size_min=0.5, size_max=1.5, density=1.0, jitter=0.1,
                      friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed)
+
+
+def dropped_pile(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64, drop_spacing: float = 2.0):
+    """pile_64k's boxes (sizes U(0.5, 1.5) per axis, density 1, friction
+    U(0.4, 0.8), horizontal jitter +-0.1) on a grid with drop_spacing between
+    layers too, at rest in the air above the static ground and without
+    manifolds: the pile before it settles.  Returns (bodies, shapes, per-body
+    friction)."""
+    lib = N.load_scene_library()
+    p = np.zeros(1, N.PILE_PARAMS_DTYPE)
+    lib.bepuscene_default_pile(N.ptr(p))
+    for k, v in dict(nx=nx, ny=ny, nz=nz, spacing=2.0, size_min=0.5, size_max=1.5, density=1.0, jitter=0.1,
+                     friction_min=0.4, friction_max=0.8, ground_size=(140.0, 1.0, 140.0), seed=seed,
+                     narrow_phase=1, drop_spacing=drop_spacing).items():
+        p[k] = v
+    h = ctypes.c_void_p()
+    st = lib.bepuscene_make_pile(N.ptr(p), ctypes.byref(h))
+    N.raise_for(st, "bepuscene_make_pile")
+    return _collect(h, with_friction=True)
 
 
 def pile_64k_collide(seed: int = 1234, nx: int = 64, ny: int = 16, nz: int = 64):

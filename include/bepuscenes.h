@@ -44,6 +44,9 @@ typedef struct bepuscene_pile_params {
     int32_t narrow_phase;      /* nonzero: every pair whose boxes are within contact_distance gets an
                                   empty BEPUGPU_MANIFOLD_GENERATED manifold (box first in box-sphere
                                   pairs) for the library's narrow phase to fill, instead of contacts */
+    float drop_spacing;        /* > 0: boxes not stacked but on a 3D grid, layer iy's centres at
+                                  drop_spacing * iy above the first layer, which starts 0.05 above the
+                                  ground, all at rest in the air and without manifolds (a pile to settle) */
 } bepuscene_pile_params;
 
 /* Towers: one scene of `body_count` bodies (boxes and spheres, 1 m, 1 kg) in
@@ -87,6 +90,9 @@ void bepuscene_copy(const bepuscene* s, bepugpu_body* bodies, bepugpu_manifold* 
 uint32_t bepuscene_params_size(int32_t kind);
 /* One collision shape per body: boxes and spheres; capsules have none. */
 void bepuscene_shapes(const bepuscene* s, bepugpu_shape* shapes);
+/* Each body's friction coefficient (static = kinetic), which a manifold between
+ * two bodies blends as their product (MaterialManager.cs:77-85). */
+void bepuscene_body_friction(const bepuscene* s, float* friction);
 void bepuscene_free(bepuscene* s);
 
 #ifdef __cplusplus

@@ -36,6 +36,7 @@ def _load():
             "oracle_last_child_solves": (ctypes.c_int64, [P]),
             "oracle_permutation_map": (ctypes.c_int64, [ctypes.c_int64, ctypes.c_int64, I]),
             "oracle_prime_count": (I, []),
+            "oracle_permutation_check": (ctypes.c_int64, [ctypes.c_int64, I, P]),
             "oracle_colour": (I, [P, I, P, I, P, I, P, P]),
             "oracle_set_shapes": (I, [P, P, I]),
             "oracle_set_islands": (I, [P, P, P, I, I]),
@@ -61,6 +62,13 @@ def permutation_map(permutation_index: int, index: int, set_size: int) -> int:
 
 def prime_count() -> int:
     return _load().oracle_prime_count()
+
+
+def permutation_check(iterations: int, set_size: int):
+    """(first permutation index that is not a permutation or -1, distinct permutations)."""
+    d = ctypes.c_int64()
+    k = _load().oracle_permutation_check(iterations, set_size, ctypes.byref(d))
+    return k, d.value
 
 
 def colour(bodies, manifolds, joints=None):

@@ -1737,6 +1737,32 @@ int64_t oracle_permutation_map(int64_t permutation_index, int64_t index, int32_t
 
 int32_t oracle_prime_count(void) { return kPrimeCount; }
 
+// PermutationTestDemo.cs:82-127: for `iterations` permutation indices from 0,
+// GetMappedIndex over [0, set_size) must be a permutation.  Returns the first
+// permutation index that is not one, or -1; *distinct receives how many
+// different permutations appeared.
+int64_t oracle_permutation_check(int64_t iterations, int32_t set_size, int64_t* distinct) {
+    PermutationMapper pm;
+    std::vector<int32_t> seen((size_t)set_size, -1);
+    std::vector<std::vector<int32_t>> perms;
+    std::vector<int32_t> cur((size_t)set_size);
+    for (int64_t k = 0; k < iterations; k++) {
+        pm.SetIndex(k);
+        for (int32_t i = 0; i < set_size; i++) {
+            const int64_t m = pm.Map(i, set_size);
+            if (m < 0 || m >= set_size || seen[(size_t)m] == (int32_t)(k & 0x7fffffff)) return k;
+            seen[(size_t)m] = (int32_t)(k & 0x7fffffff);
+            cur[(size_t)i] = (int32_t)m;
+        }
+        if (distinct) perms.push_back(cur);
+    }
+    if (distinct) {
+        std::sort(perms.begin(), perms.end());
+        *distinct = (int64_t)(std::unique(perms.begin(), perms.end()) - perms.begin());
+    }
+    return -1;
+}
+
 // Restatement of the library's colouring (deterministic greedy in list order,
 // conflicts only through dynamic bodies; colour-sorted order is stable).  A
 // GROUP_CONTINUATION record is solved inside its group's visit: it takes the

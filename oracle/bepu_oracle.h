@@ -47,6 +47,9 @@ int64_t oracle_last_child_solves(oracle_space* s);
 /* PermutationMapper (BEPUutilities/PermutationMapper.cs:27-44,113-127). */
 int64_t oracle_permutation_map(int64_t permutation_index, int64_t index, int32_t set_size);
 int32_t oracle_prime_count(void);
+/* PermutationTestDemo's check: the first permutation index whose mapping is not
+ * a permutation of [0, set_size), or -1; *distinct: different permutations seen. */
+int64_t oracle_permutation_check(int64_t iterations, int32_t set_size, int64_t* distinct);
 
 /* Restatement of the library's deterministic greedy colouring: returns the
  * colour count, or -1 on error. */

@@ -30,6 +30,16 @@ def test_permutation_mapper_bijection():
         assert block2 == set(range(set_size))
 
 
+def test_permutation_demo_full_run():
+    # PermutationTestDemo.cs:88-115 as the reference runs it: 150,000 permutation
+    # indices, set size 250, each mapping a permutation (the demo throws otherwise).
+    first_bad, distinct = oracle.permutation_check(150_000, 250)
+    assert first_bad == -1
+    # The mapping is p * (i + k) mod 250 with p one of the 503 primes (all odd and
+    # none a multiple of 5, so units mod 250): at most 100 multipliers x 250 shifts.
+    assert 0 < distinct <= 100 * 250
+
+
 def test_permutation_mapper_formula():
     # GetMappedIndex = (index * prime + prime * permutationIndex) mod setSize
     primes0 = 818660357
