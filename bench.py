@@ -352,6 +352,13 @@ def dropped_section(args, ctx, local, pg):
     from bepuphysics1_gb300.solver import profile_step
     prof = profile_step(solved, DT, flags)
     ms = statistics.mean(step_ms)
+    launches = int(solved.last_step_launches())
+    # the same steps in the persistent cooperative kernel (grid barriers between sweeps)
+    solved.set_mode(N.MODE_PERSISTENT)
+    for _ in range(3):
+        solved.step(DT, flags)
+    pers_ms, _ = timed_steps(solved, args.steps, flush, flags)
+    solved.set_mode(N.MODE_GRAPH)
     out = {"workload": "pile_64k dropped from a 64 x 16 x 64 grid (2 m spacing) and settled for "
                        f"{args.dropped_steps} steps on the device",
            "value": cips / (ms / 1000.0), "unit": "contact-iters/s", "ms_per_step": ms,
@@ -359,7 +366,7 @@ def dropped_section(args, ctx, local, pg):
            "bodies": int(nb), "manifolds": int(len(gm)), "contacts": contacts,
            "colours": int(solved.colouring()[2]), "islands": int(isl.max() + 1) if (isl >= 0).any() else 0,
            "largest_island": int(sizes.max()), "group_ctas": int(prof["groups"]),
-           "gpu_launches_per_step": int(solved.last_step_launches()),
+           "gpu_launches_per_step": launches, "persistent_ms_per_step": statistics.mean(pers_ms),
            "settle": {"steps": args.dropped_steps, "seconds": settle_s, "pair_set_changes": changes,
                       "loop_ms_median": statistics.median(loop_ms),
                       "loop_ms_last20_median": statistics.median(loop_ms[-20:]),

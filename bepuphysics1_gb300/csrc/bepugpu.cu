@@ -455,9 +455,27 @@ __global__ void k_warm(ManifoldSoA m, BodySoA b, int begin, int end) {
     int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (s < end) WarmSlot(m, b, s);
 }
+// A colour sweep: the visit's prestep lanes load before the previous sweep
+// ends (they do not change during the sweeps); state, impulses and bodies after.
 __global__ void k_solve(ManifoldSoA m, BodySoA b, StepParams p, int begin, int end) {
-    int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (s < end) SolveSlot(m, b, s, p);
+    LetDependentsLaunch();
+    const int s = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    SolveLanes L;
+    int4 h = make_int4(0, 0, 0, 0);
+    if (s < end) {
+        h = m.head[s];
+        const int count = h.z & 0xff;
+        LoadSolveLanes(m, s, count, count > 0, L);
+    }
+    WaitForPrerequisites();
+    if (s >= end) return;
+    uint2 state = m.state[s];
+    if (!(state.x & kGroupActive)) return;
+    BodyState A, B;
+    LoadPair(b, h, A, B);
+    SolveManifold(m, s, A, B, state, h.z & 0xff, p, &L);
+    StorePair(b, h, state.x, A, B);
+    m.state[s] = state;
 }
 
 // Joints (joints_device.cuh).  A colour's joints and manifolds touch different
@@ -503,6 +521,8 @@ __global__ void k_warm_mixed(ManifoldSoA m, BodySoA b, JointSoA j, int mb, int m
 }
 template <bool kAdded>
 __global__ void k_solve_mixed(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, int mb, int me, int jb, int je) {
+    LetDependentsLaunch();
+    WaitForPrerequisites();
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < je - jb) SolveJointSlot<kAdded>(j, b, jb + t, p);
     else if (mb + t - (je - jb) < me) SolveSlot(m, b, mb + t - (je - jb), p);
@@ -936,6 +956,22 @@ bepugpu_status Scene::RebuildSweepBodies(Context* ctx) {
     return BEPUGPU_OK;
 }
 
+// A sweep launch that may start while the sweep before it finishes: the
+// kernel waits for it (griddepcontrol.wait) before reading its results.
+template <typename... KArgs, typename... Args>
+static cudaError_t LaunchAfterSweep(void (*kernel)(KArgs...), int grid, int block, cudaStream_t q, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.stream = q;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t flags) {
     if (graphExec) { cudaGraphExecDestroy(graphExec); graphExec = nullptr; }
     const int T = 128;
@@ -1072,10 +1108,10 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
                 int b0 = manifoldOffsets[c], b1 = manifoldOffsets[c + 1];
                 int j0 = nj ? jointOffsets[c] : 0, j1 = nj ? jointOffsets[c + 1] : 0;
                 if (j1 > j0) {
-                    solveMixed<<<Blocks(b1 - b0 + j1 - j0, T), T, 0, stream>>>(ms, b, js, p, b0, b1, j0, j1);
+                    CK(LaunchAfterSweep(solveMixed, Blocks(b1 - b0 + j1 - j0, T), T, stream, ms, b, js, p, b0, b1, j0, j1));
                     launchesPerStep++;
                 } else if (b1 > b0) {
-                    k_solve<<<Blocks(b1 - b0, T), T, 0, stream>>>(ms, b, p, b0, b1);
+                    CK(LaunchAfterSweep(k_solve, Blocks(b1 - b0, T), T, stream, ms, b, p, b0, b1));
                     launchesPerStep++;
                 }
             }
@@ -1537,8 +1573,14 @@ bepugpu_status bepugpu_upload_constraints(bepugpu_context* c, int32_t id, const 
     // on the sweep path.
     GroupPolicy pol = s->policy;
     if (s->mode == BEPUGPU_MODE_PERSISTENT) pol.enabled = false;
+    // kind of an entry for the slot order inside a colour: a joint's record
+    // type, a manifold's nonconvex flag and contact count
+    std::vector<int32_t> kind(nm + nj);
+    for (uint32_t u = 0; u < nj; u++) kind[u] = joints[u].type;
+    for (uint32_t i = 0; i < nm; i++) kind[nj + i] = 64 + (nonConvex[i] ? 8 : 0) + std::max(0, man[i].contact_count);
     PlanGroups(pol, a.data(), bb.data(), s->colouring.colour.data(), (int32_t)nj, (int32_t)nm,
-               s->hostDynamic.data(), nb, s->colouring.colours, s->groupPlan, nonConvex.data());
+               s->hostDynamic.data(), nb, s->colouring.colours, s->groupPlan, nonConvex.data(), kind.data(),
+               follows.data());
     const GroupPlan& plan = s->groupPlan;
     s->manifoldOffsets = plan.globalOffsets;
     s->jointOffsets = plan.jointGlobalOffsets;

@@ -146,7 +146,8 @@ struct GroupPlan {
 constexpr size_t kGroupSmemBudget = 200 * 1024;
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
                 int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan,
-                const uint8_t* nonConvex = nullptr);
+                const uint8_t* nonConvex = nullptr, const int32_t* entryKind = nullptr,
+                const uint8_t* follows = nullptr);
 bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
 // Joints (joints.cu): record checks, upload into the scene's joint slots, and
 // the accumulated impulses back into records.

@@ -62,9 +62,35 @@ struct UnionFind {
 // range, each in colour-major order.  When a group holds a NONCONVEX manifold
 // (nonConvex[i] != 0; null: none), every group's shared manifold lanes have
 // room for contact friction (plan.nonConvexLanes, GroupManifoldLanes).
+//
+// Inside a colour no two entries share a dynamic body, so their order does not
+// change a sweep's result: entries of a colour take their slots sorted by
+// entryKind[u] (null: list order), stably, so that a warp's threads run the same
+// branch of the joint and manifold code.  follows[u] != 0 keeps a joint's
+// continuation records right after it (they share its kind).
 void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, const int32_t* colour, int32_t nj,
                 int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan,
-                const uint8_t* nonConvex) {
+                const uint8_t* nonConvex, const int32_t* entryKind, const uint8_t* follows) {
+    // A colour's entries (ascending) regrouped: units (an entry and the entries
+    // that follow it) stably sorted by the unit's kind.
+    auto byKind = [&](std::vector<int32_t>& list) {
+        if (!entryKind || list.size() < 2) return;
+        std::vector<std::pair<int32_t, int32_t>> units;  // (first index in list, length)
+        for (int32_t i = 0; i < (int32_t)list.size(); i++) {
+            const int32_t u = list[i];
+            if (follows && u < nj && follows[u] && !units.empty()) units.back().second++;
+            else units.push_back({i, 1});
+        }
+        std::stable_sort(units.begin(), units.end(), [&](const std::pair<int32_t, int32_t>& x,
+                                                         const std::pair<int32_t, int32_t>& y) {
+            return entryKind[list[x.first]] < entryKind[list[y.first]];
+        });
+        std::vector<int32_t> out;
+        out.reserve(list.size());
+        for (auto& un : units)
+            for (int32_t k = 0; k < un.second; k++) out.push_back(list[un.first + k]);
+        list.swap(out);
+    };
     plan = GroupPlan();
     const int32_t n = nj + nm;
     std::vector<int32_t> groupOf(n, -1);  // per updateable
@@ -163,6 +189,7 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
         for (int32_t u = 0; u < n; u++)
             if (groupOf[u] < 0) byColour[colour[u]].push_back(u);
         for (int32_t c = 0; c < colours; c++) {
+            byKind(byColour[c]);
             plan.globalOffsets[c] = slot;
             plan.jointGlobalOffsets[c] = jslot;
             for (int32_t u : byColour[c]) {
@@ -200,8 +227,16 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
         for (int32_t u : mMembers[gId]) gc = std::max(gc, colour[u] + 1);
         for (int32_t u : jMembers[gId]) gc = std::max(gc, colour[u] + 1);
         std::vector<std::vector<int32_t>> mByColour(gc), jByColour(gc);
-        for (int32_t u : mMembers[gId]) mByColour[colour[u]].push_back(u - nj);
         for (int32_t u : jMembers[gId]) jByColour[colour[u]].push_back(u);
+        {
+            std::vector<std::vector<int32_t>> ms(gc);  // manifolds as list entries, sorted by kind
+            for (int32_t u : mMembers[gId]) ms[colour[u]].push_back(u);
+            for (int32_t c = 0; c < gc; c++) {
+                byKind(ms[c]);
+                for (int32_t u : ms[c]) mByColour[c].push_back(u - nj);
+                byKind(jByColour[c]);
+            }
+        }
         d.cCount = gc;
         d.mBegin = slot;
         d.cBegin = (int32_t)plan.colourOffsets.size();

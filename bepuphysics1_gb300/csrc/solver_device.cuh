@@ -963,13 +963,45 @@ __device__ __forceinline__ void WarmStartManifold(const ManifoldSoA& m, int s, B
     }
 }
 
+// Programmatic dependent launch: a sweep kernel lets the next one start its
+// preamble (griddepcontrol.launch_dependents) and waits for the previous one's
+// completion and memory (griddepcontrol.wait) before it reads what that one
+// writes.  Both are no-ops for a kernel launched without the attribute.
+__device__ __forceinline__ void LetDependentsLaunch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void WaitForPrerequisites() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// The prestep products a solve visit reads; none of them change during the
+// sweeps, so a sweep kernel may load them before the sweep it follows ends.
+struct SolveLanes {
+    float4 J0[4], J1[4], J2[4];
+    float4 S0, S1, L1, L2, A1, A2, B1, B2, LEV;
+};
+__device__ __forceinline__ void LoadSolveLanes(const ManifoldSoA& m, int s, int count, bool friction,
+                                               SolveLanes& L) {
+    const int cap = m.capacity;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (k < count) {
+            L.J0[k] = m.pj0[k * cap + s];
+            L.J1[k] = m.pj1[k * cap + s];
+            L.J2[k] = m.pj2[k * cap + s];
+        }
+    }
+    if (friction) {
+        L.S0 = m.s0[s]; L.S1 = m.s1[s]; L.L1 = m.saxis[s]; L.L2 = m.s3[s];
+        L.A1 = m.s4[s]; L.A2 = m.s5[s]; L.B1 = m.s6[s]; L.B2 = m.s7[s];
+        L.LEV = m.lever[s];
+    }
+}
+
 // One solver visit of a manifold: Solver.UnsafeSolveIteration (Solver.cs:285-314)
 // -> ConvexContactManifoldConstraint.SolveIteration (:199-212) ->
 // SolverGroup.SolveUpdateable (SolverGroup.cs:117-150) on each child.
 // Children solve strictly in order: they are a Gauss-Seidel sequence.
+// pre: the visit's lanes already loaded (LoadSolveLanes with friction = count > 0), or null.
 template <class Body>
 __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body& A, Body& B, uint2& state,
-                                              int count, const StepParams& p) {
+                                              int count, const StepParams& p, const SolveLanes* pre = nullptr) {
     const int cap = m.capacity;
     uint32_t st = state.x, zeros = state.y;
     // UnsafeSolveIteration on the group
@@ -985,22 +1017,13 @@ __device__ __forceinline__ void SolveManifold(const ManifoldSoA& m, int s, Body&
     // Every load of the visit is issued before the sequential solves start.
     float4 acc4 = m.penacc[s];
     float accs[4] = {acc4.x, acc4.y, acc4.z, acc4.w};
-    float4 J0[4], J1[4], J2[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        if (k < count) {
-            J0[k] = m.pj0[k * cap + s];
-            J1[k] = m.pj1[k * cap + s];
-            J2[k] = m.pj2[k * cap + s];
-        }
-    }
+    SolveLanes Lv;
+    if (pre) Lv = *pre;
+    else LoadSolveLanes(m, s, count, (st & (kSlidingBit | kTwistBit)) != 0, Lv);
+    const float4 *J0 = Lv.J0, *J1 = Lv.J1, *J2 = Lv.J2;
     float4 f = m.fricacc[s];
-    float4 S0, S1, L1, L2, A1, A2, B1, B2, LEV;
-    if (st & (kSlidingBit | kTwistBit)) {
-        S0 = m.s0[s]; S1 = m.s1[s]; L1 = m.saxis[s]; L2 = m.s3[s];
-        A1 = m.s4[s]; A2 = m.s5[s]; B1 = m.s6[s]; B2 = m.s7[s];
-        LEV = m.lever[s];
-    }
+    const float4 S0 = Lv.S0, S1 = Lv.S1, L1 = Lv.L1, L2 = Lv.L2, A1 = Lv.A1, A2 = Lv.A2, B1 = Lv.B1, B2 = Lv.B2,
+                 LEV = Lv.LEV;
     // SolveUpdateable bookkeeping for child c (its zero-impulse nibble) given
     // its |impulse|; `bit` is its activity bit.
     auto accountBit = [&](int c, uint32_t bit, float r) {
