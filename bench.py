@@ -295,8 +295,8 @@ def sweep_section(args, ctx, local, pg, peak, peak_kind):
 def dropped_section(args, ctx, local, pg):
     """Config 2 as written: pile_64k's 65,536 boxes on a 64 x 16 x 64 grid
     with 2 m between layers too, dropped onto the ground and settled with the
-    device broad phase, the pair records (bepuphysics1_gb300/pairs.py), the
-    device narrow phase and the solver.  120 steps (2 s) are not enough for
+    device broad phase and pair bookkeeping (bepugpu_update_pairs: records
+    and colouring on the device), the device narrow phase and the solver.  120 steps (2 s) are not enough for
     the top layers, which fall about 16 m, to land: the state after 120 steps
     is reported and the pile settles for --dropped-steps in all.  Then the
     settled heap's pair set, its contacts regenerated by the narrow phase each
@@ -304,14 +304,13 @@ def dropped_section(args, ctx, local, pg):
     import torch
     from bepuphysics1_gb300 import native as N
     from bepuphysics1_gb300 import scenes
-    from bepuphysics1_gb300.pairs import PairRecords
     from bepuphysics1_gb300.solver import GpuSpace, islands_of
     bodies, shapes, friction = scenes.dropped_pile()
     nb = len(bodies)
     space = GpuSpace(ctx, bodies, None, capacity=(nb, 8 * nb, 0), shapes=shapes)
-    records = PairRecords(friction, shapes)
+    space.set_materials(np.stack([friction, friction, np.zeros_like(friction)], 1))
     flags = N.STEP_ALL | N.STEP_COLLIDE
-    loop_ms, changes, after120 = [], 0, None
+    loop_ms, counts, after120 = [], [], None
     t0 = time.perf_counter()
     for step in range(args.dropped_steps):
         if step == 120:
@@ -321,17 +320,13 @@ def dropped_section(args, ctx, local, pg):
             after120 = {"speed_p50": float(np.median(sp120)), "speed_p99": float(np.percentile(sp120, 99)),
                         "top": float(b120["position"][d120][:, 1].max())}
         ts = time.perf_counter()
-        pairs = space.broad_phase(DT)
-        current = space.download_constraints(records.manifolds.copy())[0] if len(records.manifolds) else None
-        if records.update(pairs, current):
-            changes += 1
-            space.upload_constraints(records.manifolds)
+        counts.append(space.update_pairs(DT))  # pair bookkeeping and recolouring on the device
         space.step(DT, flags)
         ctx.synchronize()
         loop_ms.append(1000.0 * (time.perf_counter() - ts))
     settle_s = time.perf_counter() - t0
     gb = space.download_bodies(bodies.copy())
-    gm, _ = space.download_constraints(records.manifolds.copy())
+    gm, _ = space.download_constraints()
     space.close()
     dyn = gb["is_dynamic"] == 1
     speed = np.linalg.norm(gb["linear_velocity"][dyn], axis=1)
@@ -367,12 +362,12 @@ def dropped_section(args, ctx, local, pg):
            "colours": int(solved.colouring()[2]), "islands": int(isl.max() + 1) if (isl >= 0).any() else 0,
            "largest_island": int(sizes.max()), "group_ctas": int(prof["groups"]),
            "gpu_launches_per_step": launches, "persistent_ms_per_step": statistics.mean(pers_ms),
-           "settle": {"steps": args.dropped_steps, "seconds": settle_s, "pair_set_changes": changes,
+           "settle": {"steps": args.dropped_steps, "seconds": settle_s, "manifolds_final": counts[-1],
                       "loop_ms_median": statistics.median(loop_ms),
                       "loop_ms_last20_median": statistics.median(loop_ms[-20:]),
                       "after_120_steps": after120,
-                      "what": "per step: device broad phase, pair records (download, diff, upload and "
-                              "recolour when the set changed), narrow phase + solver step; host wall clock",
+                      "what": "per step: bepugpu_update_pairs (device broad phase, pair records and "
+                              "recolouring on the device), then the narrow phase + solver step; host wall clock",
                       "speed_p50_after": float(np.median(speed)), "speed_p99_after": float(np.percentile(speed, 99)),
                       "top_after": float(gb["position"][dyn][:, 1].max())},
            "parity": "the same loop bit-exact against the oracle on a 5 x 4 x 5 drop (tests/test_gpu_settle.py)",

@@ -697,6 +697,7 @@ Scene::~Scene() {
         if (e) cudaEventDestroy(e);
     ReleaseBroadPhase(this);
     ReleaseIslands(this);
+    ReleasePairs(this);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -1459,10 +1460,11 @@ bepugpu_status bepugpu_upload_bodies(bepugpu_context* c, int32_t id, const bepug
         ctx->SetError("body count %u exceeds scene capacity %u", n, s->maxBodies);
         return BEPUGPU_INVALID_ARGUMENT;
     }
-    if (s->islands) {  // the islands are set again for the new bodies
+    if (s->islands || s->pairs) {  // islands and materials are set again for the new bodies
         if (s->asyncPending) CK(cudaStreamSynchronize(s->stream));
         s->asyncPending = false;
         ReleaseIslands(s);
+        ReleasePairs(s);
         s->version++;
     }
     s->hostLinDamp.resize(n); s->hostAngDamp.resize(n); s->hostLocalM33.resize(n); s->hostDamp.resize(n);

@@ -25,6 +25,17 @@ struct BatchEngine;
 struct Scene;
 struct BroadPhaseBuffers;
 void ReleaseBroadPhase(Scene* s);  // broadphase.cu
+struct Context;
+// broadphase.cu: the pair set into device memory (sorted 64-bit keys, lower
+// body << 32 | higher), the ascending bitonic sort of 64-bit keys it uses
+// (`padded` a power of two from PaddedSize), and a filler of largest keys.
+bepugpu_status RunBroadPhase(Context* ctx, Scene* s, float dt, unsigned& found);
+const unsigned long long* BroadPhasePairs(const Scene* s);
+size_t PaddedSize(size_t n);
+void SortKeys(unsigned long long* keys, size_t padded, cudaStream_t st);
+void FillKeys(unsigned long long* keys, size_t n, cudaStream_t st);
+struct PairBuffers;                // pairs.cu
+void ReleasePairs(Scene* s);
 struct IslandBuffers;               // islands.cu
 struct StepParams;
 void ReleaseIslands(Scene* s);
@@ -348,6 +359,7 @@ struct Scene {
     bool persistentAdded = false;  // the persistent variant persistentBlocks was sized for
     BroadPhaseBuffers* broadPhase = nullptr;  // device buffers of bepugpu_broad_phase (broadphase.cu)
     IslandBuffers* islands = nullptr;         // bepugpu_set_islands (islands.cu); null: every island awake
+    PairBuffers* pairs = nullptr;             // bepugpu_update_pairs (pairs.cu): materials and scratch
     // With islands the deactivation stage runs first, in its own launches
     // (LaunchIslandStage); the other stages then run without it.
     uint32_t StageFlags(uint32_t flags) const {

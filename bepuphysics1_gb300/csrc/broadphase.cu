@@ -192,6 +192,8 @@ __global__ void __launch_bounds__(kSortBlock) k_bitonic_tile(unsigned long long*
     keys[base + t + kSortBlock] = s[t + kSortBlock];
 }
 
+}  // namespace
+
 // The power of two at or above n, at least one tile.
 size_t PaddedSize(size_t n) {
     size_t p = kSortTile;
@@ -210,6 +212,13 @@ void SortKeys(unsigned long long* keys, size_t padded, cudaStream_t st) {
         k_bitonic_tile<<<(unsigned)(padded / kSortTile), kSortBlock, 0, st>>>(keys, (int)k, (int)k, kSortTile / 2);
     }
 }
+
+// keys[0, n) set to the largest key (sorts last).
+void FillKeys(unsigned long long* keys, size_t n, cudaStream_t st) {
+    if (n) k_fill_keys<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(keys, n);
+}
+
+namespace {
 
 // BoundingBox.Intersects (BoundingBox.cs:58-66) and the NoBroadPhase rule of
 // two kinematic bodies.
@@ -318,24 +327,16 @@ cudaError_t Grow(T*& p, size_t& cap, size_t want) {
 
 using namespace bepugpu;
 
-extern "C" bepugpu_status bepugpu_broad_phase(bepugpu_context* c, int32_t id, float dt, int32_t* pairs,
-                                              uint32_t max_pairs, uint32_t* pair_count) {
-    NvtxRange range("bepugpu_broad_phase");
-    auto* ctx = reinterpret_cast<Context*>(c);
-    if (!ctx) return BEPUGPU_INVALID_ARGUMENT;
-    cudaSetDevice(ctx->device);
-    Scene* s = FindScene(ctx, id);
-    if (!s) return SceneMissing(ctx, id);
-    if (!pair_count || (max_pairs && !pairs) || !(dt >= 0) || !std::isfinite(dt)) {
-        ctx->SetError("broad_phase: pair_count is required, pairs when max_pairs > 0, and dt >= 0 finite");
-        return BEPUGPU_INVALID_ARGUMENT;
-    }
+namespace bepugpu {
+// The broad phase of scene s into s->broadPhase->pairs: `found` keys
+// (lower << 32 | higher), ascending.  The stream is synchronised.
+bepugpu_status RunBroadPhase(Context* ctx, Scene* s, float dt, unsigned& found) {
+    found = 0;
     const int n = s->b.count;
     if ((size_t)n != s->hostShapes.size()) {
         ctx->SetError("broad_phase needs one shape for each of the %d bodies (bepugpu_upload_shapes)", n);
         return BEPUGPU_INVALID_OPERATION;
     }
-    *pair_count = 0;
     if (n < 2) return BEPUGPU_OK;
     if (s->asyncPending) {
         CK(cudaStreamSynchronize(s->stream));
@@ -371,7 +372,6 @@ extern "C" bepugpu_status bepugpu_broad_phase(bepugpu_context* c, int32_t id, fl
                                                                                     sortedEntries - entries);
     SortKeys(bp.keys, sortedEntries, st);
     CK(cudaGetLastError());
-    unsigned found = 0;
     for (int attempt = 0; attempt < 2; attempt++) {
         CK(cudaMemsetAsync(bp.words + kWPairs, 0, sizeof(unsigned), st));
         if (entries)
@@ -397,6 +397,31 @@ extern "C" bepugpu_status bepugpu_broad_phase(bepugpu_context* c, int32_t id, fl
         SortKeys(bp.pairs, sortedPairs, st);
         CK(cudaGetLastError());
     }
+    return BEPUGPU_OK;
+}
+
+const unsigned long long* BroadPhasePairs(const Scene* s) { return s->broadPhase ? s->broadPhase->pairs : nullptr; }
+}  // namespace bepugpu
+
+extern "C" bepugpu_status bepugpu_broad_phase(bepugpu_context* c, int32_t id, float dt, int32_t* pairs,
+                                              uint32_t max_pairs, uint32_t* pair_count) {
+    NvtxRange range("bepugpu_broad_phase");
+    auto* ctx = reinterpret_cast<Context*>(c);
+    if (!ctx) return BEPUGPU_INVALID_ARGUMENT;
+    cudaSetDevice(ctx->device);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    if (!pair_count || (max_pairs && !pairs) || !(dt >= 0) || !std::isfinite(dt)) {
+        ctx->SetError("broad_phase: pair_count is required, pairs when max_pairs > 0, and dt >= 0 finite");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    *pair_count = 0;
+    unsigned found = 0;
+    bepugpu_status bst = RunBroadPhase(ctx, s, dt, found);
+    if (bst != BEPUGPU_OK) return bst;
+    if (!found) return BEPUGPU_OK;
+    const cudaStream_t st = s->stream;
+    BroadPhaseBuffers& bp = *s->broadPhase;
     const uint32_t nw = std::min<uint32_t>(found, max_pairs);
     std::vector<unsigned long long> host(nw);
     if (nw) {

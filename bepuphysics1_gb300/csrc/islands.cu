@@ -22,6 +22,7 @@
 #include "../../include/bepugpu.h"
 #include "bepugpu_internal.h"
 #include "joints_device.cuh"
+#include "scan_device.cuh"
 #include "solver_device.cuh"
 
 namespace bepugpu {
@@ -69,29 +70,6 @@ __global__ void k_island_wakes(ManifoldSoA m, JointSoA j, BodySoA b, StepParams 
     }
     WakeThrough(b, h.x, h.y, p, wakeAt);
     WakeThrough(b, h.y, h.x, p, wakeAt);
-}
-
-// Inclusive sum over the block (blockDim.x a multiple of 32, at most 1,024).
-__device__ __forceinline__ int BlockInclusiveSum(int v, int* warpSums) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, v, o);
-        if (lane >= o) v += u;
-    }
-    if (lane == 31) warpSums[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-        int w = lane < warps ? warpSums[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += u;
-        }
-        if (lane < warps) warpSums[lane] = w;
-    }
-    __syncthreads();
-    const int before = warp ? warpSums[warp - 1] : 0;
-    __syncthreads();
-    return v + before;
 }
 
 // The wakes (island.IsActive = true, allowDeactivation = false), then

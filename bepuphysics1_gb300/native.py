@@ -150,6 +150,8 @@ GPU_EXPORTS = {
     "bepugpu_upload_shapes": (_I, [_P, _I, _P, _U]),
     "bepugpu_broad_phase": (_I, [_P, _I, _F, _P, _U, ctypes.POINTER(_U)]),
     "bepugpu_set_islands": (_I, [_P, _I, _P, _U, _P, _U, _I]),
+    "bepugpu_set_materials": (_I, [_P, _I, _P, _U]),
+    "bepugpu_update_pairs": (_I, [_P, _I, _F, ctypes.POINTER(_U)]),
     "bepugpu_get_islands": (_I, [_P, _I, _P, _U, ctypes.POINTER(_I)]),
     "bepugpu_step_host": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),
     "bepugpu_step_state": (_I, [_P, _I, _P, _U, _P, _U, ctypes.c_float, _U]),

@@ -148,6 +148,21 @@ class GpuSpace:
         self.manifold_count = len(manifolds)
         self.joint_count = len(joints)
 
+    def set_materials(self, materials: np.ndarray):
+        """bepugpu_set_materials: per body (kinetic friction, static friction,
+        bounciness), blended by product into new pairs' records."""
+        mat = np.ascontiguousarray(materials, np.float32).reshape(-1, 3)
+        self.ctx.check(self.ctx.lib.bepugpu_set_materials(self.ctx.handle, self.id, N.ptr(mat), len(mat)))
+
+    def update_pairs(self, dt: float) -> int:
+        """bepugpu_update_pairs: the manifold list follows the broad phase's pair
+        set on the device (new GENERATED records, ended pairs dropped, recoloured).
+        Returns the new manifold count."""
+        n = ctypes.c_uint32()
+        self.ctx.check(self.ctx.lib.bepugpu_update_pairs(self.ctx.handle, self.id, float(dt), ctypes.byref(n)))
+        self.manifold_count = n.value
+        return n.value
+
     def update_bodies(self, bodies: np.ndarray):
         """bepugpu_update_bodies: new position, orientation and velocities only."""
         bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 9
+#define BEPUGPU_ABI_VERSION 10
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -463,6 +463,27 @@ bepugpu_status bepugpu_set_islands(bepugpu_context* ctx, int32_t scene, const in
  * (synchronises the scene's stream). */
 bepugpu_status bepugpu_get_islands(bepugpu_context* ctx, int32_t scene, uint32_t* island_flags,
                                    uint32_t islands, int32_t* deactivation_index);
+
+/* The narrow phase's pair bookkeeping on the device (NarrowPhase.cs:143-178
+ * adds a pair handler for a new overlap, :254-332 drops one whose bounding
+ * boxes stopped overlapping), for scenes whose constraints are all GENERATED
+ * manifolds: bepugpu_update_pairs runs the broad phase (as
+ * bepugpu_broad_phase) and makes the manifold list follow its pair set with
+ * no host round trip.  The records of pairs still reported keep their
+ * contacts, impulses and relative order; records of pairs that ended go;
+ * each new pair gets an empty GENERATED record after them, in ascending pair
+ * order -- ACTIVE | SOLVER_RULE, the box first in a box-sphere pair,
+ * NONCONVEX when a sphere takes part, the two bodies' materials blended by
+ * product (MaterialManager.cs:77-85) -- exactly the records a host that
+ * downloaded, diffed and uploaded them with bepugpu_upload_constraints would
+ * give.  The list is then coloured on the device with the same colouring
+ * (greedy in list order), and every manifold goes to the colour-sweep path;
+ * islands are cleared.  Needs bepugpu_upload_shapes and bepugpu_set_materials
+ * (three floats a body: kinetic friction, static friction, bounciness).
+ * *manifold_count receives the new record count; more pairs than the scene's
+ * manifold capacity return BEPUGPU_INVALID_OPERATION with nothing changed. */
+bepugpu_status bepugpu_set_materials(bepugpu_context* ctx, int32_t scene, const float* materials, uint32_t count);
+bepugpu_status bepugpu_update_pairs(bepugpu_context* ctx, int32_t scene, float dt, uint32_t* manifold_count);
 
 /* Rewrites manifold records in place without recolouring.  Body pairs and the
  * manifold count must be those of the last bepugpu_upload_constraints (checked
