@@ -195,12 +195,22 @@ __global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, 
     }
     for (int q = 0; q < 4; q++) k.orientation[q] = r.orientation[q];
 }
+// State records cross the host link (records in page-locked host memory are
+// read and written in place), so a block moves its records as one contiguous
+// run of 16-byte words through shared memory: consecutive threads, consecutive words.
+constexpr int kStateBlock = 128;
+
 // State records into the body lanes and the kept records (bepugpu_step_state).
-__global__ void k_update_body_state_records(const bepugpu_body_state* __restrict__ in, int n, BodySoA b,
-                                            bepugpu_body* kept) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4* w4 = (const float4*)(in + i);  // 64-byte records: four 16-byte loads
+__global__ void __launch_bounds__(kStateBlock) k_update_body_state_records(const bepugpu_body_state* __restrict__ in,
+                                                                           int n, BodySoA b, bepugpu_body* kept) {
+    __shared__ float4 buf[4 * kStateBlock];
+    const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, n - first);
+    const float4* src = (const float4*)(in + first);
+    for (int k = threadIdx.x; k < 4 * rows; k += kStateBlock) buf[k] = src[k];
+    __syncthreads();
+    const int i = first + threadIdx.x;
+    if (threadIdx.x >= rows) return;
+    const float4* w4 = buf + 4 * threadIdx.x;  // 64-byte records: four 16-byte words
     const float4 r0 = w4[0], r1 = w4[1], r2 = w4[2], r3 = w4[3];
     // r0 = p.xyz q.x, r1 = q.yzw v.x, r2 = v.yz w.xy, r3 = w.z activity previous timeBelow
     const float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i];
@@ -219,21 +229,29 @@ __global__ void k_update_body_state_records(const bepugpu_body_state* __restrict
     k.velocity_time_below_limit = r3.w;
 }
 // Body lanes -> state records.
-__global__ void k_pack_body_state(BodySoA b, bepugpu_body_state* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.count) return;
-    const float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i], a = b.act[i];
-    float4* o = (float4*)(out + i);
-    o[0] = make_float4(p.x, p.y, p.z, q.x);
-    o[1] = make_float4(q.y, q.z, q.w, v.x);
-    o[2] = make_float4(v.y, v.z, w.x, w.y);
-    o[3] = make_float4(w.z, a.z, a.x, a.y);
+__global__ void __launch_bounds__(kStateBlock) k_pack_body_state(BodySoA b, bepugpu_body_state* __restrict__ out) {
+    __shared__ float4 buf[4 * kStateBlock];
+    const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, b.count - first);
+    const int i = first + threadIdx.x;
+    if (threadIdx.x < rows) {
+        const float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i], a = b.act[i];
+        float4* o = buf + 4 * threadIdx.x;
+        o[0] = make_float4(p.x, p.y, p.z, q.x);
+        o[1] = make_float4(q.y, q.z, q.w, v.x);
+        o[2] = make_float4(v.y, v.z, w.x, w.y);
+        o[3] = make_float4(w.z, a.z, a.x, a.y);
+    }
+    __syncthreads();
+    float4* dst = (float4*)(out + first);
+    for (int k = threadIdx.x; k < 4 * rows; k += kStateBlock) dst[k] = buf[k];
 }
 // Manifold slots -> state records, in record order.
-__global__ void k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__ slot_of, int n,
-                                      bepugpu_manifold_state* __restrict__ out) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+__global__ void __launch_bounds__(kStateBlock) k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__ slot_of,
+                                                                     int n, bepugpu_manifold_state* __restrict__ out) {
+    __shared__ float4 buf[5 * kStateBlock];
+    const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, n - first);
+    const int i = first + threadIdx.x;
+    if (threadIdx.x < rows) {
     const int s = slot_of[i], cap = m.capacity;
     const int count = m.head[s].z & 0xff;
     const float4 pa = m.penacc[s], f = m.fricacc[s], ax = m.saxis[s];
@@ -244,12 +262,16 @@ __global__ void k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__
         id[k] = k < count ? __float_as_int(m.cnrm[k * cap + s].w) : 0;
         fi[k] = k < count ? m.cfr[k * cap + s].w : 0.f;
     }
-    float4* o = (float4*)(out + i);
+    float4* o = buf + 5 * threadIdx.x;
     o[0] = make_float4(__int_as_float(count), __int_as_float(id[0]), __int_as_float(id[1]), __int_as_float(id[2]));
     o[1] = make_float4(__int_as_float(id[3]), count > 0 ? pa.x : 0.f, count > 1 ? pa.y : 0.f, count > 2 ? pa.z : 0.f);
     o[2] = make_float4(count > 3 ? pa.w : 0.f, f.x, f.y, f.z);
     o[3] = make_float4(ax.x, ax.y, ax.z, fi[0]);
     o[4] = make_float4(fi[1], fi[2], fi[3], 0.f);
+    }
+    __syncthreads();
+    float4* dst = (float4*)(out + first);
+    for (int k = threadIdx.x; k < 5 * rows; k += kStateBlock) dst[k] = buf[k];
 }
 __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
                                          int n, ManifoldSoA m, int* check) {
@@ -1736,20 +1758,34 @@ bepugpu_status CheckStateArrays(Context* ctx, Scene* s, const void* bodies, uint
     }
     return BEPUGPU_OK;
 }
-// Packs the scene's state into the staging buffer and copies it into the
-// caller's arrays (asynchronous on the scene's stream).
+// The device's address of a page-locked host array (cudaHostAlloc or
+// cudaHostRegister memory is mapped into the device's address space), or
+// null for pageable memory.  Kernels then read and write the caller's array
+// over the host link themselves (NVLink-C2C on Grace), with no staging copy.
+void* PinnedDeviceAddress(const void* p) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Packs the scene's state into the caller's arrays (asynchronous on the
+// scene's stream): straight into page-locked arrays, else through the
+// staging buffer and a copy.
 bepugpu_status QueueStateDownload(Context* ctx, Scene* s, bepugpu_body_state* bodies, uint32_t nb,
                                   bepugpu_manifold_state* man, uint32_t nm) {
     auto* sb = (bepugpu_body_state*)s->staging;
     auto* sm = (bepugpu_manifold_state*)((char*)s->staging + s->stagingManifoldsAt);
-    if (nb) {
-        k_pack_body_state<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, sb);
+    auto* db = nb ? (bepugpu_body_state*)PinnedDeviceAddress(bodies) : nullptr;
+    auto* dm = nm ? (bepugpu_manifold_state*)PinnedDeviceAddress(man) : nullptr;
+    if (nb) k_pack_body_state<<<Blocks(nb, kStateBlock), kStateBlock, 0, s->stream>>>(s->b, db ? db : sb);
+    if (nm) k_pack_manifold_state<<<Blocks(nm, kStateBlock), kStateBlock, 0, s->stream>>>(s->m, s->slotOf, (int)nm, dm ? dm : sm);
+    if (nb && !db)
         CK(cudaMemcpyAsync(bodies, sb, sizeof(bepugpu_body_state) * nb, cudaMemcpyDeviceToHost, s->stream));
-    }
-    if (nm) {
-        k_pack_manifold_state<<<Blocks(nm, 256), 256, 0, s->stream>>>(s->m, s->slotOf, (int)nm, sm);
+    if (nm && !dm)
         CK(cudaMemcpyAsync(man, sm, sizeof(bepugpu_manifold_state) * nm, cudaMemcpyDeviceToHost, s->stream));
-    }
     CK(cudaGetLastError());
     return BEPUGPU_OK;
 }
@@ -1787,8 +1823,13 @@ bepugpu_status bepugpu_step_state(bepugpu_context* c, int32_t id, bepugpu_body_s
     }
     auto* sb = (bepugpu_body_state*)s->staging;
     if (nb) {
-        CK(cudaMemcpyAsync(sb, bodies, sizeof(bepugpu_body_state) * nb, cudaMemcpyHostToDevice, s->stream));
-        k_update_body_state_records<<<Blocks(nb, 256), 256, 0, s->stream>>>(sb, (int)nb, s->b, s->bodyRecords);
+        // page-locked caller arrays are read in place, others through the staging buffer
+        auto* in = (const bepugpu_body_state*)PinnedDeviceAddress(bodies);
+        if (!in) {
+            CK(cudaMemcpyAsync(sb, bodies, sizeof(bepugpu_body_state) * nb, cudaMemcpyHostToDevice, s->stream));
+            in = sb;
+        }
+        k_update_body_state_records<<<Blocks(nb, kStateBlock), kStateBlock, 0, s->stream>>>(in, (int)nb, s->b, s->bodyRecords);
         k_world_inertia<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, s->localM33);
         CK(cudaGetLastError());
     }
