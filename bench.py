@@ -415,17 +415,68 @@ def islands_section(args, ctx, local, pg):
         pg.barrier()
     asleep_ms, _ = timed_steps(space, args.steps, flush, N.STEP_ALL)
     f, idx = space.get_islands()
+    launches = int(space.last_step_launches())
+    space.close()
+    batched = islands_batch(args, ctx)
     out = {"workload": "64 x 16 x 64 unit cubes in 4,096 column islands", "islands": int(len(f)),
            "without_islands_ms_per_step": statistics.mean(plain_ms),
            "awake_ms_per_step": statistics.mean(awake_ms), "asleep_ms_per_step": statistics.mean(asleep_ms),
            "all_asleep_after_steps": asleep_at, "asleep_now": int(np.count_nonzero((f & N.ISLAND_ACTIVE) == 0)),
-           "launches_per_step": int(space.last_step_launches()),
+           "launches_per_step": launches,
            "what": "DeactivationManager.Update on the device (1 launch without moving kinematic bodies, 2 with) "
                    "before the group step; a group whose "
                    "islands all sleep returns after loading its bodies",
-           "l2": "flushed between timed steps (512 MiB write)"}
-    space.close()
+           "l2": "flushed between timed steps (512 MiB write)", "batched_columns": batched}
     return out
+
+
+def islands_batch(args, ctx):
+    """1,024 scenes of four columns of eight unit cubes with islands through
+    bepugpu_batch_step, 8 steps a call: scene-steps/s while awake and once
+    their islands sleep (a group whose islands all sleep returns at once)."""
+    from bepuphysics1_gb300 import native as N
+    from bepuphysics1_gb300 import scenes
+    from bepuphysics1_gb300.solver import GpuSpace, batch_step, islands_of, last_call_stats
+    spaces = []
+    for i in range(1024):
+        b, m, _ = scenes.make_pile(nx=2, ny=8, nz=2, spacing=2.0, size_min=1.0, size_max=1.0, jitter=0.02,
+                                   friction_min=0.6, friction_max=0.6, ground_size=(10.0, 1.0, 10.0), seed=12000 + i)
+        b = b.copy()
+        b["activity"] &= ~np.uint32(N.BODY_ALWAYS_ACTIVE)
+        sp = GpuSpace(ctx, b, m)
+        sp.set_islands(islands_of(b, m))
+        spaces.append(sp)
+    steps = 8
+
+    def timed(calls):
+        ms = []
+        for _ in range(calls):
+            batch_step(ctx, spaces, DT, steps)
+            ms.append(last_call_stats(ctx)[1])
+        return statistics.median(ms)
+
+    for _ in range(3):
+        batch_step(ctx, spaces, DT, steps)
+    awake_ms = timed(5)
+    calls, asleep_share = 8, 0.0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < 20.0:
+        batch_step(ctx, spaces, DT, steps)
+        calls += 1
+        if calls % 25 == 0:
+            flags = np.concatenate([sp.get_islands()[0] for sp in spaces])
+            asleep_share = float(np.mean((flags & N.ISLAND_ACTIVE) == 0))
+            if asleep_share > 0.99:
+                break
+    asleep_ms = timed(5)
+    flags = np.concatenate([sp.get_islands()[0] for sp in spaces])
+    for sp in spaces:
+        sp.close()
+    n = len(spaces)
+    return {"scenes": n, "steps_per_call": steps, "awake_scene_steps_per_s": n * steps / (awake_ms / 1000.0),
+            "asleep_scene_steps_per_s": n * steps / (asleep_ms / 1000.0), "awake_ms_per_call": awake_ms,
+            "asleep_ms_per_call": asleep_ms, "islands_asleep": float(np.mean((flags & N.ISLAND_ACTIVE) == 0)),
+            "steps_until_measured": calls * steps}
 
 
 def pile1k_section(args, ctx, local, pg):

@@ -67,6 +67,9 @@ struct Batch : BatchEngine {
     SceneView* viewsDev = nullptr;
     size_t viewsCap = 0;
     ClassLaunch shared, global;
+    std::vector<int4> islandWork;  // the island stage of scenes with islands (AddIslandWork)
+    int4* islandDev = nullptr;
+    size_t islandCap = 0;
     cudaGraphExec_t graph = nullptr;
     // key of the cached graph
     std::vector<int32_t> keyScenes;
@@ -84,6 +87,7 @@ struct Batch : BatchEngine {
         if (viewsDev) cudaFree(viewsDev);
         if (shared.dev) cudaFree(shared.dev);
         if (global.dev) cudaFree(global.dev);
+        if (islandDev) cudaFree(islandDev);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);
@@ -109,18 +113,18 @@ cudaError_t Ensure(T*& p, size_t& cap, size_t n) {
 
 template <bool kShared>
 cudaError_t LaunchBatchClass(Batch& bt, ClassLaunch& c, const StepParams& p, uint32_t flags, int threads,
-                             int passes) {
+                             int passes, int firstPass = 0) {
     if (c.work.empty()) return cudaSuccess;
     bt.launches += passes;
     return LaunchBatchedGroups(kShared, bt.viewsDev, c.dev, (int)c.work.size(), p, flags, c.Bc, c.Lc, c.members,
-                               threads, passes, bt.stream, c.nonConvex);
+                               threads, passes, bt.stream, c.nonConvex, firstPass);
 }
 
 }  // namespace
 
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
                                 uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
-                                cudaStream_t stream, bool nonConvex) {
+                                cudaStream_t stream, bool nonConvex, int firstPass) {
     if (n <= 0) return cudaSuccess;
     size_t smemBytes = GroupSmemBytes(shared, Bc, Lc, 0, nonConvex);
     auto kernel = shared ? k_batch_groups<true> : k_batch_groups<false>;
@@ -128,7 +132,7 @@ cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4*
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
         if (e != cudaSuccess) return e;
     }
-    for (int pass = 0; pass < passes; pass++) {
+    for (int pass = firstPass; pass < firstPass + passes; pass++) {
         kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass,
                                                                                   nonConvex);
         cudaError_t e = cudaGetLastError();
@@ -147,11 +151,14 @@ SceneView MakeView(const Scene& s) {
     v.t.colourOffsets = s.groupColourOffsetsDev;
     v.t.jointRefs = nullptr;  // batched scenes hold no joints
     v.t.jointColourOffsets = nullptr;
+    FillIslandView(s, v.isl);
     return v;
 }
 
 bool Scene::BatchReady(uint32_t flags) const {
-    return SweepEmpty() && jointCount == 0 && generatedCount == 0 && !kin.Needed(flags) && !islands;
+    // scenes with islands batch while no kinematic body can wake an island
+    return SweepEmpty() && jointCount == 0 && generatedCount == 0 && !kin.Needed(StageFlags(flags)) &&
+           (!islands || !IslandWakesPossible(this));
 }
 
 }  // namespace bepugpu
@@ -245,6 +252,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         int passes = 0;  // launches per class: the most steps any batched scene asked for
         bt.shared = ClassLaunch{{}, 1, 1, 0, false, bt.shared.dev, bt.shared.cap};
         bt.global = ClassLaunch{{}, 1, 1, 0, false, bt.global.dev, bt.global.cap};
+        bt.islandWork.clear();
         for (uint32_t i = 0; i < count; i++) {
             Scene* s = list[i];
             if (!ready[i] || stepCount[i] == 0) continue;
@@ -252,6 +260,7 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             const GroupPlan& g = s->groupPlan;
             const int vi = (int)views.size();
             views.push_back(MakeView(*s));
+            if (flags & BEPUGPU_STEP_DEACTIVATION) AddIslandWork(*s, vi, (int)stepCount[i], bt.islandWork);
             for (int k = g.shared.begin; k < g.shared.end; k++)
                 bt.shared.work.push_back(make_int4(vi, k, (int)stepCount[i], 0));
             for (int k = g.global.begin; k < g.global.end; k++)
@@ -275,7 +284,8 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
         }
         if ((e = Ensure(bt.viewsDev, bt.viewsCap, std::max<size_t>(views.size(), 1))) ||
             (e = Ensure(bt.shared.dev, bt.shared.cap, std::max<size_t>(bt.shared.work.size(), 1))) ||
-            (e = Ensure(bt.global.dev, bt.global.cap, std::max<size_t>(bt.global.work.size(), 1)))) {
+            (e = Ensure(bt.global.dev, bt.global.cap, std::max<size_t>(bt.global.work.size(), 1))) ||
+            (e = Ensure(bt.islandDev, bt.islandCap, std::max<size_t>(bt.islandWork.size(), 1)))) {
             ctx->SetError("batch tables: %s", cudaGetErrorString(e));
             return e == cudaErrorMemoryAllocation ? BEPUGPU_OUT_OF_MEMORY : BEPUGPU_CUDA_ERROR;
         }
@@ -287,6 +297,9 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             (!bt.global.work.empty() &&
              (e = cudaMemcpyAsync(bt.global.dev, bt.global.work.data(), sizeof(int4) * bt.global.work.size(),
                                   cudaMemcpyHostToDevice, bt.stream))) ||
+            (!bt.islandWork.empty() &&
+             (e = cudaMemcpyAsync(bt.islandDev, bt.islandWork.data(), sizeof(int4) * bt.islandWork.size(),
+                                  cudaMemcpyHostToDevice, bt.stream))) ||
             (e = cudaStreamSynchronize(bt.stream))) {
             ctx->SetError("batch tables: %s", cudaGetErrorString(e));
             return BEPUGPU_CUDA_ERROR;
@@ -296,8 +309,20 @@ static bepugpu_status BatchStep(bepugpu_context* c, const int32_t* scenes, const
             ctx->SetError("batch capture: %s", cudaGetErrorString(e));
             return BEPUGPU_CUDA_ERROR;
         }
-        cudaError_t le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads, passes);
-        if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads, passes);
+        cudaError_t le = cudaSuccess;
+        if (bt.islandWork.empty()) {
+            le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads, passes);
+            if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads, passes);
+        } else {
+            // step by step: the island stage of step k before any group's step k
+            for (int pass = 0; pass < passes && le == cudaSuccess; pass++) {
+                le = LaunchBatchedIslands(bt.viewsDev, bt.islandDev, (int)bt.islandWork.size(), p,
+                                          ctx->settings.maximum_deactivation_attempts_per_frame, pass, bt.stream);
+                bt.launches++;
+                if (le == cudaSuccess) le = LaunchBatchClass<true>(bt, bt.shared, p, flags, ctx->batchThreads, 1, pass);
+                if (le == cudaSuccess) le = LaunchBatchClass<false>(bt, bt.global, p, flags, ctx->batchThreads, 1, pass);
+            }
+        }
         cudaGraph_t graph = nullptr;
         e = cudaStreamEndCapture(bt.stream, &graph);
         if (le != cudaSuccess || e != cudaSuccess) {

@@ -378,16 +378,35 @@ struct BatchEngine {
     virtual ~BatchEngine() = default;
 };
 
+// A scene's island state for batched launches (islands.cu; n = 0 without islands).
+struct IslandView {
+    uint32_t* flags;
+    const int32_t* members;
+    int32_t* candidates;
+    int32_t* wakeAt;
+    int32_t* index;
+    unsigned int* done;
+    int n;
+};
+void FillIslandView(const Scene& s, IslandView& v);
+
 // Batched launches (batch.cu): one CTA per work item {view, group, steps}.
 struct SceneView {
     ManifoldSoA m;
     BodySoA b;
     GroupTables t;
+    IslandView isl;
 };
 SceneView MakeView(const Scene& s);
 cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4* work, int n, const StepParams& p,
                                 uint32_t flags, int Bc, int Lc, int members, int threads, int passes,
-                                cudaStream_t stream, bool nonConvex = false);
+                                cudaStream_t stream, bool nonConvex = false, int firstPass = 0);
+// The island stage of the batched scenes with islands (islands.cu): work items
+// {view, body block of 256, the scene's blocks, steps}, for step `pass`.
+cudaError_t LaunchBatchedIslands(const SceneView* views, const int4* work, int n, const StepParams& p,
+                                 int maxAttempts, int pass, cudaStream_t stream);
+// Work items of LaunchBatchedIslands for view `vi` of scene s stepping `steps` times.
+void AddIslandWork(const Scene& s, int vi, int steps, std::vector<int4>& work);
 
 struct Context {
     int device = 0;

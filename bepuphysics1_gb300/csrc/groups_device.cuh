@@ -126,7 +126,7 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
         const bool asleep = IslandAsleep(b, gi);
         asleepAll &= asleep ? 1 : 0;
         if (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_FORCES)) act = b.act[gi];
-        if (flags & BEPUGPU_STEP_DEACTIVATION) {
+        if ((flags & BEPUGPU_STEP_DEACTIVATION) && !b.islandOf) {  // with islands the island stage did it
             CandidacyMath(v, w, true, act, p);  // a group's bodies are dynamic
             b.act[gi] = act;
         }

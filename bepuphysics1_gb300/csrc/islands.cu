@@ -166,6 +166,40 @@ __global__ void k_island_members(BodySoA b, StepParams p, int32_t* wakeAt, int32
     if (threadIdx.x == 0) *done = 0u;
 }
 
+// The island stage of batched scenes: a block per work item {view, body block,
+// the scene's blocks, steps}; the last block of a scene runs its
+// DeactivateObjects (batched scenes have no kinematic body that can wake an island).
+__global__ void k_batch_island_members(const SceneView* __restrict__ views, const int4* __restrict__ work,
+                                       StepParams p, int maxAttempts, int pass) {
+    const int4 w = work[blockIdx.x];
+    if (pass >= w.w) return;
+    const SceneView& v = views[w.x];
+    const BodySoA b = v.b;
+    const int i = w.y * blockDim.x + threadIdx.x;
+    if (i < b.count) {
+        const bool dynamic = b.pos[i].w != 0.f;
+        float4 act = b.act[i];
+        if (dynamic) {
+            const int island = b.islandOf[i];
+            CandidacyMath(b.vlin[i], b.vang[i], true, act, p, (b.islandFlags[island] & BEPUGPU_ISLAND_ACTIVE) != 0);
+            if (__float_as_uint(act.z) & kCandidate) atomicAdd(v.isl.candidates + island, 1);
+        } else {
+            CandidacyMath(b.vlin[i], b.vang[i], false, act, p);
+        }
+        b.act[i] = act;
+    }
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(v.isl.done, 1u) == (unsigned)w.z - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    DeactivateObjects(v.isl.flags, v.isl.members, v.isl.candidates, v.isl.wakeAt, v.isl.index, v.isl.n, maxAttempts,
+                      false);
+    if (threadIdx.x == 0) *v.isl.done = 0u;
+}
+
 // Every joint and every manifold with contacts keeps its dynamic bodies in
 // one island; *bad receives the lowest slot (joints after manifolds) that does not.
 __global__ void k_check_islands(ManifoldSoA m, JointSoA j, BodySoA b, int* bad) {
@@ -204,6 +238,30 @@ void ReleaseIslands(Scene* s) {
 void ApplyIslandViews(Scene* s) {
     s->b.islandOf = s->islands ? s->islands->islandOf : nullptr;
     s->b.islandFlags = s->islands ? s->islands->flags : nullptr;
+}
+
+void FillIslandView(const Scene& s, IslandView& v) {
+    const IslandBuffers* I = s.islands;
+    v.flags = I ? I->flags : nullptr;
+    v.members = I ? I->members : nullptr;
+    v.candidates = I ? I->candidates : nullptr;
+    v.wakeAt = I ? I->wakeAt : nullptr;
+    v.index = I ? I->index : nullptr;
+    v.done = I ? I->done : nullptr;
+    v.n = I ? I->n : 0;
+}
+
+void AddIslandWork(const Scene& s, int vi, int steps, std::vector<int4>& work) {
+    if (!s.islands) return;
+    const int blocks = std::max(1, (s.b.count + 255) / 256);
+    for (int k = 0; k < blocks; k++) work.push_back(make_int4(vi, k, blocks, steps));
+}
+
+cudaError_t LaunchBatchedIslands(const SceneView* views, const int4* work, int n, const StepParams& p,
+                                 int maxAttempts, int pass, cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_batch_island_members<<<(unsigned)n, 256, 0, stream>>>(views, work, p, maxAttempts, pass);
+    return cudaGetLastError();
 }
 
 // Kinematic members can wake islands in this step: one moves or is always

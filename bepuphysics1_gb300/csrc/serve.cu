@@ -319,7 +319,7 @@ struct Server {
         if (ready.empty()) return false;
         w.slotIds.clear();
         w.reqs.clear();
-        std::vector<int4> shared, global;
+        std::vector<int4> shared, global, islandW;  // islandW: the island stage of scenes with islands
         int sBc = 1, sLc = 1, sMem = 0, gBc = 1, gMem = 0, passes = 0;
         bool sNonConvex = false;  // a shared-lane group holds a NONCONVEX manifold
         std::vector<int> plain;
@@ -400,6 +400,7 @@ struct Server {
             w.reqs.push_back(r);
             if (cfg.batching && s->BatchReady(cfg.flags)) {
                 for (uint32_t k = 0; k < r.steps; k++) s->kin.Advance(cfg.flags);
+                if (cfg.flags & BEPUGPU_STEP_DEACTIVATION) AddIslandWork(*s, id, (int)r.steps, islandW);
                 const GroupPlan& gp = s->groupPlan;
                 passes = std::max(passes, (int)r.steps);
                 for (int k = gp.shared.begin; k < gp.shared.end; k++) shared.push_back(make_int4(id, k, (int)r.steps, 0));
@@ -454,7 +455,7 @@ struct Server {
                           "scene table copy");
         }
         dirtyViews.clear();
-        size_t nWork = shared.size() + global.size();
+        size_t nWork = shared.size() + global.size() + islandW.size();
         if (e == cudaSuccess && nWork > w.workCap) {
             if (w.workDev) cudaFree(w.workDev);
             if (w.workHost) cudaFreeHost(w.workHost);
@@ -473,19 +474,31 @@ struct Server {
         if (e == cudaSuccess && nWork) {
             std::copy(shared.begin(), shared.end(), w.workHost);
             std::copy(global.begin(), global.end(), w.workHost + shared.size());
+            std::copy(islandW.begin(), islandW.end(), w.workHost + shared.size() + global.size());
             check(cudaMemcpyAsync(w.workDev, w.workHost, sizeof(int4) * nWork, cudaMemcpyHostToDevice, w.stream),
                   "work list copy");
-            if (e == cudaSuccess && !shared.empty()) {
-                check(LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc, sMem,
-                                          0, passes, w.stream, sNonConvex),
-                      "group launch");
-                statLaunches += passes;
-            }
-            if (e == cudaSuccess && !global.empty()) {
-                check(LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p,
-                                          cfg.flags, gBc, 1, gMem, 0, passes, w.stream),
-                      "group launch");
-                statLaunches += passes;
+            // with islands, step by step: the island stage of step k before any group's step k
+            const int rounds = islandW.empty() ? 1 : passes, per = islandW.empty() ? passes : 1;
+            for (int round = 0; round < rounds && e == cudaSuccess; round++) {
+                if (!islandW.empty()) {
+                    const int attempts = sink.settings.maximum_deactivation_attempts_per_frame;
+                    check(LaunchBatchedIslands(viewsDev, w.workDev + shared.size() + global.size(),
+                                               (int)islandW.size(), p, attempts, round, w.stream),
+                          "island launch");
+                    statLaunches++;
+                }
+                if (e == cudaSuccess && !shared.empty()) {
+                    check(LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc,
+                                              sMem, 0, per, w.stream, sNonConvex, round),
+                          "group launch");
+                    statLaunches += per;
+                }
+                if (e == cudaSuccess && !global.empty()) {
+                    check(LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p,
+                                              cfg.flags, gBc, 1, gMem, 0, per, w.stream, false, round),
+                          "group launch");
+                    statLaunches += per;
+                }
             }
         }
         // one-scene path: each scene's own stream, joined into the wave's event

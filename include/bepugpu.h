@@ -452,8 +452,9 @@ bepugpu_status bepugpu_broad_phase(bepugpu_context* ctx, int32_t scene, float dt
  *
  * bepugpu_upload_bodies and bepugpu_upload_constraints clear the islands (the
  * scene is stepped with every island awake until they are set again); so does
- * islands = 0.  Scenes with islands are stepped one at a time (batch and
- * serve refuse them). */
+ * islands = 0.  Batch and serve take scenes with islands into their batched
+ * launches while no kinematic body can wake an island, else step them one
+ * at a time. */
 #define BEPUGPU_ISLAND_ACTIVE             1u  /* SimulationIsland.isActive */
 #define BEPUGPU_ISLAND_ALLOW_DEACTIVATION 2u  /* SimulationIsland.allowDeactivation (default true) */
 bepugpu_status bepugpu_set_islands(bepugpu_context* ctx, int32_t scene, const int32_t* island_of_body,

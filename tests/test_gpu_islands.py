@@ -172,3 +172,86 @@ def test_set_islands_checks(gpu_context):
     sp.island_count = 0
     assert len(sp.get_islands()[0]) == 0
     sp.close()
+
+
+def _sleepy_towers(n, seed):
+    out = []
+    for i, k in enumerate(scenes.batch_body_counts(n, 8, 96, seed)):
+        b, m, _ = scenes.make_tower(int(k), seed=seed * 1000 + i)
+        b = b.copy()
+        b["activity"] &= ~np.uint32(N.BODY_ALWAYS_ACTIVE)
+        out.append((b, m))
+    return out
+
+
+def _island_spaces(ctx, pool):
+    spaces = []
+    for b, m in pool:
+        sp = GpuSpace(ctx, b, m)
+        sp.set_islands(islands_of(b, m))
+        spaces.append(sp)
+    return spaces
+
+
+def _assert_same_spaces(ctx, a, b, pool):
+    for sa, sb, (bb, mm) in zip(a, b, pool):
+        x, y = sa.download_bodies(bb.copy()), sb.download_bodies(bb.copy())
+        for f in ("position", "orientation", "linear_velocity", "angular_velocity", "velocity_time_below_limit"):
+            np.testing.assert_array_equal(x[f], y[f], err_msg=f)
+        np.testing.assert_array_equal(sa.download_constraints(mm.copy())[0]["contacts"]["penetration_impulse"],
+                                      sb.download_constraints(mm.copy())[0]["contacts"]["penetration_impulse"])
+        fa, ia = sa.get_islands()
+        fb, ib = sb.get_islands()
+        np.testing.assert_array_equal(fa, fb)
+        assert ia == ib
+
+
+def test_batched_island_scenes_step_as_alone(gpu_context):
+    """Towers with islands through bepugpu_batch_step (the batched island stage,
+    then the batched groups) equal the same towers stepped one at a time, until
+    and after their islands sleep."""
+    from bepuphysics1_gb300.solver import batch_step, last_call_stats
+    gpu_context.set_settings(default_settings())
+    pool = _sleepy_towers(24, 7)
+    alone = _island_spaces(gpu_context, pool)
+    batched = _island_spaces(gpu_context, pool)
+    for rnd in range(30):
+        for sp in alone:
+            for _ in range(8):
+                sp.step(float(DT))
+        batch_step(gpu_context, batched, float(DT), 8)
+        if rnd == 10:
+            launches, _ = last_call_stats(gpu_context)
+            assert launches > 0  # the island scenes took the batched launch
+    _assert_same_spaces(gpu_context, alone, batched, pool)
+    asleep = sum(int(np.count_nonzero((sp.get_islands()[0] & N.ISLAND_ACTIVE) == 0)) for sp in batched)
+    assert asleep > 0
+    for sp in alone + batched:
+        sp.close()
+
+
+def test_served_island_scenes_step_as_alone(gpu_context):
+    from bepuphysics1_gb300.serve import Server
+    gpu_context.set_settings(default_settings())
+    pool = _sleepy_towers(16, 9)
+    alone = _island_spaces(gpu_context, pool)
+    served = _island_spaces(gpu_context, pool)
+    srv = Server(gpu_context, dt=float(DT))
+    for sp in served:
+        srv.add(sp)
+    for rnd in range(12):
+        for sp in alone:
+            for _ in range(16):
+                sp.step(float(DT))
+        for sp in served:
+            while srv.submit(sp.id, 16, rnd) == N.QUEUE_FULL:
+                pass
+        srv.drain()
+        while len(srv.poll()):
+            pass
+    for sp in served:
+        srv.release(sp)
+    srv.close()
+    _assert_same_spaces(gpu_context, alone, served, pool)
+    for sp in alone + served:
+        sp.close()
