@@ -70,6 +70,9 @@ def parse_args():
                     help="island groups: whole steps of small islands in one CTA")
     ap.add_argument("--group-target", type=int, default=64, help="manifolds packed per group CTA")
     ap.add_argument("--group-threads", type=int, default=0, help="threads per group CTA (0 = from the plan)")
+    ap.add_argument("--group-prologue", type=int, default=-1, choices=[-1, 0, 1],
+                    help="island groups' refresh, body updates and prestep: 0 in the group kernel, "
+                         "1 as grid-wide launches before it, -1 by scene size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-seconds", type=float, default=10.0)
@@ -773,7 +776,11 @@ def chain_section(args, local, rank, world, pg):
         warm_b + prestep_b + body_b + joint_visit_bytes * (CHAIN_ITERATIONS + 2)  # + warm start and prestep
     peak, peak_kind = measured_hbm_peak()
     achieved = step_bytes / (total_ms / args.steps / 1000.0) / 1e9
-    out["roofline"] = {"bound": "hbm", "kernel": "k_groups (joint islands)", "achieved": achieved, "peak": peak,
+    # bepugpu_set_group_prologue's default: groups holding joints and >= 8,192 constraints are split
+    out["split_prologue"] = len(joints) + len(manifolds) >= 8192
+    out["roofline"] = {"bound": "hbm", "kernel": "k_groups (joint islands)" + (
+                           ", after k_group_refresh_force and k_group_prestep" if out["split_prologue"] else ""),
+                       "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                        "algorithmic_bytes_per_step": step_bytes,
                        "algorithmic": "manifolds: the step formula with a census of solve visits; joints: "
@@ -1170,10 +1177,13 @@ def main():
     ctx = Context(local, settings)
     policy = (0 if args.groups == "off" else 1, 1024, 4096, args.group_target, args.group_threads)
     space = GpuSpace(ctx, bodies, manifolds, group_policy=policy)
+    space.set_group_prologue(args.group_prologue)
     space.set_mode(N.MODE_GRAPH if args.mode == "graph" else N.MODE_PERSISTENT)
     if args.mode == "persistent":
         ctx.check(ctx.lib.bepugpu_set_persistent_blocks_per_sm(ctx.handle, space.id, args.persistent_blocks))
     colours = space.colouring()[2]
+    # bepugpu_set_group_prologue(-1) splits only groups holding joints: the pile's stay in the kernel
+    split_prologue = args.groups == "on" and args.group_prologue == 1
 
     for _ in range(max(args.warmup, 3)):
         space.step(DT, N.STEP_ALL)
@@ -1380,7 +1390,9 @@ def main():
                        "step": "refresh+forces+solve+positions", "mode": args.mode,
                        "island_groups": {"enabled": args.groups == "on", "ctas": int(prof["groups"]),
                                          "target_manifolds": args.group_target,
-                                         "threads": args.group_threads or "plan"},
+                                         "threads": args.group_threads or "plan",
+                                         "prologue": "grid-wide launches" if split_prologue
+                                         else "in the group kernel"},
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "flushed between timed steps (512 MiB write)"},
             "gpu_launches": int(launches),

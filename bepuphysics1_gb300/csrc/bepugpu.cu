@@ -1033,14 +1033,15 @@ bepugpu_status Scene::BuildGraph(Context* ctx, const StepParams& p, uint32_t fla
     // position update of moving kinematic bodies therefore has to follow.
     CK(cudaEventRecordWithFlags(evGroup[0], stream, cudaEventRecordExternal));
     if (!groupPlan.groups.empty()) {
-        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false);
+        int groupLaunches = 0;
+        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false, &groupLaunches);
         if (gs != BEPUGPU_OK) {
             cudaGraph_t dropped;
             cudaStreamEndCapture(stream, &dropped);
             if (dropped) cudaGraphDestroy(dropped);
             return gs;
         }
-        launchesPerStep += GroupLaunchCount(groupPlan);
+        launchesPerStep += groupLaunches;
     }
     CK(cudaEventRecordWithFlags(evGroup[1], stream, cudaEventRecordExternal));
     const ManifoldSoA ms = SweepManifolds();
@@ -1191,9 +1192,10 @@ bepugpu_status Scene::RunPersistent(Context* ctx, const StepParams& p, uint32_t 
     }
     CK(cudaEventRecord(evGroup[0], stream));
     if (!groupPlan.groups.empty()) {
-        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false);
+        int groupLaunches = 0;
+        bepugpu_status gs = LaunchGroups(ctx, this, p, flags, false, &groupLaunches);
         if (gs != BEPUGPU_OK) return gs;
-        launchesPerStep += GroupLaunchCount(groupPlan);
+        launchesPerStep += groupLaunches;
     }
     CK(cudaEventRecord(evGroup[1], stream));
     PersistentArgs a;
@@ -2090,6 +2092,23 @@ bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* c, int32_t id, uin
         return BEPUGPU_INVALID_ARGUMENT;
     }
     s->policy.sharedLanesBudget = bytes;
+    return BEPUGPU_OK;
+}
+
+bepugpu_status bepugpu_set_group_prologue(bepugpu_context* c, int32_t id, int32_t mode) {
+    auto* ctx = reinterpret_cast<Context*>(c);
+    CTX_CHECK(ctx);
+    Scene* s = FindScene(ctx, id);
+    if (!s) return SceneMissing(ctx, id);
+    if (mode < -1 || mode > 1) {
+        ctx->SetError("group prologue mode must be -1, 0 or 1");
+        return BEPUGPU_INVALID_ARGUMENT;
+    }
+    if (s->groupPrologue != mode && s->graphExec) {  // the step graph holds the launches
+        cudaGraphExecDestroy(s->graphExec);
+        s->graphExec = nullptr;
+    }
+    s->groupPrologue = mode;
     return BEPUGPU_OK;
 }
 

@@ -159,13 +159,24 @@ void PlanGroups(const GroupPolicy& pol, const int32_t* a, const int32_t* b, cons
                 int32_t nm, const uint8_t* dynamic, int32_t nb, int32_t colours, GroupPlan& plan,
                 const uint8_t* nonConvex = nullptr, const int32_t* entryKind = nullptr,
                 const uint8_t* follows = nullptr);
-bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count);
+// Launches a step of every island group (launches: incremented per kernel
+// launch).  With the split prologue (SplitGroupPrologue) two grid-wide
+// launches run the groups' refresh, body updates and prestep first.
+bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count,
+                            int* launches = nullptr);
+bool SplitGroupPrologue(const Scene* s, uint32_t flags);
+// The split prologue's default: scenes whose groups hold joints and at least
+// this many constraints.  Measured on GB300: joint chains (151,073 bodies,
+// 196,608 joints) step 7 % faster split, 12 % with the added joint types;
+// contact-only groups (the 65,536-box pile, towers) 7-13 % slower, the group
+// CTA's own pass over its bodies and manifolds being cheaper there than two
+// more launches and the copy of the solve lanes.
+constexpr int32_t kSplitPrologueConstraints = 8192;
 // Joints (joints.cu): record checks, upload into the scene's joint slots, and
 // the accumulated impulses back into records.
 bepugpu_status CheckJointRecords(Context* ctx, const bepugpu_joint* joints, uint32_t nj, int32_t bodies);
 bepugpu_status UploadJoints(Context* ctx, Scene* s, const bepugpu_joint* joints, uint32_t nj);
 bepugpu_status DownloadJoints(Context* ctx, Scene* s, bepugpu_joint* joints, uint32_t nj);
-int GroupLaunchCount(const GroupPlan& g);
 // Damping flags bit 2 marks a body stepped by a group kernel.
 constexpr uint32_t kOwnedByGroup = 4u;
 
@@ -280,6 +291,7 @@ struct Scene {
         return s;
     }
     int groupThreadsOverride = 0;    // 0 = derived from the plan
+    int groupPrologue = -1;          // split group prologue: 1 on, 0 off, -1 by size (SplitGroupPrologue)
     bool phaseEvents = true;         // the step graph records the sweep-path phase events
     bool planStale = false;          // dynamic flags changed since the constraints were planned
     uint64_t batchStamp = 0;         // last batched call listing the scene (duplicate check)

@@ -28,10 +28,33 @@ namespace bepugpu {
 
 template <bool kCensus, bool kShared, int kJoints>
 __global__ void k_groups(ManifoldSoA m, BodySoA b, JointSoA j, StepParams p, uint32_t flags, GroupTables t,
-                         int groupBase, int Bc, int Lc, int Jc, unsigned long long* census, bool nonConvex) {
+                         int groupBase, int Bc, int Lc, int Jc, unsigned long long* census, bool nonConvex,
+                         bool prestepped) {
     extern __shared__ float4 smem[];
     const GroupDesc g = t.groups[groupBase + blockIdx.x];
-    GroupStep<kCensus, kShared, kJoints>(m, b, j, p, flags, t, g, Bc, Lc, Jc, smem, census, nonConvex);
+    GroupStep<kCensus, kShared, kJoints>(m, b, j, p, flags, t, g, Bc, Lc, Jc, smem, census, nonConvex, prestepped);
+}
+
+// The group step's first stages as grid-wide launches (the split prologue):
+// the contact refresh of the groups' manifold slots [s0, s1) beside the
+// candidacy and force updates of their bodies (list[0, n)), then the prestep
+// of those slots into the global solve lanes.  One thread per manifold or
+// body fills the GPU where a group CTA runs its few threads over them in turn;
+// the group kernel then copies the lanes into shared memory
+// (GroupStep's `prestepped`).  The same device routines as the colour-sweep
+// path's k_refresh_force_list and k_prestep.
+__global__ void k_group_refresh_force(ManifoldSoA m, BodySoA b, StepParams p, const int32_t* __restrict__ list, int n,
+                                      int s0, int s1, uint32_t flags) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, nm = s1 - s0;
+    if (t < nm) {
+        if (flags & BEPUGPU_STEP_REFRESH_CONTACTS) RefreshManifold(m, b, s0 + t, p);
+    } else if (t - nm < n) {
+        if (flags & (BEPUGPU_STEP_FORCES | BEPUGPU_STEP_DEACTIVATION)) StartBodyStep(b, list[t - nm], p, flags);
+    }
+}
+__global__ void k_group_prestep(ManifoldSoA m, BodySoA b, StepParams p, int s0, int s1) {
+    const int s = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < s1) PrestepManifold(m, b, s, p);
 }
 
 // ------------------------------------------------------------------ host side --
@@ -300,7 +323,7 @@ int ClassThreads(const GroupClass& c, int override_) {
 
 template <bool kShared, int kJoints>
 bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const StepParams& p, uint32_t flags,
-                           bool count, GroupTables t) {
+                           bool count, GroupTables t, bool prestepped, int* launches) {
     if (c.end <= c.begin) return BEPUGPU_OK;
     const int Bc = std::max(c.maxLocal, 1), Lc = std::max(c.maxManifolds, 1), Jc = std::max(c.maxJoints, 1);
     const bool nonConvex = s->groupPlan.nonConvexLanes;
@@ -323,10 +346,11 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
     const cudaError_t earlier = cudaGetLastError();
     if (count)
         k_groups<true, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
-            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census(), nonConvex);
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, s->Census(), nonConvex, prestepped);
     else
         k_groups<false, kShared, kJoints><<<blocks, threads, smemBytes, s->stream>>>(
-            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr, nonConvex);
+            s->m, s->b, s->j, p, flags, t, c.begin, Bc, Lc, Jc, nullptr, nonConvex, prestepped);
+    if (launches) (*launches)++;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         ctx->SetError("group kernel launch (%u CTAs of %d threads, %zu bytes of shared memory): %s%s%s", blocks,
@@ -338,13 +362,15 @@ bepugpu_status LaunchClass(Context* ctx, Scene* s, const GroupClass& c, const St
 }
 }  // namespace
 
-int GroupLaunchCount(const GroupPlan& g) {
-    int n = 0;
-    for (const GroupClass* c : {&g.shared, &g.global, &g.sharedJoints, &g.globalJoints}) n += c->end > c->begin;
-    return n;
+bool SplitGroupPrologue(const Scene* s, uint32_t flags) {
+    const GroupPlan& g = s->groupPlan;
+    if (g.groups.empty() || !(flags & BEPUGPU_STEP_SOLVE)) return false;
+    if (s->groupPrologue >= 0) return s->groupPrologue == 1;
+    const int32_t held = (g.groups.back().mEnd - g.globalCount) + (g.groups.back().jEnd - g.jointGlobalCount);
+    return g.groupJoints && held >= kSplitPrologueConstraints;
 }
 
-bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count) {
+bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_t flags, bool count, int* launches) {
     const GroupPlan& g = s->groupPlan;
     if (g.groups.empty()) return BEPUGPU_OK;
     GroupTables t;
@@ -354,14 +380,33 @@ bepugpu_status LaunchGroups(Context* ctx, Scene* s, const StepParams& p, uint32_
     t.colourOffsets = s->groupColourOffsetsDev;
     t.jointRefs = s->groupJointRefsDev;
     t.jointColourOffsets = s->groupJointColourOffsetsDev;
-    bepugpu_status st = LaunchClass<true, false>(ctx, s, g.shared, p, flags, count, t);
-    if (st == BEPUGPU_OK) st = LaunchClass<false, false>(ctx, s, g.global, p, flags, count, t);
+    const bool split = SplitGroupPrologue(s, flags);
+    if (split) {
+        // every group's manifold slots follow the sweep part's; its bodies are the body list
+        const int s0 = g.globalCount, s1 = g.groups.back().mEnd, nb = g.groups.back().bEnd;
+        const int T = 128;
+        const cudaError_t earlier = cudaGetLastError();
+        if (s1 - s0 + nb > 0)
+            k_group_refresh_force<<<(s1 - s0 + nb + T - 1) / T, T, 0, s->stream>>>(s->m, s->b, p, t.bodies, nb, s0,
+                                                                                    s1, flags);
+        if (s1 > s0) k_group_prestep<<<(s1 - s0 + T - 1) / T, T, 0, s->stream>>>(s->m, s->b, p, s0, s1);
+        if (launches) *launches += (s1 - s0 + nb > 0) + (s1 > s0);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            ctx->SetError("group prologue launch: %s%s%s", cudaGetErrorString(e),
+                          earlier != cudaSuccess ? "; earlier error: " : "",
+                          earlier != cudaSuccess ? cudaGetErrorString(earlier) : "");
+            return BEPUGPU_CUDA_ERROR;
+        }
+    }
+    bepugpu_status st = LaunchClass<true, false>(ctx, s, g.shared, p, flags, count, t, split, launches);
+    if (st == BEPUGPU_OK) st = LaunchClass<false, false>(ctx, s, g.global, p, flags, count, t, split, launches);
     if (s->addedJointTypes) {
-        if (st == BEPUGPU_OK) st = LaunchClass<true, 2>(ctx, s, g.sharedJoints, p, flags, count, t);
-        if (st == BEPUGPU_OK) st = LaunchClass<false, 2>(ctx, s, g.globalJoints, p, flags, count, t);
+        if (st == BEPUGPU_OK) st = LaunchClass<true, 2>(ctx, s, g.sharedJoints, p, flags, count, t, split, launches);
+        if (st == BEPUGPU_OK) st = LaunchClass<false, 2>(ctx, s, g.globalJoints, p, flags, count, t, split, launches);
     } else {
-        if (st == BEPUGPU_OK) st = LaunchClass<true, 1>(ctx, s, g.sharedJoints, p, flags, count, t);
-        if (st == BEPUGPU_OK) st = LaunchClass<false, 1>(ctx, s, g.globalJoints, p, flags, count, t);
+        if (st == BEPUGPU_OK) st = LaunchClass<true, 1>(ctx, s, g.sharedJoints, p, flags, count, t, split, launches);
+        if (st == BEPUGPU_OK) st = LaunchClass<false, 1>(ctx, s, g.globalJoints, p, flags, count, t, split, launches);
     }
     return st;
 }

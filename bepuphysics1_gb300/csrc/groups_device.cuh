@@ -32,6 +32,18 @@ struct GroupBodies {
     }
 };
 
+// Asynchronous global -> shared copies (cp.async), waited for with
+// CopyAsyncWait before the block barrier that publishes them.
+__device__ __forceinline__ void CopyAsync16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void CopyAsync8(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void CopyAsyncWait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Shared memory of one CTA: 6 body lanes per body; with kShared also 24 float4
 // lanes, a state word and a ref pair per manifold (400 bytes), plus 4 lanes
 // when the groups hold NONCONVEX manifolds (nonConvex: 464 bytes); with joints
@@ -55,11 +67,16 @@ __host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int
 // contact friction lanes (GroupManifoldLanes); a NONCONVEX manifold keeps its
 // friction direction and impulse in lanes 12-15 (the sliding lanes it does not
 // use), its prestep angular A in lanes 16-19 and angular B in lanes 25-28.
+// prestepped: the group's bodies went through the candidacy and force updates
+// and its manifolds through the refresh and the prestep in grid-wide launches
+// before this one (k_group_refresh_force, k_group_prestep; joints: none), so
+// the step starts by copying bodies and solve lanes into shared memory.
 template <bool kCensus, bool kShared, int kJoints>
 __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const JointSoA& jt,
                                           const StepParams& p, uint32_t flags, const GroupTables& t,
                                           const GroupDesc& g, int Bc, int Lc, int Jc, float4* smem,
-                                          unsigned long long* census, bool nonConvex = false) {
+                                          unsigned long long* census, bool nonConvex = false,
+                                          bool prestepped = false) {
     const int nLocal = g.bEnd - g.bBegin, nm = g.mEnd - g.mBegin;
     GroupBodies bv;
     bv.pos = smem;
@@ -119,59 +136,124 @@ __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b
     // sleeping island skips the force update and reads as not dynamic for the
     // rest of the step: pos.w = 0 in shared memory.
     int asleepAll = b.islandOf != nullptr;
-    for (int i = tid; i < nLocal; i += T) {
-        int gi = t.bodies[g.bBegin + i];
-        float4 v = b.vlin[gi], w = b.vang[gi], q = b.quat[gi], a, c;
-        float4 act = make_float4(0.f, 0.f, 0.f, 0.f);
-        const bool asleep = IslandAsleep(b, gi);
-        asleepAll &= asleep ? 1 : 0;
-        if (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_FORCES)) act = b.act[gi];
-        if ((flags & BEPUGPU_STEP_DEACTIVATION) && !b.islandOf) {  // with islands the island stage did it
-            CandidacyMath(v, w, true, act, p);  // a group's bodies are dynamic
-            b.act[gi] = act;
+    if (prestepped) {
+        // Bodies, then (shared lanes) every solve lane the prestep wrote, as
+        // asynchronous copies; a sleeping body's pos.w is cleared after them.
+        for (int i = tid; i < nLocal; i += T) {
+            const int gi = t.bodies[g.bBegin + i];
+            CopyAsync16(bv.pos + i, b.pos + gi);
+            CopyAsync16(bv.quat + i, b.quat + gi);
+            CopyAsync16(bv.vlin + i, b.vlin + gi);
+            CopyAsync16(bv.vang + i, b.vang + gi);
+            CopyAsync16(bv.inv0 + i, b.inv0 + gi);
+            CopyAsync16(bv.inv1 + i, b.inv1 + gi);
         }
-        if ((flags & BEPUGPU_STEP_FORCES) && !asleep) {
-            ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], act, b.rawDamp + gi, a, c, p);
-        } else {
-            a = b.inv0[gi];
-            c = b.inv1[gi];
+        if (kShared) {
+            const int cap = m.capacity;
+            for (int j = tid; j < nm; j += T) {
+                const int s = g.mBegin + j;
+                const bool nc = nonConvex && ((((uint32_t)m.head[s].z) >> 8) & kManifoldNonConvex);
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    CopyAsync16(ml.pj0 + k * Lc + j, m.pj0 + k * cap + s);
+                    CopyAsync16(ml.pj1 + k * Lc + j, m.pj1 + k * cap + s);
+                    CopyAsync16(ml.pj2 + k * Lc + j, m.pj2 + k * cap + s);
+                }
+                if (nc) {
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        CopyAsync16(ml.cfr + k * Lc + j, m.cfr + k * cap + s);
+                        CopyAsync16(ml.cfa + k * Lc + j, m.cfa + k * cap + s);
+                        CopyAsync16(ml.cfb + k * Lc + j, m.cfb + k * cap + s);
+                    }
+                } else {
+                    CopyAsync16(ml.s0 + j, m.s0 + s);
+                    CopyAsync16(ml.s1 + j, m.s1 + s);
+                    CopyAsync16(ml.saxis + j, m.saxis + s);
+                    CopyAsync16(ml.s3 + j, m.s3 + s);
+                    CopyAsync16(ml.s4 + j, m.s4 + s);
+                    CopyAsync16(ml.s5 + j, m.s5 + s);
+                    CopyAsync16(ml.s6 + j, m.s6 + s);
+                    CopyAsync16(ml.s7 + j, m.s7 + s);
+                }
+                CopyAsync16(ml.lever + j, m.lever + s);
+                CopyAsync16(ml.penacc + j, m.penacc + s);
+                CopyAsync16(ml.fricacc + j, m.fricacc + s);
+                CopyAsync16(ml.head + j, m.head + s);
+                CopyAsync8(ml.state + j, m.state + s);
+                CopyAsync8(sRefs + j, t.refs + s);
+                if (kCensus) {  // lanes in global memory: prestep products written once and read once
+                    unsigned long long c4 = (unsigned long long)(m.head[s].z & 0xff);
+                    atomicAdd(census + 3, 288ull + 112ull * c4);
+                }
+            }
+        } else if (kCensus) {
+            for (int j = tid; j < nm; j += T)
+                atomicAdd(census + 3, 288ull + 112ull * (unsigned long long)(m.head[g.mBegin + j].z & 0xff));
         }
-        float4 pos = b.pos[gi];
-        if (asleep) pos.w = 0.f;
-        bv.pos[i] = pos;
-        bv.quat[i] = q;
-        bv.vlin[i] = v;
-        bv.vang[i] = w;
-        bv.inv0[i] = a;
-        bv.inv1[i] = c;
+        CopyAsyncWait();
+        for (int i = tid; i < nLocal; i += T) {
+            const bool asleep = IslandAsleep(b, t.bodies[g.bBegin + i]);
+            asleepAll &= asleep ? 1 : 0;
+            if (asleep) bv.pos[i].w = 0.f;
+        }
+    } else {
+        for (int i = tid; i < nLocal; i += T) {
+            int gi = t.bodies[g.bBegin + i];
+            float4 v = b.vlin[gi], w = b.vang[gi], q = b.quat[gi], a, c;
+            float4 act = make_float4(0.f, 0.f, 0.f, 0.f);
+            const bool asleep = IslandAsleep(b, gi);
+            asleepAll &= asleep ? 1 : 0;
+            if (flags & (BEPUGPU_STEP_DEACTIVATION | BEPUGPU_STEP_FORCES)) act = b.act[gi];
+            if ((flags & BEPUGPU_STEP_DEACTIVATION) && !b.islandOf) {  // with islands the island stage did it
+                CandidacyMath(v, w, true, act, p);  // a group's bodies are dynamic
+                b.act[gi] = act;
+            }
+            if ((flags & BEPUGPU_STEP_FORCES) && !asleep) {
+                ForceMath(v, w, q, b.loc0[gi], b.loc1[gi], b.damp[gi], act, b.rawDamp + gi, a, c, p);
+            } else {
+                a = b.inv0[gi];
+                c = b.inv1[gi];
+            }
+            float4 pos = b.pos[gi];
+            if (asleep) pos.w = 0.f;
+            bv.pos[i] = pos;
+            bv.quat[i] = q;
+            bv.vlin[i] = v;
+            bv.vang[i] = w;
+            bv.inv0[i] = a;
+            bv.inv1[i] = c;
+        }
     }
     // A group whose islands all sleep has nothing to do: no active constraint,
     // no manifold with an active entry (an active kinematic body touching one
     // of its islands would have woken it), no body to move.
     if (__syncthreads_and(asleepAll)) return;
     // Refresh, lanes in, prestep: a thread keeps the same manifolds throughout.
-    for (int j = tid; j < nm; j += T) {
-        const int s = g.mBegin + j;
-        int2 r = t.refs[s];
-        // with islands, a pair between two inactive entries is not refreshed (NarrowPhase.cs:300-332)
-        auto entryActive = [&](int ref) {
-            return ref >= 0 ? bv.pos[ref].w != 0.f : (ref <= -2 && b.act[-2 - ref].y <= 0.f);
-        };
-        if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && (!b.islandOf || entryActive(r.x) || entryActive(r.y)))
-            RefreshManifoldV(m, bv, s, r.x, r.y, p);
-        if (kShared) {
-            ml.penacc[j] = m.penacc[s];  // after the refresh, which may compact them
-            ml.fricacc[j] = m.fricacc[s];
-            sRefs[j] = r;
-        }
-        if (flags & BEPUGPU_STEP_SOLVE) PrestepManifoldIO(m, s, ml, lbase + j, bv, r.x, r.y, p);
-        if (kCensus) {
-            // Compulsory DRAM bytes of the step for this manifold.  Lanes in shared memory:
-            // head, refs, 3 input lanes per contact, material, axis and impulses read once,
-            // positions, impulses and axis written once: 136 + 64 c.  Lanes in global
-            // memory add the prestep products written once: 288 + 112 c.
-            unsigned long long c4 = (unsigned long long)(m.head[s].z & 0xff);
-            atomicAdd(census + 3, kShared ? 136ull + 64ull * c4 : 288ull + 112ull * c4);
+    if (!prestepped) {
+        for (int j = tid; j < nm; j += T) {
+            const int s = g.mBegin + j;
+            int2 r = t.refs[s];
+            // with islands, a pair between two inactive entries is not refreshed (NarrowPhase.cs:300-332)
+            auto entryActive = [&](int ref) {
+                return ref >= 0 ? bv.pos[ref].w != 0.f : (ref <= -2 && b.act[-2 - ref].y <= 0.f);
+            };
+            if ((flags & BEPUGPU_STEP_REFRESH_CONTACTS) && (!b.islandOf || entryActive(r.x) || entryActive(r.y)))
+                RefreshManifoldV(m, bv, s, r.x, r.y, p);
+            if (kShared) {
+                ml.penacc[j] = m.penacc[s];  // after the refresh, which may compact them
+                ml.fricacc[j] = m.fricacc[s];
+                sRefs[j] = r;
+            }
+            if (flags & BEPUGPU_STEP_SOLVE) PrestepManifoldIO(m, s, ml, lbase + j, bv, r.x, r.y, p);
+            if (kCensus) {
+                // Compulsory DRAM bytes of the step for this manifold.  Lanes in shared memory:
+                // head, refs, 3 input lanes per contact, material, axis and impulses read once,
+                // positions, impulses and axis written once: 136 + 64 c.  Lanes in global
+                // memory add the prestep products written once: 288 + 112 c.
+                unsigned long long c4 = (unsigned long long)(m.head[s].z & 0xff);
+                atomicAdd(census + 3, kShared ? 136ull + 64ull * c4 : 288ull + 112ull * c4);
+            }
         }
     }
     if (kJoints && (flags & BEPUGPU_STEP_SOLVE))

@@ -170,6 +170,7 @@ GPU_EXPORTS = {
     "bepugpu_set_persistent_blocks_per_sm": (_I, [_P, _I, _I]),
     "bepugpu_set_group_policy": (_I, [_P, _I, _I, _I, _I, _I, _I]),
     "bepugpu_set_group_smem_budget": (_I, [_P, _I, _U]),
+    "bepugpu_set_group_prologue": (_I, [_P, _I, _I]),
     "bepugpu_set_batch_threads": (_I, [_P, _I]),
     "bepugpu_last_step_ms": (_I, [_P, _I, ctypes.POINTER(_F)]),
     "bepugpu_last_step_launches": (_I, [_P, _I, ctypes.POINTER(_U)]),

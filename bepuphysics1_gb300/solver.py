@@ -135,6 +135,12 @@ class GpuSpace:
         their solve lanes in global memory (next upload_constraints)."""
         self.ctx.check(self.ctx.lib.bepugpu_set_group_smem_budget(self.ctx.handle, self.id, int(nbytes)))
 
+    def set_group_prologue(self, mode: int):
+        """bepugpu_set_group_prologue: the island groups' refresh, body updates
+        and prestep inside the group kernel (0), as grid-wide launches before
+        it (1), or by scene size (-1, the default)."""
+        self.ctx.check(self.ctx.lib.bepugpu_set_group_prologue(self.ctx.handle, self.id, int(mode)))
+
     def upload_bodies(self, bodies: np.ndarray):
         bodies = np.ascontiguousarray(bodies, dtype=N.BODY_DTYPE)
         self.ctx.check(self.ctx.lib.bepugpu_upload_bodies(self.ctx.handle, self.id, N.ptr(bodies), len(bodies)))

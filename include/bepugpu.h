@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 10
+#define BEPUGPU_ABI_VERSION 11
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -636,6 +636,16 @@ bepugpu_status bepugpu_set_group_policy(bepugpu_context* ctx, int32_t scene, int
  * 0 keeps every group's lanes in global memory.  At most 200 KiB (default).
  * Takes effect at the next bepugpu_upload_constraints. */
 bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* ctx, int32_t scene, uint32_t bytes);
+
+/* Where island groups run the first stages of their step (the contact
+ * refresh, the candidacy and force updates of their bodies, the manifolds'
+ * prestep): 0 inside the group kernel, each CTA over its own group; 1 as two
+ * grid-wide launches before it, one thread per manifold or body, the group
+ * kernel then copying the solve lanes into shared memory; -1 (default) the
+ * grid-wide launches when the groups hold joints and at least 8,192
+ * constraints.  The results are the same bit for bit.  Takes effect at the
+ * next step. */
+bepugpu_status bepugpu_set_group_prologue(bepugpu_context* ctx, int32_t scene, int32_t mode);
 
 /* Persistent mode: resident blocks per SM of the cooperative launch (1 or 2). */
 bepugpu_status bepugpu_set_persistent_blocks_per_sm(bepugpu_context* ctx, int32_t scene, int32_t blocks);
