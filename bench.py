@@ -79,7 +79,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the many-scene batching section")
     ap.add_argument("--batch-scenes", type=int, default=4096)
     ap.add_argument("--batch-rounds", type=int, default=5, help="timed rounds of the plain and batched paths")
-    ap.add_argument("--tune-seconds", type=float, default=20.0, help="autotuner time limit")
+    ap.add_argument("--tune-seconds", type=float, default=30.0, help="autotuner time limit")
     ap.add_argument("--tune-out", default=None, help="write the autotuner's trials to this JSON file")
     ap.add_argument("--batch-cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-chains", action="store_true", help="skip the mixed joints-and-contacts section")
@@ -612,31 +612,49 @@ def batch_section(args, local, rank, world, pg):
         if pg:
             pg.barrier()
 
-    # plain path: one bepugpu_step per scene, each its own graph launch
-    for _ in range(max(args.warmup, 3)):
+    # autotuned batched path (every trial starts from the records' state)
+    # the search starts from the best setting of earlier tunings of this mix
+    res = autotune.tune(ctx, spaces, records, DT, start=autotune.BatchConfig(128, 100 * 1024, 128, 16),
+                        max_seconds=args.tune_seconds)
+    if args.tune_out:
+        autotune.save(args.tune_out, res, BATCH_WORKLOAD)
+    best = res.best
+    K = best.steps_per_launch
+    calls = max(args.batch_rounds, 3)
+
+    def from_records():
+        """The records' state, then 3 warm-up steps on the plain path: the
+        plain and the batched timings start from the same scene state."""
+        autotune.restore_state(spaces, records)
+        for _ in range(3):
+            for sp in spaces:
+                sp.step(DT, N.STEP_ALL)
+        ctx.synchronize()
+
+    # plain path: one bepugpu_step per scene, each its own graph launch, over
+    # the same steps as the batched timing (after K untimed steps, the batched
+    # path's graph-capturing first call)
+    from_records()
+    for _ in range(K):
         for sp in spaces:
             sp.step(DT, N.STEP_ALL)
     ctx.synchronize()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(args.batch_rounds):
+    for _ in range(calls * K):
         for sp in spaces:
             sp.step(DT, N.STEP_ALL)
     ctx.synchronize()
     plain_s = time.perf_counter() - t0
+    plain_steps = calls * K
     plain_launches = sum(sp.last_step_launches() for sp in spaces)
 
-    # autotuned batched path
-    res = autotune.tune(ctx, spaces, records, DT, max_seconds=args.tune_seconds)
-    if args.tune_out:
-        autotune.save(args.tune_out, res, BATCH_WORKLOAD)
-    best = res.best
     per_k = {}
-    for k in sorted({1, best.steps_per_launch}):
+    for k in sorted({1, K}):
+        from_records()
         barrier()
-        t = autotune.measure(ctx, spaces, DT, k, calls=max(args.batch_rounds, 3))
-        per_k[k] = t
-    tb = per_k[best.steps_per_launch]
+        per_k[k] = autotune.measure(ctx, spaces, DT, k, calls=calls)
+    tb = per_k[K]
     t1 = per_k[1]
 
     def whole(v):
@@ -647,7 +665,7 @@ def batch_section(args, local, rank, world, pg):
         pg.all_reduce(x)
         return float(x.item())
 
-    plain_rate = whole(n * args.batch_rounds / plain_s)
+    plain_rate = whole(n * plain_steps / plain_s)
     batched_rate = whole(tb.scene_steps_per_s)
     batched_1 = whole(t1.scene_steps_per_s)
 
@@ -676,9 +694,12 @@ def batch_section(args, local, rank, world, pg):
         "config": {"scenes": args.batch_scenes, "bodies": bodies, "manifolds": manifolds, "contacts": contacts,
                    "body_counts": "log-uniform in [8, 2048], towers of height 4..32 on a per-scene ground",
                    "iterations": BATCH_ITERATIONS, "dt": float(DT), "setup_s": setup_s},
-        "plain": {"value": plain_rate, "unit": "scene-steps/s", "rounds": args.batch_rounds,
-                  "ms_per_round": 1000 * plain_s / args.batch_rounds, "gpu_launches_per_round": int(plain_launches),
+        "plain": {"value": plain_rate, "unit": "scene-steps/s", "rounds": plain_steps,
+                  "ms_per_round": 1000 * plain_s / plain_steps, "gpu_launches_per_round": int(plain_launches),
                   "path": "bepugpu_step per scene (one graph launch per scene-step), host clock"},
+        "window": f"both paths from the records' state: 3 warm-up steps, {K} untimed steps, then the "
+                  f"{calls * K} timed steps ({calls} batched calls of {K}); the 1-step-per-launch figure "
+                  f"times steps 5..{4 + calls}",
         "batched": {"value": batched_rate, "unit": "scene-steps/s", "steps_per_launch": best.steps_per_launch,
                     "ms_per_call": 1000 * n * best.steps_per_launch / tb.scene_steps_per_s,
                     "device_ms_per_call": tb.device_ms_per_launch, "gpu_launches_per_call": tb.launches,

@@ -35,8 +35,9 @@ namespace bepugpu {
 // than a loop inside the CTA: the loop keeps the step's body state live across
 // iterations and pushes the kernel past the register file into spills.
 template <bool kShared>
-__global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
-                               uint32_t flags, int Bc, int Lc, int pass, bool nonConvex) {
+__device__ __forceinline__ void BatchGroupStep(const SceneView* __restrict__ views, const int4* __restrict__ work,
+                                               const StepParams& p, uint32_t flags, int Bc, int Lc, int pass,
+                                               bool nonConvex) {
     extern __shared__ float4 smem[];
     __shared__ SceneView sv;
     const int4 w = work[blockIdx.x];  // scene view, group, steps
@@ -49,6 +50,20 @@ __global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* 
     __syncthreads();
     const GroupDesc g = sv.t.groups[w.y];
     GroupStep<false, kShared, false>(sv.m, sv.b, JointSoA{}, p, flags, sv.t, g, Bc, Lc, 0, smem, nullptr, nonConvex);
+}
+template <bool kShared>
+__global__ void k_batch_groups(const SceneView* __restrict__ views, const int4* __restrict__ work, StepParams p,
+                               uint32_t flags, int Bc, int Lc, int pass, bool nonConvex) {
+    BatchGroupStep<kShared>(views, work, p, flags, Bc, Lc, pass, nonConvex);
+}
+// The same kernel held to 168 registers a thread, for 128-thread CTAs: three
+// of them fit an SM's 65,536 registers where the unbounded build's 176 fit
+// two; ptxas spills a few bytes outside the sweeps.
+template <bool kShared>
+__global__ void __maxnreg__(168) k_batch_groups_r168(const SceneView* __restrict__ views,
+                                                     const int4* __restrict__ work, StepParams p, uint32_t flags,
+                                                     int Bc, int Lc, int pass, bool nonConvex) {
+    BatchGroupStep<kShared>(views, work, p, flags, Bc, Lc, pass, nonConvex);
 }
 
 namespace {
@@ -127,14 +142,15 @@ cudaError_t LaunchBatchedGroups(bool shared, const SceneView* views, const int4*
                                 cudaStream_t stream, bool nonConvex, int firstPass) {
     if (n <= 0) return cudaSuccess;
     size_t smemBytes = GroupSmemBytes(shared, Bc, Lc, 0, nonConvex);
-    auto kernel = shared ? k_batch_groups<true> : k_batch_groups<false>;
+    const int T = ThreadsFor(members, threads);
+    auto kernel = T == 128 ? (shared ? k_batch_groups_r168<true> : k_batch_groups_r168<false>)
+                           : (shared ? k_batch_groups<true> : k_batch_groups<false>);
     if (smemBytes > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemBytes);
         if (e != cudaSuccess) return e;
     }
     for (int pass = firstPass; pass < firstPass + passes; pass++) {
-        kernel<<<(unsigned)n, ThreadsFor(members, threads), smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass,
-                                                                                  nonConvex);
+        kernel<<<(unsigned)n, T, smemBytes, stream>>>(views, work, p, flags, Bc, Lc, pass, nonConvex);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
