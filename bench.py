@@ -170,10 +170,10 @@ def measured_hbm_peak():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch(kernel: str):
-    """DRAM bytes per launch of `kernel` on the pile from the committed ncu
-    summary (profiles/<kernel>_pile64k.md), if any."""
-    p = ROOT / "profiles" / f"{kernel}_pile64k.md"
+def ncu_traffic_per_launch(kernel: str, workload: str = "pile64k"):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/<kernel>_<workload>.md), if any."""
+    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -683,8 +683,18 @@ def batch_section(args, local, rank, world, pg):
     peak, peak_kind = measured_hbm_peak()
     call_bytes = step_bytes * best.steps_per_launch
     achieved = call_bytes / (tb.device_ms_per_launch / 1000.0) / 1e9 if tb.device_ms_per_launch > 0 else 0.0
+    # ncu's DRAM bytes of one launch over the first 512 scenes of the mix, scaled
+    # by manifolds to this launch's scenes (each scene's records move about once)
+    traffic = ncu_traffic_per_launch("k_batch_groups", "towers512")
+    if traffic is not None:
+        first512 = records[:512] if world == 1 and n >= 512 else batch_records(512)
+        traffic = traffic * manifolds / max(sum(len(m) for _, m in first512), 1)
     batch_roofline = {"bound": "hbm", "kernel": "k_batch_groups", "achieved": achieved, "peak": peak,
                       "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                      "traffic": None if traffic is None else traffic * K,
+                      "traffic_note": "ncu DRAM bytes of one launch over 512 scenes (profiles/"
+                                      "k_batch_groups_towers512.md) scaled by manifolds to this call's scenes, "
+                                      "times its launches",
                       "algorithmic_bytes_per_call": call_bytes, "device_ms_per_call": tb.device_ms_per_launch,
                       "launches_per_call": tb.launches,
                       "algorithmic": "per scene-step: 76 d + 136 + 48 c per executed solve visit (census), one "
