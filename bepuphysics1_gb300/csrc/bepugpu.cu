@@ -46,12 +46,10 @@ __global__ void k_unpack_bodies(const bepugpu_body* __restrict__ rec, int n, Bod
     b.act[i] = make_float4(r.previous_velocity, r.velocity_time_below_limit, __uint_as_float(r.activity), 0.f);
 }
 
-// World inverse inertia at upload (Entity orientation setter: R^T L R), so a
-// solve-only step without the force stage sees the same tensor as the oracle.
-__global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= b.count) return;
-    float4 q = b.quat[i], l0 = b.loc0[i], l1 = b.loc1[i];
+// World inverse inertia R^T L R of a body with orientation q and local inverse
+// inertia L (rows l0.xyz, l0.w l1.xy, l1.zw L33): the first eight entries in
+// a, c and the last returned (kept in the angular velocity lane's w).
+__device__ __forceinline__ float WorldInertia(float4 q, float4 l0, float4 l1, float L33, float4& a, float4& c) {
     float qX2 = q.x + q.x, qY2 = q.y + q.y, qZ2 = q.z + q.z;
     float XX = qX2 * q.x, YY = qY2 * q.y, ZZ = qZ2 * q.z;
     float XY = qX2 * q.y, XZ = qX2 * q.z, XW = qX2 * q.w;
@@ -59,8 +57,7 @@ __global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
     float R11 = 1 - YY - ZZ, R21 = XY - ZW, R31 = XZ + YW;
     float R12 = XY + ZW, R22 = 1 - XX - ZZ, R32 = YZ - XW;
     float R13 = XZ - YW, R23 = YZ + XW, R33 = 1 - XX - YY;
-    float L11 = l0.x, L12 = l0.y, L13 = l0.z, L21 = l0.w, L22 = l1.x, L23 = l1.y, L31 = l1.z, L32 = l1.w,
-          L33 = localM33[i];
+    float L11 = l0.x, L12 = l0.y, L13 = l0.z, L21 = l0.w, L22 = l1.x, L23 = l1.y, L31 = l1.z, L32 = l1.w;
     float m11 = R11 * L11 + R21 * L21 + R31 * L31;
     float m12 = R11 * L12 + R21 * L22 + R31 * L32;
     float m13 = R11 * L13 + R21 * L23 + R31 * L33;
@@ -70,7 +67,6 @@ __global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
     float m31 = R13 * L11 + R23 * L21 + R33 * L31;
     float m32 = R13 * L12 + R23 * L22 + R33 * L32;
     float m33 = R13 * L13 + R23 * L23 + R33 * L33;
-    float4 a, c, w = b.vang[i];
     a.x = m11 * R11 + m12 * R21 + m13 * R31;
     a.y = m11 * R12 + m12 * R22 + m13 * R32;
     a.z = m11 * R13 + m12 * R23 + m13 * R33;
@@ -79,7 +75,15 @@ __global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
     c.y = m21 * R13 + m22 * R23 + m23 * R33;
     c.z = m31 * R11 + m32 * R21 + m33 * R31;
     c.w = m31 * R12 + m32 * R22 + m33 * R32;
-    w.w = m31 * R13 + m32 * R23 + m33 * R33;
+    return m31 * R13 + m32 * R23 + m33 * R33;
+}
+// World inverse inertia at upload (Entity orientation setter: R^T L R), so a
+// solve-only step without the force stage sees the same tensor as the oracle.
+__global__ void k_world_inertia(BodySoA b, const float* __restrict__ localM33) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= b.count) return;
+    float4 a, c, w = b.vang[i];
+    w.w = WorldInertia(b.quat[i], b.loc0[i], b.loc1[i], localM33[i], a, c);
     b.inv0[i] = a;
     b.inv1[i] = c;
     b.vang[i] = w;
@@ -200,9 +204,11 @@ __global__ void k_update_body_state(const bepugpu_body* __restrict__ in, int n, 
 // run of 16-byte words through shared memory: consecutive threads, consecutive words.
 constexpr int kStateBlock = 128;
 
-// State records into the body lanes and the kept records (bepugpu_step_state).
+// State records into the body lanes and the kept records (bepugpu_step_state),
+// with the world inverse inertia of the new orientation (k_world_inertia).
 __global__ void __launch_bounds__(kStateBlock) k_update_body_state_records(const bepugpu_body_state* __restrict__ in,
-                                                                           int n, BodySoA b, bepugpu_body* kept) {
+                                                                           int n, BodySoA b, bepugpu_body* kept,
+                                                                           const float* __restrict__ localM33) {
     __shared__ float4 buf[4 * kStateBlock];
     const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, n - first);
     const float4* src = (const float4*)(in + first);
@@ -213,11 +219,15 @@ __global__ void __launch_bounds__(kStateBlock) k_update_body_state_records(const
     const float4* w4 = buf + 4 * threadIdx.x;  // 64-byte records: four 16-byte words
     const float4 r0 = w4[0], r1 = w4[1], r2 = w4[2], r3 = w4[3];
     // r0 = p.xyz q.x, r1 = q.yzw v.x, r2 = v.yz w.xy, r3 = w.z activity previous timeBelow
-    const float4 p = b.pos[i], v = b.vlin[i], w = b.vang[i];
+    const float4 p = b.pos[i], v = b.vlin[i], q = make_float4(r0.w, r1.x, r1.y, r1.z);
+    float4 ia, ic;
+    const float m33 = WorldInertia(q, b.loc0[i], b.loc1[i], localM33[i], ia, ic);
     b.pos[i] = make_float4(r0.x, r0.y, r0.z, p.w);
-    b.quat[i] = make_float4(r0.w, r1.x, r1.y, r1.z);
+    b.quat[i] = q;
     b.vlin[i] = make_float4(r1.w, r2.x, r2.y, v.w);
-    b.vang[i] = make_float4(r2.z, r2.w, r3.x, w.w);
+    b.vang[i] = make_float4(r2.z, r2.w, r3.x, m33);
+    b.inv0[i] = ia;
+    b.inv1[i] = ic;
     b.act[i] = make_float4(r3.z, r3.w, r3.y, 0.f);
     bepugpu_body& k = kept[i];
     k.position[0] = r0.x; k.position[1] = r0.y; k.position[2] = r0.z;
@@ -228,10 +238,10 @@ __global__ void __launch_bounds__(kStateBlock) k_update_body_state_records(const
     k.previous_velocity = r3.z;
     k.velocity_time_below_limit = r3.w;
 }
-// Body lanes -> state records.
-__global__ void __launch_bounds__(kStateBlock) k_pack_body_state(BodySoA b, bepugpu_body_state* __restrict__ out) {
-    __shared__ float4 buf[4 * kStateBlock];
-    const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, b.count - first);
+// Body lanes -> state records (one block's share).
+__device__ __forceinline__ void PackBodyState(const BodySoA& b, bepugpu_body_state* __restrict__ out, int block,
+                                              float4* buf) {
+    const int first = block * kStateBlock, rows = min(kStateBlock, b.count - first);
     const int i = first + threadIdx.x;
     if (threadIdx.x < rows) {
         const float4 p = b.pos[i], q = b.quat[i], v = b.vlin[i], w = b.vang[i], a = b.act[i];
@@ -245,11 +255,10 @@ __global__ void __launch_bounds__(kStateBlock) k_pack_body_state(BodySoA b, bepu
     float4* dst = (float4*)(out + first);
     for (int k = threadIdx.x; k < 4 * rows; k += kStateBlock) dst[k] = buf[k];
 }
-// Manifold slots -> state records, in record order.
-__global__ void __launch_bounds__(kStateBlock) k_pack_manifold_state(ManifoldSoA m, const int32_t* __restrict__ slot_of,
-                                                                     int n, bepugpu_manifold_state* __restrict__ out) {
-    __shared__ float4 buf[5 * kStateBlock];
-    const int first = blockIdx.x * kStateBlock, rows = min(kStateBlock, n - first);
+// Manifold slots -> state records, in record order (one block's share).
+__device__ __forceinline__ void PackManifoldState(const ManifoldSoA& m, const int32_t* __restrict__ slot_of, int n,
+                                                  bepugpu_manifold_state* __restrict__ out, int block, float4* buf) {
+    const int first = block * kStateBlock, rows = min(kStateBlock, n - first);
     const int i = first + threadIdx.x;
     if (threadIdx.x < rows) {
     const int s = slot_of[i], cap = m.capacity;
@@ -272,6 +281,16 @@ __global__ void __launch_bounds__(kStateBlock) k_pack_manifold_state(ManifoldSoA
     __syncthreads();
     float4* dst = (float4*)(out + first);
     for (int k = threadIdx.x; k < 5 * rows; k += kStateBlock) dst[k] = buf[k];
+}
+// Both downloads in one launch: blocks [0, bodyBlocks) pack body state
+// records, the rest manifold state records.
+__global__ void __launch_bounds__(kStateBlock) k_pack_state(BodySoA b, bepugpu_body_state* __restrict__ bodies,
+                                                            int bodyBlocks, ManifoldSoA m,
+                                                            const int32_t* __restrict__ slot_of, int nm,
+                                                            bepugpu_manifold_state* __restrict__ manifolds) {
+    __shared__ float4 buf[5 * kStateBlock];
+    if ((int)blockIdx.x < bodyBlocks) PackBodyState(b, bodies, blockIdx.x, buf);
+    else PackManifoldState(m, slot_of, nm, manifolds, blockIdx.x - bodyBlocks, buf);
 }
 __global__ void k_check_manifold_records(const bepugpu_manifold* __restrict__ rec, const int32_t* __restrict__ slot_of,
                                          int n, ManifoldSoA m, int* check) {
@@ -1782,8 +1801,10 @@ bepugpu_status QueueStateDownload(Context* ctx, Scene* s, bepugpu_body_state* bo
     auto* sm = (bepugpu_manifold_state*)((char*)s->staging + s->stagingManifoldsAt);
     auto* db = nb ? (bepugpu_body_state*)PinnedDeviceAddress(bodies) : nullptr;
     auto* dm = nm ? (bepugpu_manifold_state*)PinnedDeviceAddress(man) : nullptr;
-    if (nb) k_pack_body_state<<<Blocks(nb, kStateBlock), kStateBlock, 0, s->stream>>>(s->b, db ? db : sb);
-    if (nm) k_pack_manifold_state<<<Blocks(nm, kStateBlock), kStateBlock, 0, s->stream>>>(s->m, s->slotOf, (int)nm, dm ? dm : sm);
+    const int bodyBlocks = nb ? Blocks(nb, kStateBlock) : 0, manifoldBlocks = nm ? Blocks(nm, kStateBlock) : 0;
+    if (bodyBlocks + manifoldBlocks)
+        k_pack_state<<<bodyBlocks + manifoldBlocks, kStateBlock, 0, s->stream>>>(s->b, db ? db : sb, bodyBlocks, s->m,
+                                                                                 s->slotOf, (int)nm, dm ? dm : sm);
     if (nb && !db)
         CK(cudaMemcpyAsync(bodies, sb, sizeof(bepugpu_body_state) * nb, cudaMemcpyDeviceToHost, s->stream));
     if (nm && !dm)
@@ -1831,8 +1852,8 @@ bepugpu_status bepugpu_step_state(bepugpu_context* c, int32_t id, bepugpu_body_s
             CK(cudaMemcpyAsync(sb, bodies, sizeof(bepugpu_body_state) * nb, cudaMemcpyHostToDevice, s->stream));
             in = sb;
         }
-        k_update_body_state_records<<<Blocks(nb, kStateBlock), kStateBlock, 0, s->stream>>>(in, (int)nb, s->b, s->bodyRecords);
-        k_world_inertia<<<Blocks(nb, 256), 256, 0, s->stream>>>(s->b, s->localM33);
+        k_update_body_state_records<<<Blocks(nb, kStateBlock), kStateBlock, 0, s->stream>>>(in, (int)nb, s->b,
+                                                                                          s->bodyRecords, s->localM33);
         CK(cudaGetLastError());
     }
     st = s->Step(ctx, dt, flags & BEPUGPU_STEP_ALL);
