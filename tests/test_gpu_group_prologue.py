@@ -45,6 +45,25 @@ def test_pile_1k_and_towers(gpu_context, policy):
         p.close()
 
 
+@pytest.mark.parametrize("flags", [N.STEP_SOLVE, N.STEP_SOLVE | N.STEP_FORCES,
+                                   N.STEP_ALL & ~N.STEP_REFRESH_CONTACTS & ~N.STEP_COLLIDE,
+                                   N.STEP_ALL & ~N.STEP_DEACTIVATION & ~N.STEP_COLLIDE])
+def test_stage_subsets(gpu_context, flags):
+    b, m, _ = scenes.make_tower(800, seed=5)
+    p = _split_pair(gpu_context, b, m, policy=MIXED)
+    _run_exact(p, 2, 6, flags=flags)
+    p.close()
+
+
+def test_persistent_mode_with_sweeps(gpu_context):
+    """Groups beside the colour sweeps of the persistent kernel."""
+    b, m, _ = scenes.make_tower(1200, seed=19)
+    p = Pair(gpu_context, b, m, group_policy=MIXED, mode=N.MODE_PERSISTENT)
+    p.gpu.set_group_prologue(1)
+    _run_exact(p, 3, 7)
+    p.close()
+
+
 def test_nonconvex_towers(gpu_context):
     b, m, _ = scenes.make_tower(600, seed=14, sphere_fraction=0.5)
     assert np.any(m["flags"] & N.MANIFOLD_NONCONVEX)
