@@ -986,6 +986,8 @@ def collide_section(args, local, rank, world, pg):
 
 SERVE_WORKLOAD = "serve_16k"
 SERVE_ITERATIONS = 8
+SERVE_GROUP_MANIFOLDS = 128  # the batch autotuner's best for the tower mix
+SERVE_THREADS = 128
 
 
 def serve_records(n, rank=0, world=1):
@@ -1077,7 +1079,9 @@ def serve_section(args, local, rank, world, pg):
     settings = batch_settings()
     settings["iteration_limit"] = SERVE_ITERATIONS
     ctx = Context(local, settings)
-    spaces = [GpuSpace(ctx, b, m) for b, m in records]
+    # the batch autotuner's setting for towers (128 manifolds per group, 128-thread
+    # batched CTAs); the plain path steps the same group plans with their own CTA sizes
+    spaces = [GpuSpace(ctx, b, m, group_policy=(1, 1024, 4096, SERVE_GROUP_MANIFOLDS, 0)) for b, m in records]
     setup_s = time.perf_counter() - t0
     ids = [sp.id for sp in spaces]
     rates = [float(r) for r in args.serve_rates.split(",") if r]
@@ -1087,6 +1091,7 @@ def serve_section(args, local, rank, world, pg):
                       "manifolds": int(sum(len(m) for _, m in records)),
                       "body_counts": "log-uniform in [16, 4096], towers of height 4..32",
                       "iterations": SERVE_ITERATIONS, "k": [1, 4, 16], "arrival_window_s": args.serve_seconds,
+                      "group_manifolds": SERVE_GROUP_MANIFOLDS, "batched_threads": SERVE_THREADS,
                       "setup_s": setup_s, "latency": "submit to completion seen by the server, steady clock"}}
 
     def run(mode_rates, **kw):
@@ -1116,12 +1121,13 @@ def serve_section(args, local, rank, world, pg):
         srv.close()
         return res
 
-    out["batched"] = run(rates, batching=True, budget_bytes=120 << 30)
+    out["batched"] = run(rates, batching=True, budget_bytes=120 << 30, threads=SERVE_THREADS)
     out["batched"]["device_budget_bytes"] = 120 << 30
     out["plain"] = run(plain_rates, batching=False, budget_bytes=120 << 30)
     total = out["batched"]["resident_bytes"]
     spill_rate = [float(r) for r in args.serve_spill_rates.split(",") if r]
-    out["batched_half_budget"] = run(spill_rate, batching=True, budget_bytes=max(total // 2, 1 << 20))
+    out["batched_half_budget"] = run(spill_rate, batching=True, budget_bytes=max(total // 2, 1 << 20),
+                                     threads=SERVE_THREADS)
     out["batched_half_budget"]["device_budget_bytes"] = max(total // 2, 1 << 20)
     by_rate = {lv["rate"]: lv for lv in out["plain"]["levels"]}
     out["vs_plain"] = [{"rate": lv["rate"], "p99_ms_batched": lv["p99_ms"],

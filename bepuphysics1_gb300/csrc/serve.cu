@@ -489,13 +489,14 @@ struct Server {
                 }
                 if (e == cudaSuccess && !shared.empty()) {
                     check(LaunchBatchedGroups(true, viewsDev, w.workDev, (int)shared.size(), p, cfg.flags, sBc, sLc,
-                                              sMem, 0, per, w.stream, sNonConvex, round),
+                                              sMem, (int)cfg.threads, per, w.stream, sNonConvex, round),
                           "group launch");
                     statLaunches += per;
                 }
                 if (e == cudaSuccess && !global.empty()) {
                     check(LaunchBatchedGroups(false, viewsDev, w.workDev + shared.size(), (int)global.size(), p,
-                                              cfg.flags, gBc, 1, gMem, 0, per, w.stream, false, round),
+                                              cfg.flags, gBc, 1, gMem, (int)cfg.threads, per, w.stream, false,
+                                              round),
                           "group launch");
                     statLaunches += per;
                 }
@@ -635,8 +636,10 @@ bepugpu_status bepugpu_server_create(bepugpu_context* c, const bepugpu_server_co
     if (!ctx || !config || !out) return BEPUGPU_INVALID_ARGUMENT;
     if (!Ring<int>::ValidCapacity(config->queue_capacity) || config->max_wave_scenes < 1 ||
         config->max_waves_in_flight < 1 || config->max_waves_in_flight > 4 || !(config->dt > 0) ||
-        config->device_budget_bytes == 0) {
-        ctx->SetError("server config: queue capacity a power of two >= 2, waves 1..4, dt > 0, a budget");
+        config->device_budget_bytes == 0 ||
+        (config->threads != 0 && (config->threads < 32 || config->threads > 256 || config->threads % 32))) {
+        ctx->SetError("server config: queue capacity a power of two >= 2, waves 1..4, dt > 0, a budget, "
+                      "threads 0 or a multiple of 32 in [32, 256]");
         return BEPUGPU_INVALID_ARGUMENT;
     }
     cudaSetDevice(ctx->device);

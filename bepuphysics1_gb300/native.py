@@ -81,7 +81,8 @@ CHAIN_PARAMS_DTYPE = np.dtype([
 
 SERVER_CONFIG_DTYPE = np.dtype([
     ("device_budget_bytes", "<u8"), ("max_wave_scenes", "<u4"), ("max_waves_in_flight", "<u4"),
-    ("queue_capacity", "<u4"), ("batching", "<u4"), ("dt", "<f4"), ("flags", "<u4"), ("reserved", "<u4", 4),
+    ("queue_capacity", "<u4"), ("batching", "<u4"), ("dt", "<f4"), ("flags", "<u4"), ("threads", "<u4"),
+    ("reserved", "<u4", 3),
 ])
 COMPLETION_DTYPE = np.dtype([
     ("tag", "<u8"), ("scene", "<i4"), ("status", "<i4"), ("steps", "<u4"), ("wave", "<u4"),

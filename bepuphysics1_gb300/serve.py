@@ -29,7 +29,8 @@ def clock_us() -> float:
 class Server:
     def __init__(self, ctx: Context, budget_bytes: int | None = None, batching: bool = True,
                  max_wave_scenes: int | None = None, waves_in_flight: int | None = None,
-                 queue_capacity: int | None = None, dt: float | None = None, flags: int = N.STEP_ALL):
+                 queue_capacity: int | None = None, dt: float | None = None, flags: int = N.STEP_ALL,
+                 threads: int = 0):
         self.ctx = ctx
         self.lib = ctx.lib
         cfg = default_config()
@@ -45,6 +46,7 @@ class Server:
             cfg["dt"] = float(dt)
         cfg["batching"] = 1 if batching else 0
         cfg["flags"] = flags
+        cfg["threads"] = int(threads)
         self.config = cfg
         h = ctypes.c_void_p()
         c = np.array(cfg, N.SERVER_CONFIG_DTYPE).reshape(1)

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BEPUGPU_ABI_VERSION 11
+#define BEPUGPU_ABI_VERSION 12
 #define BEPUGPU_MAX_CONTACTS 4
 
 typedef enum bepugpu_status {
@@ -781,7 +781,9 @@ typedef struct bepugpu_server_config {
     uint32_t batching;             /* 1 continuous batching, 0 one launch per scene step */
     float dt;
     uint32_t flags;                /* BEPUGPU_STEP_* */
-    uint32_t reserved[4];
+    uint32_t threads;              /* CTA size of the batched waves: 0 from each group plan, else a
+                                      multiple of 32 in [32, 256] (bepugpu_set_batch_threads's rule) */
+    uint32_t reserved[3];
 } bepugpu_server_config;
 
 typedef struct bepugpu_completion {

@@ -37,7 +37,7 @@ def test_binding_covers_header():
 
 def test_record_sizes():
     lib = N.load_gpu_library()
-    assert lib.bepugpu_abi_version() == 11
+    assert lib.bepugpu_abi_version() == 12
     assert lib.bepugpu_record_size(0) == N.SETTINGS_DTYPE.itemsize
     assert lib.bepugpu_record_size(1) == N.BODY_DTYPE.itemsize == 116
     assert lib.bepugpu_record_size(2) == N.CONTACT_DTYPE.itemsize == 80
