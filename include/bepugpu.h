@@ -644,7 +644,8 @@ bepugpu_status bepugpu_set_group_smem_budget(bepugpu_context* ctx, int32_t scene
  * kernel then copying the solve lanes into shared memory; -1 (default) the
  * grid-wide launches when the groups hold joints and at least 8,192
  * constraints.  The results are the same bit for bit.  Takes effect at the
- * next step. */
+ * next step.  No reference counterpart: it only chooses how the GPU runs the
+ * stages of Space.cs:496-513. */
 bepugpu_status bepugpu_set_group_prologue(bepugpu_context* ctx, int32_t scene, int32_t mode);
 
 /* Persistent mode: resident blocks per SM of the cooperative launch (1 or 2). */
