@@ -94,6 +94,7 @@ def parse_args():
     ap.add_argument("--collide-cpu-seconds", type=float, default=8.0)
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
+    ap.add_argument("--serve-waves", type=int, default=4, help="batched waves in flight (1..4)")
     ap.add_argument("--serve-rates", default="1000,20000,100000,200000",
                     help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-plain-rates", default="1000,20000")
@@ -1121,7 +1122,8 @@ def serve_section(args, local, rank, world, pg):
         srv.close()
         return res
 
-    out["batched"] = run(rates, batching=True, budget_bytes=120 << 30, threads=SERVE_THREADS)
+    out["batched"] = run(rates, batching=True, budget_bytes=120 << 30, threads=SERVE_THREADS,
+                         waves_in_flight=args.serve_waves)
     out["batched"]["device_budget_bytes"] = 120 << 30
     out["plain"] = run(plain_rates, batching=False, budget_bytes=120 << 30)
     total = out["batched"]["resident_bytes"]
