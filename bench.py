@@ -1093,6 +1093,7 @@ def serve_section(args, local, rank, world, pg):
                       "body_counts": "log-uniform in [16, 4096], towers of height 4..32",
                       "iterations": SERVE_ITERATIONS, "k": [1, 4, 16], "arrival_window_s": args.serve_seconds,
                       "group_manifolds": SERVE_GROUP_MANIFOLDS, "batched_threads": SERVE_THREADS,
+                      "batched_waves_in_flight": args.serve_waves,
                       "setup_s": setup_s, "latency": "submit to completion seen by the server, steady clock"}}
 
     def run(mode_rates, **kw):
