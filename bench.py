@@ -95,6 +95,7 @@ def parse_args():
     ap.add_argument("--serve-scenes", type=int, default=16384)
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per load level")
     ap.add_argument("--serve-waves", type=int, default=4, help="batched waves in flight (1..4)")
+    ap.add_argument("--serve-wave-scenes", type=int, default=4096, help="scenes per batched wave at most")
     ap.add_argument("--serve-rates", default="1000,20000,100000,200000",
                     help="Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-plain-rates", default="1000,20000")
@@ -1093,7 +1094,7 @@ def serve_section(args, local, rank, world, pg):
                       "body_counts": "log-uniform in [16, 4096], towers of height 4..32",
                       "iterations": SERVE_ITERATIONS, "k": [1, 4, 16], "arrival_window_s": args.serve_seconds,
                       "group_manifolds": SERVE_GROUP_MANIFOLDS, "batched_threads": SERVE_THREADS,
-                      "batched_waves_in_flight": args.serve_waves,
+                      "batched_waves_in_flight": args.serve_waves, "batched_wave_scenes": args.serve_wave_scenes,
                       "setup_s": setup_s, "latency": "submit to completion seen by the server, steady clock"}}
 
     def run(mode_rates, **kw):
@@ -1124,7 +1125,7 @@ def serve_section(args, local, rank, world, pg):
         return res
 
     out["batched"] = run(rates, batching=True, budget_bytes=120 << 30, threads=SERVE_THREADS,
-                         waves_in_flight=args.serve_waves)
+                         waves_in_flight=args.serve_waves, max_wave_scenes=args.serve_wave_scenes)
     out["batched"]["device_budget_bytes"] = 120 << 30
     out["plain"] = run(plain_rates, batching=False, budget_bytes=120 << 30)
     total = out["batched"]["resident_bytes"]
