@@ -69,8 +69,9 @@ __host__ __device__ constexpr size_t GroupSmemBytes(bool shared, int bodies, int
 // use), its prestep angular A in lanes 16-19 and angular B in lanes 25-28.
 // prestepped: the group's bodies went through the candidacy and force updates
 // and its manifolds through the refresh and the prestep in grid-wide launches
-// before this one (k_group_refresh_force, k_group_prestep; joints: none), so
-// the step starts by copying bodies and solve lanes into shared memory.
+// before this one (k_group_refresh_force, k_group_prestep), so the step starts
+// by copying bodies and manifold solve lanes into shared memory; the group's
+// joints are prestepped here as without it.
 template <bool kCensus, bool kShared, int kJoints>
 __device__ __forceinline__ void GroupStep(const ManifoldSoA& m, const BodySoA& b, const JointSoA& jt,
                                           const StepParams& p, uint32_t flags, const GroupTables& t,
